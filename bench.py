@@ -1,0 +1,366 @@
+"""Benchmark of the fused forward + adjoint of one monotone component.
+
+Workload (the metric's configuration): one MonotoneComponent with input
+dimension 8, total-order-4 multi-index set (495 terms), ProbabilistHermite
+basis (normalised), SoftPlus rectifier, AdaptiveClenshawCurtis quadrature
+(quadPts 5, abs = rel tol 1e-6, maxSub 30); coefficients N(0, 0.05^2),
+1,000,000 points N(0, I_8), sensitivities N(0, 1), all float64 from seeded
+generators (synthetic data; the reference publishes no dataset for this path).
+
+One step = Evaluate + LogDeterminant + CoeffGrad + LogDeterminantCoeffGrad of
+every point, with the coefficient gradients contracted over the points
+(sum_i sens_i dT_i/dc + sum_i dlogdet_i/dc), in one fused pass.
+
+`value` is points/s with inputs resident in HBM (device time of the fused
+call, CUDA events on its stream, L2 flushed between steps).  `e2e` is the
+same through the C ABI with pinned host buffers (host->device copy of points
+and sensitivities and device->host copy of T, logdet and the gradient inside
+the timed region).  `--impl reference` times the reference algorithm (the
+CPU restatement in oracle/, all host threads) on bounded samples.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIM, ORDER, NPTS = 8, 4, 1_000_000
+TOL, MAXSUB = 1e-6, 30
+METRIC = "fused fwd+adjoint points/s (dim-8, order-4, FP64)"
+
+
+def synth(n, seed_pts=1, seed_sens=2):
+    x = np.random.default_rng(seed_pts).standard_normal((DIM, n))
+    s = np.random.default_rng(seed_sens).standard_normal((1, n))
+    return x, s
+
+
+def coeffs(nterms):
+    return np.random.default_rng(0).normal(0.0, 0.05, nterms)
+
+
+def prefix_stats():
+    """|M| (prefix nodes incl. root), T, nB and sum over term-carrying prefixes
+    of max(depth-1, 0) for the total-order set -- inputs of the FLOP model."""
+    from mpart_gb300 import FixedMultiIndexSet
+    ms = FixedMultiIndexSet(DIM, ORDER)
+    prefixes = {}
+    for t in range(ms.Size()):
+        m = ms.IndexToMulti(t)
+        key = tuple(m[:-1])
+        prefixes.setdefault(key, 0)
+        prefixes[key] += 1
+    nodes = len(prefixes)
+    sc = sum(max(sum(1 for v in k if v > 0) - 1, 0) for k in prefixes)
+    return nodes, ms.Size(), (DIM - 1) * ORDER, sc
+
+
+def flops_per_point(evals_per_point):
+    """Algorithmic FP64 flops of the fused algorithm per point (FMA = 2,
+    exp/log/reciprocal = 1 each), with the mean integrand evaluations per
+    point E and intervals I = (E - 2) / 3:
+      A  prefix products + coefficient FMAs      (|M|-1) + 2T
+      L  leading-coordinate recurrences          3 nB
+      N  per node: basis 4P, df 2P, g/g' 8, h 2, adjoint parts P   -> 7P + 10
+      Q  per interval: coarse/fine sums of h and of the P adjoint parts -> 18 + 10P
+      X  endpoint x_D terms (log-det)            9P + 10
+      W  per-point weights                       4(P+1)
+      C  reduction over points: products + FMAs  S_C + 2T"""
+    nodes, T, nB, sc = prefix_stats()
+    P = ORDER
+    E = evals_per_point
+    I = (E - 2.0) / 3.0
+    return ((nodes - 1) + 2 * T) + 3 * nB + E * (7 * P + 10) + I * (18 + 10 * P) + (9 * P + 10) + 4 * (P + 1) + \
+        (sc + 2 * T)
+
+
+def mean_evals(sample=20000):
+    """Mean integrand evaluations per point from the oracle's node counts (the
+    GPU follows the same subdivision tree)."""
+    from oracle import oracle as O
+    O.build()
+    s, d, o = O.total_order(DIM, ORDER)
+    c = O.OracleComponent(DIM, s, d, o, abs_tol=TOL, rel_tol=TOL, max_sub=MAXSUB)
+    x, _ = synth(sample)
+    _, nev, _ = c.evaluate(coeffs(c.num_terms), x, return_evals=True)
+    return float(nev.mean())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.p = None
+        self.index = index
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [v.strip() for v in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except Exception:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the reference algorithm on the host cores
+# ----------------------------------------------------------------------------
+def cpu_reference_step(comp, coef, x, s):
+    """Evaluate, LogDeterminant, CoeffGrad(sens) and LogDeterminantCoeffGrad
+    (the reference's four calls, MonotoneComponent.h), reduced over points."""
+    comp.evaluate(coef, x)
+    comp.logdet(coef, x)
+    g = comp.coeff_grad(coef, x, s[0])
+    lg = comp.logdet_coeff_grad(coef, x)
+    return g.sum(axis=1) + lg.sum(axis=1)
+
+
+def cpu_baseline(target_seconds=12.0):
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    s_, d_, o_ = O.total_order(DIM, ORDER)
+    comp = O.OracleComponent(DIM, s_, d_, o_, abs_tol=TOL, rel_tol=TOL, max_sub=MAXSUB)
+    coef = coeffs(comp.num_terms)
+    n = 2000
+    x, s = synth(n)
+    t0 = time.perf_counter()
+    cpu_reference_step(comp, coef, x, s)
+    dt = time.perf_counter() - t0
+    n2 = int(min(NPTS, max(n, n * target_seconds / max(dt, 1e-6))))
+    x, s = synth(n2)
+    t0 = time.perf_counter()
+    cpu_reference_step(comp, coef, x, s)
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": f"first {n2} of the {NPTS} points (same seeds), reference algorithm restated in "
+                      f"oracle/ (C++17 + OpenMP, {cores} threads): Evaluate + LogDeterminant + CoeffGrad + "
+                      f"LogDeterminantCoeffGrad, gradients summed over points"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    s_, d_, o_ = O.total_order(DIM, ORDER)
+    comp = O.OracleComponent(DIM, s_, d_, o_, abs_tol=TOL, rel_tol=TOL, max_sub=MAXSUB)
+    coef = coeffs(comp.num_terms)
+    n = int(os.environ.get("MPGB_REF_SAMPLE", "20000"))
+    x, s = synth(n)
+    for _ in range(args.warmup):
+        cpu_reference_step(comp, coef, x[:, :min(n, 2000)], s[:, :min(n, 2000)])
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_reference_step(comp, coef, x, s)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = n / dt
+    sample = (f"{n} of the {NPTS} points per step (same seeds); reference algorithm restated in oracle/ "
+              f"(C++17 + OpenMP, {cores} threads); the reference itself does not build here")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"MonotoneComponent dim {DIM}, total order {ORDER} (495 terms), ProbHermite + "
+                                   f"SoftPlus, ACC tol {TOL}, {NPTS} points", "points": NPTS, "sample_points": n},
+            "cpu_baseline": {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import mpart_gb300 as M
+    M.load()
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=TOL, quadRelTol=TOL,
+                        quadMaxSub=MAXSUB)
+    comp = M.CreateComponent(M.FixedMultiIndexSet(DIM, ORDER), opts)
+    coef = coeffs(comp.numCoeffs)
+    comp.SetCoeffs(coef)
+    N = args.points
+    xh, sh = synth(N)
+    x = torch.as_tensor(xh, device=dev)
+    s = torch.as_tensor(sh, device=dev)
+    out_T = torch.zeros(1, N, dtype=torch.float64, device=dev)
+    out_ld = torch.zeros(N, dtype=torch.float64, device=dev)
+    cg = torch.zeros(comp.numCoeffs, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        comp.FusedForwardAdjointImpl(x, sens=s, logdet_sens_scale=1.0, out_eval=out_T, out_logdet=out_ld,
+                                     coeff_grad=cg)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        for k in range(args.steps):
+            flush.fill_(float(k))  # L2 flush (256 MB > 129 MB L2) between steps, outside the events
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    times = [a.elapsed_time(b) for a, b in ev]
+    t_step = float(np.mean(times)) * 1e-3
+    t_tot = torch.tensor([t_step * args.steps], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t_tot, op=dist.ReduceOp.MAX)
+    t_step_max = t_tot.item() / args.steps
+    value = world * N / t_step_max
+
+    # e2e: C ABI with pinned host buffers (copies inside the timed region).
+    xp = torch.as_tensor(xh).pin_memory()
+    sp = torch.as_tensor(sh).pin_memory()
+    Tp = torch.zeros(1, N, dtype=torch.float64).pin_memory()
+    ldp = torch.zeros(N, dtype=torch.float64).pin_memory()
+    cgp = torch.zeros(comp.numCoeffs, dtype=torch.float64).pin_memory()
+
+    def step_e2e():
+        comp.FusedForwardAdjointImpl(xp, sens=sp, logdet_sens_scale=1.0, out_eval=Tp, out_logdet=ldp,
+                                     coeff_grad=cgp)
+
+    for _ in range(2):
+        step_e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_e2e()
+    torch.cuda.synchronize()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        te = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        t_e2e = te.item()
+    h2d = xh.nbytes + sh.nbytes
+    d2h = Tp.numel() * 8 + ldp.numel() * 8 + cgp.numel() * 8
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # roofline: FP64 pipe; peak from the DFMA probe (MEASURED_PEAKS.json has no FP64 entry).
+    peak_tf, _ = M.fp64_probe()
+    E = mean_evals()
+    fpp = flops_per_point(E)
+    achieved = fpp * N / t_step / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "fused_adjoint_c2_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof))["bytes_per_point"] * N
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": t_step_max * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"MonotoneComponent dim {DIM}, total order {ORDER} (495 terms), ProbHermite + "
+                               f"SoftPlus, ACC tol {TOL}/maxSub {MAXSUB}, {N} points, fused Evaluate + LogDeterminant "
+                               f"+ CoeffGrad + LogDeterminantCoeffGrad", "points": N, "dim": DIM, "order": ORDER,
+                   "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * N / t_e2e, "unit": "points/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": None,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": achieved / peak_tf, "traffic": traffic,
+                     "peak_source": "DFMA probe in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                     "flops_per_point": fpp, "evals_per_point": E},
+        "clocks": clk.summary(),
+    }
+    line["cpu_baseline"] = cpu_baseline()
+    # launches per step: gather + fused + per-component reduction
+    line["gpu_launches"] = 3 * args.steps
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
+    ap.add_argument("--points", type=int, default=NPTS)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

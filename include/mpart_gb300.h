@@ -1,0 +1,178 @@
+/*
+ * C ABI of the GB300 monotone-component path (libmpart_gb300.so).
+ *
+ * Plain pointers, sizes and strides only.  A matrix is (data, rows, cols,
+ * row_stride, col_stride) in elements, one column per point, exactly the
+ * (ptr, (rows, cols), (rowStride, colStride)) tuples that the reference's
+ * Python binding passes to its *Impl methods
+ * (bindings/python/package/torch_helpers.py:3-30, MParT/Utilities/ArrayConversions.h:102-115).
+ * data may point to device memory or to host memory; host matrices are
+ * staged through device buffers inside the call.
+ *
+ * Every call returns MPGB_OK or a negative error code; mpgb_last_error()
+ * gives the message of the last failure on the calling thread.  Calls are
+ * ordered on the given CUDA stream (NULL = default stream) and synchronous
+ * unless mpgb_set_async(map, 1) was called.
+ */
+#ifndef MPART_GB300_H
+#define MPART_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mpgb_map mpgb_map;
+
+enum {
+    MPGB_OK = 0,
+    MPGB_ERR_INVALID_ARGUMENT = -1, /* std::invalid_argument in the reference */
+    MPGB_ERR_RUNTIME = -2,          /* std::runtime_error in the reference */
+    MPGB_ERR_CUDA = -3,             /* CUDA runtime failure */
+    MPGB_ERR_INTEGRAND = -4         /* g(df) overflowed (MonotoneIntegrand.h:183-190 throws) */
+};
+
+enum { MPGB_BASIS_PROBABILIST_HERMITE = 0, MPGB_BASIS_PHYSICIST_HERMITE = 1, MPGB_BASIS_HERMITE_FUNCTIONS = 2 };
+enum { MPGB_POS_EXP = 0, MPGB_POS_SOFTPLUS = 1 };
+enum { MPGB_QUAD_CLENSHAW_CURTIS = 0, MPGB_QUAD_ADAPTIVE_SIMPSON = 1, MPGB_QUAD_ADAPTIVE_CLENSHAW_CURTIS = 2 };
+
+/* Status bits reported by mpgb_check_status. */
+enum {
+    MPGB_STATUS_INTEGRAND_INF = 1,
+    MPGB_STATUS_INTEGRAND_NAN = 2,
+    MPGB_STATUS_QUAD_BUDGET = 4,
+    MPGB_STATUS_NO_BRACKET = 8
+};
+
+/* MapOptions (MParT/MapOptions.h:58-123); same field meanings and defaults. */
+typedef struct mpgb_map_options {
+    int basis_type;
+    int pos_func_type;
+    int quad_type;
+    double quad_abs_tol;
+    double quad_rel_tol;
+    unsigned int quad_max_sub;
+    unsigned int quad_min_sub;
+    unsigned int quad_pts;
+    int cont_deriv;
+    int basis_norm;
+    double nugget;
+} mpgb_map_options;
+
+typedef struct mpgb_matrix {
+    double* data;
+    int64_t rows;
+    int64_t cols;
+    int64_t row_stride;
+    int64_t col_stride;
+} mpgb_matrix;
+
+/* Library version string. */
+const char* mpgb_version(void);
+/* Message of the last error on this thread. */
+const char* mpgb_last_error(void);
+
+/* MapOptions{} defaults (MParT/MapOptions.h:58-123). */
+int mpgb_map_options_default(mpgb_map_options* opts);
+
+/* MapFactory::CreateComponent with a compressed FixedMultiIndexSet
+ * (src/MapFactory.cpp:22-27; MParT/MultiIndices/FixedMultiIndexSet.h:43-46).
+ * nz_starts has num_terms+1 entries. */
+int mpgb_create_component(unsigned int dim, unsigned int num_terms, const unsigned int* nz_starts,
+                          const unsigned int* nz_dims, const unsigned int* nz_orders, const mpgb_map_options* opts,
+                          mpgb_map** out);
+
+/* MapFactory::CreateComponent(FixedMultiIndexSet(dim, order), opts)
+ * (src/MultiIndices/FixedMultiIndexSet.cpp:208-233). */
+int mpgb_create_component_total_order(unsigned int dim, unsigned int order, const mpgb_map_options* opts,
+                                      mpgb_map** out);
+
+/* MapFactory::CreateTriangular (src/MapFactory.cpp:105-124). */
+int mpgb_create_triangular(unsigned int input_dim, unsigned int output_dim, unsigned int total_order,
+                           const mpgb_map_options* opts, mpgb_map** out);
+
+/* TriangularMap(components, moveCoeffs) (src/TriangularMap.cpp:9-62).  The new
+ * map keeps references to the components; their handles stay valid. */
+int mpgb_create_triangular_from_components(mpgb_map* const* components, unsigned int n, int move_coeffs,
+                                           mpgb_map** out);
+
+/* Releases a handle (components held by a triangular map stay alive until it is destroyed). */
+int mpgb_map_destroy(mpgb_map* map);
+
+/* inputDim, outputDim, numCoeffs (MParT/ParameterizedFunctionBase.h:184-186). */
+int mpgb_map_dims(const mpgb_map* map, unsigned int* input_dim, unsigned int* output_dim, unsigned int* num_coeffs);
+
+/* TriangularMap::NumComponents / GetComponent (MParT/TriangularMap.h:65-66).
+ * A component handle must be released with mpgb_map_destroy. */
+int mpgb_map_num_components(const mpgb_map* map, unsigned int* n);
+int mpgb_map_get_component(mpgb_map* map, unsigned int i, mpgb_map** out);
+
+/* ParameterizedFunctionBase::SetCoeffs, deep copy (src/ParameterizedFunctionBase.cpp:185-207).
+ * is_host = 1 when coeffs is a host pointer. */
+int mpgb_set_coeffs(mpgb_map* map, const double* coeffs, unsigned int n, int is_host, void* stream);
+
+/* ParameterizedFunctionBase::WrapCoeffs, aliases device memory (src/ParameterizedFunctionBase.cpp:219-228). */
+int mpgb_wrap_coeffs(mpgb_map* map, double* device_coeffs, unsigned int n);
+
+/* ParameterizedFunctionBase::CoeffMap (host copy of the coefficients). */
+int mpgb_get_coeffs(const mpgb_map* map, double* host_out, unsigned int n);
+
+/* Device pointer of the current coefficients (NULL when unset). */
+int mpgb_coeffs_device_ptr(const mpgb_map* map, double** out);
+
+/* 1 = asynchronous calls (no synchronisation or status check inside calls). */
+int mpgb_set_async(mpgb_map* map, int async);
+
+/* Synchronise the stream, return and clear the status bits of the last calls. */
+int mpgb_check_status(mpgb_map* map, void* stream, int* status);
+
+/* ConditionalMapBase/ParameterizedFunctionBase::EvaluateImpl
+ * (MParT/ParameterizedFunctionBase.h:97-98; MonotoneComponent.h:255-299). out is outputDim x N. */
+int mpgb_evaluate(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream);
+
+/* ConditionalMapBase::LogDeterminantImpl (MParT/ConditionalMapBase.h:96-97). out is 1 x N. */
+int mpgb_log_determinant(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream);
+
+/* ConditionalMapBase::InverseImpl (MParT/ConditionalMapBase.h:125-127; MonotoneComponent.h:330-443)
+ * with the "xtol"/"ytol" options.  x1 has inputDim-outputDim or inputDim rows and N (or 1) columns;
+ * info (optional, device int[outputDim*N]) receives the root finder's status per point. */
+int mpgb_inverse(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
+                 int* device_info, void* stream);
+
+/* ParameterizedFunctionBase::CoeffGradImpl (MParT/ParameterizedFunctionBase.h:163-165). out is numCoeffs x N. */
+int mpgb_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix out, void* stream);
+
+/* ParameterizedFunctionBase::GradientImpl (MParT/ParameterizedFunctionBase.h:133-135). out is inputDim x N. */
+int mpgb_gradient(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix out, void* stream);
+
+/* ConditionalMapBase::LogDeterminantCoeffGradImpl (MParT/ConditionalMapBase.h:151-152). out is numCoeffs x N. */
+int mpgb_log_determinant_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream);
+
+/* ConditionalMapBase::LogDeterminantInputGradImpl (MParT/ConditionalMapBase.h:167-168). out is inputDim x N. */
+int mpgb_log_determinant_input_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream);
+
+/* Fused forward + adjoint: the MpartTorchAutograd forward and backward calls
+ * (bindings/python/package/torch_helpers.py:39-114) in one pass.  Any output may
+ * have data == NULL.  sens is outputDim x N; logdet_sens is 1 x N (data NULL =
+ * logdet_sens_scale for every point).  coeff_grad (numCoeffs doubles, device or
+ * host) receives sum_i [sens dT/dc + logdet_sens dlogdet/dc]; input_grad is
+ * inputDim x N with the same combination of input gradients. */
+int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix logdet_sens,
+                       double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet, double* coeff_grad,
+                       mpgb_matrix input_grad, void* stream);
+
+/* FastGaussianReverseKLObjective::ObjectivePlusCoeffGradImpl (src/MapObjective.cpp:221-234)
+ * for every component of the map at once.  loss (outputDim doubles) and grad
+ * (numCoeffs doubles) may be device or host pointers. */
+int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad, void* stream);
+
+/* FP64 throughput probe: DFMA chains over blocks x threads x iters x 8; writes the
+ * kernel time in milliseconds (CUDA events on the stream). */
+int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPART_GB300_H */

@@ -1,0 +1,235 @@
+// C++ API of the GB300 monotone-component path.  Mirrors the reference's
+// host classes (MParT/ParameterizedFunctionBase.h, MParT/ConditionalMapBase.h,
+// MParT/TriangularMap.h, MParT/MapFactory.h, MParT/MapOptions.h,
+// MParT/MultiIndices/FixedMultiIndexSet.h) with device pointers in place of
+// Kokkos device views.  Every *Impl call takes caller-allocated outputs, like
+// the reference's virtual *Impl methods; calls are stream ordered and, unless
+// the object is put in asynchronous mode, synchronous from the host's view.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace mpgb {
+
+enum class BasisTypes { ProbabilistHermite, PhysicistHermite, HermiteFunctions };
+enum class PosFuncTypes { Exp, SoftPlus };
+enum class QuadTypes { ClenshawCurtis, AdaptiveSimpson, AdaptiveClenshawCurtis };
+
+// MParT/MapOptions.h:58-123 (the fields this path reads; same defaults).
+struct MapOptions {
+    BasisTypes basisType = BasisTypes::ProbabilistHermite;
+    PosFuncTypes posFuncType = PosFuncTypes::SoftPlus;
+    QuadTypes quadType = QuadTypes::AdaptiveSimpson;
+    double quadAbsTol = 1e-6;
+    double quadRelTol = 1e-6;
+    unsigned int quadMaxSub = 30;
+    unsigned int quadMinSub = 0;
+    unsigned int quadPts = 5;
+    bool contDeriv = true;
+    bool basisNorm = true;
+    double nugget = 0.0;
+};
+
+// A strided 2-D array (the reference's StridedMatrix = View<T**, LayoutStride>,
+// MParT/Utilities/ArrayConversions.h:17).  Points are rows x cols with one
+// column per point.  data may be device memory, or host memory for the
+// host-staging overloads.
+struct StridedMatrix {
+    double* data = nullptr;
+    int64_t rows = 0, cols = 0;
+    int64_t rowStride = 0, colStride = 0;
+    StridedMatrix() = default;
+    StridedMatrix(double* d, int64_t r, int64_t c, int64_t rs, int64_t cs)
+        : data(d), rows(r), cols(c), rowStride(rs), colStride(cs) {}
+    static StridedMatrix RowMajor(double* d, int64_t r, int64_t c) { return StridedMatrix(d, r, c, c, 1); }
+    bool empty() const { return data == nullptr || rows == 0 || cols == 0; }
+};
+
+// Compressed multi-index set (MParT/MultiIndices/FixedMultiIndexSet.h).
+class FixedMultiIndexSet {
+public:
+    // Total-order set (src/MultiIndices/FixedMultiIndexSet.cpp:208-233).
+    FixedMultiIndexSet(unsigned int dim, unsigned int maxOrder, unsigned int minOrder = 0);
+    // Compressed form; each term's nonzero dims are sorted increasingly.
+    FixedMultiIndexSet(unsigned int dim, std::vector<unsigned int> nzStarts, std::vector<unsigned int> nzDims,
+                       std::vector<unsigned int> nzOrders);
+    unsigned int Length() const { return dim_; }
+    unsigned int Size() const { return (unsigned int)nzStarts.size() - 1; }
+    std::vector<unsigned int> MaxDegrees() const { return maxDegrees; }
+    std::vector<unsigned int> IndexToMulti(unsigned int index) const;
+    int MultiToIndex(std::vector<unsigned int> const& multi) const;
+    std::vector<unsigned int> NonzeroDiagonalEntries() const;
+
+    std::vector<unsigned int> nzStarts, nzDims, nzOrders, maxDegrees;
+
+private:
+    unsigned int dim_;
+    void CalculateMaxDegrees();
+};
+
+struct ComponentProgram;
+struct MapWorkspace;
+
+// MParT/ParameterizedFunctionBase.h
+class ParameterizedFunctionBase {
+public:
+    ParameterizedFunctionBase(unsigned int inDim, unsigned int outDim, unsigned int nCoeffs)
+        : inputDim(inDim), outputDim(outDim), numCoeffs(nCoeffs) {}
+    virtual ~ParameterizedFunctionBase();
+
+    // Deep copy into coefficient storage owned by (or already wrapped by) this object
+    // (src/ParameterizedFunctionBase.cpp:185-207).  host = true for a host pointer.
+    virtual void SetCoeffs(const double* coeffs, unsigned int n, bool host = false, cudaStream_t stream = 0);
+    // Alias caller-owned device memory (src/ParameterizedFunctionBase.cpp:219-228).
+    virtual void WrapCoeffs(double* deviceCoeffs, unsigned int n);
+    double* Coeffs() const { return coeffs_; }
+    bool CheckCoefficients() const { return coeffs_ != nullptr; }
+    void CheckCoefficients(std::string const& functionName) const;
+    std::vector<double> CoeffMap() const;  // host copy
+
+    virtual void EvaluateImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream = 0) = 0;
+    virtual void GradientImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                              cudaStream_t stream = 0) = 0;
+    virtual void CoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                               cudaStream_t stream = 0) = 0;
+
+    const unsigned int inputDim, outputDim, numCoeffs;
+
+    // Asynchronous mode: calls neither synchronise nor read the status word;
+    // CheckStatus() does both later.  Needed for CUDA-graph capture.
+    void SetAsync(bool async) { async_ = async; }
+    bool Async() const { return async_; }
+
+protected:
+    virtual void OnCoeffsChanged() {}
+    double* coeffs_ = nullptr;
+    double* owned_ = nullptr;
+    bool async_ = false;
+};
+
+class MonotoneMapBase;
+
+// MParT/ConditionalMapBase.h
+class ConditionalMapBase : public ParameterizedFunctionBase {
+public:
+    using ParameterizedFunctionBase::ParameterizedFunctionBase;
+    virtual void LogDeterminantImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream = 0) = 0;
+    virtual void InverseImpl(StridedMatrix const& x1, StridedMatrix const& r, StridedMatrix const& output,
+                             cudaStream_t stream = 0) = 0;
+    virtual void LogDeterminantCoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                             cudaStream_t stream = 0) = 0;
+    virtual void LogDeterminantInputGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                             cudaStream_t stream = 0) = 0;
+};
+
+// Inverse solver options (MonotoneComponent.h:353-396).
+struct InverseOptions {
+    double xtol = 1e-6;
+    double ytol = 1e-6;
+};
+
+// Maps made of monotone components (a single MonotoneComponent or a
+// TriangularMap of them) share one execution engine.
+class MonotoneMapBase : public ConditionalMapBase {
+public:
+    MonotoneMapBase(unsigned int inDim, unsigned int outDim, unsigned int nCoeffs, MapOptions const& opts);
+    ~MonotoneMapBase() override;
+
+    void EvaluateImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream = 0) override;
+    void GradientImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                      cudaStream_t stream = 0) override;
+    void CoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                       cudaStream_t stream = 0) override;
+    void LogDeterminantImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream = 0) override;
+    void InverseImpl(StridedMatrix const& x1, StridedMatrix const& r, StridedMatrix const& output,
+                     cudaStream_t stream = 0) override;
+    void InverseImpl(StridedMatrix const& x1, StridedMatrix const& r, StridedMatrix const& output,
+                     InverseOptions const& opts, int* deviceInfo, cudaStream_t stream);
+    void LogDeterminantCoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                     cudaStream_t stream = 0) override;
+    void LogDeterminantInputGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                     cudaStream_t stream = 0) override;
+
+    // Fused forward + adjoint in one pass over the points.  Any output may be
+    // empty.  coeffGrad (device, numCoeffs) receives
+    //   sum_i [ sens(c,i) dT_c(x_i)/dc + logdetSens(i) d logdet(x_i)/dc ]
+    // and inputGrad (inputDim x N) the same combination of input gradients.
+    // logdetSens may be empty, in which case logdetSensScale is used for all points.
+    void FusedForwardAdjoint(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& logdetSens,
+                             double logdetSensScale, StridedMatrix const& outEval, StridedMatrix const& outLogDet,
+                             double* coeffGrad, StridedMatrix const& inputGrad, cudaStream_t stream = 0);
+
+    // Standard-normal reverse KL of every component at once
+    // (FastGaussianReverseKLObjective, src/MapObjective.cpp:93-234): per component
+    // loss_c = mean(0.5 T_c^2 - logdet_c) and its coefficient gradient.
+    // lossPerComp (device, outputDim) and grad (device, numCoeffs) are written.
+    void KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream = 0);
+
+    int CheckStatus(cudaStream_t stream = 0);  // synchronise, read and clear the status word
+    // Grow-only device buffer `slot` (0..7) of at least `bytes`, for host staging.
+    double* StagingBuffer(int slot, size_t bytes, cudaStream_t stream);
+    MapOptions const& Options() const { return opts_; }
+    unsigned int NumMonotoneComponents() const { return (unsigned int)parts_.size(); }
+
+    struct Part;
+    std::vector<Part> const& Parts() const { return parts_; }
+
+    struct Part {
+        std::shared_ptr<ComponentProgram> prog;
+        ParameterizedFunctionBase* owner;  // object holding the coefficients of this part
+        unsigned int coeffOffset;          // offset inside the owner's coefficients
+        unsigned int mapCoeffOffset;       // offset inside this map's coefficient vector
+        unsigned int outRow;
+    };
+
+protected:
+    MapOptions opts_;
+    std::vector<Part> parts_;
+    std::unique_ptr<MapWorkspace> ws_;
+    void Prepare(cudaStream_t stream);
+    void Finish(cudaStream_t stream, const char* fn);
+};
+
+// MParT/MonotoneComponent.h, constructed through MapFactory::CreateComponent.
+class MonotoneComponent : public MonotoneMapBase {
+public:
+    MonotoneComponent(FixedMultiIndexSet const& mset, MapOptions const& opts);
+    FixedMultiIndexSet const& GetMultiIndexSet() const { return mset_; }
+    std::vector<unsigned int> DiagonalCoeffIndices() const { return mset_.NonzeroDiagonalEntries(); }
+
+private:
+    FixedMultiIndexSet mset_;
+};
+
+// MParT/TriangularMap.h
+class TriangularMap : public MonotoneMapBase {
+public:
+    TriangularMap(std::vector<std::shared_ptr<ConditionalMapBase>> const& components, bool moveCoeffs = false);
+    void SetCoeffs(const double* coeffs, unsigned int n, bool host = false, cudaStream_t stream = 0) override;
+    void WrapCoeffs(double* deviceCoeffs, unsigned int n) override;
+    std::shared_ptr<ConditionalMapBase> GetComponent(unsigned int i) { return comps_.at(i); }
+    unsigned int NumComponents() const { return (unsigned int)comps_.size(); }
+
+private:
+    std::vector<std::shared_ptr<ConditionalMapBase>> comps_;
+};
+
+namespace MapFactory {
+// src/MapFactory.cpp:22-27 and :105-124.
+std::shared_ptr<ConditionalMapBase> CreateComponent(FixedMultiIndexSet const& mset, MapOptions opts);
+std::shared_ptr<ConditionalMapBase> CreateTriangular(unsigned int inputDim, unsigned int outputDim,
+                                                     unsigned int totalOrder, MapOptions options = MapOptions());
+}  // namespace MapFactory
+
+// Thrown when the rectified integrand overflows (the reference throws from
+// MonotoneIntegrand.h:183-190).
+struct IntegrandError : public std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+}  // namespace mpgb

@@ -1,0 +1,370 @@
+"""GB300-native monotone transport-map components (the per-point hot path of
+MParT) behind MParT's own ConditionalMapBase / TriangularMap interface.
+
+Python mirror of the reference's pybind module (bindings/python/src/*.cpp):
+the classes below forward to the C ABI in include/mpart_gb300.h.  Arrays may
+be torch tensors (CUDA tensors stay on the device) or numpy arrays (staged
+through the device inside the call).  Points are D x N, one column per point,
+like the reference's *Impl methods."""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from typing import Sequence
+
+import numpy as np
+
+from . import _capi
+from ._capi import IntegrandError, MpgbError, check, load, mpgb_map_options, mpgb_matrix
+
+__all__ = [
+    "BasisTypes", "PosFuncTypes", "QuadTypes", "MapOptions", "FixedMultiIndexSet", "ConditionalMapBase",
+    "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load",
+]
+
+
+class BasisTypes(enum.IntEnum):
+    ProbabilistHermite = 0
+    PhysicistHermite = 1
+    HermiteFunctions = 2
+
+
+class PosFuncTypes(enum.IntEnum):
+    Exp = 0
+    SoftPlus = 1
+
+
+class QuadTypes(enum.IntEnum):
+    ClenshawCurtis = 0
+    AdaptiveSimpson = 1
+    AdaptiveClenshawCurtis = 2
+
+
+class MapOptions:
+    """MParT/MapOptions.h:58-123 (same field names and defaults)."""
+
+    def __init__(self, **kw):
+        self.basisType = BasisTypes.ProbabilistHermite
+        self.posFuncType = PosFuncTypes.SoftPlus
+        self.quadType = QuadTypes.AdaptiveSimpson
+        self.quadAbsTol = 1e-6
+        self.quadRelTol = 1e-6
+        self.quadMaxSub = 30
+        self.quadMinSub = 0
+        self.quadPts = 5
+        self.contDeriv = True
+        self.basisNorm = True
+        self.nugget = 0.0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"MapOptions has no field {k}")
+            setattr(self, k, v)
+
+    def _c(self) -> mpgb_map_options:
+        return mpgb_map_options(int(self.basisType), int(self.posFuncType), int(self.quadType),
+                                float(self.quadAbsTol), float(self.quadRelTol), int(self.quadMaxSub),
+                                int(self.quadMinSub), int(self.quadPts), int(bool(self.contDeriv)),
+                                int(bool(self.basisNorm)), float(self.nugget))
+
+
+class FixedMultiIndexSet:
+    """Compressed multi-index set (MParT/MultiIndices/FixedMultiIndexSet.h).
+    ``FixedMultiIndexSet(dim, maxOrder)`` is the total-order set in the
+    reference's term order (src/MultiIndices/FixedMultiIndexSet.cpp:508-549)."""
+
+    def __init__(self, dim: int, maxOrder: int | None = None, *, nzStarts=None, nzDims=None, nzOrders=None):
+        self.dim = int(dim)
+        if maxOrder is not None:
+            starts, dims, orders = [], [], []
+            work = [0] * self.dim
+
+            def rec(d, rem):
+                if d < self.dim - 1:
+                    for p in range(rem + 1):
+                        work[d] = p
+                        rec(d + 1, rem - p)
+                else:
+                    for p in range(rem + 1):
+                        work[d] = p
+                        starts.append(len(dims))
+                        for i in range(self.dim):
+                            if work[i] > 0:
+                                dims.append(i)
+                                orders.append(work[i])
+            rec(0, int(maxOrder))
+            starts.append(len(dims))
+            nzStarts, nzDims, nzOrders = starts, dims, orders
+        self.nzStarts = np.ascontiguousarray(nzStarts, dtype=np.uint32)
+        self.nzDims = np.ascontiguousarray(nzDims if nzDims is not None else [], dtype=np.uint32)
+        self.nzOrders = np.ascontiguousarray(nzOrders if nzOrders is not None else [], dtype=np.uint32)
+
+    @classmethod
+    def from_multis(cls, multis):
+        """Terms given densely, one row per term."""
+        multis = np.asarray(multis, dtype=np.int64)
+        starts, dims, orders = [0], [], []
+        for row in multis:
+            for d, o in enumerate(row):
+                if o > 0:
+                    dims.append(d)
+                    orders.append(int(o))
+            starts.append(len(dims))
+        return cls(multis.shape[1], nzStarts=starts, nzDims=dims, nzOrders=orders)
+
+    def Size(self):
+        return len(self.nzStarts) - 1
+
+    def Length(self):
+        return self.dim
+
+    def IndexToMulti(self, i):
+        m = np.zeros(self.dim, dtype=np.int64)
+        for j in range(self.nzStarts[i], self.nzStarts[i + 1]):
+            m[self.nzDims[j]] = self.nzOrders[j]
+        return m
+
+
+def _is_torch(x):
+    return type(x).__module__.startswith("torch")
+
+
+def _stream_of(*arrs):
+    for a in arrs:
+        if a is not None and _is_torch(a) and a.is_cuda:
+            import torch
+            return C.c_void_p(torch.cuda.current_stream(a.device).cuda_stream)
+    return C.c_void_p(0)
+
+
+def _mat(x, allow_none=True) -> mpgb_matrix:
+    """A matrix view (pointer, shape, strides in elements) of a 2-D (or 1-D =
+    1 x N) float64 torch tensor or numpy array."""
+    if x is None:
+        if not allow_none:
+            raise ValueError("array required")
+        return mpgb_matrix(None, 0, 0, 0, 0)
+    if _is_torch(x):
+        if x.dtype.__repr__() != "torch.float64":
+            raise ValueError(f"Currently only tensors with float64 datatype can be converted.  Current dtype is {x.dtype}")
+        if x.dim() == 1:
+            return mpgb_matrix(C.c_void_p(x.data_ptr()), 1, x.shape[0], x.shape[0] * x.stride(0), x.stride(0))
+        if x.dim() != 2:
+            raise ValueError("Currently only 1d and 2d tensors can be converted.")
+        return mpgb_matrix(C.c_void_p(x.data_ptr()), x.shape[0], x.shape[1], x.stride(0), x.stride(1))
+    a = x
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64:
+        raise ValueError("expected a float64 numpy array or torch tensor")
+    if a.ndim == 1:
+        return mpgb_matrix(C.c_void_p(a.ctypes.data), 1, a.shape[0], a.shape[0] * (a.strides[0] // 8),
+                           a.strides[0] // 8)
+    return mpgb_matrix(C.c_void_p(a.ctypes.data), a.shape[0], a.shape[1], a.strides[0] // 8, a.strides[1] // 8)
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch(x):
+        return C.c_void_p(x.data_ptr())
+    return C.c_void_p(x.ctypes.data)
+
+
+def _zeros_like_dev(ref, shape):
+    if _is_torch(ref):
+        import torch
+        return torch.zeros(shape, dtype=torch.float64, device=ref.device)
+    return np.zeros(shape)
+
+
+class ConditionalMapBase:
+    """Handle on a map (MParT/ConditionalMapBase.h / ParameterizedFunctionBase.h)."""
+
+    def __init__(self, handle: C.c_void_p, keep: Sequence = ()):
+        self._h = handle
+        self._keep = list(keep)  # objects whose lifetime must cover this one (wrapped coefficients)
+        self._wrapped = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _capi._lib is not None:
+            _capi._lib.mpgb_map_destroy(h)
+            self._h = None
+
+    def _dims(self):
+        i, o, n = C.c_uint(), C.c_uint(), C.c_uint()
+        check(load().mpgb_map_dims(self._h, C.byref(i), C.byref(o), C.byref(n)))
+        return i.value, o.value, n.value
+
+    @property
+    def inputDim(self):
+        return self._dims()[0]
+
+    @property
+    def outputDim(self):
+        return self._dims()[1]
+
+    @property
+    def numCoeffs(self):
+        return self._dims()[2]
+
+    # ---- coefficients -------------------------------------------------
+    def SetCoeffs(self, coeffs):
+        """Deep copy (src/ParameterizedFunctionBase.cpp:185-207)."""
+        if _is_torch(coeffs) and coeffs.is_cuda:
+            c = coeffs.detach().contiguous().double()
+            check(load().mpgb_set_coeffs(self._h, C.c_void_p(c.data_ptr()), c.numel(), 0, _stream_of(c)))
+        else:
+            c = np.ascontiguousarray(np.asarray(coeffs.detach().cpu() if _is_torch(coeffs) else coeffs,
+                                                dtype=np.float64).reshape(-1))
+            check(load().mpgb_set_coeffs(self._h, C.c_void_p(c.ctypes.data), c.size, 1, C.c_void_p(0)))
+
+    def WrapCoeffs(self, coeffs):
+        """Aliases a CUDA float64 tensor (src/ParameterizedFunctionBase.cpp:219-228)."""
+        if not (_is_torch(coeffs) and coeffs.is_cuda and coeffs.is_contiguous()):
+            raise ValueError("WrapCoeffs needs a contiguous CUDA float64 tensor")
+        check(load().mpgb_wrap_coeffs(self._h, C.c_void_p(coeffs.data_ptr()), coeffs.numel()))
+        self._wrapped = coeffs
+
+    def CoeffMap(self):
+        out = np.zeros(self.numCoeffs)
+        check(load().mpgb_get_coeffs(self._h, C.c_void_p(out.ctypes.data), out.size))
+        return out
+
+    def SetAsync(self, flag: bool):
+        check(load().mpgb_set_async(self._h, int(bool(flag))))
+
+    def CheckStatus(self, stream=None):
+        st = C.c_int(0)
+        check(load().mpgb_check_status(self._h, stream if stream is not None else C.c_void_p(0), C.byref(st)))
+        return st.value
+
+    # ---- *Impl (caller-allocated outputs) ------------------------------
+    def EvaluateImpl(self, pts, out):
+        check(load().mpgb_evaluate(self._h, _mat(pts), _mat(out), _stream_of(pts, out)))
+
+    def LogDeterminantImpl(self, pts, out):
+        check(load().mpgb_log_determinant(self._h, _mat(pts), _mat(out), _stream_of(pts, out)))
+
+    def InverseImpl(self, x1, r, out, xtol=1e-6, ytol=1e-6, info=None):
+        check(load().mpgb_inverse(self._h, _mat(x1), _mat(r), _mat(out), float(xtol), float(ytol), _ptr(info),
+                                  _stream_of(x1, r, out)))
+
+    def CoeffGradImpl(self, pts, sens, out):
+        check(load().mpgb_coeff_grad(self._h, _mat(pts), _mat(sens), _mat(out), _stream_of(pts, sens, out)))
+
+    def GradientImpl(self, pts, sens, out):
+        check(load().mpgb_gradient(self._h, _mat(pts), _mat(sens), _mat(out), _stream_of(pts, sens, out)))
+
+    def LogDeterminantCoeffGradImpl(self, pts, out):
+        check(load().mpgb_log_determinant_coeff_grad(self._h, _mat(pts), _mat(out), _stream_of(pts, out)))
+
+    def LogDeterminantInputGradImpl(self, pts, out):
+        check(load().mpgb_log_determinant_input_grad(self._h, _mat(pts), _mat(out), _stream_of(pts, out)))
+
+    def FusedForwardAdjointImpl(self, pts, sens=None, logdet_sens=None, logdet_sens_scale=0.0, out_eval=None,
+                                out_logdet=None, coeff_grad=None, input_grad=None):
+        check(load().mpgb_fused_fwd_adj(self._h, _mat(pts), _mat(sens), _mat(logdet_sens), float(logdet_sens_scale),
+                                        _mat(out_eval), _mat(out_logdet), _ptr(coeff_grad), _mat(input_grad),
+                                        _stream_of(pts, sens, out_eval)))
+
+    # ---- allocating versions (the reference's Evaluate(pts) etc.) --------
+    def Evaluate(self, pts):
+        out = _zeros_like_dev(pts, (self.outputDim, pts.shape[1]))
+        self.EvaluateImpl(pts, out)
+        return out
+
+    def LogDeterminant(self, pts):
+        out = _zeros_like_dev(pts, (pts.shape[1],))
+        self.LogDeterminantImpl(pts, out)
+        return out
+
+    def Inverse(self, x1, r, xtol=1e-6, ytol=1e-6):
+        out = _zeros_like_dev(r, (self.outputDim, r.shape[1]))
+        self.InverseImpl(x1, r, out, xtol, ytol)
+        return out
+
+    def CoeffGrad(self, pts, sens):
+        out = _zeros_like_dev(pts, (self.numCoeffs, pts.shape[1]))
+        self.CoeffGradImpl(pts, sens, out)
+        return out
+
+    def Gradient(self, pts, sens):
+        out = _zeros_like_dev(pts, (self.inputDim, pts.shape[1]))
+        self.GradientImpl(pts, sens, out)
+        return out
+
+    def LogDeterminantCoeffGrad(self, pts):
+        out = _zeros_like_dev(pts, (self.numCoeffs, pts.shape[1]))
+        self.LogDeterminantCoeffGradImpl(pts, out)
+        return out
+
+    def LogDeterminantInputGrad(self, pts):
+        out = _zeros_like_dev(pts, (self.inputDim, pts.shape[1]))
+        self.LogDeterminantInputGradImpl(pts, out)
+        return out
+
+    def KLObjective(self, pts):
+        """Per-component standard-normal reverse KL (FastGaussianReverseKLObjective)
+        and its coefficient gradient: returns (loss per component, gradient)."""
+        loss = _zeros_like_dev(pts, (self.outputDim,))
+        grad = _zeros_like_dev(pts, (self.numCoeffs,))
+        check(load().mpgb_kl_objective(self._h, _mat(pts), _ptr(loss), _ptr(grad), _stream_of(pts)))
+        return loss, grad
+
+    def torch(self, store_coeffs=True, return_logdet=False):
+        from .torch import TorchConditionalMapBase
+        return TorchConditionalMapBase(self, store_coeffs=store_coeffs, return_logdet=return_logdet)
+
+
+class TriangularMap(ConditionalMapBase):
+    """TriangularMap(components, moveCoeffs) (src/TriangularMap.cpp:9-62)."""
+
+    def __init__(self, components: Sequence[ConditionalMapBase] = (), moveCoeffs: bool = False, *, _handle=None):
+        if _handle is not None:
+            super().__init__(_handle)
+            return
+        arr = (C.c_void_p * len(components))(*[c._h for c in components])
+        h = C.c_void_p()
+        check(load().mpgb_create_triangular_from_components(arr, len(components), int(bool(moveCoeffs)),
+                                                            C.byref(h)))
+        super().__init__(h, keep=list(components))
+
+    def NumComponents(self):
+        n = C.c_uint()
+        check(load().mpgb_map_num_components(self._h, C.byref(n)))
+        return n.value
+
+    def GetComponent(self, i):
+        h = C.c_void_p()
+        check(load().mpgb_map_get_component(self._h, int(i), C.byref(h)))
+        return ConditionalMapBase(h, keep=[self])
+
+
+def CreateComponent(mset: FixedMultiIndexSet, opts: MapOptions | None = None) -> ConditionalMapBase:
+    """MapFactory::CreateComponent (src/MapFactory.cpp:22-27)."""
+    opts = opts or MapOptions()
+    o = opts._c()
+    h = C.c_void_p()
+    s = mset.nzStarts
+    d = mset.nzDims if mset.nzDims.size else np.zeros(1, np.uint32)
+    r = mset.nzOrders if mset.nzOrders.size else np.zeros(1, np.uint32)
+    up = C.POINTER(C.c_uint)
+    check(load().mpgb_create_component(mset.dim, mset.Size(), s.ctypes.data_as(up), d.ctypes.data_as(up),
+                                       r.ctypes.data_as(up), C.byref(o), C.byref(h)))
+    return ConditionalMapBase(h)
+
+
+def CreateTriangular(inputDim: int, outputDim: int, totalOrder: int, opts: MapOptions | None = None) -> TriangularMap:
+    """MapFactory::CreateTriangular (src/MapFactory.cpp:105-124)."""
+    opts = opts or MapOptions()
+    o = opts._c()
+    h = C.c_void_p()
+    check(load().mpgb_create_triangular(int(inputDim), int(outputDim), int(totalOrder), C.byref(o), C.byref(h)))
+    return TriangularMap(_handle=h)
+
+
+def fp64_probe(blocks=152 * 8, threads=256, iters=4096):
+    """DFMA throughput probe; returns (TFLOP/s, ms)."""
+    ms = C.c_float(0)
+    check(load().mpgb_fp64_probe(blocks, threads, iters, C.c_void_p(0), C.byref(ms)))
+    flops = 2.0 * 8 * blocks * threads * iters
+    return flops / (ms.value * 1e-3) / 1e12, ms.value

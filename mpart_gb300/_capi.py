@@ -1,0 +1,118 @@
+"""ctypes binding of include/mpart_gb300.h.  Loads the in-tree
+libmpart_gb300.so and fails loudly when it is missing: there is no CPU
+fallback for the product path."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmpart_gb300.so")
+
+MPGB_OK = 0
+MPGB_ERR_INVALID_ARGUMENT = -1
+MPGB_ERR_RUNTIME = -2
+MPGB_ERR_CUDA = -3
+MPGB_ERR_INTEGRAND = -4
+
+
+class mpgb_map_options(C.Structure):
+    _fields_ = [
+        ("basis_type", C.c_int),
+        ("pos_func_type", C.c_int),
+        ("quad_type", C.c_int),
+        ("quad_abs_tol", C.c_double),
+        ("quad_rel_tol", C.c_double),
+        ("quad_max_sub", C.c_uint),
+        ("quad_min_sub", C.c_uint),
+        ("quad_pts", C.c_uint),
+        ("cont_deriv", C.c_int),
+        ("basis_norm", C.c_int),
+        ("nugget", C.c_double),
+    ]
+
+
+class mpgb_matrix(C.Structure):
+    _fields_ = [
+        ("data", C.c_void_p),
+        ("rows", C.c_int64),
+        ("cols", C.c_int64),
+        ("row_stride", C.c_int64),
+        ("col_stride", C.c_int64),
+    ]
+
+
+# Every symbol the header declares, with its signature.
+_MAP = C.c_void_p
+_MAPP = C.POINTER(C.c_void_p)
+_UP = C.POINTER(C.c_uint)
+SIGNATURES = {
+    "mpgb_version": (C.c_char_p, []),
+    "mpgb_last_error": (C.c_char_p, []),
+    "mpgb_map_options_default": (C.c_int, [C.POINTER(mpgb_map_options)]),
+    "mpgb_create_component": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_create_component_total_order": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_create_triangular": (C.c_int, [C.c_uint, C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_create_triangular_from_components": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint, C.c_int, _MAPP]),
+    "mpgb_map_destroy": (C.c_int, [_MAP]),
+    "mpgb_map_dims": (C.c_int, [_MAP, _UP, _UP, _UP]),
+    "mpgb_map_num_components": (C.c_int, [_MAP, _UP]),
+    "mpgb_map_get_component": (C.c_int, [_MAP, C.c_uint, _MAPP]),
+    "mpgb_set_coeffs": (C.c_int, [_MAP, C.c_void_p, C.c_uint, C.c_int, C.c_void_p]),
+    "mpgb_wrap_coeffs": (C.c_int, [_MAP, C.c_void_p, C.c_uint]),
+    "mpgb_get_coeffs": (C.c_int, [_MAP, C.c_void_p, C.c_uint]),
+    "mpgb_coeffs_device_ptr": (C.c_int, [_MAP, C.POINTER(C.c_void_p)]),
+    "mpgb_set_async": (C.c_int, [_MAP, C.c_int]),
+    "mpgb_check_status": (C.c_int, [_MAP, C.c_void_p, C.POINTER(C.c_int)]),
+    "mpgb_evaluate": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_log_determinant": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_inverse": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, C.c_double, C.c_void_p,
+                               C.c_void_p]),
+    "mpgb_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_gradient": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_log_determinant_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_log_determinant_input_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
+    "mpgb_fused_fwd_adj": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, mpgb_matrix,
+                                     mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
+    "mpgb_kl_objective": (C.c_int, [_MAP, mpgb_matrix, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"libmpart_gb300.so not found at {LIB_PATH}; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (no CPU fallback exists)")
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class MpgbError(RuntimeError):
+    pass
+
+
+class IntegrandError(MpgbError):
+    pass
+
+
+def check(rc: int):
+    if rc == MPGB_OK:
+        return
+    msg = load().mpgb_last_error().decode(errors="replace")
+    if rc == MPGB_ERR_INVALID_ARGUMENT:
+        raise ValueError(msg)
+    if rc == MPGB_ERR_INTEGRAND:
+        raise IntegrandError(msg)
+    raise MpgbError(msg)

@@ -1,0 +1,1581 @@
+// Host side of the GB300 monotone-component path: multi-index sets, the
+// prefix-tree planner, the map classes of include/mpart_gb300.hpp and the C
+// ABI of include/mpart_gb300.h.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/mpart_gb300.h"
+#include "../../include/mpart_gb300.hpp"
+#include "mpgb_launch.h"
+#include "mpgb_types.h"
+
+namespace mpgb {
+
+static const double kPiHost = 3.14159265358979323846;
+
+#define MPGB_CUDA(call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            std::ostringstream os_;                                                                       \
+            os_ << "CUDA error " << cudaGetErrorName(e_) << " (" << cudaGetErrorString(e_) << ") at " #call; \
+            throw CudaError(os_.str());                                                                   \
+        }                                                                                                 \
+    } while (0)
+
+struct CudaError : public std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// ---------------------------------------------------------------------------
+// FixedMultiIndexSet
+// ---------------------------------------------------------------------------
+static void fillTotalOrder(unsigned dim, unsigned maxOrder, unsigned minOrder, std::vector<unsigned>& work,
+                           unsigned currDim, std::vector<unsigned>& starts, std::vector<unsigned>& dims,
+                           std::vector<unsigned>& orders) {
+    // Recursive enumeration of FixedMultiIndexSet::FillTotalOrder
+    // (src/MultiIndices/FixedMultiIndexSet.cpp:508-549): dimension 0 outermost,
+    // the last dimension fastest; nonzeros listed in increasing dimension.
+    if (currDim + 1 < dim) {
+        for (unsigned p = 0; p <= maxOrder; ++p) {
+            work[currDim] = p;
+            fillTotalOrder(dim, maxOrder - p, minOrder, work, currDim + 1, starts, dims, orders);
+        }
+    } else {
+        for (unsigned p = 0; p <= maxOrder; ++p) {
+            work[currDim] = p;
+            unsigned tot = 0;
+            for (unsigned i = 0; i <= currDim; ++i) tot += work[i];
+            if (tot >= minOrder) {
+                starts.push_back((unsigned)dims.size());
+                for (unsigned i = 0; i < dim; ++i)
+                    if (work[i] > 0) {
+                        dims.push_back(i);
+                        orders.push_back(work[i]);
+                    }
+            }
+        }
+    }
+}
+
+FixedMultiIndexSet::FixedMultiIndexSet(unsigned int dim, unsigned int maxOrder, unsigned int minOrder) : dim_(dim) {
+    if (dim == 0) throw std::invalid_argument("FixedMultiIndexSet: dimension must be positive.");
+    std::vector<unsigned> work(dim, 0);
+    fillTotalOrder(dim, maxOrder, minOrder, work, 0, nzStarts, nzDims, nzOrders);
+    nzStarts.push_back((unsigned)nzDims.size());
+    CalculateMaxDegrees();
+}
+
+FixedMultiIndexSet::FixedMultiIndexSet(unsigned int dim, std::vector<unsigned int> starts,
+                                       std::vector<unsigned int> dims, std::vector<unsigned int> orders)
+    : nzStarts(std::move(starts)), nzDims(std::move(dims)), nzOrders(std::move(orders)), dim_(dim) {
+    if (dim == 0) throw std::invalid_argument("FixedMultiIndexSet: dimension must be positive.");
+    if (nzStarts.empty() || nzStarts.front() != 0 || nzStarts.back() != nzDims.size() ||
+        nzDims.size() != nzOrders.size())
+        throw std::invalid_argument("FixedMultiIndexSet: inconsistent compressed arrays.");
+    for (size_t t = 0; t + 1 < nzStarts.size(); ++t) {
+        if (nzStarts[t + 1] < nzStarts[t]) throw std::invalid_argument("FixedMultiIndexSet: nzStarts must increase.");
+        // Sort each term's nonzeros by dimension (FixedMultiIndexSet.h:36-41).
+        std::vector<std::pair<unsigned, unsigned>> nz;
+        for (unsigned i = nzStarts[t]; i < nzStarts[t + 1]; ++i) {
+            if (nzDims[i] >= dim) throw std::invalid_argument("FixedMultiIndexSet: dimension index out of range.");
+            if (nzOrders[i] == 0) throw std::invalid_argument("FixedMultiIndexSet: stored orders must be nonzero.");
+            nz.push_back({nzDims[i], nzOrders[i]});
+        }
+        std::sort(nz.begin(), nz.end());
+        for (size_t j = 1; j < nz.size(); ++j)
+            if (nz[j].first == nz[j - 1].first)
+                throw std::invalid_argument("FixedMultiIndexSet: repeated dimension within a term.");
+        for (size_t j = 0; j < nz.size(); ++j) {
+            nzDims[nzStarts[t] + j] = nz[j].first;
+            nzOrders[nzStarts[t] + j] = nz[j].second;
+        }
+    }
+    CalculateMaxDegrees();
+}
+
+void FixedMultiIndexSet::CalculateMaxDegrees() {
+    maxDegrees.assign(dim_, 0);
+    for (size_t i = 0; i < nzOrders.size(); ++i) maxDegrees[nzDims[i]] = std::max(maxDegrees[nzDims[i]], nzOrders[i]);
+}
+
+std::vector<unsigned int> FixedMultiIndexSet::IndexToMulti(unsigned int index) const {
+    if (index >= Size()) throw std::out_of_range("FixedMultiIndexSet::IndexToMulti: index out of range.");
+    std::vector<unsigned int> m(dim_, 0);
+    for (unsigned i = nzStarts[index]; i < nzStarts[index + 1]; ++i) m[nzDims[i]] = nzOrders[i];
+    return m;
+}
+
+int FixedMultiIndexSet::MultiToIndex(std::vector<unsigned int> const& multi) const {
+    for (unsigned t = 0; t < Size(); ++t)
+        if (IndexToMulti(t) == multi) return (int)t;
+    return -1;
+}
+
+std::vector<unsigned int> FixedMultiIndexSet::NonzeroDiagonalEntries() const {
+    std::vector<unsigned int> out;
+    for (unsigned t = 0; t < Size(); ++t)
+        if (nzStarts[t + 1] > nzStarts[t] && nzDims[nzStarts[t + 1] - 1] == dim_ - 1) out.push_back(t);
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// Component program: the multi-index set reorganised as a prefix tree over
+// the leading coordinates (see mpgb_device.cuh for the factorisation).
+// ---------------------------------------------------------------------------
+template <class T>
+static T* toDevice(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    T* d = nullptr;
+    MPGB_CUDA(cudaMalloc(&d, v.size() * sizeof(T)));
+    MPGB_CUDA(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return d;
+}
+
+struct ComponentProgram {
+    int D = 0, P = 0, nB = 0, nNodes = 0, nSlots = 0, nCNodes = 0, maxDepth = 0, numTerms = 0;
+    std::vector<uint32_t> nodeA, nodeSlot, nodeC;
+    std::vector<uint16_t> nodeCRows;
+    std::vector<int32_t> slotTerm, leadDeg, rowOff;
+    uint32_t *dNodeA = nullptr, *dNodeSlot = nullptr, *dNodeC = nullptr;
+    uint16_t* dNodeCRows = nullptr;
+    int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr;
+    // Work per point (FP64 operations of phases A and C), for load balancing.
+    double weight = 1.0;
+
+    explicit ComponentProgram(FixedMultiIndexSet const& ms) {
+        D = (int)ms.Length();
+        numTerms = (int)ms.Size();
+        const auto& md = ms.maxDegrees;
+        P = (int)md[D - 1];
+        if (P > kMaxLastOrder) {
+            std::ostringstream os;
+            os << "MonotoneComponent: order " << P << " in the last input exceeds the supported maximum "
+               << kMaxLastOrder << ".";
+            throw std::invalid_argument(os.str());
+        }
+        leadDeg.resize(std::max(D - 1, 0));
+        rowOff.resize(std::max(D - 1, 0));
+        for (int d = 0; d + 1 < D; ++d) {
+            leadDeg[d] = (int)md[d];
+            rowOff[d] = nB;
+            nB += (int)md[d];
+        }
+        if (nB >= (1 << 14)) throw std::invalid_argument("MonotoneComponent: basis table too large.");
+        // Trie over the leading-coordinate prefixes.
+        struct TNode {
+            int parent, depth, dim, order;
+            std::map<std::pair<int, int>, int> children;
+            std::map<int, int> kTerm;
+        };
+        std::vector<TNode> tn;
+        tn.push_back({-1, 0, 0, 0, {}, {}});
+        for (int t = 0; t < numTerms; ++t) {
+            int b = (int)ms.nzStarts[t], e = (int)ms.nzStarts[t + 1];
+            int k = 0;
+            if (e > b && (int)ms.nzDims[e - 1] == D - 1) {
+                k = (int)ms.nzOrders[e - 1];
+                --e;
+            }
+            int cur = 0;
+            for (int i = b; i < e; ++i) {
+                std::pair<int, int> key((int)ms.nzDims[i], (int)ms.nzOrders[i]);
+                auto it = tn[cur].children.find(key);
+                if (it == tn[cur].children.end()) {
+                    TNode nn{cur, tn[cur].depth + 1, key.first, key.second, {}, {}};
+                    tn.push_back(nn);
+                    int id = (int)tn.size() - 1;
+                    tn[cur].children[key] = id;
+                    cur = id;
+                } else {
+                    cur = it->second;
+                }
+            }
+            if (tn[cur].kTerm.count(k))
+                throw std::invalid_argument("MonotoneComponent: the multi-index set contains a repeated term.");
+            tn[cur].kTerm[k] = t;
+        }
+        // DFS pre-order, children in increasing (dim, order).
+        std::vector<int> order;
+        std::vector<int> stack{0};
+        while (!stack.empty()) {
+            int n = stack.back();
+            stack.pop_back();
+            order.push_back(n);
+            for (auto it = tn[n].children.rbegin(); it != tn[n].children.rend(); ++it) stack.push_back(it->second);
+        }
+        nNodes = (int)order.size();
+        std::vector<int> slotOf(tn.size(), -1), nkOf(tn.size(), 0), browOf(tn.size(), 0);
+        for (int n : order) {
+            const TNode& t = tn[n];
+            if (t.depth > kMaxDepth) throw std::invalid_argument("MonotoneComponent: too many nonzero factors in a term.");
+            maxDepth = std::max(maxDepth, t.depth);
+            int nk = t.kTerm.empty() ? 0 : t.kTerm.rbegin()->first + 1;
+            int brow = (t.depth > 0) ? rowOff[t.dim] + t.order - 1 : 0;
+            int slot = (int)slotTerm.size();
+            for (int k = 0; k < nk; ++k) {
+                auto it = t.kTerm.find(k);
+                slotTerm.push_back(it == t.kTerm.end() ? -1 : it->second);
+            }
+            slotOf[n] = slot;
+            nkOf[n] = nk;
+            browOf[n] = brow;
+            nodeA.push_back((uint32_t)t.depth | ((uint32_t)nk << 5) | ((uint32_t)t.dim << 10) | ((uint32_t)brow << 18));
+            nodeSlot.push_back((uint32_t)slot);
+        }
+        nSlots = (int)slotTerm.size();
+        if (nSlots >= (1 << 22)) throw std::invalid_argument("MonotoneComponent: too many terms.");
+        // Nodes carrying terms, grouped by (depth, nk) for uniform warps in the reduction.
+        std::vector<int> cn;
+        for (int n : order)
+            if (nkOf[n] > 0) cn.push_back(n);
+        std::stable_sort(cn.begin(), cn.end(), [&](int a, int b) {
+            if (tn[a].depth != tn[b].depth) return tn[a].depth < tn[b].depth;
+            return nkOf[a] < nkOf[b];
+        });
+        nCNodes = (int)cn.size();
+        nodeCRows.assign((size_t)nCNodes * kMaxDepth, 0);
+        double opsA = 0, opsC = 0;
+        for (int j = 0; j < nCNodes; ++j) {
+            int n = cn[j];
+            nodeC.push_back((uint32_t)tn[n].depth | ((uint32_t)nkOf[n] << 5) | ((uint32_t)slotOf[n] << 10));
+            std::vector<int> path;
+            for (int q = n; q != 0; q = tn[q].parent) path.push_back(browOf[q]);
+            std::reverse(path.begin(), path.end());
+            for (size_t q = 0; q < path.size(); ++q) nodeCRows[(size_t)j * kMaxDepth + q] = (uint16_t)path[q];
+            opsC += std::max(tn[n].depth - 1, 0) + nkOf[n];
+        }
+        for (int n : order) opsA += (tn[n].depth > 0 ? 1 : 0) + nkOf[n];
+        weight = opsA + opsC + 3.0 * nB + 60.0;
+        dNodeA = toDevice(nodeA);
+        dNodeSlot = toDevice(nodeSlot);
+        dNodeC = toDevice(nodeC);
+        dNodeCRows = toDevice(nodeCRows);
+        dSlotTerm = toDevice(slotTerm);
+        dLeadDeg = toDevice(leadDeg);
+        dRowOff = toDevice(rowOff);
+    }
+    ~ComponentProgram() {
+        cudaFree(dNodeA);
+        cudaFree(dNodeSlot);
+        cudaFree(dNodeC);
+        cudaFree(dNodeCRows);
+        cudaFree(dSlotTerm);
+        cudaFree(dLeadDeg);
+        cudaFree(dRowOff);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Per-map device workspace (grow-only buffers).
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t b, cudaStream_t s) {
+        if (b <= bytes) return;
+        if (p) {
+            MPGB_CUDA(cudaStreamSynchronize(s));
+            MPGB_CUDA(cudaFree(p));
+            p = nullptr;
+        }
+        size_t nb = std::max<size_t>(b, 256);
+        MPGB_CUDA(cudaMalloc(&p, nb));
+        bytes = nb;
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    template <class T>
+    T* as() const { return (T*)p; }
+};
+
+struct GatherDescHost {
+    const double* src;
+    const int32_t* slotTerm;
+    int slotOffset;
+    int nSlots;
+};
+
+struct MapWorkspace {
+    DevBuf comps, cm, gather, items, partials, rowBase, lossPart, lossSlots, logdetRows, status;
+    DevBuf stage[8];
+    std::vector<CompDesc> hostComps;
+    std::vector<GatherDescHost> hostGather;
+    int totalSlots = 0;
+    int numSMs = 0;
+    QuadParams quad{};
+    BasisConsts bc{};
+    int pmax = 1, dmax = 1, nBmax = 0, depthMax = 0;
+    bool built = false;
+};
+
+}  // namespace mpgb
+
+// Coefficient gather over several components (separate translation unit needs no kernel here).
+namespace mpgb {
+__global__ void gatherMultiKernel(const GatherDescHost* descs, int nComps, double* cm) {
+    const int c = blockIdx.y;
+    if (c >= nComps) return;
+    const GatherDescHost g = descs[c];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < g.nSlots; s += gridDim.x * blockDim.x) {
+        const int t = g.slotTerm[s];
+        cm[g.slotOffset + s] = (t >= 0) ? g.src[t] : 0.0;
+    }
+}
+
+__global__ void sumRowsKernel(const double* rows, int nRows, long long N, double* out, long long outStride) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    double s = 0.0;
+    for (int r = 0; r < nRows; ++r) s += rows[(long long)r * N + i];
+    out[i * outStride] = s;
+}
+}  // namespace mpgb
+
+namespace mpgb {
+
+// ---------------------------------------------------------------------------
+// ParameterizedFunctionBase
+// ---------------------------------------------------------------------------
+ParameterizedFunctionBase::~ParameterizedFunctionBase() {
+    if (owned_) cudaFree(owned_);
+}
+
+void ParameterizedFunctionBase::SetCoeffs(const double* coeffs, unsigned int n, bool host, cudaStream_t stream) {
+    if (n != numCoeffs) {
+        std::ostringstream os;
+        os << "Error in ParameterizedFunctionBase<MemorySpace>::SetCoeffs.  Expected coefficient vector with size "
+           << numCoeffs << ", but new coefficients have size " << n << ".";
+        throw std::invalid_argument(os.str());
+    }
+    if (!coeffs_) {
+        if (!owned_ && numCoeffs > 0) MPGB_CUDA(cudaMalloc(&owned_, numCoeffs * sizeof(double)));
+        coeffs_ = owned_;
+    }
+    if (numCoeffs > 0) {
+        if (host) {
+            MPGB_CUDA(cudaMemcpyAsync(coeffs_, coeffs, n * sizeof(double), cudaMemcpyHostToDevice, stream));
+            MPGB_CUDA(cudaStreamSynchronize(stream));
+        } else {
+            MPGB_CUDA(cudaMemcpyAsync(coeffs_, coeffs, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        }
+    }
+    OnCoeffsChanged();
+}
+
+void ParameterizedFunctionBase::WrapCoeffs(double* deviceCoeffs, unsigned int n) {
+    if (n != numCoeffs) {
+        std::ostringstream os;
+        os << "Error in ParameterizedFunctionBase<MemorySpace>::WrapCoeffs.  Expected coefficient vector with size "
+           << numCoeffs << ", but new coefficients have size " << n << ".";
+        throw std::invalid_argument(os.str());
+    }
+    coeffs_ = deviceCoeffs;
+    OnCoeffsChanged();
+}
+
+void ParameterizedFunctionBase::CheckCoefficients(std::string const& functionName) const {
+    if (!CheckCoefficients()) {
+        std::ostringstream os;
+        os << "Error in \"" << functionName
+           << "\", the coefficients have not been set yet.  Make sure to call SetCoeffs() before calling this function.";
+        throw std::runtime_error(os.str());
+    }
+}
+
+std::vector<double> ParameterizedFunctionBase::CoeffMap() const {
+    CheckCoefficients("CoeffMap");
+    std::vector<double> h(numCoeffs);
+    if (numCoeffs) MPGB_CUDA(cudaMemcpy(h.data(), coeffs_, numCoeffs * sizeof(double), cudaMemcpyDeviceToHost));
+    return h;
+}
+
+// ---------------------------------------------------------------------------
+// MonotoneMapBase
+// ---------------------------------------------------------------------------
+static void ccRule(unsigned numPts, double* wts, double* pts) {
+    // Clenshaw-Curtis points and weights on [-1,1] (Quadrature.h:212-258).
+    if (numPts == 1) { pts[0] = 0.0; wts[0] = 2.0; return; }
+    for (unsigned i = 0; i < numPts; ++i) pts[i] = std::cos((numPts - (i + 1)) * kPiHost / (numPts - 1));
+    pts[0] = -1.0;
+    if (numPts % 2 == 1) pts[(numPts - 1) / 2] = 0.0;
+    pts[numPts - 1] = 1.0;
+    for (unsigned i = 0; i < numPts; ++i) {
+        wts[i] = 1.0;
+        const double theta = i * kPiHost / (numPts - 1);
+        for (unsigned j = 0; j < (numPts - 1) / 2; ++j) {
+            const double b = (2 * (j + 1) == (numPts - 1)) ? 1.0 : 2.0;
+            wts[i] = wts[i] - b * std::cos(2.0 * (j + 1) * theta) / (4 * (j + 1) * (j + 1) - 1);
+        }
+    }
+    wts[0] = wts[0] / (numPts - 1.0);
+    for (unsigned i = 1; i < numPts - 1; ++i) wts[i] = 2.0 * wts[i] / (numPts - 1.0);
+    wts[numPts - 1] = wts[numPts - 1] / (numPts - 1.0);
+}
+
+static unsigned factorialU(unsigned d) {
+    unsigned out = 1;
+    for (unsigned i = 2; i <= d; ++i) out *= i;
+    return out;
+}
+
+static void validateOptions(MapOptions const& o) {
+    if (o.quadType != QuadTypes::AdaptiveClenshawCurtis)
+        throw std::invalid_argument("MapOptions: only quadType = AdaptiveClenshawCurtis is provided on this path.");
+    if (o.basisType == BasisTypes::PhysicistHermite)
+        throw std::invalid_argument("MapOptions: basisType must be ProbabilistHermite or HermiteFunctions.");
+    if (!o.contDeriv)
+        throw std::invalid_argument("MapOptions: contDeriv = false (discrete derivative) is not provided on this path.");
+    if (o.quadMaxSub < 1 || o.quadMaxSub > (unsigned)kMaxSubCap)
+        throw std::invalid_argument("MapOptions: quadMaxSub must be in [1, 32].");
+    if (o.quadMinSub >= o.quadMaxSub) throw std::invalid_argument("MapOptions: quadMinSub must be below quadMaxSub.");
+    if (o.quadPts < 3) throw std::invalid_argument("MapOptions: quadPts must be at least 3.");
+    if (!(o.quadAbsTol >= 0) || !(o.quadRelTol >= 0)) throw std::invalid_argument("MapOptions: negative tolerance.");
+    if (!(o.nugget >= 0)) throw std::invalid_argument("MapOptions: nugget must be non-negative.");
+}
+
+MonotoneMapBase::MonotoneMapBase(unsigned int inDim, unsigned int outDim, unsigned int nCoeffs, MapOptions const& opts)
+    : ConditionalMapBase(inDim, outDim, nCoeffs), opts_(opts), ws_(new MapWorkspace()) {}
+
+MonotoneMapBase::~MonotoneMapBase() = default;
+
+// Builds the launch tables on first use.
+void MonotoneMapBase::Prepare(cudaStream_t stream) {
+    MapWorkspace& W = *ws_;
+    if (!W.built) {
+        int dev = 0;
+        MPGB_CUDA(cudaGetDevice(&dev));
+        MPGB_CUDA(cudaDeviceGetAttribute(&W.numSMs, cudaDevAttrMultiProcessorCount, dev));
+        // Quadrature rule: level = (unsigned) log2(quadPts - 2) (src/MapFactoryImpl4.cpp:18).
+        const unsigned level = (unsigned)std::log2((double)(opts_.quadPts - 2));
+        if (level < 1 || (int)level > kMaxQuadLevel)
+            throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
+        QuadParams& q = W.quad;
+        q.nCoarse = (1 << level) + 1;
+        q.nFine = (1 << (level + 1)) + 1;
+        ccRule(q.nCoarse, q.cWts, q.cPts);
+        ccRule(q.nFine, q.fWts, q.fPts);
+        q.maxSub = (int)opts_.quadMaxSub;
+        q.minSub = (int)opts_.quadMinSub;
+        q.absTol = opts_.quadAbsTol;
+        q.relTol = opts_.quadRelTol;
+        q.maxIntervals = 1LL << 24;
+        BasisConsts& b = W.bc;
+        const bool norm = opts_.basisNorm;
+        for (int k = 0; k <= kMaxLastOrder; ++k) {
+            b.invNorm[k] = norm ? 1.0 / std::sqrt(std::sqrt(2.0 * kPiHost) * factorialU(k)) : 1.0;
+            double fact = 1.0;
+            for (int i = 2; i <= k; ++i) fact *= i;
+            b.hfScale[k] = std::pow(kPiHost, -0.25) * std::pow(std::pow(2.0, k) * fact, -0.5);
+        }
+        for (int i = 0; i < kMaxLastOrder + 8; ++i) {
+            b.hfR1[i] = std::sqrt(0.5 * (i - 1.0 > 0 ? i - 1.0 : 0.0));
+            b.hfR2[i] = i > 0 ? 1.0 / std::sqrt(0.5 * i) : 0.0;
+        }
+        b.piQuarter = std::pow(kPiHost, -0.25);
+        // phit_k(0).
+        {
+            double he[kMaxLastOrder + 1], H[kMaxLastOrder + 1];
+            he[0] = 1.0; he[1] = 0.0;
+            H[0] = 1.0; H[1] = 0.0;
+            for (int k = 2; k <= kMaxLastOrder; ++k) {
+                he[k] = -(k - 1.0) * he[k - 2];
+                H[k] = -2.0 * (k - 1.0) * H[k - 2];
+            }
+            b.v0[0] = 1.0;
+            for (int k = 1; k <= kMaxLastOrder; ++k) {
+                if (opts_.basisType == BasisTypes::HermiteFunctions)
+                    b.v0[k] = (k == 1) ? 0.0 : b.hfScale[k - 2] * H[k - 2];
+                else
+                    b.v0[k] = he[k] * b.invNorm[k];
+            }
+        }
+        // Component descriptors.
+        W.hostComps.clear();
+        W.hostGather.clear();
+        int slotOff = 0, pm = 1;
+        W.dmax = 1; W.nBmax = 0; W.depthMax = 0;
+        for (auto& pt : parts_) {
+            const ComponentProgram& p = *pt.prog;
+            CompDesc c{};
+            c.D = p.D; c.P = p.P; c.nB = p.nB; c.nNodes = p.nNodes; c.nSlots = p.nSlots; c.nCNodes = p.nCNodes;
+            c.maxDepth = p.maxDepth; c.numTerms = p.numTerms; c.outRow = (int)pt.outRow;
+            c.coeffOffset = (int)pt.mapCoeffOffset; c.slotOffset = slotOff;
+            c.nodeA = p.dNodeA; c.nodeSlot = p.dNodeSlot; c.nodeC = p.dNodeC; c.nodeCRows = p.dNodeCRows;
+            c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
+            W.hostComps.push_back(c);
+            slotOff += p.nSlots;
+            pm = std::max(pm, p.P);
+            W.dmax = std::max(W.dmax, p.D);
+            W.nBmax = std::max(W.nBmax, p.nB);
+            W.depthMax = std::max(W.depthMax, p.maxDepth);
+        }
+        W.totalSlots = slotOff;
+        W.pmax = instantiatedPmax(pm);
+        W.comps.ensure(W.hostComps.size() * sizeof(CompDesc), stream);
+        MPGB_CUDA(cudaMemcpy(W.comps.p, W.hostComps.data(), W.hostComps.size() * sizeof(CompDesc),
+                             cudaMemcpyHostToDevice));
+        W.cm.ensure(std::max(1, W.totalSlots) * sizeof(double), stream);
+        W.status.ensure(sizeof(int) * 4, stream);
+        MPGB_CUDA(cudaMemset(W.status.p, 0, sizeof(int) * 4));
+        W.built = true;
+    }
+    // Coefficient sources: each part reads its owner's current pointer.
+    std::vector<GatherDescHost> g;
+    int off = 0;
+    for (auto& pt : parts_) {
+        pt.owner->CheckCoefficients("MonotoneComponent");
+        g.push_back({pt.owner->Coeffs() + pt.coeffOffset, pt.prog->dSlotTerm, off, pt.prog->nSlots});
+        off += pt.prog->nSlots;
+    }
+    bool same = g.size() == W.hostGather.size();
+    for (size_t i = 0; same && i < g.size(); ++i) same = g[i].src == W.hostGather[i].src;
+    if (!same) {
+        W.gather.ensure(g.size() * sizeof(GatherDescHost), stream);
+        MPGB_CUDA(cudaMemcpyAsync(W.gather.p, g.data(), g.size() * sizeof(GatherDescHost), cudaMemcpyHostToDevice,
+                                  stream));
+        MPGB_CUDA(cudaStreamSynchronize(stream));
+        W.hostGather = g;
+    }
+    int maxSlots = 1;
+    for (auto& x : g) maxSlots = std::max(maxSlots, x.nSlots);
+    dim3 grid((maxSlots + 255) / 256, (unsigned)g.size());
+    gatherMultiKernel<<<grid, 256, 0, stream>>>(W.gather.as<GatherDescHost>(), (int)g.size(), W.cm.as<double>());
+    MPGB_CUDA(cudaGetLastError());
+}
+
+void MonotoneMapBase::Finish(cudaStream_t stream, const char* fn) {
+    if (async_) return;
+    int st = CheckStatus(stream);
+    if (st & kStatusInf) {
+        std::ostringstream os;
+        os << fn << ": MonotoneIntegrand: nan was encountered in value of g(df(...)).";
+        throw IntegrandError(os.str());
+    }
+    if (st & kStatusBudget) {
+        std::ostringstream os;
+        os << fn << ": adaptive quadrature exceeded its interval budget.";
+        throw std::runtime_error(os.str());
+    }
+}
+
+double* MonotoneMapBase::StagingBuffer(int slot, size_t bytes, cudaStream_t stream) {
+    if (slot < 0 || slot >= 8) throw std::invalid_argument("StagingBuffer: slot out of range.");
+    ws_->stage[slot].ensure(bytes, stream);
+    return ws_->stage[slot].as<double>();
+}
+
+int MonotoneMapBase::CheckStatus(cudaStream_t stream) {
+    MapWorkspace& W = *ws_;
+    if (!W.status.p) return 0;
+    int st = 0;
+    MPGB_CUDA(cudaMemcpyAsync(&st, W.status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    MPGB_CUDA(cudaStreamSynchronize(stream));
+    MPGB_CUDA(cudaMemsetAsync(W.status.p, 0, sizeof(int), stream));
+    return st;
+}
+
+namespace {
+
+struct LaunchCommon {
+    FusedParams prm{};
+    int needJ = 0, needE = 0;
+};
+
+constexpr int kTpb = 128;
+
+void checkMatrix(const StridedMatrix& m, int64_t rows, int64_t cols, const char* what, const char* fn) {
+    if (m.rows != rows || m.cols != cols) {
+        std::ostringstream os;
+        os << fn << ": " << what << " has shape (" << m.rows << "," << m.cols << "), expected (" << rows << "," << cols
+           << ").";
+        throw std::invalid_argument(os.str());
+    }
+    if (rows > 0 && cols > 0 && m.data == nullptr) {
+        std::ostringstream os;
+        os << fn << ": " << what << " has no data.";
+        throw std::invalid_argument(os.str());
+    }
+}
+
+}  // namespace
+
+// Fill the parameter fields common to every fused launch.
+static void baseParams(MapWorkspace& W, const MapOptions& o, FusedParams& p, long long N) {
+    p.comps = W.comps.as<CompDesc>();
+    p.cm = W.cm.as<double>();
+    p.N = N;
+    p.tpb = kTpb;
+    p.nugget = o.nugget;
+    p.dmax = W.dmax;
+    p.nBmax = W.nBmax;
+    p.depthMax = W.depthMax;
+    p.quad = W.quad;
+    p.bc = W.bc;
+    p.statusWord = W.status.as<int>();
+}
+
+static int basisCode(const MapOptions& o) {
+    return o.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite;
+}
+static int posCode(const MapOptions& o) { return o.posFuncType == PosFuncTypes::Exp ? kPosExp : kPosSoftPlus; }
+
+// Items of style "all components per tile" (per-point sums across components).
+static std::vector<WorkItem> itemsAllComps(long long N, int nComps) {
+    long long nTiles = (N + kTpb - 1) / kTpb;
+    std::vector<WorkItem> v;
+    v.reserve(nTiles);
+    for (long long t = 0; t < nTiles; ++t) v.push_back({0, nComps, (int)t, 1, 0, 0, 0});
+    return v;
+}
+
+// Items of style "one component, a range of tiles".  Heavier components first.
+static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Part>& parts, long long N, int numSMs,
+                                          bool reduced, std::vector<long long>* rowBaseOut,
+                                          std::vector<std::vector<int>>* itemsOfComp) {
+    const int nComps = (int)parts.size();
+    const long long nTiles = (N + kTpb - 1) / kTpb;
+    std::vector<int> order(nComps);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return parts[a].prog->weight > parts[b].prog->weight; });
+    double wsum = 0;
+    for (auto& p : parts) wsum += p.prog->weight;
+    const double target = (double)numSMs * 8.0;
+    std::vector<WorkItem> v;
+    long long base = 0;
+    if (itemsOfComp) itemsOfComp->assign(nComps, {});
+    for (int c : order) {
+        long long tilesPer = 1;
+        if (reduced) {
+            double share = std::max(1.0, target * parts[c].prog->weight / wsum);
+            long long nItemsC = std::min<long long>(nTiles, (long long)std::ceil(share));
+            nItemsC = std::max<long long>(1, nItemsC);
+            tilesPer = (nTiles + nItemsC - 1) / nItemsC;
+        }
+        for (long long t = 0; t < nTiles; t += tilesPer) {
+            WorkItem w{c, c + 1, (int)t, (int)std::min<long long>(tilesPer, nTiles - t), 0, 0, 0};
+            if (reduced) {
+                w.partialBase = base;
+                w.lossSlot = (int)v.size();
+                if (rowBaseOut) rowBaseOut->push_back(base);
+                base += parts[c].prog->numTerms;
+            }
+            if (itemsOfComp) (*itemsOfComp)[c].push_back((int)v.size());
+            v.push_back(w);
+        }
+    }
+    return v;
+}
+
+static void uploadItems(MapWorkspace& W, const std::vector<WorkItem>& items, cudaStream_t stream) {
+    W.items.ensure(items.size() * sizeof(WorkItem), stream);
+    MPGB_CUDA(cudaMemcpyAsync(W.items.p, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                              stream));
+}
+
+static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nItems, int needJ, int needE,
+                   cudaStream_t stream) {
+    p.items = W.items.as<WorkItem>();
+    if (nItems == 0) return;
+    const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, (p.flags & kFlagInput) != 0);
+    if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
+    MPGB_CUDA(launchFused(basisCode(o), posCode(o), W.pmax, p, nItems, needJ, needE, stream));
+}
+
+void MonotoneMapBase::EvaluateImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream) {
+    CheckCoefficients("Evaluate");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "EvaluateImpl");
+    checkMatrix(output, outputDim, N, "output", "EvaluateImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsPerComp(parts_, N, W.numSMs, false, nullptr, nullptr);
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagEval;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.outEval = output.data; p.evalRs = output.rowStride; p.evalCs = output.colStride;
+    launch(W, opts_, p, (int)items.size(), 0, 0, stream);
+    Finish(stream, "Evaluate");
+}
+
+void MonotoneMapBase::LogDeterminantImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream) {
+    CheckCoefficients("LogDeterminant");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "LogDeterminantImpl");
+    if (output.rows * output.cols != N) throw std::invalid_argument("LogDeterminantImpl: output must hold N values.");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsAllComps(N, (int)parts_.size());
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagLogDet;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.outLogDet = output.data;
+    p.logDetStride = (output.rows == 1) ? output.colStride : output.rowStride;
+    launch(W, opts_, p, (int)items.size(), 0, 0, stream);
+    Finish(stream, "LogDeterminant");
+}
+
+void MonotoneMapBase::CoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                                    cudaStream_t stream) {
+    CheckCoefficients("CoeffGrad");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "CoeffGradImpl");
+    checkMatrix(sens, outputDim, N, "sens", "CoeffGradImpl");
+    checkMatrix(output, numCoeffs, N, "output", "CoeffGradImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsPerComp(parts_, N, W.numSMs, false, nullptr, nullptr);
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagCoefDenseT;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.sens = sens.data; p.sensRs = sens.rowStride; p.sensCs = sens.colStride;
+    p.outDense = output.data; p.denseRs = output.rowStride; p.denseCs = output.colStride;
+    launch(W, opts_, p, (int)items.size(), 1, 0, stream);
+    Finish(stream, "CoeffGrad");
+}
+
+void MonotoneMapBase::LogDeterminantCoeffGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                                  cudaStream_t stream) {
+    CheckCoefficients("LogDeterminantCoeffGrad");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "LogDeterminantCoeffGradImpl");
+    checkMatrix(output, numCoeffs, N, "output", "LogDeterminantCoeffGradImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsPerComp(parts_, N, W.numSMs, false, nullptr, nullptr);
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagCoefDenseL;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.outDense = output.data; p.denseRs = output.rowStride; p.denseCs = output.colStride;
+    launch(W, opts_, p, (int)items.size(), 0, 0, stream);
+    Finish(stream, "LogDeterminantCoeffGrad");
+}
+
+void MonotoneMapBase::GradientImpl(StridedMatrix const& pts, StridedMatrix const& sens, StridedMatrix const& output,
+                                   cudaStream_t stream) {
+    CheckCoefficients("Gradient");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "GradientImpl");
+    checkMatrix(sens, outputDim, N, "sens", "GradientImpl");
+    checkMatrix(output, inputDim, N, "output", "GradientImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsAllComps(N, (int)parts_.size());
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagInput;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.sens = sens.data; p.sensRs = sens.rowStride; p.sensCs = sens.colStride;
+    p.lsens = nullptr; p.lsensScale = 0.0;
+    p.outInput = output.data; p.inputRs = output.rowStride; p.inputCs = output.colStride;
+    launch(W, opts_, p, (int)items.size(), 1, 1, stream);
+    Finish(stream, "Gradient");
+}
+
+void MonotoneMapBase::LogDeterminantInputGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
+                                                  cudaStream_t stream) {
+    CheckCoefficients("LogDeterminantInputGrad");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "LogDeterminantInputGradImpl");
+    checkMatrix(output, inputDim, N, "output", "LogDeterminantInputGradImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    auto items = itemsAllComps(N, (int)parts_.size());
+    uploadItems(W, items, stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagInput;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.sens = nullptr;
+    p.lsens = nullptr; p.lsensScale = 1.0;
+    p.outInput = output.data; p.inputRs = output.rowStride; p.inputCs = output.colStride;
+    launch(W, opts_, p, (int)items.size(), 0, 0, stream);
+    Finish(stream, "LogDeterminantInputGrad");
+}
+
+void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& r, StridedMatrix const& output,
+                                  cudaStream_t stream) {
+    InverseImpl(x1, r, output, InverseOptions(), nullptr, stream);
+}
+
+void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& r, StridedMatrix const& output,
+                                  InverseOptions const& io, int* deviceInfo, cudaStream_t stream) {
+    CheckCoefficients("Inverse");
+    if (io.xtol < 0 || io.ytol < 0) throw std::invalid_argument("Invalid tolerance given to MonotoneComponent::Inverse.");
+    if (io.xtol <= std::numeric_limits<double>::epsilon() && io.ytol <= std::numeric_limits<double>::epsilon())
+        throw std::invalid_argument(
+            "Invalid tolerances given to MonotoneComponent::Inverse.  Either \"xtol\" or \"ytol\" must be nonzero.");
+    const long long N = r.cols;
+    if (r.rows != outputDim) throw std::invalid_argument("InverseImpl: r must have outputDim rows.");
+    if (x1.cols != N && x1.cols != 1) {
+        std::ostringstream os;
+        os << "x1 and r have different numbers of columns.  x1.extent(1)=" << x1.cols << ", but r.extent(1)=" << N;
+        throw std::invalid_argument(os.str());
+    }
+    if (x1.rows > inputDim) throw std::invalid_argument("InverseImpl: x1 has too many rows.");
+    checkMatrix(output, outputDim, N, "output", "InverseImpl");
+    if (N == 0) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    InverseParams p{};
+    p.comps = W.comps.as<CompDesc>();
+    p.nComps = (int)parts_.size();
+    p.cm = W.cm.as<double>();
+    p.N = N;
+    p.tpb = kTpb;
+    p.extra = (int)(inputDim - outputDim);
+    p.x1 = x1.data; p.x1Rs = x1.rowStride; p.x1Cs = x1.colStride; p.x1Rows = (int)x1.rows; p.x1Cols = (int)x1.cols;
+    p.r = r.data; p.rRs = r.rowStride; p.rCs = r.colStride;
+    p.out = output.data; p.outRs = output.rowStride; p.outCs = output.colStride;
+    p.info = deviceInfo; p.infoStride = N;
+    p.statusWord = W.status.as<int>();
+    p.xtol = io.xtol; p.ytol = io.ytol;
+    p.nugget = opts_.nugget;
+    p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
+    p.quad = W.quad; p.bc = W.bc;
+    const int nBlocks = (int)((N + kTpb - 1) / kTpb);
+    MPGB_CUDA(launchInverse(basisCode(opts_), posCode(opts_), W.pmax, p, nBlocks, stream));
+    Finish(stream, "Inverse");
+}
+
+void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatrix const& sens,
+                                          StridedMatrix const& logdetSens, double logdetSensScale,
+                                          StridedMatrix const& outEval, StridedMatrix const& outLogDet,
+                                          double* coeffGrad, StridedMatrix const& inputGrad, cudaStream_t stream) {
+    CheckCoefficients("FusedForwardAdjoint");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "FusedForwardAdjoint");
+    if (!sens.empty()) checkMatrix(sens, outputDim, N, "sens", "FusedForwardAdjoint");
+    if (!logdetSens.empty() && logdetSens.rows * logdetSens.cols != N)
+        throw std::invalid_argument("FusedForwardAdjoint: logdet_sens must hold N values.");
+    if (!outEval.empty()) checkMatrix(outEval, outputDim, N, "out_eval", "FusedForwardAdjoint");
+    if (!outLogDet.empty() && outLogDet.rows * outLogDet.cols != N)
+        throw std::invalid_argument("FusedForwardAdjoint: out_logdet must hold N values.");
+    if (!inputGrad.empty()) checkMatrix(inputGrad, inputDim, N, "input_grad", "FusedForwardAdjoint");
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    const int nComps = (int)parts_.size();
+    const long long ldStrideL = logdetSens.empty() ? 0 : ((logdetSens.rows == 1) ? logdetSens.colStride : logdetSens.rowStride);
+    if (N == 0) {
+        if (coeffGrad) MPGB_CUDA(cudaMemsetAsync(coeffGrad, 0, numCoeffs * sizeof(double), stream));
+        Finish(stream, "FusedForwardAdjoint");
+        return;
+    }
+    // Pass 1: per-component outputs and the reduced coefficient adjoint.
+    const bool wantCoef = coeffGrad != nullptr;
+    const bool wantLogDet = !outLogDet.empty();
+    if (wantCoef || !outEval.empty() || wantLogDet) {
+        std::vector<long long> rowBase;
+        std::vector<std::vector<int>> itemsOf;
+        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf);
+        uploadItems(W, items, stream);
+        FusedParams p{};
+        baseParams(W, opts_, p, N);
+        p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+        p.flags = 0;
+        if (!outEval.empty()) {
+            p.flags |= kFlagEval;
+            p.outEval = outEval.data; p.evalRs = outEval.rowStride; p.evalCs = outEval.colStride;
+        }
+        if (wantLogDet) {
+            // Per-component log-dets into scratch rows, summed in component order below.
+            W.logdetRows.ensure((size_t)nComps * N * sizeof(double), stream);
+            p.flags |= kFlagLogDet;
+            p.outLogDet = W.logdetRows.as<double>();
+            p.logDetStride = 1;
+        }
+        int needJ = 0;
+        if (wantCoef) {
+            p.flags |= kFlagCoefReduced;
+            p.sens = sens.data; p.sensRs = sens.rowStride; p.sensCs = sens.colStride;
+            p.lsens = logdetSens.data; p.lsensStride = ldStrideL; p.lsensScale = logdetSensScale;
+            size_t nPart = rowBase.empty() ? 1 : (size_t)(rowBase.back() + parts_[items.back().c0].prog->numTerms);
+            size_t tot = 0;
+            for (auto& it : items) tot = std::max<size_t>(tot, (size_t)it.partialBase + parts_[it.c0].prog->numTerms);
+            nPart = std::max(nPart, tot);
+            W.partials.ensure(nPart * sizeof(double), stream);
+            p.partials = W.partials.as<double>();
+            needJ = sens.empty() ? 0 : 1;
+        }
+        if (wantLogDet) {
+            // The kernel adds log-dets over its component range and writes them at
+            // outLogDet[i]; with one component per item, offset rows by component.
+            // Launch per component so that each writes its own row.
+            for (int c = 0; c < nComps; ++c) {
+                std::vector<WorkItem> sub;
+                for (int id : itemsOf[c]) sub.push_back(items[id]);
+                uploadItems(W, sub, stream);
+                FusedParams q = p;
+                q.outLogDet = W.logdetRows.as<double>() + (size_t)c * N;
+                launch(W, opts_, q, (int)sub.size(), needJ, 0, stream);
+            }
+            uploadItems(W, items, stream);
+            sumRowsKernel<<<(unsigned)((N + 255) / 256), 256, 0, stream>>>(
+                W.logdetRows.as<double>(), nComps, N, outLogDet.data,
+                (outLogDet.rows == 1) ? outLogDet.colStride : outLogDet.rowStride);
+            MPGB_CUDA(cudaGetLastError());
+        } else {
+            launch(W, opts_, p, (int)items.size(), needJ, 0, stream);
+        }
+        if (wantCoef) {
+            // Fixed-order reduction of each component's partial rows.
+            std::vector<long long> rb;
+            W.rowBase.ensure(sizeof(long long) * std::max<size_t>(1, rowBase.size()), stream);
+            for (int c = 0; c < nComps; ++c) {
+                for (int id : itemsOf[c]) rb.push_back(items[id].partialBase);
+            }
+            MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice,
+                                      stream));
+            size_t off = 0;
+            for (int c = 0; c < nComps; ++c) {
+                const int nr = (int)itemsOf[c].size();
+                MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>() + off, nr,
+                                           parts_[c].prog->numTerms, 1.0, coeffGrad + parts_[c].mapCoeffOffset, 0,
+                                           stream));
+                off += nr;
+            }
+        }
+    }
+    // Pass 2: input gradient (sums over components per point).
+    if (!inputGrad.empty()) {
+        auto items = itemsAllComps(N, nComps);
+        uploadItems(W, items, stream);
+        FusedParams p{};
+        baseParams(W, opts_, p, N);
+        p.flags = kFlagInput;
+        p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+        p.sens = sens.data; p.sensRs = sens.rowStride; p.sensCs = sens.colStride;
+        p.lsens = logdetSens.data; p.lsensStride = ldStrideL; p.lsensScale = logdetSensScale;
+        p.outInput = inputGrad.data; p.inputRs = inputGrad.rowStride; p.inputCs = inputGrad.colStride;
+        const int nj = sens.empty() ? 0 : 1;
+        launch(W, opts_, p, (int)items.size(), nj, nj, stream);
+    }
+    Finish(stream, "FusedForwardAdjoint");
+}
+
+void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream) {
+    CheckCoefficients("KLObjective");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "KLObjective");
+    if (N == 0) throw std::invalid_argument("KLObjective: no samples.");
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    const int nComps = (int)parts_.size();
+    std::vector<long long> rowBase;
+    std::vector<std::vector<int>> itemsOf;
+    auto items = itemsPerComp(parts_, N, W.numSMs, true, &rowBase, &itemsOf);
+    uploadItems(W, items, stream);
+    size_t tot = 1;
+    for (auto& it : items) tot = std::max<size_t>(tot, (size_t)it.partialBase + parts_[it.c0].prog->numTerms);
+    W.partials.ensure(tot * sizeof(double), stream);
+    W.lossPart.ensure(items.size() * sizeof(double), stream);
+    FusedParams p{};
+    baseParams(W, opts_, p, N);
+    p.flags = kFlagKL | kFlagCoefReduced;
+    p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+    p.sensScale = 1.0 / (double)N;
+    p.lsensScale = -1.0 / (double)N;
+    p.partials = W.partials.as<double>();
+    p.lossPartials = W.lossPart.as<double>();
+    launch(W, opts_, p, (int)items.size(), 1, 0, stream);
+    std::vector<long long> rb;
+    std::vector<int> ls;
+    for (int c = 0; c < nComps; ++c)
+        for (int id : itemsOf[c]) {
+            rb.push_back(items[id].partialBase);
+            ls.push_back(items[id].lossSlot);
+        }
+    W.rowBase.ensure(rb.size() * sizeof(long long), stream);
+    W.lossSlots.ensure(ls.size() * sizeof(int), stream);
+    MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
+    MPGB_CUDA(cudaMemcpyAsync(W.lossSlots.p, ls.data(), ls.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    size_t off = 0;
+    for (int c = 0; c < nComps; ++c) {
+        const int nr = (int)itemsOf[c].size();
+        MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>() + off, nr,
+                                   parts_[c].prog->numTerms, 1.0, grad + parts_[c].mapCoeffOffset, 0, stream));
+        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), W.lossSlots.as<int>() + off, nr, 1.0 / (double)N,
+                                lossPerComp + c, stream));
+        off += nr;
+    }
+    Finish(stream, "KLObjective");
+}
+
+// ---------------------------------------------------------------------------
+// MonotoneComponent / TriangularMap / MapFactory
+// ---------------------------------------------------------------------------
+MonotoneComponent::MonotoneComponent(FixedMultiIndexSet const& mset, MapOptions const& opts)
+    : MonotoneMapBase(mset.Length(), 1, mset.Size(), opts), mset_(mset) {
+    validateOptions(opts);
+    auto prog = std::make_shared<ComponentProgram>(mset);
+    parts_.push_back({prog, this, 0, 0, 0});
+}
+
+static void collectParts(ConditionalMapBase* comp, unsigned row, unsigned coeffOff,
+                         std::vector<MonotoneMapBase::Part>& out, const MapOptions** optsSeen) {
+    auto* mono = dynamic_cast<MonotoneMapBase*>(comp);
+    if (!mono) throw std::invalid_argument("TriangularMap: components must be monotone components or triangular maps.");
+    if (*optsSeen) {
+        const MapOptions& a = **optsSeen;
+        const MapOptions& b = mono->Options();
+        if (a.basisType != b.basisType || a.posFuncType != b.posFuncType || a.quadAbsTol != b.quadAbsTol ||
+            a.quadRelTol != b.quadRelTol || a.quadMaxSub != b.quadMaxSub || a.quadMinSub != b.quadMinSub ||
+            a.quadPts != b.quadPts || a.basisNorm != b.basisNorm || a.nugget != b.nugget)
+            throw std::invalid_argument("TriangularMap: components must share basis, rectifier and quadrature options.");
+    } else {
+        *optsSeen = &mono->Options();
+    }
+    (void)row;
+    (void)coeffOff;
+}
+
+TriangularMap::TriangularMap(std::vector<std::shared_ptr<ConditionalMapBase>> const& components, bool moveCoeffs)
+    : MonotoneMapBase(components.empty() ? 0 : components.back()->inputDim,
+                      [&] { unsigned s = 0; for (auto& c : components) s += c->outputDim; return s; }(),
+                      [&] { unsigned s = 0; for (auto& c : components) s += c->numCoeffs; return s; }(),
+                      MapOptions()),
+      comps_(components) {
+    if (components.empty()) throw std::invalid_argument("TriangularMap: no components.");
+    for (unsigned i = 0; i < comps_.size(); ++i) {
+        if (comps_[i]->outputDim > comps_[i]->inputDim) {
+            std::ostringstream os;
+            os << "In TriangularMap constructor, the output dimension (" << comps_[i]->outputDim << ") of component " << i
+               << " is greater than the input dimension (" << comps_[i]->inputDim << ").";
+            throw std::invalid_argument(os.str());
+        }
+    }
+    for (unsigned i = 1; i < comps_.size(); ++i) {
+        if (comps_[i]->inputDim != comps_[i - 1]->inputDim + comps_[i]->outputDim) {
+            std::ostringstream os;
+            os << "In TriangularMap constructor, the input dimension of component " << i << " is "
+               << comps_[i]->inputDim << ", but is expected to be the sum of the input dimension for component " << i - 1
+               << "and output dimension for component " << i << ", which is " << comps_[i - 1]->inputDim << " + "
+               << comps_[i]->outputDim << " = " << comps_[i - 1]->inputDim + comps_[i]->outputDim << ".";
+            throw std::invalid_argument(os.str());
+        }
+    }
+    const MapOptions* seen = nullptr;
+    unsigned row = 0, coff = 0;
+    for (auto& c : comps_) {
+        collectParts(c.get(), row, coff, parts_, &seen);
+        auto* mono = dynamic_cast<MonotoneMapBase*>(c.get());
+        for (auto& sub : mono->Parts()) {
+            Part np = sub;
+            np.outRow = row + sub.outRow;
+            np.mapCoeffOffset = coff + sub.mapCoeffOffset;
+            parts_.push_back(np);
+        }
+        row += c->outputDim;
+        coff += c->numCoeffs;
+    }
+    opts_ = *seen;
+    if (moveCoeffs) {
+        std::vector<double> all;
+        for (unsigned i = 0; i < comps_.size(); ++i) {
+            if (!comps_[i]->CheckCoefficients()) {
+                std::ostringstream os;
+                os << "In TriangularMap constructor, moveCoeffs set to true, but component " << i
+                   << " doesn't have coeffs set";
+                throw std::invalid_argument(os.str());
+            }
+            auto h = comps_[i]->CoeffMap();
+            all.insert(all.end(), h.begin(), h.end());
+        }
+        MPGB_CUDA(cudaMalloc(&owned_, std::max<size_t>(1, all.size()) * sizeof(double)));
+        if (!all.empty())
+            MPGB_CUDA(cudaMemcpy(owned_, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+        WrapCoeffs(owned_, numCoeffs);
+    }
+}
+
+void TriangularMap::SetCoeffs(const double* coeffs, unsigned int n, bool host, cudaStream_t stream) {
+    ConditionalMapBase::SetCoeffs(coeffs, n, host, stream);
+    unsigned off = 0;
+    for (auto& c : comps_) {
+        c->WrapCoeffs(coeffs_ + off, c->numCoeffs);
+        off += c->numCoeffs;
+    }
+}
+
+void TriangularMap::WrapCoeffs(double* deviceCoeffs, unsigned int n) {
+    ConditionalMapBase::WrapCoeffs(deviceCoeffs, n);
+    unsigned off = 0;
+    for (auto& c : comps_) {
+        c->WrapCoeffs(coeffs_ + off, c->numCoeffs);
+        off += c->numCoeffs;
+    }
+}
+
+namespace MapFactory {
+std::shared_ptr<ConditionalMapBase> CreateComponent(FixedMultiIndexSet const& mset, MapOptions opts) {
+    auto c = std::make_shared<MonotoneComponent>(mset, opts);
+    // Zero-initialised coefficients (src/MapFactoryImpl4.cpp:26-27).
+    std::vector<double> z(c->numCoeffs, 0.0);
+    c->SetCoeffs(z.data(), c->numCoeffs, true);
+    return c;
+}
+
+std::shared_ptr<ConditionalMapBase> CreateTriangular(unsigned int inputDim, unsigned int outputDim,
+                                                     unsigned int totalOrder, MapOptions options) {
+    if (outputDim == 0 || outputDim > inputDim)
+        throw std::invalid_argument("CreateTriangular: need 0 < outputDim <= inputDim.");
+    validateOptions(options);
+    std::vector<std::shared_ptr<ConditionalMapBase>> comps(outputDim);
+    const unsigned extra = inputDim - outputDim;
+    for (unsigned i = 0; i < outputDim; ++i) {
+        FixedMultiIndexSet mset(i + extra + 1, totalOrder);
+        comps[i] = std::make_shared<MonotoneComponent>(mset, options);
+    }
+    auto out = std::make_shared<TriangularMap>(comps);
+    std::vector<double> z(out->numCoeffs, 0.0);
+    out->SetCoeffs(z.data(), out->numCoeffs, true);
+    return out;
+}
+}  // namespace MapFactory
+
+}  // namespace mpgb
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace mpgb;
+
+struct mpgb_map {
+    std::shared_ptr<ConditionalMapBase> obj;
+};
+
+namespace {
+thread_local std::string g_lastError;
+
+template <class F>
+int guard(F&& f) {
+    try {
+        f();
+        return MPGB_OK;
+    } catch (IntegrandError const& e) {
+        g_lastError = e.what();
+        return MPGB_ERR_INTEGRAND;
+    } catch (CudaError const& e) {
+        g_lastError = e.what();
+        return MPGB_ERR_CUDA;
+    } catch (std::invalid_argument const& e) {
+        g_lastError = e.what();
+        return MPGB_ERR_INVALID_ARGUMENT;
+    } catch (std::out_of_range const& e) {
+        g_lastError = e.what();
+        return MPGB_ERR_INVALID_ARGUMENT;
+    } catch (std::exception const& e) {
+        g_lastError = e.what();
+        return MPGB_ERR_RUNTIME;
+    } catch (...) {
+        g_lastError = "unknown error";
+        return MPGB_ERR_RUNTIME;
+    }
+}
+
+MapOptions toOptions(const mpgb_map_options* o) {
+    MapOptions m;
+    if (!o) return m;
+    if (o->basis_type < 0 || o->basis_type > 2) throw std::invalid_argument("invalid basis_type");
+    if (o->pos_func_type < 0 || o->pos_func_type > 1) throw std::invalid_argument("invalid pos_func_type");
+    if (o->quad_type < 0 || o->quad_type > 2) throw std::invalid_argument("invalid quad_type");
+    m.basisType = (BasisTypes)o->basis_type;
+    m.posFuncType = (PosFuncTypes)o->pos_func_type;
+    m.quadType = (QuadTypes)o->quad_type;
+    m.quadAbsTol = o->quad_abs_tol;
+    m.quadRelTol = o->quad_rel_tol;
+    m.quadMaxSub = o->quad_max_sub;
+    m.quadMinSub = o->quad_min_sub;
+    m.quadPts = o->quad_pts;
+    m.contDeriv = o->cont_deriv != 0;
+    m.basisNorm = o->basis_norm != 0;
+    m.nugget = o->nugget;
+    return m;
+}
+
+MonotoneMapBase* mono(mpgb_map* m) {
+    if (!m || !m->obj) throw std::invalid_argument("null map handle");
+    auto* p = dynamic_cast<MonotoneMapBase*>(m->obj.get());
+    if (!p) throw std::invalid_argument("map is not a monotone map");
+    return p;
+}
+
+bool isHostPtr(const void* p) {
+    if (!p) return false;
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
+StridedMatrix toSM(const mpgb_matrix& m) { return StridedMatrix(m.data, m.rows, m.cols, m.row_stride, m.col_stride); }
+
+// Host staging: host matrices are copied to (or from) contiguous row-major
+// device buffers owned by the map (grow-only, reused across calls).
+struct Stager {
+    cudaStream_t s;
+    MonotoneMapBase* m;
+    int next = 0;
+    std::vector<std::pair<StridedMatrix, StridedMatrix>> copyBack;  // (device, host)
+    bool staged = false;
+    Stager(cudaStream_t st, MonotoneMapBase* map) : s(st), m(map) {}
+    static void copy2D(const StridedMatrix& dst, const StridedMatrix& src, cudaMemcpyKind kind, cudaStream_t s) {
+        if (src.rows == 0 || src.cols == 0) return;
+        if (src.colStride == 1 && dst.colStride == 1) {
+            MPGB_CUDA(cudaMemcpy2DAsync(dst.data, dst.rowStride * 8, src.data, src.rowStride * 8, src.cols * 8,
+                                        src.rows, kind, s));
+        } else if (src.rows == 1) {
+            MPGB_CUDA(cudaMemcpy2DAsync(dst.data, dst.colStride * 8, src.data, src.colStride * 8, 8, src.cols, kind, s));
+        } else {
+            for (int64_t r = 0; r < src.rows; ++r)
+                MPGB_CUDA(cudaMemcpy2DAsync(dst.data + r * dst.rowStride, dst.colStride * 8,
+                                            src.data + r * src.rowStride, src.colStride * 8, 8, src.cols, kind, s));
+        }
+    }
+    double* buffer(size_t n) {
+        if (next >= 8) throw std::invalid_argument("too many host-staged arrays in one call");
+        staged = true;
+        return m->StagingBuffer(next++, std::max<size_t>(1, n) * 8, s);
+    }
+    StridedMatrix in(const mpgb_matrix& mm) {
+        StridedMatrix h = toSM(mm);
+        if (!mm.data || !isHostPtr(mm.data)) return h;
+        StridedMatrix dm(buffer((size_t)mm.rows * mm.cols), mm.rows, mm.cols, mm.cols, 1);
+        copy2D(dm, h, cudaMemcpyHostToDevice, s);
+        return dm;
+    }
+    StridedMatrix out(const mpgb_matrix& mm) {
+        StridedMatrix h = toSM(mm);
+        if (!mm.data || !isHostPtr(mm.data)) return h;
+        StridedMatrix dm(buffer((size_t)mm.rows * mm.cols), mm.rows, mm.cols, mm.cols, 1);
+        copyBack.push_back({dm, h});
+        return dm;
+    }
+    double* outVec(double* p, size_t n) {
+        if (!p || !isHostPtr(p)) return p;
+        double* d = buffer(n);
+        copyBack.push_back({StridedMatrix(d, 1, (int64_t)n, (int64_t)n, 1), StridedMatrix(p, 1, (int64_t)n, (int64_t)n, 1)});
+        return d;
+    }
+    void finish() {
+        for (auto& pr : copyBack) copy2D(pr.second, pr.first, cudaMemcpyDeviceToHost, s);
+        if (staged) MPGB_CUDA(cudaStreamSynchronize(s));
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* mpgb_version(void) { return "mpart_gb300 0.1.0 (sm_103a, FP64)"; }
+const char* mpgb_last_error(void) { return g_lastError.c_str(); }
+
+int mpgb_map_options_default(mpgb_map_options* o) {
+    return guard([&] {
+        if (!o) throw std::invalid_argument("null options");
+        MapOptions m;
+        o->basis_type = (int)m.basisType;
+        o->pos_func_type = (int)m.posFuncType;
+        o->quad_type = (int)m.quadType;
+        o->quad_abs_tol = m.quadAbsTol;
+        o->quad_rel_tol = m.quadRelTol;
+        o->quad_max_sub = m.quadMaxSub;
+        o->quad_min_sub = m.quadMinSub;
+        o->quad_pts = m.quadPts;
+        o->cont_deriv = m.contDeriv;
+        o->basis_norm = m.basisNorm;
+        o->nugget = m.nugget;
+    });
+}
+
+int mpgb_create_component(unsigned int dim, unsigned int num_terms, const unsigned int* nz_starts,
+                          const unsigned int* nz_dims, const unsigned int* nz_orders, const mpgb_map_options* opts,
+                          mpgb_map** out) {
+    return guard([&] {
+        if (!out || !nz_starts) throw std::invalid_argument("null argument");
+        std::vector<unsigned> s(nz_starts, nz_starts + num_terms + 1);
+        const unsigned nnz = s.back();
+        if (nnz > 0 && (!nz_dims || !nz_orders)) throw std::invalid_argument("null nonzero arrays");
+        std::vector<unsigned> d(nz_dims, nz_dims + nnz), o(nz_orders, nz_orders + nnz);
+        FixedMultiIndexSet ms(dim, s, d, o);
+        *out = new mpgb_map{MapFactory::CreateComponent(ms, toOptions(opts))};
+    });
+}
+
+int mpgb_create_component_total_order(unsigned int dim, unsigned int order, const mpgb_map_options* opts,
+                                      mpgb_map** out) {
+    return guard([&] {
+        if (!out) throw std::invalid_argument("null argument");
+        FixedMultiIndexSet ms(dim, order);
+        *out = new mpgb_map{MapFactory::CreateComponent(ms, toOptions(opts))};
+    });
+}
+
+int mpgb_create_triangular(unsigned int input_dim, unsigned int output_dim, unsigned int total_order,
+                           const mpgb_map_options* opts, mpgb_map** out) {
+    return guard([&] {
+        if (!out) throw std::invalid_argument("null argument");
+        *out = new mpgb_map{MapFactory::CreateTriangular(input_dim, output_dim, total_order, toOptions(opts))};
+    });
+}
+
+int mpgb_create_triangular_from_components(mpgb_map* const* components, unsigned int n, int move_coeffs,
+                                           mpgb_map** out) {
+    return guard([&] {
+        if (!out || !components) throw std::invalid_argument("null argument");
+        std::vector<std::shared_ptr<ConditionalMapBase>> v;
+        for (unsigned i = 0; i < n; ++i) {
+            if (!components[i]) throw std::invalid_argument("null component");
+            v.push_back(components[i]->obj);
+        }
+        *out = new mpgb_map{std::make_shared<TriangularMap>(v, move_coeffs != 0)};
+    });
+}
+
+int mpgb_map_destroy(mpgb_map* map) {
+    return guard([&] { delete map; });
+}
+
+int mpgb_map_dims(const mpgb_map* map, unsigned int* in, unsigned int* outd, unsigned int* nc) {
+    return guard([&] {
+        if (!map) throw std::invalid_argument("null map handle");
+        if (in) *in = map->obj->inputDim;
+        if (outd) *outd = map->obj->outputDim;
+        if (nc) *nc = map->obj->numCoeffs;
+    });
+}
+
+int mpgb_map_num_components(const mpgb_map* map, unsigned int* n) {
+    return guard([&] {
+        if (!map || !n) throw std::invalid_argument("null argument");
+        auto* t = dynamic_cast<TriangularMap*>(map->obj.get());
+        *n = t ? t->NumComponents() : 1;
+    });
+}
+
+int mpgb_map_get_component(mpgb_map* map, unsigned int i, mpgb_map** out) {
+    return guard([&] {
+        if (!map || !out) throw std::invalid_argument("null argument");
+        auto* t = dynamic_cast<TriangularMap*>(map->obj.get());
+        if (!t) {
+            if (i != 0) throw std::out_of_range("component index out of range");
+            *out = new mpgb_map{map->obj};
+            return;
+        }
+        if (i >= t->NumComponents()) throw std::out_of_range("component index out of range");
+        *out = new mpgb_map{t->GetComponent(i)};
+    });
+}
+
+int mpgb_set_coeffs(mpgb_map* map, const double* coeffs, unsigned int n, int is_host, void* stream) {
+    return guard([&] {
+        if (!map) throw std::invalid_argument("null map handle");
+        if (n && !coeffs) throw std::invalid_argument("null coefficients");
+        map->obj->SetCoeffs(coeffs, n, is_host != 0, (cudaStream_t)stream);
+        if (!map->obj->Async()) MPGB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    });
+}
+
+int mpgb_wrap_coeffs(mpgb_map* map, double* device_coeffs, unsigned int n) {
+    return guard([&] {
+        if (!map) throw std::invalid_argument("null map handle");
+        map->obj->WrapCoeffs(device_coeffs, n);
+    });
+}
+
+int mpgb_get_coeffs(const mpgb_map* map, double* host_out, unsigned int n) {
+    return guard([&] {
+        if (!map || !host_out) throw std::invalid_argument("null argument");
+        if (n != map->obj->numCoeffs) throw std::invalid_argument("wrong coefficient count");
+        auto v = map->obj->CoeffMap();
+        std::copy(v.begin(), v.end(), host_out);
+    });
+}
+
+int mpgb_coeffs_device_ptr(const mpgb_map* map, double** out) {
+    return guard([&] {
+        if (!map || !out) throw std::invalid_argument("null argument");
+        *out = map->obj->Coeffs();
+    });
+}
+
+int mpgb_set_async(mpgb_map* map, int async) {
+    return guard([&] {
+        if (!map) throw std::invalid_argument("null map handle");
+        map->obj->SetAsync(async != 0);
+    });
+}
+
+int mpgb_check_status(mpgb_map* map, void* stream, int* status) {
+    return guard([&] {
+        int st = mono(map)->CheckStatus((cudaStream_t)stream);
+        if (status) *status = st;
+    });
+}
+
+int mpgb_evaluate(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto O = st.out(out);
+        mono(map)->EvaluateImpl(P, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_log_determinant(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto O = st.out(out);
+        mono(map)->LogDeterminantImpl(P, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_inverse(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
+                 int* device_info, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto X = st.in(x1);
+        auto R = st.in(r);
+        auto O = st.out(out);
+        InverseOptions io;
+        io.xtol = xtol;
+        io.ytol = ytol;
+        mono(map)->InverseImpl(X, R, O, io, device_info, s);
+        st.finish();
+    });
+}
+
+int mpgb_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto S = st.in(sens);
+        auto O = st.out(out);
+        mono(map)->CoeffGradImpl(P, S, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_gradient(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto S = st.in(sens);
+        auto O = st.out(out);
+        mono(map)->GradientImpl(P, S, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_log_determinant_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto O = st.out(out);
+        mono(map)->LogDeterminantCoeffGradImpl(P, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_log_determinant_input_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto O = st.out(out);
+        mono(map)->LogDeterminantInputGradImpl(P, O, s);
+        st.finish();
+    });
+}
+
+int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix logdet_sens,
+                       double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet, double* coeff_grad,
+                       mpgb_matrix input_grad, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        auto* m = mono(map);
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto S = st.in(sens);
+        auto L = st.in(logdet_sens);
+        auto E = st.out(out_eval);
+        auto D = st.out(out_logdet);
+        auto G = st.out(input_grad);
+        double* cg = st.outVec(coeff_grad, m->numCoeffs);
+        m->FusedForwardAdjoint(P, S, L, logdet_sens_scale, E, D, cg, G, s);
+        st.finish();
+    });
+}
+
+int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad, void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        auto* m = mono(map);
+        if (!loss || !grad) throw std::invalid_argument("null output");
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        double* l = st.outVec(loss, m->outputDim);
+        double* g = st.outVec(grad, m->numCoeffs);
+        m->KLObjective(P, l, g, s);
+        st.finish();
+    });
+}
+
+int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        double* d = nullptr;
+        MPGB_CUDA(cudaMalloc(&d, 8));
+        cudaEvent_t e0, e1;
+        MPGB_CUDA(cudaEventCreate(&e0));
+        MPGB_CUDA(cudaEventCreate(&e1));
+        MPGB_CUDA(cudaEventRecord(e0, s));
+        MPGB_CUDA(launchDfmaPeak(d, blocks, threads, iters, s));
+        MPGB_CUDA(cudaEventRecord(e1, s));
+        MPGB_CUDA(cudaEventSynchronize(e1));
+        float t = 0;
+        MPGB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        if (ms) *ms = t;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+// Dispatch of the fused/inverse kernels and the small helper kernels.
+#include "mpgb_types.h"
+#include "mpgb_launch.h"
+
+namespace mpgb {
+
+template <int BASIS, int POS, int PMAX>
+cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int needE, cudaStream_t stream);
+template <int BASIS, int POS, int PMAX>
+cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t stream);
+
+// --------------------------------------------------------------------------
+// Coefficient gather: cm[slot] = coeffs[component offset + slotTerm[slot]].
+// --------------------------------------------------------------------------
+__global__ void gatherKernel(const int32_t* slotGlobalTerm, int nSlots, const double* coeffs, double* cm) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nSlots) {
+        const int t = slotGlobalTerm[s];
+        cm[s] = (t >= 0) ? coeffs[t] : 0.0;
+    }
+}
+
+// Fixed-order reduction of partial rows: out[t] = scale * sum_r part[base_r + t].
+// Block = 32 terms x 8 row groups; the 8 group sums are added in order.
+__global__ void reduceRowsKernel(const double* part, const long long* rowBase, int nRows, int nTerms,
+                                 double scale, double* out, int accumulate) {
+    __shared__ double red[8][33];
+    const int t = blockIdx.x * 32 + threadIdx.x;
+    const int g = threadIdx.y;
+    double s = 0.0;
+    if (t < nTerms)
+        for (int r = g; r < nRows; r += 8) s += part[rowBase[r] + t];
+    red[g][threadIdx.x] = s;
+    __syncthreads();
+    if (g == 0 && t < nTerms) {
+        double v = 0.0;
+        for (int q = 0; q < 8; ++q) v += red[q][threadIdx.x];
+        v *= scale;
+        out[t] = accumulate ? out[t] + v : v;
+    }
+}
+
+__global__ void sumLossKernel(const double* lossPart, const int* slots, int n, double scale, double* out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) s += lossPart[slots[j]];
+        *out = s * scale;
+    }
+}
+
+// FP64 peak probe: independent DFMA chains (8 per thread).
+__global__ void dfmaPeakKernel(double* out, int iters, double seed) {
+    double x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = seed + j * 1e-3 + threadIdx.x * 1e-9;
+    const double m = 0.999999, c = 1e-7;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fma(x[j], m, c);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    if (s == 12345.678) out[0] = s;
+}
+
+// --------------------------------------------------------------------------
+// Dispatch.
+// --------------------------------------------------------------------------
+template <int BASIS, int POS>
+static cudaError_t launchFusedBP(const FusedParams& prm, int pmax, int nItems, int needJ, int needE,
+                                 cudaStream_t stream) {
+    switch (pmax) {
+        case 1: return launchFusedP<BASIS, POS, 1>(prm, nItems, needJ, needE, stream);
+        case 2: return launchFusedP<BASIS, POS, 2>(prm, nItems, needJ, needE, stream);
+        case 3: return launchFusedP<BASIS, POS, 3>(prm, nItems, needJ, needE, stream);
+        case 4: return launchFusedP<BASIS, POS, 4>(prm, nItems, needJ, needE, stream);
+        case 5: return launchFusedP<BASIS, POS, 5>(prm, nItems, needJ, needE, stream);
+        case 6: return launchFusedP<BASIS, POS, 6>(prm, nItems, needJ, needE, stream);
+        case 8: return launchFusedP<BASIS, POS, 8>(prm, nItems, needJ, needE, stream);
+        case 12: return launchFusedP<BASIS, POS, 12>(prm, nItems, needJ, needE, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int BASIS, int POS>
+static cudaError_t launchInverseBP(const InverseParams& prm, int pmax, int nBlocks, cudaStream_t stream) {
+    switch (pmax) {
+        case 1: return launchInverseP<BASIS, POS, 1>(prm, nBlocks, stream);
+        case 2: return launchInverseP<BASIS, POS, 2>(prm, nBlocks, stream);
+        case 3: return launchInverseP<BASIS, POS, 3>(prm, nBlocks, stream);
+        case 4: return launchInverseP<BASIS, POS, 4>(prm, nBlocks, stream);
+        case 5: return launchInverseP<BASIS, POS, 5>(prm, nBlocks, stream);
+        case 6: return launchInverseP<BASIS, POS, 6>(prm, nBlocks, stream);
+        case 8: return launchInverseP<BASIS, POS, 8>(prm, nBlocks, stream);
+        case 12: return launchInverseP<BASIS, POS, 12>(prm, nBlocks, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+int instantiatedPmax(int p) {
+    if (p <= 6) return p < 1 ? 1 : p;
+    if (p <= 8) return 8;
+    if (p <= 12) return 12;
+    return -1;
+}
+
+cudaError_t launchFused(int basis, int pos, int pmax, const FusedParams& prm, int nItems, int needJ, int needE,
+                        cudaStream_t stream) {
+    if (basis == kBasisProbHermite) {
+        if (pos == kPosSoftPlus) return launchFusedBP<kBasisProbHermite, kPosSoftPlus>(prm, pmax, nItems, needJ, needE, stream);
+        return launchFusedBP<kBasisProbHermite, kPosExp>(prm, pmax, nItems, needJ, needE, stream);
+    }
+    if (pos == kPosSoftPlus) return launchFusedBP<kBasisHermiteFunctions, kPosSoftPlus>(prm, pmax, nItems, needJ, needE, stream);
+    return launchFusedBP<kBasisHermiteFunctions, kPosExp>(prm, pmax, nItems, needJ, needE, stream);
+}
+
+cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm, int nBlocks, cudaStream_t stream) {
+    if (basis == kBasisProbHermite) {
+        if (pos == kPosSoftPlus) return launchInverseBP<kBasisProbHermite, kPosSoftPlus>(prm, pmax, nBlocks, stream);
+        return launchInverseBP<kBasisProbHermite, kPosExp>(prm, pmax, nBlocks, stream);
+    }
+    if (pos == kPosSoftPlus) return launchInverseBP<kBasisHermiteFunctions, kPosSoftPlus>(prm, pmax, nBlocks, stream);
+    return launchInverseBP<kBasisHermiteFunctions, kPosExp>(prm, pmax, nBlocks, stream);
+}
+
+size_t fusedSmemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input) {
+    size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)(depthMax + 1) * tpb +
+               (size_t)(pmax + 1) * tpb;
+    if (input) {
+        n += (size_t)nBmax * (tpb + 1) + (size_t)dmax * tpb +
+             (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
+    }
+    return n * sizeof(double);
+}
+
+cudaError_t launchGather(const int32_t* slotGlobalTerm, int nSlots, const double* coeffs, double* cm,
+                         cudaStream_t stream) {
+    if (nSlots <= 0) return cudaSuccess;
+    gatherKernel<<<(nSlots + 255) / 256, 256, 0, stream>>>(slotGlobalTerm, nSlots, coeffs, cm);
+    return cudaGetLastError();
+}
+
+cudaError_t launchReduceRows(const double* part, const long long* rowBase, int nRows, int nTerms, double scale,
+                             double* out, int accumulate, cudaStream_t stream) {
+    if (nTerms <= 0) return cudaSuccess;
+    dim3 blk(32, 8);
+    reduceRowsKernel<<<(nTerms + 31) / 32, blk, 0, stream>>>(part, rowBase, nRows, nTerms, scale, out, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
+                          cudaStream_t stream) {
+    sumLossKernel<<<1, 32, 0, stream>>>(lossPart, slots, n, scale, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream) {
+    dfmaPeakKernel<<<blocks, threads, 0, stream>>>(out, iters, 1.0);
+    return cudaGetLastError();
+}
+
+}  // namespace mpgb

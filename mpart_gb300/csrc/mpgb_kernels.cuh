@@ -1,0 +1,682 @@
+// Fused FP64 kernels for MParT monotone components on sm_103a.
+//
+// One thread per point.  A block holds a tile of points and walks a range of
+// components; per point and component:
+//   phase A  prefix products Phi_m over the leading coordinates (shared-memory
+//            stack, one multiply per prefix node) and the per-order sums
+//            a_k = sum_m c_(m,k) Phi_m;
+//   phase B  adaptive Clenshaw-Curtis quadrature of the rectified diagonal
+//            derivative (MParT/Quadrature.h:819-968) on a per-thread stack,
+//            carrying the value integrand and, for adjoints, the per-order
+//            integrals J_k = int x_D g'(d_D f) phit'_k dt and the x_D-derivative
+//            integrand (MonotoneIntegrand.h:118-203);
+//   phase C  adjoints: per-point weights w_k turn into dense per-term outputs
+//            (Phi_m w_k), a per-block reduction over points (owner-computes:
+//            one thread per prefix node) or an input gradient (forward-mode
+//            over the prefix tree).
+// No atomics on values: reduced adjoints go through per-item partial rows and
+// a fixed-order reduction, so results are bitwise reproducible.
+#pragma once
+#include <cstdio>
+#include "mpgb_types.h"
+#include "mpgb_launch.h"
+
+namespace mpgb {
+
+// --------------------------------------------------------------------------
+// Integrand at one node t in [0,1]:  h = x_D (g(df) + eps), plus adjoint parts.
+// --------------------------------------------------------------------------
+template <int PMAX, bool NEEDJ, bool NEEDE>
+struct NodeVal {
+    double h;
+    double F[NEEDJ ? PMAX : 1];  // x_D g'(df) phit'_k(y), k = 1..P
+    double E;                    // d/dx_D of the integrand (MonotoneIntegrand.h:193-201)
+};
+
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+__device__ __forceinline__ void evalNode(double t, double xd, const double* a, int P, const BasisConsts& bc,
+                                         double nugget, NodeVal<PMAX, NEEDJ, NEEDE>& o, int& st) {
+    double d1[PMAX + 1], d2[PMAX + 1];
+    const double y = t * xd;
+    lastBasis<BASIS, PMAX, false, true, NEEDE>(y, P, bc, nullptr, d1, d2);
+    double df = 0.0;
+#pragma unroll
+    for (int k = 1; k <= PMAX; ++k) df = fma(a[k], d1[k], df);
+    double g, gp;
+    posEval<POS>(df, g, gp);
+    o.h = xd * (g + nugget);
+    if (isinf(g)) st |= kStatusInf;
+    else if (isnan(o.h)) st |= kStatusNaN;
+    if constexpr (NEEDJ) {
+        const double q = xd * gp;
+#pragma unroll
+        for (int k = 1; k <= PMAX; ++k) o.F[k - 1] = q * d1[k];
+    }
+    if constexpr (NEEDE) {
+        double d2f = 0.0;
+#pragma unroll
+        for (int k = 2; k <= PMAX; ++k) d2f = fma(a[k], d2[k], d2f);
+        o.E = fma(d2f, (xd * t) * gp, g + nugget);
+    } else {
+        o.E = 0.0;
+    }
+}
+
+template <int PMAX, bool NEEDJ, bool NEEDE>
+struct QuadOut {
+    double Ih;
+    double J[NEEDJ ? PMAX : 1];
+    double IE;
+};
+
+// AdaptiveClenshawCurtis::Integrate on [0,1] (Quadrature.h:819-968) with the
+// QuadError::First metric (:441-481).  Depth-first, left-first bisection; the
+// stack keeps (right end, level, integrand at right end).  Intervals, nodes,
+// accept/reject tests and the order in which accepted fine sums are added are
+// the reference's.
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+__device__ __forceinline__ void integrate(const double* a, int P, double xd, const QuadParams& Q, const BasisConsts& bc,
+                                       double nugget, QuadOut<PMAX, NEEDJ, NEEDE>& R, int& st) {
+    using NV = NodeVal<PMAX, NEEDJ, NEEDE>;
+    constexpr int NJ = NEEDJ ? PMAX : 1;
+    double stX[kMaxSubCap];
+    int stL[kMaxSubCap];
+    double stH[kMaxSubCap];
+    double stF[kMaxSubCap][NJ];
+    double stE[kMaxSubCap];
+
+    R.Ih = 0.0;
+    R.IE = 0.0;
+#pragma unroll
+    for (int k = 0; k < NJ; ++k) R.J[k] = 0.0;
+
+    NV A, B, M, V;
+    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(0.0, xd, a, P, bc, nugget, A, st);
+    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(1.0, xd, a, P, bc, nugget, B, st);
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    if (st & (kStatusInf | kStatusNaN)) { R.Ih = nan; return; }
+
+    const int cR = Q.nCoarse - 1, cM = cR / 2, fR = Q.nFine - 1, fM = fR / 2;
+    double lo = 0.0, hi = 1.0;
+    int level = 0, sp = 0;
+    long long nIntervals = 0;
+    while (true) {
+        const double m = 0.5 * (lo + hi);
+        const double s = 0.5 * (hi - lo);
+        evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m, xd, a, P, bc, nugget, M, st);
+        double ic = (s * Q.cWts[0]) * A.h;
+        ic = fma(s * Q.cWts[cM], M.h, ic);
+        ic = fma(s * Q.cWts[cR], B.h, ic);
+        const double w0 = s * Q.fWts[0], wM = s * Q.fWts[fM], wR = s * Q.fWts[fR];
+        double ih = w0 * A.h;
+        ih = fma(wM, M.h, ih);
+        ih = fma(wR, B.h, ih);
+        double iF[NJ];
+        double iE = 0.0;
+        if constexpr (NEEDJ) {
+#pragma unroll
+            for (int k = 0; k < NJ; ++k) iF[k] = fma(wR, B.F[k], fma(wM, M.F[k], w0 * A.F[k]));
+        }
+        if constexpr (NEEDE) iE = fma(wR, B.E, fma(wM, M.E, w0 * A.E));
+        // Coarse interior points other than the midpoint (level >= 2 rules).
+        for (int i = 1; i < cR; ++i) {
+            if (i == cM) continue;
+            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.cPts[i], xd, a, P, bc, nugget, V, st);
+            ic = fma(s * Q.cWts[i], V.h, ic);
+            const double wf = s * Q.fWts[2 * i];
+            ih = fma(wf, V.h, ih);
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) iF[k] = fma(wf, V.F[k], iF[k]);
+            }
+            if constexpr (NEEDE) iE = fma(wf, V.E, iE);
+        }
+        // Points only in the fine rule.
+        for (int i = 1; i < Q.nFine; i += 2) {
+            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.fPts[i], xd, a, P, bc, nugget, V, st);
+            const double wf = s * Q.fWts[i];
+            ih = fma(wf, V.h, ih);
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) iF[k] = fma(wf, V.F[k], iF[k]);
+            }
+            if constexpr (NEEDE) iE = fma(wf, V.E, iE);
+        }
+        if (st & (kStatusInf | kStatusNaN)) { R.Ih = nan; return; }
+        const double err = fabs(ih - ic);
+        const double tol = fmax(Q.relTol * fabs(ic), Q.absTol);
+        const bool accept = ((err < tol) || (level == Q.maxSub - 1)) && (level >= Q.minSub);
+        if (accept) {
+            R.Ih += ih;
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) R.J[k] += iF[k];
+            }
+            if constexpr (NEEDE) R.IE += iE;
+            if (sp == 0) break;
+            --sp;
+            lo = hi;
+            A = B;
+            hi = stX[sp];
+            level = stL[sp];
+            B.h = stH[sp];
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) B.F[k] = stF[sp][k];
+            }
+            if constexpr (NEEDE) B.E = stE[sp];
+        } else {
+            stX[sp] = hi;
+            stL[sp] = level + 1;
+            stH[sp] = B.h;
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) stF[sp][k] = B.F[k];
+            }
+            if constexpr (NEEDE) stE[sp] = B.E;
+            ++sp;
+            hi = m;
+            B = M;
+            ++level;
+        }
+        if (++nIntervals >= Q.maxIntervals) {
+            st |= kStatusBudget;
+            R.Ih = nan;
+            return;
+        }
+    }
+}
+
+// Value-only integral for the inverse solver.
+template <int BASIS, int POS, int PMAX>
+__device__ __forceinline__ double integrateValue(const double* a, int P, double xd, const QuadParams& Q,
+                                                 const BasisConsts& bc, double nugget, int& st) {
+    QuadOut<PMAX, false, false> R;
+    integrate<BASIS, POS, PMAX, false, false>(a, P, xd, Q, bc, nugget, R, st);
+    return R.Ih;
+}
+
+// --------------------------------------------------------------------------
+// Shared-memory helpers.  Per-thread tables are stored row-major with one
+// column per thread ([row][tpb + pad]) so that a warp reading the same row
+// touches consecutive words.
+// --------------------------------------------------------------------------
+struct SmemLayout {
+    double* X;   // [dmax][tpb]        coordinates of the tile's points
+    double* B;   // [nBmax][tpb+1]     leading-coordinate basis values
+    double* Bd;  // [nBmax][tpb+1]     their derivatives (input gradient)
+    double* S;   // [depthMax+1][tpb]  prefix-product stack
+    double* W;   // [PMAX+1][tpb]      per-point adjoint weights
+    double* GX;  // [dmax][tpb]        input gradient accumulators
+    double* DS;  // [tri(depthMax+1)][tpb]  forward-mode derivative stack
+    int bstride;
+};
+
+__host__ __device__ inline size_t smemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input) {
+    size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)(depthMax + 1) * tpb +
+               (size_t)(pmax + 1) * tpb;
+    if (input) {
+        n += (size_t)nBmax * (tpb + 1) + (size_t)dmax * tpb +
+             (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
+    }
+    return n * sizeof(double);
+}
+
+__device__ inline SmemLayout carveSmem(double* base, int tpb, int dmax, int nBmax, int depthMax, int pmax,
+                                       bool input) {
+    SmemLayout L;
+    L.bstride = tpb + 1;
+    double* p = base;
+    L.X = p; p += (size_t)dmax * tpb;
+    L.B = p; p += (size_t)nBmax * (tpb + 1);
+    L.S = p; p += (size_t)(depthMax + 1) * tpb;
+    L.W = p; p += (size_t)(pmax + 1) * tpb;
+    if (input) {
+        L.Bd = p; p += (size_t)nBmax * (tpb + 1);
+        L.GX = p; p += (size_t)dmax * tpb;
+        L.DS = p;
+    } else {
+        L.Bd = nullptr; L.GX = nullptr; L.DS = nullptr;
+    }
+    return L;
+}
+
+// Fill the leading-coordinate basis table for one thread.
+template <int BASIS, bool DERIV>
+__device__ __forceinline__ void fillLead(const CompDesc& c, const SmemLayout& L, int tid, const BasisConsts& bc) {
+    for (int d = 0; d < c.D - 1; ++d) {
+        const int p = __ldg(&c.leadDeg[d]);
+        const int r = __ldg(&c.rowOff[d]);
+        const double x = L.X[d * blockDim.x + tid];
+        leadBasis<BASIS, DERIV>(x, p, bc, &L.B[r * L.bstride + tid], DERIV ? &L.Bd[r * L.bstride + tid] : nullptr,
+                                L.bstride);
+    }
+}
+
+// Phase A: a_k = sum_m c_(m,k) Phi_m for this thread's point.
+template <int PMAX>
+__device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, int tid, const double* cm,
+                                       double* a) {
+#pragma unroll
+    for (int k = 0; k <= PMAX; ++k) a[k] = 0.0;
+    const int tpb = blockDim.x;
+    L.S[tid] = 1.0;
+    for (int n = 0; n < c.nNodes; ++n) {
+        const uint32_t w = __ldg(&c.nodeA[n]);
+        const int depth = w & 31;
+        const int nk = (w >> 5) & 31;
+        const int brow = w >> 18;
+        double phi = 1.0;
+        if (depth > 0) {
+            phi = L.S[(depth - 1) * tpb + tid] * L.B[brow * L.bstride + tid];
+            L.S[depth * tpb + tid] = phi;
+        }
+        if (nk) accumCoeffs<PMAX>(nk, phi, cm + __ldg(&c.nodeSlot[n]), a);
+    }
+}
+
+// --------------------------------------------------------------------------
+// The fused kernel.
+// --------------------------------------------------------------------------
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+__global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ FusedParams prm) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int tpb = blockDim.x;
+    const bool inputMode = (prm.flags & kFlagInput) != 0;
+    const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, inputMode);
+    const WorkItem item = prm.items[blockIdx.x];
+    const int flags = prm.flags;
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    const double ninf = __longlong_as_double(0xfff0000000000000ULL);
+
+    for (int tile = item.tile0; tile < item.tile0 + item.nTiles; ++tile) {
+        const long long i = (long long)tile * tpb + tid;
+        const bool active = i < prm.N;
+        int st = 0;
+        // Coordinates of the tile (the largest component of the range reads the most).
+        const int dneed = prm.comps[item.c1 - 1].D;
+        for (int d = 0; d < dneed; ++d)
+            L.X[d * tpb + tid] = active ? prm.pts[d * prm.ptsRs + i * prm.ptsCs] : 0.0;
+        double logdetSum = 0.0;
+        double lossAcc = 0.0;
+        if (inputMode)
+            for (int d = 0; d < dneed; ++d) L.GX[d * tpb + tid] = 0.0;
+
+        for (int ci = item.c0; ci < item.c1; ++ci) {
+            const CompDesc& c = prm.comps[ci];
+            const double* cm = prm.cm + c.slotOffset;
+            const int P = c.P;
+            if (inputMode) fillLead<BASIS, true>(c, L, tid, prm.bc);
+            else fillLead<BASIS, false>(c, L, tid, prm.bc);
+
+            double a[PMAX + 1];
+            phaseA<PMAX>(c, L, tid, cm, a);
+            const double xd = L.X[(c.D - 1) * tpb + tid];
+
+            // Last-coordinate basis at 0 and at x_D.
+            const double* v0 = prm.bc.v0;
+            double d1x[PMAX + 1], d2x[PMAX + 1];
+            lastBasis<BASIS, PMAX, false, true, true>(xd, P, prm.bc, nullptr, d1x, d2x);
+            double dfx = 0.0, d2fx = 0.0, f0 = 0.0;
+#pragma unroll
+            for (int k = 0; k <= PMAX; ++k) {
+                f0 = fma(a[k], v0[k], f0);
+                dfx = fma(a[k], d1x[k], dfx);
+                d2fx = fma(a[k], d2x[k], d2fx);
+            }
+            double gx, gpx;
+            posEval<POS>(dfx, gx, gpx);
+
+            const bool needT = (flags & (kFlagEval | kFlagCoefDenseT | kFlagKL)) != 0 ||
+                               (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput)));
+            QuadOut<PMAX, NEEDJ, NEEDE> R;
+            R.Ih = 0.0; R.IE = 0.0;
+#pragma unroll
+            for (int k = 0; k < (NEEDJ ? PMAX : 1); ++k) R.J[k] = 0.0;
+            if (needT && active) integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
+            const double T = R.Ih + f0;
+            const double logdet = (gx <= 0.0) ? ninf : log(gx);
+
+            if ((flags & kFlagEval) && active) prm.outEval[(long long)c.outRow * prm.evalRs + i * prm.evalCs] = T;
+            if (flags & kFlagLogDet) logdetSum += logdet;
+
+            // Per-point adjoint weights.
+            double sens = 0.0, lsens = 0.0;
+            if (flags & kFlagKL) {
+                sens = T * prm.sensScale;
+                lsens = prm.lsensScale;
+                if (active) lossAcc += 0.5 * T * T - logdet;
+            } else {
+                if (prm.sens && active) sens = prm.sens[(long long)c.outRow * prm.sensRs + i * prm.sensCs];
+                if (flags & (kFlagCoefReduced | kFlagInput))
+                    lsens = prm.lsens ? (active ? prm.lsens[i * prm.lsensStride] : 0.0) : prm.lsensScale;
+            }
+            if (!active) { sens = 0.0; lsens = 0.0; }
+            const double ldScale = gpx * (1.0 / gx);
+            double wT[PMAX + 1], wL[PMAX + 1];
+#pragma unroll
+            for (int k = 0; k <= PMAX; ++k) {
+                const double Jk = (NEEDJ && k >= 1) ? R.J[k >= 1 ? k - 1 : 0] : 0.0;
+                wT[k] = sens * (v0[k] + Jk);
+                wL[k] = lsens * (ldScale * d1x[k]);
+            }
+
+            // Dense per-term outputs (CoeffGradImpl / LogDeterminantCoeffGradImpl).
+            if ((flags & (kFlagCoefDenseT | kFlagCoefDenseL)) && active) {
+                const bool useT = (flags & kFlagCoefDenseT) != 0;
+                double wd[PMAX + 1];
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) wd[k] = useT ? wT[k] : (ldScale * d1x[k]);
+                L.S[tid] = 1.0;
+                for (int n = 0; n < c.nNodes; ++n) {
+                    const uint32_t w = __ldg(&c.nodeA[n]);
+                    const int depth = w & 31, nk = (w >> 5) & 31, brow = w >> 18;
+                    double phi = 1.0;
+                    if (depth > 0) {
+                        phi = L.S[(depth - 1) * tpb + tid] * L.B[brow * L.bstride + tid];
+                        L.S[depth * tpb + tid] = phi;
+                    }
+                    if (nk) {
+                        const int slot = __ldg(&c.nodeSlot[n]);
+#pragma unroll
+                        for (int k = 0; k <= PMAX; ++k) {
+                            if (k < nk) {
+                                const int t = __ldg(&c.slotTerm[slot + k]);
+                                if (t >= 0)
+                                    prm.outDense[(long long)(c.coeffOffset + t) * prm.denseRs + i * prm.denseCs] =
+                                        phi * wd[k];
+                            }
+                        }
+                    }
+                }
+            }
+
+            // Input gradient: forward mode over the prefix tree.
+            if (inputMode) {
+                double w[PMAX + 1];
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) w[k] = wT[k] + wL[k];
+                // Triangular stack: DS[tri(l) + j] = d Phi_l / d (factor j), j = 1..l.
+                int dims[kMaxDepth + 1];
+                L.S[tid] = 1.0;
+                for (int n = 0; n < c.nNodes; ++n) {
+                    const uint32_t wd = __ldg(&c.nodeA[n]);
+                    const int depth = wd & 31, nk = (wd >> 5) & 31, dim = (wd >> 10) & 255, brow = wd >> 18;
+                    if (depth > 0) {
+                        const double bv = L.B[brow * L.bstride + tid];
+                        const double bd = L.Bd[brow * L.bstride + tid];
+                        const double pphi = L.S[(depth - 1) * tpb + tid];
+                        L.S[depth * tpb + tid] = pphi * bv;
+                        const int tl = depth * (depth + 1) / 2, tp = (depth - 1) * depth / 2;
+                        for (int j = 1; j < depth; ++j)
+                            L.DS[(tl + j) * tpb + tid] = L.DS[(tp + j) * tpb + tid] * bv;
+                        L.DS[(tl + depth) * tpb + tid] = pphi * bd;
+                        dims[depth] = dim;
+                    }
+                    if (nk && depth > 0) {
+                        const double* cs = cm + __ldg(&c.nodeSlot[n]);
+                        double beta = 0.0;
+                        for (int k = 0; k < nk; ++k) beta = fma(__ldg(&cs[k]), w[k < PMAX ? k : PMAX], beta);
+                        const int tl = depth * (depth + 1) / 2;
+                        for (int j = 1; j <= depth; ++j) {
+                            double* g = &L.GX[dims[j] * tpb + tid];
+                            *g = fma(beta, L.DS[(tl + j) * tpb + tid], *g);
+                        }
+                    }
+                }
+                // Last coordinate: quadrature of the x_D-derivative integrand and the
+                // log-det term (MonotoneComponent.h:811-815, :892-925).
+                double gxd = lsens * (ldScale * d2fx);
+                if constexpr (NEEDE) gxd = fma(sens, R.IE, gxd);
+                double* g = &L.GX[(c.D - 1) * tpb + tid];
+                *g += gxd;
+            }
+
+            // Reduced combined adjoint: owner-computes over the block's points.
+            if (flags & kFlagCoefReduced) {
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) L.W[k * tpb + tid] = wT[k] + wL[k];
+                __syncthreads();
+                const bool first = (tile == item.tile0);
+                double* part = prm.partials + item.partialBase;
+                for (int n = tid; n < c.nCNodes; n += tpb) {
+                    const uint32_t w = __ldg(&c.nodeC[n]);
+                    const int depth = w & 31, nk = (w >> 5) & 31, slot = w >> 10;
+                    const uint16_t* rows = c.nodeCRows + (size_t)n * kMaxDepth;
+                    int r[kMaxDepth];
+#pragma unroll
+                    for (int q = 0; q < kMaxDepth; ++q) r[q] = (q < depth) ? (int)__ldg(&rows[q]) : 0;
+                    double acc[PMAX + 1];
+#pragma unroll
+                    for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
+                    for (int j = 0; j < tpb; ++j) {
+                        const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
+                        accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
+                    }
+#pragma unroll
+                    for (int k = 0; k <= PMAX; ++k) {
+                        if (k < nk) {
+                            const int t = __ldg(&c.slotTerm[slot + k]);
+                            if (t >= 0) {
+                                double* dst = part + t;
+                                *dst = first ? acc[k] : (*dst + acc[k]);
+                            }
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            if (prm.statusWord && st) atomicOr(prm.statusWord, st);
+        }  // components
+
+        if (active) {
+            if (flags & kFlagLogDet) prm.outLogDet[i * prm.logDetStride] = logdetSum;
+            if (inputMode) {
+                const int dneed2 = prm.comps[item.c1 - 1].D;
+                for (int d = 0; d < dneed2; ++d)
+                    prm.outInput[d * prm.inputRs + i * prm.inputCs] = L.GX[d * tpb + tid];
+            }
+            if (flags & kFlagStatusArray) prm.status[i * prm.statusStride] = st;
+        }
+        if (flags & kFlagKL) {
+            // Block sum of the loss in a fixed order (thread 0 adds the smem column).
+            __syncthreads();
+            L.W[tid] = lossAcc;
+            __syncthreads();
+            if (tid == 0) {
+                double s = 0.0;
+                for (int j = 0; j < tpb; ++j) s += L.W[j];
+                double* dst = prm.lossPartials + item.lossSlot;
+                *dst = (tile == item.tile0) ? s : (*dst + s);
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+    (void)nan;
+}
+
+// --------------------------------------------------------------------------
+// Inverse: all components of the map, in order, for a tile of points
+// (TriangularMap::InverseInplace, src/TriangularMap.cpp:161-184, with
+// MonotoneComponent::InverseImpl, MonotoneComponent.h:330-443, and
+// RootFinding::InverseSingleBracket, RootFinding.h:125-178).
+// --------------------------------------------------------------------------
+template <int PMAX>
+struct ACoef {
+    double a[PMAX + 1];
+};
+
+template <int BASIS, int POS, int PMAX>
+__device__ __noinline__ double integrateValueNI(const ACoef<PMAX> A, int P, double xd, const QuadParams* Q,
+                                                const BasisConsts* bc, double nugget, int* st) {
+    int s = 0;
+    const double I = integrateValue<BASIS, POS, PMAX>(A.a, P, xd, *Q, *bc, nugget, s);
+    *st |= s;
+    return I;
+}
+
+template <int BASIS, int POS, int PMAX>
+struct InverseEval {
+    ACoef<PMAX> A;
+    int P;
+    double f0;
+    const QuadParams* Q;
+    const BasisConsts* bc;
+    double nugget;
+    int* st;
+    __device__ double operator()(double x) const {
+        return integrateValueNI<BASIS, POS, PMAX>(A, P, x, Q, bc, nugget, st) + f0;
+    }
+};
+
+template <class F>
+__device__ void findBracket(const F& f, double& xlb, double& ylb, double& xub, double& yub, const double yd,
+                            int& info) {
+    const unsigned maxIts = 128;
+    double stepSize = 1.0;
+    info = 0;
+    ylb = f(xlb);
+    yub = f(xub);
+    if (ylb > yd) {
+        double t = ylb; ylb = yub; yub = t;
+        t = xlb; xlb = xub; xub = t;
+        unsigned i;
+        for (i = 0; i < maxIts; ++i) {
+            xlb = xub - stepSize;
+            ylb = f(xlb);
+            if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { info = -1; return; }
+            if (ylb > yd) { yub = ylb; xub = xlb; stepSize *= 2.0; }
+            else break;
+        }
+        if (i >= maxIts) info = -2;
+    } else {
+        unsigned i;
+        for (i = 0; i < maxIts; ++i) {
+            xub = xlb + stepSize;
+            yub = f(xub);
+            if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { info = -1; return; }
+            if (yub < yd) { ylb = yub; xlb = xub; stepSize *= 2.0; }
+            else break;
+        }
+        if (i >= maxIts) info = -2;
+    }
+}
+
+__device__ __forceinline__ double findXITP(double xlb, double xub, double ylb, double yub, double k1, double k2,
+                                           double nhalf, double n0, int it, double xtol) {
+    const double xb = 0.5 * (xub + xlb);
+    double xf = (xub * ylb - xlb * yub) / (ylb - yub);
+    const double sigma = ((xb - xf) > 0) ? 1.0 : -1.0;
+    const double delta = fmin(k1 * pow((xub - xlb), k2), fabs(xb - xf));
+    xf += delta * sigma;
+    const double rho = fmin(xtol * pow(2.0, nhalf + n0 - it) - 0.5 * (xub - xlb), fabs(xf - xb));
+    return xb - sigma * rho;
+}
+
+template <class F>
+__device__ double inverseSingleBracket(double yd, const F& f, double x0, double xtol, double ftol, int& info) {
+    const unsigned maxIts = 10000;
+    double xlb, xub, ylb, yub, xc, yc;
+    info = 0;
+    xlb = xub = x0;
+    ylb = yub = f(xlb);
+    int binfo = 0;
+    findBracket(f, xlb, ylb, xub, yub, yd, binfo);
+    if ((binfo < 0) || (((ylb > yd) || (yub < yd)))) {
+        info = -2;
+        return __longlong_as_double(0x7ff8000000000000ULL);
+    }
+    const double k1 = 0.1, k2 = 2.0;
+    const double nhalf = ceil(log2(0.5 * (xub - xlb) / xtol));
+    const double n0 = 1.0;
+    unsigned it;
+    for (it = 0; it < maxIts; ++it) {
+        xc = findXITP(xlb, xub, ylb, yub, k1, k2, nhalf, n0, (int)it, xtol);
+        yc = f(xc);
+        if (fabs(yc - yd) < ftol) return xc;
+        else if (yc > yd) { xub = xc; yub = yc; }
+        else { xlb = xc; ylb = yc; }
+        if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) break;
+    }
+    return 0.5 * (xub + xlb);
+}
+
+template <int BASIS, int POS, int PMAX>
+__global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ InverseParams prm) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int tpb = blockDim.x;
+    const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
+    const long long i = (long long)blockIdx.x * tpb + tid;
+    const bool active = i < prm.N;
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    const int inDim = prm.comps[prm.nComps - 1].D;
+    // fullOut = [x1; 0] (TriangularMap.cpp:146-159)
+    const long long xi = (prm.x1Cols == 1) ? 0 : i;
+    for (int d = 0; d < inDim; ++d) {
+        double v = 0.0;
+        if (active && d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+        L.X[d * tpb + tid] = v;
+    }
+    int stAll = 0;
+    for (int ci = 0; ci < prm.nComps; ++ci) {
+        const CompDesc& c = prm.comps[ci];
+        const double* cm = prm.cm + c.slotOffset;
+        fillLead<BASIS, false>(c, L, tid, prm.bc);
+        ACoef<PMAX> A;
+        phaseA<PMAX>(c, L, tid, cm, A.a);
+        double result = nan;
+        int info = 0;
+        if (active) {
+            bool hasNan = false;
+            for (int d = 0; d < c.D; ++d) hasNan |= isnan(L.X[d * tpb + tid]);
+            if (!hasNan) {
+                double f0 = 0.0;
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) f0 = fma(A.a[k], prm.bc.v0[k], f0);
+                int st = 0;
+                InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
+                const double yd = prm.r[(long long)ci * prm.rRs + i * prm.rCs];
+                result = inverseSingleBracket(yd, f, L.X[(c.D - 1) * tpb + tid], prm.xtol, prm.ytol, info);
+                if (info < 0) st |= kStatusNoBracket;
+                stAll |= st;
+            }
+            L.X[(c.D - 1) * tpb + tid] = result;
+            prm.out[(long long)ci * prm.outRs + i * prm.outCs] = result;
+            if (prm.info) prm.info[(long long)ci * prm.infoStride + i] = info;
+        }
+    }
+    if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
+}
+
+// --------------------------------------------------------------------------
+// Per-order launchers (instantiated in mpgb_inst_*.cu).
+// --------------------------------------------------------------------------
+template <int BASIS, int POS, int PMAX>
+cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int needE, cudaStream_t stream) {
+    const bool input = (prm.flags & kFlagInput) != 0;
+    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, input);
+    auto run = [&](auto kern) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<nItems, prm.tpb, smem, stream>>>(prm);
+        return cudaGetLastError();
+    };
+    if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, true>);
+    if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, false>);
+    return run(fusedKernel<BASIS, POS, PMAX, false, false>);
+}
+
+template <int BASIS, int POS, int PMAX>
+cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t stream) {
+    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
+    auto kern = inverseKernel<BASIS, POS, PMAX>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nBlocks, prm.tpb, smem, stream>>>(prm);
+    return cudaGetLastError();
+}
+
+}  // namespace mpgb

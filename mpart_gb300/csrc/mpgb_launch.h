@@ -1,0 +1,24 @@
+// Host-callable launchers of the kernels in mpgb_kernels.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include "mpgb_types.h"
+
+namespace mpgb {
+
+// Smallest instantiated last-coordinate order >= p, or -1.
+int instantiatedPmax(int p);
+
+size_t fusedSmemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input);
+
+cudaError_t launchFused(int basis, int pos, int pmax, const FusedParams& prm, int nItems, int needJ, int needE,
+                        cudaStream_t stream);
+cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm, int nBlocks, cudaStream_t stream);
+cudaError_t launchGather(const int32_t* slotGlobalTerm, int nSlots, const double* coeffs, double* cm,
+                         cudaStream_t stream);
+cudaError_t launchReduceRows(const double* part, const long long* rowBase, int nRows, int nTerms, double scale,
+                             double* out, int accumulate, cudaStream_t stream);
+cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
+                          cudaStream_t stream);
+cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
+
+}  // namespace mpgb

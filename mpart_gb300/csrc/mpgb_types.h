@@ -1,0 +1,99 @@
+// Launch-time structures shared by the host planner and the kernels.
+#pragma once
+#include <stdint.h>
+#include "mpgb_device.cuh"
+
+namespace mpgb {
+
+// One monotone component as the kernels see it.  Device arrays are built by
+// the host planner from the component's multi-index set (see Program in
+// mpgb_host.cu) and live as long as the component object.
+struct CompDesc {
+    int D;          // input dimension of the component
+    int P;          // largest order in the last coordinate
+    int nB;         // rows of the per-point basis table (orders >= 1 of the leading coordinates)
+    int nNodes;     // prefix-tree nodes (phase A / dense outputs / input gradient), DFS pre-order
+    int nSlots;     // dense (node, k) coefficient slots
+    int nCNodes;    // prefix nodes that carry terms (reduced coefficient adjoint), sorted by (depth, nk)
+    int maxDepth;   // deepest prefix (number of nonzero leading factors)
+    int numTerms;   // coefficients of this component
+    int outRow;     // output row of this component in the map output
+    int coeffOffset;  // offset of its block in the map coefficient vector
+    int slotOffset;   // offset of its slots in the map-wide gathered coefficient table
+    int pad_;
+    const uint32_t* nodeA;   // [nNodes] depth | nk<<5 | dim<<10 | brow<<18
+    const uint32_t* nodeSlot;  // [nNodes] first slot of the node
+    const uint32_t* nodeC;   // [nCNodes] depth | nk<<5 | slot<<10
+    const uint16_t* nodeCRows;  // [nCNodes * kMaxDepth] basis rows along the path
+    const int32_t* slotTerm; // [nSlots] coefficient index within the component, or -1
+    const int32_t* leadDeg;  // [D-1] largest order per leading coordinate
+    const int32_t* rowOff;   // [D-1] first basis row of each leading coordinate
+};
+
+// A block's work: points [tile0*TPB, (tile0+nTiles)*TPB) of components [c0, c1).
+struct WorkItem {
+    int c0, c1;
+    int tile0, nTiles;
+    long long partialBase;  // first double of this item's partial row (reduced adjoint)
+    int lossSlot;           // index into the loss partials (KL)
+    int pad_;
+};
+
+enum FusedFlags : int {
+    kFlagEval = 1,          // write T_c(x) to outEval row outRow
+    kFlagLogDet = 2,        // sum log d_D T_c over the component range into outLogDet
+    kFlagCoefDenseT = 4,    // dense sens-scaled coefficient gradient of T (CoeffGradImpl)
+    kFlagCoefDenseL = 8,    // dense coefficient gradient of log-det (LogDeterminantCoeffGradImpl)
+    kFlagCoefReduced = 16,  // sum over points of the combined weights into partial rows
+    kFlagInput = 32,        // combined input gradient into outInput (GradientImpl / LogDeterminantInputGradImpl)
+    kFlagKL = 64,           // sens_c = T_c * sensScale, lsens = lsensScale, loss partials
+    kFlagStatusArray = 128, // per-point status words
+};
+
+struct FusedParams {
+    const CompDesc* comps;
+    const WorkItem* items;
+    const double* cm;       // gathered coefficients (all components)
+    long long N;
+    int flags;
+    int tpb;
+    // inputs
+    const double* pts; long long ptsRs, ptsCs;
+    const double* sens; long long sensRs, sensCs;   // one row per component (map output row)
+    const double* lsens; long long lsensStride;     // log-det sensitivity per point (or null = lsensScale)
+    double sensScale, lsensScale;
+    // outputs
+    double* outEval; long long evalRs, evalCs;
+    double* outLogDet; long long logDetStride;
+    double* outDense; long long denseRs, denseCs;   // numCoeffs x N
+    double* outInput; long long inputRs, inputCs;   // inputDim x N
+    double* partials;
+    double* lossPartials;
+    int* status; long long statusStride;
+    int* statusWord;
+    double nugget;
+    int dmax, nBmax, depthMax, pad_;
+    QuadParams quad;
+    BasisConsts bc;
+};
+
+struct InverseParams {
+    const CompDesc* comps;
+    int nComps;
+    const double* cm;
+    long long N;
+    int tpb;
+    int extra;               // inputDim - outputDim
+    const double* x1; long long x1Rs, x1Cs; int x1Rows; int x1Cols;  // x1Cols == 1 broadcasts
+    const double* r; long long rRs, rCs;
+    double* out; long long outRs, outCs;
+    int* info; long long infoStride;
+    int* statusWord;
+    double xtol, ytol;
+    double nugget;
+    int dmax, nBmax, depthMax, pad_;
+    QuadParams quad;
+    BasisConsts bc;
+};
+
+}  // namespace mpgb

@@ -1,0 +1,328 @@
+"""Parity of the sm_103a kernels (called through the C ABI) with the CPU
+oracle on the same seeded inputs.
+
+Tolerance: an entry passes when |gpu - oracle| <= 1e-10 * max(|oracle|,
+1e-6 * max|oracle over the array|); the floor only matters for entries a
+million times smaller than the array's largest.  Inverses are compared to
+the solver's own tolerance (|dx| <= 2 xtol, or |dT| <= 2 ytol)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def assert_parity(a, b, rtol=RTOL, floor=1e-6, what=""):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, f"{what}: shape {a.shape} vs {b.shape}"
+    if b.size == 0:
+        return
+    scale = np.nanmax(np.abs(b)) if np.isfinite(b).any() else 1.0
+    tol = rtol * np.maximum(np.abs(b), floor * scale)
+    same = (a == b) | (np.isnan(a) & np.isnan(b))
+    bad = ~same & ~(np.abs(a - b) <= tol)
+    if bad.any():
+        i = np.argmax(np.where(bad, np.abs(a - b) / np.maximum(tol, 1e-300), 0))
+        raise AssertionError(f"{what}: {bad.sum()} of {b.size} entries outside tolerance; worst at {np.unravel_index(i, b.shape)}: "
+                             f"gpu={a.flat[i]!r} oracle={b.flat[i]!r}")
+
+
+def T(x):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float64, device="cuda")
+
+
+def H(t):
+    return t.detach().cpu().numpy()
+
+
+def opts(M, basis=0, pos=1, tol=1e-6, maxsub=30):
+    return M.MapOptions(basisType=M.BasisTypes(basis), posFuncType=M.PosFuncTypes(pos),
+                        quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=tol, quadRelTol=tol,
+                        quadMaxSub=maxsub)
+
+
+def oracle_tri(O, inp, out, order, basis=0, pos=1, tol=1e-6, maxsub=30):
+    return O.OracleTriangularMap(inp, out, order, basis=basis, normalize=True, posfunc=pos, abs_tol=tol,
+                                 rel_tol=tol, max_sub=maxsub)
+
+
+# ----------------------------------------------------------------------------
+# C1: 2 x 2 triangular map, total order 3, ProbabilistHermite + SoftPlus.
+# ----------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def c1(gpu, oracle):
+    M, O = gpu, oracle
+    rng0, rng1 = np.random.default_rng(0), np.random.default_rng(1)
+    tm = M.CreateTriangular(2, 2, 3, opts(M))
+    om = oracle_tri(O, 2, 2, 3)
+    coef = rng0.normal(0.0, 0.1, tm.numCoeffs)
+    x = rng1.standard_normal((2, 10000))
+    tm.SetCoeffs(coef)
+    return M, O, tm, om, coef, x
+
+
+def test_c1_evaluate_logdet(c1):
+    M, O, tm, om, coef, x = c1
+    y = H(tm.Evaluate(T(x)))
+    assert_parity(y, om.evaluate(coef, x), what="Evaluate")
+    ld = H(tm.LogDeterminant(T(x)))
+    assert_parity(ld, om.logdet(coef, x), what="LogDeterminant")
+
+
+def test_c1_inverse(c1):
+    M, O, tm, om, coef, x = c1
+    r = om.evaluate(coef, x)
+    for x1 in (x, np.zeros((0, x.shape[1]))):
+        xi = H(tm.Inverse(T(x1), T(r)))
+        ref = om.inverse(coef, x1, r)
+        assert np.all(np.abs(xi - ref) <= 2e-6), f"inverse differs by {np.max(np.abs(xi - ref))}"
+        assert np.max(np.abs(xi - x)) < 1e-5
+
+
+def test_c1_coefficient_gradients(c1):
+    M, O, tm, om, coef, x = c1
+    xs = x[:, :2000]
+    sens = np.random.default_rng(7).standard_normal((2, xs.shape[1]))
+    g = H(tm.CoeffGrad(T(xs), T(sens)))
+    assert_parity(g, om.coeff_grad(coef, xs, sens), what="CoeffGrad")
+    lg = H(tm.LogDeterminantCoeffGrad(T(xs)))
+    assert_parity(lg, om.logdet_coeff_grad(coef, xs), what="LogDeterminantCoeffGrad")
+
+
+def test_c1_input_gradients(c1):
+    M, O, tm, om, coef, x = c1
+    xs = x[:, :2000]
+    sens = np.random.default_rng(8).standard_normal((2, xs.shape[1]))
+    g = H(tm.Gradient(T(xs), T(sens)))
+    assert_parity(g, om.gradient(coef, xs, sens), what="Gradient")
+    lg = H(tm.LogDeterminantInputGrad(T(xs)))
+    assert_parity(lg, om.logdet_input_grad(coef, xs), what="LogDeterminantInputGrad")
+
+
+def test_c1_fused_reduced_adjoint(c1):
+    import torch
+    M, O, tm, om, coef, x = c1
+    sens = np.random.default_rng(9).standard_normal((2, x.shape[1]))
+    lsens = np.random.default_rng(10).standard_normal(x.shape[1])
+    out = torch.zeros(2, x.shape[1], dtype=torch.float64, device="cuda")
+    ld = torch.zeros(x.shape[1], dtype=torch.float64, device="cuda")
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device="cuda")
+    ig = torch.zeros(2, x.shape[1], dtype=torch.float64, device="cuda")
+    tm.FusedForwardAdjointImpl(T(x), sens=T(sens), logdet_sens=T(lsens), out_eval=out, out_logdet=ld,
+                               coeff_grad=cg, input_grad=ig)
+    assert_parity(H(out), om.evaluate(coef, x), what="fused eval")
+    assert_parity(H(ld), om.logdet(coef, x), what="fused logdet")
+    ref_cg = om.coeff_grad(coef, x, sens).sum(axis=1) + (om.logdet_coeff_grad(coef, x) * lsens).sum(axis=1)
+    assert_parity(H(cg), ref_cg, floor=1e-3, what="fused coefficient gradient")
+    ref_ig = om.gradient(coef, x, sens) + om.logdet_input_grad(coef, x) * lsens
+    assert_parity(H(ig), ref_ig, what="fused input gradient")
+
+
+def test_c1_kl_objective(c1):
+    M, O, tm, om, coef, x = c1
+    loss, grad = tm.KLObjective(T(x))
+    cs = om.split(coef)
+    for i, c in enumerate(om.comps):
+        l, g = O.fast_gaussian_reverse_kl(c, cs[i], x[:c.input_dim])
+        assert_parity(H(loss)[i:i + 1], [l], what=f"KL loss comp {i}")
+        assert_parity(H(grad)[om.offsets[i]:om.offsets[i + 1]], g, floor=1e-3, what=f"KL grad comp {i}")
+
+
+def test_c1_host_buffers_match_device(c1):
+    M, O, tm, om, coef, x = c1
+    xs = np.ascontiguousarray(x[:, :500])
+    y_host = tm.Evaluate(xs)  # numpy in -> staged through the device
+    y_dev = H(tm.Evaluate(T(xs)))
+    np.testing.assert_array_equal(y_host, y_dev)
+    # strided (transposed) host input
+    xt = np.asfortranarray(xs)
+    np.testing.assert_array_equal(tm.Evaluate(xt), y_dev)
+
+
+# ----------------------------------------------------------------------------
+# C2 (reduced size): one component, D = 8, total order 4 (495 terms).
+# ----------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def c2(gpu, oracle):
+    M, O = gpu, oracle
+    ms = M.FixedMultiIndexSet(8, 4)
+    comp = M.CreateComponent(ms, opts(M))
+    s, d, o = O.total_order(8, 4)
+    oc = O.OracleComponent(8, s, d, o)
+    coef = np.random.default_rng(0).normal(0.0, 0.05, comp.numCoeffs)
+    x = np.random.default_rng(1).standard_normal((8, 3000))
+    comp.SetCoeffs(coef)
+    return M, O, comp, oc, coef, x
+
+
+def test_c2_forward(c2):
+    M, O, comp, oc, coef, x = c2
+    assert comp.numCoeffs == 495
+    assert_parity(H(comp.Evaluate(T(x)))[0], oc.evaluate(coef, x), what="C2 Evaluate")
+    assert_parity(H(comp.LogDeterminant(T(x))), oc.logdet(coef, x), what="C2 LogDeterminant")
+
+
+def test_c2_dense_and_reduced_adjoint(c2):
+    import torch
+    M, O, comp, oc, coef, x = c2
+    xs = x[:, :600]
+    sens = np.random.default_rng(5).standard_normal((1, xs.shape[1]))
+    dense = H(comp.CoeffGrad(T(xs), T(sens)))
+    ref = oc.coeff_grad(coef, xs, sens[0])
+    assert_parity(dense, ref, what="C2 CoeffGrad dense")
+    ldense = H(comp.LogDeterminantCoeffGrad(T(xs)))
+    lref = oc.logdet_coeff_grad(coef, xs)
+    assert_parity(ldense, lref, what="C2 LogDeterminantCoeffGrad dense")
+    cg = torch.zeros(comp.numCoeffs, dtype=torch.float64, device="cuda")
+    comp.FusedForwardAdjointImpl(T(xs), sens=T(sens), logdet_sens_scale=1.0, coeff_grad=cg)
+    assert_parity(H(cg), ref.sum(axis=1) + lref.sum(axis=1), floor=1e-3, what="C2 fused reduced")
+
+
+def test_c2_central_differences(c2):
+    """Coefficient gradient of sum(sens*T) against central differences (h = 1e-6)."""
+    import torch
+    M, O, comp, oc, coef, x = c2
+    xs = x[:, :400]
+    sens = np.random.default_rng(6).standard_normal((1, xs.shape[1]))
+    cg = torch.zeros(comp.numCoeffs, dtype=torch.float64, device="cuda")
+    comp.FusedForwardAdjointImpl(T(xs), sens=T(sens), coeff_grad=cg)
+    cg = H(cg)
+    h = 1e-6
+    for j in [0, 1, 7, 100, 250, 494]:
+        cp, cm = coef.copy(), coef.copy()
+        cp[j] += h
+        cm[j] -= h
+        comp.SetCoeffs(cp)
+        fp = (H(comp.Evaluate(T(xs)))[0] * sens[0]).sum()
+        comp.SetCoeffs(cm)
+        fm = (H(comp.Evaluate(T(xs)))[0] * sens[0]).sum()
+        assert cg[j] == pytest.approx((fp - fm) / (2 * h), rel=1e-5, abs=1e-6)
+    comp.SetCoeffs(coef)
+
+
+# ----------------------------------------------------------------------------
+# C3 (reduced size): Hermite functions + Exp, tol 1e-7, banana samples.
+# ----------------------------------------------------------------------------
+def banana(n, seed):
+    rng = np.random.default_rng(seed)
+    x1 = rng.standard_normal(n)
+    x2 = x1 ** 2 + 0.5 * rng.standard_normal(n)
+    xs = [x1, x2]
+    for _ in range(4):
+        xs.append(0.8 * xs[-1] + 0.6 * rng.standard_normal(n))
+    return np.stack(xs)
+
+
+def test_c3_hermite_functions_exp(gpu, oracle):
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(4, 4, 5, opts(M, basis=2, pos=0, tol=1e-7))
+    om = oracle_tri(O, 4, 4, 5, basis=2, pos=0, tol=1e-7)
+    coef = np.random.default_rng(3).normal(0.0, 0.02, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    x = banana(800, 11)[:4]
+    assert_parity(H(tm.Evaluate(T(x))), om.evaluate(coef, x), what="HF Evaluate")
+    assert_parity(H(tm.LogDeterminant(T(x))), om.logdet(coef, x), what="HF LogDeterminant")
+    loss, grad = tm.KLObjective(T(x))
+    cs = om.split(coef)
+    for i, c in enumerate(om.comps):
+        l, g = O.fast_gaussian_reverse_kl(c, cs[i], x[:c.input_dim])
+        assert_parity(H(loss)[i:i + 1], [l], what=f"HF KL loss {i}")
+        assert_parity(H(grad)[om.offsets[i]:om.offsets[i + 1]], g, floor=1e-3, what=f"HF KL grad {i}")
+    sens = np.random.default_rng(4).standard_normal((4, 300))
+    assert_parity(H(tm.Gradient(T(x[:, :300]), T(sens))), om.gradient(coef, x[:, :300], sens), what="HF Gradient")
+
+
+# ----------------------------------------------------------------------------
+# C5 (reduced size): 16-D triangular map, total order 3, tol 1e-8, inverse to xtol 1e-10.
+# ----------------------------------------------------------------------------
+def test_c5_inverse_small(gpu, oracle):
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(16, 16, 3, opts(M, tol=1e-8))
+    om = oracle_tri(O, 16, 16, 3, tol=1e-8)
+    coef = np.random.default_rng(0).normal(0.0, 0.03, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    r = np.random.default_rng(1).standard_normal((16, 150))
+    xi = H(tm.Inverse(T(np.zeros((0, 150))), T(r), xtol=1e-10, ytol=1e-10))
+    ref = om.inverse(coef, np.zeros((0, 150)), r, xtol=1e-10, ytol=1e-10)
+    assert np.max(np.abs(xi - ref)) <= 1e-8, np.max(np.abs(xi - ref))
+    back = H(tm.Evaluate(T(xi)))
+    assert np.max(np.abs(back - r)) < 1e-8
+
+
+# ----------------------------------------------------------------------------
+# Edge cases and error behaviour.
+# ----------------------------------------------------------------------------
+def test_empty_and_shape_errors(c1):
+    import torch
+    M, O, tm, om, coef, x = c1
+    e = torch.zeros(2, 0, dtype=torch.float64, device="cuda")
+    tm.EvaluateImpl(e, torch.zeros(2, 0, dtype=torch.float64, device="cuda"))
+    with pytest.raises(ValueError):
+        tm.EvaluateImpl(T(x[:, :10]), torch.zeros(3, 10, dtype=torch.float64, device="cuda"))
+    with pytest.raises(ValueError):
+        tm.SetCoeffs(np.zeros(tm.numCoeffs + 1))
+
+
+def test_nan_points_and_overflow(gpu, oracle):
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(1, 1, 1, opts(M, pos=0))
+    tm.SetCoeffs(np.array([0.0, 1.0]))
+    r = np.array([[0.5, float("nan")]])
+    xi = H(tm.Inverse(T(np.zeros((0, 2))), T(r)))
+    assert math.isfinite(xi[0, 0]) and math.isnan(xi[0, 1])
+    y = H(tm.Evaluate(T(np.array([[0.3, float("nan")]]))))
+    assert math.isfinite(y[0, 0]) and math.isnan(y[0, 1])
+    tm.SetCoeffs(np.array([0.0, 800.0]))
+    with pytest.raises(M.IntegrandError):
+        tm.Evaluate(T(np.array([[1.0]])))
+    tm.SetCoeffs(np.array([0.0, 1.0]))
+    tm.Evaluate(T(np.array([[1.0]])))  # status cleared, usable again
+
+
+def test_component_reuse_and_wrap(gpu, oracle):
+    import torch
+    M, O = gpu, oracle
+    c0 = M.CreateComponent(M.FixedMultiIndexSet(1, 2), opts(M))
+    c1 = M.CreateComponent(M.FixedMultiIndexSet(2, 2), opts(M))
+    c0.SetCoeffs(np.array([0.1, 0.2, 0.3]))
+    c1.SetCoeffs(np.linspace(-0.2, 0.2, 6))
+    tm = M.TriangularMap([c0, c1], moveCoeffs=True)
+    assert tm.numCoeffs == 9
+    np.testing.assert_allclose(tm.CoeffMap(), np.r_[[0.1, 0.2, 0.3], np.linspace(-0.2, 0.2, 6)])
+    x = np.random.default_rng(2).standard_normal((2, 64))
+    y = H(tm.Evaluate(T(x)))
+    np.testing.assert_array_equal(y[0], H(c0.Evaluate(T(x[:1])))[0])
+    np.testing.assert_array_equal(y[1], H(c1.Evaluate(T(x)))[0])
+    w = torch.tensor(tm.CoeffMap() * 2.0, dtype=torch.float64, device="cuda")
+    tm.WrapCoeffs(w)
+    y2 = H(tm.Evaluate(T(x)))
+    assert not np.allclose(y2, y)
+    w.copy_(torch.tensor(tm.CoeffMap() / 2.0, device="cuda"))
+    np.testing.assert_array_equal(H(tm.Evaluate(T(x))), y)
+
+
+def test_torch_autograd(gpu, oracle):
+    import torch
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(2, 2, 3, opts(M))
+    om = oracle_tri(O, 2, 2, 3)
+    coef = np.random.default_rng(0).normal(0.0, 0.1, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    mod = tm.torch(store_coeffs=True, return_logdet=True)
+    x = torch.tensor(np.random.default_rng(1).standard_normal((50, 2)), dtype=torch.float64, device="cuda",
+                     requires_grad=True)
+    y, ld = mod(x)
+    loss = (y ** 2).sum() + ld.sum()
+    loss.backward()
+    xn = H(x).T
+    yr = om.evaluate(coef, xn)
+    sens = 2 * yr
+    ref_c = om.coeff_grad(coef, xn, sens).sum(axis=1) + om.logdet_coeff_grad(coef, xn).sum(axis=1)
+    assert_parity(H(mod.coeffs.grad), ref_c, floor=1e-3, what="autograd coeff grad")
+    ref_x = om.gradient(coef, xn, sens) + om.logdet_input_grad(coef, xn)
+    assert_parity(H(x.grad).T, ref_x, what="autograd input grad")

@@ -1,0 +1,51 @@
+"""Host-side logic that needs no GPU: multi-index sets, options, array views."""
+import numpy as np
+import pytest
+
+import mpart_gb300 as M
+
+
+def test_total_order_matches_oracle(oracle):
+    for dim, order in [(1, 3), (2, 3), (3, 2), (8, 4), (6, 5)]:
+        ms = M.FixedMultiIndexSet(dim, order)
+        s, d, o = oracle.total_order(dim, order)
+        np.testing.assert_array_equal(ms.nzStarts, s)
+        np.testing.assert_array_equal(ms.nzDims, d)
+        np.testing.assert_array_equal(ms.nzOrders, o)
+    assert M.FixedMultiIndexSet(8, 4).Size() == 495
+    assert M.FixedMultiIndexSet(16, 3).Size() == 969
+
+
+def test_from_multis_round_trip():
+    multis = np.array([[0, 0], [0, 1], [2, 0]])
+    ms = M.FixedMultiIndexSet.from_multis(multis)
+    assert ms.Size() == 3
+    for i in range(3):
+        np.testing.assert_array_equal(ms.IndexToMulti(i), multis[i])
+
+
+def test_map_options_defaults():
+    o = M.MapOptions()
+    assert o.quadType == M.QuadTypes.AdaptiveSimpson and o.quadMaxSub == 30 and o.basisNorm
+    o = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=1e-8)
+    c = o._c()
+    assert c.quad_type == 2 and c.quad_abs_tol == 1e-8
+    with pytest.raises(AttributeError):
+        M.MapOptions(nonsense=1)
+
+
+def test_matrix_views():
+    from mpart_gb300 import _mat
+    a = np.arange(12.0).reshape(3, 4)
+    m = _mat(a)
+    assert (m.rows, m.cols, m.row_stride, m.col_stride) == (3, 4, 4, 1)
+    m = _mat(a.T)
+    assert (m.rows, m.cols, m.row_stride, m.col_stride) == (4, 3, 1, 4)
+    m = _mat(a[1])
+    assert (m.rows, m.cols, m.col_stride) == (1, 4, 1)
+    import torch
+    t = torch.zeros(5, 7, dtype=torch.float64)[:, ::2]
+    m = _mat(t)
+    assert (m.rows, m.cols, m.row_stride, m.col_stride) == (5, 4, 7, 2)
+    with pytest.raises(ValueError):
+        _mat(torch.zeros(3, dtype=torch.float32))
