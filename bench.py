@@ -260,6 +260,12 @@ def run_gpu(args):
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
+    if args.profile:
+        # Profiling mode (for ncu): the fused step only, no e2e / baselines.
+        for _ in range(args.steps):
+            step()
+        torch.cuda.synchronize()
+        return
     if world > 1:
         dist.barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -340,12 +346,39 @@ def run_gpu(args):
                      "flops_per_point": fpp, "evals_per_point": E},
         "clocks": clk.summary(),
     }
+    line["plain_path"] = plain_path(M, coef, x, s, N, dev)
+    line["plain_path"]["fused_speedup"] = line["plain_path"]["ms_per_step"] / (t_step * 1e3)
     line["cpu_baseline"] = cpu_baseline()
     # launches per step: gather + fused + per-component reduction
     line["gpu_launches"] = 3 * args.steps
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def plain_path(M, coef, x, s, N, dev):
+    """The reference-structured GPU path (separate Evaluate, LogDeterminant,
+    CoeffGrad and LogDeterminantCoeffGrad launches with full-width quadrature
+    and dense outputs, then column sums) on the same inputs."""
+    import torch
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=TOL, quadRelTol=TOL,
+                        quadMaxSub=MAXSUB)
+    p = M.PlainComponent(DIM, ORDER, opts)
+    c = torch.as_tensor(coef, device=dev)
+    sv = s[0].contiguous()
+    ev = torch.zeros(N, dtype=torch.float64, device=dev)
+    ld = torch.zeros(N, dtype=torch.float64, device=dev)
+    cg = torch.zeros(p.numCoeffs, dtype=torch.float64, device=dev)
+    p.FwdAdj(c, x, sv, ev, ld, cg)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    p.FwdAdj(c, x, sv, ev, ld, cg)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    del p
+    return {"points_per_s": N / (ms * 1e-3), "ms_per_step": ms}
 
 
 def main():
@@ -355,6 +388,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--points", type=int, default=NPTS)
+    ap.add_argument("--profile", action="store_true", help="fused step only (for profilers)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

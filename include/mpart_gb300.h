@@ -171,6 +171,23 @@ int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad
  * kernel time in milliseconds (CUDA events on the stream). */
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms);
 
+/* ------------------------------------------------------------------------
+ * Reference-structured ("plain") GPU path, the comparator of the fused path:
+ * the reference's own structure (MParT/MonotoneComponent.h:255-299, :487-531,
+ * :684-741, :824-874) on the device -- per-node term loops over all terms,
+ * quadrature of the full numTerms+1 vector with a global per-thread
+ * workspace, dense numTerms x N outputs and one launch per operation.
+ * One total-order component; device pointers; points are dim x N row-major.
+ * ------------------------------------------------------------------------ */
+typedef struct mpgb_plain mpgb_plain;
+int mpgb_plain_create(unsigned int dim, unsigned int order, const mpgb_map_options* opts, mpgb_plain** out);
+int mpgb_plain_destroy(mpgb_plain* plain);
+int mpgb_plain_num_terms(const mpgb_plain* plain, unsigned int* n);
+/* Evaluate, LogDeterminant, CoeffGrad(sens) and LogDeterminantCoeffGrad as
+ * separate launches; coeff_grad receives the column sums of both dense outputs. */
+int mpgb_plain_fwd_adj(mpgb_plain* plain, const double* coeffs, const double* pts, long long n_pts,
+                       const double* sens, double* out_eval, double* out_logdet, double* coeff_grad, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -362,6 +362,33 @@ def CreateTriangular(inputDim: int, outputDim: int, totalOrder: int, opts: MapOp
     return TriangularMap(_handle=h)
 
 
+class PlainComponent:
+    """Reference-structured GPU comparator (see include/mpart_gb300.h): one
+    total-order component evaluated with the reference's per-node term loops
+    and full-width quadrature, as separate launches."""
+
+    def __init__(self, dim: int, order: int, opts: MapOptions | None = None):
+        o = (opts or MapOptions())._c()
+        h = C.c_void_p()
+        check(load().mpgb_plain_create(int(dim), int(order), C.byref(o), C.byref(h)))
+        self._h = h
+        n = C.c_uint()
+        check(load().mpgb_plain_num_terms(h, C.byref(n)))
+        self.numCoeffs = n.value
+        self.dim = int(dim)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.mpgb_plain_destroy(self._h)
+            self._h = None
+
+    def FwdAdj(self, coeffs, pts, sens, out_eval=None, out_logdet=None, coeff_grad=None):
+        """All arrays are contiguous CUDA float64 tensors; pts is dim x N."""
+        n = pts.shape[1]
+        check(load().mpgb_plain_fwd_adj(self._h, _ptr(coeffs), _ptr(pts), n, _ptr(sens), _ptr(out_eval),
+                                        _ptr(out_logdet), _ptr(coeff_grad), _stream_of(pts)))
+
+
 def fp64_probe(blocks=152 * 8, threads=256, iters=4096):
     """DFMA throughput probe; returns (TFLOP/s, ms)."""
     ms = C.c_float(0)

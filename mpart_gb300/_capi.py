@@ -76,6 +76,11 @@ SIGNATURES = {
                                      mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_kl_objective": (C.c_int, [_MAP, mpgb_matrix, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "mpgb_plain_create": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_plain_destroy": (C.c_int, [_MAP]),
+    "mpgb_plain_num_terms": (C.c_int, [_MAP, _UP]),
+    "mpgb_plain_fwd_adj": (C.c_int, [_MAP, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

@@ -1,0 +1,123 @@
+"""Committed golden fixtures (tests/golden/*.npz, made by make_golden.py from
+the oracle).  On CPU the oracle must reproduce them on this machine (a pin
+against drift across compilers and platforms); on the GPU the kernels must
+match them within the parity tolerance of test_gpu_parity.py."""
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, f"{name}.npz")))
+
+
+def close(a, b, rtol, floor=1e-6, what=""):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, what
+    scale = np.nanmax(np.abs(b)) if np.isfinite(b).any() else 1.0
+    ok = (a == b) | (np.isnan(a) & np.isnan(b)) | (np.abs(a - b) <= rtol * np.maximum(np.abs(b), floor * scale))
+    assert ok.all(), f"{what}: {np.count_nonzero(~ok)} entries differ, max |diff| {np.nanmax(np.abs(a - b))}"
+
+
+# ---------------------------------------------------------------- CPU pins
+def test_oracle_reproduces_c1(oracle):
+    g = load("c1")
+    tm = oracle.OracleTriangularMap(2, 2, 3)
+    c, x = g["coef"], g["x"]
+    close(tm.evaluate(c, x), g["evaluate"], 1e-12, what="c1 evaluate")
+    close(tm.logdet(c, x), g["logdet"], 1e-12, what="c1 logdet")
+    close(tm.coeff_grad(c, x, g["sens"]), g["coeff_grad"], 1e-12, what="c1 coeff_grad")
+    close(tm.gradient(c, x, g["sens"]), g["gradient"], 1e-12, what="c1 gradient")
+    close(tm.inverse(c, np.zeros((0, x.shape[1])), g["evaluate"]), g["inverse_cold"], 1e-9, what="c1 inverse")
+
+
+def test_oracle_reproduces_c2(oracle):
+    g = load("c2")
+    s, d, o = oracle.total_order(8, 4)
+    comp = oracle.OracleComponent(8, s, d, o)
+    ev, nev, _ = comp.evaluate(g["coef"], g["x"], return_evals=True)
+    close(ev, g["evaluate"], 1e-12, what="c2 evaluate")
+    np.testing.assert_array_equal(nev, g["nevals"])
+
+
+# ---------------------------------------------------------------- GPU parity
+def _t(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def _h(t):
+    return t.detach().cpu().numpy()
+
+
+def _opts(M, basis=0, pos=1, tol=1e-6):
+    return M.MapOptions(basisType=M.BasisTypes(basis), posFuncType=M.PosFuncTypes(pos),
+                        quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=tol, quadRelTol=tol)
+
+
+@pytest.mark.gpu
+def test_gpu_matches_golden_c1(gpu):
+    M = gpu
+    g = load("c1")
+    tm = M.CreateTriangular(2, 2, 3, _opts(M))
+    tm.SetCoeffs(g["coef"])
+    x = _t(g["x"])
+    close(_h(tm.Evaluate(x)), g["evaluate"], 1e-10, what="evaluate")
+    close(_h(tm.LogDeterminant(x)), g["logdet"], 1e-10, what="logdet")
+    close(_h(tm.CoeffGrad(x, _t(g["sens"]))), g["coeff_grad"], 1e-10, what="coeff_grad")
+    close(_h(tm.LogDeterminantCoeffGrad(x)), g["logdet_coeff_grad"], 1e-10, what="logdet_coeff_grad")
+    close(_h(tm.Gradient(x, _t(g["sens"]))), g["gradient"], 1e-10, what="gradient")
+    close(_h(tm.LogDeterminantInputGrad(x)), g["logdet_input_grad"], 1e-10, what="logdet_input_grad")
+    n = g["x"].shape[1]
+    xi = _h(tm.Inverse(x, _t(g["evaluate"])))
+    assert np.max(np.abs(xi - g["inverse_warm"])) <= 2e-6
+    xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(g["evaluate"])))
+    assert np.max(np.abs(xi - g["inverse_cold"])) <= 2e-6
+    loss, grad = tm.KLObjective(x)
+    close(_h(loss), g["kl_loss"], 1e-10, what="kl loss")
+    close(_h(grad), g["kl_grad"], 1e-10, floor=1e-3, what="kl grad")
+
+
+@pytest.mark.gpu
+def test_gpu_matches_golden_c2(gpu):
+    import torch
+    M = gpu
+    g = load("c2")
+    comp = M.CreateComponent(M.FixedMultiIndexSet(8, 4), _opts(M))
+    comp.SetCoeffs(g["coef"])
+    x = _t(g["x"])
+    close(_h(comp.Evaluate(x))[0], g["evaluate"], 1e-10, what="c2 evaluate")
+    close(_h(comp.LogDeterminant(x)), g["logdet"], 1e-10, what="c2 logdet")
+    cg = torch.zeros(comp.numCoeffs, dtype=torch.float64, device="cuda")
+    comp.FusedForwardAdjointImpl(x, sens=_t(g["sens"][None, :]), logdet_sens_scale=1.0, coeff_grad=cg)
+    close(_h(cg), g["coeff_grad_sum"] + g["logdet_coeff_grad_sum"], 1e-10, floor=1e-3, what="c2 adjoint")
+
+
+@pytest.mark.gpu
+def test_gpu_matches_golden_c3(gpu):
+    M = gpu
+    g = load("c3")
+    tm = M.CreateTriangular(6, 6, 5, _opts(M, basis=2, pos=0, tol=1e-7))
+    tm.SetCoeffs(g["coef"])
+    x = _t(g["x"])
+    close(_h(tm.Evaluate(x)), g["evaluate"], 1e-10, what="c3 evaluate")
+    close(_h(tm.LogDeterminant(x)), g["logdet"], 1e-10, what="c3 logdet")
+    loss, grad = tm.KLObjective(x)
+    close(_h(loss), g["kl_loss"], 1e-10, what="c3 kl loss")
+    close(_h(grad), g["kl_grad"], 1e-10, floor=1e-3, what="c3 kl grad")
+
+
+@pytest.mark.gpu
+def test_gpu_matches_golden_c5(gpu):
+    M = gpu
+    g = load("c5")
+    tm = M.CreateTriangular(16, 16, 3, _opts(M, tol=1e-8))
+    tm.SetCoeffs(g["coef"])
+    n = g["r"].shape[1]
+    xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(g["r"]), xtol=1e-10, ytol=1e-10))
+    assert np.max(np.abs(xi - g["inverse"])) <= 1e-8
