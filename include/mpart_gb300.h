@@ -124,6 +124,12 @@ int mpgb_coeffs_device_ptr(const mpgb_map* map, double** out);
 /* 1 = asynchronous calls (no synchronisation or status check inside calls). */
 int mpgb_set_async(mpgb_map* map, int async);
 
+/* 1 (default) = points are processed grouped by |x_D| of each component's last
+ * input (a stable counting sort on the device) so that warps hold points of
+ * similar quadrature cost; 0 = in input order.  Results differ only by
+ * summation order. */
+int mpgb_set_point_ordering(mpgb_map* map, int on);
+
 /* Synchronise the stream, return and clear the status bits of the last calls. */
 int mpgb_check_status(mpgb_map* map, void* stream, int* status);
 
@@ -166,6 +172,46 @@ int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_ma
  * for every component of the map at once.  loss (outputDim doubles) and grad
  * (numCoeffs doubles) may be device or host pointers. */
 int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad, void* stream);
+
+/* Training options: limited-memory BFGS per component (NLopt's LD_LBFGS is
+ * not available; the stopping fields follow TrainOptions, MParT/TrainMap.h:19-58,
+ * with 0 disabling a criterion).  mode 0: one batched launch set per step,
+ * replayed from a CUDA graph; 1: batched, direct launches; 2: one launch set
+ * per component (unbatched). */
+typedef struct mpgb_train_options {
+    int max_iters;
+    int max_evals;
+    double ftol_rel;
+    double ftol_abs;
+    double xtol_rel;
+    double xtol_abs;
+    double gtol;
+    int memory;
+    int mode;
+} mpgb_train_options;
+
+typedef struct mpgb_train_result {
+    double total_loss;  /* sum of the component objectives (TrainMap's return value) */
+    int iterations;     /* largest number of accepted iterations over the components */
+    int evaluations;    /* largest number of objective evaluations over the components */
+    int steps;          /* batched objective evaluations performed */
+    double ms_per_step; /* device time per step (CUDA events) */
+    double total_ms;    /* wall time of the training loop */
+} mpgb_train_result;
+
+int mpgb_train_options_default(mpgb_train_options* opts);
+
+/* TrainMap with a standard-normal KLObjective on a triangular map
+ * (src/TrainMap.cpp:144-216): every component minimises its
+ * FastGaussianReverseKLObjective.  samples is inputDim x N on the device;
+ * loss_per_comp (host, outputDim) receives the final objectives; the map's
+ * coefficients are set to the result. */
+int mpgb_train_map(mpgb_map* map, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
+                   mpgb_train_result* result, void* stream);
+
+/* Device time of one KL objective + gradient step of all components in the given mode (see
+ * mpgb_train_options.mode), averaged over `steps` steps after three warm-up steps. */
+int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream);
 
 /* FP64 throughput probe: DFMA chains over blocks x threads x iters x 8; writes the
  * kernel time in milliseconds (CUDA events on the stream). */

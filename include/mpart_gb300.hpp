@@ -169,8 +169,13 @@ public:
     // loss_c = mean(0.5 T_c^2 - logdet_c) and its coefficient gradient.
     // lossPerComp (device, outputDim) and grad (device, numCoeffs) are written.
     void KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream = 0);
+    // Same for one component only (onlyComp >= 0), or all (onlyComp = -1).
+    void KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, int onlyComp, cudaStream_t stream);
 
     int CheckStatus(cudaStream_t stream = 0);  // synchronise, read and clear the status word
+    // Process points grouped by |x_D| (default on); results do not depend on it
+    // beyond summation order.
+    void SetPointOrdering(bool on);
     // Grow-only device buffer `slot` (0..7) of at least `bytes`, for host staging.
     double* StagingBuffer(int slot, size_t bytes, cudaStream_t stream);
     MapOptions const& Options() const { return opts_; }

@@ -229,6 +229,10 @@ class ConditionalMapBase:
         check(load().mpgb_get_coeffs(self._h, C.c_void_p(out.ctypes.data), out.size))
         return out
 
+    def SetPointOrdering(self, flag: bool):
+        """Group points by |x_D| before the quadrature-bearing kernels (default on)."""
+        check(load().mpgb_set_point_ordering(self._h, int(bool(flag))))
+
     def SetAsync(self, flag: bool):
         check(load().mpgb_set_async(self._h, int(bool(flag))))
 
@@ -360,6 +364,33 @@ def CreateTriangular(inputDim: int, outputDim: int, totalOrder: int, opts: MapOp
     h = C.c_void_p()
     check(load().mpgb_create_triangular(int(inputDim), int(outputDim), int(totalOrder), C.byref(o), C.byref(h)))
     return TriangularMap(_handle=h)
+
+
+def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, ftol_rel=0.0, ftol_abs=0.0,
+             xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0):
+    """TrainMap with a standard-normal KL objective (src/TrainMap.cpp:166-216):
+    every component minimises its reverse KL with L-BFGS; samples is a CUDA
+    float64 tensor, inputDim x N.  mode 0 replays one batched step from a CUDA
+    graph, 1 launches it directly, 2 launches each component separately.
+    Returns (final loss per component, result dict); the map keeps the result."""
+    from ._capi import mpgb_train_options, mpgb_train_result
+    o = mpgb_train_options()
+    check(load().mpgb_train_options_default(C.byref(o)))
+    o.max_iters, o.max_evals, o.memory, o.mode = int(max_iters), int(max_evals), int(memory), int(mode)
+    o.ftol_rel, o.ftol_abs, o.xtol_rel, o.xtol_abs, o.gtol = ftol_rel, ftol_abs, xtol_rel, xtol_abs, gtol
+    loss = np.zeros(tmap.outputDim)
+    r = mpgb_train_result()
+    check(load().mpgb_train_map(tmap._h, _mat(samples), C.byref(o), C.c_void_p(loss.ctypes.data), C.byref(r),
+                                _stream_of(samples)))
+    return loss, {"total_loss": r.total_loss, "iterations": r.iterations, "evaluations": r.evaluations,
+                  "steps": r.steps, "ms_per_step": r.ms_per_step, "total_ms": r.total_ms}
+
+
+def KLStepTime(tmap: ConditionalMapBase, samples, mode=0, steps=10):
+    """Device milliseconds of one KL objective + gradient step (see TrainMap modes)."""
+    ms = C.c_double(0)
+    check(load().mpgb_kl_step_time(tmap._h, _mat(samples), int(mode), int(steps), C.byref(ms), _stream_of(samples)))
+    return ms.value
 
 
 class PlainComponent:

@@ -42,6 +42,17 @@ class mpgb_matrix(C.Structure):
     ]
 
 
+class mpgb_train_options(C.Structure):
+    _fields_ = [("max_iters", C.c_int), ("max_evals", C.c_int), ("ftol_rel", C.c_double), ("ftol_abs", C.c_double),
+                ("xtol_rel", C.c_double), ("xtol_abs", C.c_double), ("gtol", C.c_double), ("memory", C.c_int),
+                ("mode", C.c_int)]
+
+
+class mpgb_train_result(C.Structure):
+    _fields_ = [("total_loss", C.c_double), ("iterations", C.c_int), ("evaluations", C.c_int), ("steps", C.c_int),
+                ("ms_per_step", C.c_double), ("total_ms", C.c_double)]
+
+
 # Every symbol the header declares, with its signature.
 _MAP = C.c_void_p
 _MAPP = C.POINTER(C.c_void_p)
@@ -63,6 +74,7 @@ SIGNATURES = {
     "mpgb_get_coeffs": (C.c_int, [_MAP, C.c_void_p, C.c_uint]),
     "mpgb_coeffs_device_ptr": (C.c_int, [_MAP, C.POINTER(C.c_void_p)]),
     "mpgb_set_async": (C.c_int, [_MAP, C.c_int]),
+    "mpgb_set_point_ordering": (C.c_int, [_MAP, C.c_int]),
     "mpgb_check_status": (C.c_int, [_MAP, C.c_void_p, C.POINTER(C.c_int)]),
     "mpgb_evaluate": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
     "mpgb_log_determinant": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
@@ -76,6 +88,10 @@ SIGNATURES = {
                                      mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_kl_objective": (C.c_int, [_MAP, mpgb_matrix, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "mpgb_train_options_default": (C.c_int, [C.POINTER(mpgb_train_options)]),
+    "mpgb_train_map": (C.c_int, [_MAP, mpgb_matrix, C.POINTER(mpgb_train_options), C.c_void_p,
+                                 C.POINTER(mpgb_train_result), C.c_void_p]),
+    "mpgb_kl_step_time": (C.c_int, [_MAP, mpgb_matrix, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
     "mpgb_plain_create": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
     "mpgb_plain_destroy": (C.c_int, [_MAP]),
     "mpgb_plain_num_terms": (C.c_int, [_MAP, _UP]),

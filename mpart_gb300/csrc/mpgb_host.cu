@@ -304,6 +304,18 @@ struct GatherDescHost {
     int nSlots;
 };
 
+// Launch tables of a KL step, cached per (N, component subset) so that a
+// step issues only kernel launches (capturable in a CUDA graph).
+struct KLPlan {
+    long long N = -1;
+    int onlyComp = -2;
+    int nItems = 0;
+    std::vector<std::vector<int>> itemsOf;
+    std::vector<int> rowOff;  // first row of each component in rowBase/lossSlots
+    DevBuf items, rowBase, lossSlots;
+    size_t partialDoubles = 0;
+};
+
 struct MapWorkspace {
     DevBuf comps, cm, gather, items, partials, rowBase, lossPart, lossSlots, logdetRows, status;
     DevBuf stage[8];
@@ -315,6 +327,9 @@ struct MapWorkspace {
     BasisConsts bc{};
     int pmax = 1, dmax = 1, nBmax = 0, depthMax = 0;
     bool built = false;
+    std::vector<std::unique_ptr<KLPlan>> klPlans;
+    DevBuf perm, sortHist;
+    bool ordering = true;
 };
 
 }  // namespace mpgb
@@ -567,6 +582,8 @@ void MonotoneMapBase::Finish(cudaStream_t stream, const char* fn) {
     }
 }
 
+void MonotoneMapBase::SetPointOrdering(bool on) { ws_->ordering = on; }
+
 double* MonotoneMapBase::StagingBuffer(int slot, size_t bytes, cudaStream_t stream) {
     if (slot < 0 || slot >= 8) throw std::invalid_argument("StagingBuffer: slot out of range.");
     ws_->stage[slot].ensure(bytes, stream);
@@ -638,27 +655,26 @@ static std::vector<WorkItem> itemsAllComps(long long N, int nComps) {
 }
 
 // Items of style "one component, a range of tiles".  Heavier components first.
+// With reduced outputs each component is cut into at most 4 items per SM,
+// independently of the other components of the launch, so a batched launch
+// and per-component launches produce the same partial rows.
 static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Part>& parts, long long N, int numSMs,
                                           bool reduced, std::vector<long long>* rowBaseOut,
-                                          std::vector<std::vector<int>>* itemsOfComp) {
+                                          std::vector<std::vector<int>>* itemsOfComp, int onlyComp = -1) {
     const int nComps = (int)parts.size();
     const long long nTiles = (N + kTpb - 1) / kTpb;
-    std::vector<int> order(nComps);
-    std::iota(order.begin(), order.end(), 0);
+    std::vector<int> order;
+    for (int c = 0; c < nComps; ++c)
+        if (onlyComp < 0 || c == onlyComp) order.push_back(c);
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return parts[a].prog->weight > parts[b].prog->weight; });
-    double wsum = 0;
-    for (auto& p : parts) wsum += p.prog->weight;
-    const double target = (double)numSMs * 8.0;
     std::vector<WorkItem> v;
     long long base = 0;
     if (itemsOfComp) itemsOfComp->assign(nComps, {});
     for (int c : order) {
         long long tilesPer = 1;
         if (reduced) {
-            double share = std::max(1.0, target * parts[c].prog->weight / wsum);
-            long long nItemsC = std::min<long long>(nTiles, (long long)std::ceil(share));
-            nItemsC = std::max<long long>(1, nItemsC);
+            const long long nItemsC = std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * 4));
             tilesPer = (nTiles + nItemsC - 1) / nItemsC;
         }
         for (long long t = 0; t < nTiles; t += tilesPer) {
@@ -680,6 +696,27 @@ static void uploadItems(MapWorkspace& W, const std::vector<WorkItem>& items, cud
     W.items.ensure(items.size() * sizeof(WorkItem), stream);
     MPGB_CUDA(cudaMemcpyAsync(W.items.p, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice,
                               stream));
+}
+
+// Processing order for per-component launches: each component's points
+// sorted (stably) by |x_D| of its own last coordinate.
+static void orderPoints(MapWorkspace& W, const std::vector<MonotoneMapBase::Part>& parts, StridedMatrix const& pts,
+                        FusedParams& p, int onlyComp, cudaStream_t stream) {
+    p.perm = nullptr;
+    p.permStride = 0;
+    const long long N = pts.cols;
+    if (!W.ordering || N < 2 * kTpb) return;
+    const size_t nComps = parts.size();
+    W.perm.ensure(nComps * (size_t)N * sizeof(int), stream);
+    W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
+    for (size_t c = 0; c < nComps; ++c) {
+        if (onlyComp >= 0 && (int)c != onlyComp) continue;
+        const double* xd = pts.data + (int64_t)(parts[c].prog->D - 1) * pts.rowStride;
+        MPGB_CUDA(launchSortByLast(xd, pts.colStride, N, W.sortHist.as<int>(), W.perm.as<int>() + c * (size_t)N,
+                                   stream));
+    }
+    p.perm = W.perm.as<int>();
+    p.permStride = N;
 }
 
 static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nItems, int needJ, int needE,
@@ -706,6 +743,7 @@ void MonotoneMapBase::EvaluateImpl(StridedMatrix const& pts, StridedMatrix const
     p.flags = kFlagEval;
     p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
     p.outEval = output.data; p.evalRs = output.rowStride; p.evalCs = output.colStride;
+    orderPoints(W, parts_, pts, p, -1, stream);
     launch(W, opts_, p, (int)items.size(), 0, 0, stream);
     Finish(stream, "Evaluate");
 }
@@ -748,6 +786,7 @@ void MonotoneMapBase::CoeffGradImpl(StridedMatrix const& pts, StridedMatrix cons
     p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
     p.sens = sens.data; p.sensRs = sens.rowStride; p.sensCs = sens.colStride;
     p.outDense = output.data; p.denseRs = output.rowStride; p.denseCs = output.colStride;
+    orderPoints(W, parts_, pts, p, -1, stream);
     launch(W, opts_, p, (int)items.size(), 1, 0, stream);
     Finish(stream, "CoeffGrad");
 }
@@ -897,6 +936,7 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
         baseParams(W, opts_, p, N);
         p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
         p.flags = 0;
+        orderPoints(W, parts_, pts, p, -1, stream);
         if (!outEval.empty()) {
             p.flags |= kFlagEval;
             p.outEval = outEval.data; p.evalRs = outEval.rowStride; p.evalCs = outEval.colStride;
@@ -977,22 +1017,59 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
     Finish(stream, "FusedForwardAdjoint");
 }
 
+static KLPlan& klPlan(MapWorkspace& W, const std::vector<MonotoneMapBase::Part>& parts, long long N, int onlyComp,
+                      cudaStream_t stream) {
+    static thread_local int dummy = 0;
+    (void)dummy;
+    for (auto& p : W.klPlans)
+        if (p->N == N && p->onlyComp == onlyComp) return *p;
+    W.klPlans.emplace_back(new KLPlan());
+    KLPlan& P = *W.klPlans.back();
+    P.N = N;
+    P.onlyComp = onlyComp;
+    std::vector<long long> rowBase;
+    auto items = itemsPerComp(parts, N, W.numSMs, true, &rowBase, &P.itemsOf, onlyComp);
+    P.nItems = (int)items.size();
+    for (auto& it : items)
+        P.partialDoubles = std::max<size_t>(P.partialDoubles, (size_t)it.partialBase + parts[it.c0].prog->numTerms);
+    std::vector<long long> rb;
+    std::vector<int> ls;
+    P.rowOff.assign(parts.size() + 1, 0);
+    for (size_t c = 0; c < parts.size(); ++c) {
+        P.rowOff[c] = (int)rb.size();
+        for (int id : P.itemsOf[c]) {
+            rb.push_back(items[id].partialBase);
+            ls.push_back(items[id].lossSlot);
+        }
+    }
+    P.rowOff[parts.size()] = (int)rb.size();
+    P.items.ensure(items.size() * sizeof(WorkItem), stream);
+    P.rowBase.ensure(std::max<size_t>(1, rb.size()) * sizeof(long long), stream);
+    P.lossSlots.ensure(std::max<size_t>(1, ls.size()) * sizeof(int), stream);
+    MPGB_CUDA(cudaMemcpy(P.items.p, items.data(), items.size() * sizeof(WorkItem), cudaMemcpyHostToDevice));
+    if (!rb.empty()) {
+        MPGB_CUDA(cudaMemcpy(P.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice));
+        MPGB_CUDA(cudaMemcpy(P.lossSlots.p, ls.data(), ls.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return P;
+}
+
 void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream) {
+    KLObjective(pts, lossPerComp, grad, -1, stream);
+}
+
+void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, int onlyComp,
+                                  cudaStream_t stream) {
     CheckCoefficients("KLObjective");
     const long long N = pts.cols;
     checkMatrix(pts, inputDim, N, "pts", "KLObjective");
     if (N == 0) throw std::invalid_argument("KLObjective: no samples.");
+    if (onlyComp >= (int)parts_.size()) throw std::out_of_range("KLObjective: component index out of range.");
     Prepare(stream);
     MapWorkspace& W = *ws_;
-    const int nComps = (int)parts_.size();
-    std::vector<long long> rowBase;
-    std::vector<std::vector<int>> itemsOf;
-    auto items = itemsPerComp(parts_, N, W.numSMs, true, &rowBase, &itemsOf);
-    uploadItems(W, items, stream);
-    size_t tot = 1;
-    for (auto& it : items) tot = std::max<size_t>(tot, (size_t)it.partialBase + parts_[it.c0].prog->numTerms);
-    W.partials.ensure(tot * sizeof(double), stream);
-    W.lossPart.ensure(items.size() * sizeof(double), stream);
+    KLPlan& P = klPlan(W, parts_, N, onlyComp, stream);
+    W.partials.ensure(std::max<size_t>(1, P.partialDoubles) * sizeof(double), stream);
+    W.lossPart.ensure(std::max(1, P.nItems) * sizeof(double), stream);
     FusedParams p{};
     baseParams(W, opts_, p, N);
     p.flags = kFlagKL | kFlagCoefReduced;
@@ -1001,26 +1078,18 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     p.lsensScale = -1.0 / (double)N;
     p.partials = W.partials.as<double>();
     p.lossPartials = W.lossPart.as<double>();
-    launch(W, opts_, p, (int)items.size(), 1, 0, stream);
-    std::vector<long long> rb;
-    std::vector<int> ls;
-    for (int c = 0; c < nComps; ++c)
-        for (int id : itemsOf[c]) {
-            rb.push_back(items[id].partialBase);
-            ls.push_back(items[id].lossSlot);
-        }
-    W.rowBase.ensure(rb.size() * sizeof(long long), stream);
-    W.lossSlots.ensure(ls.size() * sizeof(int), stream);
-    MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice, stream));
-    MPGB_CUDA(cudaMemcpyAsync(W.lossSlots.p, ls.data(), ls.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-    size_t off = 0;
-    for (int c = 0; c < nComps; ++c) {
-        const int nr = (int)itemsOf[c].size();
-        MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>() + off, nr,
+    p.items = P.items.as<WorkItem>();
+    orderPoints(W, parts_, pts, p, onlyComp, stream);
+    const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
+    if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
+    MPGB_CUDA(launchFused(basisCode(opts_), posCode(opts_), W.pmax, p, P.nItems, 1, 0, stream));
+    for (int c = 0; c < (int)parts_.size(); ++c) {
+        if (onlyComp >= 0 && c != onlyComp) continue;
+        const int nr = P.rowOff[c + 1] - P.rowOff[c];
+        MPGB_CUDA(launchReduceRows(W.partials.as<double>(), P.rowBase.as<long long>() + P.rowOff[c], nr,
                                    parts_[c].prog->numTerms, 1.0, grad + parts_[c].mapCoeffOffset, 0, stream));
-        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), W.lossSlots.as<int>() + off, nr, 1.0 / (double)N,
+        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), P.lossSlots.as<int>() + P.rowOff[c], nr, 1.0 / (double)N,
                                 lossPerComp + c, stream));
-        off += nr;
     }
     Finish(stream, "KLObjective");
 }
@@ -1167,6 +1236,13 @@ using namespace mpgb;
 struct mpgb_map {
     std::shared_ptr<ConditionalMapBase> obj;
 };
+
+namespace mpgb {
+int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
+                 mpgb_train_result* res, void* stream, char* err, int errLen);
+int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream,
+                   char* err, int errLen);
+}
 
 namespace {
 thread_local std::string g_lastError;
@@ -1426,6 +1502,10 @@ int mpgb_coeffs_device_ptr(const mpgb_map* map, double** out) {
     });
 }
 
+int mpgb_set_point_ordering(mpgb_map* map, int on) {
+    return guard([&] { mono(map)->SetPointOrdering(on != 0); });
+}
+
 int mpgb_set_async(mpgb_map* map, int async) {
     return guard([&] {
         if (!map) throw std::invalid_argument("null map handle");
@@ -1555,6 +1635,38 @@ int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad
         m->KLObjective(P, l, g, s);
         st.finish();
     });
+}
+
+int mpgb_train_options_default(mpgb_train_options* o) {
+    return guard([&] {
+        if (!o) throw std::invalid_argument("null options");
+        std::memset(o, 0, sizeof(*o));
+        o->max_iters = 100;
+        o->max_evals = 1000;
+        o->memory = 10;
+        o->mode = 0;
+    });
+}
+
+int mpgb_train_map(mpgb_map* map, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
+                   mpgb_train_result* result, void* stream) {
+    char err[512] = {0};
+    int rc = MPGB_OK;
+    int g = guard([&] {
+        rc = trainMapImpl(mono(map), samples, opts, loss_per_comp, result, stream, err, sizeof(err));
+    });
+    if (g != MPGB_OK) return g;
+    if (rc != MPGB_OK) g_lastError = err;
+    return rc;
+}
+
+int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream) {
+    char err[512] = {0};
+    int rc = MPGB_OK;
+    int g = guard([&] { rc = klStepTimeImpl(mono(map), samples, mode, steps, ms_per_step, stream, err, sizeof(err)); });
+    if (g != MPGB_OK) return g;
+    if (rc != MPGB_OK) g_lastError = err;
+    return rc;
 }
 
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms) {

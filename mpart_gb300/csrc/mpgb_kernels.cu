@@ -40,6 +40,84 @@ __global__ void reduceRowsKernel(const double* part, const long long* rowBase, i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Stable counting sort of points by |x_D| (256 buckets of width 1/32, NaN and
+// |x_D| >= 8 in the last).  The per-point cost of the adaptive quadrature grows
+// with |x_D|; grouping points of similar cost keeps a warp's lanes busy.
+// Deterministic: bucket-major, original order within a bucket.
+// ---------------------------------------------------------------------------
+constexpr int kSortBuckets = 256;
+constexpr int kSortChunk = 1024;
+
+__device__ __forceinline__ int sortKey(double x) {
+    const double a = fabs(x);
+    if (!(a < 8.0)) return kSortBuckets - 1;
+    return (int)(a * 32.0);
+}
+
+__global__ void keyHistKernel(const double* xd, long long stride, long long N, int* hist) {
+    __shared__ int h[kSortBuckets];
+    for (int t = threadIdx.x; t < kSortBuckets; t += blockDim.x) h[t] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * kSortChunk;
+    for (int j = threadIdx.x; j < kSortChunk; j += blockDim.x) {
+        const long long i = base + j;
+        if (i < N) atomicAdd(&h[sortKey(xd[i * stride])], 1);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kSortBuckets; t += blockDim.x) hist[(long long)blockIdx.x * kSortBuckets + t] = h[t];
+}
+
+// One block of kSortBuckets threads: hist[blk][b] -> first output slot of (blk, b).
+__global__ void keyScanKernel(int* hist, int nBlk) {
+    __shared__ int tot[kSortBuckets];
+    const int b = threadIdx.x;
+    int s = 0;
+    for (int k = 0; k < nBlk; ++k) s += hist[(long long)k * kSortBuckets + b];
+    tot[b] = s;
+    __syncthreads();
+    if (b == 0) {
+        int run = 0;
+        for (int q = 0; q < kSortBuckets; ++q) {
+            const int v = tot[q];
+            tot[q] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int run = tot[b];
+    for (int k = 0; k < nBlk; ++k) {
+        const int v = hist[(long long)k * kSortBuckets + b];
+        hist[(long long)k * kSortBuckets + b] = run;
+        run += v;
+    }
+}
+
+// One warp per chunk, chunk order kept within each bucket.
+__global__ void keyScatterKernel(const double* xd, long long stride, long long N, const int* off, int* perm) {
+    __shared__ int cnt[kSortBuckets];
+    const int lane = threadIdx.x;
+    for (int t = lane; t < kSortBuckets; t += 32) cnt[t] = 0;
+    __syncwarp();
+    const long long base = (long long)blockIdx.x * kSortChunk;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c = 0; c < kSortChunk / 32; ++c) {
+        const long long i = base + c * 32 + lane;
+        const bool active = i < N;
+        const int key = active ? sortKey(xd[i * stride]) : kSortBuckets + lane;
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        const int rank = __popc(grp & lt);
+        int slot = 0;
+        if (active) slot = cnt[key];
+        __syncwarp();
+        if (active) {
+            perm[off[(long long)blockIdx.x * kSortBuckets + key] + slot + rank] = (int)i;
+            if (rank == 0) cnt[key] = slot + __popc(grp);
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void sumLossKernel(const double* lossPart, const int* slots, int n, double scale, double* out) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         double s = 0.0;
@@ -152,6 +230,18 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
 cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
                           cudaStream_t stream) {
     sumLossKernel<<<1, 32, 0, stream>>>(lossPart, slots, n, scale, out);
+    return cudaGetLastError();
+}
+
+size_t sortScratchInts(long long N) { return (size_t)((N + kSortChunk - 1) / kSortChunk) * kSortBuckets; }
+
+cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
+                             cudaStream_t stream) {
+    if (N <= 0) return cudaSuccess;
+    const int nBlk = (int)((N + kSortChunk - 1) / kSortChunk);
+    keyHistKernel<<<nBlk, 256, 0, stream>>>(xd, stride, N, hist);
+    keyScanKernel<<<1, kSortBuckets, 0, stream>>>(hist, nBlk);
+    keyScatterKernel<<<nBlk, 32, 0, stream>>>(xd, stride, N, hist, perm);
     return cudaGetLastError();
 }
 

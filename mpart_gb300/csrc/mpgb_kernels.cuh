@@ -291,8 +291,9 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
     const double ninf = __longlong_as_double(0xfff0000000000000ULL);
 
     for (int tile = item.tile0; tile < item.tile0 + item.nTiles; ++tile) {
-        const long long i = (long long)tile * tpb + tid;
-        const bool active = i < prm.N;
+        const long long slotIdx = (long long)tile * tpb + tid;
+        const bool active = slotIdx < prm.N;
+        const long long i = (active && prm.perm) ? (long long)prm.perm[item.c0 * prm.permStride + slotIdx] : slotIdx;
         int st = 0;
         // Coordinates of the tile (the largest component of the range reads the most).
         const int dneed = prm.comps[item.c1 - 1].D;

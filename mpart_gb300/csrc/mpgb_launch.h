@@ -19,6 +19,10 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
                              double* out, int accumulate, cudaStream_t stream);
 cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
                           cudaStream_t stream);
+// Stable counting sort of points by |x_D|: perm[j] = index of the j-th point.
+size_t sortScratchInts(long long N);
+cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
+                             cudaStream_t stream);
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
 
 }  // namespace mpgb

@@ -1,0 +1,363 @@
+// Map training: standard-normal reverse KL of a triangular map, minimised
+// component by component as TrainMap does for a KLObjective with a
+// standard-normal density (src/TrainMap.cpp:144-164, :166-216).  The
+// reference hands each component to NLopt in turn; here every component's
+// optimiser runs in lockstep and one batched launch (optionally replayed from
+// a CUDA graph) evaluates all of their requests at once.  The optimiser is a
+// limited-memory BFGS (two-loop recursion, Nocedal & Wright Alg. 7.4 / 7.5)
+// with a backtracking Armijo line search; NLopt itself is not available.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <sstream>
+#include <vector>
+
+#include "../../include/mpart_gb300.h"
+#include "../../include/mpart_gb300.hpp"
+
+namespace mpgb {
+
+namespace {
+
+#define TR_CUDA(call)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) throw std::runtime_error(std::string("CUDA error in trainer: ") +      \
+                                                        cudaGetErrorString(e_));                     \
+    } while (0)
+
+struct TrainOpts {
+    int maxIters = 100;
+    int maxEvals = 1000;
+    double ftolRel = 0.0, ftolAbs = 0.0, xtolRel = 0.0, xtolAbs = 0.0, gtol = 0.0;
+    int memory = 10;
+};
+
+// Reverse-communication L-BFGS on one component's coefficients.
+class LBFGS {
+public:
+    enum State { kInit, kLineSearch, kDone };
+    LBFGS(const double* x0, int n, const TrainOpts& o) : n_(n), o_(o), x_(x0, x0 + n), trial_(x0, x0 + n) {}
+
+    // Point the caller must evaluate next (valid unless done()).
+    const std::vector<double>& request() const { return trial_; }
+    bool done() const { return state_ == kDone; }
+    int iterations() const { return iters_; }
+    int evaluations() const { return evals_; }
+    double f() const { return f_; }
+    const std::vector<double>& x() const { return x_; }
+    double gradNorm() const {
+        double s = 0;
+        for (double v : g_) s += v * v;
+        return std::sqrt(s);
+    }
+
+    void tell(double f, const double* g) {
+        ++evals_;
+        if (state_ == kInit) {
+            f_ = f;
+            g_.assign(g, g + n_);
+            if (!std::isfinite(f) || converged0()) { state_ = kDone; return; }
+            newDirection(true);
+            return;
+        }
+        // line search
+        const double gd = dot(gPrevDir_, d_);
+        if (std::isfinite(f) && f <= f_ + 1e-4 * alpha_ * gd) {
+            // accept
+            std::vector<double> s(n_), y(n_);
+            double maxdx = 0, maxrel = 0;
+            for (int i = 0; i < n_; ++i) {
+                s[i] = trial_[i] - x_[i];
+                y[i] = g[i] - g_[i];
+                maxdx = std::max(maxdx, std::fabs(s[i]));
+                if (trial_[i] != 0) maxrel = std::max(maxrel, std::fabs(s[i]) / std::fabs(trial_[i]));
+            }
+            const double sy = dot(s, y);
+            if (sy > 1e-12 * std::sqrt(dot(s, s) * dot(y, y))) {
+                S_.push_back(s);
+                Y_.push_back(y);
+                rho_.push_back(1.0 / sy);
+                if ((int)S_.size() > o_.memory) {
+                    S_.erase(S_.begin());
+                    Y_.erase(Y_.begin());
+                    rho_.erase(rho_.begin());
+                }
+            }
+            const double df = std::fabs(f - f_);
+            x_ = trial_;
+            f_ = f;
+            g_.assign(g, g + n_);
+            ++iters_;
+            if (iters_ >= o_.maxIters || evals_ >= o_.maxEvals || df <= o_.ftolAbs || df <= o_.ftolRel * std::fabs(f) ||
+                maxdx <= o_.xtolAbs || (o_.xtolRel > 0 && maxrel <= o_.xtolRel) || converged0()) {
+                state_ = kDone;
+                trial_ = x_;
+                return;
+            }
+            newDirection(false);
+            return;
+        }
+        // backtrack (quadratic interpolation, safeguarded to [0.1, 0.5] of the step)
+        if (evals_ >= o_.maxEvals || ++backtracks_ > 40) {
+            state_ = kDone;
+            trial_ = x_;
+            return;
+        }
+        double a = alpha_;
+        double an = -gd * a * a / (2.0 * (f - f_ - gd * a));
+        if (!std::isfinite(an)) an = 0.5 * a;
+        an = std::min(std::max(an, 0.1 * a), 0.5 * a);
+        alpha_ = an;
+        for (int i = 0; i < n_; ++i) trial_[i] = x_[i] + alpha_ * d_[i];
+    }
+
+private:
+    static double dot(const std::vector<double>& a, const std::vector<double>& b) {
+        double s = 0;
+        for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+        return s;
+    }
+    bool converged0() const { return o_.gtol > 0 && gradNorm() <= o_.gtol; }
+
+    void newDirection(bool first) {
+        // Two-loop recursion: d = -H g.
+        std::vector<double> q = g_;
+        const int m = (int)S_.size();
+        std::vector<double> a(m);
+        for (int i = m - 1; i >= 0; --i) {
+            a[i] = rho_[i] * dot(S_[i], q);
+            for (int j = 0; j < n_; ++j) q[j] -= a[i] * Y_[i][j];
+        }
+        double gamma = 1.0;
+        if (m > 0) gamma = dot(S_[m - 1], Y_[m - 1]) / dot(Y_[m - 1], Y_[m - 1]);
+        for (int j = 0; j < n_; ++j) q[j] *= gamma;
+        for (int i = 0; i < m; ++i) {
+            const double b = rho_[i] * dot(Y_[i], q);
+            for (int j = 0; j < n_; ++j) q[j] += S_[i][j] * (a[i] - b);
+        }
+        d_.resize(n_);
+        for (int j = 0; j < n_; ++j) d_[j] = -q[j];
+        if (dot(d_, g_) >= 0) {  // not a descent direction: restart from steepest descent
+            S_.clear(); Y_.clear(); rho_.clear();
+            for (int j = 0; j < n_; ++j) d_[j] = -g_[j];
+        }
+        alpha_ = 1.0;
+        if (first || S_.empty()) {
+            double gn = 0;
+            for (double v : g_) gn = std::max(gn, std::fabs(v));
+            alpha_ = gn > 0 ? std::min(1.0, 1.0 / gn) : 1.0;
+        }
+        gPrevDir_ = g_;
+        backtracks_ = 0;
+        for (int i = 0; i < n_; ++i) trial_[i] = x_[i] + alpha_ * d_[i];
+        state_ = kLineSearch;
+    }
+
+    int n_;
+    TrainOpts o_;
+    std::vector<double> x_, trial_, g_, d_, gPrevDir_;
+    double f_ = 0, alpha_ = 1;
+    std::vector<std::vector<double>> S_, Y_;
+    std::vector<double> rho_;
+    State state_ = kInit;
+    int iters_ = 0, evals_ = 0, backtracks_ = 0;
+};
+
+struct Pinned {
+    double* p = nullptr;
+    explicit Pinned(size_t n) { TR_CUDA(cudaMallocHost(&p, std::max<size_t>(1, n) * sizeof(double))); }
+    ~Pinned() { if (p) cudaFreeHost(p); }
+};
+struct Dev {
+    double* p = nullptr;
+    explicit Dev(size_t n) { TR_CUDA(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(double))); }
+    ~Dev() { if (p) cudaFree(p); }
+};
+
+// One KL evaluation of all components: coefficients in, losses and gradients out.
+struct KLStep {
+    MonotoneMapBase& map;
+    StridedMatrix pts;
+    cudaStream_t s;
+    int mode;  // 0 batched (graph), 1 batched (direct launches), 2 one launch set per component
+    double* dCoef;
+    Pinned hCoef, hLoss, hGrad;
+    Dev dLoss, dGrad;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned nc, no;
+
+    KLStep(MonotoneMapBase& m, StridedMatrix const& p, cudaStream_t st, int md)
+        : map(m), pts(p), s(st), mode(md), dCoef(m.Coeffs()), hCoef(m.numCoeffs), hLoss(m.outputDim),
+          hGrad(m.numCoeffs), dLoss(m.outputDim), dGrad(m.numCoeffs), nc(m.numCoeffs), no(m.outputDim) {
+        // Warm-up (builds launch tables, sets kernel attributes) outside any capture.
+        map.KLObjective(pts, dLoss.p, dGrad.p, mode == 2 ? 0 : -1, s);
+        if (mode == 2)
+            for (unsigned c = 1; c < map.NumMonotoneComponents(); ++c) map.KLObjective(pts, dLoss.p, dGrad.p, (int)c, s);
+        TR_CUDA(cudaStreamSynchronize(s));
+        if (mode == 0) {
+            const bool wasAsync = map.Async();
+            map.SetAsync(true);
+            TR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            enqueue();
+            TR_CUDA(cudaStreamEndCapture(s, &graph));
+            map.SetAsync(wasAsync);
+            TR_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        }
+    }
+    ~KLStep() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    void enqueue() {
+        TR_CUDA(cudaMemcpyAsync(dCoef, hCoef.p, nc * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (mode == 2) {
+            for (unsigned c = 0; c < map.NumMonotoneComponents(); ++c) map.KLObjective(pts, dLoss.p, dGrad.p, (int)c, s);
+        } else {
+            map.KLObjective(pts, dLoss.p, dGrad.p, -1, s);
+        }
+        TR_CUDA(cudaMemcpyAsync(hLoss.p, dLoss.p, no * sizeof(double), cudaMemcpyDeviceToHost, s));
+        TR_CUDA(cudaMemcpyAsync(hGrad.p, dGrad.p, nc * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    void run() {
+        if (mode == 0) {
+            TR_CUDA(cudaGraphLaunch(exec, s));
+        } else {
+            const bool wasAsync = map.Async();
+            map.SetAsync(true);
+            enqueue();
+            map.SetAsync(wasAsync);
+        }
+        TR_CUDA(cudaStreamSynchronize(s));
+    }
+};
+
+}  // namespace
+}  // namespace mpgb
+
+namespace mpgb {
+
+int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
+                        mpgb_train_result* res, void* stream, char* err, int errLen) {
+    try {
+        auto* map = static_cast<MonotoneMapBase*>(mapObj);
+        if (!map || !opts) throw std::invalid_argument("null argument");
+        map->CheckCoefficients("TrainMap");
+        cudaStream_t s = (cudaStream_t)stream;
+        StridedMatrix pts(samples.data, samples.rows, samples.cols, samples.row_stride, samples.col_stride);
+        TrainOpts o;
+        o.maxIters = opts->max_iters;
+        o.maxEvals = opts->max_evals;
+        o.ftolRel = opts->ftol_rel;
+        o.ftolAbs = opts->ftol_abs;
+        o.xtolRel = opts->xtol_rel;
+        o.xtolAbs = opts->xtol_abs;
+        o.gtol = opts->gtol;
+        o.memory = opts->memory > 0 ? opts->memory : 10;
+        const auto& parts = map->Parts();
+        std::vector<double> x0 = map->CoeffMap();
+        KLStep step(*map, pts, s, opts->mode);
+        std::vector<LBFGS> opt;
+        for (auto& p : parts) opt.emplace_back(x0.data() + p.mapCoeffOffset, (int)(
+                                                   (&p == &parts.back() ? map->numCoeffs : (&p + 1)->mapCoeffOffset) -
+                                                   p.mapCoeffOffset), o);
+        int steps = 0;
+        double stepMs = 0.0;
+        cudaEvent_t e0, e1;
+        TR_CUDA(cudaEventCreate(&e0));
+        TR_CUDA(cudaEventCreate(&e1));
+        const auto t0 = std::chrono::steady_clock::now();
+        while (true) {
+            bool any = false;
+            for (size_t c = 0; c < opt.size(); ++c) {
+                const auto& r = opt[c].request();
+                std::memcpy(step.hCoef.p + parts[c].mapCoeffOffset, r.data(), r.size() * sizeof(double));
+                any |= !opt[c].done();
+            }
+            if (!any) break;
+            TR_CUDA(cudaEventRecord(e0, s));
+            step.run();
+            TR_CUDA(cudaEventRecord(e1, s));
+            TR_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            stepMs += ms;
+            ++steps;
+            int st = map->CheckStatus(s);
+            if (st & 1) throw IntegrandError("TrainMap: MonotoneIntegrand: g(df) overflowed during training.");
+            for (size_t c = 0; c < opt.size(); ++c)
+                if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
+        }
+        const double totalMs =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::vector<double> xf(map->numCoeffs);
+        double total = 0;
+        int iters = 0, evals = 0;
+        for (size_t c = 0; c < opt.size(); ++c) {
+            std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c].x().data(), opt[c].x().size() * sizeof(double));
+            if (loss_per_comp) loss_per_comp[c] = opt[c].f();
+            total += opt[c].f();
+            iters = std::max(iters, opt[c].iterations());
+            evals = std::max(evals, opt[c].evaluations());
+        }
+        map->SetCoeffs(xf.data(), map->numCoeffs, true, s);
+        if (res) {
+            res->total_loss = total;
+            res->iterations = iters;
+            res->evaluations = evals;
+            res->steps = steps;
+            res->ms_per_step = steps ? stepMs / steps : 0.0;
+            res->total_ms = totalMs;
+        }
+        return MPGB_OK;
+    } catch (IntegrandError const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_INTEGRAND;
+    } catch (std::invalid_argument const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_INVALID_ARGUMENT;
+    } catch (std::exception const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_RUNTIME;
+    }
+}
+
+int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream,
+                           char* err, int errLen) {
+    try {
+        auto* map = static_cast<MonotoneMapBase*>(mapObj);
+        if (!map || steps <= 0) throw std::invalid_argument("bad argument");
+        cudaStream_t s = (cudaStream_t)stream;
+        StridedMatrix pts(samples.data, samples.rows, samples.cols, samples.row_stride, samples.col_stride);
+        KLStep step(*map, pts, s, mode);
+        std::vector<double> x0 = map->CoeffMap();
+        std::memcpy(step.hCoef.p, x0.data(), x0.size() * sizeof(double));
+        for (int i = 0; i < 3; ++i) step.run();
+        cudaEvent_t e0, e1;
+        TR_CUDA(cudaEventCreate(&e0));
+        TR_CUDA(cudaEventCreate(&e1));
+        double tot = 0;
+        for (int i = 0; i < steps; ++i) {
+            TR_CUDA(cudaEventRecord(e0, s));
+            step.run();
+            TR_CUDA(cudaEventRecord(e1, s));
+            TR_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            tot += ms;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms_per_step = tot / steps;
+        return MPGB_OK;
+    } catch (std::exception const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_RUNTIME;
+    }
+}
+
+}  // namespace mpgb

@@ -71,6 +71,9 @@ struct FusedParams {
     double* lossPartials;
     int* status; long long statusStride;
     int* statusWord;
+    // Optional processing order: point index of slot j for component c is
+    // perm[c * permStride + j] (items of one component only).
+    const int* perm; long long permStride;
     double nugget;
     int dmax, nBmax, depthMax, pad_;
     QuadParams quad;

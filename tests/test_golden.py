@@ -120,4 +120,7 @@ def test_gpu_matches_golden_c5(gpu):
     tm.SetCoeffs(g["coef"])
     n = g["r"].shape[1]
     xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(g["r"]), xtol=1e-10, ytol=1e-10))
-    assert np.max(np.abs(xi - g["inverse"])) <= 1e-8
+    # points where the reference's bracket search fails are NaN in both
+    assert np.array_equal(np.isnan(xi), np.isnan(g["inverse"]))
+    ok = ~np.isnan(g["inverse"])
+    assert np.max(np.abs(xi - g["inverse"])[ok]) <= 1e-8
