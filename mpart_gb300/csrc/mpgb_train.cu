@@ -189,9 +189,14 @@ struct KLStep {
     cudaGraphExec_t exec = nullptr;
     unsigned nc, no;
 
-    KLStep(MonotoneMapBase& m, StridedMatrix const& p, cudaStream_t st, int md)
-        : map(m), pts(p), s(st), mode(md), dCoef(m.Coeffs()), hCoef(m.numCoeffs), hLoss(m.outputDim),
+    // The step runs on a private non-blocking stream (a graph cannot be
+    // captured on the legacy default stream); the caller's stream is
+    // synchronised first.
+    KLStep(MonotoneMapBase& m, StridedMatrix const& p, cudaStream_t user, int md)
+        : map(m), pts(p), s(nullptr), mode(md), dCoef(m.Coeffs()), hCoef(m.numCoeffs), hLoss(m.outputDim),
           hGrad(m.numCoeffs), dLoss(m.outputDim), dGrad(m.numCoeffs), nc(m.numCoeffs), no(m.outputDim) {
+        TR_CUDA(cudaStreamSynchronize(user));
+        TR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
         // Warm-up (builds launch tables, sets kernel attributes) outside any capture.
         map.KLObjective(pts, dLoss.p, dGrad.p, mode == 2 ? 0 : -1, s);
         if (mode == 2)
@@ -210,6 +215,10 @@ struct KLStep {
     ~KLStep() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
     }
     void enqueue() {
         TR_CUDA(cudaMemcpyAsync(dCoef, hCoef.p, nc * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -277,15 +286,15 @@ int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* op
                 any |= !opt[c].done();
             }
             if (!any) break;
-            TR_CUDA(cudaEventRecord(e0, s));
+            TR_CUDA(cudaEventRecord(e0, step.s));
             step.run();
-            TR_CUDA(cudaEventRecord(e1, s));
+            TR_CUDA(cudaEventRecord(e1, step.s));
             TR_CUDA(cudaEventSynchronize(e1));
             float ms = 0;
             TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             stepMs += ms;
             ++steps;
-            int st = map->CheckStatus(s);
+            int st = map->CheckStatus(step.s);
             if (st & 1) throw IntegrandError("TrainMap: MonotoneIntegrand: g(df) overflowed during training.");
             for (size_t c = 0; c < opt.size(); ++c)
                 if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
@@ -342,9 +351,9 @@ int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, doubl
         TR_CUDA(cudaEventCreate(&e1));
         double tot = 0;
         for (int i = 0; i < steps; ++i) {
-            TR_CUDA(cudaEventRecord(e0, s));
+            TR_CUDA(cudaEventRecord(e0, step.s));
             step.run();
-            TR_CUDA(cudaEventRecord(e1, s));
+            TR_CUDA(cudaEventRecord(e1, step.s));
             TR_CUDA(cudaEventSynchronize(e1));
             float ms = 0;
             TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
