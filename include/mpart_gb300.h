@@ -173,6 +173,20 @@ int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_ma
  * (numCoeffs doubles) may be device or host pointers. */
 int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad, void* stream);
 
+/* Same results as mpgb_fused_fwd_adj without allocating any memory, for
+ * callers that may not allocate while they run (code inside a custom
+ * allocator, allocation-free real-time loops, hosts that manage the whole
+ * device heap).  No counterpart in the reference.  Scratch comes from a fixed
+ * 64 MiB array in device memory that the library holds on every GPU it is
+ * loaded on; calls needing more are rejected (MPGB_ERR_INVALID_ARGUMENT).
+ * Device pointers only; out_logdet only for one-component maps; no input
+ * gradient.  All calls share the array, so calls that overlap on the GPU
+ * race.  The first call on a device looks up the array's address: make it
+ * before any stream capture.  Synchronises the stream before returning. */
+int mpgb_fused_fwd_adj_noalloc(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix logdet_sens,
+                               double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet,
+                               double* coeff_grad, void* stream);
+
 /* Training options: limited-memory BFGS per component (NLopt's LD_LBFGS is
  * not available; the stopping fields follow TrainOptions, MParT/TrainMap.h:19-58,
  * with 0 disabling a criterion).  mode 0: one batched launch set per step,

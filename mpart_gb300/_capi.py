@@ -86,6 +86,8 @@ SIGNATURES = {
     "mpgb_log_determinant_input_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
     "mpgb_fused_fwd_adj": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, mpgb_matrix,
                                      mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
+    "mpgb_fused_fwd_adj_noalloc": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, mpgb_matrix,
+                                             mpgb_matrix, C.c_void_p, C.c_void_p]),
     "mpgb_kl_objective": (C.c_int, [_MAP, mpgb_matrix, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
     "mpgb_train_options_default": (C.c_int, [C.POINTER(mpgb_train_options)]),

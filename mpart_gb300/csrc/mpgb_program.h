@@ -1,0 +1,188 @@
+// Internal: the component program (prefix-tree tables on the device) and
+// small host helpers shared by the host translation units.
+#pragma once
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mpart_gb300.hpp"
+#include "mpgb_types.h"
+
+namespace mpgb {
+
+#define MPGB_CUDA(call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            std::ostringstream os_;                                                                       \
+            os_ << "CUDA error " << cudaGetErrorName(e_) << " (" << cudaGetErrorString(e_) << ") at " #call; \
+            throw CudaError(os_.str());                                                                   \
+        }                                                                                                 \
+    } while (0)
+
+struct CudaError : public std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// ---------------------------------------------------------------------------
+// Component program: the multi-index set reorganised as a prefix tree over
+// the leading coordinates (see mpgb_device.cuh for the factorisation).
+// ---------------------------------------------------------------------------
+template <class T>
+static T* toDevice(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    T* d = nullptr;
+    MPGB_CUDA(cudaMalloc(&d, v.size() * sizeof(T)));
+    MPGB_CUDA(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return d;
+}
+
+struct ComponentProgram {
+    int D = 0, P = 0, nB = 0, nNodes = 0, nSlots = 0, nCNodes = 0, maxDepth = 0, numTerms = 0;
+    std::vector<uint32_t> nodeA, nodeSlot, nodeC;
+    std::vector<uint16_t> nodeCRows;
+    std::vector<int32_t> slotTerm, leadDeg, rowOff;
+    uint32_t *dNodeA = nullptr, *dNodeSlot = nullptr, *dNodeC = nullptr;
+    uint16_t* dNodeCRows = nullptr;
+    int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr;
+    // Work per point (FP64 operations of phases A and C), for load balancing.
+    double weight = 1.0;
+
+    explicit ComponentProgram(FixedMultiIndexSet const& ms) {
+        D = (int)ms.Length();
+        numTerms = (int)ms.Size();
+        const auto& md = ms.maxDegrees;
+        P = (int)md[D - 1];
+        if (P > kMaxLastOrder) {
+            std::ostringstream os;
+            os << "MonotoneComponent: order " << P << " in the last input exceeds the supported maximum "
+               << kMaxLastOrder << ".";
+            throw std::invalid_argument(os.str());
+        }
+        leadDeg.resize(std::max(D - 1, 0));
+        rowOff.resize(std::max(D - 1, 0));
+        for (int d = 0; d + 1 < D; ++d) {
+            leadDeg[d] = (int)md[d];
+            rowOff[d] = nB;
+            nB += (int)md[d];
+        }
+        if (nB >= (1 << 14)) throw std::invalid_argument("MonotoneComponent: basis table too large.");
+        // Trie over the leading-coordinate prefixes.
+        struct TNode {
+            int parent, depth, dim, order;
+            std::map<std::pair<int, int>, int> children;
+            std::map<int, int> kTerm;
+        };
+        std::vector<TNode> tn;
+        tn.push_back({-1, 0, 0, 0, {}, {}});
+        for (int t = 0; t < numTerms; ++t) {
+            int b = (int)ms.nzStarts[t], e = (int)ms.nzStarts[t + 1];
+            int k = 0;
+            if (e > b && (int)ms.nzDims[e - 1] == D - 1) {
+                k = (int)ms.nzOrders[e - 1];
+                --e;
+            }
+            int cur = 0;
+            for (int i = b; i < e; ++i) {
+                std::pair<int, int> key((int)ms.nzDims[i], (int)ms.nzOrders[i]);
+                auto it = tn[cur].children.find(key);
+                if (it == tn[cur].children.end()) {
+                    TNode nn{cur, tn[cur].depth + 1, key.first, key.second, {}, {}};
+                    tn.push_back(nn);
+                    int id = (int)tn.size() - 1;
+                    tn[cur].children[key] = id;
+                    cur = id;
+                } else {
+                    cur = it->second;
+                }
+            }
+            if (tn[cur].kTerm.count(k))
+                throw std::invalid_argument("MonotoneComponent: the multi-index set contains a repeated term.");
+            tn[cur].kTerm[k] = t;
+        }
+        // DFS pre-order, children in increasing (dim, order).
+        std::vector<int> order;
+        std::vector<int> stack{0};
+        while (!stack.empty()) {
+            int n = stack.back();
+            stack.pop_back();
+            order.push_back(n);
+            for (auto it = tn[n].children.rbegin(); it != tn[n].children.rend(); ++it) stack.push_back(it->second);
+        }
+        nNodes = (int)order.size();
+        std::vector<int> slotOf(tn.size(), -1), nkOf(tn.size(), 0), browOf(tn.size(), 0);
+        for (int n : order) {
+            const TNode& t = tn[n];
+            if (t.depth > kMaxDepth) throw std::invalid_argument("MonotoneComponent: too many nonzero factors in a term.");
+            maxDepth = std::max(maxDepth, t.depth);
+            int nk = t.kTerm.empty() ? 0 : t.kTerm.rbegin()->first + 1;
+            int brow = (t.depth > 0) ? rowOff[t.dim] + t.order - 1 : 0;
+            int slot = (int)slotTerm.size();
+            for (int k = 0; k < nk; ++k) {
+                auto it = t.kTerm.find(k);
+                slotTerm.push_back(it == t.kTerm.end() ? -1 : it->second);
+            }
+            slotOf[n] = slot;
+            nkOf[n] = nk;
+            browOf[n] = brow;
+            nodeA.push_back((uint32_t)t.depth | ((uint32_t)nk << 5) | ((uint32_t)t.dim << 10) | ((uint32_t)brow << 18));
+            nodeSlot.push_back((uint32_t)slot);
+        }
+        nSlots = (int)slotTerm.size();
+        if (nSlots >= (1 << 22)) throw std::invalid_argument("MonotoneComponent: too many terms.");
+        // Nodes carrying terms, grouped by (depth, nk) for uniform warps in the reduction.
+        std::vector<int> cn;
+        for (int n : order)
+            if (nkOf[n] > 0) cn.push_back(n);
+        std::stable_sort(cn.begin(), cn.end(), [&](int a, int b) {
+            if (tn[a].depth != tn[b].depth) return tn[a].depth < tn[b].depth;
+            return nkOf[a] < nkOf[b];
+        });
+        nCNodes = (int)cn.size();
+        nodeCRows.assign((size_t)nCNodes * kMaxDepth, 0);
+        double opsA = 0, opsC = 0;
+        for (int j = 0; j < nCNodes; ++j) {
+            int n = cn[j];
+            nodeC.push_back((uint32_t)tn[n].depth | ((uint32_t)nkOf[n] << 5) | ((uint32_t)slotOf[n] << 10));
+            std::vector<int> path;
+            for (int q = n; q != 0; q = tn[q].parent) path.push_back(browOf[q]);
+            std::reverse(path.begin(), path.end());
+            for (size_t q = 0; q < path.size(); ++q) nodeCRows[(size_t)j * kMaxDepth + q] = (uint16_t)path[q];
+            opsC += std::max(tn[n].depth - 1, 0) + nkOf[n];
+        }
+        for (int n : order) opsA += (tn[n].depth > 0 ? 1 : 0) + nkOf[n];
+        weight = opsA + opsC + 3.0 * nB + 60.0;
+        dNodeA = toDevice(nodeA);
+        dNodeSlot = toDevice(nodeSlot);
+        dNodeC = toDevice(nodeC);
+        dNodeCRows = toDevice(nodeCRows);
+        dSlotTerm = toDevice(slotTerm);
+        dLeadDeg = toDevice(leadDeg);
+        dRowOff = toDevice(rowOff);
+    }
+    ~ComponentProgram() {
+        cudaFree(dNodeA);
+        cudaFree(dNodeSlot);
+        cudaFree(dNodeC);
+        cudaFree(dNodeCRows);
+        cudaFree(dSlotTerm);
+        cudaFree(dLeadDeg);
+        cudaFree(dRowOff);
+    }
+};
+
+// Records the message returned by mpgb_last_error() on this thread.
+void setLastError(const std::string& msg);
+
+}  // namespace mpgb
+
+// Handle behind the C ABI's opaque mpgb_map.
+struct mpgb_map {
+    std::shared_ptr<mpgb::ConditionalMapBase> obj;
+};
