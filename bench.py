@@ -17,6 +17,16 @@ same through the C ABI with pinned host buffers (host->device copy of points
 and sensitivities and device->host copy of T, logdet and the gradient inside
 the timed region).  `--impl reference` times the reference algorithm (the
 CPU restatement in oracle/, all host threads) on bounded samples.
+
+The line also carries `kl_train`, the KL training workload: a 6-D
+TriangularMap of total order 5 (HermiteFunctions basis, Exp rectifier, ACC tol
+1e-7) trained from zero coefficients on 200,000 samples of a synthetic banana
+target (x1 ~ N(0,1), x2 = x1^2 + 0.5 N(0,1), x_k = 0.8 x_{k-1} + 0.6 N(0,1)),
+standard-normal reference density, 100 L-BFGS iterations.  It reports the
+objective, the gradient norm and the device ms of one KL step (objective and
+gradient of every component) as one CUDA-graph replay of the batched launch,
+as direct batched launches, and as the per-component launch sequence, beside
+the oracle's time for the same step on the host cores.
 """
 from __future__ import annotations
 
@@ -36,6 +46,7 @@ sys.path.insert(0, ROOT)
 DIM, ORDER, NPTS = 8, 4, 1_000_000
 TOL, MAXSUB = 1e-6, 30
 METRIC = "fused fwd+adjoint points/s (dim-8, order-4, FP64)"
+KL_DIM, KL_ORDER, KL_N, KL_TOL, KL_ITERS = 6, 5, 200_000, 1e-7, 100
 
 
 def synth(n, seed_pts=1, seed_sens=2):
@@ -46,6 +57,89 @@ def synth(n, seed_pts=1, seed_sens=2):
 
 def coeffs(nterms):
     return np.random.default_rng(0).normal(0.0, 0.05, nterms)
+
+
+def banana(n, seed=11):
+    """Synthetic banana target: x1 ~ N(0,1), x2 = x1^2 + 0.5 N(0,1),
+    x_k = 0.8 x_{k-1} + 0.6 N(0,1) for k = 3..KL_DIM."""
+    rng = np.random.default_rng(seed)
+    x1 = rng.standard_normal(n)
+    xs = [x1, x1 ** 2 + 0.5 * rng.standard_normal(n)]
+    while len(xs) < KL_DIM:
+        xs.append(0.8 * xs[-1] + 0.6 * rng.standard_normal(n))
+    return np.stack(xs)
+
+
+def kl_train(M, dev):
+    """KL training workload on the device: 100 L-BFGS iterations from zero
+    coefficients with the CUDA-graph step; then, at the trained coefficients,
+    the step time of the four launch modes (graph-batched, direct-batched, one
+    fused launch set per component, and per component the reference
+    objective's call sequence with dense outputs); then the same training with
+    the per-component modes (objectives compared)."""
+    import torch
+    opts = M.MapOptions(basisType=M.BasisTypes.HermiteFunctions, posFuncType=M.PosFuncTypes.Exp,
+                        quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=KL_TOL, quadRelTol=KL_TOL)
+    X = torch.as_tensor(banana(KL_N), device=dev)
+    tm = M.CreateTriangular(KL_DIM, KL_DIM, KL_ORDER, opts)
+    tm.SetCoeffs(np.zeros(tm.numCoeffs))
+    l0 = M.launch_count()
+    loss_g, r_g = M.TrainMap(tm, X, max_iters=KL_ITERS, mode=0)
+    launches = M.launch_count() - l0
+    trained = np.array(tm.CoeffMap())
+    ms = {m: M.KLStepTime(tm, X, mode=m, steps=10) for m in (0, 1, 2, 3)}
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+    tm.SetCoeffs(np.zeros(tm.numCoeffs))
+    loss_p, r_p = M.TrainMap(tm, X, max_iters=KL_ITERS, mode=2)
+    tm.SetCoeffs(np.zeros(tm.numCoeffs))
+    loss_r, r_r = M.TrainMap(tm, X, max_iters=KL_ITERS, mode=3)
+    return {
+        "workload": f"TriangularMap {KL_DIM}-D, total order {KL_ORDER} ({tm.numCoeffs} coefficients), "
+                    f"HermiteFunctions + Exp, ACC tol {KL_TOL}, {KL_N} banana samples, standard-normal KL, "
+                    f"{KL_ITERS} L-BFGS iterations from zero coefficients",
+        "objective": float(r_g["total_loss"]), "objective_per_component": [float(v) for v in loss_g],
+        "grad_norm": float(r_g["grad_norm"]), "iterations": int(r_g["iterations"]),
+        "steps": int(r_g["steps"]), "train_ms_per_step": float(r_g["ms_per_step"]),
+        "train_total_ms": float(r_g["total_ms"]), "gpu_launches": int(launches),
+        "step_ms_at_trained_coeffs": {"graph_batched": ms[0], "direct_batched": ms[1],
+                                      "per_component_fused": ms[2], "per_component_reference_calls": ms[3]},
+        "batched_speedup_vs_reference_calls": ms[3] / ms[0],
+        "batched_speedup_vs_per_component_fused": ms[2] / ms[0],
+        "objective_max_rel_diff_vs_per_component_fused": rel(loss_g, loss_p),
+        "objective_max_rel_diff_vs_reference_calls": rel(loss_g, loss_r),
+        "reference_calls_train_ms_per_step": float(r_r["ms_per_step"]),
+    }, trained
+
+
+def kl_cpu_step_ms(coeffs, target_seconds=8.0):
+    """The oracle's KL step (every component's FastGaussianReverseKLObjective
+    value and gradient, src/MapObjective.cpp:185-234, as TrainMap evaluates
+    them one component at a time) at the given coefficients on a bounded
+    sample, scaled to KL_N."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    tmo = O.OracleTriangularMap(KL_DIM, KL_DIM, KL_ORDER, basis=O.BASIS_HERMITE_FUNCTIONS, posfunc=O.POS_EXP,
+                                abs_tol=KL_TOL, rel_tol=KL_TOL)
+    c = np.asarray(coeffs, dtype=np.float64)
+    X = banana(KL_N)
+
+    def step(n):
+        t0 = time.perf_counter()
+        for comp, cc in zip(tmo.comps, tmo.split(c)):
+            O.fast_gaussian_reverse_kl(comp, cc, np.ascontiguousarray(X[:comp.input_dim, :n]))
+        return time.perf_counter() - t0
+
+    n = 2000
+    dt = step(n)
+    n2 = int(min(KL_N, max(n, n * target_seconds / max(dt, 1e-6))))
+    dt = step(n2)
+    return {"ms_per_step": dt * 1e3 * KL_N / n2, "cores": cores, "kind": "port",
+            "sample": f"first {n2} of the {KL_N} samples at the trained coefficients, scaled to {KL_N}"}
 
 
 def prefix_stats():
@@ -257,6 +351,16 @@ def run_gpu(args):
         comp.FusedForwardAdjointImpl(x, sens=s, logdet_sens_scale=1.0, out_eval=out_T, out_logdet=out_ld,
                                      coeff_grad=cg)
 
+    if args.profile and args.variant != "full":
+        # Phase isolation for profiling: evaluate only (A + value quadrature),
+        # log-det only (A), or the reduced adjoint without quadrature (A + C).
+        variants = {
+            "eval": lambda: comp.EvaluateImpl(x, out_T),
+            "logdet": lambda: comp.LogDeterminantImpl(x, out_ld),
+            "reduce": lambda: comp.FusedForwardAdjointImpl(x, logdet_sens_scale=1.0, coeff_grad=cg),
+        }
+        step = variants[args.variant]
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -269,6 +373,7 @@ def run_gpu(args):
     if world > 1:
         dist.barrier()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = M.launch_count()
     with Clocks(local) as clk:
         torch.cuda.synchronize()
         for k in range(args.steps):
@@ -277,6 +382,7 @@ def run_gpu(args):
             step()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+    launches = M.launch_count() - launches0
     if world > 1:
         dist.barrier()
     times = [a.elapsed_time(b) for a, b in ev]
@@ -323,10 +429,13 @@ def run_gpu(args):
     fpp = flops_per_point(E)
     achieved = fpp * N / t_step / 1e12
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "fused_adjoint_c2_traffic.json")
+    # DRAM bytes of one fused launch from the committed ncu capture (same
+    # workload), scaled to this run's point count.
+    prof = os.path.join(ROOT, "profiles", "fusedKernel_dim8_order4_1M.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof))["bytes_per_point"] * N
+            pr = json.load(open(prof))
+            traffic = (pr["dram_bytes_read"] + pr["dram_bytes_write"]) * N / pr["points"]
         except Exception:
             traffic = None
     line = {
@@ -339,7 +448,7 @@ def run_gpu(args):
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * N / t_e2e, "unit": "points/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": None,
+        "gpu_launches": launches,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf, "traffic": traffic,
                      "peak_source": "DFMA probe in this run (MEASURED_PEAKS.json has no FP64 figure)",
@@ -349,8 +458,12 @@ def run_gpu(args):
     line["plain_path"] = plain_path(M, coef, x, s, N, dev)
     line["plain_path"]["fused_speedup"] = line["plain_path"]["ms_per_step"] / (t_step * 1e3)
     line["cpu_baseline"] = cpu_baseline()
-    # launches per step: gather + fused + per-component reduction
-    line["gpu_launches"] = 3 * args.steps
+    if not args.no_kl:
+        kl, trained = kl_train(M, dev)
+        kl["cpu_step"] = kl_cpu_step_ms(trained)
+        kl["cpu_step"]["speedup_graph"] = (kl["cpu_step"]["ms_per_step"] /
+                                           kl["step_ms_at_trained_coeffs"]["graph_batched"])
+        line["kl_train"] = kl
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -389,6 +502,9 @@ def main():
     ap.add_argument("--impl", default="mine", choices=["mine", "reference"])
     ap.add_argument("--points", type=int, default=NPTS)
     ap.add_argument("--profile", action="store_true", help="fused step only (for profilers)")
+    ap.add_argument("--no-kl", action="store_true", help="skip the KL training workload")
+    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce"],
+                    help="with --profile: which part of the step to run")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -168,6 +168,17 @@ int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_ma
                        double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet, double* coeff_grad,
                        mpgb_matrix input_grad, void* stream);
 
+/* Implicit-function derivative of Inverse (TriangularMap::InverseImpl,
+ * src/TriangularMap.cpp:146-184, has no derivative in the reference).  pts is
+ * inputDim x N = [x1; x] with x = Inverse(x1, r); w is outputDim x N, the
+ * weights of L = sum_{k,i} w(k,i) x(k,i).  coeff_grad (numCoeffs doubles, may
+ * be NULL) receives dL/dc = -sum_i lambda_i^T dT/dc(x_i), where
+ * (dT/dx)^T lambda = w is solved per point by back-substitution over the
+ * components; pts_grad (inputDim x N, data may be NULL) receives
+ * [dL/dx1; dL/dr] = [-lambda^T dT/dx1; lambda]. */
+int mpgb_inverse_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix w, double* coeff_grad, mpgb_matrix pts_grad,
+                            void* stream);
+
 /* FastGaussianReverseKLObjective::ObjectivePlusCoeffGradImpl (src/MapObjective.cpp:221-234)
  * for every component of the map at once.  loss (outputDim doubles) and grad
  * (numCoeffs doubles) may be device or host pointers. */
@@ -190,8 +201,11 @@ int mpgb_fused_fwd_adj_noalloc(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens,
 /* Training options: limited-memory BFGS per component (NLopt's LD_LBFGS is
  * not available; the stopping fields follow TrainOptions, MParT/TrainMap.h:19-58,
  * with 0 disabling a criterion).  mode 0: one batched launch set per step,
- * replayed from a CUDA graph; 1: batched, direct launches; 2: one launch set
- * per component (unbatched). */
+ * replayed from a CUDA graph; 1: batched, direct launches; 2: one fused launch
+ * set per component (unbatched); 3: per component, the reference objective's
+ * call sequence (FastGaussianReverseKLObjective::CommonEval,
+ * src/MapObjective.cpp:185-234: Evaluate, LogDeterminant, CoeffGrad and
+ * LogDeterminantCoeffGrad into dense outputs, then reductions). */
 typedef struct mpgb_train_options {
     int max_iters;
     int max_evals;
@@ -211,6 +225,7 @@ typedef struct mpgb_train_result {
     int steps;          /* batched objective evaluations performed */
     double ms_per_step; /* device time per step (CUDA events) */
     double total_ms;    /* wall time of the training loop */
+    double grad_norm;   /* Euclidean norm of the gradient at the result, over all components */
 } mpgb_train_result;
 
 int mpgb_train_options_default(mpgb_train_options* opts);
@@ -230,6 +245,12 @@ int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, d
 /* FP64 throughput probe: DFMA chains over blocks x threads x iters x 8; writes the
  * kernel time in milliseconds (CUDA events on the stream). */
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms);
+
+/* Number of kernels this library has launched since it was loaded, over all
+ * threads (graph replays count their kernel nodes; launches captured into a
+ * graph count nothing).  No counterpart in the reference: it lets a caller
+ * confirm how many device launches a call made. */
+long long mpgb_launch_count(void);
 
 /* ------------------------------------------------------------------------
  * Reference-structured ("plain") GPU path, the comparator of the fused path:

@@ -164,6 +164,18 @@ public:
                              double logdetSensScale, StridedMatrix const& outEval, StridedMatrix const& outLogDet,
                              double* coeffGrad, StridedMatrix const& inputGrad, cudaStream_t stream = 0);
 
+    // Implicit-function adjoint of the inverse (no counterpart in the
+    // reference, which does not differentiate Inverse).  pts = [x1; x]
+    // (inputDim x N) with x = Inverse(x1, r); w (outputDim x N) holds the
+    // weights of the functional L = sum_{k,i} w(k,i) x(k,i).  With
+    // (dT/dx)^T lambda = w solved per point by back-substitution over the
+    // components (last first), coeffGrad (device, numCoeffs; may be null)
+    // receives dL/dc = -sum_i lambda_i^T dT/dc(x_i), and ptsGrad (inputDim x N;
+    // may be empty) receives [dL/dx1; dL/dr] = [-lambda^T dT/dx1; lambda].
+    // One launch per component; dT/dx_D is taken as g(df(x)) + nugget.
+    void InverseCoeffGrad(StridedMatrix const& pts, StridedMatrix const& w, double* coeffGrad,
+                          StridedMatrix const& ptsGrad, cudaStream_t stream = 0);
+
     // Standard-normal reverse KL of every component at once
     // (FastGaussianReverseKLObjective, src/MapObjective.cpp:93-234): per component
     // loss_c = mean(0.5 T_c^2 - logdet_c) and its coefficient gradient.

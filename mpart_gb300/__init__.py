@@ -270,6 +270,27 @@ class ConditionalMapBase:
                                         _mat(out_eval), _mat(out_logdet), _ptr(coeff_grad), _mat(input_grad),
                                         _stream_of(pts, sens, out_eval)))
 
+    def InverseCoeffGradImpl(self, pts, w, coeff_grad=None, pts_grad=None):
+        """Implicit-function adjoint of Inverse: pts = [x1; x] at the solution,
+        w the weights of L = sum w * x; coeff_grad <- dL/dc, pts_grad <- [dL/dx1; dL/dr]."""
+        check(load().mpgb_inverse_coeff_grad(self._h, _mat(pts), _mat(w), _ptr(coeff_grad), _mat(pts_grad),
+                                             _stream_of(pts, w)))
+
+    def InverseCoeffGrad(self, x1, x, w):
+        """Returns (dL/dc, dL/dx1, dL/dr) for L = sum w * x with x = Inverse(x1, r)."""
+        extra = self.inputDim - self.outputDim
+        if not extra:
+            pts = x
+        elif _is_torch(x):
+            import torch
+            pts = torch.cat([x1[:extra].expand(extra, x.shape[1]), x], dim=0).contiguous()
+        else:
+            pts = np.concatenate([np.broadcast_to(x1[:extra], (extra, x.shape[1])), x], axis=0)
+        cg = _zeros_like_dev(x, (self.numCoeffs,))
+        pg = _zeros_like_dev(x, (self.inputDim, x.shape[1]))
+        self.InverseCoeffGradImpl(pts, w, cg, pg)
+        return cg, pg[:extra], pg[extra:]
+
     # ---- allocating versions (the reference's Evaluate(pts) etc.) --------
     def Evaluate(self, pts):
         out = _zeros_like_dev(pts, (self.outputDim, pts.shape[1]))
@@ -371,7 +392,9 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
     """TrainMap with a standard-normal KL objective (src/TrainMap.cpp:166-216):
     every component minimises its reverse KL with L-BFGS; samples is a CUDA
     float64 tensor, inputDim x N.  mode 0 replays one batched step from a CUDA
-    graph, 1 launches it directly, 2 launches each component separately.
+    graph, 1 launches it directly, 2 launches each component separately, 3 runs
+    per component the reference objective's call sequence (Evaluate,
+    LogDeterminant, CoeffGrad, LogDeterminantCoeffGrad with dense outputs).
     Returns (final loss per component, result dict); the map keeps the result."""
     from ._capi import mpgb_train_options, mpgb_train_result
     o = mpgb_train_options()
@@ -383,7 +406,8 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
     check(load().mpgb_train_map(tmap._h, _mat(samples), C.byref(o), C.c_void_p(loss.ctypes.data), C.byref(r),
                                 _stream_of(samples)))
     return loss, {"total_loss": r.total_loss, "iterations": r.iterations, "evaluations": r.evaluations,
-                  "steps": r.steps, "ms_per_step": r.ms_per_step, "total_ms": r.total_ms}
+                  "steps": r.steps, "ms_per_step": r.ms_per_step, "total_ms": r.total_ms,
+                  "grad_norm": r.grad_norm}
 
 
 def KLStepTime(tmap: ConditionalMapBase, samples, mode=0, steps=10):
@@ -418,6 +442,12 @@ class PlainComponent:
         n = pts.shape[1]
         check(load().mpgb_plain_fwd_adj(self._h, _ptr(coeffs), _ptr(pts), n, _ptr(sens), _ptr(out_eval),
                                         _ptr(out_logdet), _ptr(coeff_grad), _stream_of(pts)))
+
+
+def launch_count():
+    """Kernels the library has launched since it was loaded (graph replays
+    count their kernel nodes)."""
+    return int(load().mpgb_launch_count())
 
 
 def fp64_probe(blocks=152 * 8, threads=256, iters=4096):

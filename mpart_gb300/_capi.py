@@ -50,7 +50,7 @@ class mpgb_train_options(C.Structure):
 
 class mpgb_train_result(C.Structure):
     _fields_ = [("total_loss", C.c_double), ("iterations", C.c_int), ("evaluations", C.c_int), ("steps", C.c_int),
-                ("ms_per_step", C.c_double), ("total_ms", C.c_double)]
+                ("ms_per_step", C.c_double), ("total_ms", C.c_double), ("grad_norm", C.c_double)]
 
 
 # Every symbol the header declares, with its signature.
@@ -89,7 +89,9 @@ SIGNATURES = {
     "mpgb_fused_fwd_adj_noalloc": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, mpgb_matrix,
                                              mpgb_matrix, C.c_void_p, C.c_void_p]),
     "mpgb_kl_objective": (C.c_int, [_MAP, mpgb_matrix, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mpgb_inverse_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "mpgb_launch_count": (C.c_longlong, []),
     "mpgb_train_options_default": (C.c_int, [C.POINTER(mpgb_train_options)]),
     "mpgb_train_map": (C.c_int, [_MAP, mpgb_matrix, C.POINTER(mpgb_train_options), C.c_void_p,
                                  C.POINTER(mpgb_train_result), C.c_void_p]),

@@ -169,6 +169,7 @@ struct MapWorkspace {
     bool built = false;
     std::vector<std::unique_ptr<KLPlan>> klPlans;
     DevBuf perm, sortHist;
+    DevBuf implicitAcc;  // back-substitution sums when the caller wants no input gradient
     bool ordering = true;
 };
 
@@ -405,6 +406,7 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
     dim3 grid((maxSlots + 255) / 256, (unsigned)g.size());
     gatherMultiKernel<<<grid, 256, 0, stream>>>(W.gather.as<GatherDescHost>(), (int)g.size(), W.cm.as<double>());
     MPGB_CUDA(cudaGetLastError());
+    countLaunches(stream, 1);
 }
 
 void MonotoneMapBase::Finish(cudaStream_t stream, const char* fn) {
@@ -490,14 +492,17 @@ static std::vector<WorkItem> itemsAllComps(long long N, int nComps) {
     long long nTiles = (N + kTpb - 1) / kTpb;
     std::vector<WorkItem> v;
     v.reserve(nTiles);
-    for (long long t = 0; t < nTiles; ++t) v.push_back({0, nComps, (int)t, 1, 0, 0, 0});
+    for (long long t = 0; t < nTiles; ++t) v.push_back({0, nComps, (int)t, 1, 0, 0, 1});
     return v;
 }
 
-// Items of style "one component, a range of tiles".  Heavier components first.
+// Items of style "one component, a set of tiles".  Heavier components first.
 // With reduced outputs each component is cut into at most 4 items per SM,
 // independently of the other components of the launch, so a batched launch
-// and per-component launches produce the same partial rows.
+// and per-component launches produce the same partial rows.  Item k of a
+// component takes tiles k, k + nItems, k + 2 nItems, ...: points are processed
+// in order of |x_D| (quadrature cost grows with it), and striding gives every
+// item the same mix of cheap and expensive tiles.
 static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Part>& parts, long long N, int numSMs,
                                           bool reduced, std::vector<long long>* rowBaseOut,
                                           std::vector<std::vector<int>>* itemsOfComp, int onlyComp = -1) {
@@ -512,13 +517,10 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
     long long base = 0;
     if (itemsOfComp) itemsOfComp->assign(nComps, {});
     for (int c : order) {
-        long long tilesPer = 1;
-        if (reduced) {
-            const long long nItemsC = std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * 4));
-            tilesPer = (nTiles + nItemsC - 1) / nItemsC;
-        }
-        for (long long t = 0; t < nTiles; t += tilesPer) {
-            WorkItem w{c, c + 1, (int)t, (int)std::min<long long>(tilesPer, nTiles - t), 0, 0, 0};
+        const long long nItemsC =
+            reduced ? std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * 4)) : nTiles;
+        for (long long t = 0; t < nItemsC; ++t) {
+            WorkItem w{c, c + 1, (int)t, (int)((nTiles - t + nItemsC - 1) / nItemsC), 0, 0, (int)nItemsC};
             if (reduced) {
                 w.partialBase = base;
                 w.lossSlot = (int)v.size();
@@ -818,6 +820,7 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
                 W.logdetRows.as<double>(), nComps, N, outLogDet.data,
                 (outLogDet.rows == 1) ? outLogDet.colStride : outLogDet.rowStride);
             MPGB_CUDA(cudaGetLastError());
+            countLaunches(stream, 1);
         } else {
             launch(W, opts_, p, (int)items.size(), needJ, 0, stream);
         }
@@ -932,6 +935,77 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
                                 lossPerComp + c, stream));
     }
     Finish(stream, "KLObjective");
+}
+
+// Implicit-function adjoint of the inverse.  For the functional
+// L = sum w(k,i) x(k,i) of x = T^{-1}(x1, r) the adjoint solves, per point,
+// (dT/dx)^T lambda = w: lambda_k = (w_k - sum_{m>k} lambda_m dT_m/dx_k) / dT_k/dx_k,
+// components last to first.  Each component is one fused launch over all
+// points: it reads the running sums from ptsGrad, forms lambda_k, adds
+// lambda_k dT_k/dx_j (forward mode over the prefix tree plus the parameter
+// quadrature) to rows j < k, and reduces lambda_k dT_k/dc into partial rows;
+// dL/dc_k = -sum_i lambda_k dT_k/dc.
+void MonotoneMapBase::InverseCoeffGrad(StridedMatrix const& pts, StridedMatrix const& w, double* coeffGrad,
+                                       StridedMatrix const& ptsGrad, cudaStream_t stream) {
+    CheckCoefficients("InverseCoeffGrad");
+    const long long N = pts.cols;
+    checkMatrix(pts, inputDim, N, "pts", "InverseCoeffGrad");
+    checkMatrix(w, outputDim, N, "w", "InverseCoeffGrad");
+    if (!ptsGrad.empty()) checkMatrix(ptsGrad, inputDim, N, "pts_grad", "InverseCoeffGrad");
+    const int extra = (int)inputDim - (int)outputDim;
+    for (auto& pt : parts_)
+        if (pt.prog->D - 1 != extra + (int)pt.outRow)
+            throw std::invalid_argument("InverseCoeffGrad: component inputs are not triangular in the map outputs.");
+    if (!coeffGrad && ptsGrad.empty()) return;
+    Prepare(stream);
+    MapWorkspace& W = *ws_;
+    if (N == 0) {
+        if (coeffGrad) MPGB_CUDA(cudaMemsetAsync(coeffGrad, 0, numCoeffs * sizeof(double), stream));
+        Finish(stream, "InverseCoeffGrad");
+        return;
+    }
+    StridedMatrix G = ptsGrad;
+    if (G.empty()) {
+        W.implicitAcc.ensure((size_t)inputDim * N * sizeof(double), stream);
+        G = StridedMatrix(W.implicitAcc.as<double>(), inputDim, N, N, 1);
+    }
+    // Components in decreasing output row.
+    std::vector<int> order(parts_.size());
+    for (size_t c = 0; c < parts_.size(); ++c) order[c] = (int)c;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return parts_[a].outRow > parts_[b].outRow; });
+    const bool wantCoef = coeffGrad != nullptr;
+    for (size_t q = 0; q < order.size(); ++q) {
+        const int c = order[q];
+        std::vector<long long> rowBase;
+        std::vector<std::vector<int>> itemsOf;
+        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf, c);
+        uploadItems(W, items, stream);
+        FusedParams p{};
+        baseParams(W, opts_, p, N);
+        p.flags = kFlagInput | kFlagImplicit | (q == 0 ? kFlagImplicitFirst : 0) | (wantCoef ? kFlagCoefReduced : 0);
+        p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
+        p.sens = w.data; p.sensRs = w.rowStride; p.sensCs = w.colStride;
+        p.lsens = nullptr; p.lsensScale = 0.0;
+        p.outInput = G.data; p.inputRs = G.rowStride; p.inputCs = G.colStride;
+        p.negRows = (q + 1 == order.size()) ? extra : 0;
+        if (wantCoef) {
+            size_t nPart = 1;
+            for (auto& it : items) nPart = std::max<size_t>(nPart, (size_t)it.partialBase + parts_[c].prog->numTerms);
+            W.partials.ensure(nPart * sizeof(double), stream);
+            p.partials = W.partials.as<double>();
+        }
+        orderPoints(W, parts_, pts, p, c, stream);
+        launch(W, opts_, p, (int)items.size(), 1, 0, stream);
+        if (wantCoef) {
+            W.rowBase.ensure(sizeof(long long) * std::max<size_t>(1, rowBase.size()), stream);
+            MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rowBase.data(), rowBase.size() * sizeof(long long),
+                                      cudaMemcpyHostToDevice, stream));
+            MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>(), (int)rowBase.size(),
+                                       parts_[c].prog->numTerms, -1.0, coeffGrad + parts_[c].mapCoeffOffset, 0,
+                                       stream));
+        }
+    }
+    Finish(stream, "InverseCoeffGrad");
 }
 
 // ---------------------------------------------------------------------------
@@ -1467,6 +1541,21 @@ int mpgb_fused_fwd_adj(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_ma
     });
 }
 
+int mpgb_inverse_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix w, double* coeff_grad, mpgb_matrix pts_grad,
+                            void* stream) {
+    return guard([&] {
+        cudaStream_t s = (cudaStream_t)stream;
+        auto* m = mono(map);
+        Stager st(s, mono(map));
+        auto P = st.in(pts);
+        auto Wt = st.in(w);
+        auto G = st.out(pts_grad);
+        double* cg = st.outVec(coeff_grad, m->numCoeffs);
+        m->InverseCoeffGrad(P, Wt, cg, G, s);
+        st.finish();
+    });
+}
+
 int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad, void* stream) {
     return guard([&] {
         cudaStream_t s = (cudaStream_t)stream;
@@ -1512,6 +1601,8 @@ int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, d
     if (rc != MPGB_OK) g_lastError = err;
     return rc;
 }
+
+long long mpgb_launch_count(void) { return mpgb::launchCount(); }
 
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms) {
     return guard([&] {

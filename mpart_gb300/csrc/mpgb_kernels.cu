@@ -1,4 +1,6 @@
 // Dispatch of the fused/inverse kernels and the small helper kernels.
+#include <atomic>
+
 #include "mpgb_types.h"
 #include "mpgb_launch.h"
 
@@ -126,6 +128,34 @@ __global__ void sumLossKernel(const double* lossPart, const int* slots, int n, d
     }
 }
 
+// The reference objective's reductions over dense per-point outputs
+// (FastGaussianReverseKLObjective, src/MapObjective.cpp:185-234): block b < nTerms
+// sums grad_b = invN sum_i (sT(b,i) - sL(b,i)); block nTerms sums the loss
+// invN sum_i (0.5 T_i^2 - ld_i).  Fixed-order (strided, then tree) sums.
+__global__ void denseKLReduceKernel(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,
+                                    long long N, double invN, double* loss, double* grad) {
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    double s = 0.0;
+    if (b < nTerms) {
+        const double* a = dT + (long long)b * N;
+        const double* c = dL + (long long)b * N;
+        for (long long i = threadIdx.x; i < N; i += blockDim.x) s += a[i] - c[i];
+    } else {
+        for (long long i = threadIdx.x; i < N; i += blockDim.x) s += 0.5 * T[i] * T[i] - ld[i];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (b < nTerms) grad[b] = red[0] * invN;
+        else *loss = red[0] * invN;
+    }
+}
+
 // FP64 peak probe: independent DFMA chains (8 per thread).
 __global__ void dfmaPeakKernel(double* out, int iters, double seed) {
     double x[8];
@@ -202,6 +232,19 @@ cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm
     return launchInverseBP<kBasisHermiteFunctions, kPosExp>(prm, pmax, nBlocks, stream);
 }
 
+static std::atomic<long long> g_launches{0};
+
+void countLaunches(cudaStream_t stream, long long n) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) {
+        cudaGetLastError();  // the query's own error; the launch error was read before
+        return;
+    }
+    if (cs == cudaStreamCaptureStatusNone) g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+
+long long launchCount() { return g_launches.load(std::memory_order_relaxed); }
+
 size_t fusedSmemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input) {
     size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)(depthMax + 1) * tpb +
                (size_t)(pmax + 1) * tpb;
@@ -216,7 +259,9 @@ cudaError_t launchGather(const int32_t* slotGlobalTerm, int nSlots, const double
                          cudaStream_t stream) {
     if (nSlots <= 0) return cudaSuccess;
     gatherKernel<<<(nSlots + 255) / 256, 256, 0, stream>>>(slotGlobalTerm, nSlots, coeffs, cm);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 cudaError_t launchReduceRows(const double* part, const long long* rowBase, int nRows, int nTerms, double scale,
@@ -224,13 +269,17 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
     if (nTerms <= 0) return cudaSuccess;
     dim3 blk(32, 8);
     reduceRowsKernel<<<(nTerms + 31) / 32, blk, 0, stream>>>(part, rowBase, nRows, nTerms, scale, out, accumulate);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
                           cudaStream_t stream) {
     sumLossKernel<<<1, 32, 0, stream>>>(lossPart, slots, n, scale, out);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 size_t sortScratchInts(long long N) { return (size_t)((N + kSortChunk - 1) / kSortChunk) * kSortBuckets; }
@@ -242,12 +291,24 @@ cudaError_t launchSortByLast(const double* xd, long long stride, long long N, in
     keyHistKernel<<<nBlk, 256, 0, stream>>>(xd, stride, N, hist);
     keyScanKernel<<<1, kSortBuckets, 0, stream>>>(hist, nBlk);
     keyScatterKernel<<<nBlk, 32, 0, stream>>>(xd, stride, N, hist, perm);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 3);
+    return e;
+}
+
+cudaError_t launchDenseKLReduce(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,
+                                long long N, double* loss, double* grad, cudaStream_t stream) {
+    denseKLReduceKernel<<<nTerms + 1, 256, 0, stream>>>(T, ld, dT, dL, nTerms, N, 1.0 / (double)N, loss, grad);
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream) {
     dfmaPeakKernel<<<blocks, threads, 0, stream>>>(out, iters, 1.0);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 }  // namespace mpgb

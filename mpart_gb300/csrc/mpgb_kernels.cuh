@@ -290,7 +290,8 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const double ninf = __longlong_as_double(0xfff0000000000000ULL);
 
-    for (int tile = item.tile0; tile < item.tile0 + item.nTiles; ++tile) {
+    for (int tj = 0; tj < item.nTiles; ++tj) {
+        const int tile = item.tile0 + tj * item.tileStride;
         const long long slotIdx = (long long)tile * tpb + tid;
         const bool active = slotIdx < prm.N;
         const long long i = (active && prm.perm) ? (long long)prm.perm[item.c0 * prm.permStride + slotIdx] : slotIdx;
@@ -301,8 +302,11 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
             L.X[d * tpb + tid] = active ? prm.pts[d * prm.ptsRs + i * prm.ptsCs] : 0.0;
         double logdetSum = 0.0;
         double lossAcc = 0.0;
-        if (inputMode)
-            for (int d = 0; d < dneed; ++d) L.GX[d * tpb + tid] = 0.0;
+        if (inputMode) {
+            const bool carry = (flags & kFlagImplicit) && !(flags & kFlagImplicitFirst) && active;
+            for (int d = 0; d < dneed; ++d)
+                L.GX[d * tpb + tid] = carry ? prm.outInput[d * prm.inputRs + i * prm.inputCs] : 0.0;
+        }
 
         for (int ci = item.c0; ci < item.c1; ++ci) {
             const CompDesc& c = prm.comps[ci];
@@ -352,6 +356,13 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
                 if (prm.sens && active) sens = prm.sens[(long long)c.outRow * prm.sensRs + i * prm.sensCs];
                 if (flags & (kFlagCoefReduced | kFlagInput))
                     lsens = prm.lsens ? (active ? prm.lsens[i * prm.lsensStride] : 0.0) : prm.lsensScale;
+                if (flags & kFlagImplicit) {
+                    // lambda = (w - sum_{m > k} lambda_m dT_m/dx_D) / (g(df) + nugget)
+                    double* gd = &L.GX[(c.D - 1) * tpb + tid];
+                    sens = active ? (sens - *gd) / (gx + prm.nugget) : 0.0;
+                    *gd = sens;
+                    lsens = 0.0;
+                }
             }
             if (!active) { sens = 0.0; lsens = 0.0; }
             const double ldScale = gpx * (1.0 / gx);
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
                 double gxd = lsens * (ldScale * d2fx);
                 if constexpr (NEEDE) gxd = fma(sens, R.IE, gxd);
                 double* g = &L.GX[(c.D - 1) * tpb + tid];
-                *g += gxd;
+                if (!(flags & kFlagImplicit)) *g += gxd;  // implicit mode keeps lambda there
             }
 
             // Reduced combined adjoint: owner-computes over the block's points.
@@ -439,7 +450,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
 #pragma unroll
                 for (int k = 0; k <= PMAX; ++k) L.W[k * tpb + tid] = wT[k] + wL[k];
                 __syncthreads();
-                const bool first = (tile == item.tile0);
+                const bool first = (tj == 0);
                 double* part = prm.partials + item.partialBase;
                 for (int n = tid; n < c.nCNodes; n += tpb) {
                     const uint32_t w = __ldg(&c.nodeC[n]);
@@ -475,8 +486,10 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
             if (flags & kFlagLogDet) prm.outLogDet[i * prm.logDetStride] = logdetSum;
             if (inputMode) {
                 const int dneed2 = prm.comps[item.c1 - 1].D;
-                for (int d = 0; d < dneed2; ++d)
-                    prm.outInput[d * prm.inputRs + i * prm.inputCs] = L.GX[d * tpb + tid];
+                for (int d = 0; d < dneed2; ++d) {
+                    const double v = L.GX[d * tpb + tid];
+                    prm.outInput[d * prm.inputRs + i * prm.inputCs] = (d < prm.negRows) ? -v : v;
+                }
             }
             if (flags & kFlagStatusArray) prm.status[i * prm.statusStride] = st;
         }
@@ -489,7 +502,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
                 double s = 0.0;
                 for (int j = 0; j < tpb; ++j) s += L.W[j];
                 double* dst = prm.lossPartials + item.lossSlot;
-                *dst = (tile == item.tile0) ? s : (*dst + s);
+                *dst = (tj == 0) ? s : (*dst + s);
             }
             __syncthreads();
         }
@@ -663,7 +676,9 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         kern<<<nItems, prm.tpb, smem, stream>>>(prm);
-        return cudaGetLastError();
+        e = cudaGetLastError();
+        countLaunches(stream, 1);
+        return e;
     };
     if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, true>);
     if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, false>);
@@ -677,7 +692,9 @@ cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t s
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nBlocks, prm.tpb, smem, stream>>>(prm);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 }  // namespace mpgb

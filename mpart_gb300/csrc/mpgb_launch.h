@@ -24,5 +24,16 @@ size_t sortScratchInts(long long N);
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
                              cudaStream_t stream);
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
+// Loss and gradient of the standard-normal reverse KL from dense outputs:
+// T, ld (N), dT = dT/dc scaled by T, dL = dlogdet/dc (nTerms x N, row-major).
+cudaError_t launchDenseKLReduce(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,
+                                long long N, double* loss, double* grad, cudaStream_t stream);
+
+// Count of kernels this library has launched since it was loaded (all
+// threads).  Every launch site calls countLaunches after reading its launch
+// error; launches into a stream that is being captured are not counted, and
+// a graph replay counts the kernel nodes of the graph.
+void countLaunches(cudaStream_t stream, long long n);
+long long launchCount();
 
 }  // namespace mpgb

@@ -213,7 +213,7 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         const long long tilesPer = (nTiles + nItemsC - 1) / nItemsC;
         rowOff[c] = (int)rowBase.size();
         for (long long t = 0; t < nTiles; t += tilesPer) {
-            WorkItem w{c, c + 1, (int)t, (int)std::min<long long>(tilesPer, nTiles - t), partBase, (int)items.size(), 0};
+            WorkItem w{c, c + 1, (int)t, (int)std::min<long long>(tilesPer, nTiles - t), partBase, (int)items.size(), 1};
             rowBase.push_back(partBase);
             partBase += p.numTerms;
             items.push_back(w);
@@ -250,6 +250,7 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
     for (auto& g : gather) maxSlots = std::max(maxSlots, g.nSlots);
     gatherNA<<<dim3((maxSlots + 255) / 256, nComps), 256, 0, stream>>>((const GatherDesc*)(base + oGather), nComps, cm);
     MPGB_CUDA(cudaGetLastError());
+    countLaunches(stream, 1);
 
     if (coeffGrad && N == 0) MPGB_CUDA(cudaMemsetAsync(coeffGrad, 0, map.numCoeffs * sizeof(double), stream));
     if (N > 0 && (coeffGrad || outEval.data || outLogDet.data)) {

@@ -17,6 +17,7 @@
 
 #include "../../include/mpart_gb300.h"
 #include "mpgb_device.cuh"
+#include "mpgb_launch.h"
 
 namespace mpgb {
 namespace plain {
@@ -451,7 +452,9 @@ int mpgb_plain_fwd_adj(mpgb_plain* h, const double* coeffs, const double* pts, l
         plainKernel<<<h->blocks, h->threads, 0, s>>>(c, 3, pts, rs, N, nullptr, nullptr, h->dense, h->scratch);
         rowSumKernel<<<c.T, 256, 0, s>>>(h->dense, c.T, N, coeff_grad, 1);
     }
-    return cudaGetLastError() == cudaSuccess ? MPGB_OK : MPGB_ERR_CUDA;
+    const cudaError_t e = cudaGetLastError();
+    mpgb::countLaunches(s, (out_eval ? 1 : 0) + (out_logdet ? 1 : 0) + (coeff_grad ? 4 : 0));
+    return e == cudaSuccess ? MPGB_OK : MPGB_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -10,11 +10,14 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <sstream>
 #include <vector>
 
 #include "../../include/mpart_gb300.h"
 #include "../../include/mpart_gb300.hpp"
+#include "mpgb_launch.h"
+#include "mpgb_program.h"
 
 namespace mpgb {
 
@@ -181,12 +184,18 @@ struct KLStep {
     MonotoneMapBase& map;
     StridedMatrix pts;
     cudaStream_t s;
-    int mode;  // 0 batched (graph), 1 batched (direct launches), 2 one launch set per component
+    // 0 batched (graph), 1 batched (direct launches), 2 one fused launch set per
+    // component, 3 per component the reference objective's call sequence
+    // (Evaluate, LogDeterminant, CoeffGrad with sens = T and
+    // LogDeterminantCoeffGrad into dense outputs, then reductions).
+    int mode;
     double* dCoef;
     Pinned hCoef, hLoss, hGrad;
     Dev dLoss, dGrad;
+    std::unique_ptr<Dev> dT, dLd, dDenseT, dDenseL;  // mode 3 buffers
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    long long graphKernels = 0;  // kernel nodes of the captured step
     unsigned nc, no;
 
     // The step runs on a private non-blocking stream (a graph cannot be
@@ -197,6 +206,21 @@ struct KLStep {
           hGrad(m.numCoeffs), dLoss(m.outputDim), dGrad(m.numCoeffs), nc(m.numCoeffs), no(m.outputDim) {
         TR_CUDA(cudaStreamSynchronize(user));
         TR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        if (mode == 3) {
+            size_t maxTerms = 1;
+            for (auto& p : map.Parts()) {
+                if (!dynamic_cast<MonotoneMapBase*>(p.owner) || p.owner->numCoeffs != (unsigned)p.prog->numTerms)
+                    throw std::invalid_argument("KL mode 3 needs a map made of monotone components.");
+                maxTerms = std::max<size_t>(maxTerms, p.prog->numTerms);
+            }
+            const size_t n = (size_t)pts.cols;
+            dT.reset(new Dev(n));
+            dLd.reset(new Dev(n));
+            dDenseT.reset(new Dev(maxTerms * n));
+            dDenseL.reset(new Dev(maxTerms * n));
+            run();
+            return;
+        }
         // Warm-up (builds launch tables, sets kernel attributes) outside any capture.
         map.KLObjective(pts, dLoss.p, dGrad.p, mode == 2 ? 0 : -1, s);
         if (mode == 2)
@@ -210,6 +234,15 @@ struct KLStep {
             TR_CUDA(cudaStreamEndCapture(s, &graph));
             map.SetAsync(wasAsync);
             TR_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            size_t nNodes = 0;
+            TR_CUDA(cudaGraphGetNodes(graph, nullptr, &nNodes));
+            std::vector<cudaGraphNode_t> nodes(nNodes);
+            if (nNodes) TR_CUDA(cudaGraphGetNodes(graph, nodes.data(), &nNodes));
+            for (auto n : nodes) {
+                cudaGraphNodeType t;
+                TR_CUDA(cudaGraphNodeGetType(n, &t));
+                if (t == cudaGraphNodeTypeKernel) ++graphKernels;
+            }
         }
     }
     ~KLStep() {
@@ -222,7 +255,27 @@ struct KLStep {
     }
     void enqueue() {
         TR_CUDA(cudaMemcpyAsync(dCoef, hCoef.p, nc * sizeof(double), cudaMemcpyHostToDevice, s));
-        if (mode == 2) {
+        if (mode == 3) {
+            const long long n = pts.cols;
+            for (auto& p : map.Parts()) {
+                auto* comp = dynamic_cast<MonotoneMapBase*>(p.owner);
+                const int nt = p.prog->numTerms;
+                StridedMatrix sl(pts.data, p.prog->D, n, pts.rowStride, pts.colStride);
+                StridedMatrix T(dT->p, 1, n, n, 1), Ld(dLd->p, 1, n, n, 1);
+                StridedMatrix DT(dDenseT->p, nt, n, n, 1), DL(dDenseL->p, nt, n, n, 1);
+                // Asynchronous like the batched modes: an overflowing trial
+                // shows as a non-finite objective; run() clears the status.
+                const bool wasAsync = comp->Async();
+                comp->SetAsync(true);
+                comp->EvaluateImpl(sl, T, s);
+                comp->LogDeterminantImpl(sl, Ld, s);
+                comp->CoeffGradImpl(sl, T, DT, s);
+                comp->LogDeterminantCoeffGradImpl(sl, DL, s);
+                comp->SetAsync(wasAsync);
+                TR_CUDA(launchDenseKLReduce(dT->p, dLd->p, dDenseT->p, dDenseL->p, nt, n, dLoss.p + p.outRow,
+                                            dGrad.p + p.mapCoeffOffset, s));
+            }
+        } else if (mode == 2) {
             for (unsigned c = 0; c < map.NumMonotoneComponents(); ++c) map.KLObjective(pts, dLoss.p, dGrad.p, (int)c, s);
         } else {
             map.KLObjective(pts, dLoss.p, dGrad.p, -1, s);
@@ -233,6 +286,7 @@ struct KLStep {
     void run() {
         if (mode == 0) {
             TR_CUDA(cudaGraphLaunch(exec, s));
+            countLaunches(s, graphKernels);
         } else {
             const bool wasAsync = map.Async();
             map.SetAsync(true);
@@ -240,6 +294,8 @@ struct KLStep {
             map.SetAsync(wasAsync);
         }
         TR_CUDA(cudaStreamSynchronize(s));
+        if (mode == 3)
+            for (auto& p : map.Parts()) dynamic_cast<MonotoneMapBase*>(p.owner)->CheckStatus(s);
     }
 };
 
@@ -294,8 +350,10 @@ int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* op
             TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             stepMs += ms;
             ++steps;
-            int st = map->CheckStatus(step.s);
-            if (st & 1) throw IntegrandError("TrainMap: MonotoneIntegrand: g(df) overflowed during training.");
+            // A trial point whose integrand overflows gives its component a
+            // non-finite objective, which the line search rejects (it steps
+            // back); only an overflow at the starting point is an error.
+            map->CheckStatus(step.s);
             for (size_t c = 0; c < opt.size(); ++c)
                 if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
         }
@@ -303,10 +361,15 @@ int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* op
             std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        for (size_t c = 0; c < opt.size(); ++c)
+            if (!std::isfinite(opt[c].f()))
+                throw IntegrandError("TrainMap: MonotoneIntegrand: the objective is not finite at the starting "
+                                     "coefficients (g(df) overflowed).");
         std::vector<double> xf(map->numCoeffs);
-        double total = 0;
+        double total = 0, gn2 = 0;
         int iters = 0, evals = 0;
         for (size_t c = 0; c < opt.size(); ++c) {
+            gn2 += opt[c].gradNorm() * opt[c].gradNorm();
             std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c].x().data(), opt[c].x().size() * sizeof(double));
             if (loss_per_comp) loss_per_comp[c] = opt[c].f();
             total += opt[c].f();
@@ -321,6 +384,7 @@ int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* op
             res->steps = steps;
             res->ms_per_step = steps ? stepMs / steps : 0.0;
             res->total_ms = totalMs;
+            res->grad_norm = std::sqrt(gn2);
         }
         return MPGB_OK;
     } catch (IntegrandError const& e) {

@@ -30,13 +30,16 @@ struct CompDesc {
     const int32_t* rowOff;   // [D-1] first basis row of each leading coordinate
 };
 
-// A block's work: points [tile0*TPB, (tile0+nTiles)*TPB) of components [c0, c1).
+// A block's work: tiles tile0, tile0 + tileStride, ... (nTiles of them) of
+// components [c0, c1); tile t covers processing slots [t*TPB, (t+1)*TPB).
+// A stride equal to the number of items of the component spreads points that
+// were sorted by cost evenly over the items.
 struct WorkItem {
     int c0, c1;
     int tile0, nTiles;
     long long partialBase;  // first double of this item's partial row (reduced adjoint)
     int lossSlot;           // index into the loss partials (KL)
-    int pad_;
+    int tileStride;         // distance between consecutive tiles of the item (>= 1)
 };
 
 enum FusedFlags : int {
@@ -48,6 +51,13 @@ enum FusedFlags : int {
     kFlagInput = 32,        // combined input gradient into outInput (GradientImpl / LogDeterminantInputGradImpl)
     kFlagKL = 64,           // sens_c = T_c * sensScale, lsens = lsensScale, loss partials
     kFlagStatusArray = 128, // per-point status words
+    // Implicit differentiation of the inverse (one component per launch, in
+    // reverse output order): outInput holds the running back-substitution
+    // sums acc_j = sum_{m > j} lambda_m dT_m/dx_j on entry; the launch sets
+    // lambda = (sens - acc_D) / dT/dx_D, stores it in row D-1, adds
+    // lambda dT/dx_j to rows j < D-1 and reduces lambda dT/dc.
+    kFlagImplicit = 256,
+    kFlagImplicitFirst = 512,  // with kFlagImplicit: the sums start at zero (first launch)
 };
 
 struct FusedParams {
@@ -75,7 +85,8 @@ struct FusedParams {
     // perm[c * permStride + j] (items of one component only).
     const int* perm; long long permStride;
     double nugget;
-    int dmax, nBmax, depthMax, pad_;
+    int dmax, nBmax, depthMax;
+    int negRows;            // kFlagImplicit: rows [0, negRows) of outInput are negated when written
     QuadParams quad;
     BasisConsts bc;
 };

@@ -54,6 +54,49 @@ class MpartTorchAutograd(torch.autograd.Function):
         return grad, coeff_grad, None, None
 
 
+class MpartTorchInverse(torch.autograd.Function):
+    """Inverse with a backward pass by the implicit-function rule (one
+    InverseCoeffGrad call: dL/dc, dL/dr and dL/dx1 of the incoming gradient).
+    The reference's TorchConditionalMapBase.inverse is not differentiable."""
+
+    @staticmethod
+    def forward(ctx, x1, r, coeffs, f):
+        if coeffs is not None:
+            c = coeffs.detach().to(device=r.device, dtype=torch.float64).contiguous()
+            f.WrapCoeffs(c)
+            ctx.c = c
+        x1d = x1.detach().to(torch.float64)
+        rd = r.detach().to(torch.float64)
+        out = torch.zeros(f.outputDim, rd.shape[1], dtype=torch.float64, device=rd.device)
+        f.InverseImpl(x1d, rd, out)
+        ctx.f = f
+        ctx.save_for_backward(x1, r, coeffs, out)
+        return out.to(r.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        x1, r, coeffs, out = ctx.saved_tensors
+        f = ctx.f
+        if coeffs is not None:
+            f.WrapCoeffs(ctx.c)
+        extra = f.inputDim - f.outputDim
+        n = out.shape[1]
+        pts = torch.cat([x1.detach().to(torch.float64)[:extra].expand(extra, n), out], dim=0).contiguous()
+        w = grad_out.detach().to(torch.float64).contiguous()
+        want_c = coeffs is not None and coeffs.requires_grad
+        cg = torch.zeros(f.numCoeffs, dtype=torch.float64, device=out.device) if want_c else None
+        pg = torch.zeros(f.inputDim, n, dtype=torch.float64, device=out.device)
+        f.InverseCoeffGradImpl(pts, w, cg, pg)
+        g_x1 = None
+        if x1.requires_grad:
+            g_x1 = torch.zeros_like(x1, dtype=torch.float64)
+            g_x1[:extra] = pg[:extra] if x1.shape[1] == n else pg[:extra].sum(dim=1, keepdim=True)
+            g_x1 = g_x1.to(x1.dtype)
+        g_r = pg[extra:].to(r.dtype) if r.requires_grad else None
+        g_c = cg.to(coeffs.dtype) if want_c else None
+        return g_x1, g_r, g_c, None
+
+
 class TorchConditionalMapBase(torch.nn.Module):
 
     def __init__(self, f, store_coeffs=True, return_logdet=False, dtype=torch.double, device="cuda"):
@@ -78,13 +121,9 @@ class TorchConditionalMapBase(torch.nn.Module):
         return MpartTorchAutograd.apply(x.T, coeffs, self.f, False).T
 
     def inverse(self, x, r, coeffs=None):
+        """Inverse (bindings/python/package/torch.py inverse), differentiable in
+        coeffs, r and the conditioning columns of x by the implicit-function rule."""
         coeffs = self.coeffs if coeffs is None else coeffs
-        c = coeffs.detach().double().contiguous()
-        self.f.WrapCoeffs(c)
-        x = x.double()
-        r = r.double()
         if x.shape[1] != self.f.inputDim and (x.shape[1] + r.shape[1]) == self.f.inputDim:
             x = torch.hstack([x, r])
-        out = torch.zeros((self.f.outputDim, x.shape[0]), dtype=torch.float64, device=x.device)
-        self.f.InverseImpl(x.T, r.T, out)
-        return out.T
+        return MpartTorchInverse.apply(x.T, r.T, coeffs, self.f).T

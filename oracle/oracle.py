@@ -126,6 +126,7 @@ class OracleComponent:
         self.num_coeffs = self.num_terms
         self.input_dim = self.dim
         self.output_dim = 1
+        self.nugget = float(nugget)
         L = lib()
         d = self.dims if len(self.dims) else np.zeros(1, np.uint32)
         o = self.orders if len(self.orders) else np.zeros(1, np.uint32)
@@ -345,3 +346,29 @@ def kl_objective(tmap: OracleTriangularMap, coeffs, pts):
     gx = tmap.coeff_grad(coeffs, pts, -T) + tmap.logdet_coeff_grad(coeffs, pts)
     grad = (-1.0 / N) * gx.sum(axis=1)
     return loss, grad
+
+
+def inverse_coeff_grad(tmap: OracleTriangularMap, coeffs, pts, w):
+    """Implicit-function derivative of TriangularMap::InverseImpl
+    (src/TriangularMap.cpp:146-184; the reference itself does not
+    differentiate it).  pts = [x1; x] at the solution x = T^{-1}(x1, r), w the
+    weights of L = sum w * x.  Solves (dT/dx)^T lambda = w per point, last
+    component first: lambda_k = (w_k - sum_{m>k} lambda_m dT_m/dx_k) / dT_k/dx_k
+    with dT_k/dx_k = ContinuousDerivative + nugget (MonotoneComponent.h:487-531)
+    and the off-diagonal terms from GradientImpl (MonotoneComponent.h:824-874).
+    Returns (dL/dc = -sum_i lambda^T dT/dc, [dL/dx1; dL/dr] = [-lambda^T dT/dx1; lambda])."""
+    cs = tmap.split(coeffs)
+    N = pts.shape[1]
+    extra = tmap.input_dim - tmap.output_dim
+    acc = np.zeros((tmap.input_dim, N))
+    grad = np.zeros(tmap.num_coeffs)
+    for k in reversed(range(len(tmap.comps))):
+        c = tmap.comps[k]
+        D = c.input_dim
+        p = np.ascontiguousarray(pts[:D])
+        lam = (w[k] - acc[D - 1]) / (c.cont_derivative(cs[k], p) + c.nugget)
+        acc[D - 1] = lam
+        acc[:D - 1] += c.gradient(cs[k], p, lam)[:D - 1]
+        grad[tmap.offsets[k]:tmap.offsets[k + 1]] = -c.coeff_grad(cs[k], p, lam).sum(axis=1)
+    acc[:extra] *= -1.0
+    return grad, acc

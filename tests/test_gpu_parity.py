@@ -399,6 +399,30 @@ def test_kl_batched_equals_per_component(gpu):
     ms_direct = M.KLStepTime(tm, x, mode=1, steps=3)
     ms_unbatched = M.KLStepTime(tm, x, mode=2, steps=3)
     assert ms_graph > 0 and ms_direct > 0 and ms_unbatched > 0
+    # graph replays count their kernel nodes: the same launches as direct mode
+    counts = []
+    for mode in (0, 1):
+        n0 = M.launch_count()
+        M.KLStepTime(tm, x, mode=mode, steps=5)
+        counts.append(M.launch_count() - n0)
+    assert counts[0] == counts[1] > 0
+
+
+def test_launch_count_of_fused_call(c2):
+    """A fused call on one component launches the sort (3 kernels), the
+    coefficient gather, the fused kernel, the log-det row sum and the
+    fixed-order reduction of the partial rows."""
+    import torch
+    M, O, comp, oc, coef, x = c2
+    xs = T(x)
+    n = x.shape[1]
+    ev = torch.zeros(1, n, dtype=torch.float64, device="cuda")
+    ld = torch.zeros(n, dtype=torch.float64, device="cuda")
+    cg = torch.zeros(comp.numCoeffs, dtype=torch.float64, device="cuda")
+    n0 = M.launch_count()
+    comp.FusedForwardAdjointImpl(xs, sens=T(np.ones((1, n))), logdet_sens_scale=1.0, out_eval=ev, out_logdet=ld,
+                                 coeff_grad=cg)
+    assert M.launch_count() - n0 == 7
 
 
 def test_train_map_matches_oracle_objective(gpu, oracle):
@@ -422,6 +446,11 @@ def test_train_map_matches_oracle_objective(gpu, oracle):
         loss2, _ = M.TrainMap(tm2, T(x), max_iters=15, mode=mode)
         np.testing.assert_array_equal(loss2, loss)
         np.testing.assert_array_equal(tm2.CoeffMap(), coef)
+    # the reference objective's call sequence (dense outputs, separate
+    # reductions) sums in another order: the same objective to rounding
+    tm3 = M.CreateTriangular(3, 3, 3, opts(M, basis=2, pos=0, tol=1e-7))
+    loss3, _ = M.TrainMap(tm3, T(x), max_iters=15, mode=3)
+    np.testing.assert_allclose(loss3, loss, rtol=1e-10)
 
 
 def test_point_ordering_invariance_and_determinism(c2):
