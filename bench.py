@@ -87,10 +87,19 @@ def kl_train(M, dev):
     loss_g, r_g = M.TrainMap(tm, X, max_iters=KL_ITERS, mode=0)
     launches = M.launch_count() - l0
     trained = np.array(tm.CoeffMap())
-    ms = {m: M.KLStepTime(tm, X, mode=m, steps=10) for m in (0, 1, 2, 3)}
+    steps = {m: M.KLStepTime(tm, X, mode=m, steps=10, return_values=True) for m in (0, 1, 2, 3)}
+    ms = {m: v[0] for m, v in steps.items()}
 
     def rel(a, b):
         return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+    gscale = np.abs(steps[0][2]).max()
+    step_diff = {
+        "loss_max_rel_diff_reference_calls": rel(steps[3][1], steps[0][1]),
+        "grad_max_abs_diff_over_max_reference_calls": float(np.abs(steps[3][2] - steps[0][2]).max() / gscale),
+        "loss_max_rel_diff_per_component_fused": rel(steps[2][1], steps[0][1]),
+        "grad_max_abs_diff_over_max_per_component_fused": float(np.abs(steps[2][2] - steps[0][2]).max() / gscale),
+    }
 
     tm.SetCoeffs(np.zeros(tm.numCoeffs))
     loss_p, r_p = M.TrainMap(tm, X, max_iters=KL_ITERS, mode=2)
@@ -108,8 +117,10 @@ def kl_train(M, dev):
                                       "per_component_fused": ms[2], "per_component_reference_calls": ms[3]},
         "batched_speedup_vs_reference_calls": ms[3] / ms[0],
         "batched_speedup_vs_per_component_fused": ms[2] / ms[0],
-        "objective_max_rel_diff_vs_per_component_fused": rel(loss_g, loss_p),
-        "objective_max_rel_diff_vs_reference_calls": rel(loss_g, loss_r),
+        "step_values_at_trained_coeffs": step_diff,
+        "train_objective_max_rel_diff_vs_per_component_fused": rel(loss_g, loss_p),
+        "train_objective_max_rel_diff_vs_reference_calls": rel(loss_g, loss_r),
+        "train_objective_per_component_reference_calls": [float(v) for v in loss_r],
         "reference_calls_train_ms_per_step": float(r_r["ms_per_step"]),
     }, trained
 

@@ -239,12 +239,48 @@ int mpgb_train_map(mpgb_map* map, mpgb_matrix samples, const mpgb_train_options*
                    mpgb_train_result* result, void* stream);
 
 /* Device time of one KL objective + gradient step of all components in the given mode (see
- * mpgb_train_options.mode), averaged over `steps` steps after three warm-up steps. */
-int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream);
+ * mpgb_train_options.mode) at the map's coefficients, averaged over `steps` steps after three
+ * warm-up steps.  loss (outputDim) and grad (numCoeffs), host pointers that may be NULL,
+ * receive the objective and gradient of the last step. */
+int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
+                      double* grad, void* stream);
 
 /* FP64 throughput probe: DFMA chains over blocks x threads x iters x 8; writes the
  * kernel time in milliseconds (CUDA events on the stream). */
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms);
+
+/* ------------------------------------------------------------------------
+ * Batch of independent maps (no counterpart in the reference, which runs one
+ * map per call): forward, log-determinant and reduced coefficient adjoint of
+ * every map in one persistent launch.  Maps may differ in dimension, order and
+ * point count but share basis, rectifier and quadrature options; last-
+ * coordinate orders up to 8.  Every pointer passed to a batch call is device
+ * memory; arrays of matrices and of gradient pointers have one entry per map,
+ * and an entry with data == NULL is skipped (sens: no value term).
+ * ------------------------------------------------------------------------ */
+typedef struct mpgb_batch mpgb_batch;
+
+int mpgb_batch_create(mpgb_map* const* maps, int n, mpgb_batch** out);
+int mpgb_batch_destroy(mpgb_batch* batch);
+
+/* coeff_grad[m] (numCoeffs_m doubles) receives
+ * sum_i [sens_m dT_m/dc + logdet_sens_scale dlogdet_m/dc] over the points of map m. */
+int mpgb_batch_fwd_adj(mpgb_batch* batch, const mpgb_matrix* pts, const mpgb_matrix* sens, double logdet_sens_scale,
+                       const mpgb_matrix* out_eval, const mpgb_matrix* out_logdet, double* const* coeff_grad,
+                       void* stream);
+
+/* Autotuner: times, on these inputs, block sizes 64 and 128 and 1, 2, 4, 8 or 16
+ * tiles of points per work item for every (input dimension, order) bucket of
+ * the batch's components, and keeps the fastest; best_ms receives the device
+ * time of one launch with the chosen configuration. */
+int mpgb_batch_autotune(mpgb_batch* batch, const mpgb_matrix* pts, const mpgb_matrix* sens, double logdet_sens_scale,
+                        int reps, double* best_ms, void* stream);
+
+/* The tuning in use: block size, and tiles per item for each bucket (up to max_buckets entries). */
+int mpgb_batch_tuning(mpgb_batch* batch, int* tpb, int max_buckets, int* n_buckets, int* dims, int* orders,
+                      int* tiles);
+int mpgb_batch_set_tuning(mpgb_batch* batch, int tpb, int n_buckets, const int* dims, const int* orders,
+                          const int* tiles);
 
 /* Number of kernels this library has launched since it was loaded, over all
  * threads (graph replays count their kernel nodes; launches captured into a

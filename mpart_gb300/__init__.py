@@ -410,11 +410,75 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
                   "grad_norm": r.grad_norm}
 
 
-def KLStepTime(tmap: ConditionalMapBase, samples, mode=0, steps=10):
-    """Device milliseconds of one KL objective + gradient step (see TrainMap modes)."""
+def KLStepTime(tmap: ConditionalMapBase, samples, mode=0, steps=10, return_values=False):
+    """Device milliseconds of one KL objective + gradient step (see TrainMap
+    modes); with return_values, also the step's loss per component and gradient."""
     ms = C.c_double(0)
-    check(load().mpgb_kl_step_time(tmap._h, _mat(samples), int(mode), int(steps), C.byref(ms), _stream_of(samples)))
-    return ms.value
+    loss = np.zeros(tmap.outputDim)
+    grad = np.zeros(tmap.numCoeffs)
+    check(load().mpgb_kl_step_time(tmap._h, _mat(samples), int(mode), int(steps), C.byref(ms),
+                                   C.c_void_p(loss.ctypes.data), C.c_void_p(grad.ctypes.data), _stream_of(samples)))
+    return (ms.value, loss, grad) if return_values else ms.value
+
+
+class MapBatch:
+    """Many independent maps evaluated together (mpgb_batch_*): forward,
+    log-determinant and reduced coefficient adjoint of every map in one
+    persistent launch; points per work item from the autotuner.  All arrays
+    are CUDA float64 tensors, one per map."""
+
+    def __init__(self, maps: Sequence[ConditionalMapBase]):
+        self._maps = list(maps)
+        arr = (C.c_void_p * len(self._maps))(*[m._h for m in self._maps])
+        h = C.c_void_p()
+        check(load().mpgb_batch_create(arr, len(self._maps), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _capi._lib is not None:
+            _capi._lib.mpgb_batch_destroy(self._h)
+            self._h = None
+
+    def _mats(self, xs):
+        n = len(self._maps)
+        if xs is None:
+            return None
+        if len(xs) != n:
+            raise ValueError(f"expected {n} arrays, one per map")
+        return (_capi.mpgb_matrix * n)(*[_mat(x) for x in xs])
+
+    def FusedForwardAdjoint(self, pts, sens=None, logdet_sens_scale=0.0, out_eval=None, out_logdet=None,
+                            coeff_grad=None):
+        n = len(self._maps)
+        grads = None
+        if coeff_grad is not None:
+            grads = (C.c_void_p * n)(*[None if g is None else g.data_ptr() for g in coeff_grad])
+        check(load().mpgb_batch_fwd_adj(self._h, self._mats(pts), self._mats(sens), float(logdet_sens_scale),
+                                        self._mats(out_eval), self._mats(out_logdet), grads, _stream_of(*pts)))
+
+    def Autotune(self, pts, sens=None, logdet_sens_scale=0.0, reps=2):
+        """Times the candidate configurations on these inputs and keeps the
+        fastest; returns the device ms of one launch with it."""
+        ms = C.c_double(0)
+        check(load().mpgb_batch_autotune(self._h, self._mats(pts), self._mats(sens), float(logdet_sens_scale),
+                                         int(reps), C.byref(ms), _stream_of(*pts)))
+        return ms.value
+
+    def Tuning(self):
+        """(block size, {(input dim, order): tiles per item})."""
+        tpb, nb = C.c_int(0), C.c_int(0)
+        check(load().mpgb_batch_tuning(self._h, C.byref(tpb), 0, C.byref(nb), None, None, None))
+        d, o, t = (C.c_int * max(1, nb.value))(), (C.c_int * max(1, nb.value))(), (C.c_int * max(1, nb.value))()
+        check(load().mpgb_batch_tuning(self._h, C.byref(tpb), nb.value, C.byref(nb), d, o, t))
+        return tpb.value, {(d[i], o[i]): t[i] for i in range(nb.value)}
+
+    def SetTuning(self, tpb, tiles):
+        items = sorted(tiles.items())
+        n = len(items)
+        d = (C.c_int * max(1, n))(*[k[0] for k, _ in items])
+        o = (C.c_int * max(1, n))(*[k[1] for k, _ in items])
+        t = (C.c_int * max(1, n))(*[v for _, v in items])
+        check(load().mpgb_batch_set_tuning(self._h, int(tpb), n, d, o, t))
 
 
 class PlainComponent:

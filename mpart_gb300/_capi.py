@@ -92,10 +92,22 @@ SIGNATURES = {
     "mpgb_inverse_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
     "mpgb_launch_count": (C.c_longlong, []),
+    "mpgb_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "mpgb_batch_destroy": (C.c_int, [C.c_void_p]),
+    "mpgb_batch_fwd_adj": (C.c_int, [C.c_void_p, C.POINTER(mpgb_matrix), C.POINTER(mpgb_matrix), C.c_double,
+                                     C.POINTER(mpgb_matrix), C.POINTER(mpgb_matrix), C.POINTER(C.c_void_p),
+                                     C.c_void_p]),
+    "mpgb_batch_autotune": (C.c_int, [C.c_void_p, C.POINTER(mpgb_matrix), C.POINTER(mpgb_matrix), C.c_double, C.c_int,
+                                      C.POINTER(C.c_double), C.c_void_p]),
+    "mpgb_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mpgb_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int)]),
     "mpgb_train_options_default": (C.c_int, [C.POINTER(mpgb_train_options)]),
     "mpgb_train_map": (C.c_int, [_MAP, mpgb_matrix, C.POINTER(mpgb_train_options), C.c_void_p,
                                  C.POINTER(mpgb_train_result), C.c_void_p]),
-    "mpgb_kl_step_time": (C.c_int, [_MAP, mpgb_matrix, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    "mpgb_kl_step_time": (C.c_int, [_MAP, mpgb_matrix, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_void_p,
+                                    C.c_void_p, C.c_void_p]),
     "mpgb_plain_create": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
     "mpgb_plain_destroy": (C.c_int, [_MAP]),
     "mpgb_plain_num_terms": (C.c_int, [_MAP, _UP]),

@@ -304,56 +304,60 @@ MonotoneMapBase::MonotoneMapBase(unsigned int inDim, unsigned int outDim, unsign
 MonotoneMapBase::~MonotoneMapBase() = default;
 
 // Builds the launch tables on first use.
+// Quadrature rules and basis constants of a launch (both engines).
+void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b) {
+    // Quadrature rule: level = (unsigned) log2(quadPts - 2) (src/MapFactoryImpl4.cpp:18).
+    const unsigned level = (unsigned)std::log2((double)(o.quadPts - 2));
+    if (level < 1 || (int)level > kMaxQuadLevel)
+        throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
+    q.nCoarse = (1 << level) + 1;
+    q.nFine = (1 << (level + 1)) + 1;
+    ccRule(q.nCoarse, q.cWts, q.cPts);
+    ccRule(q.nFine, q.fWts, q.fPts);
+    q.maxSub = (int)o.quadMaxSub;
+    q.minSub = (int)o.quadMinSub;
+    q.absTol = o.quadAbsTol;
+    q.relTol = o.quadRelTol;
+    q.maxIntervals = 1LL << 24;
+
+    const bool norm = o.basisNorm;
+    for (int k = 0; k <= kMaxLastOrder; ++k) {
+        b.invNorm[k] = norm ? 1.0 / std::sqrt(std::sqrt(2.0 * kPiHost) * factorialU(k)) : 1.0;
+        double fact = 1.0;
+        for (int i = 2; i <= k; ++i) fact *= i;
+        b.hfScale[k] = std::pow(kPiHost, -0.25) * std::pow(std::pow(2.0, k) * fact, -0.5);
+    }
+    for (int i = 0; i < kMaxLastOrder + 8; ++i) {
+        b.hfR1[i] = std::sqrt(0.5 * (i - 1.0 > 0 ? i - 1.0 : 0.0));
+        b.hfR2[i] = i > 0 ? 1.0 / std::sqrt(0.5 * i) : 0.0;
+    }
+    b.piQuarter = std::pow(kPiHost, -0.25);
+    // phit_k(0).
+    {
+        double he[kMaxLastOrder + 1], H[kMaxLastOrder + 1];
+        he[0] = 1.0; he[1] = 0.0;
+        H[0] = 1.0; H[1] = 0.0;
+        for (int k = 2; k <= kMaxLastOrder; ++k) {
+            he[k] = -(k - 1.0) * he[k - 2];
+            H[k] = -2.0 * (k - 1.0) * H[k - 2];
+        }
+        b.v0[0] = 1.0;
+        for (int k = 1; k <= kMaxLastOrder; ++k) {
+            if (o.basisType == BasisTypes::HermiteFunctions)
+                b.v0[k] = (k == 1) ? 0.0 : b.hfScale[k - 2] * H[k - 2];
+            else
+                b.v0[k] = he[k] * b.invNorm[k];
+        }
+    }
+}
+
 void MonotoneMapBase::Prepare(cudaStream_t stream) {
     MapWorkspace& W = *ws_;
     if (!W.built) {
         int dev = 0;
         MPGB_CUDA(cudaGetDevice(&dev));
         MPGB_CUDA(cudaDeviceGetAttribute(&W.numSMs, cudaDevAttrMultiProcessorCount, dev));
-        // Quadrature rule: level = (unsigned) log2(quadPts - 2) (src/MapFactoryImpl4.cpp:18).
-        const unsigned level = (unsigned)std::log2((double)(opts_.quadPts - 2));
-        if (level < 1 || (int)level > kMaxQuadLevel)
-            throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
-        QuadParams& q = W.quad;
-        q.nCoarse = (1 << level) + 1;
-        q.nFine = (1 << (level + 1)) + 1;
-        ccRule(q.nCoarse, q.cWts, q.cPts);
-        ccRule(q.nFine, q.fWts, q.fPts);
-        q.maxSub = (int)opts_.quadMaxSub;
-        q.minSub = (int)opts_.quadMinSub;
-        q.absTol = opts_.quadAbsTol;
-        q.relTol = opts_.quadRelTol;
-        q.maxIntervals = 1LL << 24;
-        BasisConsts& b = W.bc;
-        const bool norm = opts_.basisNorm;
-        for (int k = 0; k <= kMaxLastOrder; ++k) {
-            b.invNorm[k] = norm ? 1.0 / std::sqrt(std::sqrt(2.0 * kPiHost) * factorialU(k)) : 1.0;
-            double fact = 1.0;
-            for (int i = 2; i <= k; ++i) fact *= i;
-            b.hfScale[k] = std::pow(kPiHost, -0.25) * std::pow(std::pow(2.0, k) * fact, -0.5);
-        }
-        for (int i = 0; i < kMaxLastOrder + 8; ++i) {
-            b.hfR1[i] = std::sqrt(0.5 * (i - 1.0 > 0 ? i - 1.0 : 0.0));
-            b.hfR2[i] = i > 0 ? 1.0 / std::sqrt(0.5 * i) : 0.0;
-        }
-        b.piQuarter = std::pow(kPiHost, -0.25);
-        // phit_k(0).
-        {
-            double he[kMaxLastOrder + 1], H[kMaxLastOrder + 1];
-            he[0] = 1.0; he[1] = 0.0;
-            H[0] = 1.0; H[1] = 0.0;
-            for (int k = 2; k <= kMaxLastOrder; ++k) {
-                he[k] = -(k - 1.0) * he[k - 2];
-                H[k] = -2.0 * (k - 1.0) * H[k - 2];
-            }
-            b.v0[0] = 1.0;
-            for (int k = 1; k <= kMaxLastOrder; ++k) {
-                if (opts_.basisType == BasisTypes::HermiteFunctions)
-                    b.v0[k] = (k == 1) ? 0.0 : b.hfScale[k - 2] * H[k - 2];
-                else
-                    b.v0[k] = he[k] * b.invNorm[k];
-            }
-        }
+        buildLaunchConstants(opts_, W.quad, W.bc);
         // Component descriptors.
         W.hostComps.clear();
         W.hostGather.clear();
@@ -1150,8 +1154,8 @@ using namespace mpgb;
 namespace mpgb {
 int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
                  mpgb_train_result* res, void* stream, char* err, int errLen);
-int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream,
-                   char* err, int errLen);
+int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
+                   double* grad, void* stream, char* err, int errLen);
 }
 
 namespace {
@@ -1593,10 +1597,13 @@ int mpgb_train_map(mpgb_map* map, mpgb_matrix samples, const mpgb_train_options*
     return rc;
 }
 
-int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream) {
+int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
+                      double* grad, void* stream) {
     char err[512] = {0};
     int rc = MPGB_OK;
-    int g = guard([&] { rc = klStepTimeImpl(mono(map), samples, mode, steps, ms_per_step, stream, err, sizeof(err)); });
+    int g = guard([&] {
+        rc = klStepTimeImpl(mono(map), samples, mode, steps, ms_per_step, loss, grad, stream, err, sizeof(err));
+    });
     if (g != MPGB_OK) return g;
     if (rc != MPGB_OK) g_lastError = err;
     return rc;

@@ -8,6 +8,8 @@ namespace mpgb {
 
 template <int BASIS, int POS, int PMAX>
 cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int needE, cudaStream_t stream);
+template <int BASIS, int POS>
+cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int* counter, cudaStream_t stream);
 template <int BASIS, int POS, int PMAX>
 cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t stream);
 
@@ -221,6 +223,26 @@ cudaError_t launchFused(int basis, int pos, int pmax, const FusedParams& prm, in
     }
     if (pos == kPosSoftPlus) return launchFusedBP<kBasisHermiteFunctions, kPosSoftPlus>(prm, pmax, nItems, needJ, needE, stream);
     return launchFusedBP<kBasisHermiteFunctions, kPosExp>(prm, pmax, nItems, needJ, needE, stream);
+}
+
+int batchOrderClass(int p) {
+    if (p <= 2) return 2;
+    if (p <= 4) return 4;
+    if (p <= 6) return 6;
+    if (p <= 8) return 8;
+    return -1;
+}
+
+cudaError_t launchBatch(int basis, int pos, const FusedParams& prm, int nItems, int pmaxClass, int* counter,
+                        cudaStream_t stream) {
+    if (basis == kBasisProbHermite) {
+        if (pos == kPosSoftPlus)
+            return launchBatchP<kBasisProbHermite, kPosSoftPlus>(prm, nItems, pmaxClass, counter, stream);
+        return launchBatchP<kBasisProbHermite, kPosExp>(prm, nItems, pmaxClass, counter, stream);
+    }
+    if (pos == kPosSoftPlus)
+        return launchBatchP<kBasisHermiteFunctions, kPosSoftPlus>(prm, nItems, pmaxClass, counter, stream);
+    return launchBatchP<kBasisHermiteFunctions, kPosExp>(prm, nItems, pmaxClass, counter, stream);
 }
 
 cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm, int nBlocks, cudaStream_t stream) {

@@ -17,6 +17,7 @@
 // No atomics on values: reduced adjoints go through per-item partial rows and
 // a fixed-order reduction, so results are bitwise reproducible.
 #pragma once
+#include <algorithm>
 #include <cstdio>
 #include "mpgb_types.h"
 #include "mpgb_launch.h"
@@ -278,14 +279,18 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
 // --------------------------------------------------------------------------
 // The fused kernel.
 // --------------------------------------------------------------------------
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
-__global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ FusedParams prm) {
-    extern __shared__ double smem[];
+// Point data of a work item: the launch-wide fields of FusedParams, or (in a
+// batch of maps) the entry of the item's component in prm.ioTable.
+#define MPGB_IO(f) (BATCH ? tio->f : prm.f)
+
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE, bool BATCH>
+__device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem& item, double* smem) {
     const int tid = threadIdx.x;
     const int tpb = blockDim.x;
     const bool inputMode = (prm.flags & kFlagInput) != 0;
     const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, inputMode);
-    const WorkItem item = prm.items[blockIdx.x];
+    const PointIO* tio = BATCH ? &prm.ioTable[item.c0] : nullptr;
+    (void)tio;
     const int flags = prm.flags;
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const double ninf = __longlong_as_double(0xfff0000000000000ULL);
@@ -293,13 +298,13 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
     for (int tj = 0; tj < item.nTiles; ++tj) {
         const int tile = item.tile0 + tj * item.tileStride;
         const long long slotIdx = (long long)tile * tpb + tid;
-        const bool active = slotIdx < prm.N;
-        const long long i = (active && prm.perm) ? (long long)prm.perm[item.c0 * prm.permStride + slotIdx] : slotIdx;
+        const bool active = slotIdx < MPGB_IO(N);
+        const long long i = (active && MPGB_IO(perm)) ? (long long)MPGB_IO(perm)[item.c0 * MPGB_IO(permStride) + slotIdx] : slotIdx;
         int st = 0;
         // Coordinates of the tile (the largest component of the range reads the most).
         const int dneed = prm.comps[item.c1 - 1].D;
         for (int d = 0; d < dneed; ++d)
-            L.X[d * tpb + tid] = active ? prm.pts[d * prm.ptsRs + i * prm.ptsCs] : 0.0;
+            L.X[d * tpb + tid] = active ? MPGB_IO(pts)[d * MPGB_IO(ptsRs) + i * MPGB_IO(ptsCs)] : 0.0;
         double logdetSum = 0.0;
         double lossAcc = 0.0;
         if (inputMode) {
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
             const double T = R.Ih + f0;
             const double logdet = (gx <= 0.0) ? ninf : log(gx);
 
-            if ((flags & kFlagEval) && active) prm.outEval[(long long)c.outRow * prm.evalRs + i * prm.evalCs] = T;
+            if ((flags & kFlagEval) && active && MPGB_IO(outEval)) MPGB_IO(outEval)[(long long)c.outRow * MPGB_IO(evalRs) + i * MPGB_IO(evalCs)] = T;
             if (flags & kFlagLogDet) logdetSum += logdet;
 
             // Per-point adjoint weights.
@@ -353,7 +358,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
                 lsens = prm.lsensScale;
                 if (active) lossAcc += 0.5 * T * T - logdet;
             } else {
-                if (prm.sens && active) sens = prm.sens[(long long)c.outRow * prm.sensRs + i * prm.sensCs];
+                if (MPGB_IO(sens) && active) sens = MPGB_IO(sens)[(long long)c.outRow * MPGB_IO(sensRs) + i * MPGB_IO(sensCs)];
                 if (flags & (kFlagCoefReduced | kFlagInput))
                     lsens = prm.lsens ? (active ? prm.lsens[i * prm.lsensStride] : 0.0) : prm.lsensScale;
                 if (flags & kFlagImplicit) {
@@ -483,7 +488,7 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
         }  // components
 
         if (active) {
-            if (flags & kFlagLogDet) prm.outLogDet[i * prm.logDetStride] = logdetSum;
+            if (flags & kFlagLogDet) MPGB_IO(outLogDet)[i * MPGB_IO(logDetStride)] = logdetSum;
             if (inputMode) {
                 const int dneed2 = prm.comps[item.c1 - 1].D;
                 for (int d = 0; d < dneed2; ++d) {
@@ -510,6 +515,41 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
     }
     (void)nan;
 }
+
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+__global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ FusedParams prm) {
+    extern __shared__ double smem[];
+    fusedBody<BASIS, POS, PMAX, NEEDJ, NEEDE, false>(prm, prm.items[blockIdx.x], smem);
+}
+
+// Persistent launch over the work items of a batch of maps (one component of
+// one map per item, items in decreasing cost): each block takes the next item
+// from a counter until none is left.  Every item owns its outputs (output
+// rows, log-det scratch row, partial row), so results do not depend on which
+// block runs it.  The item's component selects the body compiled for the
+// smallest order class >= its last-coordinate order.  At most 128 threads a
+// block and 4 blocks an SM: the order-6 and order-8 bodies spill a little
+// there, the order-2 and order-4 bodies (most items) keep four blocks.
+template <int BASIS, int POS>
+__global__ void __launch_bounds__(128, 4) batchKernel(const __grid_constant__ FusedParams prm, int nItems,
+                                                   int* counter) {
+    extern __shared__ double smem[];
+    __shared__ int next;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(counter, 1);
+        __syncthreads();
+        const int k = next;
+        __syncthreads();
+        if (k >= nItems) break;
+        const WorkItem item = prm.items[k];
+        const int P = prm.comps[item.c0].P;
+        if (P <= 2) fusedBody<BASIS, POS, 2, true, false, true>(prm, item, smem);
+        else if (P <= 4) fusedBody<BASIS, POS, 4, true, false, true>(prm, item, smem);
+        else if (P <= 6) fusedBody<BASIS, POS, 6, true, false, true>(prm, item, smem);
+        else fusedBody<BASIS, POS, 8, true, false, true>(prm, item, smem);
+    }
+}
+#undef MPGB_IO
 
 // --------------------------------------------------------------------------
 // Inverse: all components of the map, in order, for a tile of points
@@ -683,6 +723,25 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
     if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, true>);
     if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, false>);
     return run(fusedKernel<BASIS, POS, PMAX, false, false>);
+}
+
+// Persistent batch launch: as many blocks as fit on the device at once (at
+// most one per item); `counter` must be zero on entry.
+template <int BASIS, int POS>
+cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int* counter, cudaStream_t stream) {
+    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, pmaxClass, false);
+    auto kern = batchKernel<BASIS, POS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int perSM = 0, dev = 0, nSM = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, prm.tpb, smem)) != cudaSuccess) return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const int grid = std::max(1, std::min(nItems, std::max(1, perSM) * nSM));
+    kern<<<grid, prm.tpb, smem, stream>>>(prm, nItems, counter);
+    e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
 }
 
 template <int BASIS, int POS, int PMAX>

@@ -13,6 +13,13 @@ size_t fusedSmemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool
 cudaError_t launchFused(int basis, int pos, int pmax, const FusedParams& prm, int nItems, int needJ, int needE,
                         cudaStream_t stream);
 cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm, int nBlocks, cudaStream_t stream);
+// Batch of maps: one persistent launch over prm.items (forward, log-det and
+// reduced coefficient adjoint; point data in prm.ioTable).  Components of
+// last-coordinate order p run the body of order class batchOrderClass(p)
+// (2, 4, 6 or 8; -1 above 8); pmaxClass is the largest class in the batch.
+int batchOrderClass(int p);
+cudaError_t launchBatch(int basis, int pos, const FusedParams& prm, int nItems, int pmaxClass, int* counter,
+                        cudaStream_t stream);
 cudaError_t launchGather(const int32_t* slotGlobalTerm, int nSlots, const double* coeffs, double* cm,
                          cudaStream_t stream);
 cudaError_t launchReduceRows(const double* part, const long long* rowBase, int nRows, int nTerms, double scale,

@@ -30,6 +30,9 @@ struct CudaError : public std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// Quadrature rules (AdaptiveClenshawCurtis) and basis constants for a launch.
+void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b);
+
 // ---------------------------------------------------------------------------
 // Component program: the multi-index set reorganised as a prefix tree over
 // the leading coordinates (see mpgb_device.cuh for the factorisation).

@@ -206,6 +206,8 @@ struct KLStep {
           hGrad(m.numCoeffs), dLoss(m.outputDim), dGrad(m.numCoeffs), nc(m.numCoeffs), no(m.outputDim) {
         TR_CUDA(cudaStreamSynchronize(user));
         TR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        // Every step uploads hCoef: start from the map's current coefficients.
+        TR_CUDA(cudaMemcpy(hCoef.p, dCoef, nc * sizeof(double), cudaMemcpyDefault));
         if (mode == 3) {
             size_t maxTerms = 1;
             for (auto& p : map.Parts()) {
@@ -399,8 +401,8 @@ int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* op
     }
 }
 
-int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, void* stream,
-                           char* err, int errLen) {
+int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
+                   double* grad, void* stream, char* err, int errLen) {
     try {
         auto* map = static_cast<MonotoneMapBase*>(mapObj);
         if (!map || steps <= 0) throw std::invalid_argument("bad argument");
@@ -426,6 +428,8 @@ int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, doubl
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         *ms_per_step = tot / steps;
+        if (loss) std::memcpy(loss, step.hLoss.p, map->outputDim * sizeof(double));
+        if (grad) std::memcpy(grad, step.hGrad.p, map->numCoeffs * sizeof(double));
         return MPGB_OK;
     } catch (std::exception const& e) {
         if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }

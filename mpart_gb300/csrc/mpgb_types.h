@@ -60,6 +60,17 @@ enum FusedFlags : int {
     kFlagImplicitFirst = 512,  // with kFlagImplicit: the sums start at zero (first launch)
 };
 
+// Point data of one component in a batch of maps (the launch-wide fields of
+// FusedParams with the same names, per component).
+struct PointIO {
+    const double* pts; long long ptsRs, ptsCs;
+    long long N;
+    const double* sens; long long sensRs, sensCs;
+    double* outEval; long long evalRs, evalCs;
+    double* outLogDet; long long logDetStride;
+    const int* perm; long long permStride;
+};
+
 struct FusedParams {
     const CompDesc* comps;
     const WorkItem* items;
@@ -84,6 +95,7 @@ struct FusedParams {
     // Optional processing order: point index of slot j for component c is
     // perm[c * permStride + j] (items of one component only).
     const int* perm; long long permStride;
+    const PointIO* ioTable;  // batch launches: point data per component (indexed by WorkItem::c0)
     double nugget;
     int dmax, nBmax, depthMax;
     int negRows;            // kFlagImplicit: rows [0, negRows) of outInput are negated when written

@@ -395,10 +395,15 @@ def test_kl_batched_equals_per_component(gpu):
     tm.SetCoeffs(np.random.default_rng(5).normal(0.0, 0.01, tm.numCoeffs))
     x = T(banana(5000, 12))
     lb, gb = tm.KLObjective(x)
-    ms_graph = M.KLStepTime(tm, x, mode=0, steps=3)  # graph replay
-    ms_direct = M.KLStepTime(tm, x, mode=1, steps=3)
-    ms_unbatched = M.KLStepTime(tm, x, mode=2, steps=3)
-    assert ms_graph > 0 and ms_direct > 0 and ms_unbatched > 0
+    lb, gb = H(lb), H(gb)
+    res = {m: M.KLStepTime(tm, x, mode=m, steps=3, return_values=True) for m in (0, 1, 2, 3)}
+    for m in (0, 1, 2):
+        assert res[m][0] > 0
+        np.testing.assert_array_equal(res[m][1], lb)
+        np.testing.assert_array_equal(res[m][2], gb)
+    # the reference objective's call sequence (dense outputs): same values to rounding
+    assert_parity(res[3][1], lb, what="KL loss, reference call sequence")
+    assert_parity(res[3][2], gb, floor=1e-3, what="KL gradient, reference call sequence")
     # graph replays count their kernel nodes: the same launches as direct mode
     counts = []
     for mode in (0, 1):
