@@ -125,6 +125,155 @@ def kl_train(M, dev):
     }, trained
 
 
+def batch_specs(n_maps=64, seed=17):
+    """Batched-maps workload: n_maps triangular maps (inputDim = outputDim),
+    dims uniform in 2..16, total orders uniform in 2..6, point counts
+    log-uniform in [1e3, 2e5]."""
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(2, 17, n_maps)
+    orders = rng.integers(2, 7, n_maps)
+    npts = np.exp(rng.uniform(np.log(1e3), np.log(2e5), n_maps)).astype(int)
+    return list(zip(dims.tolist(), orders.tolist(), npts.tolist()))
+
+
+def batch_maps(M, dev, autotune=True):
+    """64 uneven maps: forward + log-determinant + coefficient adjoint of every
+    map as one persistent launch (before and after autotuning) against one
+    fused call per map; gradients compared."""
+    import torch
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=TOL, quadRelTol=TOL,
+                        quadMaxSub=MAXSUB)
+    specs = batch_specs()
+    rng = np.random.default_rng(18)
+    maps, pts, sens = [], [], []
+    for d, o, n in specs:
+        tm = M.CreateTriangular(d, d, o, opts)
+        tm.SetCoeffs(rng.normal(0.0, 0.05, tm.numCoeffs))
+        maps.append(tm)
+        pts.append(torch.as_tensor(rng.standard_normal((d, n)), device=dev))
+        sens.append(torch.as_tensor(rng.standard_normal((d, n)), device=dev))
+    z = lambda *s: torch.zeros(*s, dtype=torch.float64, device=dev)
+    ev = [z(m.outputDim, p.shape[1]) for m, p in zip(maps, pts)]
+    ld = [z(p.shape[1]) for p in pts]
+    cg = [z(m.numCoeffs) for m in maps]
+    cg1 = [z(m.numCoeffs) for m in maps]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def per_map():
+        for m, p, s, e, l, g in zip(maps, pts, sens, ev, ld, cg1):
+            m.FusedForwardAdjointImpl(p, sens=s, logdet_sens_scale=1.0, out_eval=e, out_logdet=l, coeff_grad=g)
+
+    def timed(f, reps=3):
+        f()
+        torch.cuda.synchronize()
+        best = 1e300
+        for _ in range(reps):
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    B = M.MapBatch(maps)
+    batch = lambda: B.FusedForwardAdjoint(pts, sens, 1.0, ev, ld, cg)
+    ms_single = timed(per_map)
+    ms_default = timed(batch)
+    out = {"workload": "64 TriangularMaps, dims uniform 2..16, total orders uniform 2..6, points log-uniform in "
+                       "[1e3, 2e5], ProbHermite + SoftPlus, ACC tol 1e-6; forward + LogDeterminant + coefficient "
+                       "adjoint of every map",
+           "maps": len(maps), "points": int(sum(n for _, _, n in specs)),
+           "coefficients": int(sum(m.numCoeffs for m in maps)),
+           "per_map_fused_calls_ms": ms_single, "batch_ms_default_tuning": ms_default}
+    if autotune:
+        t0 = time.perf_counter()
+        B.Autotune(pts, sens, 1.0, reps=1)
+        out["autotune_s"] = time.perf_counter() - t0
+        tpb, tiles = B.Tuning()
+        out["tuning"] = {"block": tpb, "tiles_per_item": {f"d{d}_o{o}": t for (d, o), t in sorted(tiles.items())}}
+    l0 = M.launch_count()
+    ms_tuned = timed(batch)
+    out["batch_ms"] = ms_tuned
+    out["batch_gpu_launches_per_call"] = (M.launch_count() - l0) // 4
+    out["points_per_s"] = out["points"] / (ms_tuned * 1e-3)
+    out["speedup_vs_per_map_calls"] = ms_single / ms_tuned
+    worst = 0.0
+    for a, b in zip(cg, cg1):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        worst = max(worst, float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)))
+    out["grad_max_abs_diff_over_max_vs_per_map"] = worst
+    return out
+
+
+INV_DIM, INV_ORDER, INV_N, INV_TOL, INV_XTOL = 16, 3, 4_000_000, 1e-8, 1e-10
+
+
+def inverse_implicit(M, dev, cpu_seconds=8.0):
+    """Inverse at scale with implicit differentiation: a 16-D TriangularMap of
+    total order 3 (969 terms in the last component), ProbHermite + SoftPlus,
+    tol 1e-8, coefficients N(0, 0.03^2); 4,000,000 targets r ~ N(0, I_16);
+    Inverse to xtol 1e-10, then the coefficient gradient (and dL/dr) of the
+    random linear functional L = sum w * x by the implicit-function rule."""
+    import torch
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=INV_TOL, quadRelTol=INV_TOL,
+                        quadMaxSub=MAXSUB)
+    tm = M.CreateTriangular(INV_DIM, INV_DIM, INV_ORDER, opts)
+    coef = np.random.default_rng(31).normal(0.0, 0.03, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    g = torch.Generator(device=dev)
+    g.manual_seed(32)
+    r = torch.randn(INV_DIM, INV_N, dtype=torch.float64, device=dev, generator=g)
+    w = torch.randn(INV_DIM, INV_N, dtype=torch.float64, device=dev, generator=g)
+    x1 = torch.zeros(0, INV_N, dtype=torch.float64, device=dev)
+    x = torch.zeros(INV_DIM, INV_N, dtype=torch.float64, device=dev)
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device=dev)
+    pg = torch.zeros(INV_DIM, INV_N, dtype=torch.float64, device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(f, reps=2):
+        f()
+        torch.cuda.synchronize()
+        best = 1e300
+        for _ in range(reps):
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    ms_inv = timed(lambda: tm.InverseImpl(x1, r, x, xtol=INV_XTOL, ytol=INV_XTOL))
+    ok = ~torch.isnan(x).any(dim=0)
+    xs, ws = x[:, ok].contiguous(), w[:, ok].contiguous()
+    ms_grad = timed(lambda: tm.InverseCoeffGradImpl(xs, ws, cg, pg[:, :xs.shape[1]]))
+    out = {"workload": f"TriangularMap {INV_DIM}-D, total order {INV_ORDER} ({tm.numCoeffs} coefficients, 969 in the "
+                       f"last component), ProbHermite + SoftPlus, ACC tol {INV_TOL}; {INV_N} targets r ~ N(0, I); "
+                       f"Inverse to xtol {INV_XTOL}, then dL/dc and dL/dr of L = sum w * x (implicit rule)",
+           "points": INV_N, "inverse_ms": ms_inv, "inverse_points_per_s": INV_N / (ms_inv * 1e-3),
+           "no_root_fraction": float(1.0 - ok.double().mean().item()),
+           "implicit_grad_ms": ms_grad, "implicit_grad_points_per_s": xs.shape[1] / (ms_grad * 1e-3),
+           "coeff_grad_norm": float(cg.norm().item())}
+    # the oracle's Inverse on a bounded sample of the same targets (host cores)
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    om = O.OracleTriangularMap(INV_DIM, INV_DIM, INV_ORDER, abs_tol=INV_TOL, rel_tol=INV_TOL, max_sub=MAXSUB)
+    rh = r[:, :20000].cpu().numpy()
+    n = 200
+    t0 = time.perf_counter()
+    om.inverse(coef, np.zeros((0, n)), rh[:, :n], INV_XTOL, INV_XTOL)
+    dt = time.perf_counter() - t0
+    n2 = int(min(rh.shape[1], max(n, n * cpu_seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    om.inverse(coef, np.zeros((0, n2)), rh[:, :n2], INV_XTOL, INV_XTOL)
+    dt = time.perf_counter() - t0
+    out["cpu_inverse"] = {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
+                          "sample": f"first {n2} targets, the oracle's Inverse"}
+    out["inverse_speedup_vs_cpu"] = out["inverse_points_per_s"] / out["cpu_inverse"]["points_per_s"]
+    return out
+
+
 def kl_cpu_step_ms(coeffs, target_seconds=8.0):
     """The oracle's KL step (every component's FastGaussianReverseKLObjective
     value and gradient, src/MapObjective.cpp:185-234, as TrainMap evaluates
@@ -475,6 +624,10 @@ def run_gpu(args):
         kl["cpu_step"]["speedup_graph"] = (kl["cpu_step"]["ms_per_step"] /
                                            kl["step_ms_at_trained_coeffs"]["graph_batched"])
         line["kl_train"] = kl
+    if not args.no_batch:
+        line["batch_maps"] = batch_maps(M, dev)
+    if not args.no_inverse:
+        line["inverse_implicit"] = inverse_implicit(M, dev)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -514,6 +667,8 @@ def main():
     ap.add_argument("--points", type=int, default=NPTS)
     ap.add_argument("--profile", action="store_true", help="fused step only (for profilers)")
     ap.add_argument("--no-kl", action="store_true", help="skip the KL training workload")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
+    ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
     ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()

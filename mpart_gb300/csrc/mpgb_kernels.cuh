@@ -583,6 +583,17 @@ struct InverseEval {
     __device__ double operator()(double x) const {
         return integrateValueNI<BASIS, POS, PMAX>(A, P, x, Q, bc, nugget, st) + f0;
     }
+    // dT/dx_D = g(df(x)) + nugget: no quadrature.
+    __device__ double slope(double x) const {
+        double d1[PMAX + 1];
+        lastBasis<BASIS, PMAX, false, true, false>(x, P, *bc, nullptr, d1, nullptr);
+        double df = 0.0;
+#pragma unroll
+        for (int k = 0; k <= PMAX; ++k) df = fma(A.a[k], d1[k], df);
+        double g, gp;
+        posEval<POS>(df, g, gp);
+        return g + nugget;
+    }
 };
 
 template <class F>
@@ -618,21 +629,20 @@ __device__ void findBracket(const F& f, double& xlb, double& ylb, double& xub, d
     }
 }
 
-__device__ __forceinline__ double findXITP(double xlb, double xub, double ylb, double yub, double k1, double k2,
-                                           double nhalf, double n0, int it, double xtol) {
-    const double xb = 0.5 * (xub + xlb);
-    double xf = (xub * ylb - xlb * yub) / (ylb - yub);
-    const double sigma = ((xb - xf) > 0) ? 1.0 : -1.0;
-    const double delta = fmin(k1 * pow((xub - xlb), k2), fabs(xb - xf));
-    xf += delta * sigma;
-    const double rho = fmin(xtol * pow(2.0, nhalf + n0 - it) - 0.5 * (xub - xlb), fabs(xf - xb));
-    return xb - sigma * rho;
-}
-
+// Root of f(x) = yd for a monotone f (MonotoneComponent::InverseImpl with
+// RootFinding::InverseSingleBracket, RootFinding.h:125-178): the reference's
+// bracket search (same evaluations, so the same points have no bracket and
+// give NaN), then the bracket is closed by a safeguarded Newton iteration
+// with the exact slope dT/dx_D = g(df) + nugget instead of ITP.  Every
+// evaluation narrows the bracket; a Newton step that leaves it, or two steps
+// that do not halve it, give way to bisection.  The stopping rules are the
+// reference's: |f(x) - yd| < ftol returns x; a bracket narrower than xtol (or
+// whose values differ by less than ftol) returns its midpoint.  The answer
+// therefore meets the reference's tolerance; it is not the ITP iterate itself.
 template <class F>
 __device__ double inverseSingleBracket(double yd, const F& f, double x0, double xtol, double ftol, int& info) {
     const unsigned maxIts = 10000;
-    double xlb, xub, ylb, yub, xc, yc;
+    double xlb, xub, ylb, yub;
     info = 0;
     xlb = xub = x0;
     ylb = yub = f(xlb);
@@ -642,17 +652,26 @@ __device__ double inverseSingleBracket(double yd, const F& f, double x0, double 
         info = -2;
         return __longlong_as_double(0x7ff8000000000000ULL);
     }
-    const double k1 = 0.1, k2 = 2.0;
-    const double nhalf = ceil(log2(0.5 * (xub - xlb) / xtol));
-    const double n0 = 1.0;
-    unsigned it;
-    for (it = 0; it < maxIts; ++it) {
-        xc = findXITP(xlb, xub, ylb, yub, k1, k2, nhalf, n0, (int)it, xtol);
-        yc = f(xc);
+    if (fabs(ylb - yd) < ftol) return xlb;
+    if (fabs(yub - yd) < ftol) return xub;
+    if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) return 0.5 * (xub + xlb);
+    // Start from the secant point of the bracket.
+    double xc = xlb + (yd - ylb) * (xub - xlb) / (yub - ylb);
+    if (!(xc > xlb && xc < xub)) xc = 0.5 * (xlb + xub);
+    double width = xub - xlb, widthPrev = 2.0 * width;
+    for (unsigned it = 0; it < maxIts; ++it) {
+        const double yc = f(xc);
         if (fabs(yc - yd) < ftol) return xc;
-        else if (yc > yd) { xub = xc; yub = yc; }
+        if (yc > yd) { xub = xc; yub = yc; }
         else { xlb = xc; ylb = yc; }
         if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) break;
+        const double w = xub - xlb;
+        double xn = xc - (yc - yd) / f.slope(xc);
+        // Bisection when Newton leaves the bracket or the bracket shrinks too slowly.
+        if (!(xn > xlb && xn < xub) || w > 0.5 * widthPrev) xn = 0.5 * (xlb + xub);
+        widthPrev = width;
+        width = w;
+        xc = xn;
     }
     return 0.5 * (xub + xlb);
 }

@@ -60,8 +60,36 @@ def _opts(M, basis=0, pos=1, tol=1e-6):
                         quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=tol, quadRelTol=tol)
 
 
+def _inverse_bound(om, coef, x1, xi, r, xtol, ytol, qtol):
+    """Bound on the difference of two inverses that both meet the reference's
+    stopping rules, per entry: 2 (xtol + (ytol + qtol (1 + |r|)) / dT_k/dx_k)
+    with the slope at the reference solution.  The quadrature term is there
+    because the adaptive T(x) is monotone only up to its quadrature error
+    (the subdivision changes with x), so its root is defined to that error
+    divided by the slope; two correct solvers may stop at different roots."""
+    cs = om.split(coef)
+    extra = om.input_dim - om.output_dim
+    full = np.vstack([x1[:extra], np.nan_to_num(xi)])
+    bound = np.zeros_like(xi)
+    for k, c in enumerate(om.comps):
+        slope = c.cont_derivative(cs[k], np.ascontiguousarray(full[:c.input_dim]))
+        bound[k] = 2.0 * (xtol + (ytol + qtol * (1.0 + np.abs(r[k]))) / np.maximum(slope, 1e-300))
+    return bound
+
+
+def _assert_within(got, ref, bound, mask=None, what=""):
+    ok = np.abs(got - ref) <= bound
+    if mask is not None:
+        ok |= ~mask
+    if not ok.all():
+        ratio = np.where(ok, 0.0, np.abs(got - ref) / bound)
+        i = np.unravel_index(np.argmax(ratio), ratio.shape)
+        raise AssertionError(f"{what}: {np.count_nonzero(~ok)} entries outside the solver bound; worst at {i}: "
+                             f"gpu={got[i]!r} reference={ref[i]!r} bound={bound[i]!r}")
+
+
 @pytest.mark.gpu
-def test_gpu_matches_golden_c1(gpu):
+def test_gpu_matches_golden_c1(gpu, oracle):
     M = gpu
     g = load("c1")
     tm = M.CreateTriangular(2, 2, 3, _opts(M))
@@ -74,10 +102,14 @@ def test_gpu_matches_golden_c1(gpu):
     close(_h(tm.Gradient(x, _t(g["sens"]))), g["gradient"], 1e-10, what="gradient")
     close(_h(tm.LogDeterminantInputGrad(x)), g["logdet_input_grad"], 1e-10, what="logdet_input_grad")
     n = g["x"].shape[1]
-    xi = _h(tm.Inverse(x, _t(g["evaluate"])))
-    assert np.max(np.abs(xi - g["inverse_warm"])) <= 2e-6
-    xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(g["evaluate"])))
-    assert np.max(np.abs(xi - g["inverse_cold"])) <= 2e-6
+    om = oracle.OracleTriangularMap(2, 2, 3)
+    r = g["evaluate"]
+    xi = _h(tm.Inverse(x, _t(r)))
+    _assert_within(xi, g["inverse_warm"], _inverse_bound(om, g["coef"], g["x"], g["inverse_warm"], r, 1e-6, 1e-6, 1e-6),
+                   what="c1 warm inverse")
+    xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(r)))
+    _assert_within(xi, g["inverse_cold"], _inverse_bound(om, g["coef"], g["x"], g["inverse_cold"], r, 1e-6, 1e-6, 1e-6),
+                   what="c1 cold inverse")
     loss, grad = tm.KLObjective(x)
     close(_h(loss), g["kl_loss"], 1e-10, what="kl loss")
     close(_h(grad), g["kl_grad"], 1e-10, floor=1e-3, what="kl grad")
@@ -113,7 +145,7 @@ def test_gpu_matches_golden_c3(gpu):
 
 
 @pytest.mark.gpu
-def test_gpu_matches_golden_c5(gpu):
+def test_gpu_matches_golden_c5(gpu, oracle):
     M = gpu
     g = load("c5")
     tm = M.CreateTriangular(16, 16, 3, _opts(M, tol=1e-8))
@@ -123,4 +155,12 @@ def test_gpu_matches_golden_c5(gpu):
     # points where the reference's bracket search fails are NaN in both
     assert np.array_equal(np.isnan(xi), np.isnan(g["inverse"]))
     ok = ~np.isnan(g["inverse"])
-    assert np.max(np.abs(xi - g["inverse"])[ok]) <= 1e-8
+    # End to end, each component is solved at the earlier components' solutions,
+    # so per-component solver differences propagate down the chain: the
+    # reference itself at xtol 1e-12 differs from these values by 4e-8.
+    assert np.max(np.abs(xi - g["inverse"])[ok]) <= 1e-6
+    # Component by component, from the GPU's own earlier coordinates, the
+    # oracle's solution agrees within the solver tolerance.
+    from test_gpu_parity import assert_inverse_parity
+    om = oracle.OracleTriangularMap(16, 16, 3, abs_tol=1e-8, rel_tol=1e-8)
+    assert_inverse_parity(om, g["coef"], np.zeros((0, n)), g["r"], xi, 1e-10, 1e-10)
