@@ -519,7 +519,23 @@ def run_gpu(args):
             "logdet": lambda: comp.LogDeterminantImpl(x, out_ld),
             "reduce": lambda: comp.FusedForwardAdjointImpl(x, logdet_sens_scale=1.0, coeff_grad=cg),
         }
-        step = variants[args.variant]
+        if args.variant == "kl":
+            # The KL training workload's step at trained coefficients (100
+            # L-BFGS iterations with direct launches first); the profiled
+            # calls sit in the NVTX range "kl_step".
+            opts = M.MapOptions(basisType=M.BasisTypes.HermiteFunctions, posFuncType=M.PosFuncTypes.Exp,
+                                quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=KL_TOL, quadRelTol=KL_TOL)
+            X = torch.as_tensor(banana(KL_N), device=dev)
+            tm = M.CreateTriangular(KL_DIM, KL_DIM, KL_ORDER, opts)
+            tm.SetCoeffs(np.zeros(tm.numCoeffs))
+            M.TrainMap(tm, X, max_iters=KL_ITERS, mode=1)
+
+            def step():
+                torch.cuda.nvtx.range_push("kl_step")
+                tm.KLObjective(X)
+                torch.cuda.nvtx.range_pop()
+        else:
+            step = variants[args.variant]
 
     for _ in range(max(args.warmup, 3)):
         step()
@@ -669,7 +685,7 @@ def main():
     ap.add_argument("--no-kl", action="store_true", help="skip the KL training workload")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
-    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce"],
+    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce", "kl"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
     if args.impl == "reference":

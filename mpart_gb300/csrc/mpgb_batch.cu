@@ -272,7 +272,7 @@ public:
             CompDesc c{};
             c.D = p.D; c.P = p.P; c.nB = p.nB; c.nNodes = p.nNodes; c.nSlots = p.nSlots; c.nCNodes = p.nCNodes;
             c.maxDepth = p.maxDepth; c.numTerms = p.numTerms; c.outRow = (int)part.outRow;
-            c.coeffOffset = (int)part.mapCoeffOffset; c.slotOffset = bc.slotOffset;
+            c.coeffOffset = (int)part.mapCoeffOffset; c.slotOffset = bc.slotOffset; c.cSegs = p.cSegs;
             c.nodeA = p.dNodeA; c.nodeSlot = p.dNodeSlot; c.nodeC = p.dNodeC; c.nodeCRows = p.dNodeCRows;
             c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
             cd.push_back(c);
@@ -481,12 +481,14 @@ private:
             for (long long t = 0; t < nItems; ++t) {
                 WorkItem w{k, k + 1, (int)t, (int)((nTiles - t + nItems - 1) / nItems), part, 0, (int)nItems};
                 cand.push_back({w, bc.prog->weight * w.nTiles, (int)cand.size()});
-                rowBase.push_back(part);
-                part += bc.prog->numTerms;
+                for (int sg = 0; sg < bc.prog->cSegs; ++sg) {
+                    rowBase.push_back(part);
+                    part += bc.prog->numTerms;
+                }
             }
             double* out = coeffGrad[bc.map];
             if (out)
-                red.push_back({row0, (int)nItems, bc.prog->numTerms,
+                red.push_back({row0, (int)nItems * bc.prog->cSegs, bc.prog->numTerms,
                                out + maps_[bc.map]->Parts()[bc.part].mapCoeffOffset});
         }
         std::stable_sort(cand.begin(), cand.end(), [](const Cand& a, const Cand& b) { return a.cost > b.cost; });

@@ -151,7 +151,8 @@ struct KLPlan {
     int onlyComp = -2;
     int nItems = 0;
     std::vector<std::vector<int>> itemsOf;
-    std::vector<int> rowOff;  // first row of each component in rowBase/lossSlots
+    std::vector<int> rowOff;   // first row of each component in rowBase
+    std::vector<int> lossOff;  // first entry of each component in lossSlots
     DevBuf items, rowBase, lossSlots;
     size_t partialDoubles = 0;
 };
@@ -368,7 +369,7 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
             CompDesc c{};
             c.D = p.D; c.P = p.P; c.nB = p.nB; c.nNodes = p.nNodes; c.nSlots = p.nSlots; c.nCNodes = p.nCNodes;
             c.maxDepth = p.maxDepth; c.numTerms = p.numTerms; c.outRow = (int)pt.outRow;
-            c.coeffOffset = (int)pt.mapCoeffOffset; c.slotOffset = slotOff;
+            c.coeffOffset = (int)pt.mapCoeffOffset; c.slotOffset = slotOff; c.cSegs = p.cSegs;
             c.nodeA = p.dNodeA; c.nodeSlot = p.dNodeSlot; c.nodeC = p.dNodeC; c.nodeCRows = p.dNodeCRows;
             c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
             W.hostComps.push_back(c);
@@ -528,8 +529,10 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
             if (reduced) {
                 w.partialBase = base;
                 w.lossSlot = (int)v.size();
-                if (rowBaseOut) rowBaseOut->push_back(base);
-                base += parts[c].prog->numTerms;
+                for (int sg = 0; sg < parts[c].prog->cSegs; ++sg) {
+                    if (rowBaseOut) rowBaseOut->push_back(base);
+                    base += parts[c].prog->numTerms;
+                }
             }
             if (itemsOfComp) (*itemsOfComp)[c].push_back((int)v.size());
             v.push_back(w);
@@ -801,7 +804,9 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
             p.lsens = logdetSens.data; p.lsensStride = ldStrideL; p.lsensScale = logdetSensScale;
             size_t nPart = rowBase.empty() ? 1 : (size_t)(rowBase.back() + parts_[items.back().c0].prog->numTerms);
             size_t tot = 0;
-            for (auto& it : items) tot = std::max<size_t>(tot, (size_t)it.partialBase + parts_[it.c0].prog->numTerms);
+            for (auto& it : items)
+                tot = std::max<size_t>(tot, (size_t)it.partialBase +
+                                                (size_t)parts_[it.c0].prog->numTerms * parts_[it.c0].prog->cSegs);
             nPart = std::max(nPart, tot);
             W.partials.ensure(nPart * sizeof(double), stream);
             p.partials = W.partials.as<double>();
@@ -833,13 +838,15 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
             std::vector<long long> rb;
             W.rowBase.ensure(sizeof(long long) * std::max<size_t>(1, rowBase.size()), stream);
             for (int c = 0; c < nComps; ++c) {
-                for (int id : itemsOf[c]) rb.push_back(items[id].partialBase);
+                for (int id : itemsOf[c])
+                    for (int sg = 0; sg < parts_[c].prog->cSegs; ++sg)
+                        rb.push_back(items[id].partialBase + (long long)sg * parts_[c].prog->numTerms);
             }
             MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice,
                                       stream));
             size_t off = 0;
             for (int c = 0; c < nComps; ++c) {
-                const int nr = (int)itemsOf[c].size();
+                const int nr = (int)itemsOf[c].size() * parts_[c].prog->cSegs;
                 MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>() + off, nr,
                                            parts_[c].prog->numTerms, 1.0, coeffGrad + parts_[c].mapCoeffOffset, 0,
                                            stream));
@@ -878,18 +885,23 @@ static KLPlan& klPlan(MapWorkspace& W, const std::vector<MonotoneMapBase::Part>&
     auto items = itemsPerComp(parts, N, W.numSMs, true, &rowBase, &P.itemsOf, onlyComp);
     P.nItems = (int)items.size();
     for (auto& it : items)
-        P.partialDoubles = std::max<size_t>(P.partialDoubles, (size_t)it.partialBase + parts[it.c0].prog->numTerms);
+        P.partialDoubles = std::max<size_t>(P.partialDoubles, (size_t)it.partialBase + (size_t)parts[it.c0].prog->numTerms *
+                                                                                      parts[it.c0].prog->cSegs);
     std::vector<long long> rb;
     std::vector<int> ls;
     P.rowOff.assign(parts.size() + 1, 0);
+    P.lossOff.assign(parts.size() + 1, 0);
     for (size_t c = 0; c < parts.size(); ++c) {
         P.rowOff[c] = (int)rb.size();
+        P.lossOff[c] = (int)ls.size();
         for (int id : P.itemsOf[c]) {
-            rb.push_back(items[id].partialBase);
+            for (int sg = 0; sg < parts[c].prog->cSegs; ++sg)
+                rb.push_back(items[id].partialBase + (long long)sg * parts[c].prog->numTerms);
             ls.push_back(items[id].lossSlot);
         }
     }
     P.rowOff[parts.size()] = (int)rb.size();
+    P.lossOff[parts.size()] = (int)ls.size();
     P.items.ensure(items.size() * sizeof(WorkItem), stream);
     P.rowBase.ensure(std::max<size_t>(1, rb.size()) * sizeof(long long), stream);
     P.lossSlots.ensure(std::max<size_t>(1, ls.size()) * sizeof(int), stream);
@@ -935,8 +947,8 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
         const int nr = P.rowOff[c + 1] - P.rowOff[c];
         MPGB_CUDA(launchReduceRows(W.partials.as<double>(), P.rowBase.as<long long>() + P.rowOff[c], nr,
                                    parts_[c].prog->numTerms, 1.0, grad + parts_[c].mapCoeffOffset, 0, stream));
-        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), P.lossSlots.as<int>() + P.rowOff[c], nr, 1.0 / (double)N,
-                                lossPerComp + c, stream));
+        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), P.lossSlots.as<int>() + P.lossOff[c],
+                                P.lossOff[c + 1] - P.lossOff[c], 1.0 / (double)N, lossPerComp + c, stream));
     }
     Finish(stream, "KLObjective");
 }
@@ -994,7 +1006,9 @@ void MonotoneMapBase::InverseCoeffGrad(StridedMatrix const& pts, StridedMatrix c
         p.negRows = (q + 1 == order.size()) ? extra : 0;
         if (wantCoef) {
             size_t nPart = 1;
-            for (auto& it : items) nPart = std::max<size_t>(nPart, (size_t)it.partialBase + parts_[c].prog->numTerms);
+            for (auto& it : items)
+                nPart = std::max<size_t>(nPart, (size_t)it.partialBase +
+                                                    (size_t)parts_[c].prog->numTerms * parts_[c].prog->cSegs);
             W.partials.ensure(nPart * sizeof(double), stream);
             p.partials = W.partials.as<double>();
         }

@@ -456,8 +456,14 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 for (int k = 0; k <= PMAX; ++k) L.W[k * tpb + tid] = wT[k] + wL[k];
                 __syncthreads();
                 const bool first = (tj == 0);
-                double* part = prm.partials + item.partialBase;
-                for (int n = tid; n < c.nCNodes; n += tpb) {
+                // Units (node, point segment); consecutive threads share a node.
+                const int S = c.cSegs;
+                const int segLen = tpb / S;
+                const int units = c.nCNodes * S;
+                for (int u = tid; u < units; u += tpb) {
+                    const int n = (S == 4) ? (u >> 2) : (S == 1 ? u : u / S);
+                    const int sg = u - n * S;
+                    double* part = prm.partials + item.partialBase + (long long)sg * c.numTerms;
                     const uint32_t w = __ldg(&c.nodeC[n]);
                     const int depth = w & 31, nk = (w >> 5) & 31, slot = w >> 10;
                     const uint16_t* rows = c.nodeCRows + (size_t)n * kMaxDepth;
@@ -467,7 +473,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     double acc[PMAX + 1];
 #pragma unroll
                     for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
-                    for (int j = 0; j < tpb; ++j) {
+                    for (int j = sg * segLen; j < (sg + 1) * segLen; ++j) {
                         const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
                         accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
                     }

@@ -199,7 +199,7 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         d = CompDesc{};
         d.D = p.D; d.P = p.P; d.nB = p.nB; d.nNodes = p.nNodes; d.nSlots = p.nSlots; d.nCNodes = p.nCNodes;
         d.maxDepth = p.maxDepth; d.numTerms = p.numTerms; d.outRow = (int)parts[c].outRow;
-        d.coeffOffset = (int)parts[c].mapCoeffOffset; d.slotOffset = slotOff;
+        d.coeffOffset = (int)parts[c].mapCoeffOffset; d.slotOffset = slotOff; d.cSegs = p.cSegs;
         d.nodeA = p.dNodeA; d.nodeSlot = p.dNodeSlot; d.nodeC = p.dNodeC; d.nodeCRows = p.dNodeCRows;
         d.slotTerm = p.dSlotTerm; d.leadDeg = p.dLeadDeg; d.rowOff = p.dRowOff;
         parts[c].owner->CheckCoefficients("FusedForwardAdjoint (no allocation)");
@@ -214,8 +214,10 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         rowOff[c] = (int)rowBase.size();
         for (long long t = 0; t < nTiles; t += tilesPer) {
             WorkItem w{c, c + 1, (int)t, (int)std::min<long long>(tilesPer, nTiles - t), partBase, (int)items.size(), 1};
-            rowBase.push_back(partBase);
-            partBase += p.numTerms;
+            for (int sg = 0; sg < p.cSegs; ++sg) {
+                rowBase.push_back(partBase);
+                partBase += p.numTerms;
+            }
             items.push_back(w);
         }
     }

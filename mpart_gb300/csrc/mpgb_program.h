@@ -56,6 +56,10 @@ struct ComponentProgram {
     int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr;
     // Work per point (FP64 operations of phases A and C), for load balancing.
     double weight = 1.0;
+    // Reduced adjoint: the tile's points are split into cSegs segments and the
+    // block's threads take (node, segment) units, so that a few hundred nodes
+    // still keep every thread busy; each segment has its own partial row.
+    int cSegs = 1;
 
     explicit ComponentProgram(FixedMultiIndexSet const& ms) {
         D = (int)ms.Length();
@@ -161,6 +165,7 @@ struct ComponentProgram {
         }
         for (int n : order) opsA += (tn[n].depth > 0 ? 1 : 0) + nkOf[n];
         weight = opsA + opsC + 3.0 * nB + 60.0;
+        cSegs = nCNodes < 1024 ? 4 : 1;
         dNodeA = toDevice(nodeA);
         dNodeSlot = toDevice(nodeSlot);
         dNodeC = toDevice(nodeC);

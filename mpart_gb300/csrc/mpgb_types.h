@@ -20,7 +20,7 @@ struct CompDesc {
     int outRow;     // output row of this component in the map output
     int coeffOffset;  // offset of its block in the map coefficient vector
     int slotOffset;   // offset of its slots in the map-wide gathered coefficient table
-    int pad_;
+    int cSegs;        // reduced adjoint: point segments per tile = partial rows per work item (divides the block size)
     const uint32_t* nodeA;   // [nNodes] depth | nk<<5 | dim<<10 | brow<<18
     const uint32_t* nodeSlot;  // [nNodes] first slot of the node
     const uint32_t* nodeC;   // [nCNodes] depth | nk<<5 | slot<<10
@@ -37,7 +37,7 @@ struct CompDesc {
 struct WorkItem {
     int c0, c1;
     int tile0, nTiles;
-    long long partialBase;  // first double of this item's partial row (reduced adjoint)
+    long long partialBase;  // first double of this item's partial rows (cSegs rows of numTerms; reduced adjoint)
     int lossSlot;           // index into the loss partials (KL)
     int tileStride;         // distance between consecutive tiles of the item (>= 1)
 };
