@@ -63,11 +63,7 @@ struct SortSeg {
     int chunk0, nChunks;
 };
 
-__device__ __forceinline__ int bucketOf(double x) {
-    const double a = fabs(x);
-    if (!(a < 8.0)) return kBuckets - 1;
-    return (int)(a * 32.0);
-}
+__device__ __forceinline__ int bucketOf(double x) { return sortBucket(x); }
 
 __global__ void segHistKernel(const SortSeg* segs, const int* chunkSeg, int* hist) {
     __shared__ int h[kBuckets];

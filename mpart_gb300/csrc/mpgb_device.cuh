@@ -118,6 +118,16 @@ __device__ __forceinline__ double prefixProduct(int depth, const int* r, const d
     return phi;
 }
 
+// Sort bucket of a point by |x_D| (256 buckets): width 1/32 below 4, width 1/4
+// from 4 to 36, then NaN and everything larger in the last.  The adaptive
+// quadrature's cost grows with |x_D|; points of one bucket cost about the same.
+__device__ __forceinline__ int sortBucket(double x) {
+    const double a = fabs(x);
+    if (a < 4.0) return (int)(a * 32.0);
+    if (a < 36.0) return 128 + (int)((a - 4.0) * 4.0);
+    return 255;
+}
+
 // --------------------------------------------------------------------------
 // Positive bijectors (MParT/PositiveBijectors.h:12-57).  g and g' share one
 // exponential; the formulas are the reference's, including log(1 + e) rather

@@ -45,19 +45,15 @@ __global__ void reduceRowsKernel(const double* part, const long long* rowBase, i
 }
 
 // ---------------------------------------------------------------------------
-// Stable counting sort of points by |x_D| (256 buckets of width 1/32, NaN and
-// |x_D| >= 8 in the last).  The per-point cost of the adaptive quadrature grows
-// with |x_D|; grouping points of similar cost keeps a warp's lanes busy.
+// Stable counting sort of points by |x_D| (the 256 buckets of sortBucket).
+// The per-point cost of the adaptive quadrature grows with |x_D|; grouping
+// points of similar cost keeps a warp's lanes busy.
 // Deterministic: bucket-major, original order within a bucket.
 // ---------------------------------------------------------------------------
 constexpr int kSortBuckets = 256;
 constexpr int kSortChunk = 1024;
 
-__device__ __forceinline__ int sortKey(double x) {
-    const double a = fabs(x);
-    if (!(a < 8.0)) return kSortBuckets - 1;
-    return (int)(a * 32.0);
-}
+__device__ __forceinline__ int sortKey(double x) { return sortBucket(x); }
 
 __global__ void keyHistKernel(const double* xd, long long stride, long long N, int* hist) {
     __shared__ int h[kSortBuckets];

@@ -34,33 +34,94 @@ struct NodeVal {
     double E;                    // d/dx_D of the integrand (MonotoneIntegrand.h:193-201)
 };
 
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
-__device__ __forceinline__ void evalNode(double t, double xd, const double* a, int P, const BasisConsts& bc,
-                                         double nugget, NodeVal<PMAX, NEEDJ, NEEDE>& o, int& st) {
-    double d1[PMAX + 1], d2[PMAX + 1];
-    const double y = t * xd;
-    lastBasis<BASIS, PMAX, false, true, NEEDE>(y, P, bc, nullptr, d1, d2);
-    double df = 0.0;
+// Per-component constants folded into the coefficients once per point, so a
+// quadrature node pays no per-term scaling:
+//   d phit_k / dy   = cs_k * u_k(y) * env(y),   d2 phit_k / dy2 = cs_k * v_k(y) * env(y)
+// ProbabilistHermite: cs_k = k invNorm_k, u_k = He_{k-1}, v_k = (k-1) He_{k-2}, env = 1.
+// HermiteFunctions (k >= 2, j = k-2): cs_k = hfScale_j, u_k = 2j H_{j-1} - y H_j,
+// v_k = -(2j+1-y^2) H_j, env = exp(-y^2/2); k = 1 (phit_1 = y): cs = 1, u = 1, env = 1.
+template <int BASIS, int PMAX>
+__device__ __forceinline__ void scaleCoeffs(const double* a, int P, const BasisConsts& bc, double* as) {
+    as[0] = 0.0;
 #pragma unroll
-    for (int k = 1; k <= PMAX; ++k) df = fma(a[k], d1[k], df);
+    for (int k = 1; k <= PMAX; ++k) {
+        double cs;
+        if constexpr (BASIS == kBasisProbHermite) cs = double(k) * bc.invNorm[k];
+        else cs = (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
+        as[k] = (k <= P) ? a[k] * cs : 0.0;
+    }
+}
+
+template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+__device__ __forceinline__ void evalNode(double t, double xd, const double* as, int P, const BasisConsts& bc,
+                                         double nugget, NodeVal<PMAX, NEEDJ, NEEDE>& o, int& st) {
+    (void)bc;
+    const double y = t * xd;
+    double u[PMAX + 1], v[PMAX + 1];
+    double df, d2f = 0.0, env = 1.0;
+    if constexpr (BASIS == kBasisProbHermite) {
+        double he[PMAX + 1];
+        he[0] = 1.0;
+        if (PMAX >= 1) he[1] = y;
+#pragma unroll
+        for (int k = 2; k <= PMAX; ++k) he[k] = (k <= P) ? (y * he[k - 1] - (k - 1.0) * he[k - 2]) : 0.0;
+        df = 0.0;
+#pragma unroll
+        for (int k = 1; k <= PMAX; ++k) {
+            u[k] = he[k - 1];
+            df = fma(as[k], u[k], df);
+        }
+        if constexpr (NEEDE) {
+#pragma unroll
+            for (int k = 2; k <= PMAX; ++k) {
+                v[k] = (k - 1.0) * he[k - 2];
+                d2f = fma(as[k], v[k], d2f);
+            }
+        }
+    } else {
+        double H[PMAX + 1];
+        H[0] = 1.0;
+        if (PMAX >= 1) H[1] = 2.0 * y;
+#pragma unroll
+        for (int j = 2; j <= PMAX; ++j) H[j] = (j + 2 <= P) ? (2.0 * y * H[j - 1] - 2.0 * (j - 1.0) * H[j - 2]) : 0.0;
+        env = (P >= 2) ? exp(-0.5 * y * y) : 0.0;
+        double acc = 0.0, acc2 = 0.0;
+        if (PMAX >= 1) u[1] = 1.0;
+#pragma unroll
+        for (int k = 2; k <= PMAX; ++k) {
+            const int j = k - 2;
+            const double hjm1 = (j >= 1) ? (2.0 * j) * H[j > 0 ? j - 1 : 0] : 0.0;
+            u[k] = fma(-y, H[j], hjm1);
+            acc = fma(as[k], u[k], acc);
+            if constexpr (NEEDE) {
+                v[k] = -(2.0 * j + 1.0 - y * y) * H[j];
+                acc2 = fma(as[k], v[k], acc2);
+            }
+        }
+        df = fma(env, acc, (PMAX >= 1) ? as[1] : 0.0);
+        if constexpr (NEEDE) d2f = env * acc2;
+    }
     double g, gp;
     posEval<POS>(df, g, gp);
     o.h = xd * (g + nugget);
     if (isinf(g)) st |= kStatusInf;
     else if (isnan(o.h)) st |= kStatusNaN;
     if constexpr (NEEDJ) {
+        // Unscaled: J_k is multiplied by cs_k once the integral is done.
         const double q = xd * gp;
+        const double qe = q * env;
 #pragma unroll
-        for (int k = 1; k <= PMAX; ++k) o.F[k - 1] = q * d1[k];
+        for (int k = 1; k <= PMAX; ++k) {
+            if constexpr (BASIS == kBasisProbHermite) o.F[k - 1] = q * u[k];
+            else o.F[k - 1] = (k == 1) ? q : qe * u[k];
+        }
     }
     if constexpr (NEEDE) {
-        double d2f = 0.0;
-#pragma unroll
-        for (int k = 2; k <= PMAX; ++k) d2f = fma(a[k], d2[k], d2f);
         o.E = fma(d2f, (xd * t) * gp, g + nugget);
     } else {
         o.E = 0.0;
     }
+    (void)v;
 }
 
 template <int PMAX, bool NEEDJ, bool NEEDE>
@@ -91,9 +152,11 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
 #pragma unroll
     for (int k = 0; k < NJ; ++k) R.J[k] = 0.0;
 
+    double as[PMAX + 1];
+    scaleCoeffs<BASIS, PMAX>(a, P, bc, as);
     NV A, B, M, V;
-    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(0.0, xd, a, P, bc, nugget, A, st);
-    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(1.0, xd, a, P, bc, nugget, B, st);
+    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(0.0, xd, as, P, bc, nugget, A, st);
+    evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(1.0, xd, as, P, bc, nugget, B, st);
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     if (st & (kStatusInf | kStatusNaN)) { R.Ih = nan; return; }
 
@@ -104,7 +167,7 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
     while (true) {
         const double m = 0.5 * (lo + hi);
         const double s = 0.5 * (hi - lo);
-        evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m, xd, a, P, bc, nugget, M, st);
+        evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m, xd, as, P, bc, nugget, M, st);
         double ic = (s * Q.cWts[0]) * A.h;
         ic = fma(s * Q.cWts[cM], M.h, ic);
         ic = fma(s * Q.cWts[cR], B.h, ic);
@@ -122,7 +185,7 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
         // Coarse interior points other than the midpoint (level >= 2 rules).
         for (int i = 1; i < cR; ++i) {
             if (i == cM) continue;
-            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.cPts[i], xd, a, P, bc, nugget, V, st);
+            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.cPts[i], xd, as, P, bc, nugget, V, st);
             ic = fma(s * Q.cWts[i], V.h, ic);
             const double wf = s * Q.fWts[2 * i];
             ih = fma(wf, V.h, ih);
@@ -134,7 +197,7 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
         }
         // Points only in the fine rule.
         for (int i = 1; i < Q.nFine; i += 2) {
-            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.fPts[i], xd, a, P, bc, nugget, V, st);
+            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(m + s * Q.fPts[i], xd, as, P, bc, nugget, V, st);
             const double wf = s * Q.fWts[i];
             ih = fma(wf, V.h, ih);
             if constexpr (NEEDJ) {
@@ -184,6 +247,16 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
             st |= kStatusBudget;
             R.Ih = nan;
             return;
+        }
+    }
+    if constexpr (NEEDJ) {
+        // The nodes accumulated u_k (times env); apply the per-order constants.
+#pragma unroll
+        for (int k = 1; k <= PMAX; ++k) {
+            double cs;
+            if constexpr (BASIS == kBasisProbHermite) cs = double(k) * bc.invNorm[k];
+            else cs = (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
+            R.J[k - 1] *= cs;
         }
     }
 }
