@@ -106,6 +106,8 @@ int mpgb_map_dims(const mpgb_map* map, unsigned int* input_dim, unsigned int* ou
 /* TriangularMap::NumComponents / GetComponent (MParT/TriangularMap.h:65-66).
  * A component handle must be released with mpgb_map_destroy. */
 int mpgb_map_num_components(const mpgb_map* map, unsigned int* n);
+/* 1 for a TriangularMap, 0 for a single component. */
+int mpgb_map_is_triangular(const mpgb_map* map, int* is_triangular);
 int mpgb_map_get_component(mpgb_map* map, unsigned int i, mpgb_map** out);
 
 /* ParameterizedFunctionBase::SetCoeffs, deep copy (src/ParameterizedFunctionBase.cpp:185-207).
@@ -248,6 +250,39 @@ int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, d
 /* FP64 throughput probe: DFMA chains over blocks x threads x iters x 8; writes the
  * kernel time in milliseconds (CUDA events on the stream). */
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms);
+
+/* ------------------------------------------------------------------------
+ * Archives (host only; no device work except the coefficient copy of a map).
+ * Byte layouts of the reference's cereal binary archives where it has one:
+ *   MPGB_ARCHIVE_COEFFS: ParameterizedFunctionBase.Serialize / DeserializeMap
+ *     (bindings/python/src/ParameterizedFunctionBase.cpp:51-56,
+ *      bindings/python/src/Serialization.cpp:20-31);
+ *   options: MapOptions::serialize (MParT/MapOptions.h:126-130);
+ *   multi-index sets: FixedMultiIndexSet::save/load
+ *     (MParT/MultiIndices/FixedMultiIndexSet.h:115-133).
+ * MPGB_ARCHIVE_MAP is this library's whole-map archive (options, every
+ * component's multi-index set, coefficients), the counterpart of the
+ * reference's ToBytes / FromBytes / pickle, whose polymorphic cereal layout it
+ * does not reproduce.  Writers use a two-call convention: *size always
+ * receives the archive size, and the bytes are written when buf (cap bytes)
+ * is large enough; buf == NULL only queries the size.
+ * ------------------------------------------------------------------------ */
+enum { MPGB_ARCHIVE_MAP = 0, MPGB_ARCHIVE_COEFFS = 1 };
+
+int mpgb_map_to_bytes(mpgb_map* map, int layout, unsigned char* buf, size_t cap, size_t* size);
+/* Rebuilds a component or triangular map (coefficients set) from an MPGB_ARCHIVE_MAP archive. */
+int mpgb_map_from_bytes(const unsigned char* buf, size_t size, mpgb_map** out);
+/* Reads an MPGB_ARCHIVE_COEFFS archive; coeffs (num_coeffs doubles, host) may be NULL to query sizes. */
+int mpgb_coeff_archive_read(const unsigned char* buf, size_t size, unsigned int* input_dim, unsigned int* output_dim,
+                            unsigned int* num_coeffs, double* coeffs);
+int mpgb_options_to_bytes(const mpgb_map_options* opts, unsigned char* buf, size_t cap, size_t* size);
+int mpgb_options_from_bytes(const unsigned char* buf, size_t size, mpgb_map_options* out);
+int mpgb_mset_to_bytes(unsigned int dim, unsigned int num_terms, const unsigned int* nz_starts,
+                       const unsigned int* nz_dims, const unsigned int* nz_orders, unsigned char* buf, size_t cap,
+                       size_t* size);
+/* Arrays may be NULL to query dim, num_terms and nnz first. */
+int mpgb_mset_from_bytes(const unsigned char* buf, size_t size, unsigned int* dim, unsigned int* num_terms,
+                         unsigned int* nnz, unsigned int* nz_starts, unsigned int* nz_dims, unsigned int* nz_orders);
 
 /* ------------------------------------------------------------------------
  * Batch of independent maps (no counterpart in the reference, which runs one

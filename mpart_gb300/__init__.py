@@ -19,7 +19,8 @@ from ._capi import IntegrandError, MpgbError, check, load, mpgb_map_options, mpg
 
 __all__ = [
     "BasisTypes", "PosFuncTypes", "QuadTypes", "MapOptions", "FixedMultiIndexSet", "ConditionalMapBase",
-    "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load",
+    "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load", "DeserializeMap",
+    "FromBytes", "MapBatch", "TrainMap",
 ]
 
 
@@ -65,6 +66,42 @@ class MapOptions:
                                 float(self.quadAbsTol), float(self.quadRelTol), int(self.quadMaxSub),
                                 int(self.quadMinSub), int(self.quadPts), int(bool(self.contDeriv)),
                                 int(bool(self.basisNorm)), float(self.nugget))
+
+    @classmethod
+    def _from_c(cls, o: mpgb_map_options) -> "MapOptions":
+        return cls(basisType=BasisTypes(o.basis_type), posFuncType=PosFuncTypes(o.pos_func_type),
+                   quadType=QuadTypes(o.quad_type), quadAbsTol=o.quad_abs_tol, quadRelTol=o.quad_rel_tol,
+                   quadMaxSub=o.quad_max_sub, quadMinSub=o.quad_min_sub, quadPts=o.quad_pts,
+                   contDeriv=bool(o.cont_deriv), basisNorm=bool(o.basis_norm), nugget=o.nugget)
+
+    def ToBytes(self) -> bytes:
+        """The reference's cereal archive of MapOptions (MParT/MapOptions.h:126-130)."""
+        o = self._c()
+        return _archive(lambda buf, cap, size: load().mpgb_options_to_bytes(C.byref(o), buf, cap, size))
+
+    @classmethod
+    def FromBytes(cls, data: bytes) -> "MapOptions":
+        o = mpgb_map_options()
+        check(load().mpgb_options_from_bytes(data, len(data), C.byref(o)))
+        return cls._from_c(o)
+
+    def Serialize(self, filename):
+        """MapOptions.Serialize (bindings/python/src/MapOptions.cpp:74-78)."""
+        with open(filename, "wb") as f:
+            f.write(self.ToBytes())
+
+    def Deserialize(self, filename):
+        """MapOptions.Deserialize (bindings/python/src/MapOptions.cpp:79-84): fills this object and returns it."""
+        with open(filename, "rb") as f:
+            other = MapOptions.FromBytes(f.read())
+        self.__dict__.update(other.__dict__)
+        return self
+
+    def __eq__(self, other):
+        return isinstance(other, MapOptions) and self.__dict__ == other.__dict__
+
+    def __reduce__(self):
+        return (MapOptions.FromBytes, (self.ToBytes(),))
 
 
 class FixedMultiIndexSet:
@@ -123,9 +160,79 @@ class FixedMultiIndexSet:
             m[self.nzDims[j]] = self.nzOrders[j]
         return m
 
+    def ToBytes(self) -> bytes:
+        """The reference's cereal archive of the set (MParT/MultiIndices/FixedMultiIndexSet.h:115-123)."""
+        U = C.POINTER(C.c_uint)
+        s, d, o = (a.ctypes.data_as(U) if a.size else None for a in (self.nzStarts, self.nzDims, self.nzOrders))
+        return _archive(lambda buf, cap, size: load().mpgb_mset_to_bytes(self.dim, self.Size(), s, d, o, buf, cap,
+                                                                         size))
+
+    @classmethod
+    def FromBytes(cls, data: bytes) -> "FixedMultiIndexSet":
+        dim, nt, nnz = C.c_uint(), C.c_uint(), C.c_uint()
+        check(load().mpgb_mset_from_bytes(data, len(data), C.byref(dim), C.byref(nt), C.byref(nnz), None, None,
+                                          None))
+        s = np.zeros(nt.value + 1, np.uint32)
+        d = np.zeros(max(1, nnz.value), np.uint32)
+        o = np.zeros(max(1, nnz.value), np.uint32)
+        U = C.POINTER(C.c_uint)
+        check(load().mpgb_mset_from_bytes(data, len(data), None, None, None, s.ctypes.data_as(U),
+                                          d.ctypes.data_as(U), o.ctypes.data_as(U)))
+        return cls(dim.value, nzStarts=s, nzDims=d[:nnz.value], nzOrders=o[:nnz.value])
+
+    def Serialize(self, filename):
+        """FixedMultiIndexSet.Serialize (bindings/python/src/MultiIndex.cpp:243-248)."""
+        with open(filename, "wb") as f:
+            f.write(self.ToBytes())
+
+    def Deserialize(self, filename):
+        """FixedMultiIndexSet.Deserialize (bindings/python/src/MultiIndex.cpp:249-254): fills this object."""
+        with open(filename, "rb") as f:
+            other = FixedMultiIndexSet.FromBytes(f.read())
+        self.dim, self.nzStarts, self.nzDims, self.nzOrders = other.dim, other.nzStarts, other.nzDims, other.nzOrders
+        return self
+
+    def __reduce__(self):
+        return (FixedMultiIndexSet.FromBytes, (self.ToBytes(),))
+
 
 def _is_torch(x):
     return type(x).__module__.startswith("torch")
+
+
+def _archive(call) -> bytes:
+    """Two-call archive writer: query the size, then fill a buffer."""
+    size = C.c_size_t(0)
+    check(call(None, 0, C.byref(size)))
+    buf = C.create_string_buffer(max(1, size.value))
+    check(call(buf, size.value, C.byref(size)))
+    return buf.raw[:size.value]
+
+
+def DeserializeMap(filename):
+    """DeserializeMap (bindings/python/src/Serialization.cpp:20-31): reads a file
+    written by ConditionalMapBase.Serialize; returns (inputDim, outputDim, coeffs)."""
+    with open(filename, "rb") as f:
+        data = f.read()
+    i, o, n = C.c_uint(), C.c_uint(), C.c_uint()
+    check(load().mpgb_coeff_archive_read(data, len(data), C.byref(i), C.byref(o), C.byref(n), None))
+    coeffs = np.zeros(n.value)
+    check(load().mpgb_coeff_archive_read(data, len(data), None, None, None, C.c_void_p(coeffs.ctypes.data)))
+    return i.value, o.value, coeffs
+
+
+def _wrap_map(h):
+    t = C.c_int()
+    check(load().mpgb_map_is_triangular(h, C.byref(t)))
+    return TriangularMap(_handle=h) if t.value else ConditionalMapBase(h)
+
+
+def FromBytes(data: bytes):
+    """ParameterizedFunctionBase.FromBytes: rebuilds a component or triangular
+    map (with its coefficients) from ConditionalMapBase.ToBytes()."""
+    h = C.c_void_p()
+    check(load().mpgb_map_from_bytes(data, len(data), C.byref(h)))
+    return _wrap_map(h)
 
 
 def _stream_of(*arrs):
@@ -334,6 +441,22 @@ class ConditionalMapBase:
         grad = _zeros_like_dev(pts, (self.numCoeffs,))
         check(load().mpgb_kl_objective(self._h, _mat(pts), _ptr(loss), _ptr(grad), _stream_of(pts)))
         return loss, grad
+
+    # ---- archives ----------------------------------------------------------
+    def Serialize(self, filename):
+        """ParameterizedFunctionBase.Serialize (bindings/python/src/ParameterizedFunctionBase.cpp:51-56):
+        inputDim, outputDim, numCoeffs and the coefficients, in the reference's cereal layout."""
+        with open(filename, "wb") as f:
+            f.write(_archive(lambda buf, cap, size: load().mpgb_map_to_bytes(self._h, 1, buf, cap, size)))
+
+    def ToBytes(self) -> bytes:
+        """The whole map (options, multi-index sets, coefficients); FromBytes rebuilds it."""
+        return _archive(lambda buf, cap, size: load().mpgb_map_to_bytes(self._h, 0, buf, cap, size))
+
+    FromBytes = staticmethod(lambda data: FromBytes(data))
+
+    def __reduce__(self):
+        return (FromBytes, (self.ToBytes(),))
 
     def torch(self, store_coeffs=True, return_logdet=False):
         from .torch import TorchConditionalMapBase

@@ -92,6 +92,15 @@ SIGNATURES = {
     "mpgb_inverse_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
     "mpgb_launch_count": (C.c_longlong, []),
+    "mpgb_map_is_triangular": (C.c_int, [_MAP, C.POINTER(C.c_int)]),
+    "mpgb_map_to_bytes": (C.c_int, [_MAP, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "mpgb_map_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, _MAPP]),
+    "mpgb_coeff_archive_read": (C.c_int, [C.c_void_p, C.c_size_t, _UP, _UP, _UP, C.c_void_p]),
+    "mpgb_options_to_bytes": (C.c_int, [C.POINTER(mpgb_map_options), C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    "mpgb_options_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(mpgb_map_options)]),
+    "mpgb_mset_to_bytes": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, C.c_void_p, C.c_size_t,
+                                     C.POINTER(C.c_size_t)]),
+    "mpgb_mset_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, _UP, _UP, _UP, _UP, _UP, _UP]),
     "mpgb_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "mpgb_batch_destroy": (C.c_int, [C.c_void_p]),
     "mpgb_batch_fwd_adj": (C.c_int, [C.c_void_p, C.POINTER(mpgb_matrix), C.POINTER(mpgb_matrix), C.c_double,

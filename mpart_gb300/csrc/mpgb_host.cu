@@ -1392,6 +1392,13 @@ int mpgb_map_num_components(const mpgb_map* map, unsigned int* n) {
     });
 }
 
+int mpgb_map_is_triangular(const mpgb_map* map, int* is_triangular) {
+    return guard([&] {
+        if (!map || !is_triangular) throw std::invalid_argument("null argument");
+        *is_triangular = dynamic_cast<TriangularMap*>(map->obj.get()) ? 1 : 0;
+    });
+}
+
 int mpgb_map_get_component(mpgb_map* map, unsigned int i, mpgb_map** out) {
     return guard([&] {
         if (!map || !out) throw std::invalid_argument("null argument");
