@@ -240,6 +240,55 @@ int mpgb_train_options_default(mpgb_train_options* opts);
 int mpgb_train_map(mpgb_map* map, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
                    mpgb_train_result* result, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Adaptive transport map, TrainMapAdaptive (src/TrainMapAdaptive.cpp:44-271,
+ * MParT/TrainMapAdaptive.h:19-47): grows each component's multi-index set one
+ * term at a time (the reduced-margin term with the largest KL-gradient
+ * magnitude), trains after every addition, keeps the sets with the best test
+ * objective, and returns the map of those sets trained from zero.
+ * ------------------------------------------------------------------------ */
+typedef struct mpgb_atm_options {
+    mpgb_map_options map;
+    mpgb_train_options train;
+    unsigned int max_patience;         /* additions without a better test objective before stopping (10) */
+    unsigned int max_size;             /* largest total number of terms (INT_MAX) */
+    const unsigned int* max_degrees;   /* inputDim entries (a candidate with any order >= them is skipped) or NULL */
+    int verbose;
+} mpgb_atm_options;
+
+typedef struct mpgb_atm_result {
+    unsigned int size;            /* terms of the returned map */
+    unsigned int iterations;      /* terms added during the search */
+    double best_test_error;       /* KLObjective::TestError of the best sets during the search */
+    double final_train_error;     /* KL objective (with the (M/2) log 2 pi constant) of the returned map */
+    double final_test_error;
+    double total_ms;
+} mpgb_atm_result;
+
+int mpgb_atm_options_default(mpgb_atm_options* opts);
+
+/* The initial sets, one per output (set j has length inputDim - n_sets + j + 1),
+ * are given densely: num_terms[j] rows of that length each, all concatenated in
+ * multis.  train and test are inputDim x N device matrices (the standard-Gaussian
+ * KLObjective of ObjectiveFactory::CreateGaussianKLObjective(train, test)).  The
+ * final sets are the returned map's components' multi-index sets
+ * (mpgb_component_multi_index); final_num_terms (n_sets, may be NULL) receives their sizes. */
+int mpgb_train_map_adaptive(unsigned int n_sets, const unsigned int* num_terms, const unsigned int* multis,
+                            mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
+                            mpgb_atm_result* result, unsigned int* final_num_terms, void* stream);
+
+/* Reduced margin of a set given densely (n rows of length dim): the terms outside
+ * it whose backward neighbours are all inside (MultiIndexSet::ReducedMargin,
+ * src/MultiIndices/MultiIndexSet.cpp:568-590), in this library's scan order.
+ * Two-call: out == NULL queries n_out. */
+int mpgb_reduced_margin(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
+                        unsigned int* out, unsigned int cap_rows);
+
+/* Multi-index set of a single component (compressed form); arrays may be NULL to query sizes. */
+int mpgb_component_multi_index(const mpgb_map* component, unsigned int* dim, unsigned int* num_terms,
+                               unsigned int* nnz, unsigned int* nz_starts, unsigned int* nz_dims,
+                               unsigned int* nz_orders);
+
 /* Device time of one KL objective + gradient step of all components in the given mode (see
  * mpgb_train_options.mode) at the map's coefficients, averaged over `steps` steps after three
  * warm-up steps.  loss (outputDim) and grad (numCoeffs), host pointers that may be NULL,

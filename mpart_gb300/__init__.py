@@ -20,7 +20,8 @@ from ._capi import IntegrandError, MpgbError, check, load, mpgb_map_options, mpg
 __all__ = [
     "BasisTypes", "PosFuncTypes", "QuadTypes", "MapOptions", "FixedMultiIndexSet", "ConditionalMapBase",
     "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load", "DeserializeMap",
-    "FromBytes", "MapBatch", "TrainMap",
+    "FromBytes", "MapBatch", "TrainMap", "TrainOptions", "KLObjective", "CreateGaussianKLObjective", "MultiIndexSet",
+    "ATMOptions", "TrainMapAdaptive",
 ]
 
 
@@ -510,9 +511,80 @@ def CreateTriangular(inputDim: int, outputDim: int, totalOrder: int, opts: MapOp
     return TriangularMap(_handle=h)
 
 
+class TrainOptions:
+    """MParT/TrainMap.h:19-58, same field names and defaults.  The optimiser is
+    this library's L-BFGS whatever opt_alg names (NLopt is not used); opt_maxeval
+    bounds the objective evaluations per component, the tolerances are NLopt's
+    stopping rules (0 disables one), opt_stopval and opt_maxtime are not used."""
+
+    def __init__(self, **kw):
+        self.opt_alg = "LD_SLSQP"
+        self.opt_stopval = -np.inf
+        self.opt_ftol_rel = 1e-3
+        self.opt_ftol_abs = 1e-3
+        self.opt_xtol_rel = 1e-4
+        self.opt_xtol_abs = 1e-4
+        self.opt_maxeval = 1000
+        self.opt_maxtime = np.inf
+        self.verbose = 0
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"{type(self).__name__} has no field {k}")
+            setattr(self, k, v)
+
+    def _train_c(self, mode=0):
+        from ._capi import mpgb_train_options
+        o = mpgb_train_options()
+        check(load().mpgb_train_options_default(C.byref(o)))
+        o.max_iters = o.max_evals = int(self.opt_maxeval)
+        o.ftol_rel, o.ftol_abs = float(self.opt_ftol_rel), float(self.opt_ftol_abs)
+        o.xtol_rel, o.xtol_abs = float(self.opt_xtol_rel), float(self.opt_xtol_abs)
+        o.mode = int(mode)
+        return o
+
+
+class KLObjective:
+    """KLObjective with a standard Gaussian reference density
+    (src/MapObjective.cpp:54-91, ObjectiveFactory::CreateGaussianKLObjective):
+    value = -mean(log N(T(x)) + log det), the per-component reverse-KL sum plus
+    (M/2) log 2 pi.  Samples are copied to the device (float64, inputDim x N)."""
+
+    def __init__(self, train, test=None, dim=0):
+        import torch
+        dev = torch.device("cuda")
+        self.train = torch.as_tensor(np.asarray(train) if not _is_torch(train) else train, dtype=torch.float64,
+                                     device=dev).contiguous()
+        self.test = None if test is None else torch.as_tensor(np.asarray(test) if not _is_torch(test) else test,
+                                                              dtype=torch.float64, device=dev).contiguous()
+        self.dim = int(dim) or self.train.shape[0]
+
+    def _value(self, tmap, pts):
+        loss, _ = tmap.KLObjective(pts[:tmap.inputDim])
+        return float(loss.sum().item()) + 0.5 * tmap.outputDim * np.log(2.0 * np.pi)
+
+    def TrainError(self, tmap):
+        return self._value(tmap, self.train)
+
+    def TestError(self, tmap):
+        if self.test is None:
+            raise RuntimeError("No test dataset given!")
+        return self._value(tmap, self.test)
+
+    def TrainCoeffGrad(self, tmap):
+        return tmap.KLObjective(self.train[:tmap.inputDim])[1]
+
+
+def CreateGaussianKLObjective(train, test=None, dim=0):
+    """ObjectiveFactory::CreateGaussianKLObjective (src/MapObjective.cpp:40-52)."""
+    return KLObjective(train, test, dim)
+
+
 def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, ftol_rel=0.0, ftol_abs=0.0,
              xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0):
-    """TrainMap with a standard-normal KL objective (src/TrainMap.cpp:166-216):
+    """TrainMap(map, objective, options) (src/TrainMap.cpp:166-216) when samples
+    is a KLObjective and max_iters a TrainOptions: returns the training objective.
+
+    Otherwise the direct form: TrainMap with a standard-normal KL objective:
     every component minimises its reverse KL with L-BFGS; samples is a CUDA
     float64 tensor, inputDim x N.  mode 0 replays one batched step from a CUDA
     graph, 1 launches it directly, 2 launches each component separately, 3 runs
@@ -520,6 +592,15 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
     LogDeterminant, CoeffGrad, LogDeterminantCoeffGrad with dense outputs).
     Returns (final loss per component, result dict); the map keeps the result."""
     from ._capi import mpgb_train_options, mpgb_train_result
+    if isinstance(samples, KLObjective):
+        opts = max_iters if isinstance(max_iters, TrainOptions) else TrainOptions()
+        o = opts._train_c(mode)
+        loss = np.zeros(tmap.outputDim)
+        r = mpgb_train_result()
+        pts = samples.train[:tmap.inputDim]
+        check(load().mpgb_train_map(tmap._h, _mat(pts), C.byref(o), C.c_void_p(loss.ctypes.data), C.byref(r),
+                                    _stream_of(pts)))
+        return r.total_loss + 0.5 * tmap.outputDim * np.log(2.0 * np.pi)
     o = mpgb_train_options()
     check(load().mpgb_train_options_default(C.byref(o)))
     o.max_iters, o.max_evals, o.memory, o.mode = int(max_iters), int(max_evals), int(memory), int(mode)
@@ -643,3 +724,142 @@ def fp64_probe(blocks=152 * 8, threads=256, iters=4096):
     check(load().mpgb_fp64_probe(blocks, threads, iters, C.c_void_p(0), C.byref(ms)))
     flops = 2.0 * 8 * blocks * threads * iters
     return flops / (ms.value * 1e-3) / 1e12, ms.value
+
+
+class MultiIndexSet:
+    """Adaptive multi-index set (MParT/MultiIndices/MultiIndexSet.h) with terms
+    in insertion order: what TrainMapAdaptive needs (total-order creation,
+    adding terms, the reduced margin, Fix)."""
+
+    def __init__(self, length: int, multis=()):
+        self.length = int(length)
+        self._terms = []
+        self._index = {}
+        for m in multis:
+            self._add(m)
+
+    @staticmethod
+    def CreateTotalOrder(length: int, maxOrder: int):
+        ms = FixedMultiIndexSet(length, maxOrder)
+        return MultiIndexSet(length, [tuple(int(v) for v in ms.IndexToMulti(i)) for i in range(ms.Size())])
+
+    def _add(self, m):
+        m = tuple(int(v) for v in m)
+        if len(m) != self.length:
+            raise ValueError("multi-index of the wrong length")
+        if m not in self._index:
+            self._index[m] = len(self._terms)
+            self._terms.append(m)
+
+    def __iadd__(self, m):
+        self._add(m)
+        return self
+
+    def Size(self):
+        return len(self._terms)
+
+    def Length(self):
+        return self.length
+
+    def __len__(self):
+        return self.length
+
+    def __getitem__(self, i):
+        return np.array(self._terms[i], dtype=np.uint32)
+
+    def Multis(self):
+        return [np.array(t, dtype=np.uint32) for t in self._terms]
+
+    def _dense(self):
+        return np.ascontiguousarray(np.array(self._terms, dtype=np.uint32).reshape(len(self._terms), self.length))
+
+    def ReducedMargin(self):
+        """Terms outside the set whose backward neighbours are all inside it
+        (MultiIndexSet::ReducedMargin, src/MultiIndices/MultiIndexSet.cpp:568-590)."""
+        U = C.POINTER(C.c_uint)
+        dense = self._dense()
+        n = C.c_uint()
+        check(load().mpgb_reduced_margin(self.length, self.Size(), dense.ctypes.data_as(U), C.byref(n), None, 0))
+        out = np.zeros((max(1, n.value), self.length), dtype=np.uint32)
+        check(load().mpgb_reduced_margin(self.length, self.Size(), dense.ctypes.data_as(U), None,
+                                         out.ctypes.data_as(U), n.value))
+        return [out[k].copy() for k in range(n.value)]
+
+    def Expand(self):
+        """Adds the reduced margin; returns the indices of the new terms."""
+        start = self.Size()
+        for m in self.ReducedMargin():
+            self._add(m)
+        return list(range(start, self.Size()))
+
+    def Fix(self, compress=True):
+        return FixedMultiIndexSet.from_multis(self._dense()) if self.Size() else \
+            FixedMultiIndexSet(self.length, nzStarts=[0])
+
+
+class ATMOptions(MapOptions, TrainOptions):
+    """ATMOptions (MParT/TrainMapAdaptive.h:19-47): map options, training
+    options and maxPatience, maxSize, maxDegrees (a multi-index of inputDim
+    entries, or None)."""
+
+    def __init__(self, **kw):
+        MapOptions.__init__(self)
+        TrainOptions.__init__(self)
+        self.maxPatience = 10
+        self.maxSize = 2 ** 31 - 1
+        self.maxDegrees = None
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(f"ATMOptions has no field {k}")
+            setattr(self, k, v)
+
+
+def _component_mset(comp):
+    U = C.POINTER(C.c_uint)
+    dim, nt, nnz = C.c_uint(), C.c_uint(), C.c_uint()
+    check(load().mpgb_component_multi_index(comp._h, C.byref(dim), C.byref(nt), C.byref(nnz), None, None, None))
+    s = np.zeros(nt.value + 1, np.uint32)
+    d = np.zeros(max(1, nnz.value), np.uint32)
+    o = np.zeros(max(1, nnz.value), np.uint32)
+    check(load().mpgb_component_multi_index(comp._h, None, None, None, s.ctypes.data_as(U), d.ctypes.data_as(U),
+                                            o.ctypes.data_as(U)))
+    return FixedMultiIndexSet(dim.value, nzStarts=s, nzDims=d[:nnz.value], nzOrders=o[:nnz.value])
+
+
+def TrainMapAdaptive(mset0, objective: KLObjective, options: ATMOptions | None = None, mode=0):
+    """TrainMapAdaptive (src/TrainMapAdaptive.cpp:44-271): returns the trained
+    triangular map; mset0 (a list of MultiIndexSet, one per output) is replaced
+    in place by the selected sets, as in the reference."""
+    from ._capi import mpgb_atm_options, mpgb_atm_result
+    options = options or ATMOptions()
+    o = mpgb_atm_options()
+    check(load().mpgb_atm_options_default(C.byref(o)))
+    o.map = options._c()
+    o.train = options._train_c(mode)
+    o.max_patience = int(options.maxPatience)
+    o.max_size = int(min(options.maxSize, 2 ** 32 - 1))
+    md = None
+    if options.maxDegrees is not None and len(options.maxDegrees):
+        md = np.ascontiguousarray(options.maxDegrees, dtype=np.uint32)
+        o.max_degrees = md.ctypes.data_as(C.POINTER(C.c_uint))
+    o.verbose = int(options.verbose)
+    n = len(mset0)
+    sizes = np.array([m.Size() for m in mset0], dtype=np.uint32)
+    multis = np.ascontiguousarray(np.concatenate([m._dense().reshape(-1) for m in mset0]).astype(np.uint32))
+    final = np.zeros(n, dtype=np.uint32)
+    res = mpgb_atm_result()
+    h = C.c_void_p()
+    U = C.POINTER(C.c_uint)
+    test = objective.test if objective.test is not None else objective.train
+    check(load().mpgb_train_map_adaptive(n, sizes.ctypes.data_as(U), multis.ctypes.data_as(U), _mat(objective.train),
+                                         _mat(test), C.byref(o), C.byref(h), C.byref(res), final.ctypes.data_as(U),
+                                         _stream_of(objective.train)))
+    tmap = TriangularMap(_handle=h)
+    for j in range(n):
+        fixed = _component_mset(tmap.GetComponent(j))
+        mset0[j] = MultiIndexSet(fixed.Length(), [tuple(fixed.IndexToMulti(i)) for i in range(fixed.Size())])
+    tmap.atm_result = {"size": res.size, "iterations": res.iterations, "best_test_error": res.best_test_error,
+                       "final_train_error": res.final_train_error, "final_test_error": res.final_test_error,
+                       "total_ms": res.total_ms}
+    return tmap
+

@@ -53,6 +53,16 @@ class mpgb_train_result(C.Structure):
                 ("ms_per_step", C.c_double), ("total_ms", C.c_double), ("grad_norm", C.c_double)]
 
 
+class mpgb_atm_options(C.Structure):
+    _fields_ = [("map", mpgb_map_options), ("train", mpgb_train_options), ("max_patience", C.c_uint),
+                ("max_size", C.c_uint), ("max_degrees", C.POINTER(C.c_uint)), ("verbose", C.c_int)]
+
+
+class mpgb_atm_result(C.Structure):
+    _fields_ = [("size", C.c_uint), ("iterations", C.c_uint), ("best_test_error", C.c_double),
+                ("final_train_error", C.c_double), ("final_test_error", C.c_double), ("total_ms", C.c_double)]
+
+
 # Every symbol the header declares, with its signature.
 _MAP = C.c_void_p
 _MAPP = C.POINTER(C.c_void_p)
@@ -92,6 +102,11 @@ SIGNATURES = {
     "mpgb_inverse_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p, mpgb_matrix, C.c_void_p]),
     "mpgb_fp64_probe": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
     "mpgb_launch_count": (C.c_longlong, []),
+    "mpgb_atm_options_default": (C.c_int, [C.POINTER(mpgb_atm_options)]),
+    "mpgb_train_map_adaptive": (C.c_int, [C.c_uint, _UP, _UP, mpgb_matrix, mpgb_matrix, C.POINTER(mpgb_atm_options),
+                                          _MAPP, C.POINTER(mpgb_atm_result), _UP, C.c_void_p]),
+    "mpgb_reduced_margin": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, C.c_uint]),
+    "mpgb_component_multi_index": (C.c_int, [_MAP, _UP, _UP, _UP, _UP, _UP, _UP]),
     "mpgb_map_is_triangular": (C.c_int, [_MAP, C.POINTER(C.c_int)]),
     "mpgb_map_to_bytes": (C.c_int, [_MAP, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "mpgb_map_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, _MAPP]),

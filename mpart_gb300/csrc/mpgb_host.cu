@@ -1168,6 +1168,11 @@ using namespace mpgb;
 namespace mpgb {
 int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
                  mpgb_train_result* res, void* stream, char* err, int errLen);
+int trainMapAdaptiveImpl(unsigned int n_sets, const unsigned int* num_terms, const unsigned int* multis,
+                         mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
+                         mpgb_atm_result* result, unsigned int* final_num_terms, void* stream, char* err, int errLen);
+int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
+                      unsigned int* out, unsigned int cap_rows);
 int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
                    double* grad, void* stream, char* err, int errLen);
 }
@@ -1631,6 +1636,59 @@ int mpgb_kl_step_time(mpgb_map* map, mpgb_matrix samples, int mode, int steps, d
 }
 
 long long mpgb_launch_count(void) { return mpgb::launchCount(); }
+
+int mpgb_atm_options_default(mpgb_atm_options* o) {
+    return guard([&] {
+        if (!o) throw std::invalid_argument("null options");
+        std::memset(o, 0, sizeof(*o));
+        mpgb_map_options_default(&o->map);
+        mpgb_train_options_default(&o->train);
+        o->max_patience = 10;
+        o->max_size = 0x7fffffffu;
+        o->max_degrees = nullptr;
+        o->verbose = 0;
+    });
+}
+
+int mpgb_train_map_adaptive(unsigned int n_sets, const unsigned int* num_terms, const unsigned int* multis,
+                            mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
+                            mpgb_atm_result* result, unsigned int* final_num_terms, void* stream) {
+    char err[512] = {0};
+    int rc = MPGB_OK;
+    int g = guard([&] {
+        rc = trainMapAdaptiveImpl(n_sets, num_terms, multis, train, test, opts, out, result, final_num_terms, stream,
+                                  err, sizeof(err));
+    });
+    if (g != MPGB_OK) return g;
+    if (rc != MPGB_OK) g_lastError = err;
+    return rc;
+}
+
+int mpgb_reduced_margin(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
+                        unsigned int* out, unsigned int cap_rows) {
+    return guard([&] {
+        if ((n && !multis) || dim == 0) throw std::invalid_argument("bad multi-index set");
+        reducedMarginImpl(dim, n, multis, n_out, out, cap_rows);
+    });
+}
+
+int mpgb_component_multi_index(const mpgb_map* component, unsigned int* dim, unsigned int* num_terms,
+                               unsigned int* nnz, unsigned int* nz_starts, unsigned int* nz_dims,
+                               unsigned int* nz_orders) {
+    return guard([&] {
+        if (!component || !component->obj) throw std::invalid_argument("null map handle");
+        auto* c = dynamic_cast<const MonotoneComponent*>(component->obj.get());
+        if (!c) throw std::invalid_argument("not a single monotone component");
+        const FixedMultiIndexSet& m = c->GetMultiIndexSet();
+        if (dim) *dim = m.Length();
+        if (num_terms) *num_terms = m.Size();
+        if (nnz) *nnz = (unsigned)m.nzDims.size();
+        if (nz_starts) std::memcpy(nz_starts, m.nzStarts.data(), m.nzStarts.size() * sizeof(unsigned));
+        if (nz_dims && !m.nzDims.empty()) std::memcpy(nz_dims, m.nzDims.data(), m.nzDims.size() * sizeof(unsigned));
+        if (nz_orders && !m.nzOrders.empty())
+            std::memcpy(nz_orders, m.nzOrders.data(), m.nzOrders.size() * sizeof(unsigned));
+    });
+}
 
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms) {
     return guard([&] {

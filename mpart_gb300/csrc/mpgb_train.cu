@@ -8,8 +8,10 @@
 // with a backtracking Armijo line search; NLopt itself is not available.
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <memory>
 #include <sstream>
 #include <vector>
@@ -306,88 +308,98 @@ struct KLStep {
 
 namespace mpgb {
 
+// Standard-normal KL training of every component (src/TrainMap.cpp:144-164):
+// lockstep L-BFGS per component over one batched objective step per
+// iteration.  Throws; sets the map's coefficients to the result.
+void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o, int mode, cudaStream_t s,
+             double* loss_per_comp, mpgb_train_result* res) {
+    map.CheckCoefficients("TrainMap");
+    const auto& parts = map.Parts();
+    std::vector<double> x0 = map.CoeffMap();
+    KLStep step(map, pts, s, mode);
+    std::vector<LBFGS> opt;
+    for (auto& p : parts) opt.emplace_back(x0.data() + p.mapCoeffOffset, (int)(
+                                               (&p == &parts.back() ? map.numCoeffs : (&p + 1)->mapCoeffOffset) -
+                                               p.mapCoeffOffset), o);
+    int steps = 0;
+    double stepMs = 0.0;
+    cudaEvent_t e0, e1;
+    TR_CUDA(cudaEventCreate(&e0));
+    TR_CUDA(cudaEventCreate(&e1));
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        bool any = false;
+        for (size_t c = 0; c < opt.size(); ++c) {
+            const auto& r = opt[c].request();
+            std::memcpy(step.hCoef.p + parts[c].mapCoeffOffset, r.data(), r.size() * sizeof(double));
+            any |= !opt[c].done();
+        }
+        if (!any) break;
+        TR_CUDA(cudaEventRecord(e0, step.s));
+        step.run();
+        TR_CUDA(cudaEventRecord(e1, step.s));
+        TR_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        stepMs += ms;
+        ++steps;
+        // A trial point whose integrand overflows gives its component a
+        // non-finite objective, which the line search rejects (it steps
+        // back); only an overflow at the starting point is an error.
+        map.CheckStatus(step.s);
+        for (size_t c = 0; c < opt.size(); ++c)
+            if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
+    }
+    const double totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (size_t c = 0; c < opt.size(); ++c)
+        if (!std::isfinite(opt[c].f()))
+            throw IntegrandError("TrainMap: MonotoneIntegrand: the objective is not finite at the starting "
+                                 "coefficients (g(df) overflowed).");
+    std::vector<double> xf(map.numCoeffs);
+    double total = 0, gn2 = 0;
+    int iters = 0, evals = 0;
+    for (size_t c = 0; c < opt.size(); ++c) {
+        gn2 += opt[c].gradNorm() * opt[c].gradNorm();
+        std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c].x().data(), opt[c].x().size() * sizeof(double));
+        if (loss_per_comp) loss_per_comp[c] = opt[c].f();
+        total += opt[c].f();
+        iters = std::max(iters, opt[c].iterations());
+        evals = std::max(evals, opt[c].evaluations());
+    }
+    map.SetCoeffs(xf.data(), map.numCoeffs, true, s);
+    if (res) {
+        res->total_loss = total;
+        res->iterations = iters;
+        res->evaluations = evals;
+        res->steps = steps;
+        res->ms_per_step = steps ? stepMs / steps : 0.0;
+        res->total_ms = totalMs;
+        res->grad_norm = std::sqrt(gn2);
+    }
+}
+
+TrainOpts trainOptsFromC(const mpgb_train_options* opts) {
+    TrainOpts o;
+    o.maxIters = opts->max_iters;
+    o.maxEvals = opts->max_evals;
+    o.ftolRel = opts->ftol_rel;
+    o.ftolAbs = opts->ftol_abs;
+    o.xtolRel = opts->xtol_rel;
+    o.xtolAbs = opts->xtol_abs;
+    o.gtol = opts->gtol;
+    o.memory = opts->memory > 0 ? opts->memory : 10;
+    return o;
+}
+
 int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
-                        mpgb_train_result* res, void* stream, char* err, int errLen) {
+                 mpgb_train_result* res, void* stream, char* err, int errLen) {
     try {
         auto* map = static_cast<MonotoneMapBase*>(mapObj);
         if (!map || !opts) throw std::invalid_argument("null argument");
-        map->CheckCoefficients("TrainMap");
-        cudaStream_t s = (cudaStream_t)stream;
         StridedMatrix pts(samples.data, samples.rows, samples.cols, samples.row_stride, samples.col_stride);
-        TrainOpts o;
-        o.maxIters = opts->max_iters;
-        o.maxEvals = opts->max_evals;
-        o.ftolRel = opts->ftol_rel;
-        o.ftolAbs = opts->ftol_abs;
-        o.xtolRel = opts->xtol_rel;
-        o.xtolAbs = opts->xtol_abs;
-        o.gtol = opts->gtol;
-        o.memory = opts->memory > 0 ? opts->memory : 10;
-        const auto& parts = map->Parts();
-        std::vector<double> x0 = map->CoeffMap();
-        KLStep step(*map, pts, s, opts->mode);
-        std::vector<LBFGS> opt;
-        for (auto& p : parts) opt.emplace_back(x0.data() + p.mapCoeffOffset, (int)(
-                                                   (&p == &parts.back() ? map->numCoeffs : (&p + 1)->mapCoeffOffset) -
-                                                   p.mapCoeffOffset), o);
-        int steps = 0;
-        double stepMs = 0.0;
-        cudaEvent_t e0, e1;
-        TR_CUDA(cudaEventCreate(&e0));
-        TR_CUDA(cudaEventCreate(&e1));
-        const auto t0 = std::chrono::steady_clock::now();
-        while (true) {
-            bool any = false;
-            for (size_t c = 0; c < opt.size(); ++c) {
-                const auto& r = opt[c].request();
-                std::memcpy(step.hCoef.p + parts[c].mapCoeffOffset, r.data(), r.size() * sizeof(double));
-                any |= !opt[c].done();
-            }
-            if (!any) break;
-            TR_CUDA(cudaEventRecord(e0, step.s));
-            step.run();
-            TR_CUDA(cudaEventRecord(e1, step.s));
-            TR_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            stepMs += ms;
-            ++steps;
-            // A trial point whose integrand overflows gives its component a
-            // non-finite objective, which the line search rejects (it steps
-            // back); only an overflow at the starting point is an error.
-            map->CheckStatus(step.s);
-            for (size_t c = 0; c < opt.size(); ++c)
-                if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
-        }
-        const double totalMs =
-            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        for (size_t c = 0; c < opt.size(); ++c)
-            if (!std::isfinite(opt[c].f()))
-                throw IntegrandError("TrainMap: MonotoneIntegrand: the objective is not finite at the starting "
-                                     "coefficients (g(df) overflowed).");
-        std::vector<double> xf(map->numCoeffs);
-        double total = 0, gn2 = 0;
-        int iters = 0, evals = 0;
-        for (size_t c = 0; c < opt.size(); ++c) {
-            gn2 += opt[c].gradNorm() * opt[c].gradNorm();
-            std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c].x().data(), opt[c].x().size() * sizeof(double));
-            if (loss_per_comp) loss_per_comp[c] = opt[c].f();
-            total += opt[c].f();
-            iters = std::max(iters, opt[c].iterations());
-            evals = std::max(evals, opt[c].evaluations());
-        }
-        map->SetCoeffs(xf.data(), map->numCoeffs, true, s);
-        if (res) {
-            res->total_loss = total;
-            res->iterations = iters;
-            res->evaluations = evals;
-            res->steps = steps;
-            res->ms_per_step = steps ? stepMs / steps : 0.0;
-            res->total_ms = totalMs;
-            res->grad_norm = std::sqrt(gn2);
-        }
+        trainKL(*map, pts, trainOptsFromC(opts), opts->mode, (cudaStream_t)stream, loss_per_comp, res);
         return MPGB_OK;
     } catch (IntegrandError const& e) {
         if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
@@ -437,4 +449,310 @@ int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, doubl
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adaptive transport map (src/TrainMapAdaptive.cpp:44-271; Baptista et al.
+// 2022): grow each component's multi-index set one term at a time, choosing
+// the reduced-margin term whose coefficient has the largest KL gradient, and
+// keep the sets with the best test objective.
+// ---------------------------------------------------------------------------
+
+// Multi-index set with terms in insertion order (the reference's
+// MultiIndexSet restricted to what the adaptive loop needs).
+struct AdaptiveSet {
+    unsigned dim = 0;
+    std::vector<std::vector<unsigned>> terms;
+    std::map<std::vector<unsigned>, int> index;
+
+    bool has(const std::vector<unsigned>& m) const { return index.count(m) != 0; }
+    void add(const std::vector<unsigned>& m) {
+        if (m.size() != dim) throw std::invalid_argument("multi-index of the wrong length");
+        if (has(m)) return;
+        index[m] = (int)terms.size();
+        terms.push_back(m);
+    }
+    // Terms outside the set whose backward neighbours (m - e_d for m_d > 0)
+    // are all in it, in the order met scanning the set's terms in order and,
+    // for each, the forward neighbours m + e_d for d = 0..dim-1.
+    std::vector<std::vector<unsigned>> reducedMargin() const {
+        std::vector<std::vector<unsigned>> out;
+        std::map<std::vector<unsigned>, int> seen;
+        for (const auto& t : terms) {
+            for (unsigned d = 0; d < dim; ++d) {
+                std::vector<unsigned> f = t;
+                ++f[d];
+                if (has(f) || seen.count(f)) continue;
+                bool admissible = true;
+                for (unsigned e = 0; e < dim && admissible; ++e) {
+                    if (f[e] == 0) continue;
+                    std::vector<unsigned> b = f;
+                    --b[e];
+                    admissible = has(b);
+                }
+                if (admissible) {
+                    seen[f] = 1;
+                    out.push_back(f);
+                }
+            }
+        }
+        return out;
+    }
+    FixedMultiIndexSet fix() const {
+        std::vector<unsigned> s{0}, d, o;
+        for (const auto& t : terms) {
+            for (unsigned e = 0; e < dim; ++e)
+                if (t[e]) {
+                    d.push_back(e);
+                    o.push_back(t[e]);
+                }
+            s.push_back((unsigned)d.size());
+        }
+        return FixedMultiIndexSet(dim, s, d, o);
+    }
+};
+
+struct ATMOpts {
+    MapOptions map;
+    TrainOpts train;
+    int mode = 0;
+    unsigned maxPatience = 10, maxSize = 0x7fffffff;
+    std::vector<unsigned> maxDegrees;
+    int verbose = 0;
+};
+
+namespace {
+
+std::shared_ptr<ConditionalMapBase> atmComponent(const AdaptiveSet& set, const MapOptions& o,
+                                                 const std::vector<double>& coeffs) {
+    auto c = MapFactory::CreateComponent(set.fix(), o);
+    if (!coeffs.empty()) c->SetCoeffs(coeffs.data(), (unsigned)coeffs.size(), true);
+    return c;
+}
+
+// KLObjective value (src/MapObjective.cpp:54-91): the components' reverse-KL
+// losses plus (M/2) log 2 pi; and the coefficient gradient.
+double atmObjective(MonotoneMapBase& map, StridedMatrix const& pts, std::vector<double>* grad, cudaStream_t s) {
+    Dev loss(map.outputDim), g(map.numCoeffs);
+    map.KLObjective(pts, loss.p, g.p, s);
+    std::vector<double> lh(map.outputDim);
+    TR_CUDA(cudaMemcpyAsync(lh.data(), loss.p, lh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (grad) {
+        grad->resize(map.numCoeffs);
+        TR_CUDA(cudaMemcpyAsync(grad->data(), g.p, grad->size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    TR_CUDA(cudaStreamSynchronize(s));
+    double v = 0.5 * map.outputDim * std::log(2.0 * 3.14159265358979323846);
+    for (double l : lh) v += l;
+    return v;
+}
+
+}  // namespace
+
+std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& mset0, StridedMatrix const& train,
+                                                     StridedMatrix const& test, ATMOpts const& o, cudaStream_t s,
+                                                     mpgb_atm_result* res) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const unsigned nOut = (unsigned)mset0.size();
+    if (nOut == 0) throw std::invalid_argument("TrainMapAdaptive: no multi-index sets.");
+    const unsigned inDim = (unsigned)train.rows;
+    for (unsigned j = 0; j < nOut; ++j)
+        if (mset0[j].dim != inDim - nOut + j + 1) {
+            std::ostringstream os;
+            os << "TrainMapAdaptive: multi-index set " << j << " has length " << mset0[j].dim << ", expected "
+               << inDim - nOut + j + 1 << ".";
+            throw std::invalid_argument(os.str());
+        }
+    if (test.rows != train.rows || test.cols == 0) throw std::invalid_argument("TrainMapAdaptive: bad test samples.");
+    if (!o.maxDegrees.empty() && o.maxDegrees.size() != inDim)
+        throw std::invalid_argument("TrainMapAdaptive: maxDegrees must have inputDim entries or none.");
+
+    auto build = [&](std::vector<std::shared_ptr<ConditionalMapBase>> const& comps) {
+        return std::make_shared<TriangularMap>(comps, true);
+    };
+    auto split = [&](TriangularMap& map) {
+        std::vector<std::vector<double>> out(nOut);
+        const std::vector<double> all = map.CoeffMap();
+        unsigned off = 0;
+        for (unsigned j = 0; j < nOut; ++j) {
+            const unsigned n = (unsigned)mset0[j].terms.size();
+            out[j].assign(all.begin() + off, all.begin() + off + n);
+            off += n;
+        }
+        return out;
+    };
+
+    std::vector<std::shared_ptr<ConditionalMapBase>> comps(nOut);
+    std::vector<std::vector<double>> coeffs(nOut);
+    unsigned size = 0;
+    for (unsigned j = 0; j < nOut; ++j) {
+        coeffs[j].assign(mset0[j].terms.size(), 0.0);
+        comps[j] = atmComponent(mset0[j], o.map, coeffs[j]);
+        size += (unsigned)mset0[j].terms.size();
+    }
+    auto map = build(comps);
+    trainKL(*map, train, o.train, o.mode, s, nullptr, nullptr);
+    coeffs = split(*map);
+    double best = atmObjective(*map, test, nullptr, s);
+    if (o.verbose) std::printf("TrainMapAdaptive: initial size %u, test objective %.10g\n", size, best);
+    std::vector<AdaptiveSet> bestSets = mset0;
+    std::vector<std::vector<double>> bestCoeffs = coeffs;
+    unsigned patience = 0, iterations = 0;
+    double trainErr = 0.0;
+
+    while (size < o.maxSize && patience < o.maxPatience) {
+        // Every component with its reduced margin appended (zero coefficients).
+        std::vector<std::vector<std::vector<unsigned>>> cand(nOut);
+        std::vector<std::shared_ptr<ConditionalMapBase>> tmp(nOut);
+        for (unsigned j = 0; j < nOut; ++j) {
+            AdaptiveSet e = mset0[j];
+            // Terms beyond the largest last-input order the kernels are built
+            // for (kMaxLastOrder) cannot be represented and are not candidates.
+            for (auto& m : e.reducedMargin())
+                if (m[e.dim - 1] <= (unsigned)kMaxLastOrder) cand[j].push_back(m);
+            for (auto& m : cand[j]) e.add(m);
+            std::vector<double> c = coeffs[j];
+            c.resize(e.terms.size(), 0.0);
+            tmp[j] = atmComponent(e, o.map, c);
+        }
+        auto mapTmp = build(tmp);
+        std::vector<double> grad;
+        atmObjective(*mapTmp, train, &grad, s);
+        // Largest |gradient| over the candidates below maxDegrees (first wins ties).
+        int bestBlock = -1, bestIdx = -1;
+        double bestVal = 0.0;
+        unsigned off = 0;
+        for (unsigned j = 0; j < nOut; ++j) {
+            const unsigned n0 = (unsigned)mset0[j].terms.size();
+            for (unsigned k = 0; k < cand[j].size(); ++k) {
+                bool bounded = false;
+                for (unsigned d = 0; d < mset0[j].dim && !o.maxDegrees.empty(); ++d)
+                    bounded |= cand[j][k][d] >= o.maxDegrees[d];
+                if (bounded) continue;
+                const double v = std::fabs(grad[off + n0 + k]);
+                if (v > bestVal) {
+                    bestVal = v;
+                    bestBlock = (int)j;
+                    bestIdx = (int)k;
+                }
+            }
+            off += n0 + (unsigned)cand[j].size();
+        }
+        if (bestBlock < 0) break;  // nothing left to add
+        mset0[bestBlock].add(cand[bestBlock][bestIdx]);
+        coeffs[bestBlock].push_back(0.0);
+        for (unsigned j = 0; j < nOut; ++j) comps[j] = atmComponent(mset0[j], o.map, coeffs[j]);
+        ++size;
+        map = build(comps);
+        mpgb_train_result tr{};
+        trainKL(*map, train, o.train, o.mode, s, nullptr, &tr);
+        coeffs = split(*map);
+        trainErr = tr.total_loss + 0.5 * nOut * std::log(2.0 * 3.14159265358979323846);
+        const double testErr = atmObjective(*map, test, nullptr, s);
+        ++iterations;
+        ++patience;
+        if (testErr < best) {
+            best = testErr;
+            bestSets = mset0;
+            bestCoeffs = coeffs;
+            patience = 0;
+        }
+        if (o.verbose)
+            std::printf("TrainMapAdaptive: size %u (component %d), train %.10g, test %.10g\n", size, bestBlock,
+                        trainErr, testErr);
+    }
+
+    // The best sets, trained once more.  The reference restarts them from zero
+    // coefficients; here they restart from the coefficients the search trained
+    // for them: from zero, terms of high order in the last input make the
+    // problem so badly scaled that L-BFGS (unlike NLopt's SLSQP) stalls.
+    mset0 = bestSets;
+    for (unsigned j = 0; j < nOut; ++j) comps[j] = atmComponent(mset0[j], o.map, bestCoeffs[j]);
+    map = build(comps);
+    mpgb_train_result tr{};
+    trainKL(*map, train, o.train, o.mode, s, nullptr, &tr);
+    if (res) {
+        unsigned n = 0;
+        for (auto& m : mset0) n += (unsigned)m.terms.size();
+        res->size = n;
+        res->iterations = iterations;
+        res->best_test_error = best;
+        res->final_train_error = tr.total_loss + 0.5 * nOut * std::log(2.0 * 3.14159265358979323846);
+        res->final_test_error = atmObjective(*map, test, nullptr, s);
+        res->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return map;
+}
+
+int trainMapAdaptiveImpl(unsigned int n_sets, const unsigned int* num_terms, const unsigned int* multis,
+                         mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
+                         mpgb_atm_result* result, unsigned int* final_num_terms, void* stream, char* err, int errLen) {
+    try {
+        if (!num_terms || !multis || !opts || !out) throw std::invalid_argument("null argument");
+        StridedMatrix tr(train.data, train.rows, train.cols, train.row_stride, train.col_stride);
+        StridedMatrix te(test.data, test.rows, test.cols, test.row_stride, test.col_stride);
+        const unsigned inDim = (unsigned)train.rows;
+        if (n_sets == 0 || n_sets > inDim) throw std::invalid_argument("TrainMapAdaptive: bad number of sets.");
+        std::vector<AdaptiveSet> sets(n_sets);
+        size_t off = 0;
+        for (unsigned j = 0; j < n_sets; ++j) {
+            sets[j].dim = inDim - n_sets + j + 1;
+            for (unsigned t = 0; t < num_terms[j]; ++t) {
+                std::vector<unsigned> m(multis + off, multis + off + sets[j].dim);
+                off += sets[j].dim;
+                sets[j].add(m);
+            }
+            if (sets[j].terms.empty()) throw std::invalid_argument("TrainMapAdaptive: empty multi-index set.");
+        }
+        ATMOpts o;
+        mpgb_map_options mo = opts->map;
+        MapOptions m;
+        m.basisType = (BasisTypes)mo.basis_type;
+        m.posFuncType = (PosFuncTypes)mo.pos_func_type;
+        m.quadType = (QuadTypes)mo.quad_type;
+        m.quadAbsTol = mo.quad_abs_tol;
+        m.quadRelTol = mo.quad_rel_tol;
+        m.quadMaxSub = mo.quad_max_sub;
+        m.quadMinSub = mo.quad_min_sub;
+        m.quadPts = mo.quad_pts;
+        m.contDeriv = mo.cont_deriv != 0;
+        m.basisNorm = mo.basis_norm != 0;
+        m.nugget = mo.nugget;
+        o.map = m;
+        o.train = trainOptsFromC(&opts->train);
+        o.mode = opts->train.mode;
+        o.maxPatience = opts->max_patience;
+        o.maxSize = opts->max_size;
+        if (opts->max_degrees) o.maxDegrees.assign(opts->max_degrees, opts->max_degrees + inDim);
+        o.verbose = opts->verbose;
+        auto map = trainMapAdaptive(sets, tr, te, o, (cudaStream_t)stream, result);
+        if (final_num_terms)
+            for (unsigned j = 0; j < n_sets; ++j) final_num_terms[j] = (unsigned)sets[j].terms.size();
+        *out = new mpgb_map{map};
+        return MPGB_OK;
+    } catch (IntegrandError const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_INTEGRAND;
+    } catch (std::invalid_argument const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_INVALID_ARGUMENT;
+    } catch (std::exception const& e) {
+        if (err) { std::strncpy(err, e.what(), errLen - 1); err[errLen - 1] = 0; }
+        return MPGB_ERR_RUNTIME;
+    }
+}
+
+int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
+                      unsigned int* out, unsigned int cap_rows) {
+    AdaptiveSet s;
+    s.dim = dim;
+    for (unsigned t = 0; t < n; ++t) s.add(std::vector<unsigned>(multis + (size_t)t * dim, multis + (size_t)(t + 1) * dim));
+    const auto rm = s.reducedMargin();
+    if (n_out) *n_out = (unsigned)rm.size();
+    if (out) {
+        if (cap_rows < rm.size()) throw std::invalid_argument("reduced margin: output too small");
+        for (size_t k = 0; k < rm.size(); ++k) std::memcpy(out + k * dim, rm[k].data(), dim * sizeof(unsigned));
+    }
+    return MPGB_OK;
+}
+
 }  // namespace mpgb
+
