@@ -39,10 +39,20 @@ constexpr int kStatusNaN = 2;          // the integrand was NaN
 constexpr int kStatusBudget = 4;       // interval budget exhausted
 constexpr int kStatusNoBracket = 8;    // inverse: bracket search failed (info=-2)
 
-// Quadrature rule and tolerances (AdaptiveClenshawCurtis, Quadrature.h:729-1009).
+// Quadrature kinds (MapOptions::quadType values).
+constexpr int kQuadFixedCC = 0;   // ClenshawCurtis: one fixed rule on [0, 1] (Quadrature.h:114-143)
+constexpr int kQuadSimpson = 1;   // AdaptiveSimpson (Quadrature.h:497-716)
+constexpr int kQuadACC = 2;       // AdaptiveClenshawCurtis (Quadrature.h:729-1009)
+
+// Quadrature rule and tolerances.  The adaptive kinds share one traversal:
+// a coarse and a nested fine rule on [-1, 1] (fine node 2i = coarse node i),
+// scaled by the interval's half width; AdaptiveSimpson is the pair (Simpson
+// on the interval, composite Simpson on its halves).  The fixed kind uses the
+// fine rule alone.
 struct QuadParams {
     double cPts[kMaxRulePts], cWts[kMaxRulePts];
     double fPts[kMaxRulePts], fWts[kMaxRulePts];
+    int kind;
     int nCoarse, nFine;
     int maxSub, minSub;
     double absTol, relTol;

@@ -285,8 +285,6 @@ static unsigned factorialU(unsigned d) {
 }
 
 static void validateOptions(MapOptions const& o) {
-    if (o.quadType != QuadTypes::AdaptiveClenshawCurtis)
-        throw std::invalid_argument("MapOptions: only quadType = AdaptiveClenshawCurtis is provided on this path.");
     if (o.basisType == BasisTypes::PhysicistHermite)
         throw std::invalid_argument("MapOptions: basisType must be ProbabilistHermite or HermiteFunctions.");
     if (!o.contDeriv)
@@ -294,7 +292,10 @@ static void validateOptions(MapOptions const& o) {
     if (o.quadMaxSub < 1 || o.quadMaxSub > (unsigned)kMaxSubCap)
         throw std::invalid_argument("MapOptions: quadMaxSub must be in [1, 32].");
     if (o.quadMinSub >= o.quadMaxSub) throw std::invalid_argument("MapOptions: quadMinSub must be below quadMaxSub.");
-    if (o.quadPts < 3) throw std::invalid_argument("MapOptions: quadPts must be at least 3.");
+    if (o.quadType == QuadTypes::AdaptiveClenshawCurtis && o.quadPts < 3)
+        throw std::invalid_argument("MapOptions: quadPts must be at least 3.");
+    if (o.quadType == QuadTypes::ClenshawCurtis && (o.quadPts < 1 || o.quadPts > (unsigned)kMaxRulePts))
+        throw std::invalid_argument("MapOptions: ClenshawCurtis quadPts must be in [1, 33].");
     if (!(o.quadAbsTol >= 0) || !(o.quadRelTol >= 0)) throw std::invalid_argument("MapOptions: negative tolerance.");
     if (!(o.nugget >= 0)) throw std::invalid_argument("MapOptions: nugget must be non-negative.");
 }
@@ -307,14 +308,34 @@ MonotoneMapBase::~MonotoneMapBase() = default;
 // Builds the launch tables on first use.
 // Quadrature rules and basis constants of a launch (both engines).
 void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b) {
-    // Quadrature rule: level = (unsigned) log2(quadPts - 2) (src/MapFactoryImpl4.cpp:18).
-    const unsigned level = (unsigned)std::log2((double)(o.quadPts - 2));
-    if (level < 1 || (int)level > kMaxQuadLevel)
-        throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
-    q.nCoarse = (1 << level) + 1;
-    q.nFine = (1 << (level + 1)) + 1;
-    ccRule(q.nCoarse, q.cWts, q.cPts);
-    ccRule(q.nFine, q.fWts, q.fPts);
+    if (o.quadType == QuadTypes::AdaptiveClenshawCurtis) {
+        // Quadrature rule: level = (unsigned) log2(quadPts - 2) (src/MapFactoryImpl4.cpp:18).
+        const unsigned level = (unsigned)std::log2((double)(o.quadPts - 2));
+        if (level < 1 || (int)level > kMaxQuadLevel)
+            throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
+        q.kind = kQuadACC;
+        q.nCoarse = (1 << level) + 1;
+        q.nFine = (1 << (level + 1)) + 1;
+        ccRule(q.nCoarse, q.cWts, q.cPts);
+        ccRule(q.nFine, q.fWts, q.fPts);
+    } else if (o.quadType == QuadTypes::AdaptiveSimpson) {
+        // Simpson on [-1, 1] and composite Simpson on its halves.
+        q.kind = kQuadSimpson;
+        q.nCoarse = 3;
+        q.nFine = 5;
+        const double cp[3] = {-1.0, 0.0, 1.0}, cw[3] = {1.0 / 3.0, 4.0 / 3.0, 1.0 / 3.0};
+        const double fp[5] = {-1.0, -0.5, 0.0, 0.5, 1.0}, fw[5] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 3.0, 2.0 / 3.0, 1.0 / 6.0};
+        for (int i = 0; i < 3; ++i) { q.cPts[i] = cp[i]; q.cWts[i] = cw[i]; }
+        for (int i = 0; i < 5; ++i) { q.fPts[i] = fp[i]; q.fWts[i] = fw[i]; }
+    } else {
+        // ClenshawCurtis with quadPts points (ClenshawCurtisQuadrature::GetRule).
+        if (o.quadPts < 1 || o.quadPts > (unsigned)kMaxRulePts)
+            throw std::invalid_argument("MapOptions: ClenshawCurtis quadPts must be in [1, 33].");
+        q.kind = kQuadFixedCC;
+        q.nCoarse = 0;
+        q.nFine = (int)o.quadPts;
+        ccRule(q.nFine, q.fWts, q.fPts);
+    }
     q.maxSub = (int)o.quadMaxSub;
     q.minSub = (int)o.quadMinSub;
     q.absTol = o.quadAbsTol;

@@ -155,6 +155,30 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
     double as[PMAX + 1];
     scaleCoeffs<BASIS, PMAX>(a, P, bc, as);
     NV A, B, M, V;
+    if (Q.kind == kQuadFixedCC) {
+        // ClenshawCurtisQuadrature::Integrate on [0, 1]: sum_i (w_i / 2) f((1 + x_i) / 2).
+        for (int i = 0; i < Q.nFine; ++i) {
+            evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(0.5 * (1.0 + Q.fPts[i]), xd, as, P, bc, nugget, V, st);
+            const double w = 0.5 * Q.fWts[i];
+            R.Ih = fma(w, V.h, R.Ih);
+            if constexpr (NEEDJ) {
+#pragma unroll
+                for (int k = 0; k < NJ; ++k) R.J[k] = fma(w, V.F[k], R.J[k]);
+            }
+            if constexpr (NEEDE) R.IE = fma(w, V.E, R.IE);
+        }
+        if (st & (kStatusInf | kStatusNaN)) { R.Ih = __longlong_as_double(0x7ff8000000000000ULL); return; }
+        if constexpr (NEEDJ) {
+#pragma unroll
+            for (int k = 1; k <= PMAX; ++k) {
+                double cs;
+                if constexpr (BASIS == kBasisProbHermite) cs = double(k) * bc.invNorm[k];
+                else cs = (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
+                R.J[k - 1] *= cs;
+            }
+        }
+        return;
+    }
     evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(0.0, xd, as, P, bc, nugget, A, st);
     evalNode<BASIS, POS, PMAX, NEEDJ, NEEDE>(1.0, xd, as, P, bc, nugget, B, st);
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);

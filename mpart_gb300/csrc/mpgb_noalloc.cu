@@ -86,68 +86,6 @@ struct Carve {
     }
 };
 
-unsigned factorialU(unsigned d) {
-    unsigned out = 1;
-    for (unsigned i = 2; i <= d; ++i) out *= i;
-    return out;
-}
-
-void rule(unsigned n, double* w, double* p) {
-    const double PI = 3.14159265358979323846;
-    for (unsigned i = 0; i < n; ++i) p[i] = std::cos((n - (i + 1)) * PI / (n - 1));
-    p[0] = -1.0;
-    if (n % 2 == 1) p[(n - 1) / 2] = 0.0;
-    p[n - 1] = 1.0;
-    for (unsigned i = 0; i < n; ++i) {
-        w[i] = 1.0;
-        const double th = i * PI / (n - 1);
-        for (unsigned j = 0; j < (n - 1) / 2; ++j) {
-            const double b = (2 * (j + 1) == (n - 1)) ? 1.0 : 2.0;
-            w[i] = w[i] - b * std::cos(2.0 * (j + 1) * th) / (4 * (j + 1) * (j + 1) - 1);
-        }
-    }
-    w[0] /= (n - 1.0);
-    for (unsigned i = 1; i < n - 1; ++i) w[i] = 2.0 * w[i] / (n - 1.0);
-    w[n - 1] /= (n - 1.0);
-}
-
-void fillConstants(const MapOptions& o, QuadParams& q, BasisConsts& b) {
-    const double PI = 3.14159265358979323846;
-    const unsigned level = (unsigned)std::log2((double)(o.quadPts - 2));
-    if (level < 1 || (int)level > kMaxQuadLevel)
-        throw std::invalid_argument("MapOptions: quadPts gives an unsupported Clenshaw-Curtis level.");
-    q.nCoarse = (1 << level) + 1;
-    q.nFine = (1 << (level + 1)) + 1;
-    rule(q.nCoarse, q.cWts, q.cPts);
-    rule(q.nFine, q.fWts, q.fPts);
-    q.maxSub = (int)o.quadMaxSub;
-    q.minSub = (int)o.quadMinSub;
-    q.absTol = o.quadAbsTol;
-    q.relTol = o.quadRelTol;
-    q.maxIntervals = 1LL << 24;
-    for (int k = 0; k <= kMaxLastOrder; ++k) {
-        b.invNorm[k] = o.basisNorm ? 1.0 / std::sqrt(std::sqrt(2.0 * PI) * factorialU(k)) : 1.0;
-        double fact = 1.0;
-        for (int i = 2; i <= k; ++i) fact *= i;
-        b.hfScale[k] = std::pow(PI, -0.25) * std::pow(std::pow(2.0, k) * fact, -0.5);
-    }
-    for (int i = 0; i < kMaxLastOrder + 8; ++i) {
-        b.hfR1[i] = std::sqrt(0.5 * (i - 1.0 > 0 ? i - 1.0 : 0.0));
-        b.hfR2[i] = i > 0 ? 1.0 / std::sqrt(0.5 * i) : 0.0;
-    }
-    b.piQuarter = std::pow(PI, -0.25);
-    double he[kMaxLastOrder + 1], H[kMaxLastOrder + 1];
-    he[0] = 1.0; he[1] = 0.0; H[0] = 1.0; H[1] = 0.0;
-    for (int k = 2; k <= kMaxLastOrder; ++k) {
-        he[k] = -(k - 1.0) * he[k - 2];
-        H[k] = -2.0 * (k - 1.0) * H[k - 2];
-    }
-    b.v0[0] = 1.0;
-    for (int k = 1; k <= kMaxLastOrder; ++k)
-        b.v0[k] = (o.basisType == BasisTypes::HermiteFunctions) ? ((k == 1) ? 0.0 : b.hfScale[k - 2] * H[k - 2])
-                                                                 : he[k] * b.invNorm[k];
-}
-
 bool onDevice(const void* p) {
     if (!p) return true;
     cudaPointerAttributes a{};
@@ -286,7 +224,7 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         p.statusWord = dStatus;
         p.nugget = o.nugget;
         p.dmax = dmax; p.nBmax = nBmax; p.depthMax = depthMax;
-        fillConstants(o, p.quad, p.bc);
+        buildLaunchConstants(o, p.quad, p.bc);
         const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, pmax, false);
         if (smem > 227 * 1024) throw std::invalid_argument("component too large for the shared-memory tile");
         const int basis = o.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite;

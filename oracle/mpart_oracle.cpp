@@ -520,10 +520,122 @@ static void ccRule(unsigned numPts, double* wts, double* pts) {
     wts[numPts - 1] = wts[numPts - 1] / (numPts - 1.0);
 }
 
+// The three quadrature rules of MapOptions::quadType (MParT/MapOptions.h,
+// src/MapFactoryImpl4.cpp:14-31): kind 0 ClenshawCurtis (fixed, quadPts
+// points), 1 AdaptiveSimpson, 2 AdaptiveClenshawCurtis.
 struct ACC {
+    int kind = 2;
     std::vector<double> cPts, cWts, fPts, fWts;
+    std::vector<double> ruleP, ruleW;  // fixed ClenshawCurtis rule
     unsigned maxSub = 30, minSub = 0;
     double absTol = 1e-6, relTol = 1e-6;
+
+    unsigned wsSize(unsigned fdim) const {
+        if (kind == 0) return fdim;
+        if (kind == 1) return (2 * maxSub + 5) * fdim + 2 * maxSub;
+        return workspaceSize(maxSub, fdim);
+    }
+
+    // ClenshawCurtisQuadrature::Integrate (Quadrature.h:114-143).
+    template <class F>
+    void integrateFixed(double* ws, const F& f, unsigned fdim, double lb, double ub, double* res) const {
+        if ((ub - lb) < 15.0 * std::numeric_limits<double>::epsilon()) {
+            f(0.5 * (ub + lb), res);
+            for (unsigned i = 0; i < fdim; ++i) res[i] *= (ub - lb);
+            return;
+        }
+        for (unsigned j = 0; j < fdim; ++j) res[j] = 0.0;
+        double* fval = ws;
+        for (unsigned i = 0; i < ruleP.size(); ++i) {
+            f(0.5 * (ub + lb + (ub - lb) * ruleP[i]), fval);
+            if (f.failed()) {
+                for (unsigned j = 0; j < fdim; ++j) res[j] = std::numeric_limits<double>::quiet_NaN();
+                return;
+            }
+            for (unsigned j = 0; j < fdim; ++j) res[j] += 0.5 * (ub - lb) * ruleW[i] * fval[j];
+        }
+    }
+
+    // AdaptiveSimpson::Integrate (Quadrature.h:497-716): depth-first,
+    // left-first bisection; per level a record [left, right, f(leftMid),
+    // f(rightMid)]; coarse Simpson on the interval against composite Simpson
+    // on its halves; QuadError::First.
+    template <class F>
+    void integrateSimpson(double* ws, const F& f, unsigned fdim, double lb, double ub, double* res) const {
+        for (unsigned i = 0; i < fdim; ++i) res[i] = 0;
+        auto bail = [&]() {
+            if (!f.failed()) return false;
+            for (unsigned i = 0; i < fdim; ++i) res[i] = std::numeric_limits<double>::quiet_NaN();
+            return true;
+        };
+        unsigned currLevel = 0, currSegment = 0;
+        double midPt = 0.5 * (lb + ub);
+        double* leftFunc = &ws[0];
+        f(lb, leftFunc);
+        double* rightFunc = &ws[fdim];
+        f(ub, rightFunc);
+        double* midFunc = &ws[2 * fdim];
+        f(midPt, midFunc);
+        if (bail()) return;
+        double* intCoarse = &ws[3 * fdim];
+        double* intFine = &ws[4 * fdim];
+        unsigned workStart = 5 * fdim;
+        ws[workStart] = lb;
+        ws[workStart + 1] = ub;
+        while (true) {
+            double* leftPt = &ws[workStart];
+            double* rightPt = &ws[workStart + 1];
+            midPt = 0.5 * ((*leftPt) + (*rightPt));
+            const double leftMidPt = 0.5 * ((*leftPt) + midPt);
+            const double rightMidPt = 0.5 * (midPt + (*rightPt));
+            double* leftMidFunc = &ws[workStart + 2];
+            f(leftMidPt, leftMidFunc);
+            double* rightMidFunc = &ws[workStart + 2 + fdim];
+            f(rightMidPt, rightMidFunc);
+            if (bail()) return;
+            for (unsigned i = 0; i < fdim; ++i) {
+                intCoarse[i] = (((*rightPt) - (*leftPt)) / 6.0) * (leftFunc[i] + 4.0 * midFunc[i] + rightFunc[i]);
+                intFine[i] = ((midPt - (*leftPt)) / 6.0) * (leftFunc[i] + 4.0 * leftMidFunc[i] + midFunc[i]);
+                intFine[i] += (((*rightPt) - midPt) / 6.0) * (midFunc[i] + 4.0 * rightMidFunc[i] + rightFunc[i]);
+            }
+            const double error = std::fabs(intFine[0] - intCoarse[0]);
+            const double errorTol = std::fmax(relTol * std::fabs(intCoarse[0]), absTol);
+            if ((((error < errorTol) || (currLevel == maxSub - 1)) && (currLevel >= minSub)) ||
+                (std::abs(ub - lb) < 1e-14)) {
+                for (unsigned i = 0; i < fdim; ++i) res[i] += intFine[i];
+                while (((currSegment >> currLevel) & 1U) && (currLevel > 0)) {
+                    currSegment &= ~(1UL << currLevel);
+                    currLevel--;
+                }
+                if (currLevel == 0) break;
+                currSegment |= 1UL << currLevel;
+                workStart = (2 * currLevel + 5) * fdim + 2 * currLevel;
+                const unsigned prev = (2 * (currLevel - 1) + 5) * fdim + 2 * (currLevel - 1);
+                ws[workStart] = 0.5 * (ws[prev] + ws[prev + 1]);
+                ws[workStart + 1] = ws[prev + 1];
+                // values at the new interval's left, middle and right ends
+                leftFunc = &ws[0];
+                midFunc = &ws[2 * fdim];
+                rightFunc = &ws[fdim];
+                for (unsigned level = 0; level < currLevel; ++level) {
+                    if ((currSegment >> (level + 1)) & 1U) {
+                        leftFunc = midFunc;
+                        midFunc = &ws[(2 * level + 5 + 1) * fdim + 2 * level + 2];
+                    } else {
+                        rightFunc = midFunc;
+                        midFunc = &ws[(2 * level + 5) * fdim + 2 * level + 2];
+                    }
+                }
+            } else {
+                currLevel++;
+                rightFunc = midFunc;
+                midFunc = leftMidFunc;
+                workStart = (2 * currLevel + 5) * fdim + 2 * currLevel;
+                ws[workStart] = *leftPt;
+                ws[workStart + 1] = midPt;
+            }
+        }
+    }
 
     void init(unsigned level, unsigned maxSub_, double absTol_, double relTol_, unsigned minSub_) {
         unsigned nc = (unsigned)std::pow(2, level) + 1, nf = (unsigned)std::pow(2, level + 1) + 1;
@@ -536,6 +648,8 @@ struct ACC {
 
     template <class F>
     void integrate(double* ws, const F& f, unsigned fdim, double lb, double ub, double* res) const {
+        if (kind == 0) return integrateFixed(ws, f, fdim, lb, ub, res);
+        if (kind == 1) return integrateSimpson(ws, f, fdim, lb, ub, res);
         for (unsigned i = 0; i < fdim; ++i) res[i] = 0;
         auto bail = [&]() {
             if (!f.failed()) return false;
@@ -789,7 +903,7 @@ int orc_total_order_fill(unsigned dim, unsigned order, unsigned* starts, unsigne
 
 void* orc_component_new(unsigned dim, unsigned nterms, const unsigned* starts, const unsigned* dims,
                         const unsigned* orders, int basis, int normalize, int pos, double absTol, double relTol,
-                        unsigned maxSub, unsigned minSub, unsigned quadPts, double nugget) {
+                        unsigned maxSub, unsigned minSub, unsigned quadPts, double nugget, int quadType) {
     Component* C = new Component();
     C->ex.ms.dim = dim;
     C->ex.ms.starts.assign(starts, starts + nterms + 1);
@@ -803,6 +917,12 @@ void* orc_component_new(unsigned dim, unsigned nterms, const unsigned* starts, c
     // MapFactoryImpl4.cpp:18 -- level = (unsigned) log2(quadPts - 2)
     unsigned level = (unsigned)std::log2(quadPts - 2);
     C->quad.init(level, maxSub, absTol, relTol, minSub);
+    C->quad.kind = quadType;
+    if (quadType == 0) {
+        C->quad.ruleP.resize(quadPts);
+        C->quad.ruleW.resize(quadPts);
+        ccRule(quadPts, C->quad.ruleW.data(), C->quad.ruleP.data());
+    }
     C->pos = pos;
     C->nugget = nugget;
     return C;
@@ -819,7 +939,7 @@ int orc_evaluate(void* h, const double* coeffs, const double* pts, long N, long 
     View2 P{pts, rs, cs};
     ORC_PARALLEL_FOR
     for (long i = 0; i < N; ++i) {
-        std::vector<double> cache(C.ex.cacheSize), ws(ACC::workspaceSize(C.quad.maxSub, 1)), pt(C.D());
+        std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(1)), pt(C.D());
         for (unsigned d = 0; d < C.D(); ++d) pt[d] = P.at(d, i);
         C.ex.fillCache1(cache.data(), pt.data(), dNone);
         long nev = 0;
@@ -862,7 +982,7 @@ int orc_coeff_jacobian(void* h, const double* coeffs, const double* pts, long N,
     const unsigned T = C.T();
     ORC_PARALLEL_FOR
     for (long i = 0; i < N; ++i) {
-        std::vector<double> cache(C.ex.cacheSize), ws(ACC::workspaceSize(C.quad.maxSub, T + 1)), integral(T + 1), pt(C.D());
+        std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(T + 1)), integral(T + 1), pt(C.D());
         for (unsigned d = 0; d < C.D(); ++d) pt[d] = P.at(d, i);
         C.ex.fillCache1(cache.data(), pt.data(), dNone);
         Integrand ig{&C.ex, cache.data(), pt[C.D() - 1], coeffs, dParameters, C.nugget, C.pos};
@@ -897,7 +1017,7 @@ int orc_input_jacobian(void* h, const double* coeffs, const double* pts, long N,
     const unsigned D = C.D();
     ORC_PARALLEL_FOR
     for (long i = 0; i < N; ++i) {
-        std::vector<double> cache(C.ex.cacheSize), ws(ACC::workspaceSize(C.quad.maxSub, D + 1)), integral(D + 1), pt(D);
+        std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(D + 1)), integral(D + 1), pt(D);
         for (unsigned d = 0; d < D; ++d) pt[d] = P.at(d, i);
         C.ex.fillCache1(cache.data(), pt.data(), dInput);
         Integrand ig{&C.ex, cache.data(), pt[D - 1], coeffs, dInput, C.nugget, C.pos};
@@ -1010,7 +1130,7 @@ int orc_inverse(void* h, const double* coeffs, const double* xs, long numXs, lon
             if (info) info[i] = 0;
             continue;
         }
-        std::vector<double> cache(C.ex.cacheSize), ws(ACC::workspaceSize(C.quad.maxSub, 1));
+        std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(1));
         C.ex.fillCache1(cache.data(), pt.data(), dNone);
         auto f = [&](double x) { return evaluateSingle(C, cache.data(), ws.data(), x, coeffs, nullptr, nullptr); };
         int inf = 0;
@@ -1066,6 +1186,37 @@ int orc_acc_test(int id, unsigned level, unsigned maxSub, double absTol, double 
     std::vector<double> ws(ACC::workspaceSize(maxSub, fdim));
     q.integrate(ws.data(), w, fdim, lb, ub, res);
     if (nevals) *nevals = n;
+    return 0;
+}
+
+// Same test integrands through any quadrature kind (0 ClenshawCurtis with
+// `n` points, 1 AdaptiveSimpson, 2 AdaptiveClenshawCurtis of level `n`).
+int orc_quad_test(int kind, int id, unsigned n, unsigned maxSub, double absTol, double relTol, unsigned minSub,
+                  double lb, double ub, double* res, long* nevals) {
+    ACC q;
+    q.init(kind == 2 ? n : 1, maxSub, absTol, relTol, minSub);
+    q.kind = kind;
+    if (kind == 0) {
+        q.ruleP.resize(n);
+        q.ruleW.resize(n);
+        ccRule(n, q.ruleW.data(), q.ruleP.data());
+    }
+    unsigned fdim = (id == 2) ? 2 : 1;
+    long cnt = 0;
+    auto f = [&](double x, double* o) {
+        cnt++;
+        if (id == 0) o[0] = std::exp(x);
+        else if (id == 1) o[0] = (x < 0.5) ? std::exp(x) : 1.0 + std::exp(x);
+        else { o[0] = std::exp(x); o[1] = 2.0 * std::exp(x); }
+    };
+    struct Wrap {
+        decltype(f)& g;
+        void operator()(double x, double* o) const { g(x, o); }
+        int failed() const { return 0; }
+    } w{f};
+    std::vector<double> ws(q.wsSize(fdim));
+    q.integrate(ws.data(), w, fdim, lb, ub, res);
+    if (nevals) *nevals = cnt;
     return 0;
 }
 

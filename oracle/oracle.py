@@ -31,6 +31,7 @@ BASIS_PROB_HERMITE = 0
 BASIS_HERMITE_FUNCTIONS = 2
 POS_EXP = 0
 POS_SOFTPLUS = 1
+QUAD_CC, QUAD_SIMPSON, QUAD_ACC = 0, 1, 2  # MapOptions::quadType
 
 _dp = C.POINTER(C.c_double)
 _up = C.POINTER(C.c_uint)
@@ -53,7 +54,7 @@ def lib():
         L.orc_total_order_fill.argtypes = [C.c_uint, C.c_uint, _up, _up, _up]
         L.orc_component_new.restype = C.c_void_p
         L.orc_component_new.argtypes = [C.c_uint, C.c_uint, _up, _up, _up, C.c_int, C.c_int, C.c_int,
-                                        C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_uint, C.c_double]
+                                        C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_uint, C.c_double, C.c_int]
         L.orc_component_free.argtypes = [C.c_void_p]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_cache_size.argtypes = [C.c_void_p]
@@ -78,6 +79,8 @@ def lib():
         L.orc_cc_rule.argtypes = [C.c_uint, _dp, _dp]
         L.orc_acc_test.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_uint, C.c_double,
                                    C.c_double, _dp, _lp]
+        L.orc_quad_test.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_uint,
+                                    C.c_double, C.c_double, _dp, _lp]
         L.orc_rootfind_test.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _ip]
         L.orc_rootfind_test.restype = C.c_double
         L.orc_findbracket_test.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double]
@@ -117,7 +120,7 @@ class OracleComponent:
 
     def __init__(self, dim, starts, dims, orders, basis=BASIS_PROB_HERMITE, normalize=True,
                  posfunc=POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6, max_sub=30, min_sub=0, quad_pts=5,
-                 nugget=0.0):
+                 nugget=0.0, quad_type=QUAD_ACC):
         self.dim = int(dim)
         self.starts = np.ascontiguousarray(starts, np.uint32)
         self.dims = np.ascontiguousarray(dims, np.uint32)
@@ -132,7 +135,7 @@ class OracleComponent:
         o = self.orders if len(self.orders) else np.zeros(1, np.uint32)
         self._h = L.orc_component_new(self.dim, self.num_terms, self.starts.ctypes.data_as(_up),
                                       d.ctypes.data_as(_up), o.ctypes.data_as(_up), basis, int(normalize),
-                                      posfunc, abs_tol, rel_tol, max_sub, min_sub, quad_pts, nugget)
+                                      posfunc, abs_tol, rel_tol, max_sub, min_sub, quad_pts, nugget, quad_type)
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -255,14 +258,14 @@ class OracleTriangularMap:
 
     def __init__(self, input_dim, output_dim, order, basis=BASIS_PROB_HERMITE, normalize=True,
                  posfunc=POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6, max_sub=30, min_sub=0, quad_pts=5, nugget=0.0,
-                 components=None):
+                 components=None, quad_type=QUAD_ACC):
         if components is None:
             extra = input_dim - output_dim
             components = []
             for i in range(output_dim):
                 s, d, o = total_order(i + extra + 1, int(order))
                 components.append(OracleComponent(i + extra + 1, s, d, o, basis, normalize, posfunc, abs_tol,
-                                                  rel_tol, max_sub, min_sub, quad_pts, nugget))
+                                                  rel_tol, max_sub, min_sub, quad_pts, nugget, quad_type))
         self.comps = components
         self.input_dim = components[-1].input_dim
         self.output_dim = len(components)

@@ -481,3 +481,41 @@ def test_point_ordering_invariance_and_determinism(c2):
     comp.SetPointOrdering(True)
     np.testing.assert_array_equal(e1, e3)  # per-point values do not depend on the order
     assert_parity(g3, g1, floor=1e-3, what="ordered vs unordered reduction")
+
+
+# ----------------------------------------------------------------------------
+# The other quadrature rules of MapOptions::quadType: AdaptiveSimpson (the
+# reference's default) and the fixed ClenshawCurtis rule.
+# ----------------------------------------------------------------------------
+@pytest.mark.parametrize("quad,pts", [(1, 5), (0, 5), (0, 9)])
+def test_quadrature_kinds_match_oracle(gpu, oracle, quad, pts):
+    import torch
+    M, O = gpu, oracle
+    opt = M.MapOptions(quadType=M.QuadTypes(quad), quadPts=pts, quadAbsTol=1e-7, quadRelTol=1e-7)
+    tm = M.CreateTriangular(4, 3, 3, opt)
+    om = O.OracleTriangularMap(4, 3, 3, abs_tol=1e-7, rel_tol=1e-7, quad_pts=pts, quad_type=quad)
+    rng = np.random.default_rng(40 + quad + pts)
+    coef = rng.normal(0.0, 0.1, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    x = rng.standard_normal((4, 1500))
+    sens = rng.standard_normal((3, 1500))
+    xs = T(x)
+    assert_parity(H(tm.Evaluate(xs)), om.evaluate(coef, x), what="Evaluate")
+    assert_parity(H(tm.LogDeterminant(xs)), om.logdet(coef, x), what="LogDeterminant")
+    assert_parity(H(tm.CoeffGrad(xs, T(sens))), om.coeff_grad(coef, x, sens), what="CoeffGrad")
+    assert_parity(H(tm.Gradient(xs, T(sens))), om.gradient(coef, x, sens), what="Gradient")
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device="cuda")
+    tm.FusedForwardAdjointImpl(xs, sens=T(sens), logdet_sens_scale=1.0, coeff_grad=cg)
+    ref = om.coeff_grad(coef, x, sens).sum(axis=1) + om.logdet_coeff_grad(coef, x).sum(axis=1)
+    assert_parity(H(cg), ref, floor=1e-3, what="fused adjoint")
+    loss, grad = tm.KLObjective(xs)
+    l_ref, g_ref = [], []
+    for i, c in enumerate(om.comps):
+        l, g = O.fast_gaussian_reverse_kl(c, om.split(coef)[i], x[:c.input_dim])
+        l_ref.append(l)
+        g_ref.append(g)
+    assert_parity(H(loss), np.array(l_ref), what="KL loss")
+    assert_parity(H(grad), np.concatenate(g_ref), floor=1e-3, what="KL gradient")
+    r = om.evaluate(coef, x)
+    xi = H(tm.Inverse(T(x[:1]), T(r), xtol=1e-10, ytol=1e-10))
+    assert_inverse_parity(om, coef, x[:1], r, xi, 1e-10, 1e-10)

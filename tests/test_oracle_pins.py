@@ -113,6 +113,35 @@ def test_acc_known_answers(oracle):
     assert res[0] == pytest.approx(math.e - 1.0, rel=1e-10)
 
 
+def _quad(O, kind, fid, n=0, maxsub=30, tol=1e-8):
+    import ctypes as C
+    res = np.zeros(2)
+    cnt = C.c_long(0)
+    O.lib().orc_quad_test(kind, fid, n, maxsub, tol, tol, 0, 0.0, 1.0, res.ctypes.data_as(C.POINTER(C.c_double)),
+                          C.byref(cnt))
+    return res, cnt.value
+
+
+# tests/Test_Quadrature.cpp:45-116 (ClenshawCurtis, 10 points) and :223-324 (AdaptiveSimpson).
+def test_cc_and_simpson_known_answers(oracle):
+    e1 = math.e - 1.0
+    res, n = _quad(oracle, oracle.QUAD_CC, 0, n=10)
+    assert res[0] == pytest.approx(e1, rel=1e-8) and n == 10
+    res, _ = _quad(oracle, oracle.QUAD_CC, 2, n=10)
+    assert res[0] == pytest.approx(e1, rel=1e-8) and res[1] == pytest.approx(2 * e1, rel=1e-8)
+    res, _ = _quad(oracle, oracle.QUAD_SIMPSON, 0)
+    assert res[0] == pytest.approx(e1, rel=1e-4)
+    res, n = _quad(oracle, oracle.QUAD_SIMPSON, 1)
+    assert res[0] == pytest.approx(0.5 + e1, rel=1e-4)
+    assert n < 150
+    res, _ = _quad(oracle, oracle.QUAD_SIMPSON, 2)
+    assert res[0] == pytest.approx(e1, rel=1e-4) and res[1] == pytest.approx(2 * e1, rel=1e-4)
+    # the adaptive kinds agree with each other on a smooth integrand at tight tolerance
+    a, _ = _quad(oracle, oracle.QUAD_ACC, 0, n=1, tol=1e-12)
+    s, _ = _quad(oracle, oracle.QUAD_SIMPSON, 0, tol=1e-12)
+    assert a[0] == pytest.approx(e1, rel=1e-11) and s[0] == pytest.approx(e1, rel=1e-11)
+
+
 # tests/Test_RootFinding.cpp:17-113
 def test_root_finding(oracle):
     import ctypes as C
