@@ -240,6 +240,8 @@ public:
                 throw std::invalid_argument("MapBatch: maps must share basis, rectifier and quadrature options.");
         }
         opts_ = a;
+        if (!opts_.contDeriv)
+            throw std::invalid_argument("MapBatch: contDeriv = false (discrete derivative) is not provided for batches.");
         basis_ = opts_.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite;
         pos_ = opts_.posFuncType == PosFuncTypes::Exp ? kPosExp : kPosSoftPlus;
         buildLaunchConstants(opts_, quad_, bc_);

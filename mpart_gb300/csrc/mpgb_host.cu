@@ -287,8 +287,6 @@ static unsigned factorialU(unsigned d) {
 static void validateOptions(MapOptions const& o) {
     if (o.basisType == BasisTypes::PhysicistHermite)
         throw std::invalid_argument("MapOptions: basisType must be ProbabilistHermite or HermiteFunctions.");
-    if (!o.contDeriv)
-        throw std::invalid_argument("MapOptions: contDeriv = false (discrete derivative) is not provided on this path.");
     if (o.quadMaxSub < 1 || o.quadMaxSub > (unsigned)kMaxSubCap)
         throw std::invalid_argument("MapOptions: quadMaxSub must be in [1, 32].");
     if (o.quadMinSub >= o.quadMaxSub) throw std::invalid_argument("MapOptions: quadMinSub must be below quadMaxSub.");
@@ -595,6 +593,13 @@ static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nIt
     if (nItems == 0) return;
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, (p.flags & kFlagInput) != 0);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
+    // contDeriv = false: log-determinants and their coefficient adjoints come
+    // from the quadrature's x_D-derivative (the kernel variant NEEDE = 2).
+    if (!o.contDeriv && ((p.flags & (kFlagLogDet | kFlagCoefDenseL | kFlagKL)) ||
+                         ((p.flags & kFlagCoefReduced) && (p.lsens || p.lsensScale != 0.0)))) {
+        needJ = 1;
+        needE = 2;
+    }
     MPGB_CUDA(launchFused(basisCode(o), posCode(o), W.pmax, p, nItems, needJ, needE, stream));
 }
 
@@ -707,6 +712,8 @@ void MonotoneMapBase::GradientImpl(StridedMatrix const& pts, StridedMatrix const
 void MonotoneMapBase::LogDeterminantInputGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
                                                   cudaStream_t stream) {
     CheckCoefficients("LogDeterminantInputGrad");
+    // MonotoneComponent.h:216-222 throws the same for contDeriv = false.
+    if (!opts_.contDeriv) throw std::invalid_argument("Discrete derivative version is not implemented yet (To Do)");
     const long long N = pts.cols;
     checkMatrix(pts, inputDim, N, "pts", "LogDeterminantInputGradImpl");
     checkMatrix(output, inputDim, N, "output", "LogDeterminantInputGradImpl");
@@ -877,6 +884,8 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
     }
     // Pass 2: input gradient (sums over components per point).
     if (!inputGrad.empty()) {
+        if (!opts_.contDeriv && (logdetSens.data || logdetSensScale != 0.0))
+            throw std::invalid_argument("Discrete derivative version is not implemented yet (To Do)");
         auto items = itemsAllComps(N, nComps);
         uploadItems(W, items, stream);
         FusedParams p{};
@@ -962,7 +971,7 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     orderPoints(W, parts_, pts, p, onlyComp, stream);
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
-    MPGB_CUDA(launchFused(basisCode(opts_), posCode(opts_), W.pmax, p, P.nItems, 1, 0, stream));
+    MPGB_CUDA(launchFused(basisCode(opts_), posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
     for (int c = 0; c < (int)parts_.size(); ++c) {
         if (onlyComp >= 0 && c != onlyComp) continue;
         const int nr = P.rowOff[c + 1] - P.rowOff[c];

@@ -27,11 +27,14 @@ namespace mpgb {
 // --------------------------------------------------------------------------
 // Integrand at one node t in [0,1]:  h = x_D (g(df) + eps), plus adjoint parts.
 // --------------------------------------------------------------------------
-template <int PMAX, bool NEEDJ, bool NEEDE>
+// NEEDE: 0 value (and J) only; 1 adds E; 2 (discrete derivative) adds E and
+// K_k = d E / d a_k, the MixedCoeff integrand (MonotoneIntegrand.h:148-165).
+template <int PMAX, bool NEEDJ, int NEEDE>
 struct NodeVal {
     double h;
     double F[NEEDJ ? PMAX : 1];  // x_D g'(df) phit'_k(y), k = 1..P
     double E;                    // d/dx_D of the integrand (MonotoneIntegrand.h:193-201)
+    double K[NEEDE == 2 ? PMAX : 1];
 };
 
 // Per-component constants folded into the coefficients once per point, so a
@@ -52,7 +55,7 @@ __device__ __forceinline__ void scaleCoeffs(const double* a, int P, const BasisC
     }
 }
 
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+template <int BASIS, int POS, int PMAX, bool NEEDJ, int NEEDE>
 __device__ __forceinline__ void evalNode(double t, double xd, const double* as, int P, const BasisConsts& bc,
                                          double nugget, NodeVal<PMAX, NEEDJ, NEEDE>& o, int& st) {
     (void)bc;
@@ -106,6 +109,20 @@ __device__ __forceinline__ void evalNode(double t, double xd, const double* as, 
     o.h = xd * (g + nugget);
     if (isinf(g)) st |= kStatusInf;
     else if (isnan(o.h)) st |= kStatusNaN;
+    if constexpr (NEEDE == 2) {
+        // (x_D t g'' d2f + g') phit'_k + x_D t g' phit''_k, unscaled by cs_k
+        // (g'' of PositiveBijectors.h:24-27 / :49-51).
+        const double gpp = (POS == kPosExp) ? g : gp * (1.0 - gp);
+        const double c1 = fma((xd * t) * gpp, d2f, gp);
+        const double c2 = (xd * t) * gp;
+#pragma unroll
+        for (int k = 1; k <= PMAX; ++k) {
+            const double vk = (k >= 2) ? v[k] : 0.0;
+            const double kk = fma(c2, vk, c1 * u[k]);
+            if constexpr (BASIS == kBasisProbHermite) o.K[k - 1] = kk;
+            else o.K[k - 1] = (k == 1) ? kk : env * kk;
+        }
+    }
     if constexpr (NEEDJ) {
         // Unscaled: J_k is multiplied by cs_k once the integral is done.
         const double q = xd * gp;
@@ -124,33 +141,45 @@ __device__ __forceinline__ void evalNode(double t, double xd, const double* as, 
     (void)v;
 }
 
-template <int PMAX, bool NEEDJ, bool NEEDE>
+template <int PMAX, bool NEEDJ, int NEEDE>
 struct QuadOut {
     double Ih;
     double J[NEEDJ ? PMAX : 1];
     double IE;
+    double K[NEEDE == 2 ? PMAX : 1];
 };
+
+// Per-order constants cs_k of the basis derivatives (see scaleCoeffs).
+template <int BASIS>
+__device__ __forceinline__ double basisScale(int k, const BasisConsts& bc) {
+    if constexpr (BASIS == kBasisProbHermite) return double(k) * bc.invNorm[k];
+    else return (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
+}
 
 // AdaptiveClenshawCurtis::Integrate on [0,1] (Quadrature.h:819-968) with the
 // QuadError::First metric (:441-481).  Depth-first, left-first bisection; the
 // stack keeps (right end, level, integrand at right end).  Intervals, nodes,
 // accept/reject tests and the order in which accepted fine sums are added are
 // the reference's.
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+template <int BASIS, int POS, int PMAX, bool NEEDJ, int NEEDE>
 __device__ __forceinline__ void integrate(const double* a, int P, double xd, const QuadParams& Q, const BasisConsts& bc,
                                        double nugget, QuadOut<PMAX, NEEDJ, NEEDE>& R, int& st) {
     using NV = NodeVal<PMAX, NEEDJ, NEEDE>;
     constexpr int NJ = NEEDJ ? PMAX : 1;
+    constexpr int NK = NEEDE == 2 ? PMAX : 1;
     double stX[kMaxSubCap];
     int stL[kMaxSubCap];
     double stH[kMaxSubCap];
     double stF[kMaxSubCap][NJ];
     double stE[kMaxSubCap];
+    double stK[NEEDE == 2 ? kMaxSubCap : 1][NK];
 
     R.Ih = 0.0;
     R.IE = 0.0;
 #pragma unroll
     for (int k = 0; k < NJ; ++k) R.J[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NK; ++k) R.K[k] = 0.0;
 
     double as[PMAX + 1];
     scaleCoeffs<BASIS, PMAX>(a, P, bc, as);
@@ -166,16 +195,16 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) R.J[k] = fma(w, V.F[k], R.J[k]);
             }
             if constexpr (NEEDE) R.IE = fma(w, V.E, R.IE);
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) R.K[k] = fma(w, V.K[k], R.K[k]);
+            }
         }
         if (st & (kStatusInf | kStatusNaN)) { R.Ih = __longlong_as_double(0x7ff8000000000000ULL); return; }
-        if constexpr (NEEDJ) {
 #pragma unroll
-            for (int k = 1; k <= PMAX; ++k) {
-                double cs;
-                if constexpr (BASIS == kBasisProbHermite) cs = double(k) * bc.invNorm[k];
-                else cs = (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
-                R.J[k - 1] *= cs;
-            }
+        for (int k = 1; k <= PMAX; ++k) {
+            if constexpr (NEEDJ) R.J[k - 1] *= basisScale<BASIS>(k, bc);
+            if constexpr (NEEDE == 2) R.K[k - 1] *= basisScale<BASIS>(k, bc);
         }
         return;
     }
@@ -199,13 +228,17 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
         double ih = w0 * A.h;
         ih = fma(wM, M.h, ih);
         ih = fma(wR, B.h, ih);
-        double iF[NJ];
+        double iF[NJ], iK[NK];
         double iE = 0.0;
         if constexpr (NEEDJ) {
 #pragma unroll
             for (int k = 0; k < NJ; ++k) iF[k] = fma(wR, B.F[k], fma(wM, M.F[k], w0 * A.F[k]));
         }
         if constexpr (NEEDE) iE = fma(wR, B.E, fma(wM, M.E, w0 * A.E));
+        if constexpr (NEEDE == 2) {
+#pragma unroll
+            for (int k = 0; k < NK; ++k) iK[k] = fma(wR, B.K[k], fma(wM, M.K[k], w0 * A.K[k]));
+        }
         // Coarse interior points other than the midpoint (level >= 2 rules).
         for (int i = 1; i < cR; ++i) {
             if (i == cM) continue;
@@ -218,6 +251,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) iF[k] = fma(wf, V.F[k], iF[k]);
             }
             if constexpr (NEEDE) iE = fma(wf, V.E, iE);
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) iK[k] = fma(wf, V.K[k], iK[k]);
+            }
         }
         // Points only in the fine rule.
         for (int i = 1; i < Q.nFine; i += 2) {
@@ -229,6 +266,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) iF[k] = fma(wf, V.F[k], iF[k]);
             }
             if constexpr (NEEDE) iE = fma(wf, V.E, iE);
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) iK[k] = fma(wf, V.K[k], iK[k]);
+            }
         }
         if (st & (kStatusInf | kStatusNaN)) { R.Ih = nan; return; }
         const double err = fabs(ih - ic);
@@ -241,6 +282,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) R.J[k] += iF[k];
             }
             if constexpr (NEEDE) R.IE += iE;
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) R.K[k] += iK[k];
+            }
             if (sp == 0) break;
             --sp;
             lo = hi;
@@ -253,6 +298,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) B.F[k] = stF[sp][k];
             }
             if constexpr (NEEDE) B.E = stE[sp];
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) B.K[k] = stK[sp][k];
+            }
         } else {
             stX[sp] = hi;
             stL[sp] = level + 1;
@@ -262,6 +311,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
                 for (int k = 0; k < NJ; ++k) stF[sp][k] = B.F[k];
             }
             if constexpr (NEEDE) stE[sp] = B.E;
+            if constexpr (NEEDE == 2) {
+#pragma unroll
+                for (int k = 0; k < NK; ++k) stK[sp][k] = B.K[k];
+            }
             ++sp;
             hi = m;
             B = M;
@@ -273,15 +326,11 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
             return;
         }
     }
-    if constexpr (NEEDJ) {
-        // The nodes accumulated u_k (times env); apply the per-order constants.
+    // The nodes accumulated u_k (times env); apply the per-order constants.
 #pragma unroll
-        for (int k = 1; k <= PMAX; ++k) {
-            double cs;
-            if constexpr (BASIS == kBasisProbHermite) cs = double(k) * bc.invNorm[k];
-            else cs = (k == 1) ? 1.0 : bc.hfScale[k >= 2 ? k - 2 : 0];
-            R.J[k - 1] *= cs;
-        }
+    for (int k = 1; k <= PMAX; ++k) {
+        if constexpr (NEEDJ) R.J[k - 1] *= basisScale<BASIS>(k, bc);
+        if constexpr (NEEDE == 2) R.K[k - 1] *= basisScale<BASIS>(k, bc);
     }
 }
 
@@ -289,8 +338,8 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
 template <int BASIS, int POS, int PMAX>
 __device__ __forceinline__ double integrateValue(const double* a, int P, double xd, const QuadParams& Q,
                                                  const BasisConsts& bc, double nugget, int& st) {
-    QuadOut<PMAX, false, false> R;
-    integrate<BASIS, POS, PMAX, false, false>(a, P, xd, Q, bc, nugget, R, st);
+    QuadOut<PMAX, false, 0> R;
+    integrate<BASIS, POS, PMAX, false, 0>(a, P, xd, Q, bc, nugget, R, st);
     return R.Ih;
 }
 
@@ -380,7 +429,7 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
 // batch of maps) the entry of the item's component in prm.ioTable.
 #define MPGB_IO(f) (BATCH ? tio->f : prm.f)
 
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE, bool BATCH>
+template <int BASIS, int POS, int PMAX, bool NEEDJ, int NEEDE, bool BATCH>
 __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem& item, double* smem) {
     const int tid = threadIdx.x;
     const int tpb = blockDim.x;
@@ -435,15 +484,20 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             double gx, gpx;
             posEval<POS>(dfx, gx, gpx);
 
+            // (The discrete-derivative variant, NEEDE == 2, always integrates:
+            // its log-determinant is that of the quadrature approximation.)
             const bool needT = (flags & (kFlagEval | kFlagCoefDenseT | kFlagKL)) != 0 ||
-                               (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput)));
+                               (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput))) || NEEDE == 2;
             QuadOut<PMAX, NEEDJ, NEEDE> R;
             R.Ih = 0.0; R.IE = 0.0;
 #pragma unroll
             for (int k = 0; k < (NEEDJ ? PMAX : 1); ++k) R.J[k] = 0.0;
             if (needT && active) integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
             const double T = R.Ih + f0;
-            const double logdet = (gx <= 0.0) ? ninf : log(gx);
+            // dT/dx_D: g(df(x)) (ContinuousDerivative) or the x_D-derivative of
+            // the quadrature approximation (DiscreteDerivative, MonotoneComponent.h:585-638).
+            const double dT = (NEEDE == 2) ? R.IE : gx;
+            const double logdet = (dT <= 0.0) ? ninf : log(dT);
 
             if ((flags & kFlagEval) && active && MPGB_IO(outEval)) MPGB_IO(outEval)[(long long)c.outRow * MPGB_IO(evalRs) + i * MPGB_IO(evalCs)] = T;
             if (flags & kFlagLogDet) logdetSum += logdet;
@@ -468,12 +522,21 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             }
             if (!active) { sens = 0.0; lsens = 0.0; }
             const double ldScale = gpx * (1.0 / gx);
+            // d logdet / d a_k: g'/g phit'_k(x_D), or (discrete) K_k / (dT/dx_D)
+            // with K the MixedCoeff integral (DiscreteMixedJacobian, MonotoneComponent.h:928-980).
+            double dld[PMAX + 1];
+#pragma unroll
+            for (int k = 0; k <= PMAX; ++k) {
+                // (inactive lanes did not integrate: keep their weights zero)
+                if constexpr (NEEDE == 2) dld[k] = (k >= 1 && active) ? R.K[k >= 1 ? k - 1 : 0] * (1.0 / R.IE) : 0.0;
+                else dld[k] = ldScale * d1x[k];
+            }
             double wT[PMAX + 1], wL[PMAX + 1];
 #pragma unroll
             for (int k = 0; k <= PMAX; ++k) {
                 const double Jk = (NEEDJ && k >= 1) ? R.J[k >= 1 ? k - 1 : 0] : 0.0;
                 wT[k] = sens * (v0[k] + Jk);
-                wL[k] = lsens * (ldScale * d1x[k]);
+                wL[k] = lsens * dld[k];
             }
 
             // Dense per-term outputs (CoeffGradImpl / LogDeterminantCoeffGradImpl).
@@ -481,7 +544,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 const bool useT = (flags & kFlagCoefDenseT) != 0;
                 double wd[PMAX + 1];
 #pragma unroll
-                for (int k = 0; k <= PMAX; ++k) wd[k] = useT ? wT[k] : (ldScale * d1x[k]);
+                for (int k = 0; k <= PMAX; ++k) wd[k] = useT ? wT[k] : dld[k];
                 L.S[tid] = 1.0;
                 for (int n = 0; n < c.nNodes; ++n) {
                     const uint32_t w = __ldg(&c.nodeA[n]);
@@ -541,7 +604,9 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 }
                 // Last coordinate: quadrature of the x_D-derivative integrand and the
                 // log-det term (MonotoneComponent.h:811-815, :892-925).
-                double gxd = lsens * (ldScale * d2fx);
+                // (The host does not combine lsens with input gradients in the
+                // discrete mode, which the reference does not provide.)
+                double gxd = (NEEDE == 2) ? 0.0 : lsens * (ldScale * d2fx);
                 if constexpr (NEEDE) gxd = fma(sens, R.IE, gxd);
                 double* g = &L.GX[(c.D - 1) * tpb + tid];
                 if (!(flags & kFlagImplicit)) *g += gxd;  // implicit mode keeps lambda there
@@ -619,7 +684,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
     (void)nan;
 }
 
-template <int BASIS, int POS, int PMAX, bool NEEDJ, bool NEEDE>
+template <int BASIS, int POS, int PMAX, bool NEEDJ, int NEEDE>
 __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ FusedParams prm) {
     extern __shared__ double smem[];
     fusedBody<BASIS, POS, PMAX, NEEDJ, NEEDE, false>(prm, prm.items[blockIdx.x], smem);
@@ -646,10 +711,10 @@ __global__ void __launch_bounds__(128, 4) batchKernel(const __grid_constant__ Fu
         if (k >= nItems) break;
         const WorkItem item = prm.items[k];
         const int P = prm.comps[item.c0].P;
-        if (P <= 2) fusedBody<BASIS, POS, 2, true, false, true>(prm, item, smem);
-        else if (P <= 4) fusedBody<BASIS, POS, 4, true, false, true>(prm, item, smem);
-        else if (P <= 6) fusedBody<BASIS, POS, 6, true, false, true>(prm, item, smem);
-        else fusedBody<BASIS, POS, 8, true, false, true>(prm, item, smem);
+        if (P <= 2) fusedBody<BASIS, POS, 2, true, 0, true>(prm, item, smem);
+        else if (P <= 4) fusedBody<BASIS, POS, 4, true, 0, true>(prm, item, smem);
+        else if (P <= 6) fusedBody<BASIS, POS, 6, true, 0, true>(prm, item, smem);
+        else fusedBody<BASIS, POS, 8, true, 0, true>(prm, item, smem);
     }
 }
 #undef MPGB_IO
@@ -842,9 +907,10 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
         countLaunches(stream, 1);
         return e;
     };
-    if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, true>);
-    if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, false>);
-    return run(fusedKernel<BASIS, POS, PMAX, false, false>);
+    if (needE == 2) return run(fusedKernel<BASIS, POS, PMAX, true, 2>);
+    if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, 1>);
+    if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, 0>);
+    return run(fusedKernel<BASIS, POS, PMAX, false, 0>);
 }
 
 // Persistent batch launch: as many blocks as fit on the device at once (at

@@ -117,6 +117,8 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         !onDevice(outLogDet.data) || !onDevice(coeffGrad))
         throw std::invalid_argument("the no-allocation entry point takes device pointers only");
     const MapOptions& o = map.Options();
+    if (!o.contDeriv)
+        throw std::invalid_argument("contDeriv = false (discrete derivative) is not provided without allocation.");
     int dev = 0, sms = 0;
     MPGB_CUDA(cudaGetDevice(&dev));
     MPGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

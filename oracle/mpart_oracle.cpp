@@ -246,6 +246,13 @@ static double posDeriv(int kind, double x) {
     if (kind == kSoftPlus) return x < 0 ? std::exp(x) / (std::exp(x) + 1.0) : 1.0 / (1.0 + std::exp(-1.0 * x));
     return std::exp(x);
 }
+static double posSecondDeriv(int kind, double x) {
+    if (kind == kSoftPlus) {
+        const double fx = posDeriv(kind, x);
+        return fx * (1.0 - fx);
+    }
+    return std::exp(x);
+}
 
 // ----------------------------------------------------------------------------
 // MultivariateExpansionWorker (MParT/MultivariateExpansionWorker.h).
@@ -445,6 +452,7 @@ struct Integrand {
     DerivType dt;
     double nugget;
     int pos;
+    double* work = nullptr;  // numTerms doubles for the MixedCoeff mode
     mutable long nevals = 0;
     mutable int infFlag = 0;
     // Status for the quadrature loop: 1 = g(df) was infinite (the reference
@@ -456,17 +464,27 @@ struct Integrand {
     unsigned fdim() const {
         unsigned n = 1;
         if (dt == dDiagonal) n++;
-        if (dt == dParameters) n += ex->numTerms();
+        if (dt == dParameters || dt == dMixedCoeff) n += ex->numTerms();
         if (dt == dInput) n += ex->D;
         return n;
     }
     void operator()(double t, double* out) const {
         nevals++;
         const unsigned dim = ex->D;
-        if (dt == dDiagonal || dt == dInput) ex->fillCache2(cache, t * xd, dDiagonal2);
+        if (dt == dDiagonal || dt == dInput || dt == dMixedCoeff) ex->fillCache2(cache, t * xd, dDiagonal2);
         else ex->fillCache2(cache, t * xd, dDiagonal);
         double df = 0;
-        if (dt == dParameters) {
+        if (dt == dMixedCoeff) {
+            // d/dc of the Diagonal integrand (MonotoneIntegrand.h:148-165).
+            df = ex->diagonalDerivative(cache, coeffs, 1);
+            const double dgdf = posDeriv(pos, df);
+            const double df2 = ex->mixedCoeffDerivative(cache, coeffs, 2, work, 1);
+            double scale = xd * t * dgdf;
+            for (unsigned i = 0; i < ex->numTerms(); ++i) work[i] *= scale;
+            df = ex->mixedCoeffDerivative(cache, coeffs, 1, &out[1], 1);
+            scale = xd * t * df2 * posSecondDeriv(pos, df) + dgdf;
+            for (unsigned i = 0; i < ex->numTerms(); ++i) out[1 + i] = scale * out[1 + i] + work[i];
+        } else if (dt == dParameters) {
             df = ex->mixedCoeffDerivative(cache, coeffs, 1, &out[1], 1);
             double scale = xd * posDeriv(pos, df);
             for (unsigned i = 0; i < ex->numTerms(); ++i) out[1 + i] *= scale;
@@ -837,6 +855,7 @@ static double inverseSingleBracket(double yd, F& f, double x0, const double xtol
 // (the Kokkos one-thread-per-point model).
 // ----------------------------------------------------------------------------
 struct Component {
+    bool contDeriv = true;  // MapOptions::contDeriv
     Expansion ex;
     ACC quad;
     int pos = kSoftPlus;
@@ -968,8 +987,31 @@ int orc_cont_derivative(void* h, const double* coeffs, const double* pts, long N
 }
 
 // LogDeterminantImpl with contDeriv=true (MonotoneComponent.h:105-125).
+// DiscreteDerivative (MonotoneComponent.h:585-638): the Diagonal integrand
+// integrated with the value, i.e. the x_D-derivative of the quadrature
+// approximation of T.
+int orc_discrete_derivative(void* h, const double* coeffs, const double* pts, long N, long rs, long cs,
+                            double* out) {
+    Component& C = *(Component*)h;
+    View2 P{pts, rs, cs};
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(2)), pt(C.D());
+        for (unsigned d = 0; d < C.D(); ++d) pt[d] = P.at(d, i);
+        C.ex.fillCache1(cache.data(), pt.data(), dNone);
+        Integrand ig{&C.ex, cache.data(), pt[C.D() - 1], coeffs, dDiagonal, C.nugget, C.pos};
+        double both[2];
+        C.quad.integrate(ws.data(), ig, 2, 0, 1, both);
+        out[i] = both[1];
+    }
+    return 0;
+}
+
+void orc_set_cont_deriv(void* h, int on) { ((Component*)h)->contDeriv = on != 0; }
+
 int orc_logdet(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, double* out) {
-    orc_cont_derivative(h, coeffs, pts, N, rs, cs, out);
+    if (((Component*)h)->contDeriv) orc_cont_derivative(h, coeffs, pts, N, rs, cs, out);
+    else orc_discrete_derivative(h, coeffs, pts, N, rs, cs, out);
     for (long i = 0; i < N; ++i) out[i] = (out[i] <= 0) ? -std::numeric_limits<double>::infinity() : std::log(out[i]);
     return 0;
 }
@@ -1067,9 +1109,26 @@ int orc_cont_mixed_jacobian(void* h, const double* coeffs, const double* pts, lo
 int orc_logdet_coeff_grad(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, double* out,
                           long ors, long ocs) {
     Component& C = *(Component*)h;
-    orc_cont_mixed_jacobian(h, coeffs, pts, N, rs, cs, out, ors, ocs);
     std::vector<double> derivs(N);
-    orc_cont_derivative(h, coeffs, pts, N, rs, cs, derivs.data());
+    if (C.contDeriv) {
+        orc_cont_mixed_jacobian(h, coeffs, pts, N, rs, cs, out, ors, ocs);
+        orc_cont_derivative(h, coeffs, pts, N, rs, cs, derivs.data());
+    } else {
+        // DiscreteMixedJacobian (MonotoneComponent.h:928-980): the MixedCoeff integrand.
+        View2 P{pts, rs, cs};
+        const unsigned T = C.T();
+        ORC_PARALLEL_FOR
+        for (long i = 0; i < N; ++i) {
+            std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(T + 1)), integral(T + 1), work(T),
+                pt(C.D());
+            for (unsigned d = 0; d < C.D(); ++d) pt[d] = P.at(d, i);
+            C.ex.fillCache1(cache.data(), pt.data(), dNone);
+            Integrand ig{&C.ex, cache.data(), pt[C.D() - 1], coeffs, dMixedCoeff, C.nugget, C.pos, work.data()};
+            C.quad.integrate(ws.data(), ig, T + 1, 0, 1, integral.data());
+            for (unsigned t = 0; t < T; ++t) out[t * ors + i * ocs] = integral[t + 1];
+        }
+        orc_discrete_derivative(h, coeffs, pts, N, rs, cs, derivs.data());
+    }
     for (long i = 0; i < N; ++i)
         for (unsigned t = 0; t < C.T(); ++t) out[t * ors + i * ocs] *= 1.0 / derivs[i];
     return 0;
@@ -1099,6 +1158,9 @@ int orc_cont_mixed_input_jacobian(void* h, const double* coeffs, const double* p
 int orc_logdet_input_grad(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, double* out,
                           long ors, long ocs) {
     Component& C = *(Component*)h;
+    // The reference throws std::invalid_argument here ("Discrete derivative
+    // version is not implemented yet", MonotoneComponent.h:216-222).
+    if (!C.contDeriv) return -1;
     orc_cont_mixed_input_jacobian(h, coeffs, pts, N, rs, cs, out, ors, ocs);
     std::vector<double> derivs(N);
     orc_cont_derivative(h, coeffs, pts, N, rs, cs, derivs.data());

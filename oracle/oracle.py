@@ -79,6 +79,8 @@ def lib():
         L.orc_cc_rule.argtypes = [C.c_uint, _dp, _dp]
         L.orc_acc_test.argtypes = [C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_uint, C.c_double,
                                    C.c_double, _dp, _lp]
+        L.orc_set_cont_deriv.argtypes = [C.c_void_p, C.c_int]
+        L.orc_discrete_derivative.argtypes = [C.c_void_p, _dp, _dp, C.c_long, C.c_long, C.c_long, _dp]
         L.orc_quad_test.argtypes = [C.c_int, C.c_int, C.c_uint, C.c_uint, C.c_double, C.c_double, C.c_uint,
                                     C.c_double, C.c_double, _dp, _lp]
         L.orc_rootfind_test.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, _ip]
@@ -120,7 +122,7 @@ class OracleComponent:
 
     def __init__(self, dim, starts, dims, orders, basis=BASIS_PROB_HERMITE, normalize=True,
                  posfunc=POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6, max_sub=30, min_sub=0, quad_pts=5,
-                 nugget=0.0, quad_type=QUAD_ACC):
+                 nugget=0.0, quad_type=QUAD_ACC, cont_deriv=True):
         self.dim = int(dim)
         self.starts = np.ascontiguousarray(starts, np.uint32)
         self.dims = np.ascontiguousarray(dims, np.uint32)
@@ -136,6 +138,8 @@ class OracleComponent:
         self._h = L.orc_component_new(self.dim, self.num_terms, self.starts.ctypes.data_as(_up),
                                       d.ctypes.data_as(_up), o.ctypes.data_as(_up), basis, int(normalize),
                                       posfunc, abs_tol, rel_tol, max_sub, min_sub, quad_pts, nugget, quad_type)
+        self.cont_deriv = bool(cont_deriv)
+        L.orc_set_cont_deriv(self._h, int(self.cont_deriv))
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -224,7 +228,8 @@ class OracleComponent:
         coeffs = _f64(coeffs)
         pts, N, rs, cs = self._pts(pts)
         out = np.zeros((self.dim, N))
-        lib().orc_logdet_input_grad(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out), N, 1)
+        if lib().orc_logdet_input_grad(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out), N, 1) != 0:
+            raise ValueError("Discrete derivative version is not implemented yet (To Do)")
         return out
 
     def inverse(self, coeffs, xs, ys, xtol=1e-6, ytol=1e-6, return_info=False):
@@ -258,14 +263,14 @@ class OracleTriangularMap:
 
     def __init__(self, input_dim, output_dim, order, basis=BASIS_PROB_HERMITE, normalize=True,
                  posfunc=POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6, max_sub=30, min_sub=0, quad_pts=5, nugget=0.0,
-                 components=None, quad_type=QUAD_ACC):
+                 components=None, quad_type=QUAD_ACC, cont_deriv=True):
         if components is None:
             extra = input_dim - output_dim
             components = []
             for i in range(output_dim):
                 s, d, o = total_order(i + extra + 1, int(order))
                 components.append(OracleComponent(i + extra + 1, s, d, o, basis, normalize, posfunc, abs_tol,
-                                                  rel_tol, max_sub, min_sub, quad_pts, nugget, quad_type))
+                                                  rel_tol, max_sub, min_sub, quad_pts, nugget, quad_type, cont_deriv))
         self.comps = components
         self.input_dim = components[-1].input_dim
         self.output_dim = len(components)

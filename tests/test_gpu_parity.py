@@ -519,3 +519,42 @@ def test_quadrature_kinds_match_oracle(gpu, oracle, quad, pts):
     r = om.evaluate(coef, x)
     xi = H(tm.Inverse(T(x[:1]), T(r), xtol=1e-10, ytol=1e-10))
     assert_inverse_parity(om, coef, x[:1], r, xi, 1e-10, 1e-10)
+
+
+# ----------------------------------------------------------------------------
+# contDeriv = false: log-determinants of the quadrature approximation
+# (DiscreteDerivative / DiscreteMixedJacobian).
+# ----------------------------------------------------------------------------
+@pytest.mark.parametrize("basis,pos,quad", [(0, 1, 2), (2, 0, 2), (0, 1, 1)])
+def test_discrete_derivative_matches_oracle(gpu, oracle, basis, pos, quad):
+    import torch
+    M, O = gpu, oracle
+    opt = M.MapOptions(basisType=M.BasisTypes(basis), posFuncType=M.PosFuncTypes(pos), quadType=M.QuadTypes(quad),
+                       quadAbsTol=1e-7, quadRelTol=1e-7, contDeriv=False)
+    tm = M.CreateTriangular(3, 3, 3, opt)
+    om = O.OracleTriangularMap(3, 3, 3, basis=basis, posfunc=pos, abs_tol=1e-7, rel_tol=1e-7, quad_type=quad,
+                               cont_deriv=False)
+    rng = np.random.default_rng(50 + basis + pos + quad)
+    coef = rng.normal(0.0, 0.1, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    x = rng.standard_normal((3, 1200))
+    sens = rng.standard_normal((3, 1200))
+    xs = T(x)
+    assert_parity(H(tm.LogDeterminant(xs)), om.logdet(coef, x), what="discrete LogDeterminant")
+    assert_parity(H(tm.LogDeterminantCoeffGrad(xs)), om.logdet_coeff_grad(coef, x),
+                  what="discrete LogDeterminantCoeffGrad")
+    assert_parity(H(tm.Evaluate(xs)), om.evaluate(coef, x), what="Evaluate")
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device="cuda")
+    ld = torch.zeros(1200, dtype=torch.float64, device="cuda")
+    tm.FusedForwardAdjointImpl(xs, sens=T(sens), logdet_sens_scale=1.0, out_logdet=ld, coeff_grad=cg)
+    ref = om.coeff_grad(coef, x, sens).sum(axis=1) + om.logdet_coeff_grad(coef, x).sum(axis=1)
+    assert_parity(H(cg), ref, floor=1e-3, what="discrete fused adjoint")
+    assert_parity(H(ld), om.logdet(coef, x), what="discrete fused log-det")
+    loss, grad = tm.KLObjective(xs)
+    cs = om.split(coef)
+    refs = [O.fast_gaussian_reverse_kl(c, cs[i], x[:c.input_dim]) for i, c in enumerate(om.comps)]
+    assert_parity(H(loss), np.array([r[0] for r in refs]), what="discrete KL loss")
+    assert_parity(H(grad), np.concatenate([r[1] for r in refs]), floor=1e-3, what="discrete KL gradient")
+    # as in the reference (MonotoneComponent.h:216-222)
+    with pytest.raises(ValueError, match="Discrete derivative"):
+        tm.LogDeterminantInputGrad(xs)
