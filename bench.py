@@ -563,10 +563,8 @@ def run_gpu(args):
         dist.barrier()
     times = [a.elapsed_time(b) for a, b in ev]
     t_step = float(np.mean(times)) * 1e-3
-    t_tot = torch.tensor([t_step * args.steps], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t_tot, op=dist.ReduceOp.MAX)
-    t_step_max = t_tot.item() / args.steps
+    from mpart_gb300.distributed import max_over_ranks
+    t_step_max = max_over_ranks(t_step * args.steps, device=dev) / args.steps
     value = world * N / t_step_max
 
     # e2e: C ABI with pinned host buffers (copies inside the timed region).
@@ -588,10 +586,7 @@ def run_gpu(args):
         step_e2e()
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        te = torch.tensor([t_e2e], dtype=torch.float64, device=dev)
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        t_e2e = te.item()
+    t_e2e = max_over_ranks(t_e2e, device=dev)
     h2d = xh.nbytes + sh.nbytes
     d2h = Tp.numel() * 8 + ldp.numel() * 8 + cgp.numel() * 8
 
