@@ -350,35 +350,57 @@ def mean_evals(sample=20000):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region.  A reader thread stamps
+    each sample with the host clock on arrival; only samples that arrive
+    while the region is open (plus one interval after it closes) count, so a
+    sample taken while nvidia-smi starts up or after the region is dropped."""
+
+    INTERVAL_MS = 50
 
     def __init__(self, index):
         self.p = None
         self.index = index
+        self.stamped = []
+        self.t0 = self.t1 = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            if line.strip():
+                self.stamped.append((time.monotonic(), line))
 
     def __enter__(self):
+        import threading
         try:
             self.p = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}",
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+            deadline = time.monotonic() + 5.0  # wait for the sampler to be running
+            while not self.stamped and time.monotonic() < deadline:
+                time.sleep(0.01)
         except Exception:
             self.p = None
+        self.t0 = time.monotonic()
         return self
 
     def __exit__(self, *a):
+        self.t1 = time.monotonic()
         self.lines = []
         if self.p is not None:
+            time.sleep(self.INTERVAL_MS / 1000.0 * 1.5)
             self.p.terminate()
             try:
-                out, _ = self.p.communicate(timeout=5)
+                self.p.wait(timeout=5)
             except Exception:
                 self.p.kill()
-                out = ""
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            self.th.join(timeout=5)
+            hi = self.t1 + self.INTERVAL_MS / 1000.0
+            self.lines = [l for t, l in self.stamped if self.t0 < t <= hi]
 
     def summary(self):
         sm, smax, reasons = [], None, set()

@@ -255,6 +255,181 @@ static double posSecondDeriv(int kind, double x) {
 }
 
 // ----------------------------------------------------------------------------
+// Sigmoid1d (MParT/Sigmoid.h:87-446) with the Logistic sigmoid (:23-40) and
+// SoftPlus edge terms: f_0 = 1, f_1 = x, f_2 = -w_0 g(-b_0 (x - c_0)),
+// f_3 = w_1 g(b_1 (x - c_1)), f_k = sum_j w_j s(b_j (x - c_j)) over the
+// centers of term k (starting indices as in CSR).  The product of each
+// weight/width factor is formed left to right as in the reference.
+// ----------------------------------------------------------------------------
+struct Sigmoid1d {
+    std::vector<double> centers, widths, weights;
+    std::vector<unsigned> starts;
+    int order = 0;
+
+    static double logistic(double x) { return 0.5 + 0.5 * std::tanh(x / 2); }
+    static double logisticD(double x) {
+        double fx = logistic(x);
+        return fx * (1 - fx);
+    }
+    static double logisticD2(double x) {
+        double fx = logistic(x);
+        return fx * (1 - fx) * (1 - 2 * fx);
+    }
+    // ConstructStartInds (:95-130).  Returns false when the Linear sum type
+    // does not fit the number of centers.
+    static int numSigmoids(unsigned numCenters, int sumType) {
+        if (sumType == 1) return (int)numCenters - 2;
+        return (int)((std::sqrt(1 + 8 * ((double)numCenters - 2)) - 1) / 2);
+    }
+    static bool constructStarts(unsigned centerSize, int sumType, std::vector<unsigned>& out) {
+        out.clear();
+        int numTerms = numSigmoids(centerSize, sumType);
+        if (centerSize <= 2) return true;
+        if (sumType == 0) {
+            if ((int)(centerSize - 2) != (numTerms * (numTerms + 1) / 2)) return false;
+            out.resize(numTerms);
+            out[0] = 2;
+            for (int i = 1; i < numTerms; ++i) out[i] = out[i - 1] + i;
+        } else {
+            numTerms = (int)centerSize - 2;
+            out.resize(numTerms);
+            out[0] = 2;
+            for (int i = 1; i < numTerms; ++i) out[i] = out[i - 1] + 1;
+        }
+        return true;
+    }
+    // Validate (:386-431).
+    bool validate() {
+        if (centers.size() != widths.size() || centers.size() != weights.size() || centers.size() < starts.size())
+            return false;
+        if (centers.size() < 2) return false;
+        if (!starts.empty()) {
+            if (starts[0] != 2) return false;
+            for (size_t i = 1; i < starts.size(); ++i) {
+                if (starts[i] <= starts[i - 1]) return false;
+                if (starts[i] >= centers.size()) return false;
+            }
+        }
+        order = (int)starts.size() + 1 + 2;
+        return true;
+    }
+    void range(int k, int& b, int& e) const {
+        b = (int)starts[k - 4];
+        e = (int)centers.size();
+        if ((size_t)(k - 4 + 1) < starts.size()) e = (int)starts[k - 4 + 1];
+    }
+    void evalAll(double* out, unsigned maxOrder, double x) const {
+        out[0] = 1.;
+        if (maxOrder == 0) return;
+        out[1] = x;
+        if (maxOrder == 1) return;
+        out[2] = -weights[0] * posEval(kSoftPlus, -widths[0] * (x - centers[0]));
+        if (maxOrder == 2) return;
+        out[3] = weights[1] * posEval(kSoftPlus, widths[1] * (x - centers[1]));
+        if (maxOrder == 3) return;
+        for (int k = 4; k <= (int)maxOrder; ++k) {
+            out[k] = 0.;
+            int b, e;
+            range(k, b, e);
+            for (int j = b; j < e; ++j) out[k] += weights[j] * logistic(widths[j] * (x - centers[j]));
+        }
+    }
+    void evalDerivs(double* out, double* d1, unsigned maxOrder, double x) const {
+        out[0] = 1.;
+        d1[0] = 0.;
+        if (maxOrder == 0) return;
+        out[1] = x;
+        d1[1] = 1.;
+        if (maxOrder == 1) return;
+        out[2] = -weights[0] * posEval(kSoftPlus, -widths[0] * (x - centers[0]));
+        d1[2] = weights[0] * widths[0] * posDeriv(kSoftPlus, -widths[0] * (x - centers[0]));
+        if (maxOrder == 2) return;
+        out[3] = weights[1] * posEval(kSoftPlus, widths[1] * (x - centers[1]));
+        d1[3] = weights[1] * widths[1] * posDeriv(kSoftPlus, widths[1] * (x - centers[1]));
+        if (maxOrder == 3) return;
+        for (int k = 4; k <= (int)maxOrder; ++k) {
+            out[k] = 0.;
+            d1[k] = 0.;
+            int b, e;
+            range(k, b, e);
+            for (int j = b; j < e; ++j) {
+                out[k] += weights[j] * logistic(widths[j] * (x - centers[j]));
+                d1[k] += weights[j] * widths[j] * logisticD(widths[j] * (x - centers[j]));
+            }
+        }
+    }
+    void evalSecond(double* out, double* d1, double* d2, unsigned maxOrder, double x) const {
+        out[0] = 1.;
+        d1[0] = 0.;
+        d2[0] = 0.;
+        if (maxOrder == 0) return;
+        out[1] = x;
+        d1[1] = 1.;
+        d2[1] = 0.;
+        if (maxOrder == 1) return;
+        out[2] = -weights[0] * posEval(kSoftPlus, -widths[0] * (x - centers[0]));
+        d1[2] = weights[0] * widths[0] * posDeriv(kSoftPlus, -widths[0] * (x - centers[0]));
+        d2[2] = -weights[0] * widths[0] * widths[0] * posSecondDeriv(kSoftPlus, -widths[0] * (x - centers[0]));
+        if (maxOrder == 2) return;
+        out[3] = weights[1] * posEval(kSoftPlus, widths[1] * (x - centers[1]));
+        d1[3] = weights[1] * widths[1] * posDeriv(kSoftPlus, widths[1] * (x - centers[1]));
+        d2[3] = weights[1] * widths[1] * widths[1] * posSecondDeriv(kSoftPlus, widths[1] * (x - centers[1]));
+        if (maxOrder == 3) return;
+        for (int k = 4; k <= (int)maxOrder; ++k) {
+            out[k] = 0.;
+            d1[k] = 0.;
+            d2[k] = 0.;
+            int b, e;
+            range(k, b, e);
+            for (int j = b; j < e; ++j) {
+                out[k] += weights[j] * logistic(widths[j] * (x - centers[j]));
+                d1[k] += weights[j] * widths[j] * logisticD(widths[j] * (x - centers[j]));
+                d2[k] += weights[j] * widths[j] * widths[j] * logisticD2(widths[j] * (x - centers[j]));
+            }
+        }
+    }
+};
+
+// CreateSigmoid (src/MapFactory.cpp:181-254): edge terms get width edgeShape
+// and weight 1/edgeShape; Linear sums set the widths of all but the last
+// sigmoid of each term from the neighbouring centers (the last keeps width
+// 0); Constant sums sort the interior centers and use neighbour spacings.
+static bool sigmoidFromCenters(const double* c, unsigned n, double edgeShape, int sumType, Sigmoid1d& S) {
+    int numSig = Sigmoid1d::numSigmoids(n, sumType);
+    std::vector<double> hW(n, 0.0), hWt(n, 1.0), hC(c, c + n);
+    if (n < 2) return false;
+    hW[0] = edgeShape;
+    hWt[0] = 1.0 / edgeShape;
+    hW[1] = edgeShape;
+    hWt[1] = 1.0 / edgeShape;
+    if (sumType == 0) {
+        for (int i = 0; i < numSig; i++) {
+            int start = 2 + (i * (i + 1)) / 2;
+            for (int j = 0; j < i; j++) {
+                double prev, next;
+                if (j == 0 || i == 0) prev = c[0];
+                else prev = c[start + j - 1];
+                if (j == i - 1 || i == 0) next = c[1];
+                else next = c[start + j];
+                hW[start + j] = 2 / (next - prev);
+                hWt[start + j] = 1.;
+            }
+        }
+    } else if (numSig > 0) {
+        std::sort(hC.begin() + 2, hC.end());
+        if (numSig > 1) hW[2] = 4.0 / (hC[3] - hC[2]);
+        else hW[2] = 8.0 / std::abs(hC[1] - hC[0]);
+        for (int i = 1; i < numSig - 1; i++) hW[2 + i] = 8.0 / (hC[3 + i] - hC[1 + i]);
+        if (numSig > 1) hW[2 + numSig - 1] = 4.0 / (hC[2 + numSig - 1] - hC[2 + numSig - 2]);
+    }
+    S.centers = hC;
+    S.widths = hW;
+    S.weights = hWt;
+    if (!Sigmoid1d::constructStarts(n, sumType, S.starts)) return false;
+    return S.validate();
+}
+
+// ----------------------------------------------------------------------------
 // MultivariateExpansionWorker (MParT/MultivariateExpansionWorker.h).
 // Cache layout :19-40 and :94-107; FillCache1 :142-158; FillCache2 :172-201;
 // term loops :204-397; per-term products :423-554 (Identity rectifier).
@@ -265,6 +440,12 @@ struct Expansion {
     MultiSet ms;
     Basis1d basis;
     unsigned D = 0;
+    // BasisEvaluator<OffdiagHomogeneous, pair<offdiag, Sigmoid1d>, Rectifier>
+    // (MParT/BasisEvaluator.h:221-330): a sigmoid basis in the last input and
+    // a rectifier (-1 Identity, else a positive bijector) applied to the
+    // leading-input product of every term that depends on the last input.
+    const Sigmoid1d* diag = nullptr;
+    int rect = -1;
     std::vector<unsigned> startPos;
     unsigned cacheSize = 0;
 
@@ -292,6 +473,15 @@ struct Expansion {
         }
     }
     void fillCache2(double* c, double xd, DerivType dt) const {
+        if (diag) {
+            if (dt == dNone || dt == dParameters) diag->evalAll(&c[startPos[D - 1]], ms.maxDeg[D - 1], xd);
+            else if (dt == dDiagonal || dt == dInput || dt == dMixedCoeff)
+                diag->evalDerivs(&c[startPos[D - 1]], &c[startPos[2 * D - 1]], ms.maxDeg[D - 1], xd);
+            else
+                diag->evalSecond(&c[startPos[D - 1]], &c[startPos[2 * D - 1]], &c[startPos[2 * D]], ms.maxDeg[D - 1],
+                                 xd);
+            return;
+        }
         if (dt == dNone || dt == dParameters) {
             basis.evalAll(&c[startPos[D - 1]], ms.maxDeg[D - 1], xd);
         } else if (dt == dDiagonal || dt == dInput || dt == dMixedCoeff) {
@@ -307,7 +497,8 @@ struct Expansion {
         unsigned e = ms.starts[t + 1] - 1;
         for (unsigned i = ms.starts[t]; i < e; ++i) v *= cv(c, i);
         double last = cv(c, e);
-        v *= last;
+        if (rect >= 0) v = (ms.dims[e] == D - 1) ? posEval(rect, v) * last : v * last;
+        else v *= last;
         return v;
     }
     double termValDiag(unsigned t, const double* c, unsigned posIndex) const {
@@ -315,8 +506,9 @@ struct Expansion {
         unsigned e = ms.starts[t + 1] - 1;
         if (ms.dims[e] != D - 1) return 0.;
         for (unsigned i = ms.starts[t]; i < e; ++i) v *= cv(c, i);
-        double diag = c[startPos[posIndex] + ms.orders[e]];
-        v *= diag;
+        double dv = c[startPos[posIndex] + ms.orders[e]];
+        if (rect >= 0) v = posEval(rect, v);
+        v *= dv;
         return v;
     }
     double termValInputDeriv(unsigned t, int wrt, const double* c) const {
@@ -339,7 +531,14 @@ struct Expansion {
         } else {
             last = c[startPos[d] + ms.orders[e]];
         }
-        (void)wrtVal;
+        if (rect >= 0) {
+            const bool isRect = d == int(D) - 1;
+            if (wrt == int(D) - 1) v = posEval(rect, v) * wrtDeriv;
+            else if (wrt == -1) v = isRect ? posEval(rect, v) * last : v * last;
+            else if (!isRect) v *= last * wrtDeriv;
+            else v = posDeriv(rect, v * wrtVal) * v * wrtDeriv * last;
+            return v;
+        }
         v *= last * wrtDeriv;
         return v;
     }
@@ -355,10 +554,14 @@ struct Expansion {
                 v *= cv(c, i);
             }
         }
-        (void)wrtVal;
         unsigned posInd = (wrt == int(D) - 1) ? (2 * D) : (2 * D - 1);
-        double diag = c[startPos[posInd] + ms.orders[e]];
-        v *= (diag * wrtDeriv);
+        double dv = c[startPos[posInd] + ms.orders[e]];
+        if (rect >= 0) {
+            if (wrt == int(D) - 1 || wrt == -1) v = posEval(rect, v) * dv;
+            else v = posDeriv(rect, v * wrtVal) * v * wrtDeriv * dv;
+            return v;
+        }
+        v *= (dv * wrtDeriv);
         return v;
     }
     double termValMixedCoeff(unsigned t, const double* c, unsigned posIndex) const {
@@ -367,8 +570,9 @@ struct Expansion {
         unsigned e = ms.starts[t + 1] - 1;
         if (ms.dims[e] != D - 1) return 0.;
         for (unsigned i = ms.starts[t]; i < e; ++i) v *= cv(c, i);
-        double diag = c[startPos[posIndex] + ms.orders[e]];
-        v *= diag;
+        double dv = c[startPos[posIndex] + ms.orders[e]];
+        if (rect >= 0) v = posEval(rect, v);
+        v *= dv;
         return v;
     }
 
@@ -1195,6 +1399,230 @@ int orc_inverse(void* h, const double* coeffs, const double* xs, long numXs, lon
         std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(1));
         C.ex.fillCache1(cache.data(), pt.data(), dNone);
         auto f = [&](double x) { return evaluateSingle(C, cache.data(), ws.data(), x, coeffs, nullptr, nullptr); };
+        int inf = 0;
+        out[i * ostride] = inverseSingleBracket(ys[i * ystride], f, pt[D - 1], xtol, ytol, inf);
+        if (info) info[i] = inf;
+    }
+    return 0;
+}
+
+// ----------------------------------------------------------------------------
+// Sigmoid expansions: RectifiedMultivariateExpansion
+// (MParT/RectifiedMultivariateExpansion.h:40-405) and, for one input,
+// UnivariateExpansion<Sigmoid1d> (MParT/UnivariateExpansion.h:47-297).  The
+// worker is the Expansion above with the sigmoid basis in the last input and
+// the rectifier on the leading-input products.  No quadrature.
+// ----------------------------------------------------------------------------
+struct RectComponent {
+    Sigmoid1d sig;
+    Expansion ex;
+    bool univariate = false;
+    unsigned D() const { return ex.D; }
+    unsigned T() const { return ex.numTerms(); }
+};
+
+// CreateSigmoid's parameters for a vector of centers (0 ok, -1 invalid).
+// outStarts has room for nCenters entries; *nStarts receives their count.
+int orc_sigmoid_from_centers(unsigned n, const double* centers, double edgeShape, int sumType, double* outCenters,
+                             double* outWidths, double* outWeights, unsigned* outStarts, unsigned* nStarts) {
+    Sigmoid1d S;
+    if (!sigmoidFromCenters(centers, n, edgeShape, sumType, S)) return -1;
+    std::copy(S.centers.begin(), S.centers.end(), outCenters);
+    std::copy(S.widths.begin(), S.widths.end(), outWidths);
+    std::copy(S.weights.begin(), S.weights.end(), outWeights);
+    std::copy(S.starts.begin(), S.starts.end(), outStarts);
+    *nStarts = (unsigned)S.starts.size();
+    return 0;
+}
+
+static bool makeSigmoid(unsigned n, const double* c, const double* w, const double* wt, unsigned ns,
+                        const unsigned* st, Sigmoid1d& S) {
+    S.centers.assign(c, c + n);
+    S.widths.assign(w, w + n);
+    S.weights.assign(wt, wt + n);
+    S.starts.assign(st, st + ns);
+    return S.validate();
+}
+
+// Sigmoid1d::EvaluateAll / EvaluateDerivatives / EvaluateSecondDerivatives
+// (which = 0, 1, 2).  -1: invalid parameters or maxOrder above the order.
+int orc_sigmoid_eval(unsigned n, const double* c, const double* w, const double* wt, unsigned ns, const unsigned* st,
+                     int which, unsigned maxOrder, double x, double* v, double* d1, double* d2) {
+    Sigmoid1d S;
+    if (!makeSigmoid(n, c, w, wt, ns, st, S)) return -1;
+    if ((int)maxOrder > S.order) return -1;
+    if (which == 0) S.evalAll(v, maxOrder, x);
+    else if (which == 1) S.evalDerivs(v, d1, maxOrder, x);
+    else S.evalSecond(v, d1, d2, maxOrder, x);
+    return S.order;
+}
+
+// rect: -1 Identity, else the positive bijector kind.  nC == 0 puts the
+// leading-input basis in the last input as well (the unrectified test case).
+void* orc_rect_new(unsigned dim, unsigned nterms, const unsigned* starts, const unsigned* dims,
+                   const unsigned* orders, int basis, int normalize, int rect, unsigned nC, const double* centers,
+                   const double* widths, const double* weights, unsigned nStarts, const unsigned* sstarts,
+                   int univariate) {
+    RectComponent* R = new RectComponent();
+    R->ex.ms.dim = dim;
+    R->ex.ms.starts.assign(starts, starts + nterms + 1);
+    unsigned nnz = starts[nterms];
+    R->ex.ms.dims.assign(dims, dims + nnz);
+    R->ex.ms.orders.assign(orders, orders + nnz);
+    R->ex.ms.calcMaxDegrees();
+    R->ex.basis.kind = basis;
+    R->ex.basis.prob.normalize = normalize != 0;
+    R->univariate = univariate != 0;
+    R->ex.rect = R->univariate ? -1 : rect;
+    if (nC) {
+        if (!makeSigmoid(nC, centers, widths, weights, nStarts, sstarts, R->sig) ||
+            (int)R->ex.ms.maxDeg[dim - 1] > R->sig.order) {
+            delete R;
+            return nullptr;
+        }
+        R->ex.diag = &R->sig;
+    }
+    R->ex.setup();
+    return R;
+}
+void orc_rect_free(void* h) { delete (RectComponent*)h; }
+
+// EvaluateImpl (RectifiedMultivariateExpansion.h:40-75; UnivariateExpansion.h:47-75).
+int orc_rect_evaluate(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, double* out) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(R.D());
+        for (unsigned d = 0; d < R.D(); ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dNone);
+        R.ex.fillCache2(cache.data(), pt[R.D() - 1], dNone);
+        out[i] = R.ex.evaluate(cache.data(), coeffs);
+    }
+    return 0;
+}
+
+// GradientImpl (:77-139): sens(i) * grad_x T(x_i), D x N.
+int orc_rect_gradient(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, const double* sens,
+                      double* out, long ors, long ocs) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    const unsigned D = R.D();
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(D), g(D);
+        for (unsigned d = 0; d < D; ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dInput);
+        R.ex.fillCache2(cache.data(), pt[D - 1], dInput);
+        R.ex.inputDerivative(cache.data(), coeffs, g.data(), 1);
+        for (unsigned d = 0; d < D; ++d) out[d * ors + i * ocs] = g[d] * sens[i];
+    }
+    return 0;
+}
+
+// CoeffGradImpl (:141-190): sens(i) * dT/dc, T x N (row stride N).
+int orc_rect_coeff_grad(void* h, const double* coeffs, const double* pts, long N, long rs, long cs,
+                        const double* sens, double* out) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    const unsigned T = R.T();
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(R.D());
+        for (unsigned d = 0; d < R.D(); ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dParameters);
+        R.ex.fillCache2(cache.data(), pt[R.D() - 1], dParameters);
+        R.ex.coeffDerivative(cache.data(), coeffs, out + i, N);
+        for (unsigned t = 0; t < T; ++t) out[t * N + i] *= sens[i];
+    }
+    return 0;
+}
+
+// LogDeterminantImpl (:192-225): log of the diagonal derivative.
+int orc_rect_logdet(void* h, const double* coeffs, const double* pts, long N, long rs, long cs, double* out) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(R.D());
+        for (unsigned d = 0; d < R.D(); ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dNone);
+        R.ex.fillCache2(cache.data(), pt[R.D() - 1], dDiagonal);
+        out[i] = std::log(R.ex.diagonalDerivative(cache.data(), coeffs, 1));
+    }
+    return 0;
+}
+
+// LogDeterminantInputGradImpl (:279-325): [grad_x d_D T, d_D^2 T] / d_D T.
+int orc_rect_logdet_input_grad(void* h, const double* coeffs, const double* pts, long N, long rs, long cs,
+                               double* out, long ors, long ocs) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    const unsigned D = R.D();
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(D), g(D);
+        for (unsigned d = 0; d < D; ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dMixedInput);
+        R.ex.fillCache2(cache.data(), pt[D - 1], dMixedInput);
+        R.ex.mixedInputDerivative(cache.data(), coeffs, g.data(), 1);
+        R.ex.fillCache1(cache.data(), pt.data(), dDiagonal);
+        R.ex.fillCache2(cache.data(), pt[D - 1], dDiagonal);
+        double dd = R.ex.diagonalDerivative(cache.data(), coeffs, 1);
+        for (unsigned d = 0; d < D; ++d) out[d * ors + i * ocs] = g[d] / dd;
+    }
+    return 0;
+}
+
+// LogDeterminantCoeffGradImpl (:327-370): d_c d_D T / d_D T, T x N.
+int orc_rect_logdet_coeff_grad(void* h, const double* coeffs, const double* pts, long N, long rs, long cs,
+                               double* out) {
+    RectComponent& R = *(RectComponent*)h;
+    View2 P{pts, rs, cs};
+    const unsigned T = R.T();
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        std::vector<double> cache(R.ex.cacheSize), pt(R.D());
+        for (unsigned d = 0; d < R.D(); ++d) pt[d] = P.at(d, i);
+        R.ex.fillCache1(cache.data(), pt.data(), dMixedCoeff);
+        R.ex.fillCache2(cache.data(), pt[R.D() - 1], dMixedCoeff);
+        R.ex.mixedCoeffDerivative(cache.data(), coeffs, 1, out + i, N);
+        R.ex.fillCache1(cache.data(), pt.data(), dDiagonal);
+        R.ex.fillCache2(cache.data(), pt[R.D() - 1], dDiagonal);
+        double dd = R.ex.diagonalDerivative(cache.data(), coeffs, 1);
+        for (unsigned t = 0; t < T; ++t) out[t * N + i] /= dd;
+    }
+    return 0;
+}
+
+// InverseImpl (:227-277; UnivariateExpansion.h:213-250): bracketed ITP root
+// of T(x_<D, .) = r from x0 = the point's last entry (0 for one input).
+int orc_rect_inverse(void* h, const double* coeffs, const double* xs, long numXs, long rs, long cs, const double* ys,
+                     long ystride, long N, double xtol, double ytol, double* out, long ostride, int* info) {
+    RectComponent& R = *(RectComponent*)h;
+    if ((numXs != 1) && (numXs != N)) return -1;
+    View2 P{xs, rs, cs};
+    const unsigned D = R.D();
+    ORC_PARALLEL_FOR
+    for (long i = 0; i < N; ++i) {
+        long xi = (numXs == 1) ? 0 : i;
+        std::vector<double> pt(D);
+        bool hasNan = std::isnan(ys[i * ystride]) && R.univariate;
+        for (unsigned d = 0; d < D; ++d) {
+            pt[d] = R.univariate ? 0.0 : P.at(d, xi);
+            if (std::isnan(pt[d])) hasNan = true;
+        }
+        if (hasNan) {
+            out[i * ostride] = std::numeric_limits<double>::quiet_NaN();
+            if (info) info[i] = 0;
+            continue;
+        }
+        std::vector<double> cache(R.ex.cacheSize);
+        R.ex.fillCache1(cache.data(), pt.data(), dNone);
+        auto f = [&](double x) {
+            R.ex.fillCache2(cache.data(), x, dNone);
+            return R.ex.evaluate(cache.data(), coeffs);
+        };
         int inf = 0;
         out[i * ostride] = inverseSingleBracket(ys[i * ystride], f, pt[D - 1], xtol, ytol, inf);
         if (info) info[i] = inf;

@@ -87,6 +87,21 @@ def lib():
         L.orc_rootfind_test.restype = C.c_double
         L.orc_findbracket_test.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_double]
         L.orc_integrand.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int, _dp]
+        L.orc_sigmoid_from_centers.argtypes = [C.c_uint, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _up, _up]
+        L.orc_sigmoid_eval.argtypes = [C.c_uint, _dp, _dp, _dp, C.c_uint, _up, C.c_int, C.c_uint, C.c_double, _dp,
+                                       _dp, _dp]
+        L.orc_rect_new.restype = C.c_void_p
+        L.orc_rect_new.argtypes = [C.c_uint, C.c_uint, _up, _up, _up, C.c_int, C.c_int, C.c_int, C.c_uint, _dp, _dp,
+                                   _dp, C.c_uint, _up, C.c_int]
+        L.orc_rect_free.argtypes = [C.c_void_p]
+        L.orc_rect_evaluate.argtypes = pts_sig + [_dp]
+        L.orc_rect_gradient.argtypes = pts_sig + [_dp, _dp, C.c_long, C.c_long]
+        L.orc_rect_coeff_grad.argtypes = pts_sig + [_dp, _dp]
+        L.orc_rect_logdet.argtypes = pts_sig + [_dp]
+        L.orc_rect_logdet_input_grad.argtypes = pts_sig + [_dp, C.c_long, C.c_long]
+        L.orc_rect_logdet_coeff_grad.argtypes = pts_sig + [_dp]
+        L.orc_rect_inverse.argtypes = [C.c_void_p, _dp, _dp, C.c_long, C.c_long, C.c_long, _dp, C.c_long, C.c_long,
+                                       C.c_double, C.c_double, _dp, C.c_long, _ip]
         _lib = L
     return _lib
 
@@ -114,6 +129,213 @@ def total_order(dim: int, order: int):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def total_order_min(dim: int, order: int, min_order: int):
+    """FixedMultiIndexSet(dim, order, minOrder): the total-order set without the
+    terms of total order below minOrder, in the same order."""
+    s, d, o = total_order(dim, order)
+    keep = [t for t in range(len(s) - 1) if int(o[s[t]:s[t + 1]].sum()) >= min_order]
+    starts, dims, orders = [0], [], []
+    for t in keep:
+        dims.extend(d[s[t]:s[t + 1]])
+        orders.extend(o[s[t]:s[t + 1]])
+        starts.append(len(dims))
+    return np.array(starts, np.uint32), np.array(dims, np.uint32), np.array(orders, np.uint32)
+
+
+def cartesian(a, a_len, b):
+    """FixedMultiIndexSet::Cartesian (src/MultiIndices/FixedMultiIndexSet.cpp:356-397):
+    terms (i, j) with i of the first set outermost; dims of the second set
+    shifted by the first set's length."""
+    sa, da, oa = a
+    sb, db, ob = b
+    starts, dims, orders = [0], [], []
+    for i in range(len(sa) - 1):
+        for j in range(len(sb) - 1):
+            dims.extend(da[sa[i]:sa[i + 1]])
+            orders.extend(oa[sa[i]:sa[i + 1]])
+            dims.extend(int(x) + a_len for x in db[sb[j]:sb[j + 1]])
+            orders.extend(ob[sb[j]:sb[j + 1]])
+            starts.append(len(dims))
+    return np.array(starts, np.uint32), np.array(dims, np.uint32), np.array(orders, np.uint32)
+
+
+def concatenate(a, b):
+    """FixedMultiIndexSet::Concatenate (FixedMultiIndexSet.cpp:400-431)."""
+    sa, da, oa = a
+    sb, db, ob = b
+    starts = np.concatenate([np.asarray(sa[:-1], np.int64), len(da) + np.asarray(sb, np.int64)])
+    return (starts.astype(np.uint32), np.concatenate([da, db]).astype(np.uint32),
+            np.concatenate([oa, ob]).astype(np.uint32))
+
+
+def sigmoid_mset(input_dim, off_order, cross_order, num_sigmoids):
+    """Multi-index set of CreateSigmoidExpansionTemplate (src/MapFactory.cpp:284-318):
+    [leading total order x {0}] followed by [leading cross order x {1..n+3}];
+    for one input the total order n+3 set."""
+    if input_dim == 1:
+        return total_order(1, num_sigmoids + 3)
+    m1 = cartesian(total_order(input_dim - 1, off_order), input_dim - 1, total_order(1, 0))
+    m2 = cartesian(total_order(input_dim - 1, cross_order), input_dim - 1,
+                   total_order_min(1, num_sigmoids + 3, 1))
+    return concatenate(m1, m2)
+
+
+SUM_LINEAR, SUM_CONSTANT = 0, 1  # SigmoidSumSizeType
+
+
+def sigmoid_from_centers(centers, edge_shape=1.5, sum_type=SUM_LINEAR):
+    """CreateSigmoid (src/MapFactory.cpp:181-254): (centers, widths, weights, starts)."""
+    c = _f64(centers)
+    n = len(c)
+    oc, ow, owt = np.zeros(n), np.zeros(n), np.zeros(n)
+    st = np.zeros(max(n, 1), np.uint32)
+    ns = C.c_uint()
+    if lib().orc_sigmoid_from_centers(n, _ptr(c), edge_shape, sum_type, _ptr(oc), _ptr(ow), _ptr(owt),
+                                      st.ctypes.data_as(_up), C.byref(ns)) != 0:
+        raise ValueError("invalid sigmoid centers")
+    return oc, ow, owt, st[:ns.value].copy()
+
+
+def sigmoid_eval(params, x, max_order, which=2):
+    """Sigmoid1d EvaluateAll / EvaluateDerivatives / EvaluateSecondDerivatives
+    at x: (values, first, second derivatives), each max_order + 1 long."""
+    c, w, wt, st = (_f64(params[0]), _f64(params[1]), _f64(params[2]), np.ascontiguousarray(params[3], np.uint32))
+    v, d1, d2 = np.zeros(max_order + 1), np.zeros(max_order + 1), np.zeros(max_order + 1)
+    st1 = st if len(st) else np.zeros(1, np.uint32)
+    rc = lib().orc_sigmoid_eval(len(c), _ptr(c), _ptr(w), _ptr(wt), len(st), st1.ctypes.data_as(_up), which,
+                                max_order, float(x), _ptr(v), _ptr(d1), _ptr(d2))
+    if rc < 0:
+        raise ValueError("invalid sigmoid parameters or order")
+    return v, d1, d2
+
+
+class OracleSigmoidComponent:
+    """RectifiedMultivariateExpansion with HermiteFunctions in the leading
+    inputs, a Sigmoid1d in the last input and the positive bijector as
+    rectifier (MParT/RectifiedMultivariateExpansion.h), or, for one input,
+    UnivariateExpansion<Sigmoid1d> (MParT/UnivariateExpansion.h).  params =
+    (centers, widths, weights, starts); params None puts the leading basis
+    in the last input too (the reference's unrectified test case)."""
+
+    def __init__(self, dim, starts, dims, orders, params, posfunc=POS_SOFTPLUS, rectify=True,
+                 basis=BASIS_HERMITE_FUNCTIONS, normalize=True):
+        self.dim = int(dim)
+        self.starts = np.ascontiguousarray(starts, np.uint32)
+        self.dims = np.ascontiguousarray(dims, np.uint32)
+        self.orders = np.ascontiguousarray(orders, np.uint32)
+        self.num_terms = self.num_coeffs = len(self.starts) - 1
+        self.input_dim, self.output_dim = self.dim, 1
+        self.nugget = 0.0
+        self.univariate = self.dim == 1
+        d = self.dims if len(self.dims) else np.zeros(1, np.uint32)
+        o = self.orders if len(self.orders) else np.zeros(1, np.uint32)
+        if params is None:
+            c = w = wt = np.zeros(1)
+            st = np.zeros(1, np.uint32)
+            nc = ns = 0
+        else:
+            c, w, wt = _f64(params[0]), _f64(params[1]), _f64(params[2])
+            st = np.ascontiguousarray(params[3], np.uint32)
+            nc, ns = len(c), len(st)
+            if ns == 0:
+                st = np.zeros(1, np.uint32)
+        self._keep = (c, w, wt, st)
+        self._h = lib().orc_rect_new(self.dim, self.num_terms, self.starts.ctypes.data_as(_up),
+                                     d.ctypes.data_as(_up), o.ctypes.data_as(_up), basis, int(normalize),
+                                     posfunc if rectify else -1, nc, _ptr(c), _ptr(w), _ptr(wt), ns,
+                                     st.ctypes.data_as(_up), int(self.univariate))
+        if not self._h:
+            raise ValueError("invalid sigmoid expansion")
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_rect_free(self._h)
+            self._h = None
+
+    def _pts(self, pts):
+        pts = np.asarray(pts, dtype=np.float64)
+        assert pts.ndim == 2 and pts.shape[0] >= self.dim
+        rs, cs = (s // 8 for s in pts.strides)
+        return pts, pts.shape[1], rs, cs
+
+    def evaluate(self, coeffs, pts):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        out = np.zeros(N)
+        lib().orc_rect_evaluate(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out))
+        return out
+
+    def gradient(self, coeffs, pts, sens):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        sens = _f64(np.asarray(sens).reshape(-1))
+        out = np.zeros((self.dim, N))
+        lib().orc_rect_gradient(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(sens), _ptr(out), N, 1)
+        return out
+
+    def coeff_grad(self, coeffs, pts, sens):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        sens = _f64(np.asarray(sens).reshape(-1))
+        out = np.zeros((self.num_terms, N))
+        lib().orc_rect_coeff_grad(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(sens), _ptr(out))
+        return out
+
+    def logdet(self, coeffs, pts):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        out = np.zeros(N)
+        lib().orc_rect_logdet(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out))
+        return out
+
+    def cont_derivative(self, coeffs, pts):
+        with np.errstate(over="ignore"):
+            return np.exp(self.logdet(coeffs, pts))
+
+    def logdet_input_grad(self, coeffs, pts):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        out = np.zeros((self.dim, N))
+        lib().orc_rect_logdet_input_grad(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out), N, 1)
+        return out
+
+    def logdet_coeff_grad(self, coeffs, pts):
+        coeffs = _f64(coeffs)
+        pts, N, rs, cs = self._pts(pts)
+        out = np.zeros((self.num_terms, N))
+        lib().orc_rect_logdet_coeff_grad(self._h, _ptr(coeffs), _ptr(pts), N, rs, cs, _ptr(out))
+        return out
+
+    def inverse(self, coeffs, xs, ys, xtol=1e-6, ytol=1e-6, return_info=False):
+        """xs: D x (1 or N) with the initial guess in its last row; ys: N."""
+        coeffs = _f64(coeffs)
+        xs = np.asarray(xs, dtype=np.float64)
+        rs, cs = (s // 8 for s in xs.strides)
+        ys = _f64(np.asarray(ys).reshape(-1))
+        N = ys.shape[0]
+        out = np.zeros(N)
+        info = np.zeros(N, np.int32)
+        if lib().orc_rect_inverse(self._h, _ptr(coeffs), _ptr(xs), xs.shape[1], rs, cs, _ptr(ys), 1, N, xtol, ytol,
+                                  _ptr(out), 1, info.ctypes.data_as(_ip)) != 0:
+            raise ValueError("invalid argument sizes given to inverse")
+        return (out, info) if return_info else out
+
+
+def sigmoid_triangular(input_dim, output_dim, order, centers, edge_shape=1.5, sum_type=SUM_LINEAR,
+                       posfunc=POS_SOFTPLUS):
+    """CreateSigmoidTriangular (src/MapFactory.cpp:389-407): component i has
+    input dimension input_dim - output_dim + i + 1 and the centers of column i."""
+    comps = []
+    centers = np.asarray(centers, dtype=np.float64)
+    for i in range(output_dim):
+        d = input_dim - output_dim + i + 1
+        prm = sigmoid_from_centers(centers[:, i], edge_shape, sum_type)
+        nsig = len(prm[3])
+        s, dd, o = sigmoid_mset(d, order, order, nsig)
+        comps.append(OracleSigmoidComponent(d, s, dd, o, prm, posfunc))
+    return OracleTriangularMap(input_dim, output_dim, order, components=comps)
 
 
 class OracleComponent:
