@@ -58,6 +58,13 @@ typedef struct mpgb_map_options {
     int cont_deriv;
     int basis_norm;
     double nugget;
+    /* Sigmoid expansions (MParT/MapOptions.h:64-73): sigmoid_type 0 = Logistic,
+     * edge_type 0 = SoftPlus, edge_shape > 0, sigmoid_sum_type 0 = Linear,
+     * 1 = Constant (MParT/Sigmoid.h:45-48). */
+    int sigmoid_type;
+    int edge_type;
+    double edge_shape;
+    int sigmoid_sum_type;
 } mpgb_map_options;
 
 typedef struct mpgb_matrix {
@@ -96,6 +103,51 @@ int mpgb_create_triangular(unsigned int input_dim, unsigned int output_dim, unsi
  * map keeps references to the components; their handles stay valid. */
 int mpgb_create_triangular_from_components(mpgb_map* const* components, unsigned int n, int move_coeffs,
                                            mpgb_map** out);
+
+/* MapFactory::CreateSigmoidComponent (MParT/MapFactory.h:138-185, src/MapFactory.cpp:256-385):
+ * a RectifiedMultivariateExpansion (input_dim >= 2) or UnivariateExpansion
+ * (input_dim == 1) with the Sigmoid1d basis built from n_centers centers
+ * (CreateSigmoid, src/MapFactory.cpp:181-254) by opts->edge_shape and
+ * opts->sigmoid_sum_type.  The first form uses the factory's multi-index set
+ * (leading total order off_diag_order, leading cross order cross_order); the
+ * second takes the set. */
+int mpgb_create_sigmoid_component(unsigned int input_dim, unsigned int off_diag_order, unsigned int cross_order,
+                                  const double* centers, unsigned int n_centers, const mpgb_map_options* opts,
+                                  mpgb_map** out);
+int mpgb_create_sigmoid_component_mset(unsigned int dim, unsigned int num_terms, const unsigned int* nz_starts,
+                                       const unsigned int* nz_dims, const unsigned int* nz_orders,
+                                       const double* centers, unsigned int n_centers,
+                                       const mpgb_map_options* opts, mpgb_map** out);
+/* MapFactory::CreateSigmoidTriangular (MParT/MapFactory.h:186-213,
+ * src/MapFactory.cpp:389-407): centers is n_centers x output_dim (strides in
+ * doubles); column i gives the centers of component i. */
+int mpgb_create_sigmoid_triangular(unsigned int input_dim, unsigned int output_dim, unsigned int total_order,
+                                   const double* centers, unsigned int n_centers, int64_t row_stride,
+                                   int64_t col_stride, const mpgb_map_options* opts, mpgb_map** out);
+/* ConditionalMapBase::CoeffBounds (src/ConditionalMapBase.cpp:297-312): host
+ * arrays of num_coeffs. */
+int mpgb_map_coeff_bounds(const mpgb_map* map, double* lb, double* ub);
+/* Kind of a single component: 0 MonotoneComponent, 1 rectified sigmoid
+ * expansion, 2 univariate sigmoid expansion; -1 for a TriangularMap. */
+int mpgb_map_kind(const mpgb_map* map, int* kind);
+/* The Sigmoid1d parameters of a sigmoid component (host arrays of n_centers
+ * and n_starts; *n_centers / *n_starts receive the sizes; arrays may be NULL
+ * to query them). */
+int mpgb_component_sigmoid(const mpgb_map* component, double* centers, double* widths, double* weights,
+                           unsigned int* n_centers, unsigned int* starts, unsigned int* n_starts);
+/* CreateSigmoid's parameters for a vector of centers (src/MapFactory.cpp:181-254):
+ * host arrays of n (starts: room for n); *n_starts receives the start count. */
+int mpgb_sigmoid_params(const double* centers, unsigned int n, double edge_shape, int sum_type,
+                        double* out_centers, double* widths, double* weights, unsigned int* starts,
+                        unsigned int* n_starts);
+/* Sigmoid1d::EvaluateAll / EvaluateDerivatives / EvaluateSecondDerivatives
+ * (MParT/Sigmoid.h:214-366) on the device: x (device, n_x values, stride
+ * x_stride), outputs (device, (max_order+1) x n_x, row stride n_x; d1, d2 may
+ * be NULL).  which = 0, 1, 2 selects the derivative order. */
+int mpgb_sigmoid1d_evaluate(const double* centers, const double* widths, const double* weights, unsigned int n,
+                            const unsigned int* starts, unsigned int n_starts, int which, unsigned int max_order,
+                            const double* x, int64_t n_x, int64_t x_stride, double* out, double* d1, double* d2,
+                            void* stream);
 
 /* Releases a handle (components held by a triangular map stay alive until it is destroyed). */
 int mpgb_map_destroy(mpgb_map* map);

@@ -19,6 +19,10 @@ namespace mpgb {
 enum class BasisTypes { ProbabilistHermite, PhysicistHermite, HermiteFunctions };
 enum class PosFuncTypes { Exp, SoftPlus };
 enum class QuadTypes { ClenshawCurtis, AdaptiveSimpson, AdaptiveClenshawCurtis };
+// MParT/MapOptions.h:31-39 and MParT/Sigmoid.h:45-48.
+enum class SigmoidTypes { Logistic };
+enum class EdgeTypes { SoftPlus };
+enum class SigmoidSumSizeType { Linear, Constant };
 
 // MParT/MapOptions.h:58-123 (the fields this path reads; same defaults).
 struct MapOptions {
@@ -33,6 +37,11 @@ struct MapOptions {
     bool contDeriv = true;
     bool basisNorm = true;
     double nugget = 0.0;
+    // Sigmoid expansions (MParT/MapOptions.h:64-73).
+    SigmoidTypes sigmoidType = SigmoidTypes::Logistic;
+    EdgeTypes edgeType = EdgeTypes::SoftPlus;
+    double edgeShape = 1.5;
+    SigmoidSumSizeType sigmoidBasisSumType = SigmoidSumSizeType::Linear;
 };
 
 // A strided 2-D array (the reference's StridedMatrix = View<T**, LayoutStride>,
@@ -64,6 +73,11 @@ public:
     std::vector<unsigned int> IndexToMulti(unsigned int index) const;
     int MultiToIndex(std::vector<unsigned int> const& multi) const;
     std::vector<unsigned int> NonzeroDiagonalEntries() const;
+    // Terms (i, j) with i of this set outermost, the other set's dimensions
+    // after this set's (src/MultiIndices/FixedMultiIndexSet.cpp:356-397).
+    FixedMultiIndexSet Cartesian(FixedMultiIndexSet const& other) const;
+    // This set's terms followed by the other's (FixedMultiIndexSet.cpp:400-431).
+    FixedMultiIndexSet Concatenate(FixedMultiIndexSet const& other) const;
 
     std::vector<unsigned int> nzStarts, nzDims, nzOrders, maxDegrees;
 
@@ -125,6 +139,29 @@ public:
                                              cudaStream_t stream = 0) = 0;
     virtual void LogDeterminantInputGradImpl(StridedMatrix const& pts, StridedMatrix const& output,
                                              cudaStream_t stream = 0) = 0;
+    // Bounds on the coefficients (host arrays of numCoeffs): -inf / +inf
+    // unless a subclass restricts them (ConditionalMapBase::CoeffBounds,
+    // src/ConditionalMapBase.cpp:297-312).
+    virtual void FillCoeffBoundsImpl(double* lb, double* ub) const;
+};
+
+// Parameters of a Sigmoid1d basis (MParT/Sigmoid.h:87-446): centers, widths
+// and weights of the two edge terms and the sigmoids, and the first index of
+// each sigmoid term (startInds, CSR style).
+struct Sigmoid1dParams {
+    std::vector<double> centers, widths, weights;
+    std::vector<unsigned int> startInds;
+    // Highest basis order: affine part, two edge terms, one per sigmoid term.
+    int Order() const { return (int)startInds.size() + 3; }
+    // Throws std::invalid_argument when the arrays do not form a basis (Sigmoid.h:386-431).
+    void Validate() const;
+    // ConstructStartInds (Sigmoid.h:95-130).
+    static std::vector<unsigned int> ConstructStartInds(unsigned int numCenters, SigmoidSumSizeType sumType);
+    static int ComputeNumSigmoids(unsigned int numCenters, SigmoidSumSizeType sumType);
+    // CreateSigmoid (src/MapFactory.cpp:181-254): widths and weights from the
+    // centers by the factory's rule of thumb.
+    static Sigmoid1dParams FromCenters(std::vector<double> const& centers, double edgeShape,
+                                       SigmoidSumSizeType sumType);
 };
 
 // Inverse solver options (MonotoneComponent.h:353-396).
@@ -223,6 +260,32 @@ private:
     FixedMultiIndexSet mset_;
 };
 
+// Sigmoid expansions, constructed through MapFactory::CreateSigmoidComponent:
+// MParT/RectifiedMultivariateExpansion.h for two or more inputs (Hermite
+// functions in the leading inputs, the Sigmoid1d basis in the last one, the
+// positive bijector as rectifier of the leading product of every term with a
+// last-input factor) and MParT/UnivariateExpansion.h for one input.  The
+// expansion is monotone in the last input when the coefficients of those
+// terms are non-negative (the lower bounds of CoeffBounds).  Same engine as
+// the monotone components, without quadrature.
+class SigmoidComponent : public MonotoneMapBase {
+public:
+    SigmoidComponent(FixedMultiIndexSet const& mset, Sigmoid1dParams const& sigmoid, MapOptions const& opts);
+    FixedMultiIndexSet const& GetMultiIndexSet() const { return mset_; }
+    Sigmoid1dParams const& GetSigmoid() const { return sig_; }
+    bool IsUnivariate() const { return mset_.Length() == 1; }
+    // Terms that depend on the last input (all terms for one input).
+    std::vector<unsigned int> DiagonalCoeffIndices() const;
+    // 0 for DiagonalCoeffIndices (except the constant of a univariate
+    // expansion), -inf elsewhere; +inf above (RectifiedMultivariateExpansion.h:374-390,
+    // UnivariateExpansion.h:28-35).
+    void FillCoeffBoundsImpl(double* lb, double* ub) const override;
+
+private:
+    FixedMultiIndexSet mset_;
+    Sigmoid1dParams sig_;
+};
+
 // MParT/TriangularMap.h
 class TriangularMap : public MonotoneMapBase {
 public:
@@ -231,6 +294,7 @@ public:
     void WrapCoeffs(double* deviceCoeffs, unsigned int n) override;
     std::shared_ptr<ConditionalMapBase> GetComponent(unsigned int i) { return comps_.at(i); }
     unsigned int NumComponents() const { return (unsigned int)comps_.size(); }
+    void FillCoeffBoundsImpl(double* lb, double* ub) const override;  // src/TriangularMap.cpp:313-325
 
 private:
     std::vector<std::shared_ptr<ConditionalMapBase>> comps_;
@@ -241,6 +305,18 @@ namespace MapFactory {
 std::shared_ptr<ConditionalMapBase> CreateComponent(FixedMultiIndexSet const& mset, MapOptions opts);
 std::shared_ptr<ConditionalMapBase> CreateTriangular(unsigned int inputDim, unsigned int outputDim,
                                                      unsigned int totalOrder, MapOptions options = MapOptions());
+// MParT/MapFactory.h:138-213 and src/MapFactory.cpp:256-407.
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(unsigned int inputDim, unsigned int offDiagOrder,
+                                                           unsigned int crossOrder, std::vector<double> const& centers,
+                                                           MapOptions opts);
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(unsigned int inputDim, unsigned int totalOrder,
+                                                           std::vector<double> const& centers, MapOptions opts);
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(FixedMultiIndexSet const& mset,
+                                                           std::vector<double> const& centers, MapOptions opts);
+std::shared_ptr<ConditionalMapBase> CreateSigmoidTriangular(unsigned int inputDim, unsigned int outputDim,
+                                                            unsigned int totalOrder,
+                                                            std::vector<std::vector<double>> const& centers,
+                                                            MapOptions opts);
 }  // namespace MapFactory
 
 // Thrown when the rectified integrand overflows (the reference throws from

@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+import math
 from typing import Sequence
 
 import numpy as np
@@ -21,7 +22,8 @@ __all__ = [
     "BasisTypes", "PosFuncTypes", "QuadTypes", "MapOptions", "FixedMultiIndexSet", "ConditionalMapBase",
     "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load", "DeserializeMap",
     "FromBytes", "MapBatch", "TrainMap", "TrainOptions", "KLObjective", "CreateGaussianKLObjective", "MultiIndexSet",
-    "ATMOptions", "TrainMapAdaptive",
+    "ATMOptions", "TrainMapAdaptive", "SigmoidTypes", "EdgeTypes", "SigmoidSumSizeType", "SigmoidComponent",
+    "CreateSigmoidComponent", "CreateSigmoidTriangular", "Sigmoid1d",
 ]
 
 
@@ -42,6 +44,20 @@ class QuadTypes(enum.IntEnum):
     AdaptiveClenshawCurtis = 2
 
 
+class SigmoidTypes(enum.IntEnum):
+    Logistic = 0
+
+
+class EdgeTypes(enum.IntEnum):
+    SoftPlus = 0
+
+
+class SigmoidSumSizeType(enum.IntEnum):
+    """MParT/Sigmoid.h:45-48: term k of a Linear sum has k - 3 sigmoids, of a Constant sum one."""
+    Linear = 0
+    Constant = 1
+
+
 class MapOptions:
     """MParT/MapOptions.h:58-123 (same field names and defaults)."""
 
@@ -57,6 +73,10 @@ class MapOptions:
         self.contDeriv = True
         self.basisNorm = True
         self.nugget = 0.0
+        self.sigmoidType = SigmoidTypes.Logistic
+        self.edgeType = EdgeTypes.SoftPlus
+        self.edgeShape = 1.5
+        self.sigmoidBasisSumType = SigmoidSumSizeType.Linear
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(f"MapOptions has no field {k}")
@@ -66,14 +86,17 @@ class MapOptions:
         return mpgb_map_options(int(self.basisType), int(self.posFuncType), int(self.quadType),
                                 float(self.quadAbsTol), float(self.quadRelTol), int(self.quadMaxSub),
                                 int(self.quadMinSub), int(self.quadPts), int(bool(self.contDeriv)),
-                                int(bool(self.basisNorm)), float(self.nugget))
+                                int(bool(self.basisNorm)), float(self.nugget), int(self.sigmoidType),
+                                int(self.edgeType), float(self.edgeShape), int(self.sigmoidBasisSumType))
 
     @classmethod
     def _from_c(cls, o: mpgb_map_options) -> "MapOptions":
         return cls(basisType=BasisTypes(o.basis_type), posFuncType=PosFuncTypes(o.pos_func_type),
                    quadType=QuadTypes(o.quad_type), quadAbsTol=o.quad_abs_tol, quadRelTol=o.quad_rel_tol,
                    quadMaxSub=o.quad_max_sub, quadMinSub=o.quad_min_sub, quadPts=o.quad_pts,
-                   contDeriv=bool(o.cont_deriv), basisNorm=bool(o.basis_norm), nugget=o.nugget)
+                   contDeriv=bool(o.cont_deriv), basisNorm=bool(o.basis_norm), nugget=o.nugget,
+                   sigmoidType=SigmoidTypes(o.sigmoid_type), edgeType=EdgeTypes(o.edge_type),
+                   edgeShape=o.edge_shape, sigmoidBasisSumType=SigmoidSumSizeType(o.sigmoid_sum_type))
 
     def ToBytes(self) -> bytes:
         """The reference's cereal archive of MapOptions (MParT/MapOptions.h:126-130)."""
@@ -102,7 +125,12 @@ class MapOptions:
         return isinstance(other, MapOptions) and self.__dict__ == other.__dict__
 
     def __reduce__(self):
-        return (MapOptions.FromBytes, (self.ToBytes(),))
+        # (The cereal archive has no sigmoid fields: pickle every field.)
+        return (_options_from_fields, (dict(self.__dict__),))
+
+
+def _options_from_fields(fields):
+    return MapOptions(**fields)
 
 
 class FixedMultiIndexSet:
@@ -222,10 +250,12 @@ def DeserializeMap(filename):
     return i.value, o.value, coeffs
 
 
-def _wrap_map(h):
-    t = C.c_int()
-    check(load().mpgb_map_is_triangular(h, C.byref(t)))
-    return TriangularMap(_handle=h) if t.value else ConditionalMapBase(h)
+def _wrap_map(h, keep=()):
+    k = C.c_int()
+    check(load().mpgb_map_kind(h, C.byref(k)))
+    if k.value < 0:
+        return TriangularMap(_handle=h)
+    return SigmoidComponent(h, keep) if k.value > 0 else ConditionalMapBase(h, keep)
 
 
 def FromBytes(data: bytes):
@@ -459,6 +489,14 @@ class ConditionalMapBase:
     def __reduce__(self):
         return (FromBytes, (self.ToBytes(),))
 
+    def CoeffBounds(self):
+        """ConditionalMapBase::CoeffBounds (src/ConditionalMapBase.cpp:297-312): (lb, ub)."""
+        n = self.numCoeffs
+        lb, ub = np.zeros(n), np.zeros(n)
+        D = C.POINTER(C.c_double)
+        check(load().mpgb_map_coeff_bounds(self._h, lb.ctypes.data_as(D), ub.ctypes.data_as(D)))
+        return lb, ub
+
     def torch(self, store_coeffs=True, return_logdet=False):
         from .torch import TorchConditionalMapBase
         return TorchConditionalMapBase(self, store_coeffs=store_coeffs, return_logdet=return_logdet)
@@ -485,7 +523,7 @@ class TriangularMap(ConditionalMapBase):
     def GetComponent(self, i):
         h = C.c_void_p()
         check(load().mpgb_map_get_component(self._h, int(i), C.byref(h)))
-        return ConditionalMapBase(h, keep=[self])
+        return _wrap_map(h, keep=[self])
 
 
 def CreateComponent(mset: FixedMultiIndexSet, opts: MapOptions | None = None) -> ConditionalMapBase:
@@ -509,6 +547,168 @@ def CreateTriangular(inputDim: int, outputDim: int, totalOrder: int, opts: MapOp
     h = C.c_void_p()
     check(load().mpgb_create_triangular(int(inputDim), int(outputDim), int(totalOrder), C.byref(o), C.byref(h)))
     return TriangularMap(_handle=h)
+
+
+class SigmoidComponent(ConditionalMapBase):
+    """A sigmoid expansion (RectifiedMultivariateExpansion for two or more
+    inputs, UnivariateExpansion<Sigmoid1d> for one), built by
+    CreateSigmoidComponent / CreateSigmoidTriangular."""
+
+    def GetSigmoid(self):
+        """(centers, widths, weights, startInds) of the last input's Sigmoid1d basis."""
+        n, ns = C.c_uint(), C.c_uint()
+        check(load().mpgb_component_sigmoid(self._h, None, None, None, C.byref(n), None, C.byref(ns)))
+        c, w, wt = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        st = np.zeros(max(1, ns.value), np.uint32)
+        D = C.POINTER(C.c_double)
+        check(load().mpgb_component_sigmoid(self._h, c.ctypes.data_as(D), w.ctypes.data_as(D), wt.ctypes.data_as(D),
+                                            None, st.ctypes.data_as(C.POINTER(C.c_uint)), None))
+        return c, w, wt, st[:ns.value]
+
+    def Sigmoid(self):
+        return Sigmoid1d(*self.GetSigmoid())
+
+
+def _centers(c):
+    if _is_torch(c):
+        c = c.detach().cpu().numpy()
+    return np.ascontiguousarray(np.asarray(c, dtype=np.float64).reshape(-1))
+
+
+def CreateSigmoidComponent(*args) -> SigmoidComponent:
+    """MapFactory::CreateSigmoidComponent (MParT/MapFactory.h:138-185,
+    bindings/python/src/MapFactory.cpp:26-29):
+    (inputDim, totalOrder, centers, opts), (inputDim, offDiagOrder, crossOrder,
+    centers, opts) or (mset, centers, opts)."""
+    D = C.POINTER(C.c_double)
+    h = C.c_void_p()
+    if isinstance(args[0], FixedMultiIndexSet):
+        mset, centers = args[0], _centers(args[1])
+        opts = args[2] if len(args) > 2 and args[2] is not None else MapOptions()
+        o = opts._c()
+        up = C.POINTER(C.c_uint)
+        d = mset.nzDims if mset.nzDims.size else np.zeros(1, np.uint32)
+        r = mset.nzOrders if mset.nzOrders.size else np.zeros(1, np.uint32)
+        check(load().mpgb_create_sigmoid_component_mset(mset.dim, mset.Size(), mset.nzStarts.ctypes.data_as(up),
+                                                        d.ctypes.data_as(up), r.ctypes.data_as(up),
+                                                        centers.ctypes.data_as(D), len(centers), C.byref(o),
+                                                        C.byref(h)))
+        return SigmoidComponent(h)
+    if len(args) in (3, 4) and not np.isscalar(args[2]):
+        inputDim, off, centers = int(args[0]), int(args[1]), _centers(args[2])
+        cross = off
+        opts = args[3] if len(args) > 3 and args[3] is not None else MapOptions()
+    elif len(args) in (4, 5):
+        inputDim, off, cross, centers = int(args[0]), int(args[1]), int(args[2]), _centers(args[3])
+        opts = args[4] if len(args) > 4 and args[4] is not None else MapOptions()
+    else:
+        raise TypeError("CreateSigmoidComponent: unsupported arguments")
+    o = opts._c()
+    check(load().mpgb_create_sigmoid_component(inputDim, off, cross, centers.ctypes.data_as(D), len(centers),
+                                               C.byref(o), C.byref(h)))
+    return SigmoidComponent(h)
+
+
+def CreateSigmoidTriangular(inputDim: int, outputDim: int, totalOrder: int, centers,
+                            opts: MapOptions | None = None) -> TriangularMap:
+    """MapFactory::CreateSigmoidTriangular (MParT/MapFactory.h:186-213): centers
+    is (number of centers) x outputDim, column i for component i."""
+    opts = opts or MapOptions()
+    c = np.asarray(centers.detach().cpu().numpy() if _is_torch(centers) else centers, dtype=np.float64)
+    if c.ndim == 1:
+        c = c[:, None]
+    o = opts._c()
+    h = C.c_void_p()
+    check(load().mpgb_create_sigmoid_triangular(int(inputDim), int(outputDim), int(totalOrder),
+                                                c.ctypes.data_as(C.POINTER(C.c_double)), c.shape[0],
+                                                c.strides[0] // 8, c.strides[1] // 8, C.byref(o), C.byref(h)))
+    return TriangularMap(_handle=h)
+
+
+class Sigmoid1d:
+    """Sigmoid1d with the Logistic sigmoid and SoftPlus edges (MParT/Sigmoid.h;
+    bindings/python/src/Sigmoid.cpp).  Evaluations run on the GPU."""
+
+    def __init__(self, centers, widths, weights, startInds=None, sumType=SigmoidSumSizeType.Linear):
+        self.centers = _centers(centers)
+        self.widths = _centers(widths)
+        self.weights = _centers(weights)
+        if startInds is None:
+            startInds = _sigmoid_starts(len(self.centers), sumType)
+        self.startInds = np.ascontiguousarray(startInds, dtype=np.uint32)
+
+    @classmethod
+    def FromCenters(cls, centers, edgeShape=1.5, sumType=SigmoidSumSizeType.Linear):
+        """CreateSigmoid (src/MapFactory.cpp:181-254)."""
+        c = _centers(centers)
+        n = len(c)
+        oc, w, wt = np.zeros(n), np.zeros(n), np.zeros(n)
+        st = np.zeros(max(1, n), np.uint32)
+        ns = C.c_uint()
+        D = C.POINTER(C.c_double)
+        check(load().mpgb_sigmoid_params(c.ctypes.data_as(D), n, float(edgeShape), int(sumType),
+                                         oc.ctypes.data_as(D), w.ctypes.data_as(D), wt.ctypes.data_as(D),
+                                         st.ctypes.data_as(C.POINTER(C.c_uint)), C.byref(ns)))
+        return cls(oc, w, wt, st[:ns.value])
+
+    def GetOrder(self):
+        return len(self.startInds) + 3
+
+    def Evaluate(self, x, maxOrder=None, which=0):
+        """Basis values (and derivatives up to `which`) at the points x (a 1-D
+        array, evaluated on the GPU): tensors of shape (maxOrder + 1, len(x))."""
+        import torch
+        maxOrder = self.GetOrder() if maxOrder is None else int(maxOrder)
+        xt = torch.as_tensor(np.asarray(x, dtype=np.float64).reshape(-1) if not _is_torch(x) else x,
+                             dtype=torch.float64, device="cuda").reshape(-1).contiguous()
+        n = xt.shape[0]
+        outs = [torch.zeros((maxOrder + 1, n), dtype=torch.float64, device="cuda") for _ in range(which + 1)]
+        D = C.POINTER(C.c_double)
+        st = self.startInds if self.startInds.size else np.zeros(1, np.uint32)
+        check(load().mpgb_sigmoid1d_evaluate(
+            self.centers.ctypes.data_as(D), self.widths.ctypes.data_as(D), self.weights.ctypes.data_as(D),
+            len(self.centers), st.ctypes.data_as(C.POINTER(C.c_uint)), len(self.startInds), int(which), maxOrder,
+            C.c_void_p(xt.data_ptr()), n, 1, C.c_void_p(outs[0].data_ptr()),
+            C.c_void_p(outs[1].data_ptr()) if which >= 1 else None,
+            C.c_void_p(outs[2].data_ptr()) if which >= 2 else None,
+            C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        return outs
+
+    # In-place forms of the reference binding: output has maxOrder + 1 entries.
+    def EvaluateAll(self, output, x):
+        v, = self.Evaluate([x], len(output) - 1, 0)
+        output[:] = v[:, 0].cpu().numpy()
+
+    def EvaluateDerivatives(self, output, derivs, x):
+        if len(output) != len(derivs):
+            raise ValueError("Vector dimensions do not match.")
+        v, d = self.Evaluate([x], len(output) - 1, 1)
+        output[:] = v[:, 0].cpu().numpy()
+        derivs[:] = d[:, 0].cpu().numpy()
+
+    def EvaluateSecondDerivatives(self, output, derivs, derivs2, x):
+        if len(output) != len(derivs) or len(derivs) != len(derivs2):
+            raise ValueError("Vector dimensions do not match.")
+        v, d, d2 = self.Evaluate([x], len(output) - 1, 2)
+        output[:] = v[:, 0].cpu().numpy()
+        derivs[:] = d[:, 0].cpu().numpy()
+        derivs2[:] = d2[:, 0].cpu().numpy()
+
+
+def _sigmoid_starts(n, sumType):
+    """Sigmoid1d::ConstructStartInds (MParT/Sigmoid.h:95-130)."""
+    if n <= 2:
+        return []
+    if int(sumType) == int(SigmoidSumSizeType.Constant):
+        return [2 + i for i in range(n - 2)]
+    k = int((math.sqrt(1 + 8 * (n - 2)) - 1) / 2)
+    if n - 2 != k * (k + 1) // 2:
+        raise ValueError("Sigmoid: Could not construct starting indices.  The size of the centers array cannot be "
+                         "used with the Linear sum type.")
+    out = [2]
+    for i in range(1, k):
+        out.append(out[-1] + i)
+    return out
 
 
 class TrainOptions:

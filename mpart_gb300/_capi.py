@@ -29,6 +29,10 @@ class mpgb_map_options(C.Structure):
         ("cont_deriv", C.c_int),
         ("basis_norm", C.c_int),
         ("nugget", C.c_double),
+        ("sigmoid_type", C.c_int),
+        ("edge_type", C.c_int),
+        ("edge_shape", C.c_double),
+        ("sigmoid_sum_type", C.c_int),
     ]
 
 
@@ -67,6 +71,7 @@ class mpgb_atm_result(C.Structure):
 _MAP = C.c_void_p
 _MAPP = C.POINTER(C.c_void_p)
 _UP = C.POINTER(C.c_uint)
+_DP = C.POINTER(C.c_double)
 SIGNATURES = {
     "mpgb_version": (C.c_char_p, []),
     "mpgb_last_error": (C.c_char_p, []),
@@ -75,6 +80,18 @@ SIGNATURES = {
     "mpgb_create_component_total_order": (C.c_int, [C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
     "mpgb_create_triangular": (C.c_int, [C.c_uint, C.c_uint, C.c_uint, C.POINTER(mpgb_map_options), _MAPP]),
     "mpgb_create_triangular_from_components": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint, C.c_int, _MAPP]),
+    "mpgb_create_sigmoid_component": (C.c_int, [C.c_uint, C.c_uint, C.c_uint, _DP, C.c_uint,
+                                                C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_create_sigmoid_component_mset": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, _DP, C.c_uint,
+                                                     C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_create_sigmoid_triangular": (C.c_int, [C.c_uint, C.c_uint, C.c_uint, _DP, C.c_uint, C.c_int64,
+                                                 C.c_int64, C.POINTER(mpgb_map_options), _MAPP]),
+    "mpgb_map_coeff_bounds": (C.c_int, [_MAP, _DP, _DP]),
+    "mpgb_map_kind": (C.c_int, [_MAP, C.POINTER(C.c_int)]),
+    "mpgb_component_sigmoid": (C.c_int, [_MAP, _DP, _DP, _DP, _UP, _UP, _UP]),
+    "mpgb_sigmoid_params": (C.c_int, [_DP, C.c_uint, C.c_double, C.c_int, _DP, _DP, _DP, _UP, _UP]),
+    "mpgb_sigmoid1d_evaluate": (C.c_int, [_DP, _DP, _DP, C.c_uint, _UP, C.c_uint, C.c_int, C.c_uint, C.c_void_p,
+                                          C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mpgb_map_destroy": (C.c_int, [_MAP]),
     "mpgb_map_dims": (C.c_int, [_MAP, _UP, _UP, _UP]),
     "mpgb_map_num_components": (C.c_int, [_MAP, _UP]),

@@ -229,6 +229,9 @@ public:
         for (auto& m : maps) {
             auto* mm = dynamic_cast<MonotoneMapBase*>(m.get());
             if (!mm) throw std::invalid_argument("MapBatch: maps must be monotone components or triangular maps.");
+            for (auto& pt : mm->Parts())
+                if (pt.prog->kind != 0)
+                    throw std::invalid_argument("MapBatch: sigmoid expansions are not provided for batches.");
             maps_.push_back(mm);
         }
         const MapOptions& a = maps_[0]->Options();

@@ -18,6 +18,10 @@ namespace mpgb {
 
 constexpr int kBasisProbHermite = 0;
 constexpr int kBasisHermiteFunctions = 2;
+// Sigmoid expansion (RectifiedMultivariateExpansion / UnivariateExpansion):
+// Hermite functions in the leading inputs, a Sigmoid1d basis in the last one,
+// no quadrature.
+constexpr int kBasisSigmoid = 3;
 constexpr int kPosExp = 0;
 constexpr int kPosSoftPlus = 1;
 
@@ -161,6 +165,12 @@ __device__ __forceinline__ double posDeriv(double x) {
     double g, gp;
     posEval<POS>(x, g, gp);
     return gp;
+}
+
+template <int POS>
+__device__ __forceinline__ double posValue(double x) {
+    if constexpr (POS == kPosExp) return exp(x);
+    else return log(1.0 + exp(-fabs(x))) + fmax(x, 0.0);
 }
 
 // --------------------------------------------------------------------------

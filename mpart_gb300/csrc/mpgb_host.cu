@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -113,6 +114,142 @@ std::vector<unsigned int> FixedMultiIndexSet::NonzeroDiagonalEntries() const {
     return out;
 }
 
+FixedMultiIndexSet FixedMultiIndexSet::Cartesian(FixedMultiIndexSet const& other) const {
+    std::vector<unsigned> st{0}, dm, od;
+    for (unsigned i = 0; i < Size(); ++i) {
+        for (unsigned j = 0; j < other.Size(); ++j) {
+            for (unsigned k = nzStarts[i]; k < nzStarts[i + 1]; ++k) {
+                dm.push_back(nzDims[k]);
+                od.push_back(nzOrders[k]);
+            }
+            for (unsigned k = other.nzStarts[j]; k < other.nzStarts[j + 1]; ++k) {
+                dm.push_back(dim_ + other.nzDims[k]);
+                od.push_back(other.nzOrders[k]);
+            }
+            st.push_back((unsigned)dm.size());
+        }
+    }
+    return FixedMultiIndexSet(dim_ + other.Length(), st, dm, od);
+}
+
+FixedMultiIndexSet FixedMultiIndexSet::Concatenate(FixedMultiIndexSet const& other) const {
+    if (Length() != other.Length()) {
+        std::ostringstream os;
+        os << "Length of multiindices must be the same but first set has length " << Length()
+           << " multis and second set has length " << other.Length() << " multis.";
+        throw std::invalid_argument(os.str());
+    }
+    std::vector<unsigned> st(nzStarts.begin(), nzStarts.end() - 1), dm = nzDims, od = nzOrders;
+    for (unsigned v : other.nzStarts) st.push_back((unsigned)nzDims.size() + v);
+    dm.insert(dm.end(), other.nzDims.begin(), other.nzDims.end());
+    od.insert(od.end(), other.nzOrders.begin(), other.nzOrders.end());
+    return FixedMultiIndexSet(dim_, st, dm, od);
+}
+
+// ---------------------------------------------------------------------------
+// Sigmoid1d parameters
+// ---------------------------------------------------------------------------
+int Sigmoid1dParams::ComputeNumSigmoids(unsigned int numCenters, SigmoidSumSizeType sumType) {
+    if (sumType == SigmoidSumSizeType::Constant) return (int)numCenters - 2;
+    if (numCenters < 2) return -1;
+    return (int)((std::sqrt(1.0 + 8.0 * ((double)numCenters - 2.0)) - 1.0) / 2.0);
+}
+
+std::vector<unsigned int> Sigmoid1dParams::ConstructStartInds(unsigned int centerSize, SigmoidSumSizeType sumType) {
+    std::vector<unsigned int> out;
+    if (centerSize <= 2) return out;
+    int numTerms = ComputeNumSigmoids(centerSize, sumType);
+    if (sumType == SigmoidSumSizeType::Linear) {
+        if ((int)(centerSize - 2) != numTerms * (numTerms + 1) / 2)
+            throw std::invalid_argument(
+                "Sigmoid: Could not construct starting indices.  The size of the centers array cannot be used with "
+                "the Linear sum type.");
+        out.resize(numTerms);
+        out[0] = 2;
+        for (int i = 1; i < numTerms; ++i) out[i] = out[i - 1] + i;
+    } else {
+        numTerms = (int)centerSize - 2;
+        out.resize(numTerms);
+        out[0] = 2;
+        for (int i = 1; i < numTerms; ++i) out[i] = out[i - 1] + 1;
+    }
+    return out;
+}
+
+void Sigmoid1dParams::Validate() const {
+    if (centers.size() != widths.size() || centers.size() != weights.size() || centers.size() < startInds.size()) {
+        std::ostringstream os;
+        os << "Sigmoid: incompatible dims of centers and widths.\ncenters: " << centers.size()
+           << ", \nwidths: " << widths.size() << ",\nweights: " << weights.size() << "\n";
+        throw std::invalid_argument(os.str());
+    }
+    if (centers.size() < 2)
+        throw std::invalid_argument(
+            "Sigmoid: centers/widths/weights too short.\nLength should be of form 2+(1+2+3+...+n) for some order n>=0");
+    if (!startInds.empty()) {
+        if (startInds[0] != 2) {
+            std::ostringstream os;
+            os << "Sigmoid: First term must start at index 2, but has startInds(0)=" << startInds[0];
+            throw std::invalid_argument(os.str());
+        }
+        for (size_t i = 1; i < startInds.size(); ++i) {
+            if (startInds[i] <= startInds[i - 1])
+                throw std::invalid_argument("Sigmoid: Starting indices must be strictly increasing.");
+            if (startInds[i] >= centers.size()) {
+                std::ostringstream os;
+                os << "Sigmoid: All starting indices must be smaller than the number of sigmoid centers but startInds("
+                   << i << ")=" << startInds[i] << " and centers.extent(0)=" << centers.size() << ".";
+                throw std::invalid_argument(os.str());
+            }
+        }
+    }
+    if (Order() > kMaxLastOrder) {
+        std::ostringstream os;
+        os << "Sigmoid: " << startInds.size() << " sigmoid terms give order " << Order()
+           << ", above the supported maximum " << kMaxLastOrder << ".";
+        throw std::invalid_argument(os.str());
+    }
+}
+
+Sigmoid1dParams Sigmoid1dParams::FromCenters(std::vector<double> const& c, double edgeShape,
+                                             SigmoidSumSizeType sumType) {
+    const unsigned n = (unsigned)c.size();
+    if (n < 2)
+        throw std::invalid_argument(
+            "Sigmoid: centers/widths/weights too short.\nLength should be of form 2+(1+2+3+...+n) for some order n>=0");
+    const int numSig = ComputeNumSigmoids(n, sumType);
+    Sigmoid1dParams S;
+    S.centers = c;
+    S.widths.assign(n, 0.0);
+    S.weights.assign(n, 1.0);
+    S.widths[0] = edgeShape;
+    S.weights[0] = 1.0 / edgeShape;
+    S.widths[1] = edgeShape;
+    S.weights[1] = 1.0 / edgeShape;
+    if (sumType == SigmoidSumSizeType::Linear) {
+        // Term i has i + 1 sigmoids; the first i get widths from the spacing of
+        // their neighbours (the edge centers at the ends), the last keeps 0.
+        for (int i = 0; i < numSig; i++) {
+            const int start = 2 + (i * (i + 1)) / 2;
+            for (int j = 0; j < i; j++) {
+                const double prev = (j == 0 || i == 0) ? c[0] : c[start + j - 1];
+                const double next = (j == i - 1 || i == 0) ? c[1] : c[start + j];
+                S.widths[start + j] = 2 / (next - prev);
+                S.weights[start + j] = 1.;
+            }
+        }
+    } else if (numSig > 0) {
+        std::sort(S.centers.begin() + 2, S.centers.end());
+        const std::vector<double>& h = S.centers;
+        S.widths[2] = (numSig > 1) ? 4.0 / (h[3] - h[2]) : 8.0 / std::abs(h[1] - h[0]);
+        for (int i = 1; i < numSig - 1; i++) S.widths[2 + i] = 8.0 / (h[3 + i] - h[1 + i]);
+        if (numSig > 1) S.widths[2 + numSig - 1] = 4.0 / (h[2 + numSig - 1] - h[2 + numSig - 2]);
+    }
+    S.startInds = ConstructStartInds(n, sumType);
+    S.Validate();
+    return S;
+}
+
 // ---------------------------------------------------------------------------
 // Per-map device workspace (grow-only buffers).
 // ---------------------------------------------------------------------------
@@ -167,6 +304,7 @@ struct MapWorkspace {
     QuadParams quad{};
     BasisConsts bc{};
     int pmax = 1, dmax = 1, nBmax = 0, depthMax = 0;
+    int basis = 0;  // kernel family: the options' basis, or kBasisSigmoid
     bool built = false;
     std::vector<std::unique_ptr<KLPlan>> klPlans;
     DevBuf perm, sortHist;
@@ -391,6 +529,8 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
             c.coeffOffset = (int)pt.mapCoeffOffset; c.slotOffset = slotOff; c.cSegs = p.cSegs;
             c.nodeA = p.dNodeA; c.nodeSlot = p.dNodeSlot; c.nodeC = p.dNodeC; c.nodeCRows = p.dNodeCRows;
             c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
+            c.sigC = p.dSigC; c.sigW = p.dSigW; c.sigWt = p.dSigWt; c.sigStart = p.dSigStart;
+            c.sigN = (int)p.sigC.size(); c.sigNStarts = (int)p.sigStart.size(); c.rectify = p.kind == 1 ? 1 : 0;
             W.hostComps.push_back(c);
             slotOff += p.nSlots;
             pm = std::max(pm, p.P);
@@ -400,6 +540,13 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
         }
         W.totalSlots = slotOff;
         W.pmax = instantiatedPmax(pm);
+        bool anySig = false, anyMono = false;
+        for (auto& pt : parts_) (pt.prog->kind ? anySig : anyMono) = true;
+        if (anySig && anyMono)
+            throw std::invalid_argument(
+                "TriangularMap: sigmoid expansions and monotone components cannot share one map on this path.");
+        W.basis = anySig ? kBasisSigmoid
+                         : (opts_.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite);
         W.comps.ensure(W.hostComps.size() * sizeof(CompDesc), stream);
         MPGB_CUDA(cudaMemcpy(W.comps.p, W.hostComps.data(), W.hostComps.size() * sizeof(CompDesc),
                              cudaMemcpyHostToDevice));
@@ -506,9 +653,6 @@ static void baseParams(MapWorkspace& W, const MapOptions& o, FusedParams& p, lon
     p.statusWord = W.status.as<int>();
 }
 
-static int basisCode(const MapOptions& o) {
-    return o.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite;
-}
 static int posCode(const MapOptions& o) { return o.posFuncType == PosFuncTypes::Exp ? kPosExp : kPosSoftPlus; }
 
 // Items of style "all components per tile" (per-point sums across components).
@@ -600,7 +744,7 @@ static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nIt
         needJ = 1;
         needE = 2;
     }
-    MPGB_CUDA(launchFused(basisCode(o), posCode(o), W.pmax, p, nItems, needJ, needE, stream));
+    MPGB_CUDA(launchFused(W.basis, posCode(o), W.pmax, p, nItems, needJ, needE, stream));
 }
 
 void MonotoneMapBase::EvaluateImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream) {
@@ -774,7 +918,7 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
     p.quad = W.quad; p.bc = W.bc;
     const int nBlocks = (int)((N + kTpb - 1) / kTpb);
-    MPGB_CUDA(launchInverse(basisCode(opts_), posCode(opts_), W.pmax, p, nBlocks, stream));
+    MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
     Finish(stream, "Inverse");
 }
 
@@ -971,7 +1115,7 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     orderPoints(W, parts_, pts, p, onlyComp, stream);
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
-    MPGB_CUDA(launchFused(basisCode(opts_), posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
+    MPGB_CUDA(launchFused(W.basis, posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
     for (int c = 0; c < (int)parts_.size(); ++c) {
         if (onlyComp >= 0 && c != onlyComp) continue;
         const int nr = P.rowOff[c + 1] - P.rowOff[c];
@@ -1066,6 +1210,75 @@ MonotoneComponent::MonotoneComponent(FixedMultiIndexSet const& mset, MapOptions 
     parts_.push_back({prog, this, 0, 0, 0});
 }
 
+void ConditionalMapBase::FillCoeffBoundsImpl(double* lb, double* ub) const {
+    for (unsigned i = 0; i < numCoeffs; ++i) {
+        lb[i] = -std::numeric_limits<double>::infinity();
+        ub[i] = std::numeric_limits<double>::infinity();
+    }
+}
+
+// HandleSigmoidComponentErrors (src/MapFactory.cpp:320-348).
+static void validateSigmoidOptions(MapOptions const& o) {
+    static const char* btypes[] = {"ProbabilistHermite", "PhysicistHermite", "HermiteFunctions"};
+    if (o.basisType != BasisTypes::HermiteFunctions) {
+        std::ostringstream os;
+        os << "Unsupported basis type for sigmoid expansion: " << btypes[(int)o.basisType];
+        throw std::invalid_argument(os.str());
+    }
+    if (o.posFuncType != PosFuncTypes::Exp && o.posFuncType != PosFuncTypes::SoftPlus)
+        throw std::invalid_argument("Unsupported positive function type for sigmoid expansion.");
+    if (o.edgeType != EdgeTypes::SoftPlus) throw std::invalid_argument("Unsupported edge type for sigmoid expansion.");
+    if (o.sigmoidType != SigmoidTypes::Logistic)
+        throw std::invalid_argument("Unsupported sigmoid type for sigmoid expansion.");
+}
+
+// The options a sigmoid expansion keeps: the quadrature fields play no part
+// (their defaults keep the launch constants valid) and the derivative is exact.
+static MapOptions sigmoidOptions(MapOptions o) {
+    MapOptions d;
+    o.quadType = d.quadType;
+    o.quadAbsTol = d.quadAbsTol;
+    o.quadRelTol = d.quadRelTol;
+    o.quadMaxSub = d.quadMaxSub;
+    o.quadMinSub = d.quadMinSub;
+    o.quadPts = d.quadPts;
+    o.contDeriv = true;
+    o.nugget = 0.0;
+    return o;
+}
+
+SigmoidComponent::SigmoidComponent(FixedMultiIndexSet const& mset, Sigmoid1dParams const& sigmoid,
+                                   MapOptions const& opts)
+    : MonotoneMapBase(mset.Length(), 1, mset.Size(), sigmoidOptions(opts)), mset_(mset), sig_(sigmoid) {
+    validateSigmoidOptions(opts);
+    sig_.Validate();
+    const unsigned last = mset.MaxDegrees()[mset.Length() - 1];
+    if ((int)last > sig_.Order()) {
+        std::ostringstream os;
+        os << "Sigmoid basis evaluation order too large: the multi-index set uses order " << last
+           << " in the last input, the basis has order " << sig_.Order() << ".";
+        throw std::invalid_argument(os.str());
+    }
+    auto prog = std::make_shared<ComponentProgram>(mset);
+    prog->SetSigmoid(sig_, mset.Length() > 1);
+    parts_.push_back({prog, this, 0, 0, 0});
+}
+
+std::vector<unsigned int> SigmoidComponent::DiagonalCoeffIndices() const {
+    if (IsUnivariate()) {
+        std::vector<unsigned int> all(numCoeffs);
+        std::iota(all.begin(), all.end(), 0u);
+        return all;
+    }
+    return mset_.NonzeroDiagonalEntries();
+}
+
+void SigmoidComponent::FillCoeffBoundsImpl(double* lb, double* ub) const {
+    ConditionalMapBase::FillCoeffBoundsImpl(lb, ub);
+    for (unsigned i : DiagonalCoeffIndices()) lb[i] = 0.0;
+    if (IsUnivariate() && numCoeffs > 0) lb[0] = -std::numeric_limits<double>::infinity();
+}
+
 static void collectParts(ConditionalMapBase* comp, unsigned row, unsigned coeffOff,
                          std::vector<MonotoneMapBase::Part>& out, const MapOptions** optsSeen) {
     auto* mono = dynamic_cast<MonotoneMapBase*>(comp);
@@ -1143,6 +1356,14 @@ TriangularMap::TriangularMap(std::vector<std::shared_ptr<ConditionalMapBase>> co
     }
 }
 
+void TriangularMap::FillCoeffBoundsImpl(double* lb, double* ub) const {
+    unsigned off = 0;
+    for (auto& c : comps_) {
+        c->FillCoeffBoundsImpl(lb + off, ub + off);
+        off += c->numCoeffs;
+    }
+}
+
 void TriangularMap::SetCoeffs(const double* coeffs, unsigned int n, bool host, cudaStream_t stream) {
     ConditionalMapBase::SetCoeffs(coeffs, n, host, stream);
     unsigned off = 0;
@@ -1181,6 +1402,60 @@ std::shared_ptr<ConditionalMapBase> CreateTriangular(unsigned int inputDim, unsi
         FixedMultiIndexSet mset(i + extra + 1, totalOrder);
         comps[i] = std::make_shared<MonotoneComponent>(mset, options);
     }
+    auto out = std::make_shared<TriangularMap>(comps);
+    std::vector<double> z(out->numCoeffs, 0.0);
+    out->SetCoeffs(z.data(), out->numCoeffs, true);
+    return out;
+}
+
+// CreateSigmoidExpansionTemplate (src/MapFactory.cpp:256-318).
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(FixedMultiIndexSet const& mset,
+                                                           std::vector<double> const& centers, MapOptions opts) {
+    validateSigmoidOptions(opts);
+    auto sig = Sigmoid1dParams::FromCenters(centers, opts.edgeShape, opts.sigmoidBasisSumType);
+    auto c = std::make_shared<SigmoidComponent>(mset, sig, opts);
+    std::vector<double> z(c->numCoeffs, 0.0);
+    c->SetCoeffs(z.data(), c->numCoeffs, true);
+    return c;
+}
+
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(unsigned int inputDim, unsigned int offDiagOrder,
+                                                           unsigned int crossOrder, std::vector<double> const& centers,
+                                                           MapOptions opts) {
+    validateSigmoidOptions(opts);
+    if (inputDim == 0) throw std::invalid_argument("CreateSigmoidComponent: inputDim must be positive.");
+    const int numSig = Sigmoid1dParams::ComputeNumSigmoids((unsigned)centers.size(), opts.sigmoidBasisSumType);
+    if (numSig < 0) throw std::invalid_argument("Sigmoid: centers/widths/weights too short.");
+    if (inputDim == 1) return CreateSigmoidComponent(FixedMultiIndexSet(1, numSig + 3), centers, opts);
+    // Leading-input terms, then leading x sigmoid terms (order 0 excluded: it is in the first block).
+    FixedMultiIndexSet m1 = FixedMultiIndexSet(inputDim - 1, offDiagOrder).Cartesian(FixedMultiIndexSet(1, 0));
+    FixedMultiIndexSet m2 =
+        FixedMultiIndexSet(inputDim - 1, crossOrder).Cartesian(FixedMultiIndexSet(1, numSig + 3, 1));
+    return CreateSigmoidComponent(m1.Concatenate(m2), centers, opts);
+}
+
+std::shared_ptr<ConditionalMapBase> CreateSigmoidComponent(unsigned int inputDim, unsigned int totalOrder,
+                                                           std::vector<double> const& centers, MapOptions opts) {
+    return CreateSigmoidComponent(inputDim, totalOrder, totalOrder, centers, opts);
+}
+
+// src/MapFactory.cpp:389-407: component i has input dimension
+// inputDim - outputDim + i + 1 and the centers centers[i].
+std::shared_ptr<ConditionalMapBase> CreateSigmoidTriangular(unsigned int inputDim, unsigned int outputDim,
+                                                            unsigned int totalOrder,
+                                                            std::vector<std::vector<double>> const& centers,
+                                                            MapOptions opts) {
+    if (outputDim > inputDim) {
+        std::ostringstream os;
+        os << "CreateSigmoidTriangular: Output dimension " << outputDim << " cannot be greater than input dimension "
+           << inputDim;
+        throw std::invalid_argument(os.str());
+    }
+    if (outputDim == 0 || centers.size() != outputDim)
+        throw std::invalid_argument("CreateSigmoidTriangular: need one vector of centers per output.");
+    std::vector<std::shared_ptr<ConditionalMapBase>> comps(outputDim);
+    for (unsigned i = 0; i < outputDim; ++i)
+        comps[i] = CreateSigmoidComponent(inputDim - outputDim + i + 1, totalOrder, centers[i], opts);
     auto out = std::make_shared<TriangularMap>(comps);
     std::vector<double> z(out->numCoeffs, 0.0);
     out->SetCoeffs(z.data(), out->numCoeffs, true);
@@ -1261,6 +1536,12 @@ MapOptions toOptions(const mpgb_map_options* o) {
     m.contDeriv = o->cont_deriv != 0;
     m.basisNorm = o->basis_norm != 0;
     m.nugget = o->nugget;
+    if (o->sigmoid_type != 0 || o->edge_type != 0 || o->sigmoid_sum_type < 0 || o->sigmoid_sum_type > 1)
+        throw std::invalid_argument("invalid sigmoid enum value in options");
+    m.sigmoidType = SigmoidTypes::Logistic;
+    m.edgeType = EdgeTypes::SoftPlus;
+    m.edgeShape = o->edge_shape;
+    m.sigmoidBasisSumType = (SigmoidSumSizeType)o->sigmoid_sum_type;
     return m;
 }
 
@@ -1359,6 +1640,10 @@ int mpgb_map_options_default(mpgb_map_options* o) {
         o->cont_deriv = m.contDeriv;
         o->basis_norm = m.basisNorm;
         o->nugget = m.nugget;
+        o->sigmoid_type = (int)m.sigmoidType;
+        o->edge_type = (int)m.edgeType;
+        o->edge_shape = m.edgeShape;
+        o->sigmoid_sum_type = (int)m.sigmoidBasisSumType;
     });
 }
 
@@ -1403,6 +1688,130 @@ int mpgb_create_triangular_from_components(mpgb_map* const* components, unsigned
             v.push_back(components[i]->obj);
         }
         *out = new mpgb_map{std::make_shared<TriangularMap>(v, move_coeffs != 0)};
+    });
+}
+
+static std::vector<double> hostVector(const double* p, unsigned n) {
+    if (n && !p) throw std::invalid_argument("null centers");
+    return std::vector<double>(p, p + n);
+}
+
+int mpgb_create_sigmoid_component(unsigned int input_dim, unsigned int off_diag_order, unsigned int cross_order,
+                                  const double* centers, unsigned int n_centers, const mpgb_map_options* opts,
+                                  mpgb_map** out) {
+    return guard([&] {
+        if (!out) throw std::invalid_argument("null argument");
+        *out = new mpgb_map{MapFactory::CreateSigmoidComponent(input_dim, off_diag_order, cross_order,
+                                                               hostVector(centers, n_centers), toOptions(opts))};
+    });
+}
+
+int mpgb_create_sigmoid_component_mset(unsigned int dim, unsigned int num_terms, const unsigned int* nz_starts,
+                                       const unsigned int* nz_dims, const unsigned int* nz_orders,
+                                       const double* centers, unsigned int n_centers,
+                                       const mpgb_map_options* opts, mpgb_map** out) {
+    return guard([&] {
+        if (!out || !nz_starts) throw std::invalid_argument("null argument");
+        std::vector<unsigned> st(nz_starts, nz_starts + num_terms + 1);
+        const unsigned nnz = st.back();
+        if (nnz > 0 && (!nz_dims || !nz_orders)) throw std::invalid_argument("null nonzero arrays");
+        FixedMultiIndexSet ms(dim, st, std::vector<unsigned>(nz_dims, nz_dims + nnz),
+                              std::vector<unsigned>(nz_orders, nz_orders + nnz));
+        *out = new mpgb_map{MapFactory::CreateSigmoidComponent(ms, hostVector(centers, n_centers), toOptions(opts))};
+    });
+}
+
+int mpgb_create_sigmoid_triangular(unsigned int input_dim, unsigned int output_dim, unsigned int total_order,
+                                   const double* centers, unsigned int n_centers, int64_t row_stride,
+                                   int64_t col_stride, const mpgb_map_options* opts, mpgb_map** out) {
+    return guard([&] {
+        if (!out || (n_centers && !centers)) throw std::invalid_argument("null argument");
+        std::vector<std::vector<double>> cs(output_dim, std::vector<double>(n_centers));
+        for (unsigned j = 0; j < output_dim; ++j)
+            for (unsigned i = 0; i < n_centers; ++i) cs[j][i] = centers[(int64_t)i * row_stride + (int64_t)j * col_stride];
+        *out = new mpgb_map{MapFactory::CreateSigmoidTriangular(input_dim, output_dim, total_order, cs, toOptions(opts))};
+    });
+}
+
+int mpgb_map_coeff_bounds(const mpgb_map* map, double* lb, double* ub) {
+    return guard([&] {
+        if (!map || !lb || !ub) throw std::invalid_argument("null argument");
+        map->obj->FillCoeffBoundsImpl(lb, ub);
+    });
+}
+
+int mpgb_map_kind(const mpgb_map* map, int* kind) {
+    return guard([&] {
+        if (!map || !kind) throw std::invalid_argument("null argument");
+        if (dynamic_cast<TriangularMap*>(map->obj.get())) *kind = -1;
+        else if (auto* s = dynamic_cast<SigmoidComponent*>(map->obj.get())) *kind = s->IsUnivariate() ? 2 : 1;
+        else *kind = 0;
+    });
+}
+
+int mpgb_component_sigmoid(const mpgb_map* component, double* centers, double* widths, double* weights,
+                           unsigned int* n_centers, unsigned int* starts, unsigned int* n_starts) {
+    return guard([&] {
+        if (!component) throw std::invalid_argument("null map handle");
+        auto* s = dynamic_cast<SigmoidComponent*>(component->obj.get());
+        if (!s) throw std::invalid_argument("not a sigmoid expansion");
+        const Sigmoid1dParams& p = s->GetSigmoid();
+        if (n_centers) *n_centers = (unsigned)p.centers.size();
+        if (n_starts) *n_starts = (unsigned)p.startInds.size();
+        if (centers) std::copy(p.centers.begin(), p.centers.end(), centers);
+        if (widths) std::copy(p.widths.begin(), p.widths.end(), widths);
+        if (weights) std::copy(p.weights.begin(), p.weights.end(), weights);
+        if (starts) std::copy(p.startInds.begin(), p.startInds.end(), starts);
+    });
+}
+
+int mpgb_sigmoid_params(const double* centers, unsigned int n, double edge_shape, int sum_type,
+                        double* out_centers, double* widths, double* weights, unsigned int* starts,
+                        unsigned int* n_starts) {
+    return guard([&] {
+        if (sum_type < 0 || sum_type > 1) throw std::invalid_argument("invalid sigmoid sum type");
+        Sigmoid1dParams p = Sigmoid1dParams::FromCenters(hostVector(centers, n), edge_shape, (SigmoidSumSizeType)sum_type);
+        if (out_centers) std::copy(p.centers.begin(), p.centers.end(), out_centers);
+        if (widths) std::copy(p.widths.begin(), p.widths.end(), widths);
+        if (weights) std::copy(p.weights.begin(), p.weights.end(), weights);
+        if (starts) std::copy(p.startInds.begin(), p.startInds.end(), starts);
+        if (n_starts) *n_starts = (unsigned)p.startInds.size();
+    });
+}
+
+int mpgb_sigmoid1d_evaluate(const double* centers, const double* widths, const double* weights, unsigned int n,
+                            const unsigned int* starts, unsigned int n_starts, int which, unsigned int max_order,
+                            const double* x, int64_t n_x, int64_t x_stride, double* out, double* d1, double* d2,
+                            void* stream) {
+    return guard([&] {
+        if (which < 0 || which > 2) throw std::invalid_argument("which must be 0, 1 or 2");
+        Sigmoid1dParams p;
+        p.centers = hostVector(centers, n);
+        p.widths = hostVector(widths, n);
+        p.weights = hostVector(weights, n);
+        if (n_starts && !starts) throw std::invalid_argument("null starts");
+        p.startInds.assign(starts, starts + n_starts);
+        p.Validate();
+        if ((int)max_order > p.Order()) throw std::invalid_argument("Sigmoid basis evaluation order too large.");
+        if (n_x <= 0) return;
+        if (!x || !out || (which >= 1 && !d1) || (which == 2 && !d2)) throw std::invalid_argument("null array");
+        cudaStream_t s = (cudaStream_t)stream;
+        std::vector<int32_t> st(p.startInds.begin(), p.startInds.end());
+        DevBuf buf;
+        const size_t nd = 3 * (size_t)n, ni = st.size();
+        buf.ensure(nd * sizeof(double) + ni * sizeof(int32_t) + 16, s);
+        double* dp = buf.as<double>();
+        MPGB_CUDA(cudaMemcpyAsync(dp, p.centers.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+        MPGB_CUDA(cudaMemcpyAsync(dp + n, p.widths.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+        MPGB_CUDA(cudaMemcpyAsync(dp + 2 * n, p.weights.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+        int32_t* ip = (int32_t*)(dp + nd);
+        if (ni) MPGB_CUDA(cudaMemcpyAsync(ip, st.data(), ni * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        CompDesc c{};
+        c.sigC = dp; c.sigW = dp + n; c.sigWt = dp + 2 * n; c.sigStart = ip;
+        c.sigN = (int)n; c.sigNStarts = (int)ni;
+        MPGB_CUDA(launchSigmoidEval(c, (int)max_order, x, n_x, x_stride, out, which >= 1 ? d1 : nullptr,
+                                    which == 2 ? d2 : nullptr, s));
+        MPGB_CUDA(cudaStreamSynchronize(s));
     });
 }
 
@@ -1707,9 +2116,11 @@ int mpgb_component_multi_index(const mpgb_map* component, unsigned int* dim, uns
                                unsigned int* nz_orders) {
     return guard([&] {
         if (!component || !component->obj) throw std::invalid_argument("null map handle");
-        auto* c = dynamic_cast<const MonotoneComponent*>(component->obj.get());
-        if (!c) throw std::invalid_argument("not a single monotone component");
-        const FixedMultiIndexSet& m = c->GetMultiIndexSet();
+        const FixedMultiIndexSet* ms = nullptr;
+        if (auto* c = dynamic_cast<const MonotoneComponent*>(component->obj.get())) ms = &c->GetMultiIndexSet();
+        else if (auto* g = dynamic_cast<const SigmoidComponent*>(component->obj.get())) ms = &g->GetMultiIndexSet();
+        if (!ms) throw std::invalid_argument("not a single monotone component or sigmoid expansion");
+        const FixedMultiIndexSet& m = *ms;
         if (dim) *dim = m.Length();
         if (num_terms) *num_terms = m.Size();
         if (nnz) *nnz = (unsigned)m.nzDims.size();

@@ -3,6 +3,7 @@
 
 #include "mpgb_types.h"
 #include "mpgb_launch.h"
+#include "mpgb_sigmoid.cuh"
 
 namespace mpgb {
 
@@ -213,6 +214,10 @@ int instantiatedPmax(int p) {
 
 cudaError_t launchFused(int basis, int pos, int pmax, const FusedParams& prm, int nItems, int needJ, int needE,
                         cudaStream_t stream) {
+    if (basis == kBasisSigmoid) {
+        if (pos == kPosSoftPlus) return launchFusedBP<kBasisSigmoid, kPosSoftPlus>(prm, pmax, nItems, 0, 0, stream);
+        return launchFusedBP<kBasisSigmoid, kPosExp>(prm, pmax, nItems, 0, 0, stream);
+    }
     if (basis == kBasisProbHermite) {
         if (pos == kPosSoftPlus) return launchFusedBP<kBasisProbHermite, kPosSoftPlus>(prm, pmax, nItems, needJ, needE, stream);
         return launchFusedBP<kBasisProbHermite, kPosExp>(prm, pmax, nItems, needJ, needE, stream);
@@ -231,6 +236,7 @@ int batchOrderClass(int p) {
 
 cudaError_t launchBatch(int basis, int pos, const FusedParams& prm, int nItems, int pmaxClass, int* counter,
                         cudaStream_t stream) {
+    if (basis == kBasisSigmoid) return cudaErrorNotSupported;
     if (basis == kBasisProbHermite) {
         if (pos == kPosSoftPlus)
             return launchBatchP<kBasisProbHermite, kPosSoftPlus>(prm, nItems, pmaxClass, counter, stream);
@@ -242,6 +248,10 @@ cudaError_t launchBatch(int basis, int pos, const FusedParams& prm, int nItems, 
 }
 
 cudaError_t launchInverse(int basis, int pos, int pmax, const InverseParams& prm, int nBlocks, cudaStream_t stream) {
+    if (basis == kBasisSigmoid) {
+        if (pos == kPosSoftPlus) return launchInverseBP<kBasisSigmoid, kPosSoftPlus>(prm, pmax, nBlocks, stream);
+        return launchInverseBP<kBasisSigmoid, kPosExp>(prm, pmax, nBlocks, stream);
+    }
     if (basis == kBasisProbHermite) {
         if (pos == kPosSoftPlus) return launchInverseBP<kBasisProbHermite, kPosSoftPlus>(prm, pmax, nBlocks, stream);
         return launchInverseBP<kBasisProbHermite, kPosExp>(prm, pmax, nBlocks, stream);
@@ -317,6 +327,29 @@ cudaError_t launchSortByLast(const double* xd, long long stride, long long N, in
 cudaError_t launchDenseKLReduce(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,
                                 long long N, double* loss, double* grad, cudaStream_t stream) {
     denseKLReduceKernel<<<nTerms + 1, 256, 0, stream>>>(T, ld, dT, dL, nTerms, N, 1.0 / (double)N, loss, grad);
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
+}
+
+__global__ void sigmoidEvalKernel(const CompDesc c, int maxOrder, const double* x, long long n, long long stride,
+                                  double* out, double* d1, double* d2) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v[kMaxLastOrder + 1], g1[kMaxLastOrder + 1], g2[kMaxLastOrder + 1];
+    sigmoidBasis<kMaxLastOrder, true>(x[i * stride], maxOrder, c, v, g1, g2);
+    for (int k = 0; k <= maxOrder; ++k) {
+        out[k * n + i] = v[k];
+        if (d1) d1[k * n + i] = g1[k];
+        if (d2) d2[k * n + i] = g2[k];
+    }
+}
+
+cudaError_t launchSigmoidEval(const CompDesc& c, int maxOrder, const double* x, long long n, long long stride,
+                              double* out, double* d1, double* d2, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    if (maxOrder < 0 || maxOrder > kMaxLastOrder) return cudaErrorInvalidValue;
+    sigmoidEvalKernel<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(c, maxOrder, x, n, stride, out, d1, d2);
     const cudaError_t e = cudaGetLastError();
     countLaunches(stream, 1);
     return e;

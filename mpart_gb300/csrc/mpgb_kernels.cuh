@@ -21,6 +21,7 @@
 #include <cstdio>
 #include "mpgb_types.h"
 #include "mpgb_launch.h"
+#include "mpgb_sigmoid.cuh"
 
 namespace mpgb {
 
@@ -423,6 +424,41 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
 }
 
 // --------------------------------------------------------------------------
+// Sigmoid expansions (no quadrature).
+// --------------------------------------------------------------------------
+// Phase A of a sigmoid expansion: a_0 = sum_m c_(m,0) Phi_m and, for k >= 1,
+// a_k = sum_m c_(m,k) R(Phi_m) with R the rectifier when c.rectify, so that
+// T = sum_k a_k f_k(x_D).  Terms with a last-input factor and no leading
+// factor take R(1), as the reference's term products do
+// (MultivariateExpansionWorker.h:423-441).
+template <int PMAX, int POS>
+__device__ __forceinline__ void phaseARect(const CompDesc& c, const SmemLayout& L, int tid, const double* cm,
+                                           double* a) {
+#pragma unroll
+    for (int k = 0; k <= PMAX; ++k) a[k] = 0.0;
+    const int tpb = blockDim.x;
+    L.S[tid] = 1.0;
+    for (int n = 0; n < c.nNodes; ++n) {
+        const uint32_t w = __ldg(&c.nodeA[n]);
+        const int depth = w & 31;
+        const int nk = (w >> 5) & 31;
+        const int brow = w >> 18;
+        double phi = 1.0;
+        if (depth > 0) {
+            phi = L.S[(depth - 1) * tpb + tid] * L.B[brow * L.bstride + tid];
+            L.S[depth * tpb + tid] = phi;
+        }
+        if (nk) {
+            const double* cs = cm + __ldg(&c.nodeSlot[n]);
+            const double a0 = fma(__ldg(&cs[0]), phi, a[0]);
+            const double r = (c.rectify && nk > 1) ? posValue<POS>(phi) : phi;
+            accumCoeffs<PMAX>(nk, r, cs, a);
+            a[0] = a0;
+        }
+    }
+}
+
+// --------------------------------------------------------------------------
 // The fused kernel.
 // --------------------------------------------------------------------------
 // Point data of a work item: the launch-wide fields of FusedParams, or (in a
@@ -467,37 +503,63 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             else fillLead<BASIS, false>(c, L, tid, prm.bc);
 
             double a[PMAX + 1];
-            phaseA<PMAX>(c, L, tid, cm, a);
+            if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, a);
+            else phaseA<PMAX>(c, L, tid, cm, a);
             const double xd = L.X[(c.D - 1) * tpb + tid];
 
-            // Last-coordinate basis at 0 and at x_D.
-            const double* v0 = prm.bc.v0;
-            double d1x[PMAX + 1], d2x[PMAX + 1];
-            lastBasis<BASIS, PMAX, false, true, true>(xd, P, prm.bc, nullptr, d1x, d2x);
-            double dfx = 0.0, d2fx = 0.0, f0 = 0.0;
-#pragma unroll
-            for (int k = 0; k <= PMAX; ++k) {
-                f0 = fma(a[k], v0[k], f0);
-                dfx = fma(a[k], d1x[k], dfx);
-                d2fx = fma(a[k], d2x[k], d2fx);
-            }
-            double gx, gpx;
-            posEval<POS>(dfx, gx, gpx);
-
-            // (The discrete-derivative variant, NEEDE == 2, always integrates:
-            // its log-determinant is that of the quadrature approximation.)
-            const bool needT = (flags & (kFlagEval | kFlagCoefDenseT | kFlagKL)) != 0 ||
-                               (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput))) || NEEDE == 2;
+            // wv[k] = dT/da_k; d1x, d2x: last-input basis derivatives at x_D;
+            // ldx = d logdet / dx_D.
+            double wv[PMAX + 1], d1x[PMAX + 1], d2x[PMAX + 1];
+            double T, dT, gx, gpx, ldx;
             QuadOut<PMAX, NEEDJ, NEEDE> R;
             R.Ih = 0.0; R.IE = 0.0;
 #pragma unroll
             for (int k = 0; k < (NEEDJ ? PMAX : 1); ++k) R.J[k] = 0.0;
-            if (needT && active) integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
-            const double T = R.Ih + f0;
-            // dT/dx_D: g(df(x)) (ContinuousDerivative) or the x_D-derivative of
-            // the quadrature approximation (DiscreteDerivative, MonotoneComponent.h:585-638).
-            const double dT = (NEEDE == 2) ? R.IE : gx;
-            const double logdet = (dT <= 0.0) ? ninf : log(dT);
+            if constexpr (BASIS == kBasisSigmoid) {
+                // T = sum_k a_k f_k(x_D), d_D T and d_D^2 T in closed form
+                // (RectifiedMultivariateExpansion.h:40-75, :192-225).
+                sigmoidBasis<PMAX, true>(xd, P, c, wv, d1x, d2x);
+                double t = 0.0, dt = 0.0, d2t = 0.0;
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) {
+                    t = fma(a[k], wv[k], t);
+                    dt = fma(a[k], d1x[k], dt);
+                    d2t = fma(a[k], d2x[k], d2t);
+                }
+                T = t;
+                dT = dt;
+                gx = dt;
+                gpx = 0.0;
+                ldx = d2t / dt;
+            } else {
+                // Last-coordinate basis at 0 and at x_D.
+                const double* v0 = prm.bc.v0;
+                lastBasis<BASIS, PMAX, false, true, true>(xd, P, prm.bc, nullptr, d1x, d2x);
+                double dfx = 0.0, d2fx = 0.0, f0 = 0.0;
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) {
+                    f0 = fma(a[k], v0[k], f0);
+                    dfx = fma(a[k], d1x[k], dfx);
+                    d2fx = fma(a[k], d2x[k], d2fx);
+                }
+                posEval<POS>(dfx, gx, gpx);
+
+                // (The discrete-derivative variant, NEEDE == 2, always integrates:
+                // its log-determinant is that of the quadrature approximation.)
+                const bool needT = (flags & (kFlagEval | kFlagCoefDenseT | kFlagKL)) != 0 ||
+                                   (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput))) || NEEDE == 2;
+                if (needT && active) integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
+                T = R.Ih + f0;
+                // dT/dx_D: g(df(x)) (ContinuousDerivative) or the x_D-derivative of
+                // the quadrature approximation (DiscreteDerivative, MonotoneComponent.h:585-638).
+                dT = (NEEDE == 2) ? R.IE : gx;
+                ldx = gpx * (1.0 / gx) * d2fx;
+#pragma unroll
+                for (int k = 0; k <= PMAX; ++k) wv[k] = v0[k] + ((NEEDJ && k >= 1) ? R.J[k >= 1 ? k - 1 : 0] : 0.0);
+            }
+            // (A sigmoid expansion's derivative can be negative: log gives NaN
+            // there, as the reference's does.)
+            const double logdet = (BASIS != kBasisSigmoid && dT <= 0.0) ? ninf : log(dT);
 
             if ((flags & kFlagEval) && active && MPGB_IO(outEval)) MPGB_IO(outEval)[(long long)c.outRow * MPGB_IO(evalRs) + i * MPGB_IO(evalCs)] = T;
             if (flags & kFlagLogDet) logdetSum += logdet;
@@ -515,7 +577,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 if (flags & kFlagImplicit) {
                     // lambda = (w - sum_{m > k} lambda_m dT_m/dx_D) / (g(df) + nugget)
                     double* gd = &L.GX[(c.D - 1) * tpb + tid];
-                    sens = active ? (sens - *gd) / (gx + prm.nugget) : 0.0;
+                    sens = active ? (sens - *gd) / (BASIS == kBasisSigmoid ? gx : gx + prm.nugget) : 0.0;
                     *gd = sens;
                     lsens = 0.0;
                 }
@@ -523,20 +585,24 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             if (!active) { sens = 0.0; lsens = 0.0; }
             const double ldScale = gpx * (1.0 / gx);
             // d logdet / d a_k: g'/g phit'_k(x_D), or (discrete) K_k / (dT/dx_D)
-            // with K the MixedCoeff integral (DiscreteMixedJacobian, MonotoneComponent.h:928-980).
+            // with K the MixedCoeff integral (DiscreteMixedJacobian, MonotoneComponent.h:928-980),
+            // or (sigmoid expansion) f'_k(x_D) / d_D T.
             double dld[PMAX + 1];
 #pragma unroll
             for (int k = 0; k <= PMAX; ++k) {
                 // (inactive lanes did not integrate: keep their weights zero)
-                if constexpr (NEEDE == 2) dld[k] = (k >= 1 && active) ? R.K[k >= 1 ? k - 1 : 0] * (1.0 / R.IE) : 0.0;
+                if constexpr (BASIS == kBasisSigmoid) dld[k] = active ? d1x[k] * (1.0 / dT) : 0.0;
+                else if constexpr (NEEDE == 2) dld[k] = (k >= 1 && active) ? R.K[k >= 1 ? k - 1 : 0] * (1.0 / R.IE) : 0.0;
                 else dld[k] = ldScale * d1x[k];
             }
             double wT[PMAX + 1], wL[PMAX + 1];
 #pragma unroll
             for (int k = 0; k <= PMAX; ++k) {
-                const double Jk = (NEEDJ && k >= 1) ? R.J[k >= 1 ? k - 1 : 0] : 0.0;
-                wT[k] = sens * (v0[k] + Jk);
-                wL[k] = lsens * dld[k];
+                wT[k] = sens * wv[k];
+                // (a sigmoid expansion's d_D T may vanish, e.g. at zero coefficients:
+                // without a log-det weight its terms stay out)
+                if constexpr (BASIS == kBasisSigmoid) wL[k] = (lsens != 0.0) ? lsens * dld[k] : 0.0;
+                else wL[k] = lsens * dld[k];
             }
 
             // Dense per-term outputs (CoeffGradImpl / LogDeterminantCoeffGradImpl).
@@ -556,13 +622,16 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     }
                     if (nk) {
                         const int slot = __ldg(&c.nodeSlot[n]);
+                        double rv = phi;  // the term's leading factor for k >= 1
+                        if constexpr (BASIS == kBasisSigmoid)
+                            if (c.rectify && nk > 1) rv = posValue<POS>(phi);
 #pragma unroll
                         for (int k = 0; k <= PMAX; ++k) {
                             if (k < nk) {
                                 const int t = __ldg(&c.slotTerm[slot + k]);
                                 if (t >= 0)
                                     prm.outDense[(long long)(c.coeffOffset + t) * prm.denseRs + i * prm.denseCs] =
-                                        phi * wd[k];
+                                        (k == 0 ? phi : rv) * wd[k];
                             }
                         }
                     }
@@ -594,7 +663,15 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     if (nk && depth > 0) {
                         const double* cs = cm + __ldg(&c.nodeSlot[n]);
                         double beta = 0.0;
-                        for (int k = 0; k < nk; ++k) beta = fma(__ldg(&cs[k]), w[k < PMAX ? k : PMAX], beta);
+                        if constexpr (BASIS == kBasisSigmoid) {
+                            // d/dPhi [c_0 Phi w_0 + R(Phi) sum_k c_k w_k]
+                            double b1 = 0.0;
+                            for (int k = 1; k < nk; ++k) b1 = fma(__ldg(&cs[k]), w[k < PMAX ? k : PMAX], b1);
+                            const double rp = (c.rectify && nk > 1) ? posDeriv<POS>(L.S[depth * tpb + tid]) : 1.0;
+                            beta = fma(__ldg(&cs[0]), w[0], rp * b1);
+                        } else {
+                            for (int k = 0; k < nk; ++k) beta = fma(__ldg(&cs[k]), w[k < PMAX ? k : PMAX], beta);
+                        }
                         const int tl = depth * (depth + 1) / 2;
                         for (int j = 1; j <= depth; ++j) {
                             double* g = &L.GX[dims[j] * tpb + tid];
@@ -606,8 +683,9 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 // log-det term (MonotoneComponent.h:811-815, :892-925).
                 // (The host does not combine lsens with input gradients in the
                 // discrete mode, which the reference does not provide.)
-                double gxd = (NEEDE == 2) ? 0.0 : lsens * (ldScale * d2fx);
-                if constexpr (NEEDE) gxd = fma(sens, R.IE, gxd);
+                double gxd = (NEEDE == 2) ? 0.0 : lsens * ldx;
+                if constexpr (BASIS == kBasisSigmoid) gxd = fma(sens, dT, (lsens != 0.0) ? gxd : 0.0);
+                else if constexpr (NEEDE) gxd = fma(sens, R.IE, gxd);
                 double* g = &L.GX[(c.D - 1) * tpb + tid];
                 if (!(flags & kFlagImplicit)) *g += gxd;  // implicit mode keeps lambda there
             }
@@ -637,7 +715,14 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
                     for (int j = sg * segLen; j < (sg + 1) * segLen; ++j) {
                         const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
-                        accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
+                        if constexpr (BASIS == kBasisSigmoid) {
+                            const double a0 = fma(phi, L.W[j], acc[0]);
+                            const double rv = (c.rectify && nk > 1) ? posValue<POS>(phi) : phi;
+                            accumSlots<PMAX>(nk, rv, L.W + j, tpb, acc);
+                            acc[0] = a0;
+                        } else {
+                            accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
+                        }
                     }
 #pragma unroll
                     for (int k = 0; k <= PMAX; ++k) {
@@ -764,6 +849,31 @@ struct InverseEval {
     }
 };
 
+// T(x_<D, y) of a sigmoid expansion as a function of y (the reference's
+// SingleWorkerEvaluator, RectifiedMultivariateExpansion.h:392-405), and its slope.
+template <int PMAX>
+struct SigmoidInverseEval {
+    ACoef<PMAX> A;
+    int P;
+    const CompDesc* c;
+    __device__ double operator()(double y) const {
+        double v[PMAX + 1], d1[PMAX + 1];
+        sigmoidBasis<PMAX, false>(y, P, *c, v, d1, nullptr);
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k <= PMAX; ++k) t = fma(A.a[k], v[k], t);
+        return t;
+    }
+    __device__ double slope(double y) const {
+        double v[PMAX + 1], d1[PMAX + 1];
+        sigmoidBasis<PMAX, false>(y, P, *c, v, d1, nullptr);
+        double t = 0.0;
+#pragma unroll
+        for (int k = 0; k <= PMAX; ++k) t = fma(A.a[k], d1[k], t);
+        return t;
+    }
+};
+
 template <class F>
 __device__ void findBracket(const F& f, double& xlb, double& ylb, double& xub, double& yub, const double yd,
                             int& info) {
@@ -867,19 +977,28 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
         const double* cm = prm.cm + c.slotOffset;
         fillLead<BASIS, false>(c, L, tid, prm.bc);
         ACoef<PMAX> A;
-        phaseA<PMAX>(c, L, tid, cm, A.a);
+        if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a);
+        else phaseA<PMAX>(c, L, tid, cm, A.a);
         double result = nan;
         int info = 0;
         if (active) {
             bool hasNan = false;
             for (int d = 0; d < c.D; ++d) hasNan |= isnan(L.X[d * tpb + tid]);
-            if (!hasNan) {
+            const double yd = prm.r[(long long)ci * prm.rRs + i * prm.rCs];
+            if constexpr (BASIS == kBasisSigmoid) {
+                // (RectifiedMultivariateExpansion.h:227-277; UnivariateExpansion.h:213-250.
+                // A NaN target gives NaN.)
+                if (!hasNan && !isnan(yd)) {
+                    SigmoidInverseEval<PMAX> f{A, c.P, &c};
+                    result = inverseSingleBracket(yd, f, L.X[(c.D - 1) * tpb + tid], prm.xtol, prm.ytol, info);
+                    if (info < 0) stAll |= kStatusNoBracket;
+                }
+            } else if (!hasNan) {
                 double f0 = 0.0;
 #pragma unroll
                 for (int k = 0; k <= PMAX; ++k) f0 = fma(A.a[k], prm.bc.v0[k], f0);
                 int st = 0;
                 InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
-                const double yd = prm.r[(long long)ci * prm.rRs + i * prm.rCs];
                 result = inverseSingleBracket(yd, f, L.X[(c.D - 1) * tpb + tid], prm.xtol, prm.ytol, info);
                 if (info < 0) st |= kStatusNoBracket;
                 stAll |= st;
@@ -907,10 +1026,16 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
         countLaunches(stream, 1);
         return e;
     };
-    if (needE == 2) return run(fusedKernel<BASIS, POS, PMAX, true, 2>);
-    if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, 1>);
-    if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, 0>);
-    return run(fusedKernel<BASIS, POS, PMAX, false, 0>);
+    if constexpr (BASIS == kBasisSigmoid) {
+        (void)needJ;
+        (void)needE;
+        return run(fusedKernel<BASIS, POS, PMAX, false, 0>);
+    } else {
+        if (needE == 2) return run(fusedKernel<BASIS, POS, PMAX, true, 2>);
+        if (needE) return run(fusedKernel<BASIS, POS, PMAX, true, 1>);
+        if (needJ) return run(fusedKernel<BASIS, POS, PMAX, true, 0>);
+        return run(fusedKernel<BASIS, POS, PMAX, false, 0>);
+    }
 }
 
 // Persistent batch launch: as many blocks as fit on the device at once (at

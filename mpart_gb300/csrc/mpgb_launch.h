@@ -31,6 +31,10 @@ size_t sortScratchInts(long long N);
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
                              cudaStream_t stream);
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
+// Sigmoid1d basis (c.sig* fields, device arrays) at n points x[i * stride]:
+// out / d1 / d2 are (maxOrder + 1) x n, row stride n; d1, d2 may be null.
+cudaError_t launchSigmoidEval(const CompDesc& c, int maxOrder, const double* x, long long n, long long stride,
+                              double* out, double* d1, double* d2, cudaStream_t stream);
 // Loss and gradient of the standard-normal reverse KL from dense outputs:
 // T, ld (N), dT = dT/dc scaled by T, dL = dlogdet/dc (nTerms x N, row-major).
 cudaError_t launchDenseKLReduce(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,

@@ -119,6 +119,9 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
     const MapOptions& o = map.Options();
     if (!o.contDeriv)
         throw std::invalid_argument("contDeriv = false (discrete derivative) is not provided without allocation.");
+    for (int c = 0; c < nComps; ++c)
+        if (parts[c].prog->kind != 0)
+            throw std::invalid_argument("sigmoid expansions are not provided by the no-allocation entry point.");
     int dev = 0, sms = 0;
     MPGB_CUDA(cudaGetDevice(&dev));
     MPGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -60,6 +60,30 @@ struct ComponentProgram {
     // block's threads take (node, segment) units, so that a few hundred nodes
     // still keep every thread busy; each segment has its own partial row.
     int cSegs = 1;
+    // Sigmoid expansions: kind 1 = rectified (RectifiedMultivariateExpansion),
+    // kind 2 = one input without rectifier (UnivariateExpansion); kind 0 is a
+    // monotone component.  The last input's Sigmoid1d parameters live on the
+    // device next to the tree tables.
+    int kind = 0;
+    std::vector<double> sigC, sigW, sigWt;
+    std::vector<int32_t> sigStart;
+    double *dSigC = nullptr, *dSigW = nullptr, *dSigWt = nullptr;
+    int32_t* dSigStart = nullptr;
+
+    void SetSigmoid(Sigmoid1dParams const& sp, bool rectify) {
+        kind = rectify ? 1 : 2;
+        sigC = sp.centers;
+        sigW = sp.widths;
+        sigWt = sp.weights;
+        sigStart.assign(sp.startInds.begin(), sp.startInds.end());
+        dSigC = toDevice(sigC);
+        dSigW = toDevice(sigW);
+        dSigWt = toDevice(sigWt);
+        dSigStart = toDevice(sigStart);
+        // Per point: the tree walks plus a rectifier per node (phases A and C)
+        // and the sigmoid sums.
+        weight += 40.0 * nNodes + 10.0 * (double)sigC.size();
+    }
 
     explicit ComponentProgram(FixedMultiIndexSet const& ms) {
         D = (int)ms.Length();
@@ -182,6 +206,10 @@ struct ComponentProgram {
         cudaFree(dSlotTerm);
         cudaFree(dLeadDeg);
         cudaFree(dRowOff);
+        cudaFree(dSigC);
+        cudaFree(dSigW);
+        cudaFree(dSigWt);
+        cudaFree(dSigStart);
     }
 };
 

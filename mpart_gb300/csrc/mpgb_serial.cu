@@ -189,31 +189,57 @@ CoeffArchive readCoeffs(Reader& r) {
     return a;
 }
 
-// Monotone components of a map in output order (a component, or the
-// components of a triangular map, nested maps flattened).
-void components(const std::shared_ptr<ConditionalMapBase>& m, std::vector<const MonotoneComponent*>& out) {
-    if (auto* c = dynamic_cast<const MonotoneComponent*>(m.get())) {
-        out.push_back(c);
+// Components of a map in output order (a component, or the components of a
+// triangular map, nested maps flattened): monotone components or sigmoid
+// expansions (a map holds one kind).
+void components(const std::shared_ptr<ConditionalMapBase>& m, std::vector<const MonotoneMapBase*>& out) {
+    if (dynamic_cast<const MonotoneComponent*>(m.get()) || dynamic_cast<const SigmoidComponent*>(m.get())) {
+        out.push_back(dynamic_cast<const MonotoneMapBase*>(m.get()));
         return;
     }
     if (auto* t = dynamic_cast<TriangularMap*>(m.get())) {
         for (unsigned i = 0; i < t->NumComponents(); ++i) components(t->GetComponent(i), out);
         return;
     }
-    throw std::invalid_argument("only monotone components and triangular maps can be archived");
+    throw std::invalid_argument("only monotone components, sigmoid expansions and triangular maps can be archived");
 }
 
+const char* const kSigLabels[4] = {"Sigmoid centers", "Sigmoid widths", "Sigmoid weights", "Sigmoid starting indices"};
+
+// Map archive: tag, options, kind (0 component, 1 triangular map; +2 for
+// sigmoid expansions), component count, per component its multi-index set
+// (and, for sigmoid expansions, the Sigmoid1d arrays and edge/sum options),
+// then the coefficient archive.
 std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m) {
     auto* mono = dynamic_cast<MonotoneMapBase*>(m.get());
-    if (!mono) throw std::invalid_argument("only monotone components and triangular maps can be archived");
-    std::vector<const MonotoneComponent*> comps;
+    if (!mono) throw std::invalid_argument("only monotone components, sigmoid expansions and triangular maps can be archived");
+    std::vector<const MonotoneMapBase*> comps;
     components(m, comps);
+    const bool sig = dynamic_cast<const SigmoidComponent*>(comps[0]) != nullptr;
+    for (auto* c : comps)
+        if ((dynamic_cast<const SigmoidComponent*>(c) != nullptr) != sig)
+            throw std::invalid_argument("map archive: mixed component kinds");
     Writer w;
     w.str(kMapTag);
     writeOptions(w, mono->Options());
-    w.pod<uint32_t>(dynamic_cast<MonotoneComponent*>(m.get()) ? 0u : 1u);
+    const bool single = dynamic_cast<TriangularMap*>(m.get()) == nullptr;
+    w.pod<uint32_t>((single ? 0u : 1u) + (sig ? 2u : 0u));
     w.pod<uint32_t>((uint32_t)comps.size());
-    for (auto* c : comps) writeMset(w, c->GetMultiIndexSet());
+    for (auto* c : comps) {
+        if (sig) {
+            auto* sc = static_cast<const SigmoidComponent*>(c);
+            writeMset(w, sc->GetMultiIndexSet());
+            const Sigmoid1dParams& p = sc->GetSigmoid();
+            w.view<double>(kSigLabels[0], p.centers.data(), p.centers.size());
+            w.view<double>(kSigLabels[1], p.widths.data(), p.widths.size());
+            w.view<double>(kSigLabels[2], p.weights.data(), p.weights.size());
+            w.view<unsigned int>(kSigLabels[3], p.startInds.data(), p.startInds.size());
+            w.pod<double>(sc->Options().edgeShape);
+            w.pod<int32_t>((int32_t)sc->Options().sigmoidBasisSumType);
+        } else {
+            writeMset(w, static_cast<const MonotoneComponent*>(c)->GetMultiIndexSet());
+        }
+    }
     writeCoeffs(w, *m);
     return w.b;
 }
@@ -221,14 +247,34 @@ std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m
 std::shared_ptr<ConditionalMapBase> mapFromBytes(const unsigned char* buf, size_t size) {
     Reader r(buf, size);
     if (r.str() != kMapTag) throw std::invalid_argument("not a map archive written by this library");
-    const MapOptions o = readOptions(r);
+    MapOptions o = readOptions(r);
     const uint32_t kind = r.pod<uint32_t>();
     const uint32_t nc = r.pod<uint32_t>();
-    if (kind > 1 || nc == 0 || (kind == 0 && nc != 1)) throw std::invalid_argument("map archive: bad structure");
+    const bool single = (kind & 1u) == 0, sig = kind >= 2;
+    if (kind > 3 || nc == 0 || (single && nc != 1)) throw std::invalid_argument("map archive: bad structure");
     std::vector<std::shared_ptr<ConditionalMapBase>> comps;
-    for (uint32_t i = 0; i < nc; ++i) comps.push_back(MapFactory::CreateComponent(readMset(r), o));
+    for (uint32_t i = 0; i < nc; ++i) {
+        FixedMultiIndexSet ms = readMset(r);
+        if (sig) {
+            Sigmoid1dParams p;
+            p.centers = r.view<double>();
+            p.widths = r.view<double>();
+            p.weights = r.view<double>();
+            p.startInds = r.view<unsigned int>();
+            o.edgeShape = r.pod<double>();
+            const int32_t st = r.pod<int32_t>();
+            if (st < 0 || st > 1) throw std::invalid_argument("map archive: bad sigmoid sum type");
+            o.sigmoidBasisSumType = (SigmoidSumSizeType)st;
+            auto c = std::make_shared<SigmoidComponent>(ms, p, o);
+            std::vector<double> z(c->numCoeffs, 0.0);
+            c->SetCoeffs(z.data(), c->numCoeffs, true);
+            comps.push_back(c);
+        } else {
+            comps.push_back(MapFactory::CreateComponent(ms, o));
+        }
+    }
     std::shared_ptr<ConditionalMapBase> m =
-        kind == 0 ? comps[0] : std::shared_ptr<ConditionalMapBase>(std::make_shared<TriangularMap>(comps, true));
+        single ? comps[0] : std::shared_ptr<ConditionalMapBase>(std::make_shared<TriangularMap>(comps, true));
     const CoeffArchive a = readCoeffs(r);
     if (a.in != m->inputDim || a.out != m->outputDim || a.n != m->numCoeffs)
         throw std::invalid_argument("map archive: coefficient block does not match the map");
@@ -279,6 +325,12 @@ MapOptions optsFromC(const mpgb_map_options* o) {
     m.contDeriv = o->cont_deriv != 0;
     m.basisNorm = o->basis_norm != 0;
     m.nugget = o->nugget;
+    if (o->sigmoid_type != 0 || o->edge_type != 0 || o->sigmoid_sum_type < 0 || o->sigmoid_sum_type > 1)
+        throw std::invalid_argument("invalid sigmoid enum value in options");
+    m.sigmoidType = SigmoidTypes::Logistic;
+    m.edgeType = EdgeTypes::SoftPlus;
+    m.edgeShape = o->edge_shape;
+    m.sigmoidBasisSumType = (SigmoidSumSizeType)o->sigmoid_sum_type;
     return m;
 }
 
@@ -349,6 +401,11 @@ int mpgb_options_from_bytes(const unsigned char* buf, size_t size, mpgb_map_opti
         out->cont_deriv = m.contDeriv ? 1 : 0;
         out->basis_norm = m.basisNorm ? 1 : 0;
         out->nugget = m.nugget;
+        // (The archive has no sigmoid fields, MapOptions.h:126-130: defaults.)
+        out->sigmoid_type = (int)m.sigmoidType;
+        out->edge_type = (int)m.edgeType;
+        out->edge_shape = m.edgeShape;
+        out->sigmoid_sum_type = (int)m.sigmoidBasisSumType;
     });
 }
 

@@ -28,6 +28,19 @@ struct CompDesc {
     const int32_t* slotTerm; // [nSlots] coefficient index within the component, or -1
     const int32_t* leadDeg;  // [D-1] largest order per leading coordinate
     const int32_t* rowOff;   // [D-1] first basis row of each leading coordinate
+    // Sigmoid expansions (kBasisSigmoid launches): the Sigmoid1d parameters of
+    // the last input (centers, widths, weights; term k >= 4 sums the entries
+    // [sigStart[k-4], sigStart[k-3]) or up to sigN for the last term) and
+    // whether the leading products of terms with a last-input factor pass
+    // through the rectifier (RectifiedMultivariateExpansion) or not
+    // (UnivariateExpansion, one input).
+    const double* sigC;
+    const double* sigW;
+    const double* sigWt;
+    const int32_t* sigStart;
+    int sigN, sigNStarts;
+    int rectify;
+    int pad1_;
 };
 
 // A block's work: tiles tile0, tile0 + tileStride, ... (nTiles of them) of
