@@ -47,6 +47,7 @@ DIM, ORDER, NPTS = 8, 4, 1_000_000
 TOL, MAXSUB = 1e-6, 30
 METRIC = "fused fwd+adjoint points/s (dim-8, order-4, FP64)"
 KL_DIM, KL_ORDER, KL_N, KL_TOL, KL_ITERS = 6, 5, 200_000, 1e-7, 100
+SIG_DIM, SIG_ORDER, SIG_NSIG, SIG_N = 8, 3, 5, 1_000_000
 
 
 def synth(n, seed_pts=1, seed_sens=2):
@@ -271,6 +272,94 @@ def inverse_implicit(M, dev, cpu_seconds=8.0):
     out["cpu_inverse"] = {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
                           "sample": f"first {n2} targets, the oracle's Inverse"}
     out["inverse_speedup_vs_cpu"] = out["inverse_points_per_s"] / out["cpu_inverse"]["points_per_s"]
+    return out
+
+
+def sigmoid_centers(num_sig, bound=3.0):
+    """Edge centers at +-bound and, for term k, k centers spread over the
+    range (the Linear sum of the reference's sigmoid factory test)."""
+    c = [-bound, bound]
+    for k in range(1, num_sig + 1):
+        c += [1.9 * bound * (j - (k - 1) / 2) / max(k - 1, 1) for j in range(k)]
+    return np.array(c)
+
+
+def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
+    """Sigmoid expansions (CreateSigmoidTriangular): an 8-D TriangularMap of
+    RectifiedMultivariateExpansion components, total order 3, 5 sigmoid terms
+    (Linear sums), HermiteFunctions + SoftPlus rectifier, 1,000,000 points
+    N(0, I): the fused forward + log-determinant + coefficient adjoint, and
+    the batched KL step; the oracle's four reference calls on a sample of the
+    same points on the host cores."""
+    import torch
+    opts = M.MapOptions(basisType=M.BasisTypes.HermiteFunctions, posFuncType=M.PosFuncTypes.SoftPlus)
+    cen = np.column_stack([sigmoid_centers(SIG_NSIG)] * SIG_DIM)
+    tm = M.CreateSigmoidTriangular(SIG_DIM, SIG_DIM, SIG_ORDER, cen, opts)
+    lb, _ = tm.CoeffBounds()
+    rng = np.random.default_rng(41)
+    coef = rng.normal(0.0, 0.05, tm.numCoeffs)
+    coef[lb == 0.0] = np.abs(coef[lb == 0.0]) + 0.01
+    tm.SetCoeffs(coef)
+    xh = rng.standard_normal((SIG_DIM, SIG_N))
+    sh = rng.standard_normal((SIG_DIM, SIG_N))
+    x = torch.as_tensor(xh, device=dev)
+    s = torch.as_tensor(sh, device=dev)
+    ev = torch.zeros(SIG_DIM, SIG_N, dtype=torch.float64, device=dev)
+    ld = torch.zeros(SIG_N, dtype=torch.float64, device=dev)
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
+    step = lambda: tm.FusedForwardAdjointImpl(x, sens=s, logdet_sens_scale=1.0, out_eval=ev, out_logdet=ld,
+                                              coeff_grad=cg)
+    kl = lambda: tm.KLObjective(x)
+
+    def timed(f):
+        for _ in range(3):
+            f()
+        torch.cuda.synchronize()
+        ms = []
+        for k in range(steps):
+            flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            f()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    ms_fused = timed(step)
+    ms_kl = timed(kl)
+    out = {"workload": f"sigmoid TriangularMap {SIG_DIM}-D (RectifiedMultivariateExpansion components), total order "
+                       f"{SIG_ORDER}, {SIG_NSIG} sigmoid terms (Linear), HermiteFunctions + SoftPlus, "
+                       f"{tm.numCoeffs} coefficients, {SIG_N} points N(0, I); fused Evaluate + LogDeterminant + "
+                       f"CoeffGrad + LogDeterminantCoeffGrad (coefficient adjoint summed over points)",
+           "points": SIG_N, "coefficients": tm.numCoeffs, "fused_ms": ms_fused,
+           "fused_points_per_s": SIG_N / (ms_fused * 1e-3), "kl_step_ms": ms_kl,
+           "l2": "flushed between steps (256 MB write)"}
+    # the oracle on a bounded sample: the reference's four calls per component
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    om = O.sigmoid_triangular(SIG_DIM, SIG_DIM, SIG_ORDER, cen, 1.5, O.SUM_LINEAR, O.POS_SOFTPLUS)
+
+    def cpu(n):
+        xs, ss = xh[:, :n], sh[:, :n]
+        t0 = time.perf_counter()
+        om.evaluate(coef, xs)
+        om.logdet(coef, xs)
+        om.coeff_grad(coef, xs, ss).sum(axis=1)
+        om.logdet_coeff_grad(coef, xs).sum(axis=1)
+        return time.perf_counter() - t0
+
+    n = 2000
+    dt = cpu(n)
+    n2 = int(min(SIG_N, max(n, n * cpu_seconds / max(dt, 1e-6))))
+    dt = cpu(n2)
+    out["cpu_baseline"] = {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
+                           "sample": f"first {n2} of the {SIG_N} points, the oracle's Evaluate + LogDeterminant + "
+                                     f"CoeffGrad + LogDeterminantCoeffGrad per component, gradients summed"}
+    out["speedup_vs_cpu"] = out["fused_points_per_s"] / out["cpu_baseline"]["points_per_s"]
     return out
 
 
@@ -661,6 +750,8 @@ def run_gpu(args):
         line["batch_maps"] = batch_maps(M, dev)
     if not args.no_inverse:
         line["inverse_implicit"] = inverse_implicit(M, dev)
+    if not args.no_sigmoid:
+        line["sigmoid_maps"] = sigmoid_maps(M, dev)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -702,6 +793,7 @@ def main():
     ap.add_argument("--no-kl", action="store_true", help="skip the KL training workload")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
+    ap.add_argument("--no-sigmoid", action="store_true", help="skip the sigmoid-expansion workload")
     ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce", "kl"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
