@@ -292,6 +292,16 @@ struct KLPlan {
     std::vector<int> lossOff;  // first entry of each component in lossSlots
     DevBuf items, rowBase, lossSlots;
     size_t partialDoubles = 0;
+    // The step's reductions (one launch for all components).
+    DevBuf reduceDesc;
+    int nReduce = 0, maxTerms = 0;
+    // Processing order of the samples: sorted once per sample array (the
+    // points of a training run do not change between steps).  Any
+    // permutation gives the same results up to summation order, so a stale
+    // order after the caller rewrites the array in place costs only speed.
+    DevBuf perm;
+    const double* permPts = nullptr;
+    long long permRs = 0, permCs = 0;
 };
 
 struct MapWorkspace {
@@ -1084,7 +1094,57 @@ static KLPlan& klPlan(MapWorkspace& W, const std::vector<MonotoneMapBase::Part>&
         MPGB_CUDA(cudaMemcpy(P.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice));
         MPGB_CUDA(cudaMemcpy(P.lossSlots.p, ls.data(), ls.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
+    std::vector<KLReduceDesc> rd;
+    for (size_t c = 0; c < parts.size(); ++c) {
+        if (onlyComp >= 0 && (int)c != onlyComp) continue;
+        KLReduceDesc q{};
+        q.rowOff = P.rowOff[c];
+        q.nRows = P.rowOff[c + 1] - P.rowOff[c];
+        q.nTerms = parts[c].prog->numTerms;
+        q.outOff = (int)parts[c].mapCoeffOffset;
+        q.lossOff = P.lossOff[c];
+        q.nLoss = P.lossOff[c + 1] - P.lossOff[c];
+        q.comp = (int)c;
+        rd.push_back(q);
+        P.maxTerms = std::max(P.maxTerms, q.nTerms);
+    }
+    P.nReduce = (int)rd.size();
+    P.reduceDesc.ensure(std::max<size_t>(1, rd.size()) * sizeof(KLReduceDesc), stream);
+    if (!rd.empty())
+        MPGB_CUDA(cudaMemcpy(P.reduceDesc.p, rd.data(), rd.size() * sizeof(KLReduceDesc), cudaMemcpyHostToDevice));
     return P;
+}
+
+// The KL step's processing order, kept in the plan (see KLPlan::perm).  An
+// order computed inside a stream capture is not kept: its sort has not run.
+static void orderPointsKL(MapWorkspace& W, KLPlan& P, const std::vector<MonotoneMapBase::Part>& parts,
+                          StridedMatrix const& pts, FusedParams& p, int onlyComp, cudaStream_t stream) {
+    p.perm = nullptr;
+    p.permStride = 0;
+    const long long N = pts.cols;
+    if (!W.ordering || N < 2 * kTpb) return;
+    if (P.permPts != pts.data || P.permRs != pts.rowStride || P.permCs != pts.colStride) {
+        const size_t nComps = parts.size();
+        P.perm.ensure(nComps * (size_t)N * sizeof(int), stream);
+        W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
+        for (size_t c = 0; c < nComps; ++c) {
+            if (onlyComp >= 0 && (int)c != onlyComp) continue;
+            const double* xd = pts.data + (int64_t)(parts[c].prog->D - 1) * pts.rowStride;
+            MPGB_CUDA(launchSortByLast(xd, pts.colStride, N, W.sortHist.as<int>(), P.perm.as<int>() + c * (size_t)N,
+                                       stream));
+        }
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        MPGB_CUDA(cudaStreamIsCapturing(stream, &cs));
+        if (cs == cudaStreamCaptureStatusNone) {
+            P.permPts = pts.data;
+            P.permRs = pts.rowStride;
+            P.permCs = pts.colStride;
+        } else {
+            P.permPts = nullptr;
+        }
+    }
+    p.perm = P.perm.as<int>();
+    p.permStride = N;
 }
 
 void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream) {
@@ -1112,18 +1172,13 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     p.partials = W.partials.as<double>();
     p.lossPartials = W.lossPart.as<double>();
     p.items = P.items.as<WorkItem>();
-    orderPoints(W, parts_, pts, p, onlyComp, stream);
+    orderPointsKL(W, P, parts_, pts, p, onlyComp, stream);
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
     MPGB_CUDA(launchFused(W.basis, posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
-    for (int c = 0; c < (int)parts_.size(); ++c) {
-        if (onlyComp >= 0 && c != onlyComp) continue;
-        const int nr = P.rowOff[c + 1] - P.rowOff[c];
-        MPGB_CUDA(launchReduceRows(W.partials.as<double>(), P.rowBase.as<long long>() + P.rowOff[c], nr,
-                                   parts_[c].prog->numTerms, 1.0, grad + parts_[c].mapCoeffOffset, 0, stream));
-        MPGB_CUDA(launchSumLoss(W.lossPart.as<double>(), P.lossSlots.as<int>() + P.lossOff[c],
-                                P.lossOff[c + 1] - P.lossOff[c], 1.0 / (double)N, lossPerComp + c, stream));
-    }
+    MPGB_CUDA(launchKLReduce(W.partials.as<double>(), P.rowBase.as<long long>(), P.reduceDesc.as<KLReduceDesc>(),
+                             P.nReduce, P.maxTerms, grad, W.lossPart.as<double>(), P.lossSlots.as<int>(),
+                             1.0 / (double)N, lossPerComp, stream));
     Finish(stream, "KLObjective");
 }
 

@@ -1,4 +1,5 @@
 // Dispatch of the fused/inverse kernels and the small helper kernels.
+#include <algorithm>
 #include <atomic>
 
 #include "mpgb_types.h"
@@ -116,6 +117,34 @@ __global__ void keyScatterKernel(const double* xd, long long stride, long long N
             if (rank == 0) cnt[key] = slot + __popc(grp);
         }
         __syncwarp();
+    }
+}
+
+// The per-component reductions of a KL step in one launch (blockIdx.y =
+// component): gradient rows exactly as reduceRowsKernel with scale 1, the
+// loss exactly as sumLossKernel, so results equal the per-component launches.
+__global__ void klReduceKernel(const double* part, const long long* rowBase, const KLReduceDesc* descs,
+                               double* grad, const double* lossPart, const int* lossSlots, double lossScale,
+                               double* loss) {
+    __shared__ double red[8][33];
+    const KLReduceDesc q = descs[blockIdx.y];
+    const int t = blockIdx.x * 32 + threadIdx.x;
+    const int g = threadIdx.y;
+    const long long* rb = rowBase + q.rowOff;
+    double s = 0.0;
+    if (t < q.nTerms)
+        for (int r = g; r < q.nRows; r += 8) s += part[rb[r] + t];
+    red[g][threadIdx.x] = s;
+    __syncthreads();
+    if (g == 0 && t < q.nTerms) {
+        double v = 0.0;
+        for (int k = 0; k < 8; ++k) v += red[k][threadIdx.x];
+        grad[q.outOff + t] = v;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+        double l = 0.0;
+        for (int j = 0; j < q.nLoss; ++j) l += lossPart[lossSlots[q.lossOff + j]];
+        loss[q.comp] = l * lossScale;
     }
 }
 
@@ -297,6 +326,17 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
     if (nTerms <= 0) return cudaSuccess;
     dim3 blk(32, 8);
     reduceRowsKernel<<<(nTerms + 31) / 32, blk, 0, stream>>>(part, rowBase, nRows, nTerms, scale, out, accumulate);
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
+    return e;
+}
+
+cudaError_t launchKLReduce(const double* part, const long long* rowBase, const KLReduceDesc* descs, int nComps,
+                           int maxTerms, double* grad, const double* lossPart, const int* lossSlots, double lossScale,
+                           double* loss, cudaStream_t stream) {
+    if (nComps <= 0) return cudaSuccess;
+    dim3 grid((unsigned)std::max(1, (maxTerms + 31) / 32), (unsigned)nComps), blk(32, 8);
+    klReduceKernel<<<grid, blk, 0, stream>>>(part, rowBase, descs, grad, lossPart, lossSlots, lossScale, loss);
     const cudaError_t e = cudaGetLastError();
     countLaunches(stream, 1);
     return e;

@@ -26,6 +26,10 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
                              double* out, int accumulate, cudaStream_t stream);
 cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
                           cudaStream_t stream);
+// All per-component reductions of a KL step (descs: device array of nComps).
+cudaError_t launchKLReduce(const double* part, const long long* rowBase, const KLReduceDesc* descs, int nComps,
+                           int maxTerms, double* grad, const double* lossPart, const int* lossSlots, double lossScale,
+                           double* loss, cudaStream_t stream);
 // Stable counting sort of points by |x_D|: perm[j] = index of the j-th point.
 size_t sortScratchInts(long long N);
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,

@@ -73,6 +73,14 @@ enum FusedFlags : int {
     kFlagImplicitFirst = 512,  // with kFlagImplicit: the sums start at zero (first launch)
 };
 
+// One component's reductions at the end of a KL step: its partial rows
+// [rowOff, rowOff + nRows) of rowBase into grad[outOff .. outOff + nTerms) and
+// its loss partials [lossOff, lossOff + nLoss) of lossSlots into loss[comp].
+struct KLReduceDesc {
+    int rowOff, nRows, nTerms, outOff;
+    int lossOff, nLoss, comp, pad_;
+};
+
 // Point data of one component in a batch of maps (the launch-wide fields of
 // FusedParams with the same names, per component).
 struct PointIO {
