@@ -302,6 +302,7 @@ struct KLPlan {
     DevBuf perm;
     const double* permPts = nullptr;
     long long permRs = 0, permCs = 0;
+    long long rcTotal = 0;  // rectifier cache of sigmoid expansions (doubles)
 };
 
 struct MapWorkspace {
@@ -319,6 +320,7 @@ struct MapWorkspace {
     std::vector<std::unique_ptr<KLPlan>> klPlans;
     DevBuf perm, sortHist;
     DevBuf implicitAcc;  // back-substitution sums when the caller wants no input gradient
+    DevBuf rcache;       // rectifier cache of sigmoid expansions (reduced adjoints)
     bool ordering = true;
 };
 
@@ -541,6 +543,7 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
             c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
             c.sigC = p.dSigC; c.sigW = p.dSigW; c.sigWt = p.dSigWt; c.sigStart = p.dSigStart;
             c.sigN = (int)p.sigC.size(); c.sigNStarts = (int)p.sigStart.size(); c.rectify = p.kind == 1 ? 1 : 0;
+            c.nodeCIdx = p.dNodeCIdx;
             W.hostComps.push_back(c);
             slotOff += p.nSlots;
             pm = std::max(pm, p.P);
@@ -683,7 +686,8 @@ static std::vector<WorkItem> itemsAllComps(long long N, int nComps) {
 // item the same mix of cheap and expensive tiles.
 static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Part>& parts, long long N, int numSMs,
                                           bool reduced, std::vector<long long>* rowBaseOut,
-                                          std::vector<std::vector<int>>* itemsOfComp, int onlyComp = -1) {
+                                          std::vector<std::vector<int>>* itemsOfComp, int onlyComp = -1,
+                                          long long* rcTotal = nullptr) {
     const int nComps = (int)parts.size();
     const long long nTiles = (N + kTpb - 1) / kTpb;
     std::vector<int> order;
@@ -698,10 +702,14 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
         const long long nItemsC =
             reduced ? std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * 4)) : nTiles;
         for (long long t = 0; t < nItemsC; ++t) {
-            WorkItem w{c, c + 1, (int)t, (int)((nTiles - t + nItemsC - 1) / nItemsC), 0, 0, (int)nItemsC};
+            WorkItem w{c, c + 1, (int)t, (int)((nTiles - t + nItemsC - 1) / nItemsC), 0, 0, (int)nItemsC, 0};
             if (reduced) {
                 w.partialBase = base;
                 w.lossSlot = (int)v.size();
+                if (rcTotal) {
+                    w.rcBase = *rcTotal;
+                    *rcTotal += (long long)parts[c].prog->nCNodes * kTpb;
+                }
                 for (int sg = 0; sg < parts[c].prog->cSegs; ++sg) {
                     if (rowBaseOut) rowBaseOut->push_back(base);
                     base += parts[c].prog->numTerms;
@@ -712,6 +720,14 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
         }
     }
     return v;
+}
+
+// The rectifier cache of a reduced sigmoid-expansion launch (rcTotal doubles,
+// from itemsPerComp).  Above 2 GiB the reduction evaluates the rectifier again.
+static double* rectCache(MapWorkspace& W, long long rcTotal, cudaStream_t stream) {
+    if (W.basis != kBasisSigmoid || rcTotal <= 0 || rcTotal > (2LL << 30) / (long long)sizeof(double)) return nullptr;
+    W.rcache.ensure((size_t)rcTotal * sizeof(double), stream);
+    return W.rcache.as<double>();
 }
 
 static void uploadItems(MapWorkspace& W, const std::vector<WorkItem>& items, cudaStream_t stream) {
@@ -961,12 +977,14 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
     if (wantCoef || !outEval.empty() || wantLogDet) {
         std::vector<long long> rowBase;
         std::vector<std::vector<int>> itemsOf;
-        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf);
+        long long rcTotal = 0;
+        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf, -1, &rcTotal);
         uploadItems(W, items, stream);
         FusedParams p{};
         baseParams(W, opts_, p, N);
         p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
         p.flags = 0;
+        if (wantCoef) p.rcache = rectCache(W, rcTotal, stream);
         orderPoints(W, parts_, pts, p, -1, stream);
         if (!outEval.empty()) {
             p.flags |= kFlagEval;
@@ -1066,7 +1084,7 @@ static KLPlan& klPlan(MapWorkspace& W, const std::vector<MonotoneMapBase::Part>&
     P.N = N;
     P.onlyComp = onlyComp;
     std::vector<long long> rowBase;
-    auto items = itemsPerComp(parts, N, W.numSMs, true, &rowBase, &P.itemsOf, onlyComp);
+    auto items = itemsPerComp(parts, N, W.numSMs, true, &rowBase, &P.itemsOf, onlyComp, &P.rcTotal);
     P.nItems = (int)items.size();
     for (auto& it : items)
         P.partialDoubles = std::max<size_t>(P.partialDoubles, (size_t)it.partialBase + (size_t)parts[it.c0].prog->numTerms *
@@ -1172,6 +1190,7 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     p.partials = W.partials.as<double>();
     p.lossPartials = W.lossPart.as<double>();
     p.items = P.items.as<WorkItem>();
+    p.rcache = rectCache(W, P.rcTotal, stream);
     orderPointsKL(W, P, parts_, pts, p, onlyComp, stream);
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
@@ -1223,10 +1242,12 @@ void MonotoneMapBase::InverseCoeffGrad(StridedMatrix const& pts, StridedMatrix c
         const int c = order[q];
         std::vector<long long> rowBase;
         std::vector<std::vector<int>> itemsOf;
-        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf, c);
+        long long rcTotal = 0;
+        auto items = itemsPerComp(parts_, N, W.numSMs, wantCoef, &rowBase, &itemsOf, c, &rcTotal);
         uploadItems(W, items, stream);
         FusedParams p{};
         baseParams(W, opts_, p, N);
+        if (wantCoef) p.rcache = rectCache(W, rcTotal, stream);
         p.flags = kFlagInput | kFlagImplicit | (q == 0 ? kFlagImplicitFirst : 0) | (wantCoef ? kFlagCoefReduced : 0);
         p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
         p.sens = w.data; p.sensRs = w.rowStride; p.sensCs = w.colStride;

@@ -433,7 +433,7 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
 // (MultivariateExpansionWorker.h:423-441).
 template <int PMAX, int POS>
 __device__ __forceinline__ void phaseARect(const CompDesc& c, const SmemLayout& L, int tid, const double* cm,
-                                           double* a) {
+                                           double* a, double* rc) {
 #pragma unroll
     for (int k = 0; k <= PMAX; ++k) a[k] = 0.0;
     const int tpb = blockDim.x;
@@ -451,7 +451,11 @@ __device__ __forceinline__ void phaseARect(const CompDesc& c, const SmemLayout& 
         if (nk) {
             const double* cs = cm + __ldg(&c.nodeSlot[n]);
             const double a0 = fma(__ldg(&cs[0]), phi, a[0]);
-            const double r = (c.rectify && nk > 1) ? posValue<POS>(phi) : phi;
+            double r = phi;
+            if (c.rectify && nk > 1) {
+                r = posValue<POS>(phi);
+                if (rc) rc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = r;
+            }
             accumCoeffs<PMAX>(nk, r, cs, a);
             a[0] = a0;
         }
@@ -503,7 +507,12 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             else fillLead<BASIS, false>(c, L, tid, prm.bc);
 
             double a[PMAX + 1];
-            if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, a);
+            // (sigmoid expansions: the rectified products R(Phi_m) of this tile,
+            // kept for the reduction below)
+            double* rc = nullptr;
+            if constexpr (BASIS == kBasisSigmoid)
+                if (prm.rcache && (flags & kFlagCoefReduced)) rc = prm.rcache + item.rcBase;
+            if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, a, rc);
             else phaseA<PMAX>(c, L, tid, cm, a);
             const double xd = L.X[(c.D - 1) * tpb + tid];
 
@@ -717,7 +726,8 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                         const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
                         if constexpr (BASIS == kBasisSigmoid) {
                             const double a0 = fma(phi, L.W[j], acc[0]);
-                            const double rv = (c.rectify && nk > 1) ? posValue<POS>(phi) : phi;
+                            double rv = phi;
+                            if (c.rectify && nk > 1) rv = rc ? rc[(long long)n * tpb + j] : posValue<POS>(phi);
                             accumSlots<PMAX>(nk, rv, L.W + j, tpb, acc);
                             acc[0] = a0;
                         } else {
@@ -977,7 +987,7 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
         const double* cm = prm.cm + c.slotOffset;
         fillLead<BASIS, false>(c, L, tid, prm.bc);
         ACoef<PMAX> A;
-        if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a);
+        if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a, nullptr);
         else phaseA<PMAX>(c, L, tid, cm, A.a);
         double result = nan;
         int info = 0;

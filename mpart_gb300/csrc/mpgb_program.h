@@ -50,10 +50,10 @@ struct ComponentProgram {
     int D = 0, P = 0, nB = 0, nNodes = 0, nSlots = 0, nCNodes = 0, maxDepth = 0, numTerms = 0;
     std::vector<uint32_t> nodeA, nodeSlot, nodeC;
     std::vector<uint16_t> nodeCRows;
-    std::vector<int32_t> slotTerm, leadDeg, rowOff;
+    std::vector<int32_t> slotTerm, leadDeg, rowOff, nodeCIdx;
     uint32_t *dNodeA = nullptr, *dNodeSlot = nullptr, *dNodeC = nullptr;
     uint16_t* dNodeCRows = nullptr;
-    int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr;
+    int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr, *dNodeCIdx = nullptr;
     // Work per point (FP64 operations of phases A and C), for load balancing.
     double weight = 1.0;
     // Reduced adjoint: the tile's points are split into cSegs segments and the
@@ -176,6 +176,11 @@ struct ComponentProgram {
             return nkOf[a] < nkOf[b];
         });
         nCNodes = (int)cn.size();
+        {
+            std::vector<int> cOf(tn.size(), -1);
+            for (int j = 0; j < nCNodes; ++j) cOf[cn[j]] = j;
+            for (int n : order) nodeCIdx.push_back(cOf[n]);
+        }
         nodeCRows.assign((size_t)nCNodes * kMaxDepth, 0);
         double opsA = 0, opsC = 0;
         for (int j = 0; j < nCNodes; ++j) {
@@ -197,6 +202,7 @@ struct ComponentProgram {
         dSlotTerm = toDevice(slotTerm);
         dLeadDeg = toDevice(leadDeg);
         dRowOff = toDevice(rowOff);
+        dNodeCIdx = toDevice(nodeCIdx);
     }
     ~ComponentProgram() {
         cudaFree(dNodeA);
@@ -206,6 +212,7 @@ struct ComponentProgram {
         cudaFree(dSlotTerm);
         cudaFree(dLeadDeg);
         cudaFree(dRowOff);
+        cudaFree(dNodeCIdx);
         cudaFree(dSigC);
         cudaFree(dSigW);
         cudaFree(dSigWt);

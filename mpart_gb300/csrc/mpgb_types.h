@@ -41,6 +41,7 @@ struct CompDesc {
     int sigN, sigNStarts;
     int rectify;
     int pad1_;
+    const int32_t* nodeCIdx;  // [nNodes] index of the node in nodeC, or -1 (sigmoid rectifier cache)
 };
 
 // A block's work: tiles tile0, tile0 + tileStride, ... (nTiles of them) of
@@ -53,6 +54,7 @@ struct WorkItem {
     long long partialBase;  // first double of this item's partial rows (cSegs rows of numTerms; reduced adjoint)
     int lossSlot;           // index into the loss partials (KL)
     int tileStride;         // distance between consecutive tiles of the item (>= 1)
+    long long rcBase;       // first double of this item's rectifier cache (sigmoid expansions, reduced adjoint)
 };
 
 enum FusedFlags : int {
@@ -117,6 +119,10 @@ struct FusedParams {
     // perm[c * permStride + j] (items of one component only).
     const int* perm; long long permStride;
     const PointIO* ioTable;  // batch launches: point data per component (indexed by WorkItem::c0)
+    // Sigmoid expansions with a reduced adjoint: R(Phi_m) of phase A kept for
+    // the reduction, nCNodes x blockDim doubles per item at WorkItem::rcBase
+    // (null: the reduction evaluates the rectifier again).
+    double* rcache;
     double nugget;
     int dmax, nBmax, depthMax;
     int negRows;            // kFlagImplicit: rows [0, negRows) of outInput are negated when written

@@ -230,3 +230,33 @@ def test_sigmoid_archive_round_trip(gpu):
         M.TriangularMap([M.CreateComponent(M.FixedMultiIndexSet(1, 2)),
                          M.CreateSigmoidComponent(2, 1, _centers(rng, 2, 0),
                                                   _opts(M, 1, 0))], True).Evaluate(T(np.zeros((2, 4))))
+
+
+def test_sigmoid_map_torch_autograd(gpu, oracle):
+    """TorchConditionalMapBase over a sigmoid TriangularMap: the backward pass
+    (one fused adjoint call) against the oracle's CoeffGrad + LogDeterminantCoeffGrad
+    and Gradient + LogDeterminantInputGrad."""
+    M, O = gpu, oracle
+    import torch
+    rng = np.random.default_rng(21)
+    dim, order = 3, 2
+    cen = np.column_stack([_centers(rng, 3, 1) for _ in range(dim)])
+    tri = M.CreateSigmoidTriangular(dim, dim, order, cen, _opts(M, 0, 1))
+    otri = O.sigmoid_triangular(dim, dim, order, cen, 1.5, 1, O.POS_EXP)
+    lb, _ = tri.CoeffBounds()
+    c = rng.normal(0.0, 0.1, tri.numCoeffs)
+    c[lb == 0.0] = np.abs(c[lb == 0.0]) + 0.05
+    tri.SetCoeffs(c)
+    mod = tri.torch(store_coeffs=True, return_logdet=True)
+    x = rng.normal(size=(dim, 1500))
+    xt = torch.tensor(x.T, dtype=torch.float64, device="cuda", requires_grad=True)
+    y, ld = mod(xt)
+    loss = (y * y).sum() + 0.5 * ld.sum()
+    loss.backward()
+    yo = otri.evaluate(c, x)
+    ref_c = otri.coeff_grad(c, x, 2.0 * yo).sum(axis=1) + 0.5 * otri.logdet_coeff_grad(c, x).sum(axis=1)
+    ref_x = otri.gradient(c, x, 2.0 * yo) + 0.5 * otri.logdet_input_grad(c, x)
+    assert_parity(H(y).T, yo, what="torch forward")
+    assert_parity(H(ld), otri.logdet(c, x), what="torch log-determinant")
+    assert_parity(H(mod.coeffs.grad), ref_c, floor=1e-3, what="torch coefficient gradient")
+    assert_parity(H(xt.grad).T, ref_x, what="torch input gradient")
