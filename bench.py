@@ -284,13 +284,10 @@ def sigmoid_centers(num_sig, bound=3.0):
     return np.array(c)
 
 
-def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
-    """Sigmoid expansions (CreateSigmoidTriangular): an 8-D TriangularMap of
-    RectifiedMultivariateExpansion components, total order 3, 5 sigmoid terms
-    (Linear sums), HermiteFunctions + SoftPlus rectifier, 1,000,000 points
-    N(0, I): the fused forward + log-determinant + coefficient adjoint, and
-    the batched KL step; the oracle's four reference calls on a sample of the
-    same points on the host cores."""
+def sigmoid_setup(M, dev):
+    """The sigmoid workload: an 8-D sigmoid TriangularMap (total order 3, 5
+    Linear sigmoid terms, HermiteFunctions + SoftPlus), coefficients with
+    non-negative diagonal terms, 1,000,000 points N(0, I) and sensitivities."""
     import torch
     opts = M.MapOptions(basisType=M.BasisTypes.HermiteFunctions, posFuncType=M.PosFuncTypes.SoftPlus)
     cen = np.column_stack([sigmoid_centers(SIG_NSIG)] * SIG_DIM)
@@ -307,9 +304,19 @@ def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
     ev = torch.zeros(SIG_DIM, SIG_N, dtype=torch.float64, device=dev)
     ld = torch.zeros(SIG_N, dtype=torch.float64, device=dev)
     cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device=dev)
-    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
     step = lambda: tm.FusedForwardAdjointImpl(x, sens=s, logdet_sens_scale=1.0, out_eval=ev, out_logdet=ld,
                                               coeff_grad=cg)
+    return tm, cen, coef, xh, sh, x, step
+
+
+def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
+    """Sigmoid expansions (CreateSigmoidTriangular, see sigmoid_setup): the
+    fused forward + log-determinant + coefficient adjoint and the batched KL
+    step on 1,000,000 points; the oracle's four reference calls on a sample
+    of the same points on the host cores."""
+    import torch
+    tm, cen, coef, xh, sh, x, step = sigmoid_setup(M, dev)
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device=dev)
     kl = lambda: tm.KLObjective(x)
 
     def timed(f):
@@ -630,7 +637,10 @@ def run_gpu(args):
             "logdet": lambda: comp.LogDeterminantImpl(x, out_ld),
             "reduce": lambda: comp.FusedForwardAdjointImpl(x, logdet_sens_scale=1.0, coeff_grad=cg),
         }
-        if args.variant == "kl":
+        if args.variant == "sigmoid":
+            # The sigmoid workload's fused step (see sigmoid_setup).
+            step = sigmoid_setup(M, dev)[-1]
+        elif args.variant == "kl":
             # The KL training workload's step at trained coefficients (100
             # L-BFGS iterations with direct launches first); the profiled
             # calls sit in the NVTX range "kl_step".
@@ -794,7 +804,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
     ap.add_argument("--no-sigmoid", action="store_true", help="skip the sigmoid-expansion workload")
-    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce", "kl"],
+    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
     if args.impl == "reference":
