@@ -306,7 +306,7 @@ struct KLPlan {
 };
 
 struct MapWorkspace {
-    DevBuf comps, cm, gather, items, partials, rowBase, lossPart, lossSlots, logdetRows, status;
+    DevBuf comps, cm, gather, items, partials, rowBase, lossPart, lossSlots, logdetRows, status, reduceDesc;
     DevBuf stage[8];
     std::vector<CompDesc> hostComps;
     std::vector<GatherDescHost> hostGather;
@@ -743,7 +743,8 @@ static void orderPoints(MapWorkspace& W, const std::vector<MonotoneMapBase::Part
     p.perm = nullptr;
     p.permStride = 0;
     const long long N = pts.cols;
-    if (!W.ordering || N < 2 * kTpb) return;
+    // (Sigmoid expansions have no quadrature: every point costs the same.)
+    if (!W.ordering || N < 2 * kTpb || W.basis == kBasisSigmoid) return;
     const size_t nComps = parts.size();
     W.perm.ensure(nComps * (size_t)N * sizeof(int), stream);
     W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
@@ -1013,18 +1014,10 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
             needJ = sens.empty() ? 0 : 1;
         }
         if (wantLogDet) {
-            // The kernel adds log-dets over its component range and writes them at
-            // outLogDet[i]; with one component per item, offset rows by component.
-            // Launch per component so that each writes its own row.
-            for (int c = 0; c < nComps; ++c) {
-                std::vector<WorkItem> sub;
-                for (int id : itemsOf[c]) sub.push_back(items[id]);
-                uploadItems(W, sub, stream);
-                FusedParams q = p;
-                q.outLogDet = W.logdetRows.as<double>() + (size_t)c * N;
-                launch(W, opts_, q, (int)sub.size(), needJ, 0, stream);
-            }
-            uploadItems(W, items, stream);
+            // One component per item: each writes its component's row of the
+            // scratch, summed in component order below.
+            p.logDetCompStride = N;
+            launch(W, opts_, p, (int)items.size(), needJ, 0, stream);
             sumRowsKernel<<<(unsigned)((N + 255) / 256), 256, 0, stream>>>(
                 W.logdetRows.as<double>(), nComps, N, outLogDet.data,
                 (outLogDet.rows == 1) ? outLogDet.colStride : outLogDet.rowStride);
@@ -1044,14 +1037,26 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
             }
             MPGB_CUDA(cudaMemcpyAsync(W.rowBase.p, rb.data(), rb.size() * sizeof(long long), cudaMemcpyHostToDevice,
                                       stream));
-            size_t off = 0;
+            // Every component's rows in one launch.
+            std::vector<KLReduceDesc> rd(nComps);
+            int off = 0, maxTerms = 0;
             for (int c = 0; c < nComps; ++c) {
-                const int nr = (int)itemsOf[c].size() * parts_[c].prog->cSegs;
-                MPGB_CUDA(launchReduceRows(W.partials.as<double>(), W.rowBase.as<long long>() + off, nr,
-                                           parts_[c].prog->numTerms, 1.0, coeffGrad + parts_[c].mapCoeffOffset, 0,
-                                           stream));
-                off += nr;
+                KLReduceDesc& q = rd[c];
+                q = KLReduceDesc{};
+                q.rowOff = off;
+                q.nRows = (int)itemsOf[c].size() * parts_[c].prog->cSegs;
+                q.nTerms = parts_[c].prog->numTerms;
+                q.outOff = (int)parts_[c].mapCoeffOffset;
+                q.comp = c;
+                off += q.nRows;
+                maxTerms = std::max(maxTerms, q.nTerms);
             }
+            W.reduceDesc.ensure(rd.size() * sizeof(KLReduceDesc), stream);
+            MPGB_CUDA(cudaMemcpyAsync(W.reduceDesc.p, rd.data(), rd.size() * sizeof(KLReduceDesc),
+                                      cudaMemcpyHostToDevice, stream));
+            MPGB_CUDA(launchKLReduce(W.partials.as<double>(), W.rowBase.as<long long>(),
+                                     W.reduceDesc.as<KLReduceDesc>(), nComps, maxTerms, coeffGrad, nullptr, nullptr,
+                                     1.0, nullptr, stream));
         }
     }
     // Pass 2: input gradient (sums over components per point).
@@ -1140,7 +1145,7 @@ static void orderPointsKL(MapWorkspace& W, KLPlan& P, const std::vector<Monotone
     p.perm = nullptr;
     p.permStride = 0;
     const long long N = pts.cols;
-    if (!W.ordering || N < 2 * kTpb) return;
+    if (!W.ordering || N < 2 * kTpb || W.basis == kBasisSigmoid) return;
     if (P.permPts != pts.data || P.permRs != pts.rowStride || P.permCs != pts.colStride) {
         const size_t nComps = parts.size();
         P.perm.ensure(nComps * (size_t)N * sizeof(int), stream);

@@ -141,7 +141,7 @@ __global__ void klReduceKernel(const double* part, const long long* rowBase, con
         for (int k = 0; k < 8; ++k) v += red[k][threadIdx.x];
         grad[q.outOff + t] = v;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+    if (loss && blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
         double l = 0.0;
         for (int j = 0; j < q.nLoss; ++j) l += lossPart[lossSlots[q.lossOff + j]];
         loss[q.comp] = l * lossScale;

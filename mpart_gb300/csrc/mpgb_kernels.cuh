@@ -751,7 +751,9 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
         }  // components
 
         if (active) {
-            if (flags & kFlagLogDet) MPGB_IO(outLogDet)[i * MPGB_IO(logDetStride)] = logdetSum;
+            if (flags & kFlagLogDet)
+                MPGB_IO(outLogDet)[(BATCH ? 0 : item.c0 * prm.logDetCompStride) + i * MPGB_IO(logDetStride)] =
+                    logdetSum;
             if (inputMode) {
                 const int dneed2 = prm.comps[item.c1 - 1].D;
                 for (int d = 0; d < dneed2; ++d) {
@@ -791,10 +793,11 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
 // rows, log-det scratch row, partial row), so results do not depend on which
 // block runs it.  The item's component selects the body compiled for the
 // smallest order class >= its last-coordinate order.  At most 128 threads a
-// block and 4 blocks an SM: the order-6 and order-8 bodies spill a little
-// there, the order-2 and order-4 bodies (most items) keep four blocks.
+// block; the register budget of 2 blocks an SM keeps the order-6 and order-8
+// bodies free of spills (with 4 blocks an SM they spilled, and the 64-map
+// workload ran 11 % slower).
 template <int BASIS, int POS>
-__global__ void __launch_bounds__(128, 4) batchKernel(const __grid_constant__ FusedParams prm, int nItems,
+__global__ void __launch_bounds__(128, 2) batchKernel(const __grid_constant__ FusedParams prm, int nItems,
                                                    int* counter) {
     extern __shared__ double smem[];
     __shared__ int next;

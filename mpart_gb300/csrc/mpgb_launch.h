@@ -26,7 +26,8 @@ cudaError_t launchReduceRows(const double* part, const long long* rowBase, int n
                              double* out, int accumulate, cudaStream_t stream);
 cudaError_t launchSumLoss(const double* lossPart, const int* slots, int n, double scale, double* out,
                           cudaStream_t stream);
-// All per-component reductions of a KL step (descs: device array of nComps).
+// All per-component reductions of a KL step (descs: device array of nComps);
+// loss may be null (gradient rows only).
 cudaError_t launchKLReduce(const double* part, const long long* rowBase, const KLReduceDesc* descs, int nComps,
                            int maxTerms, double* grad, const double* lossPart, const int* lossSlots, double lossScale,
                            double* loss, cudaStream_t stream);

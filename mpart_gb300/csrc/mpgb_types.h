@@ -109,6 +109,7 @@ struct FusedParams {
     // outputs
     double* outEval; long long evalRs, evalCs;
     double* outLogDet; long long logDetStride;
+    long long logDetCompStride;  // items of one component c0 write row c0 (0: one row for all)
     double* outDense; long long denseRs, denseCs;   // numCoeffs x N
     double* outInput; long long inputRs, inputCs;   // inputDim x N
     double* partials;
