@@ -434,6 +434,32 @@ static unsigned factorialU(unsigned d) {
     return out;
 }
 
+MapOptions mapOptionsFromC(const mpgb_map_options* o) {
+    MapOptions m;
+    if (!o) return m;
+    if (o->basis_type < 0 || o->basis_type > 2) throw std::invalid_argument("invalid basis_type");
+    if (o->pos_func_type < 0 || o->pos_func_type > 1) throw std::invalid_argument("invalid pos_func_type");
+    if (o->quad_type < 0 || o->quad_type > 2) throw std::invalid_argument("invalid quad_type");
+    m.basisType = (BasisTypes)o->basis_type;
+    m.posFuncType = (PosFuncTypes)o->pos_func_type;
+    m.quadType = (QuadTypes)o->quad_type;
+    m.quadAbsTol = o->quad_abs_tol;
+    m.quadRelTol = o->quad_rel_tol;
+    m.quadMaxSub = o->quad_max_sub;
+    m.quadMinSub = o->quad_min_sub;
+    m.quadPts = o->quad_pts;
+    m.contDeriv = o->cont_deriv != 0;
+    m.basisNorm = o->basis_norm != 0;
+    m.nugget = o->nugget;
+    if (o->sigmoid_type != 0 || o->edge_type != 0 || o->sigmoid_sum_type < 0 || o->sigmoid_sum_type > 1)
+        throw std::invalid_argument("invalid sigmoid enum value in options");
+    m.sigmoidType = SigmoidTypes::Logistic;
+    m.edgeType = EdgeTypes::SoftPlus;
+    m.edgeShape = o->edge_shape;
+    m.sigmoidBasisSumType = (SigmoidSumSizeType)o->sigmoid_sum_type;
+    return m;
+}
+
 static void validateOptions(MapOptions const& o) {
     if (o.basisType == BasisTypes::PhysicistHermite)
         throw std::invalid_argument("MapOptions: basisType must be ProbabilistHermite or HermiteFunctions.");
@@ -1600,31 +1626,6 @@ int guard(F&& f) {
     }
 }
 
-MapOptions toOptions(const mpgb_map_options* o) {
-    MapOptions m;
-    if (!o) return m;
-    if (o->basis_type < 0 || o->basis_type > 2) throw std::invalid_argument("invalid basis_type");
-    if (o->pos_func_type < 0 || o->pos_func_type > 1) throw std::invalid_argument("invalid pos_func_type");
-    if (o->quad_type < 0 || o->quad_type > 2) throw std::invalid_argument("invalid quad_type");
-    m.basisType = (BasisTypes)o->basis_type;
-    m.posFuncType = (PosFuncTypes)o->pos_func_type;
-    m.quadType = (QuadTypes)o->quad_type;
-    m.quadAbsTol = o->quad_abs_tol;
-    m.quadRelTol = o->quad_rel_tol;
-    m.quadMaxSub = o->quad_max_sub;
-    m.quadMinSub = o->quad_min_sub;
-    m.quadPts = o->quad_pts;
-    m.contDeriv = o->cont_deriv != 0;
-    m.basisNorm = o->basis_norm != 0;
-    m.nugget = o->nugget;
-    if (o->sigmoid_type != 0 || o->edge_type != 0 || o->sigmoid_sum_type < 0 || o->sigmoid_sum_type > 1)
-        throw std::invalid_argument("invalid sigmoid enum value in options");
-    m.sigmoidType = SigmoidTypes::Logistic;
-    m.edgeType = EdgeTypes::SoftPlus;
-    m.edgeShape = o->edge_shape;
-    m.sigmoidBasisSumType = (SigmoidSumSizeType)o->sigmoid_sum_type;
-    return m;
-}
 
 MonotoneMapBase* mono(mpgb_map* m) {
     if (!m || !m->obj) throw std::invalid_argument("null map handle");
@@ -1738,7 +1739,7 @@ int mpgb_create_component(unsigned int dim, unsigned int num_terms, const unsign
         if (nnz > 0 && (!nz_dims || !nz_orders)) throw std::invalid_argument("null nonzero arrays");
         std::vector<unsigned> d(nz_dims, nz_dims + nnz), o(nz_orders, nz_orders + nnz);
         FixedMultiIndexSet ms(dim, s, d, o);
-        *out = new mpgb_map{MapFactory::CreateComponent(ms, toOptions(opts))};
+        *out = new mpgb_map{MapFactory::CreateComponent(ms, mapOptionsFromC(opts))};
     });
 }
 
@@ -1747,7 +1748,7 @@ int mpgb_create_component_total_order(unsigned int dim, unsigned int order, cons
     return guard([&] {
         if (!out) throw std::invalid_argument("null argument");
         FixedMultiIndexSet ms(dim, order);
-        *out = new mpgb_map{MapFactory::CreateComponent(ms, toOptions(opts))};
+        *out = new mpgb_map{MapFactory::CreateComponent(ms, mapOptionsFromC(opts))};
     });
 }
 
@@ -1755,7 +1756,7 @@ int mpgb_create_triangular(unsigned int input_dim, unsigned int output_dim, unsi
                            const mpgb_map_options* opts, mpgb_map** out) {
     return guard([&] {
         if (!out) throw std::invalid_argument("null argument");
-        *out = new mpgb_map{MapFactory::CreateTriangular(input_dim, output_dim, total_order, toOptions(opts))};
+        *out = new mpgb_map{MapFactory::CreateTriangular(input_dim, output_dim, total_order, mapOptionsFromC(opts))};
     });
 }
 
@@ -1783,7 +1784,7 @@ int mpgb_create_sigmoid_component(unsigned int input_dim, unsigned int off_diag_
     return guard([&] {
         if (!out) throw std::invalid_argument("null argument");
         *out = new mpgb_map{MapFactory::CreateSigmoidComponent(input_dim, off_diag_order, cross_order,
-                                                               hostVector(centers, n_centers), toOptions(opts))};
+                                                               hostVector(centers, n_centers), mapOptionsFromC(opts))};
     });
 }
 
@@ -1798,7 +1799,7 @@ int mpgb_create_sigmoid_component_mset(unsigned int dim, unsigned int num_terms,
         if (nnz > 0 && (!nz_dims || !nz_orders)) throw std::invalid_argument("null nonzero arrays");
         FixedMultiIndexSet ms(dim, st, std::vector<unsigned>(nz_dims, nz_dims + nnz),
                               std::vector<unsigned>(nz_orders, nz_orders + nnz));
-        *out = new mpgb_map{MapFactory::CreateSigmoidComponent(ms, hostVector(centers, n_centers), toOptions(opts))};
+        *out = new mpgb_map{MapFactory::CreateSigmoidComponent(ms, hostVector(centers, n_centers), mapOptionsFromC(opts))};
     });
 }
 
@@ -1810,7 +1811,7 @@ int mpgb_create_sigmoid_triangular(unsigned int input_dim, unsigned int output_d
         std::vector<std::vector<double>> cs(output_dim, std::vector<double>(n_centers));
         for (unsigned j = 0; j < output_dim; ++j)
             for (unsigned i = 0; i < n_centers; ++i) cs[j][i] = centers[(int64_t)i * row_stride + (int64_t)j * col_stride];
-        *out = new mpgb_map{MapFactory::CreateSigmoidTriangular(input_dim, output_dim, total_order, cs, toOptions(opts))};
+        *out = new mpgb_map{MapFactory::CreateSigmoidTriangular(input_dim, output_dim, total_order, cs, mapOptionsFromC(opts))};
     });
 }
 

@@ -11,6 +11,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/mpart_gb300.h"
 #include "../../include/mpart_gb300.hpp"
 #include "mpgb_types.h"
 
@@ -32,6 +33,10 @@ struct CudaError : public std::runtime_error {
 
 // Quadrature rules (AdaptiveClenshawCurtis) and basis constants for a launch.
 void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b);
+
+// MapOptions from the C ABI's struct (defaults for a null pointer); throws
+// std::invalid_argument for enum values out of range.
+MapOptions mapOptionsFromC(const mpgb_map_options* o);
 
 // ---------------------------------------------------------------------------
 // Component program: the multi-index set reorganised as a prefix tree over

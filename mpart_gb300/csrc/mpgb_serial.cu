@@ -309,30 +309,6 @@ void emit(const std::vector<unsigned char>& b, unsigned char* buf, size_t cap, s
     }
 }
 
-MapOptions optsFromC(const mpgb_map_options* o) {
-    MapOptions m;
-    if (o->basis_type < 0 || o->basis_type > 2 || o->pos_func_type < 0 || o->pos_func_type > 1 || o->quad_type < 0 ||
-        o->quad_type > 2)
-        throw std::invalid_argument("invalid enum value in options");
-    m.basisType = (BasisTypes)o->basis_type;
-    m.posFuncType = (PosFuncTypes)o->pos_func_type;
-    m.quadType = (QuadTypes)o->quad_type;
-    m.quadAbsTol = o->quad_abs_tol;
-    m.quadRelTol = o->quad_rel_tol;
-    m.quadMaxSub = o->quad_max_sub;
-    m.quadMinSub = o->quad_min_sub;
-    m.quadPts = o->quad_pts;
-    m.contDeriv = o->cont_deriv != 0;
-    m.basisNorm = o->basis_norm != 0;
-    m.nugget = o->nugget;
-    if (o->sigmoid_type != 0 || o->edge_type != 0 || o->sigmoid_sum_type < 0 || o->sigmoid_sum_type > 1)
-        throw std::invalid_argument("invalid sigmoid enum value in options");
-    m.sigmoidType = SigmoidTypes::Logistic;
-    m.edgeType = EdgeTypes::SoftPlus;
-    m.edgeShape = o->edge_shape;
-    m.sigmoidBasisSumType = (SigmoidSumSizeType)o->sigmoid_sum_type;
-    return m;
-}
 
 }  // namespace
 }  // namespace mpgb
@@ -380,7 +356,7 @@ int mpgb_options_to_bytes(const mpgb_map_options* opts, unsigned char* buf, size
     return serialGuard([&] {
         if (!opts) throw std::invalid_argument("null options");
         Writer w;
-        writeOptions(w, optsFromC(opts));
+        writeOptions(w, mapOptionsFromC(opts));
         emit(w.b, buf, cap, size);
     });
 }

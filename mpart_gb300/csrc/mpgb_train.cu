@@ -703,20 +703,7 @@ int trainMapAdaptiveImpl(unsigned int n_sets, const unsigned int* num_terms, con
             if (sets[j].terms.empty()) throw std::invalid_argument("TrainMapAdaptive: empty multi-index set.");
         }
         ATMOpts o;
-        mpgb_map_options mo = opts->map;
-        MapOptions m;
-        m.basisType = (BasisTypes)mo.basis_type;
-        m.posFuncType = (PosFuncTypes)mo.pos_func_type;
-        m.quadType = (QuadTypes)mo.quad_type;
-        m.quadAbsTol = mo.quad_abs_tol;
-        m.quadRelTol = mo.quad_rel_tol;
-        m.quadMaxSub = mo.quad_max_sub;
-        m.quadMinSub = mo.quad_min_sub;
-        m.quadPts = mo.quad_pts;
-        m.contDeriv = mo.cont_deriv != 0;
-        m.basisNorm = mo.basis_norm != 0;
-        m.nugget = mo.nugget;
-        o.map = m;
+        o.map = mapOptionsFromC(&opts->map);
         o.train = trainOptsFromC(&opts->train);
         o.mode = opts->train.mode;
         o.maxPatience = opts->max_patience;

@@ -49,3 +49,33 @@ def test_matrix_views():
     assert (m.rows, m.cols, m.row_stride, m.col_stride) == (5, 4, 7, 2)
     with pytest.raises(ValueError):
         _mat(torch.zeros(3, dtype=torch.float32))
+
+
+def test_sigmoid_parameters_match_oracle(oracle):
+    """CreateSigmoid's widths and weights (host code of the C ABI, no GPU)
+    equal the oracle's restatement bit for bit; invalid center counts raise."""
+    cases = [(np.array([-3.0, 3.0, 0.0, -1.0, 1.0, -2.0, 0.0, 2.0]), 1.5, 0),
+             (np.array([-2.0, 2.5, 1.0, -1.5, 0.3, 0.9]), 0.7, 1),
+             (np.array([-3.0, 3.0]), 2.0, 0), (np.array([-3.0, 3.0, 0.2]), 2.0, 1),
+             (np.linspace(-4, 4, 2 + 15), 1.2, 0)]
+    for c, edge, st in cases:
+        S = M.Sigmoid1d.FromCenters(c, edge, M.SigmoidSumSizeType(st))
+        ref = oracle.sigmoid_from_centers(c, edge, st)
+        for a, b in zip((S.centers, S.widths, S.weights, S.startInds), ref):
+            np.testing.assert_array_equal(a, b)
+        assert S.GetOrder() == len(ref[3]) + 3
+    with pytest.raises(ValueError, match="Linear"):
+        M.Sigmoid1d.FromCenters(np.zeros(6))  # 2 + 4 centers: not 2 + n(n+1)/2
+    with pytest.raises(ValueError):
+        M.Sigmoid1d.FromCenters(np.zeros(1))
+    with pytest.raises(ValueError, match="maximum"):
+        M.Sigmoid1d.FromCenters(np.zeros(2 + 10 * 11 // 2))  # ten sigmoid terms: order 13 > 12
+
+
+def test_sigmoid_start_indices():
+    # Sigmoid1d::ConstructStartInds (MParT/Sigmoid.h:95-130)
+    assert M.Sigmoid1d(np.zeros(8), np.ones(8), np.ones(8)).startInds.tolist() == [2, 3, 5]
+    assert M.Sigmoid1d(np.zeros(5), np.ones(5), np.ones(5),
+                       sumType=M.SigmoidSumSizeType.Constant).startInds.tolist() == [2, 3, 4]
+    with pytest.raises(ValueError):
+        M.Sigmoid1d(np.zeros(6), np.ones(6), np.ones(6))
