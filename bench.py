@@ -747,6 +747,7 @@ def run_gpu(args):
                      "flops_per_point": fpp, "evals_per_point": E},
         "clocks": clk.summary(),
     }
+    line["dense_coeff_grad"] = dense_coeff_grad(comp, x, s, N, dev)
     line["plain_path"] = plain_path(M, coef, x, s, N, dev)
     line["plain_path"]["fused_speedup"] = line["plain_path"]["ms_per_step"] / (t_step * 1e3)
     line["cpu_baseline"] = cpu_baseline()
@@ -765,6 +766,27 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def dense_coeff_grad(comp, x, s, N, dev, reps=3):
+    """CoeffGradImpl with its dense numCoeffs x N output (the reference's
+    per-point layout): 495 x 1,000,000 doubles = 3.96 GB written per call."""
+    import torch
+    out = torch.empty(comp.numCoeffs, N, dtype=torch.float64, device=dev)
+    comp.CoeffGradImpl(x, s, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 1e300
+    for _ in range(reps):
+        e0.record()
+        comp.CoeffGradImpl(x, s, out)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    nbytes = out.numel() * 8
+    del out
+    return {"ms": best, "points_per_s": N / (best * 1e-3), "output_bytes": nbytes,
+            "output_gb_per_s": nbytes / (best * 1e-3) / 1e9}
 
 
 def plain_path(M, coef, x, s, N, dev):

@@ -313,7 +313,11 @@ namespace mpgb {
 // iteration.  Throws; sets the map's coefficients to the result.
 void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o, int mode, cudaStream_t s,
              double* loss_per_comp, mpgb_train_result* res) {
-    map.CheckCoefficients("TrainMap");
+    // A map without coefficients starts from ones (src/TrainMap.cpp:168-176).
+    if (!map.CheckCoefficients()) {
+        std::vector<double> ones(map.numCoeffs, 1.0);
+        map.SetCoeffs(ones.data(), map.numCoeffs, true, s);
+    }
     const auto& parts = map.Parts();
     std::vector<double> x0 = map.CoeffMap();
     KLStep step(map, pts, s, mode);

@@ -116,3 +116,18 @@ def test_train_map_with_objective_and_options(gpu):
     assert obj2.TestError(map2) < 5.0
     assert _ks(map1, test) < 0.1
     assert _ks(map2, test) < 0.1
+
+
+@pytest.mark.gpu
+def test_train_map_starts_unset_coefficients_at_one(gpu):
+    """src/TrainMap.cpp:168-176: a map whose coefficients were never set starts
+    from ones."""
+    import torch
+    M = gpu
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis)
+    comps = [M.CreateComponent(M.FixedMultiIndexSet(d + 1, 2), opts) for d in range(2)]
+    tri = M.TriangularMap(comps, False)
+    X = torch.as_tensor(_banana(2000), device="cuda")
+    loss, res = M.TrainMap(tri, X, max_iters=0)
+    np.testing.assert_array_equal(np.asarray(tri.CoeffMap()), np.ones(tri.numCoeffs))
+    assert np.isfinite(loss).all()
