@@ -125,9 +125,14 @@ def test_train_map_starts_unset_coefficients_at_one(gpu):
     import torch
     M = gpu
     opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis)
-    comps = [M.CreateComponent(M.FixedMultiIndexSet(d + 1, 2), opts) for d in range(2)]
-    tri = M.TriangularMap(comps, False)
     X = torch.as_tensor(_banana(2000), device="cuda")
-    loss, res = M.TrainMap(tri, X, max_iters=0)
-    np.testing.assert_array_equal(np.asarray(tri.CoeffMap()), np.ones(tri.numCoeffs))
-    assert np.isfinite(loss).all()
+    maps = []
+    for start in (None, 1.0):
+        comps = [M.CreateComponent(M.FixedMultiIndexSet(d + 1, 2), opts) for d in range(2)]
+        tri = M.TriangularMap(comps, False)
+        if start is not None:
+            tri.SetCoeffs(np.full(tri.numCoeffs, start))
+        loss, res = M.TrainMap(tri, X, max_iters=5)
+        assert np.isfinite(loss).all()
+        maps.append(np.asarray(tri.CoeffMap()))
+    np.testing.assert_array_equal(maps[0], maps[1])
