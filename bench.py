@@ -137,6 +137,27 @@ def batch_specs(n_maps=64, seed=17):
     return list(zip(dims.tolist(), orders.tolist(), npts.tolist()))
 
 
+def batch_setup(M, dev):
+    """The batched-maps workload (batch_specs) as one MapBatch call."""
+    import torch
+    opts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=TOL, quadRelTol=TOL,
+                        quadMaxSub=MAXSUB)
+    rng = np.random.default_rng(18)
+    maps, pts, sens = [], [], []
+    for d, o, n in batch_specs():
+        tm = M.CreateTriangular(d, d, o, opts)
+        tm.SetCoeffs(rng.normal(0.0, 0.05, tm.numCoeffs))
+        maps.append(tm)
+        pts.append(torch.as_tensor(rng.standard_normal((d, n)), device=dev))
+        sens.append(torch.as_tensor(rng.standard_normal((d, n)), device=dev))
+    z = lambda *s: torch.zeros(*s, dtype=torch.float64, device=dev)
+    ev = [z(m.outputDim, p.shape[1]) for m, p in zip(maps, pts)]
+    ld = [z(p.shape[1]) for p in pts]
+    cg = [z(m.numCoeffs) for m in maps]
+    B = M.MapBatch(maps)
+    return lambda: B.FusedForwardAdjoint(pts, sens, 1.0, ev, ld, cg)
+
+
 def batch_maps(M, dev, autotune=True):
     """64 uneven maps: forward + log-determinant + coefficient adjoint of every
     map as one persistent launch (before and after autotuning) against one
@@ -640,6 +661,21 @@ def run_gpu(args):
         if args.variant == "sigmoid":
             # The sigmoid workload's fused step (see sigmoid_setup).
             step = sigmoid_setup(M, dev)[-1]
+        elif args.variant == "inverse":
+            # The inverse workload's map on 100,000 of its targets.
+            iopts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=INV_TOL,
+                                 quadRelTol=INV_TOL, quadMaxSub=MAXSUB)
+            tmi = M.CreateTriangular(INV_DIM, INV_DIM, INV_ORDER, iopts)
+            tmi.SetCoeffs(np.random.default_rng(31).normal(0.0, 0.03, tmi.numCoeffs))
+            g = torch.Generator(device=dev)
+            g.manual_seed(32)
+            ri = torch.randn(INV_DIM, 100_000, dtype=torch.float64, device=dev, generator=g)
+            x1i = torch.zeros(0, 100_000, dtype=torch.float64, device=dev)
+            xi = torch.zeros(INV_DIM, 100_000, dtype=torch.float64, device=dev)
+            step = lambda: tmi.InverseImpl(x1i, ri, xi, xtol=INV_XTOL, ytol=INV_XTOL)
+        elif args.variant == "batch":
+            # The batched-maps workload's batch call (default tuning).
+            step = batch_setup(M, dev)
         elif args.variant == "kl":
             # The KL training workload's step at trained coefficients (100
             # L-BFGS iterations with direct launches first); the profiled
@@ -826,7 +862,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
     ap.add_argument("--no-sigmoid", action="store_true", help="skip the sigmoid-expansion workload")
-    ap.add_argument("--variant", default="full", choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid"],
+    ap.add_argument("--variant", default="full",
+                    choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid", "inverse", "batch"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
     if args.impl == "reference":

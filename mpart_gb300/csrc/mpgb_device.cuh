@@ -42,6 +42,10 @@ constexpr int kStatusInf = 1;          // g(df) was +inf (the reference throws)
 constexpr int kStatusNaN = 2;          // the integrand was NaN
 constexpr int kStatusBudget = 4;       // interval budget exhausted
 constexpr int kStatusNoBracket = 8;    // inverse: bracket search failed (info=-2)
+// Inverse info code of a point whose bracket search ran out of its first-pass
+// budget (solved again in the second pass; never returned to callers).
+constexpr int kInfoDeferred = -3;
+constexpr unsigned kBracketIts = 128;  // FindBracket's step limit (RootFinding.h:29)
 
 // Quadrature kinds (MapOptions::quadType values).
 constexpr int kQuadFixedCC = 0;   // ClenshawCurtis: one fixed rule on [0, 1] (Quadrature.h:114-143)

@@ -321,6 +321,7 @@ struct MapWorkspace {
     DevBuf perm, sortHist;
     DevBuf implicitAcc;  // back-substitution sums when the caller wants no input gradient
     DevBuf rcache;       // rectifier cache of sigmoid expansions (reduced adjoints)
+    DevBuf inverseDefer; // two-pass inverse: count, deferred component per point, deferred list
     bool ordering = true;
 };
 
@@ -660,6 +661,9 @@ struct LaunchCommon {
 };
 
 constexpr int kTpb = 128;
+// Bracket-doubling steps per component in the inverse's first pass: a target
+// within 2^16 of the initial guess is bracketed there.
+constexpr int kFirstPassBracketIts = 16;
 
 void checkMatrix(const StridedMatrix& m, int64_t rows, int64_t cols, const char* what, const char* fn) {
     if (m.rows != rows || m.cols != cols) {
@@ -971,7 +975,25 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
     p.quad = W.quad; p.bc = W.bc;
     const int nBlocks = (int)((N + kTpb - 1) / kTpb);
+    // Two passes (see InverseParams): the first gives each point a few
+    // bracket-doubling steps per component, the second finishes the points
+    // that needed more.  Results are those of one pass with the full 128 steps.
+    const bool twoPass = N >= 2 * kTpb;
+    p.bracketBudget = twoPass ? kFirstPassBracketIts : (int)kBracketIts;
+    if (twoPass) {
+        W.inverseDefer.ensure((size_t)(2 * N + 1) * sizeof(int), stream);
+        int* base = W.inverseDefer.as<int>();
+        p.deferCount = base;
+        p.deferComp = base + 1;
+        p.deferList = base + 1 + N;
+        MPGB_CUDA(cudaMemsetAsync(p.deferCount, 0, sizeof(int), stream));
+    }
     MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
+    if (twoPass) {
+        InverseParams q = p;
+        q.list = p.deferList;
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
+    }
     Finish(stream, "Inverse");
 }
 

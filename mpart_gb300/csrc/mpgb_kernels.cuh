@@ -887,84 +887,122 @@ struct SigmoidInverseEval {
     }
 };
 
-template <class F>
-__device__ void findBracket(const F& f, double& xlb, double& ylb, double& xub, double& yub, const double yd,
-                            int& info) {
-    const unsigned maxIts = 128;
-    double stepSize = 1.0;
-    info = 0;
-    ylb = f(xlb);
-    yub = f(xub);
-    if (ylb > yd) {
-        double t = ylb; ylb = yub; yub = t;
-        t = xlb; xlb = xub; xub = t;
-        unsigned i;
-        for (i = 0; i < maxIts; ++i) {
-            xlb = xub - stepSize;
-            ylb = f(xlb);
-            if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { info = -1; return; }
-            if (ylb > yd) { yub = ylb; xub = xlb; stepSize *= 2.0; }
-            else break;
-        }
-        if (i >= maxIts) info = -2;
-    } else {
-        unsigned i;
-        for (i = 0; i < maxIts; ++i) {
-            xub = xlb + stepSize;
-            yub = f(xub);
-            if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { info = -1; return; }
-            if (yub < yd) { ylb = yub; xlb = xub; stepSize *= 2.0; }
-            else break;
-        }
-        if (i >= maxIts) info = -2;
-    }
-}
-
 // Root of f(x) = yd for a monotone f (MonotoneComponent::InverseImpl with
-// RootFinding::InverseSingleBracket, RootFinding.h:125-178): the reference's
-// bracket search (same evaluations, so the same points have no bracket and
-// give NaN), then the bracket is closed by a safeguarded Newton iteration
-// with the exact slope dT/dx_D = g(df) + nugget instead of ITP.  Every
-// evaluation narrows the bracket; a Newton step that leaves it, or two steps
-// that do not halve it, give way to bisection.  The stopping rules are the
-// reference's: |f(x) - yd| < ftol returns x; a bracket narrower than xtol (or
-// whose values differ by less than ftol) returns its midpoint.  The answer
-// therefore meets the reference's tolerance; it is not the ITP iterate itself.
-template <class F>
-__device__ double inverseSingleBracket(double yd, const F& f, double x0, double xtol, double ftol, int& info) {
-    const unsigned maxIts = 10000;
-    double xlb, xub, ylb, yub;
-    info = 0;
-    xlb = xub = x0;
-    ylb = yub = f(xlb);
-    int binfo = 0;
-    findBracket(f, xlb, ylb, xub, yub, yd, binfo);
-    if ((binfo < 0) || (((ylb > yd) || (yub < yd)))) {
-        info = -2;
-        return __longlong_as_double(0x7ff8000000000000ULL);
+// RootFinding::InverseSingleBracket and FindBracket, RootFinding.h:20-90,
+// :125-178) as a state machine that asks for one evaluation of f per step,
+// so that the lanes of a warp evaluate f together instead of one after the
+// other.  The reference's bracket search is kept step for step (same
+// evaluation points, so the same targets have no bracket and give NaN; its
+// two repeated evaluations at x0 are taken from the first), then the bracket
+// is closed by a safeguarded Newton iteration with the exact slope
+// dT/dx_D = g(df) + nugget instead of ITP.  Every evaluation narrows the
+// bracket; a Newton step that leaves it, or two steps that do not halve it,
+// give way to bisection.  The stopping rules are the reference's:
+// |f(x) - yd| < ftol returns x; a bracket narrower than xtol (or whose values
+// differ by less than ftol) returns its midpoint.  The answer therefore meets
+// the reference's tolerance; it is not the ITP iterate itself.
+struct RootSolve {
+    enum : int { kStart = 0, kBracket = 1, kNewton = 2, kDone = 3 };
+    int phase, dir, info;
+    unsigned it;
+    double x;  // next evaluation point
+    double xlb, ylb, xub, yub, step, width, widthPrev, result;
+
+    __device__ void start(double x0) {
+        phase = kStart;
+        info = 0;
+        x = x0;
     }
-    if (fabs(ylb - yd) < ftol) return xlb;
-    if (fabs(yub - yd) < ftol) return xub;
-    if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) return 0.5 * (xub + xlb);
-    // Start from the secant point of the bracket.
-    double xc = xlb + (yd - ylb) * (xub - xlb) / (yub - ylb);
-    if (!(xc > xlb && xc < xub)) xc = 0.5 * (xlb + xub);
-    double width = xub - xlb, widthPrev = 2.0 * width;
-    for (unsigned it = 0; it < maxIts; ++it) {
-        const double yc = f(xc);
-        if (fabs(yc - yd) < ftol) return xc;
-        if (yc > yd) { xub = xc; yub = yc; }
-        else { xlb = xc; ylb = yc; }
-        if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) break;
+    __device__ void finish(double r, int inf) {
+        result = r;
+        info = inf;
+        phase = kDone;
+    }
+    // The bracket is found: the checks before the solver loop and its first point.
+    __device__ void bracketed(double yd, double xtol, double ftol) {
+        if ((ylb > yd) || (yub < yd)) { finish(__longlong_as_double(0x7ff8000000000000ULL), -2); return; }
+        if (fabs(ylb - yd) < ftol) { finish(xlb, 0); return; }
+        if (fabs(yub - yd) < ftol) { finish(xub, 0); return; }
+        if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) { finish(0.5 * (xub + xlb), 0); return; }
+        double xc = xlb + (yd - ylb) * (xub - xlb) / (yub - ylb);  // secant point of the bracket
+        if (!(xc > xlb && xc < xub)) xc = 0.5 * (xlb + xub);
+        width = xub - xlb;
+        widthPrev = 2.0 * width;
+        it = 0;
+        x = xc;
+        phase = kNewton;
+    }
+    // Consumes y = f(x).  maxBracket < kBracketIts is a first-pass budget:
+    // running out of it gives kInfoDeferred instead of "no bracket".
+    template <class F>
+    __device__ void step_(double y, double yd, const F& f, double xtol, double ftol, unsigned maxBracket) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+        if (phase == kStart) {
+            xlb = xub = x;
+            ylb = yub = y;
+            step = 1.0;
+            it = 0;
+            dir = (ylb > yd) ? -1 : 1;
+            x = (dir < 0) ? xub - step : xlb + step;
+            phase = kBracket;
+            return;
+        }
+        if (phase == kBracket) {
+            bool more;
+            if (dir < 0) {
+                xlb = x;
+                ylb = y;
+                if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { finish(nan, -2); return; }
+                more = ylb > yd;
+                if (more) { yub = ylb; xub = xlb; step *= 2.0; }
+            } else {
+                xub = x;
+                yub = y;
+                if ((fabs((yub - ylb) / (xub - xlb)) < 1e-12) && ((xub - xlb) > 10)) { finish(nan, -2); return; }
+                more = yub < yd;
+                if (more) { ylb = yub; xlb = xub; step *= 2.0; }
+            }
+            if (!more) { bracketed(yd, xtol, ftol); return; }
+            if (++it >= maxBracket) { finish(nan, (maxBracket < kBracketIts) ? kInfoDeferred : -2); return; }
+            x = (dir < 0) ? xub - step : xlb + step;
+            return;
+        }
+        // Newton / bisection (at most 10000 evaluations).
+        const double xc = x;
+        if (fabs(y - yd) < ftol) { finish(xc, 0); return; }
+        if (y > yd) { xub = xc; yub = y; }
+        else { xlb = xc; ylb = y; }
+        if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) { finish(0.5 * (xub + xlb), 0); return; }
         const double w = xub - xlb;
-        double xn = xc - (yc - yd) / f.slope(xc);
+        double xn = xc - (y - yd) / f.slope(xc);
         // Bisection when Newton leaves the bracket or the bracket shrinks too slowly.
         if (!(xn > xlb && xn < xub) || w > 0.5 * widthPrev) xn = 0.5 * (xlb + xub);
         widthPrev = width;
         width = w;
-        xc = xn;
+        x = xn;
+        if (++it >= 10000u) finish(0.5 * (xub + xlb), 0);
     }
-    return 0.5 * (xub + xlb);
+};
+
+// Solves f(x) = yd for the lanes with `need` set; every lane of the warp
+// takes part in the loop (the step count is the warp's maximum), and in each
+// step the lanes still solving evaluate f together.
+template <class F>
+__device__ __forceinline__ void solveLockstep(bool need, const F& f, double yd, double x0, double xtol, double ftol,
+                                              unsigned maxBracket, double& result, int& info) {
+    RootSolve rs;
+    if (need) rs.start(x0);
+    while (__any_sync(0xffffffffu, need)) {
+        if (need) {
+            const double y = f(rs.x);
+            rs.step_(y, yd, f, xtol, ftol, maxBracket);
+            need = rs.phase != RootSolve::kDone;
+            if (!need) {
+                result = rs.result;
+                info = rs.info;
+            }
+        }
+    }
 }
 
 template <int BASIS, int POS, int PMAX>
@@ -973,53 +1011,75 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     const int tid = threadIdx.x;
     const int tpb = blockDim.x;
     const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
-    const long long i = (long long)blockIdx.x * tpb + tid;
-    const bool active = i < prm.N;
+    const long long slot = (long long)blockIdx.x * tpb + tid;
+    const bool second = prm.list != nullptr;
+    const bool active = slot < (second ? (long long)*prm.deferCount : prm.N);
+    const long long i = (active && second) ? (long long)prm.list[slot] : slot;
+    const int cStart = (active && second) ? prm.deferComp[i] : 0;
+    const unsigned budget = second ? kBracketIts : (unsigned)prm.bracketBudget;
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const int inDim = prm.comps[prm.nComps - 1].D;
-    // fullOut = [x1; 0] (TriangularMap.cpp:146-159)
+    // fullOut = [x1; 0] (TriangularMap.cpp:146-159); in the second pass the
+    // coordinates of the components solved in the first pass come from out.
     const long long xi = (prm.x1Cols == 1) ? 0 : i;
     for (int d = 0; d < inDim; ++d) {
         double v = 0.0;
-        if (active && d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+        if (active) {
+            if (d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+            else if (d - prm.extra < cStart) v = prm.out[(long long)(d - prm.extra) * prm.outRs + i * prm.outCs];
+        }
         L.X[d * tpb + tid] = v;
     }
     int stAll = 0;
+    bool stopped = !active;
+    // Every thread runs every component (the warp-wide solver loop needs all
+    // lanes); lanes that are inactive, stopped or before their start component
+    // only take part in the loop.
     for (int ci = 0; ci < prm.nComps; ++ci) {
         const CompDesc& c = prm.comps[ci];
+        const bool mine = !stopped && ci >= cStart;
         const double* cm = prm.cm + c.slotOffset;
-        fillLead<BASIS, false>(c, L, tid, prm.bc);
         ACoef<PMAX> A;
-        if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a, nullptr);
-        else phaseA<PMAX>(c, L, tid, cm, A.a);
+        if (mine) {
+            fillLead<BASIS, false>(c, L, tid, prm.bc);
+            if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a, nullptr);
+            else phaseA<PMAX>(c, L, tid, cm, A.a);
+        } else {
+#pragma unroll
+            for (int k = 0; k <= PMAX; ++k) A.a[k] = 0.0;
+        }
         double result = nan;
         int info = 0;
-        if (active) {
-            bool hasNan = false;
-            for (int d = 0; d < c.D; ++d) hasNan |= isnan(L.X[d * tpb + tid]);
-            const double yd = prm.r[(long long)ci * prm.rRs + i * prm.rCs];
-            if constexpr (BASIS == kBasisSigmoid) {
-                // (RectifiedMultivariateExpansion.h:227-277; UnivariateExpansion.h:213-250.
-                // A NaN target gives NaN.)
-                if (!hasNan && !isnan(yd)) {
-                    SigmoidInverseEval<PMAX> f{A, c.P, &c};
-                    result = inverseSingleBracket(yd, f, L.X[(c.D - 1) * tpb + tid], prm.xtol, prm.ytol, info);
-                    if (info < 0) stAll |= kStatusNoBracket;
-                }
-            } else if (!hasNan) {
-                double f0 = 0.0;
+        bool hasNan = false;
+        for (int d = 0; mine && d < c.D; ++d) hasNan |= isnan(L.X[d * tpb + tid]);
+        const double yd = mine ? prm.r[(long long)ci * prm.rRs + i * prm.rCs] : 0.0;
+        const double x0 = mine ? L.X[(c.D - 1) * tpb + tid] : 0.0;
+        if constexpr (BASIS == kBasisSigmoid) {
+            // (RectifiedMultivariateExpansion.h:227-277; UnivariateExpansion.h:213-250.
+            // A NaN target gives NaN.)
+            SigmoidInverseEval<PMAX> f{A, c.P, &c};
+            solveLockstep(mine && !hasNan && !isnan(yd), f, yd, x0, prm.xtol, prm.ytol, budget, result, info);
+        } else {
+            double f0 = 0.0;
 #pragma unroll
-                for (int k = 0; k <= PMAX; ++k) f0 = fma(A.a[k], prm.bc.v0[k], f0);
-                int st = 0;
-                InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
-                result = inverseSingleBracket(yd, f, L.X[(c.D - 1) * tpb + tid], prm.xtol, prm.ytol, info);
-                if (info < 0) st |= kStatusNoBracket;
-                stAll |= st;
-            }
-            L.X[(c.D - 1) * tpb + tid] = result;
-            prm.out[(long long)ci * prm.outRs + i * prm.outCs] = result;
-            if (prm.info) prm.info[(long long)ci * prm.infoStride + i] = info;
+            for (int k = 0; k <= PMAX; ++k) f0 = fma(A.a[k], prm.bc.v0[k], f0);
+            int st = 0;
+            InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
+            solveLockstep(mine && !hasNan, f, yd, x0, prm.xtol, prm.ytol, budget, result, info);
+            stAll |= st;
         }
+        if (!mine) continue;
+        if (info == kInfoDeferred) {
+            // Out of first-pass budget: the second pass solves this point from here.
+            prm.deferComp[i] = ci;
+            prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
+            stopped = true;
+            continue;
+        }
+        if (info < 0) stAll |= kStatusNoBracket;
+        L.X[(c.D - 1) * tpb + tid] = result;
+        prm.out[(long long)ci * prm.outRs + i * prm.outCs] = result;
+        if (prm.info) prm.info[(long long)ci * prm.infoStride + i] = info;
     }
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }

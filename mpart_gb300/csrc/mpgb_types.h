@@ -146,6 +146,19 @@ struct InverseParams {
     double xtol, ytol;
     double nugget;
     int dmax, nBmax, depthMax, pad_;
+    // Two passes: in the first (list null) every point has bracketBudget
+    // doubling steps per component; a point that needs more stops at that
+    // component, which deferComp[i] records, and i is appended to deferList.
+    // The second pass (list = deferList) runs the *deferCount points of the
+    // list from their deferComp component with the full kBracketIts steps, so
+    // the points with long or failing bracket searches share warps with each
+    // other only.  Its grid covers N points; blocks past the count return.
+    int bracketBudget;
+    int pad2_;
+    const int* list;
+    int* deferComp;
+    int* deferList;
+    int* deferCount;
     QuadParams quad;
     BasisConsts bc;
 };
