@@ -322,6 +322,7 @@ struct MapWorkspace {
     DevBuf implicitAcc;  // back-substitution sums when the caller wants no input gradient
     DevBuf rcache;       // rectifier cache of sigmoid expansions (reduced adjoints)
     DevBuf inverseDefer; // two-pass inverse: count, deferred component per point, deferred list
+    DevBuf inverseKey;   // inverse processing order: per-target sort keys
     bool ordering = true;
 };
 
@@ -987,6 +988,15 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         p.deferComp = base + 1;
         p.deferList = base + 1 + N;
         MPGB_CUDA(cudaMemsetAsync(p.deferCount, 0, sizeof(int), stream));
+    }
+    // First pass in order of sum_c |r_c|: targets of similar cost share warps.
+    if (twoPass && W.ordering) {
+        W.inverseKey.ensure((size_t)N * sizeof(double), stream);
+        W.perm.ensure((size_t)N * sizeof(int), stream);
+        W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
+        MPGB_CUDA(launchTargetKey(r.data, r.rowStride, r.colStride, (int)r.rows, N, W.inverseKey.as<double>(), stream));
+        MPGB_CUDA(launchSortByLast(W.inverseKey.as<double>(), 1, N, W.sortHist.as<int>(), W.perm.as<int>(), stream));
+        p.perm = W.perm.as<int>();
     }
     MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
     if (twoPass) {

@@ -1014,7 +1014,7 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     const long long slot = (long long)blockIdx.x * tpb + tid;
     const bool second = prm.list != nullptr;
     const bool active = slot < (second ? (long long)*prm.deferCount : prm.N);
-    const long long i = (active && second) ? (long long)prm.list[slot] : slot;
+    const long long i = !active ? slot : second ? (long long)prm.list[slot] : prm.perm ? (long long)prm.perm[slot] : slot;
     const int cStart = (active && second) ? prm.deferComp[i] : 0;
     const unsigned budget = second ? kBracketIts : (unsigned)prm.bracketBudget;
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);

@@ -156,6 +156,7 @@ struct InverseParams {
     int bracketBudget;
     int pad2_;
     const int* list;
+    const int* perm;  // first pass: point of each slot (points grouped by expected cost), or null
     int* deferComp;
     int* deferList;
     int* deferCount;
