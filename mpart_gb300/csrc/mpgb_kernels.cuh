@@ -793,12 +793,14 @@ __global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ Fused
 // rows, log-det scratch row, partial row), so results do not depend on which
 // block runs it.  The item's component selects the body compiled for the
 // smallest order class >= its last-coordinate order.  At most 128 threads a
-// block; the register budget of 2 blocks an SM keeps the order-6 and order-8
-// bodies free of spills (with 4 blocks an SM they spilled, and the 64-map
+// block.  The kernel is built per largest order class MAXC of the batch, so a
+// batch pays the registers of its own bodies only: classes 2 and 4 keep 4
+// blocks an SM; with order-6 or order-8 bodies the budget of 2 blocks an SM
+// keeps them free of spills (with 4 blocks an SM they spilled, and the 64-map
 // workload ran 11 % slower).
-template <int BASIS, int POS>
-__global__ void __launch_bounds__(128, 2) batchKernel(const __grid_constant__ FusedParams prm, int nItems,
-                                                   int* counter) {
+template <int BASIS, int POS, int MAXC>
+__global__ void __launch_bounds__(128, (MAXC <= 4) ? 4 : 2) batchKernel(const __grid_constant__ FusedParams prm,
+                                                                       int nItems, int* counter) {
     extern __shared__ double smem[];
     __shared__ int next;
     for (;;) {
@@ -809,10 +811,16 @@ __global__ void __launch_bounds__(128, 2) batchKernel(const __grid_constant__ Fu
         if (k >= nItems) break;
         const WorkItem item = prm.items[k];
         const int P = prm.comps[item.c0].P;
-        if (P <= 2) fusedBody<BASIS, POS, 2, true, 0, true>(prm, item, smem);
-        else if (P <= 4) fusedBody<BASIS, POS, 4, true, 0, true>(prm, item, smem);
-        else if (P <= 6) fusedBody<BASIS, POS, 6, true, 0, true>(prm, item, smem);
-        else fusedBody<BASIS, POS, 8, true, 0, true>(prm, item, smem);
+        if (P <= 2) {
+            fusedBody<BASIS, POS, 2, true, 0, true>(prm, item, smem);
+        } else if constexpr (MAXC >= 4) {
+            if (P <= 4) {
+                fusedBody<BASIS, POS, 4, true, 0, true>(prm, item, smem);
+            } else if constexpr (MAXC >= 6) {
+                if (P <= 6) fusedBody<BASIS, POS, 6, true, 0, true>(prm, item, smem);
+                else if constexpr (MAXC >= 8) fusedBody<BASIS, POS, 8, true, 0, true>(prm, item, smem);
+            }
+        }
     }
 }
 #undef MPGB_IO
@@ -1116,7 +1124,14 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
 template <int BASIS, int POS>
 cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int* counter, cudaStream_t stream) {
     const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, pmaxClass, false);
-    auto kern = batchKernel<BASIS, POS>;
+    void (*kern)(FusedParams, int, int*) = nullptr;
+    switch (pmaxClass) {
+        case 2: kern = batchKernel<BASIS, POS, 2>; break;
+        case 4: kern = batchKernel<BASIS, POS, 4>; break;
+        case 6: kern = batchKernel<BASIS, POS, 6>; break;
+        case 8: kern = batchKernel<BASIS, POS, 8>; break;
+        default: return cudaErrorInvalidValue;
+    }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int perSM = 0, dev = 0, nSM = 0;
