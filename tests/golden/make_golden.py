@@ -10,6 +10,7 @@ point counts:
   c2  one component, dim 8, total order 4 (495 terms), tol 1e-6
   c3  6-D triangular map, total order 5, HermiteFunctions + Exp, tol 1e-7, banana samples
   c5  16-D triangular map, total order 3, tol 1e-8, inverse to xtol 1e-10
+  sig 3-D sigmoid triangular map, total order 2, three sigmoid terms (SoftPlus)
 """
 import os
 import sys
@@ -83,8 +84,34 @@ def make_c5(n=64):
     return dict(coef=coef, r=r, inverse=tm.inverse(coef, np.zeros((0, n)), r, xtol=1e-10, ytol=1e-10))
 
 
+def make_sig(n=200):
+    """Sigmoid expansions: a 3-D sigmoid triangular map of total order 2,
+    three Linear sigmoid terms per component (CreateSigmoidTriangular),
+    HermiteFunctions + SoftPlus; non-negative coefficients on the terms with
+    a last-input factor."""
+    cen = np.array([-3.0, 3.0, 0.0, -1.5, 1.5, -2.0, 0.0, 2.0])
+    centers = np.column_stack([cen, cen * 0.8, cen * 1.2])
+    tm = O.sigmoid_triangular(3, 3, 2, centers, 1.5, O.SUM_LINEAR, O.POS_SOFTPLUS)
+    rng = np.random.default_rng(5)
+    coef = rng.normal(0.0, 0.2, tm.num_coeffs)
+    diag = []  # the CoeffBounds lower bounds: terms with a last-input factor
+    for c in tm.comps:
+        s, d = c.starts, c.dims
+        for t in range(len(s) - 1):
+            diag.append(s[t + 1] > s[t] and d[s[t + 1] - 1] == c.input_dim - 1)
+    diag = np.array(diag)
+    coef[diag] = np.abs(coef[diag]) + 0.05
+    x = rng.standard_normal((3, n))
+    sens = rng.standard_normal((3, n))
+    r = tm.evaluate(coef, x)
+    return dict(centers=centers, coef=coef, x=x, sens=sens, evaluate=r, logdet=tm.logdet(coef, x),
+                coeff_grad=tm.coeff_grad(coef, x, sens), logdet_coeff_grad=tm.logdet_coeff_grad(coef, x),
+                gradient=tm.gradient(coef, x, sens), logdet_input_grad=tm.logdet_input_grad(coef, x),
+                inverse_cold=tm.inverse(coef, np.zeros((0, n)), r))
+
+
 if __name__ == "__main__":
     O.build()
-    for name, fn in (("c1", make_c1), ("c2", make_c2), ("c3", make_c3), ("c5", make_c5)):
+    for name, fn in (("c1", make_c1), ("c2", make_c2), ("c3", make_c3), ("c5", make_c5), ("sig", make_sig)):
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fn())
         print("wrote", name)

@@ -88,6 +88,40 @@ def _assert_within(got, ref, bound, mask=None, what=""):
                              f"gpu={got[i]!r} reference={ref[i]!r} bound={bound[i]!r}")
 
 
+def _sig_oracle(oracle, g):
+    return oracle.sigmoid_triangular(3, 3, 2, g["centers"], 1.5, oracle.SUM_LINEAR, oracle.POS_SOFTPLUS)
+
+
+def test_oracle_reproduces_sig(oracle):
+    g = load("sig")
+    tm = _sig_oracle(oracle, g)
+    c, x = g["coef"], g["x"]
+    close(tm.evaluate(c, x), g["evaluate"], 1e-12, what="sig evaluate")
+    close(tm.logdet(c, x), g["logdet"], 1e-12, what="sig logdet")
+    close(tm.coeff_grad(c, x, g["sens"]), g["coeff_grad"], 1e-12, what="sig coeff_grad")
+    close(tm.logdet_input_grad(c, x), g["logdet_input_grad"], 1e-12, what="sig logdet_input_grad")
+    close(tm.inverse(c, np.zeros((0, x.shape[1])), g["evaluate"]), g["inverse_cold"], 1e-9, what="sig inverse")
+
+
+@pytest.mark.gpu
+def test_gpu_matches_golden_sig(gpu, oracle):
+    M = gpu
+    g = load("sig")
+    opts = M.MapOptions(basisType=M.BasisTypes.HermiteFunctions, posFuncType=M.PosFuncTypes.SoftPlus)
+    tm = M.CreateSigmoidTriangular(3, 3, 2, g["centers"], opts)
+    tm.SetCoeffs(g["coef"])
+    x, sens = _t(g["x"]), _t(g["sens"])
+    close(_h(tm.Evaluate(x)), g["evaluate"], 1e-10, what="sig evaluate")
+    close(_h(tm.LogDeterminant(x)), g["logdet"], 1e-10, what="sig logdet")
+    close(_h(tm.CoeffGrad(x, sens)), g["coeff_grad"], 1e-10, what="sig coeff_grad")
+    close(_h(tm.LogDeterminantCoeffGrad(x)), g["logdet_coeff_grad"], 1e-10, what="sig logdet_coeff_grad")
+    close(_h(tm.Gradient(x, sens)), g["gradient"], 1e-10, what="sig gradient")
+    close(_h(tm.LogDeterminantInputGrad(x)), g["logdet_input_grad"], 1e-10, what="sig logdet_input_grad")
+    n = g["x"].shape[1]
+    xi = _h(tm.Inverse(_t(np.zeros((0, n))), _t(g["evaluate"])))
+    assert np.abs(xi - g["inverse_cold"]).max() <= 1e-5
+
+
 @pytest.mark.gpu
 def test_gpu_matches_golden_c1(gpu, oracle):
     M = gpu
