@@ -755,10 +755,12 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
     return v;
 }
 
-// The rectifier cache of a reduced sigmoid-expansion launch (rcTotal doubles,
-// from itemsPerComp).  Above 2 GiB the reduction evaluates the rectifier again.
+// The node cache of a reduced launch (rcTotal doubles, from itemsPerComp):
+// phase A keeps per tile the rectified products of a sigmoid expansion, or
+// the deeper prefix products of a monotone component, for the reduction.
+// Above 2 GiB the reduction forms them again.
 static double* rectCache(MapWorkspace& W, long long rcTotal, cudaStream_t stream) {
-    if (W.basis != kBasisSigmoid || rcTotal <= 0 || rcTotal > (2LL << 30) / (long long)sizeof(double)) return nullptr;
+    if (rcTotal <= 0 || rcTotal > (2LL << 30) / (long long)sizeof(double)) return nullptr;
     W.rcache.ensure((size_t)rcTotal * sizeof(double), stream);
     return W.rcache.as<double>();
 }

@@ -401,10 +401,14 @@ __device__ __forceinline__ void fillLead(const CompDesc& c, const SmemLayout& L,
     }
 }
 
-// Phase A: a_k = sum_m c_(m,k) Phi_m for this thread's point.
+// Phase A: a_k = sum_m c_(m,k) Phi_m for this thread's point.  With pc, the
+// products of the term-carrying nodes of depth >= 2 are kept there (one row of
+// blockDim doubles per node of nodeC) for the reduction, which would form them
+// again from the basis table; the incremental product here multiplies the
+// same factors in the same order as prefixProduct, so the values are equal.
 template <int PMAX>
 __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, int tid, const double* cm,
-                                       double* a) {
+                                       double* a, double* pc = nullptr) {
 #pragma unroll
     for (int k = 0; k <= PMAX; ++k) a[k] = 0.0;
     const int tpb = blockDim.x;
@@ -419,7 +423,10 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
             phi = L.S[(depth - 1) * tpb + tid] * L.B[brow * L.bstride + tid];
             L.S[depth * tpb + tid] = phi;
         }
-        if (nk) accumCoeffs<PMAX>(nk, phi, cm + __ldg(&c.nodeSlot[n]), a);
+        if (nk) {
+            if (pc && depth >= 2) pc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = phi;
+            accumCoeffs<PMAX>(nk, phi, cm + __ldg(&c.nodeSlot[n]), a);
+        }
     }
 }
 
@@ -509,11 +516,10 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             double a[PMAX + 1];
             // (sigmoid expansions: the rectified products R(Phi_m) of this tile,
             // kept for the reduction below)
-            double* rc = nullptr;
-            if constexpr (BASIS == kBasisSigmoid)
-                if (prm.rcache && (flags & kFlagCoefReduced)) rc = prm.rcache + item.rcBase;
+            // (monotone components: the products of the deeper prefix nodes)
+            double* rc = (prm.rcache && (flags & kFlagCoefReduced)) ? prm.rcache + item.rcBase : nullptr;
             if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, a, rc);
-            else phaseA<PMAX>(c, L, tid, cm, a);
+            else phaseA<PMAX>(c, L, tid, cm, a, rc);
             const double xd = L.X[(c.D - 1) * tpb + tid];
 
             // wv[k] = dT/da_k; d1x, d2x: last-input basis derivatives at x_D;
@@ -722,15 +728,18 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     double acc[PMAX + 1];
 #pragma unroll
                     for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
+                    // (monotone components: products kept by phase A for nodes of depth >= 2)
+                    const double* kept = (BASIS != kBasisSigmoid && rc && depth >= 2) ? rc + (long long)n * tpb : nullptr;
                     for (int j = sg * segLen; j < (sg + 1) * segLen; ++j) {
-                        const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
                         if constexpr (BASIS == kBasisSigmoid) {
+                            const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
                             const double a0 = fma(phi, L.W[j], acc[0]);
                             double rv = phi;
                             if (c.rectify && nk > 1) rv = rc ? rc[(long long)n * tpb + j] : posValue<POS>(phi);
                             accumSlots<PMAX>(nk, rv, L.W + j, tpb, acc);
                             acc[0] = a0;
                         } else {
+                            const double phi = kept ? kept[j] : prefixProduct(depth, r, L.B, L.bstride, j);
                             accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
                         }
                     }
