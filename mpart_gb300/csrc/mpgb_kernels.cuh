@@ -730,17 +730,21 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
                     // (monotone components: products kept by phase A for nodes of depth >= 2)
                     const double* kept = (BASIS != kBasisSigmoid && rc && depth >= 2) ? rc + (long long)n * tpb : nullptr;
-                    for (int j = sg * segLen; j < (sg + 1) * segLen; ++j) {
-                        if constexpr (BASIS == kBasisSigmoid) {
+                    if (kept) {
+                        for (int j = sg * segLen; j < (sg + 1) * segLen; ++j)
+                            accumSlots<PMAX>(nk, kept[j], L.W + j, tpb, acc);
+                    } else {
+                        for (int j = sg * segLen; j < (sg + 1) * segLen; ++j) {
                             const double phi = prefixProduct(depth, r, L.B, L.bstride, j);
-                            const double a0 = fma(phi, L.W[j], acc[0]);
-                            double rv = phi;
-                            if (c.rectify && nk > 1) rv = rc ? rc[(long long)n * tpb + j] : posValue<POS>(phi);
-                            accumSlots<PMAX>(nk, rv, L.W + j, tpb, acc);
-                            acc[0] = a0;
-                        } else {
-                            const double phi = kept ? kept[j] : prefixProduct(depth, r, L.B, L.bstride, j);
-                            accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
+                            if constexpr (BASIS == kBasisSigmoid) {
+                                const double a0 = fma(phi, L.W[j], acc[0]);
+                                double rv = phi;
+                                if (c.rectify && nk > 1) rv = rc ? rc[(long long)n * tpb + j] : posValue<POS>(phi);
+                                accumSlots<PMAX>(nk, rv, L.W + j, tpb, acc);
+                                acc[0] = a0;
+                            } else {
+                                accumSlots<PMAX>(nk, phi, L.W + j, tpb, acc);
+                            }
                         }
                     }
 #pragma unroll
