@@ -401,11 +401,17 @@ __device__ __forceinline__ void fillLead(const CompDesc& c, const SmemLayout& L,
     }
 }
 
+// Depth from which phase A keeps the prefix products of monotone components
+// for the reduction (shallower products cost the reduction at most one
+// multiply and are formed again).
+constexpr int kKeepMinDepth = 2;
+
 // Phase A: a_k = sum_m c_(m,k) Phi_m for this thread's point.  With pc, the
-// products of the term-carrying nodes of depth >= 2 are kept there (one row of
-// blockDim doubles per node of nodeC) for the reduction, which would form them
-// again from the basis table; the incremental product here multiplies the
-// same factors in the same order as prefixProduct, so the values are equal.
+// products of the term-carrying nodes of depth >= kKeepMinDepth are kept there
+// (one row of blockDim doubles per node of nodeC) for the reduction, which
+// would form them again from the basis table; the incremental product here
+// multiplies the same factors in the same order as prefixProduct, so the
+// values are equal.
 template <int PMAX>
 __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, int tid, const double* cm,
                                        double* a, double* pc = nullptr) {
@@ -424,7 +430,7 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
             L.S[depth * tpb + tid] = phi;
         }
         if (nk) {
-            if (pc && depth >= 2) pc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = phi;
+            if (pc && depth >= kKeepMinDepth) pc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = phi;
             accumCoeffs<PMAX>(nk, phi, cm + __ldg(&c.nodeSlot[n]), a);
         }
     }
@@ -728,9 +734,19 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     double acc[PMAX + 1];
 #pragma unroll
                     for (int k = 0; k <= PMAX; ++k) acc[k] = 0.0;
-                    // (monotone components: products kept by phase A for nodes of depth >= 2)
-                    const double* kept = (BASIS != kBasisSigmoid && rc && depth >= 2) ? rc + (long long)n * tpb : nullptr;
-                    if (kept) {
+                    // (monotone components: products kept by phase A for the deeper nodes)
+                    const double* kept =
+                        (BASIS != kBasisSigmoid && rc && depth >= kKeepMinDepth) ? rc + (long long)n * tpb : nullptr;
+                    if (kept && segLen % 8 == 0) {
+                        // Eight loads in flight before their sums.
+                        for (int j = sg * segLen; j < (sg + 1) * segLen; j += 8) {
+                            double v[8];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) v[q] = kept[j + q];
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) accumSlots<PMAX>(nk, v[q], L.W + j + q, tpb, acc);
+                        }
+                    } else if (kept) {
                         for (int j = sg * segLen; j < (sg + 1) * segLen; ++j)
                             accumSlots<PMAX>(nk, kept[j], L.W + j, tpb, acc);
                     } else {
