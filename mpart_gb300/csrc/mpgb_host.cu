@@ -323,6 +323,7 @@ struct MapWorkspace {
     DevBuf rcache;       // rectifier cache of sigmoid expansions (reduced adjoints)
     DevBuf inverseDefer; // two-pass inverse: count, deferred component per point, deferred list
     DevBuf inverseKey;   // inverse processing order: per-target sort keys
+    DevBuf inverseA;     // inverse: a_k of the component being solved, (pmax + 1) x N
     bool ordering = true;
 };
 
@@ -980,30 +981,50 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
     p.quad = W.quad; p.bc = W.bc;
     const int nBlocks = (int)((N + kTpb - 1) / kTpb);
-    // Two passes (see InverseParams): the first gives each point a few
-    // bracket-doubling steps per component, the second finishes the points
-    // that needed more.  Results are those of one pass with the full 128 steps.
     const bool twoPass = N >= 2 * kTpb;
-    p.bracketBudget = twoPass ? kFirstPassBracketIts : (int)kBracketIts;
-    if (twoPass) {
-        W.inverseDefer.ensure((size_t)(2 * N + 1) * sizeof(int), stream);
-        int* base = W.inverseDefer.as<int>();
-        p.deferCount = base;
-        p.deferComp = base + 1;
-        p.deferList = base + 1 + N;
-        MPGB_CUDA(cudaMemsetAsync(p.deferCount, 0, sizeof(int), stream));
+    if (!twoPass) {
+        // Few points: one launch solves every component in turn.
+        p.bracketBudget = (int)kBracketIts;
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
+        Finish(stream, "Inverse");
+        return;
     }
-    // First pass in order of sum_c |r_c|: targets of similar cost share warps.
-    if (twoPass && W.ordering) {
+    // One component at a time, in two passes each (see InverseParams): the
+    // first gives every point a few bracket-doubling steps, the second
+    // finishes the points that needed more.  Results are those of one pass
+    // with the full 128 steps.  For monotone components a key launch first
+    // forms phase A of every point (kept for the solver) and a root estimate,
+    // and the first pass takes the points in order of |estimate| (a stable
+    // counting sort): lanes whose solver steps integrate over similar ranges
+    // share warps.
+    W.inverseDefer.ensure((size_t)(2 * N + 1) * sizeof(int), stream);
+    int* base = W.inverseDefer.as<int>();
+    p.deferCount = base;
+    p.deferComp = base + 1;
+    p.deferList = base + 1 + N;
+    p.bracketBudget = kFirstPassBracketIts;
+    const bool keyed = W.ordering && W.basis != kBasisSigmoid;
+    if (keyed) {
         W.inverseKey.ensure((size_t)N * sizeof(double), stream);
+        W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
         W.perm.ensure((size_t)N * sizeof(int), stream);
         W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
-        MPGB_CUDA(launchTargetKey(r.data, r.rowStride, r.colStride, (int)r.rows, N, W.inverseKey.as<double>(), stream));
-        MPGB_CUDA(launchSortByLast(W.inverseKey.as<double>(), 1, N, W.sortHist.as<int>(), W.perm.as<int>(), stream));
-        p.perm = W.perm.as<int>();
     }
-    MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
-    if (twoPass) {
+    for (int c = 0; c < p.nComps; ++c) {
+        p.compBegin = c;
+        p.compEnd = c + 1;
+        if (keyed) {
+            InverseParams k = p;
+            k.keyPass = 1;
+            k.acoef = W.inverseA.as<double>();
+            k.key = W.inverseKey.as<double>();
+            MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, k, nBlocks, stream));
+            MPGB_CUDA(launchSortByLast(k.key, 1, N, W.sortHist.as<int>(), W.perm.as<int>(), stream));
+            p.perm = W.perm.as<int>();
+            p.acoef = k.acoef;
+        }
+        MPGB_CUDA(cudaMemsetAsync(p.deferCount, 0, sizeof(int), stream));
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
         InverseParams q = p;
         q.list = p.deferList;
         MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));

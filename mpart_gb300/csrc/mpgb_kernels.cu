@@ -395,25 +395,6 @@ cudaError_t launchSigmoidEval(const CompDesc& c, int maxOrder, const double* x, 
     return e;
 }
 
-// Sort key of an inverse target: sum over the components of |r_c| (the
-// bracket search and the quadratures grow with the size of the solution).
-__global__ void targetKeyKernel(const double* r, long long rs, long long cs, int rows, long long n, double* key) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double s = 0.0;
-    for (int c = 0; c < rows; ++c) s += fabs(r[c * rs + i * cs]);
-    key[i] = s;
-}
-
-cudaError_t launchTargetKey(const double* r, long long rs, long long cs, int rows, long long n, double* key,
-                            cudaStream_t stream) {
-    if (n <= 0) return cudaSuccess;
-    targetKeyKernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(r, rs, cs, rows, n, key);
-    const cudaError_t e = cudaGetLastError();
-    countLaunches(stream, 1);
-    return e;
-}
-
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream) {
     dfmaPeakKernel<<<blocks, threads, 0, stream>>>(out, iters, 1.0);
     const cudaError_t e = cudaGetLastError();

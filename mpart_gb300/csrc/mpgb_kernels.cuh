@@ -1052,12 +1052,14 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     const bool second = prm.list != nullptr;
     const bool active = slot < (second ? (long long)*prm.deferCount : prm.N);
     const long long i = !active ? slot : second ? (long long)prm.list[slot] : prm.perm ? (long long)prm.perm[slot] : slot;
-    const int cStart = (active && second) ? prm.deferComp[i] : 0;
+    const int cStart = (active && second) ? prm.deferComp[i] : prm.compBegin;
+    const int cEnd = prm.compEnd > 0 ? prm.compEnd : prm.nComps;
     const unsigned budget = second ? kBracketIts : (unsigned)prm.bracketBudget;
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const int inDim = prm.comps[prm.nComps - 1].D;
-    // fullOut = [x1; 0] (TriangularMap.cpp:146-159); in the second pass the
-    // coordinates of the components solved in the first pass come from out.
+    // fullOut = [x1; 0] (TriangularMap.cpp:146-159); the coordinates of the
+    // components solved before (earlier launches, or the first pass) come
+    // from out.
     const long long xi = (prm.x1Cols == 1) ? 0 : i;
     for (int d = 0; d < inDim; ++d) {
         double v = 0.0;
@@ -1072,12 +1074,15 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     // Every thread runs every component (the warp-wide solver loop needs all
     // lanes); lanes that are inactive, stopped or before their start component
     // only take part in the loop.
-    for (int ci = 0; ci < prm.nComps; ++ci) {
+    for (int ci = prm.compBegin; ci < cEnd; ++ci) {
         const CompDesc& c = prm.comps[ci];
         const bool mine = !stopped && ci >= cStart;
         const double* cm = prm.cm + c.slotOffset;
         ACoef<PMAX> A;
-        if (mine) {
+        if (mine && prm.acoef) {
+#pragma unroll
+            for (int k = 0; k <= PMAX; ++k) A.a[k] = prm.acoef[(long long)k * prm.N + i];
+        } else if (mine) {
             fillLead<BASIS, false>(c, L, tid, prm.bc);
             if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a, nullptr);
             else phaseA<PMAX>(c, L, tid, cm, A.a);
@@ -1119,6 +1124,42 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
         if (prm.info) prm.info[(long long)ci * prm.infoStride + i] = info;
     }
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
+}
+
+// Key pass of the Inverse for component compBegin (monotone components):
+// phase A of every point, kept in acoef for the solver launches, and the root
+// estimate (r_c - T(x_<c, 0)) / dT/dx_D(x_<c, 0) of one Newton step from 0 as
+// the sort key.  The quadratures of a point's solver steps cost in proportion
+// to the range [0, x] they integrate, which the estimate predicts.
+template <int BASIS, int POS, int PMAX>
+__global__ void __launch_bounds__(256) inverseKeyKernel(const __grid_constant__ InverseParams prm) {
+    extern __shared__ double smem[];
+    const int tid = threadIdx.x;
+    const int tpb = blockDim.x;
+    const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
+    const long long i = (long long)blockIdx.x * tpb + tid;
+    if (i >= prm.N) return;  // no block-wide synchronisation below
+    const CompDesc& c = prm.comps[prm.compBegin];
+    const long long xi = (prm.x1Cols == 1) ? 0 : i;
+    for (int d = 0; d < c.D; ++d) {
+        double v = 0.0;
+        if (d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+        else if (d - prm.extra < prm.compBegin) v = prm.out[(long long)(d - prm.extra) * prm.outRs + i * prm.outCs];
+        L.X[d * tpb + tid] = v;
+    }
+    ACoef<PMAX> A;
+    fillLead<BASIS, false>(c, L, tid, prm.bc);
+    phaseA<PMAX>(c, L, tid, prm.cm + c.slotOffset, A.a);
+    double f0 = 0.0;
+#pragma unroll
+    for (int k = 0; k <= PMAX; ++k) {
+        prm.acoef[(long long)k * prm.N + i] = A.a[k];
+        f0 = fma(A.a[k], prm.bc.v0[k], f0);
+    }
+    int st = 0;
+    const InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
+    const double yd = prm.r[(long long)prm.compBegin * prm.rRs + i * prm.rCs];
+    prm.key[i] = (yd - f0) / f.slope(0.0);
 }
 
 // --------------------------------------------------------------------------
@@ -1176,8 +1217,16 @@ cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int*
 
 template <int BASIS, int POS, int PMAX>
 cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t stream) {
-    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
-    auto kern = inverseKernel<BASIS, POS, PMAX>;
+    // Solver launches that read phase A from acoef use the coordinate rows of
+    // the layout (its first part) only.
+    const size_t smem = (prm.acoef && !prm.keyPass)
+                            ? (size_t)prm.dmax * prm.tpb * sizeof(double)
+                            : smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
+    void (*kern)(InverseParams) = inverseKernel<BASIS, POS, PMAX>;
+    if (prm.keyPass) {
+        if constexpr (BASIS == kBasisSigmoid) return cudaErrorInvalidValue;
+        else kern = inverseKeyKernel<BASIS, POS, PMAX>;
+    }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<nBlocks, prm.tpb, smem, stream>>>(prm);

@@ -36,9 +36,6 @@ size_t sortScratchInts(long long N);
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
                              cudaStream_t stream);
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
-// key[i] = sum_c |r(c, i)| for the inverse's processing order.
-cudaError_t launchTargetKey(const double* r, long long rs, long long cs, int rows, long long n, double* key,
-                            cudaStream_t stream);
 // Sigmoid1d basis (c.sig* fields, device arrays) at n points x[i * stride]:
 // out / d1 / d2 are (maxOrder + 1) x n, row stride n; d1, d2 may be null.
 cudaError_t launchSigmoidEval(const CompDesc& c, int maxOrder, const double* x, long long n, long long stride,

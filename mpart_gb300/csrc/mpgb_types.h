@@ -145,21 +145,32 @@ struct InverseParams {
     int* statusWord;
     double xtol, ytol;
     double nugget;
-    int dmax, nBmax, depthMax, pad_;
+    int dmax, nBmax, depthMax;
+    // Components [compBegin, compEnd) are solved (compEnd 0: to the last);
+    // the coordinates of the components before compBegin come from out.
+    int compBegin;
     // Two passes: in the first (list null) every point has bracketBudget
     // doubling steps per component; a point that needs more stops at that
     // component, which deferComp[i] records, and i is appended to deferList.
     // The second pass (list = deferList) runs the *deferCount points of the
     // list from their deferComp component with the full kBracketIts steps, so
     // the points with long or failing bracket searches share warps with each
-    // other only.  Its grid covers N points; blocks past the count return.
+    // other only.  Its grid covers N points; threads past the count only take
+    // part in the warp loops.
     int bracketBudget;
-    int pad2_;
+    int compEnd;
     const int* list;
     const int* perm;  // first pass: point of each slot (points grouped by expected cost), or null
     int* deferComp;
     int* deferList;
     int* deferCount;
+    // Key pass (keyPass = 1, component compBegin): phase A of every point goes
+    // to acoef (row k at acoef + k N) and a root estimate to key.  The solver
+    // launches then read the a_k from acoef (when non-null).
+    double* acoef;
+    double* key;
+    int keyPass;
+    int pad3_;
     QuadParams quad;
     BasisConsts bc;
 };
