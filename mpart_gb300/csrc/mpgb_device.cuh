@@ -46,6 +46,10 @@ constexpr int kStatusNoBracket = 8;    // inverse: bracket search failed (info=-
 // budget (solved again in the second pass; never returned to callers).
 constexpr int kInfoDeferred = -3;
 constexpr unsigned kBracketIts = 128;  // FindBracket's step limit (RootFinding.h:29)
+// Largest sort key of a deferred inverse point: below 36, so that deferred
+// points stay out of sortBucket's last bucket, which holds the NaN keys of
+// the points that were not deferred.
+constexpr double kDeferKeyMax = 30.0;
 
 // Quadrature kinds (MapOptions::quadType values).
 constexpr int kQuadFixedCC = 0;   // ClenshawCurtis: one fixed rule on [0, 1] (Quadrature.h:114-143)

@@ -321,7 +321,7 @@ struct MapWorkspace {
     DevBuf perm, sortHist;
     DevBuf implicitAcc;  // back-substitution sums when the caller wants no input gradient
     DevBuf rcache;       // rectifier cache of sigmoid expansions (reduced adjoints)
-    DevBuf inverseDefer; // two-pass inverse: count, deferred component per point, deferred list
+    DevBuf inverseDefer; // two-pass inverse: number of deferred points
     DevBuf inverseKey;   // inverse processing order: per-target sort keys
     DevBuf inverseA;     // inverse: a_k of the component being solved, (pmax + 1) x N
     bool ordering = true;
@@ -665,8 +665,7 @@ struct LaunchCommon {
 constexpr int kTpb = 128;
 // Bracket-doubling steps per component in the inverse's first pass: roots
 // within 7 of the initial guess are bracketed there, the rest wait for the
-// second pass (16-D order-3 map, 1M standard-normal targets: 2.22 s with 3
-// steps, 2.43 s with 4, 2.92 s with 16).
+// second pass.
 constexpr int kFirstPassBracketIts = 3;
 
 void checkMatrix(const StridedMatrix& m, int64_t rows, int64_t cols, const char* what, const char* fn) {
@@ -981,53 +980,58 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
     p.quad = W.quad; p.bc = W.bc;
     const int nBlocks = (int)((N + kTpb - 1) / kTpb);
-    const bool twoPass = N >= 2 * kTpb;
-    if (!twoPass) {
+    if (N < 2 * kTpb) {
         // Few points: one launch solves every component in turn.
         p.bracketBudget = (int)kBracketIts;
         MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
         Finish(stream, "Inverse");
         return;
     }
-    // One component at a time, in two passes each (see InverseParams): the
-    // first gives every point a few bracket-doubling steps, the second
-    // finishes the points that needed more.  Results are those of one pass
-    // with the full 128 steps.  For monotone components a key launch first
-    // forms phase A of every point (kept for the solver) and a root estimate,
-    // and the first pass takes the points in order of |estimate| (a stable
-    // counting sort): lanes whose solver steps integrate over similar ranges
-    // share warps.
-    W.inverseDefer.ensure((size_t)(2 * N + 1) * sizeof(int), stream);
-    int* base = W.inverseDefer.as<int>();
-    p.deferCount = base;
-    p.deferComp = base + 1;
-    p.deferList = base + 1 + N;
-    p.bracketBudget = kFirstPassBracketIts;
+    // One component at a time, in two passes (see InverseParams): the first
+    // gives every point kFirstPassBracketIts bracket-doubling steps, the
+    // second finishes the points that needed more.  For monotone components a
+    // key launch first forms phase A of every point (kept for the solver) and
+    // a root estimate, and the first pass takes the points in order of
+    // |estimate|; the second takes the deferred points in order of the
+    // estimate the first pass leaves for them (stable counting sorts).  Lanes
+    // whose solver steps integrate over similar ranges then share warps.
+    W.inverseDefer.ensure(sizeof(int), stream);
+    W.inverseKey.ensure((size_t)N * sizeof(double), stream);
+    W.perm.ensure((size_t)N * sizeof(int), stream);
+    W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
+    int* deferCount = W.inverseDefer.as<int>();
+    double* key = W.inverseKey.as<double>();
+    int* perm = W.perm.as<int>();
     const bool keyed = W.ordering && W.basis != kBasisSigmoid;
-    if (keyed) {
-        W.inverseKey.ensure((size_t)N * sizeof(double), stream);
-        W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
-        W.perm.ensure((size_t)N * sizeof(int), stream);
-        W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
-    }
+    if (keyed) W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
     for (int c = 0; c < p.nComps; ++c) {
-        p.compBegin = c;
-        p.compEnd = c + 1;
+        InverseParams first = p;
+        first.compBegin = c;
+        first.compEnd = c + 1;
+        first.bracketBudget = kFirstPassBracketIts;
         if (keyed) {
-            InverseParams k = p;
+            InverseParams k = first;
             k.keyPass = 1;
             k.acoef = W.inverseA.as<double>();
-            k.key = W.inverseKey.as<double>();
+            k.key = key;
             MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, k, nBlocks, stream));
-            MPGB_CUDA(launchSortByLast(k.key, 1, N, W.sortHist.as<int>(), W.perm.as<int>(), stream));
-            p.perm = W.perm.as<int>();
-            p.acoef = k.acoef;
+            MPGB_CUDA(launchSortByLast(key, 1, N, W.sortHist.as<int>(), perm, stream));
+            first.perm = perm;
+            first.acoef = k.acoef;
         }
-        MPGB_CUDA(cudaMemsetAsync(p.deferCount, 0, sizeof(int), stream));
-        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, p, nBlocks, stream));
-        InverseParams q = p;
-        q.list = p.deferList;
-        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
+        MPGB_CUDA(cudaMemsetAsync(key, 0xff, (size_t)N * sizeof(double), stream));  // NaN: not deferred
+        MPGB_CUDA(cudaMemsetAsync(deferCount, 0, sizeof(int), stream));
+        first.deferKey = key;
+        first.deferCount = deferCount;
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, first, nBlocks, stream));
+        MPGB_CUDA(launchSortByLast(key, 1, N, W.sortHist.as<int>(), perm, stream));
+        InverseParams second = first;
+        second.perm = perm;
+        second.listCount = deferCount;
+        second.bracketBudget = (int)kBracketIts;
+        second.deferKey = nullptr;
+        second.deferCount = nullptr;
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, second, nBlocks, stream));
     }
     Finish(stream, "Inverse");
 }

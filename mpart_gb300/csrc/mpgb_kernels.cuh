@@ -1000,7 +1000,13 @@ struct RootSolve {
                 if (more) { ylb = yub; xlb = xub; step *= 2.0; }
             }
             if (!more) { bracketed(yd, xtol, ftol); return; }
-            if (++it >= maxBracket) { finish(nan, (maxBracket < kBracketIts) ? kInfoDeferred : -2); return; }
+            if (++it >= maxBracket) {
+                // Out of a first-pass budget: the result is a root estimate
+                // for ordering the second pass (a Newton step from here).
+                if (maxBracket < kBracketIts) finish(x + (yd - y) / f.slope(x), kInfoDeferred);
+                else finish(nan, -2);
+                return;
+            }
             x = (dir < 0) ? xub - step : xlb + step;
             return;
         }
@@ -1049,12 +1055,16 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     const int tpb = blockDim.x;
     const SmemLayout L = carveSmem(smem, tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, false);
     const long long slot = (long long)blockIdx.x * tpb + tid;
-    const bool second = prm.list != nullptr;
-    const bool active = slot < (second ? (long long)*prm.deferCount : prm.N);
-    const long long i = !active ? slot : second ? (long long)prm.list[slot] : prm.perm ? (long long)prm.perm[slot] : slot;
-    const int cStart = (active && second) ? prm.deferComp[i] : prm.compBegin;
+    const bool second = prm.listCount != nullptr;
+    const long long n = second ? (long long)*prm.listCount : prm.N;
+    const bool active = slot < n;
+    // perm lists the points by increasing cost estimate; both passes take it
+    // from the end, so the expensive blocks start first and the cheap ones
+    // fill the tail of the launch.
+    const long long i = !active ? slot : prm.perm ? (long long)prm.perm[n - 1 - slot] : slot;
+    const int cStart = prm.compBegin;
     const int cEnd = prm.compEnd > 0 ? prm.compEnd : prm.nComps;
-    const unsigned budget = second ? kBracketIts : (unsigned)prm.bracketBudget;
+    const unsigned budget = (unsigned)prm.bracketBudget;
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const int inDim = prm.comps[prm.nComps - 1].D;
     // fullOut = [x1; 0] (TriangularMap.cpp:146-159); the coordinates of the
@@ -1112,9 +1122,12 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
         }
         if (!mine) continue;
         if (info == kInfoDeferred) {
-            // Out of first-pass budget: the second pass solves this point from here.
-            prm.deferComp[i] = ci;
-            prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
+            // Out of the first pass's budget: the second pass solves the point.
+            // result is a root estimate (a Newton step from the last bracket
+            // point); the key orders the deferred points by its magnitude.
+            const double kk = log2(1.0 + fabs(result));
+            prm.deferKey[i] = isnan(kk) ? kDeferKeyMax : fmin(kk, kDeferKeyMax);
+            atomicAdd(prm.deferCount, 1);
             stopped = true;
             continue;
         }

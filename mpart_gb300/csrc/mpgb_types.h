@@ -149,20 +149,20 @@ struct InverseParams {
     // Components [compBegin, compEnd) are solved (compEnd 0: to the last);
     // the coordinates of the components before compBegin come from out.
     int compBegin;
-    // Two passes: in the first (list null) every point has bracketBudget
-    // doubling steps per component; a point that needs more stops at that
-    // component, which deferComp[i] records, and i is appended to deferList.
-    // The second pass (list = deferList) runs the *deferCount points of the
-    // list from their deferComp component with the full kBracketIts steps, so
-    // the points with long or failing bracket searches share warps with each
-    // other only.  Its grid covers N points; threads past the count only take
-    // part in the warp loops.
+    // Two passes per component.  The first takes every point (in perm order
+    // when perm is set) with bracketBudget doubling steps; a point that needs
+    // more stops, adds one to *deferCount and writes its sort key (from a
+    // root estimate) to deferKey[i].  The second (listCount set) takes the
+    // *listCount points of perm, the deferred ones sorted by that key, with
+    // the full kBracketIts steps.  Restarted with a larger budget a solve
+    // repeats the same evaluations, so the results are those of one pass with
+    // the full budget.  The second pass's grid covers N points; threads past
+    // the count only take part in the warp loops.
     int bracketBudget;
     int compEnd;
-    const int* list;
-    const int* perm;  // first pass: point of each slot (points grouped by expected cost), or null
-    int* deferComp;
-    int* deferList;
+    const int* perm;  // the points by increasing expected cost (taken from the end), or null
+    const int* listCount;
+    double* deferKey;
     int* deferCount;
     // Key pass (keyPass = 1, component compBegin): phase A of every point goes
     // to acoef (row k at acoef + k N) and a root estimate to key.  The solver
