@@ -1031,7 +1031,10 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         second.bracketBudget = (int)kBracketIts;
         second.deferKey = nullptr;
         second.deferCount = nullptr;
-        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, second, nBlocks, stream));
+        // One warp per block: the second pass often has few points, whose
+        // warps then spread over the SMs instead of sharing a few of them.
+        second.tpb = 32;
+        MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, second, (int)((N + 31) / 32), stream));
     }
     Finish(stream, "Inverse");
 }
