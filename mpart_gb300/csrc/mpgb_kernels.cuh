@@ -88,7 +88,7 @@ __device__ __forceinline__ void evalNode(double t, double xd, const double* as, 
         if (PMAX >= 1) H[1] = 2.0 * y;
 #pragma unroll
         for (int j = 2; j <= PMAX; ++j) H[j] = (j + 2 <= P) ? (2.0 * y * H[j - 1] - 2.0 * (j - 1.0) * H[j - 2]) : 0.0;
-        env = (P >= 2) ? exp(-0.5 * y * y) : 0.0;
+        env = (P >= 2) ? fm::expT(-0.5 * y * y) : 0.0;
         double acc = 0.0, acc2 = 0.0;
         if (PMAX >= 1) u[1] = 1.0;
 #pragma unroll
