@@ -282,6 +282,35 @@ def test_c5_inverse_small(gpu, oracle):
     assert np.max(np.abs(back - r[:, ok])) < 1e-7
 
 
+@pytest.mark.parametrize("basis,pos,scale,rscale", [(0, 1, 0.05, 3.0), (2, 0, 0.1, 2.0)])
+def test_inverse_two_pass_far_and_missing_roots(gpu, oracle, basis, pos, scale, rscale):
+    """More than 256 targets take the per-component two-pass solver (points in
+    the order of a root estimate; targets needing more than 3 bracket
+    doublings finished in a second, sorted pass).  Wide targets give far roots
+    and targets without a root (NaN, as in the reference); the results match
+    the oracle component by component and do not depend on the processing
+    order (point ordering off: bitwise-equal roots).  The scales keep the
+    integrand finite at the far roots (with larger Hermite-function
+    coefficients exp(df) overflows there, which the GPU reports as an
+    IntegrandError)."""
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(4, 4, 3, opts(M, basis=basis, pos=pos, tol=1e-8))
+    om = oracle_tri(O, 4, 4, 3, basis=basis, pos=pos, tol=1e-8)
+    coef = np.random.default_rng(11).normal(0.0, scale, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    n = 777
+    r = rscale * np.random.default_rng(12).standard_normal((4, n))
+    x1 = np.zeros((0, n))
+    xi = H(tm.Inverse(T(x1), T(r), xtol=1e-10, ytol=1e-10))
+    assert_inverse_parity(om, coef, x1, r, xi, 1e-10, 1e-10)
+    # the workload reaches the second pass: some roots lie beyond 7
+    assert np.nanmax(np.abs(xi)) > 7.0
+    tm.SetPointOrdering(False)
+    xu = H(tm.Inverse(T(x1), T(r), xtol=1e-10, ytol=1e-10))
+    tm.SetPointOrdering(True)
+    np.testing.assert_array_equal(xu, xi)
+
+
 # ----------------------------------------------------------------------------
 # Edge cases and error behaviour.
 # ----------------------------------------------------------------------------
