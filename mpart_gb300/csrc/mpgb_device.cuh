@@ -84,6 +84,12 @@ struct BasisConsts {
     // HermiteFunction.h:26-46): r1[i] = sqrt((i-1)/2), r2[i] = 1/sqrt(i/2).
     double hfR1[kMaxLastOrder + 8], hfR2[kMaxLastOrder + 8];
     double piQuarter;  // pi^(-1/4)
+    // Derivatives of the leading-coordinate basis from the basis itself:
+    // probabilist Hermite phi_k' = leadDR[k] phi_(k-1) (k >= 2, leadDR[k] =
+    // k invNorm[k] / invNorm[k-1]) and phi_1' = leadDR[1] = invNorm[1];
+    // Hermite functions psi_j' = -x psi_j + hfSq2j[j] psi_(j-1), hfSq2j[j] = sqrt(2 j).
+    double leadDR[kMaxLastOrder + 1];
+    double hfSq2j[kMaxLastOrder + 8];
     // phit_k(0) for k = 0..kMaxLastOrder (phit_0 = 1).
     double v0[kMaxLastOrder + 1];
 };
@@ -258,34 +264,26 @@ __device__ __forceinline__ void lastBasis(double y, int P, const BasisConsts& bc
 }
 
 // --------------------------------------------------------------------------
-// Values (and optionally first derivatives) of orders 1..p of the basis in
-// one of the leading coordinates, written to out[(o-1)*stride] and
-// dout[(o-1)*stride].  Follows EvaluateAll (OrthogonalPolynomial.h:25-43,
-// HermiteFunction.h:26-46) up to rounding.
+// Values of orders 1..p of the basis in one of the leading coordinates,
+// written to out[(o-1)*stride].  Follows EvaluateAll (OrthogonalPolynomial.h:25-43,
+// HermiteFunction.h:26-46) up to rounding.  Their derivatives follow from the
+// values (leadDeriv).
 // --------------------------------------------------------------------------
-template <int BASIS, bool DERIV>
-__device__ __forceinline__ void leadBasis(double x, int p, const BasisConsts& bc, double* out, double* dout,
-                                          int stride) {
+template <int BASIS>
+__device__ __forceinline__ void leadBasis(double x, int p, const BasisConsts& bc, double* out, int stride) {
     if (p <= 0) return;
     if constexpr (BASIS == kBasisProbHermite) {
         double hm2 = 1.0, hm1 = x;  // He_0, He_1
-        double dm2 = 0.0, dm1 = 1.0;
         out[0] = x * bc.invNorm[1];
-        if constexpr (DERIV) dout[0] = bc.invNorm[1];
         for (int k = 2; k <= p; ++k) {
             const double h = x * hm1 - (k - 1.0) * hm2;
             out[(k - 1) * stride] = h * bc.invNorm[k];
-            if constexpr (DERIV) {
-                dout[(k - 1) * stride] = (double(k) * bc.invNorm[k]) * hm1;
-            }
             hm2 = hm1;
             hm1 = h;
-            (void)dm1; (void)dm2;
         }
     } else {
         // phi_1 = x; phi_{i+2} = psi_i by the normalised recurrence.
         out[0] = x;
-        if constexpr (DERIV) dout[0] = 1.0;
         if (p >= 2) {
             const double e = fm::expT(-0.5 * x * x);
             double pm2 = bc.piQuarter * e;             // psi_0
@@ -301,16 +299,23 @@ __device__ __forceinline__ void leadBasis(double x, int p, const BasisConsts& bc
                 pm2 = pm1;
                 pm1 = v;
             }
-            if constexpr (DERIV) {
-                // psi_j' = sqrt(j/2) psi_{j-1} - sqrt((j+1)/2) psi_{j+1}
-                //        = -x psi_j + sqrt(2 j) psi_{j-1}
-                for (int j = 0; j + 2 <= p; ++j) {
-                    const double pj = out[(j + 1) * stride];
-                    const double pjm1 = (j >= 1) ? out[j * stride] : 0.0;
-                    dout[(j + 1) * stride] = -x * pj + sqrt(2.0 * j) * pjm1;
-                }
-            }
         }
+    }
+}
+
+// Derivative of the leading-coordinate basis function of order k at x, from
+// its value v and the value vm1 of order k - 1 in the same coordinate
+// (used for k >= 2): probabilist Hermite phi_k' = k invNorm[k] He_(k-1)
+// (OrthogonalPolynomial.h:62-110); Hermite functions phi_1' = 1 and
+// psi_j' = -x psi_j + sqrt(2 j) psi_(j-1) (HermiteFunction.h:56-104).
+template <int BASIS>
+__device__ __forceinline__ double leadDeriv(int k, double x, double v, double vm1, const BasisConsts& bc) {
+    if constexpr (BASIS == kBasisProbHermite) {
+        return (k == 1) ? bc.leadDR[1] : bc.leadDR[k] * vm1;
+    } else {
+        if (k == 1) return 1.0;
+        if (k == 2) return -x * v;
+        return fma(-x, v, bc.hfSq2j[k - 2] * vm1);
     }
 }
 

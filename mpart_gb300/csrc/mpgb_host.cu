@@ -531,6 +531,10 @@ void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b) {
         b.hfR2[i] = i > 0 ? 1.0 / std::sqrt(0.5 * i) : 0.0;
     }
     b.piQuarter = std::pow(kPiHost, -0.25);
+    b.leadDR[0] = 0.0;
+    b.leadDR[1] = b.invNorm[1];
+    for (int k = 2; k <= kMaxLastOrder; ++k) b.leadDR[k] = k * b.invNorm[k] / b.invNorm[k - 1];
+    for (int j = 0; j < kMaxLastOrder + 8; ++j) b.hfSq2j[j] = std::sqrt(2.0 * j);
     // phit_k(0).
     {
         double he[kMaxLastOrder + 1], H[kMaxLastOrder + 1];

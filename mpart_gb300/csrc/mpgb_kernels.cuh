@@ -352,7 +352,6 @@ __device__ __forceinline__ double integrateValue(const double* a, int P, double 
 struct SmemLayout {
     double* X;   // [dmax][tpb]        coordinates of the tile's points
     double* B;   // [nBmax][tpb+1]     leading-coordinate basis values
-    double* Bd;  // [nBmax][tpb+1]     their derivatives (input gradient)
     double* S;   // [depthMax+1][tpb]  prefix-product stack
     double* W;   // [PMAX+1][tpb]      per-point adjoint weights
     double* GX;  // [dmax][tpb]        input gradient accumulators
@@ -364,8 +363,7 @@ __host__ __device__ inline size_t smemBytes(int tpb, int dmax, int nBmax, int de
     size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)(depthMax + 1) * tpb +
                (size_t)(pmax + 1) * tpb;
     if (input) {
-        n += (size_t)nBmax * (tpb + 1) + (size_t)dmax * tpb +
-             (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
+        n += (size_t)dmax * tpb + (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
     }
     return n * sizeof(double);
 }
@@ -380,24 +378,22 @@ __device__ inline SmemLayout carveSmem(double* base, int tpb, int dmax, int nBma
     L.S = p; p += (size_t)(depthMax + 1) * tpb;
     L.W = p; p += (size_t)(pmax + 1) * tpb;
     if (input) {
-        L.Bd = p; p += (size_t)nBmax * (tpb + 1);
         L.GX = p; p += (size_t)dmax * tpb;
         L.DS = p;
     } else {
-        L.Bd = nullptr; L.GX = nullptr; L.DS = nullptr;
+        L.GX = nullptr; L.DS = nullptr;
     }
     return L;
 }
 
 // Fill the leading-coordinate basis table for one thread.
-template <int BASIS, bool DERIV>
+template <int BASIS>
 __device__ __forceinline__ void fillLead(const CompDesc& c, const SmemLayout& L, int tid, const BasisConsts& bc) {
     for (int d = 0; d < c.D - 1; ++d) {
         const int p = __ldg(&c.leadDeg[d]);
         const int r = __ldg(&c.rowOff[d]);
         const double x = L.X[d * blockDim.x + tid];
-        leadBasis<BASIS, DERIV>(x, p, bc, &L.B[r * L.bstride + tid], DERIV ? &L.Bd[r * L.bstride + tid] : nullptr,
-                                L.bstride);
+        leadBasis<BASIS>(x, p, bc, &L.B[r * L.bstride + tid], L.bstride);
     }
 }
 
@@ -516,8 +512,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             const CompDesc& c = prm.comps[ci];
             const double* cm = prm.cm + c.slotOffset;
             const int P = c.P;
-            if (inputMode) fillLead<BASIS, true>(c, L, tid, prm.bc);
-            else fillLead<BASIS, false>(c, L, tid, prm.bc);
+            fillLead<BASIS>(c, L, tid, prm.bc);
 
             double a[PMAX + 1];
             // (sigmoid expansions: the rectified products R(Phi_m) of this tile,
@@ -672,7 +667,10 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                     const int depth = wd & 31, nk = (wd >> 5) & 31, dim = (wd >> 10) & 255, brow = wd >> 18;
                     if (depth > 0) {
                         const double bv = L.B[brow * L.bstride + tid];
-                        const double bd = L.Bd[brow * L.bstride + tid];
+                        // order of this factor within its coordinate's rows
+                        const int ko = brow - __ldg(&c.rowOff[dim]) + 1;
+                        const double bd = leadDeriv<BASIS>(ko, L.X[dim * tpb + tid], bv,
+                                                           ko > 1 ? L.B[(brow - 1) * L.bstride + tid] : 0.0, prm.bc);
                         const double pphi = L.S[(depth - 1) * tpb + tid];
                         L.S[depth * tpb + tid] = pphi * bv;
                         const int tl = depth * (depth + 1) / 2, tp = (depth - 1) * depth / 2;
@@ -1093,7 +1091,7 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
 #pragma unroll
             for (int k = 0; k <= PMAX; ++k) A.a[k] = prm.acoef[(long long)k * prm.N + i];
         } else if (mine) {
-            fillLead<BASIS, false>(c, L, tid, prm.bc);
+            fillLead<BASIS>(c, L, tid, prm.bc);
             if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, A.a, nullptr);
             else phaseA<PMAX>(c, L, tid, cm, A.a);
         } else {
@@ -1161,7 +1159,7 @@ __global__ void __launch_bounds__(256) inverseKeyKernel(const __grid_constant__ 
         L.X[d * tpb + tid] = v;
     }
     ACoef<PMAX> A;
-    fillLead<BASIS, false>(c, L, tid, prm.bc);
+    fillLead<BASIS>(c, L, tid, prm.bc);
     phaseA<PMAX>(c, L, tid, prm.cm + c.slotOffset, A.a);
     double f0 = 0.0;
 #pragma unroll
