@@ -673,6 +673,27 @@ def run_gpu(args):
             x1i = torch.zeros(0, 100_000, dtype=torch.float64, device=dev)
             xi = torch.zeros(INV_DIM, 100_000, dtype=torch.float64, device=dev)
             step = lambda: tmi.InverseImpl(x1i, ri, xi, xtol=INV_XTOL, ytol=INV_XTOL)
+        elif args.variant == "implicit":
+            # The inverse workload's map: Inverse of 500,000 of its targets,
+            # then the implicit gradient (InverseCoeffGradImpl) at the finite
+            # roots; a step is one implicit-gradient call (16 fused launches,
+            # the last component's first).
+            iopts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=INV_TOL,
+                                 quadRelTol=INV_TOL, quadMaxSub=MAXSUB)
+            tmi = M.CreateTriangular(INV_DIM, INV_DIM, INV_ORDER, iopts)
+            tmi.SetCoeffs(np.random.default_rng(31).normal(0.0, 0.03, tmi.numCoeffs))
+            g = torch.Generator(device=dev)
+            g.manual_seed(32)
+            ri = torch.randn(INV_DIM, 500_000, dtype=torch.float64, device=dev, generator=g)
+            wi = torch.randn(INV_DIM, 500_000, dtype=torch.float64, device=dev, generator=g)
+            x1i = torch.zeros(0, 500_000, dtype=torch.float64, device=dev)
+            xi = torch.zeros(INV_DIM, 500_000, dtype=torch.float64, device=dev)
+            tmi.InverseImpl(x1i, ri, xi, xtol=INV_XTOL, ytol=INV_XTOL)
+            fin = ~torch.isnan(xi).any(dim=0)
+            xs, ws = xi[:, fin].contiguous(), wi[:, fin].contiguous()
+            cgi = torch.zeros(tmi.numCoeffs, dtype=torch.float64, device=dev)
+            pgi = torch.zeros(INV_DIM, xs.shape[1], dtype=torch.float64, device=dev)
+            step = lambda: tmi.InverseCoeffGradImpl(xs, ws, cgi, pgi)
         elif args.variant == "batch":
             # The batched-maps workload's batch call (default tuning).
             step = batch_setup(M, dev)
@@ -863,7 +884,7 @@ def main():
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
     ap.add_argument("--no-sigmoid", action="store_true", help="skip the sigmoid-expansion workload")
     ap.add_argument("--variant", default="full",
-                    choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid", "inverse", "batch"],
+                    choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid", "inverse", "implicit", "batch"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
     if args.impl == "reference":
