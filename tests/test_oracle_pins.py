@@ -320,3 +320,19 @@ def test_integrand_overflow_flag(oracle):
     assert st[0] == 1 and math.isnan(out[0])
     out, nev, st = c.evaluate([0.0, 1.0], np.array([[float("nan")]]), return_evals=True)
     assert st[0] == 2 and math.isnan(out[0]) and nev[0] <= 3
+
+
+# tests/Test_MonotoneComponent.cpp:443-557 (inverse round trips), on the
+# workloads of the GPU's two-pass inverse test: far roots and targets without
+# a root.  The finite roots reproduce their targets.
+@pytest.mark.parametrize("basis,pos,scale,rscale,bound", [(0, 1, 0.05, 3.0, 1e-9), (2, 0, 0.1, 2.0, 1e-8)])
+def test_inverse_round_trip_far_roots(oracle, basis, pos, scale, rscale, bound):
+    om = oracle.OracleTriangularMap(4, 4, 3, basis=basis, normalize=True, posfunc=pos, abs_tol=1e-8, rel_tol=1e-8,
+                                    max_sub=30)
+    coef = np.random.default_rng(11).normal(0.0, scale, om.num_coeffs)
+    r = rscale * np.random.default_rng(12).standard_normal((4, 777))
+    x = om.inverse(coef, np.zeros((0, 777)), r, 1e-10, 1e-10)
+    ok = ~np.isnan(x).any(axis=0)
+    assert ok.sum() > 500 and np.nanmax(np.abs(x)) > 7.0
+    back = om.evaluate(coef, np.where(ok, x, 0.0))
+    assert np.abs(back - r)[:, ok].max() < bound
