@@ -47,6 +47,12 @@ DIM, ORDER, NPTS = 8, 4, 1_000_000
 TOL, MAXSUB = 1e-6, 30
 METRIC = "fused fwd+adjoint points/s (dim-8, order-4, FP64)"
 KL_DIM, KL_ORDER, KL_N, KL_TOL, KL_ITERS = 6, 5, 200_000, 1e-7, 100
+# CPU legs run in a child process on the oracle's timing build (the same
+# source with the compiler's default floating-point contraction, -O3
+# -fopenmp) with the threads bound one per core.
+TIMING_ENV = {"OMP_PROC_BIND": "spread", "OMP_PLACES": "threads", "MPGB_ORACLE_BUILD": "timing"}
+CPU_BUILD = ("oracle/ timing build (g++ -O3 -fopenmp, default FP contraction; no -march=native), "
+             "OMP_PROC_BIND=spread OMP_PLACES=threads")
 SIG_DIM, SIG_ORDER, SIG_NSIG, SIG_N = 8, 3, 5, 1_000_000
 
 
@@ -264,34 +270,26 @@ def inverse_implicit(M, dev, cpu_seconds=8.0):
             best = min(best, e0.elapsed_time(e1))
         return best
 
+    xn = torch.zeros_like(x)
+    ms_newton = timed(lambda: tm.InverseImpl(x1, r, xn, xtol=INV_XTOL, ytol=INV_XTOL, method="Newton"))
     ms_inv = timed(lambda: tm.InverseImpl(x1, r, x, xtol=INV_XTOL, ytol=INV_XTOL))
     ok = ~torch.isnan(x).any(dim=0)
+    newton_dx = float((xn[:, ok] - x[:, ok]).abs().max().item()) if bool(ok.any()) else 0.0
+    del xn
     xs, ws = x[:, ok].contiguous(), w[:, ok].contiguous()
     ms_grad = timed(lambda: tm.InverseCoeffGradImpl(xs, ws, cg, pg[:, :xs.shape[1]]))
     out = {"workload": f"TriangularMap {INV_DIM}-D, total order {INV_ORDER} ({tm.numCoeffs} coefficients, 969 in the "
                        f"last component), ProbHermite + SoftPlus, ACC tol {INV_TOL}; {INV_N} targets r ~ N(0, I); "
                        f"Inverse to xtol {INV_XTOL}, then dL/dc and dL/dr of L = sum w * x (implicit rule)",
-           "points": INV_N, "inverse_ms": ms_inv, "inverse_points_per_s": INV_N / (ms_inv * 1e-3),
+           "points": INV_N, "inverse_method": "Bracket (FindBracket + ITP, the reference's solver)",
+           "inverse_ms": ms_inv, "inverse_points_per_s": INV_N / (ms_inv * 1e-3),
+           "inverse_newton_ms": ms_newton, "inverse_newton_points_per_s": INV_N / (ms_newton * 1e-3),
+           "newton_vs_itp_max_abs_dx": newton_dx,
            "no_root_fraction": float(1.0 - ok.double().mean().item()),
            "implicit_grad_ms": ms_grad, "implicit_grad_points_per_s": xs.shape[1] / (ms_grad * 1e-3),
            "coeff_grad_norm": float(cg.norm().item())}
     # the oracle's Inverse on a bounded sample of the same targets (host cores)
-    from oracle import oracle as O
-    O.build()
-    cores = os.cpu_count() or 1
-    O.set_threads(cores)
-    om = O.OracleTriangularMap(INV_DIM, INV_DIM, INV_ORDER, abs_tol=INV_TOL, rel_tol=INV_TOL, max_sub=MAXSUB)
-    rh = r[:, :20000].cpu().numpy()
-    n = 200
-    t0 = time.perf_counter()
-    om.inverse(coef, np.zeros((0, n)), rh[:, :n], INV_XTOL, INV_XTOL)
-    dt = time.perf_counter() - t0
-    n2 = int(min(rh.shape[1], max(n, n * cpu_seconds / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    om.inverse(coef, np.zeros((0, n2)), rh[:, :n2], INV_XTOL, INV_XTOL)
-    dt = time.perf_counter() - t0
-    out["cpu_inverse"] = {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
-                          "sample": f"first {n2} targets, the oracle's Inverse"}
+    out["cpu_inverse"] = cpu_leg("inverse", coef=coef, r=r[:, :20000].cpu().numpy(), seconds=cpu_seconds)
     out["inverse_speedup_vs_cpu"] = out["inverse_points_per_s"] / out["cpu_inverse"]["points_per_s"]
     return out
 
@@ -365,14 +363,45 @@ def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
            "fused_points_per_s": SIG_N / (ms_fused * 1e-3), "kl_step_ms": ms_kl,
            "l2": "flushed between steps (256 MB write)"}
     # the oracle on a bounded sample: the reference's four calls per component
+    nmax = 400_000
+    out["cpu_baseline"] = cpu_leg("sigmoid", cen=cen, coef=coef, x=xh[:, :nmax], s=sh[:, :nmax], seconds=cpu_seconds)
+    out["speedup_vs_cpu"] = out["fused_points_per_s"] / out["cpu_baseline"]["points_per_s"]
+    return out
+
+
+def leg_inverse(a):
+    """The oracle's Inverse of the inverse workload's map on a bounded sample
+    of its targets (child process, timing build)."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
     O.set_threads(cores)
-    om = O.sigmoid_triangular(SIG_DIM, SIG_DIM, SIG_ORDER, cen, 1.5, O.SUM_LINEAR, O.POS_SOFTPLUS)
+    om = O.OracleTriangularMap(INV_DIM, INV_DIM, INV_ORDER, abs_tol=INV_TOL, rel_tol=INV_TOL, max_sub=MAXSUB)
+    coef, rh, seconds = a["coef"], a["r"], float(a["seconds"])
+    n = 200
+    t0 = time.perf_counter()
+    om.inverse(coef, np.zeros((0, n)), rh[:, :n], INV_XTOL, INV_XTOL)
+    dt = time.perf_counter() - t0
+    n2 = int(min(rh.shape[1], max(n, n * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    om.inverse(coef, np.zeros((0, n2)), rh[:, :n2], INV_XTOL, INV_XTOL)
+    dt = time.perf_counter() - t0
+    return {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
+            "sample": f"first {n2} targets, the oracle's Inverse (FindBracket + ITP); {CPU_BUILD}"}
+
+
+def leg_sigmoid(a):
+    """The oracle's four reference calls per component of the sigmoid map on a
+    bounded sample of its points (child process, timing build)."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    om = O.sigmoid_triangular(SIG_DIM, SIG_DIM, SIG_ORDER, a["cen"], 1.5, O.SUM_LINEAR, O.POS_SOFTPLUS)
+    coef, xh, sh, seconds = a["coef"], a["x"], a["s"], float(a["seconds"])
 
     def cpu(n):
-        xs, ss = xh[:, :n], sh[:, :n]
+        xs, ss = np.ascontiguousarray(xh[:, :n]), np.ascontiguousarray(sh[:, :n])
         t0 = time.perf_counter()
         om.evaluate(coef, xs)
         om.logdet(coef, xs)
@@ -382,13 +411,39 @@ def sigmoid_maps(M, dev, steps=10, cpu_seconds=8.0):
 
     n = 2000
     dt = cpu(n)
-    n2 = int(min(SIG_N, max(n, n * cpu_seconds / max(dt, 1e-6))))
+    n2 = int(min(xh.shape[1], max(n, n * seconds / max(dt, 1e-6))))
     dt = cpu(n2)
-    out["cpu_baseline"] = {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
-                           "sample": f"first {n2} of the {SIG_N} points, the oracle's Evaluate + LogDeterminant + "
-                                     f"CoeffGrad + LogDeterminantCoeffGrad per component, gradients summed"}
-    out["speedup_vs_cpu"] = out["fused_points_per_s"] / out["cpu_baseline"]["points_per_s"]
-    return out
+    return {"points_per_s": n2 / dt, "cores": cores, "kind": "port",
+            "sample": f"first {n2} of the {SIG_N} points, the oracle's Evaluate + LogDeterminant + CoeffGrad + "
+                      f"LogDeterminantCoeffGrad per component, gradients summed; {CPU_BUILD}"}
+
+
+def cpu_leg(name, **arrays):
+    """Runs a CPU leg of this benchmark in a child process (the oracle's
+    timing build, threads bound one per core) and returns its JSON result.
+    Arrays travel through a temporary .npz file."""
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "in.npz")
+        np.savez(f, **{k: np.asarray(v) for k, v in arrays.items()})
+        env = dict(os.environ, **TIMING_ENV)
+        if name == "c2-parity":
+            env.pop("MPGB_ORACLE_BUILD")  # parity: the strict build
+        r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", name, "--cpu-in", f],
+                           env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CPU leg {name} failed: {r.stderr[-2000:]}")
+        return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_cpu_leg(args):
+    a = dict(np.load(args.cpu_in)) if args.cpu_in else {}
+    legs = {"c2": lambda: cpu_baseline(),
+            "c2-parity": lambda: leg_c2_parity(a),
+            "kl": lambda: kl_cpu_step_ms(a["coeffs"]),
+            "inverse": lambda: leg_inverse(a),
+            "sigmoid": lambda: leg_sigmoid(a)}
+    print(json.dumps(legs[args.cpu_leg]()), flush=True)
 
 
 def kl_cpu_step_ms(coeffs, target_seconds=8.0):
@@ -416,7 +471,7 @@ def kl_cpu_step_ms(coeffs, target_seconds=8.0):
     n2 = int(min(KL_N, max(n, n * target_seconds / max(dt, 1e-6))))
     dt = step(n2)
     return {"ms_per_step": dt * 1e3 * KL_N / n2, "cores": cores, "kind": "port",
-            "sample": f"first {n2} of the {KL_N} samples at the trained coefficients, scaled to {KL_N}"}
+            "sample": f"first {n2} of the {KL_N} samples at the trained coefficients, scaled to {KL_N}; {CPU_BUILD}"}
 
 
 def prefix_stats():
@@ -579,13 +634,53 @@ def cpu_baseline(target_seconds=12.0):
     return {"value": n2 / dt, "unit": "points/s", "cores": cores, "kind": "port",
             "sample": f"first {n2} of the {NPTS} points (same seeds), reference algorithm restated in "
                       f"oracle/ (C++17 + OpenMP, {cores} threads): Evaluate + LogDeterminant + CoeffGrad + "
-                      f"LogDeterminantCoeffGrad, gradients summed over points"}
+                      f"LogDeterminantCoeffGrad, gradients summed over points; {CPU_BUILD}"}
+
+
+def leg_c2_parity(a, chunk=50_000):
+    """The timed run's outputs (T, log-det, reduced coefficient gradient)
+    against the oracle's parity build on every one of the NPTS points (child
+    process).  Per entry the bar of the GPU tests: |gpu - oracle| <=
+    1e-10 max(|oracle|, 1e-6 max|oracle|), the gradient (a sum over points)
+    floored at 1e-3 of its largest entry."""
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    s_, d_, o_ = O.total_order(DIM, ORDER)
+    comp = O.OracleComponent(DIM, s_, d_, o_, abs_tol=TOL, rel_tol=TOL, max_sub=MAXSUB)
+    coef = coeffs(comp.num_terms)
+    x, sv = synth(NPTS)
+    T = np.empty(NPTS)
+    ld = np.empty(NPTS)
+    cg = np.zeros(comp.num_terms)
+    t0 = time.perf_counter()
+    for k in range(0, NPTS, chunk):
+        xs, ss = np.ascontiguousarray(x[:, k:k + chunk]), sv[:, k:k + chunk]
+        T[k:k + chunk] = comp.evaluate(coef, xs)
+        ld[k:k + chunk] = comp.logdet(coef, xs)
+        cg += comp.coeff_grad(coef, xs, ss[0]).sum(axis=1) + comp.logdet_coeff_grad(coef, xs).sum(axis=1)
+    dt = time.perf_counter() - t0
+
+    def check(g, r, floor):
+        scale = np.max(np.abs(r))
+        tol = 1e-10 * np.maximum(np.abs(r), floor * scale)
+        bad = ~((g == r) | (np.abs(g - r) <= tol))
+        rel = np.abs(g - r) / np.maximum(np.abs(r), floor * scale)
+        return {"entries": int(r.size), "outside_tol": int(bad.sum()), "max_rel_err": float(rel.max())}
+
+    return {"points": NPTS, "oracle_s": dt, "tolerance": "1e-10 relative (floor 1e-6 of the largest entry; "
+                                                         "1e-3 for the gradient summed over points)",
+            "evaluate": check(a["T"], T, 1e-6), "logdet": check(a["ld"], ld, 1e-6),
+            "coeff_grad": check(a["cg"], cg, 1e-3)}
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    # the timing build with threads bound one per core (before the OpenMP
+    # runtime is loaded with the oracle)
+    os.environ.update(TIMING_ENV)
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
@@ -603,7 +698,7 @@ def run_reference(args):
     dt = (time.perf_counter() - t0) / args.steps
     v = n / dt
     sample = (f"{n} of the {NPTS} points per step (same seeds); reference algorithm restated in oracle/ "
-              f"(C++17 + OpenMP, {cores} threads); the reference itself does not build here")
+              f"(C++17 + OpenMP, {cores} threads); {CPU_BUILD}; the reference itself does not build here")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -661,8 +756,8 @@ def run_gpu(args):
         if args.variant == "sigmoid":
             # The sigmoid workload's fused step (see sigmoid_setup).
             step = sigmoid_setup(M, dev)[-1]
-        elif args.variant == "inverse":
-            # The inverse workload's map on 100,000 of its targets.
+        elif args.variant in ("inverse", "inverse-newton"):
+            # The inverse workload's map on 100,000 of its targets (ITP, or the Newton option).
             iopts = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, quadAbsTol=INV_TOL,
                                  quadRelTol=INV_TOL, quadMaxSub=MAXSUB)
             tmi = M.CreateTriangular(INV_DIM, INV_DIM, INV_ORDER, iopts)
@@ -672,7 +767,8 @@ def run_gpu(args):
             ri = torch.randn(INV_DIM, 100_000, dtype=torch.float64, device=dev, generator=g)
             x1i = torch.zeros(0, 100_000, dtype=torch.float64, device=dev)
             xi = torch.zeros(INV_DIM, 100_000, dtype=torch.float64, device=dev)
-            step = lambda: tmi.InverseImpl(x1i, ri, xi, xtol=INV_XTOL, ytol=INV_XTOL)
+            meth = "Newton" if args.variant == "inverse-newton" else "Bracket"
+            step = lambda: tmi.InverseImpl(x1i, ri, xi, xtol=INV_XTOL, ytol=INV_XTOL, method=meth)
         elif args.variant == "implicit":
             # The inverse workload's map: Inverse of 500,000 of its targets,
             # then the implicit gradient (InverseCoeffGradImpl) at the finite
@@ -807,10 +903,14 @@ def run_gpu(args):
     line["dense_coeff_grad"] = dense_coeff_grad(comp, x, s, N, dev)
     line["plain_path"] = plain_path(M, coef, x, s, N, dev)
     line["plain_path"]["fused_speedup"] = line["plain_path"]["ms_per_step"] / (t_step * 1e3)
-    line["cpu_baseline"] = cpu_baseline()
+    line["cpu_baseline"] = cpu_leg("c2")
+    if not args.no_parity and N == NPTS:
+        # the timed step's outputs (last timed step) against the oracle on every point
+        line["parity_full"] = cpu_leg("c2-parity", T=out_T.cpu().numpy().reshape(-1), ld=out_ld.cpu().numpy(),
+                                      cg=cg.cpu().numpy())
     if not args.no_kl:
         kl, trained = kl_train(M, dev)
-        kl["cpu_step"] = kl_cpu_step_ms(trained)
+        kl["cpu_step"] = cpu_leg("kl", coeffs=trained)
         kl["cpu_step"]["speedup_graph"] = (kl["cpu_step"]["ms_per_step"] /
                                            kl["step_ms_at_trained_coeffs"]["graph_batched"])
         line["kl_train"] = kl
@@ -883,11 +983,17 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-maps workload")
     ap.add_argument("--no-inverse", action="store_true", help="skip the inverse / implicit-gradient workload")
     ap.add_argument("--no-sigmoid", action="store_true", help="skip the sigmoid-expansion workload")
+    ap.add_argument("--no-parity", action="store_true", help="skip the full-size parity check against the oracle")
+    ap.add_argument("--cpu-leg", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-in", default=None, help=argparse.SUPPRESS)
     ap.add_argument("--variant", default="full",
-                    choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid", "inverse", "implicit", "batch"],
+                    choices=["full", "eval", "logdet", "reduce", "kl", "sigmoid", "inverse", "inverse-newton", "implicit",
+                             "batch"],
                     help="with --profile: which part of the step to run")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.cpu_leg:
+        run_cpu_leg(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

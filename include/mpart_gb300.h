@@ -200,6 +200,20 @@ int mpgb_log_determinant(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* 
 int mpgb_inverse(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
                  int* device_info, void* stream);
 
+/* Root solvers of mpgb_inverse_method. */
+enum {
+    MPGB_INVERSE_BRACKET = 0, /* the reference's "Bracket" method: FindBracket + ITP (RootFinding.h:20-178) */
+    MPGB_INVERSE_NEWTON = 1   /* FindBracket, then safeguarded Newton steps with the exact slope dT/dx_D */
+};
+
+/* mpgb_inverse with the "Method" option of MonotoneComponent::InverseImpl
+ * (MonotoneComponent.h:340-351).  mpgb_inverse uses MPGB_INVERSE_BRACKET, whose
+ * iterates are the reference's; MPGB_INVERSE_NEWTON meets the same xtol/ytol
+ * stopping rules in about a seventh of the integrand quadratures, at a root
+ * that can differ from ITP's by up to xtol + ytol / (dT/dx_D). */
+int mpgb_inverse_method(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
+                        int method, int* device_info, void* stream);
+
 /* ParameterizedFunctionBase::CoeffGradImpl (MParT/ParameterizedFunctionBase.h:163-165). out is numCoeffs x N. */
 int mpgb_coeff_grad(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix out, void* stream);
 
@@ -244,10 +258,14 @@ int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad
  * device heap).  No counterpart in the reference.  Scratch comes from a fixed
  * 64 MiB array in device memory that the library holds on every GPU it is
  * loaded on; calls needing more are rejected (MPGB_ERR_INVALID_ARGUMENT).
- * Device pointers only; out_logdet only for one-component maps; no input
- * gradient.  All calls share the array, so calls that overlap on the GPU
- * race.  The first call on a device looks up the array's address: make it
- * before any stream capture.  Synchronises the stream before returning. */
+ * Device pointers of the current device (or managed memory) only;
+ * out_logdet only for one-component maps; no input gradient.  All calls
+ * share the array, so calls that overlap on the GPU race.  The array's
+ * address is looked up once per device when a map is created there, which
+ * under CUDA's lazy module loading is when the driver reserves the array; if
+ * that look-up failed, the first call on the device makes it (and reserves
+ * the array): make that first call during start-up, before any stream
+ * capture.  Synchronises the stream before returning. */
 int mpgb_fused_fwd_adj_noalloc(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix logdet_sens,
                                double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet,
                                double* coeff_grad, void* stream);

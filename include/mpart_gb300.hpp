@@ -164,10 +164,14 @@ struct Sigmoid1dParams {
                                        SigmoidSumSizeType sumType);
 };
 
-// Inverse solver options (MonotoneComponent.h:353-396).
+// Inverse solver options (MonotoneComponent.h:353-396).  method 0 is the
+// reference's "Bracket" method (FindBracket + ITP, RootFinding.h:20-178);
+// method 1 closes the same bracket by safeguarded Newton steps with the exact
+// slope, to the same tolerances, in fewer evaluations (not the ITP iterate).
 struct InverseOptions {
     double xtol = 1e-6;
     double ytol = 1e-6;
+    int method = 0;
 };
 
 // Maps made of monotone components (a single MonotoneComponent or a

@@ -306,6 +306,18 @@ def _ptr(x):
     return C.c_void_p(x.ctypes.data)
 
 
+_INVERSE_METHODS = {"Bracket": 0, "Newton": 1}
+
+
+def _inverse_method(method) -> int:
+    """The "Method" option of MonotoneComponent::InverseImpl (MonotoneComponent.h:340-351):
+    "Bracket" (the reference's FindBracket + ITP) or "Newton"."""
+    if method not in _INVERSE_METHODS:
+        raise ValueError(f"Invalid method given to MonotoneComponent::Inverse.  Given \"{method}\", "
+                         f"but valid options are {sorted(_INVERSE_METHODS)}.")
+    return _INVERSE_METHODS[method]
+
+
 def _zeros_like_dev(ref, shape):
     if _is_torch(ref):
         import torch
@@ -386,9 +398,11 @@ class ConditionalMapBase:
     def LogDeterminantImpl(self, pts, out):
         check(load().mpgb_log_determinant(self._h, _mat(pts), _mat(out), _stream_of(pts, out)))
 
-    def InverseImpl(self, x1, r, out, xtol=1e-6, ytol=1e-6, info=None):
-        check(load().mpgb_inverse(self._h, _mat(x1), _mat(r), _mat(out), float(xtol), float(ytol), _ptr(info),
-                                  _stream_of(x1, r, out)))
+    def InverseImpl(self, x1, r, out, xtol=1e-6, ytol=1e-6, info=None, method="Bracket"):
+        """method "Bracket" is the reference's FindBracket + ITP; "Newton" closes
+        the same bracket by safeguarded Newton steps (same stopping rules)."""
+        check(load().mpgb_inverse_method(self._h, _mat(x1), _mat(r), _mat(out), float(xtol), float(ytol),
+                                         _inverse_method(method), _ptr(info), _stream_of(x1, r, out)))
 
     def CoeffGradImpl(self, pts, sens, out):
         check(load().mpgb_coeff_grad(self._h, _mat(pts), _mat(sens), _mat(out), _stream_of(pts, sens, out)))
@@ -440,9 +454,9 @@ class ConditionalMapBase:
         self.LogDeterminantImpl(pts, out)
         return out
 
-    def Inverse(self, x1, r, xtol=1e-6, ytol=1e-6):
+    def Inverse(self, x1, r, xtol=1e-6, ytol=1e-6, method="Bracket"):
         out = _zeros_like_dev(r, (self.outputDim, r.shape[1]))
-        self.InverseImpl(x1, r, out, xtol, ytol)
+        self.InverseImpl(x1, r, out, xtol, ytol, method=method)
         return out
 
     def CoeffGrad(self, pts, sens):

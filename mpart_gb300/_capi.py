@@ -107,6 +107,8 @@ SIGNATURES = {
     "mpgb_log_determinant": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),
     "mpgb_inverse": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, C.c_double, C.c_void_p,
                                C.c_void_p]),
+    "mpgb_inverse_method": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_double, C.c_double, C.c_int,
+                                      C.c_void_p, C.c_void_p]),
     "mpgb_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_void_p]),
     "mpgb_gradient": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, mpgb_matrix, C.c_void_p]),
     "mpgb_log_determinant_coeff_grad": (C.c_int, [_MAP, mpgb_matrix, mpgb_matrix, C.c_void_p]),

@@ -48,6 +48,9 @@ constexpr int kStatusNoBracket = 8;    // inverse: bracket search failed (info=-
 // budget (solved again in the second pass; never returned to callers).
 constexpr int kInfoDeferred = -3;
 constexpr unsigned kBracketIts = 128;  // FindBracket's step limit (RootFinding.h:29)
+// Inverse root solvers (InverseParams::method).
+constexpr int kInverseITP = 0;     // the reference's FindBracket + ITP (default)
+constexpr int kInverseNewton = 1;  // FindBracket + safeguarded Newton with the exact slope
 // Largest sort key of a deferred inverse point: below 36, so that deferred
 // points stay out of sortBucket's last bucket, which holds the NaN keys of
 // the points that were not deferred.

@@ -955,6 +955,9 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     if (io.xtol <= std::numeric_limits<double>::epsilon() && io.ytol <= std::numeric_limits<double>::epsilon())
         throw std::invalid_argument(
             "Invalid tolerances given to MonotoneComponent::Inverse.  Either \"xtol\" or \"ytol\" must be nonzero.");
+    if (io.method != kInverseITP && io.method != kInverseNewton)
+        throw std::invalid_argument(
+            "Invalid method given to MonotoneComponent::Inverse.  Valid options are 0 (\"Bracket\") and 1 (Newton).");
     const long long N = r.cols;
     if (r.rows != outputDim) throw std::invalid_argument("InverseImpl: r must have outputDim rows.");
     if (x1.cols != N && x1.cols != 1) {
@@ -980,6 +983,7 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     p.info = deviceInfo; p.infoStride = N;
     p.statusWord = W.status.as<int>();
     p.xtol = io.xtol; p.ytol = io.ytol;
+    p.method = io.method;
     p.nugget = opts_.nugget;
     p.dmax = W.dmax; p.nBmax = W.nBmax; p.depthMax = W.depthMax;
     p.quad = W.quad; p.bc = W.bc;
@@ -991,14 +995,6 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         Finish(stream, "Inverse");
         return;
     }
-    // One component at a time, in two passes (see InverseParams): the first
-    // gives every point kFirstPassBracketIts bracket-doubling steps, the
-    // second finishes the points that needed more.  For monotone components a
-    // key launch first forms phase A of every point (kept for the solver) and
-    // a root estimate, and the first pass takes the points in order of
-    // |estimate|; the second takes the deferred points in order of the
-    // estimate the first pass leaves for them (stable counting sorts).  Lanes
-    // whose solver steps integrate over similar ranges then share warps.
     W.inverseDefer.ensure(sizeof(int), stream);
     W.inverseKey.ensure((size_t)N * sizeof(double), stream);
     W.perm.ensure((size_t)N * sizeof(int), stream);
@@ -1006,23 +1002,48 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     int* deferCount = W.inverseDefer.as<int>();
     double* key = W.inverseKey.as<double>();
     int* perm = W.perm.as<int>();
-    const bool keyed = W.ordering && W.basis != kBasisSigmoid;
-    if (keyed) W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
+    if (W.basis != kBasisSigmoid) {
+        // Monotone components, one at a time: a key launch forms phase A of
+        // every point (kept in inverseA for the solver) and a root estimate;
+        // the points are sorted by |estimate| (the cost of a solver step grows
+        // with the range [0, x] its quadrature covers); a persistent queue
+        // launch solves them, expensive ones first, one integrand node per
+        // lane and loop iteration (inverseQueueKernel).
+        W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
+        for (int c = 0; c < p.nComps; ++c) {
+            InverseParams k = p;
+            k.compBegin = c;
+            k.compEnd = c + 1;
+            k.keyPass = 1;
+            k.acoef = W.inverseA.as<double>();
+            k.key = key;
+            MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, k, nBlocks, stream));
+            InverseParams q = p;
+            q.compBegin = c;
+            q.compEnd = c + 1;
+            q.acoef = k.acoef;
+            q.bracketBudget = (int)kBracketIts;
+            if (W.ordering) {
+                MPGB_CUDA(launchSortByLast(key, 1, N, W.sortHist.as<int>(), perm, stream));
+                q.perm = perm;
+            }
+            MPGB_CUDA(cudaMemsetAsync(deferCount, 0, sizeof(int), stream));
+            q.queue = deferCount;
+            q.queuePass = 1;
+            MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
+        }
+        Finish(stream, "Inverse");
+        return;
+    }
+    // Sigmoid expansions, one component at a time, in two passes (see
+    // InverseParams): the first gives every point kFirstPassBracketIts
+    // bracket-doubling steps, the second finishes the points that needed
+    // more, sorted by the root estimate the first pass leaves for them.
     for (int c = 0; c < p.nComps; ++c) {
         InverseParams first = p;
         first.compBegin = c;
         first.compEnd = c + 1;
         first.bracketBudget = kFirstPassBracketIts;
-        if (keyed) {
-            InverseParams k = first;
-            k.keyPass = 1;
-            k.acoef = W.inverseA.as<double>();
-            k.key = key;
-            MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, k, nBlocks, stream));
-            MPGB_CUDA(launchSortByLast(key, 1, N, W.sortHist.as<int>(), perm, stream));
-            first.perm = perm;
-            first.acoef = k.acoef;
-        }
         MPGB_CUDA(cudaMemsetAsync(key, 0xff, (size_t)N * sizeof(double), stream));  // NaN: not deferred
         MPGB_CUDA(cudaMemsetAsync(deferCount, 0, sizeof(int), stream));
         first.deferKey = key;
@@ -2081,6 +2102,11 @@ int mpgb_log_determinant(mpgb_map* map, mpgb_matrix pts, mpgb_matrix out, void* 
 
 int mpgb_inverse(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
                  int* device_info, void* stream) {
+    return mpgb_inverse_method(map, x1, r, out, xtol, ytol, MPGB_INVERSE_BRACKET, device_info, stream);
+}
+
+int mpgb_inverse_method(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, double xtol, double ytol,
+                        int method, int* device_info, void* stream) {
     return guard([&] {
         cudaStream_t s = (cudaStream_t)stream;
         Stager st(s, mono(map));
@@ -2090,6 +2116,7 @@ int mpgb_inverse(mpgb_map* map, mpgb_matrix x1, mpgb_matrix r, mpgb_matrix out, 
         InverseOptions io;
         io.xtol = xtol;
         io.ytol = ytol;
+        io.method = method;
         mono(map)->InverseImpl(X, R, O, io, device_info, s);
         st.finish();
     });

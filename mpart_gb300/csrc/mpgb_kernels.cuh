@@ -922,26 +922,59 @@ struct SigmoidInverseEval {
     }
 };
 
+// 2^e for the integer-valued (or infinite / NaN) exponents of the ITP
+// truncation, exactly as pow(2.0, e) gives them.
+__device__ __forceinline__ double exp2Int(double e) {
+    if (isnan(e)) return e;
+    if (e > 4096.0) return __longlong_as_double(0x7ff0000000000000ULL);
+    if (e < -4096.0) return 0.0;
+    return ldexp(1.0, (int)e);
+}
+
+// The ITP point of RootFinding::Find_x_ITP (RootFinding.h:92-106) with the
+// constants of InverseSingleBracket (k1 = 0.1, k2 = 2, n0 = 1, :145-149), in
+// the reference's operation order and without FMA contraction, so that the
+// iterates are those of the reference's host build.  pow(w, 2) is w * w
+// (libm's pow returns the correctly rounded square).
+__device__ __forceinline__ double itpPoint(double xlb, double xub, double ylb, double yub, double nhalf, unsigned it,
+                                           double xtol) {
+    const double xb = __dmul_rn(0.5, __dadd_rn(xub, xlb));
+    double xf = __ddiv_rn(__dsub_rn(__dmul_rn(xub, ylb), __dmul_rn(xlb, yub)), __dsub_rn(ylb, yub));
+    const double sigma = (__dsub_rn(xb, xf) > 0) ? 1.0 : -1.0;
+    const double w = __dsub_rn(xub, xlb);
+    const double delta = fmin(__dmul_rn(0.1, __dmul_rn(w, w)), fabs(__dsub_rn(xb, xf)));
+    xf = __dadd_rn(xf, __dmul_rn(delta, sigma));
+    const double p2 = exp2Int(__dsub_rn(__dadd_rn(nhalf, 1.0), (double)it));
+    const double rho = fmin(__dsub_rn(__dmul_rn(xtol, p2), __dmul_rn(0.5, w)), fabs(__dsub_rn(xf, xb)));
+    return __dsub_rn(xb, __dmul_rn(sigma, rho));
+}
+
 // Root of f(x) = yd for a monotone f (MonotoneComponent::InverseImpl with
 // RootFinding::InverseSingleBracket and FindBracket, RootFinding.h:20-90,
 // :125-178) as a state machine that asks for one evaluation of f per step,
 // so that the lanes of a warp evaluate f together instead of one after the
 // other.  The reference's bracket search is kept step for step (same
 // evaluation points, so the same targets have no bracket and give NaN; its
-// two repeated evaluations at x0 are taken from the first), then the bracket
-// is closed by a safeguarded Newton iteration with the exact slope
-// dT/dx_D = g(df) + nugget instead of ITP.  Every evaluation narrows the
-// bracket; a Newton step that leaves it, or two steps that do not halve it,
-// give way to bisection.  The stopping rules are the reference's:
-// |f(x) - yd| < ftol returns x; a bracket narrower than xtol (or whose values
-// differ by less than ftol) returns its midpoint.  The answer therefore meets
-// the reference's tolerance; it is not the ITP iterate itself.
+// two repeated evaluations at x0 are taken from the first).
+//
+// kInverseITP closes the bracket as the reference does: ITP points
+// (itpPoint), |f(x) - yd| < ftol returns x, and the loop stops when the
+// bracket is narrower than xtol or its values differ by less than ftol,
+// returning the midpoint; at most 10000 iterations.
+//
+// kInverseNewton closes it by a safeguarded Newton iteration with the exact
+// slope dT/dx_D = g(df) + nugget: every evaluation narrows the bracket; a
+// Newton step that leaves it, or two steps that do not halve it, give way to
+// bisection.  Same stopping rules, so the answer meets the reference's
+// tolerance, in about a seventh of ITP's evaluations; it is not the ITP
+// iterate itself.
 struct RootSolve {
-    enum : int { kStart = 0, kBracket = 1, kNewton = 2, kDone = 3 };
+    enum : int { kStart = 0, kBracket = 1, kNewton = 2, kDone = 3, kITP = 4 };
     int phase, dir, info;
     unsigned it;
     double x;  // next evaluation point
     double xlb, ylb, xub, yub, step, width, widthPrev, result;
+    double nhalf;  // ITP: ceil(log2(0.5 (xub - xlb) / xtol)) of the initial bracket
 
     __device__ void start(double x0) {
         phase = kStart;
@@ -952,6 +985,14 @@ struct RootSolve {
         result = r;
         info = inf;
         phase = kDone;
+    }
+    // The bracket is found: the reference's check of it and the first ITP point.
+    __device__ void bracketedITP(double yd, double xtol) {
+        if ((ylb > yd) || (yub < yd)) { finish(__longlong_as_double(0x7ff8000000000000ULL), -2); return; }
+        nhalf = ceil(log2(__ddiv_rn(__dmul_rn(0.5, __dsub_rn(xub, xlb)), xtol)));
+        it = 0;
+        x = itpPoint(xlb, xub, ylb, yub, nhalf, it, xtol);
+        phase = kITP;
     }
     // The bracket is found: the checks before the solver loop and its first point.
     __device__ void bracketed(double yd, double xtol, double ftol) {
@@ -970,8 +1011,20 @@ struct RootSolve {
     // Consumes y = f(x).  maxBracket < kBracketIts is a first-pass budget:
     // running out of it gives kInfoDeferred instead of "no bracket".
     template <class F>
-    __device__ void step_(double y, double yd, const F& f, double xtol, double ftol, unsigned maxBracket) {
+    __device__ void step_(double y, double yd, const F& f, double xtol, double ftol, unsigned maxBracket,
+                          int method) {
         const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+        if (phase == kITP) {
+            // One iteration of InverseSingleBracket's loop (RootFinding.h:152-170).
+            const double xc = x;
+            if (fabs(y - yd) < ftol) { finish(xc, 0); return; }
+            if (y > yd) { xub = xc; yub = y; }
+            else { xlb = xc; ylb = y; }
+            if (((xub - xlb) < xtol) || ((yub - ylb) < ftol)) { finish(0.5 * (xub + xlb), 0); return; }
+            if (++it >= 10000u) { finish(0.5 * (xub + xlb), 0); return; }
+            x = itpPoint(xlb, xub, ylb, yub, nhalf, it, xtol);
+            return;
+        }
         if (phase == kStart) {
             xlb = xub = x;
             ylb = yub = y;
@@ -997,7 +1050,11 @@ struct RootSolve {
                 more = yub < yd;
                 if (more) { ylb = yub; xlb = xub; step *= 2.0; }
             }
-            if (!more) { bracketed(yd, xtol, ftol); return; }
+            if (!more) {
+                if (method == kInverseITP) bracketedITP(yd, xtol);
+                else bracketed(yd, xtol, ftol);
+                return;
+            }
             if (++it >= maxBracket) {
                 // Out of a first-pass budget: the result is a root estimate
                 // for ordering the second pass (a Newton step from here).
@@ -1030,13 +1087,13 @@ struct RootSolve {
 // step the lanes still solving evaluate f together.
 template <class F>
 __device__ __forceinline__ void solveLockstep(bool need, const F& f, double yd, double x0, double xtol, double ftol,
-                                              unsigned maxBracket, double& result, int& info) {
+                                              unsigned maxBracket, int method, double& result, int& info) {
     RootSolve rs;
     if (need) rs.start(x0);
     while (__any_sync(0xffffffffu, need)) {
         if (need) {
             const double y = f(rs.x);
-            rs.step_(y, yd, f, xtol, ftol, maxBracket);
+            rs.step_(y, yd, f, xtol, ftol, maxBracket, method);
             need = rs.phase != RootSolve::kDone;
             if (!need) {
                 result = rs.result;
@@ -1108,14 +1165,14 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
             // (RectifiedMultivariateExpansion.h:227-277; UnivariateExpansion.h:213-250.
             // A NaN target gives NaN.)
             SigmoidInverseEval<PMAX> f{A, c.P, &c};
-            solveLockstep(mine && !hasNan && !isnan(yd), f, yd, x0, prm.xtol, prm.ytol, budget, result, info);
+            solveLockstep(mine && !hasNan && !isnan(yd), f, yd, x0, prm.xtol, prm.ytol, budget, prm.method, result, info);
         } else {
             double f0 = 0.0;
 #pragma unroll
             for (int k = 0; k <= PMAX; ++k) f0 = fma(A.a[k], prm.bc.v0[k], f0);
             int st = 0;
             InverseEval<BASIS, POS, PMAX> f{A, c.P, f0, &prm.quad, &prm.bc, prm.nugget, &st};
-            solveLockstep(mine && !hasNan, f, yd, x0, prm.xtol, prm.ytol, budget, result, info);
+            solveLockstep(mine && !hasNan, f, yd, x0, prm.xtol, prm.ytol, budget, prm.method, result, info);
             stAll |= st;
         }
         if (!mine) continue;
@@ -1133,6 +1190,238 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
         L.X[(c.D - 1) * tpb + tid] = result;
         prm.out[(long long)ci * prm.outRs + i * prm.outCs] = result;
         if (prm.info) prm.info[(long long)ci * prm.infoStride + i] = info;
+    }
+    if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
+}
+
+// Inverse of one monotone component (compBegin) from a queue of points, one
+// integrand node per lane and loop iteration.
+//
+// A lane owns one point at a time.  The adaptive quadrature of T at its
+// solver's current iterate is a small state machine: the endpoint t = 1,
+// then per interval the midpoint, the other interior coarse nodes and the
+// fine-only nodes, then the accept test of AdaptiveClenshawCurtis::Integrate
+// (Quadrature.h:819-968).  Every loop iteration each lane evaluates exactly
+// one node, so the lanes of a warp evaluate the integrand together whatever
+// the interval counts of their quadratures and the step counts of their
+// solves (a lockstep solver waits for the slowest lane at every quadrature
+// and every step).  A lane whose solve ends writes the root and takes the
+// next point; one atomic per warp serves all its lanes that need one.  The
+// points come in perm order from the expensive end (root estimates from the
+// key pass), so the launch ends on cheap points.
+//
+// The operations of each quadrature are those of `integrate`, in the same
+// order, so T and the solver's iterates are those of one sequential solve.
+// t = 0 is the same node for every quadrature of a point:
+// h(0) = x_D (g(d_D f(x_<D, 0)) + nugget) is formed from its per-point factor.
+template <int BASIS, int POS, int PMAX>
+__global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant__ InverseParams prm) {
+    __shared__ double sOff[kMaxRulePts], sCw[kMaxRulePts], sFw[kMaxRulePts];
+    __shared__ int sIsC[kMaxRulePts];
+    __shared__ int sPer;
+    const QuadParams& Q = prm.quad;
+    const bool fixed = Q.kind == kQuadFixedCC;
+    const int cR = Q.nCoarse - 1, cM = cR / 2, fR = Q.nFine - 1, fM = fR / 2;
+    if (threadIdx.x == 0) {
+        // Nodes of an interval after its midpoint, in the order of `integrate`.
+        int j = 1;
+        for (int i = 1; i < cR; ++i) {
+            if (i == cM) continue;
+            sOff[j] = Q.cPts[i]; sCw[j] = Q.cWts[i]; sFw[j] = Q.fWts[2 * i]; sIsC[j] = 1;
+            ++j;
+        }
+        for (int i = 1; i < Q.nFine; i += 2) {
+            sOff[j] = Q.fPts[i]; sCw[j] = 0.0; sFw[j] = Q.fWts[i]; sIsC[j] = 0;
+            ++j;
+        }
+        sPer = fixed ? Q.nFine : j;
+    }
+    __syncthreads();
+    const int nPer = sPer;
+    const int comp = prm.compBegin;
+    const CompDesc& c = prm.comps[comp];
+    const int D = c.D, P = c.P;
+    const long long N = prm.N;
+    const int lane = threadIdx.x & 31;
+    const unsigned kFull = 0xffffffffu;
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    const double nugget = prm.nugget;
+
+    bool have = false, need = true;
+    long long i = 0;
+    double yd = 0.0, f0 = 0.0, G0 = 0.0;
+    ACoef<PMAX> A;
+    double as[PMAX + 1];
+#pragma unroll
+    for (int k = 0; k <= PMAX; ++k) { A.a[k] = 0.0; as[k] = 0.0; }
+    RootSolve rs;
+    rs.phase = RootSolve::kDone;
+    double xd = 0.0, lo = 0.0, hi = 1.0, hA = 0.0, hB = 0.0, hM = 0.0, ic = 0.0, ih = 0.0, Ih = 0.0;
+    int level = 0, sp = 0, j = 0, qst = 0, stAll = 0;
+    long long nInt = 0;
+    double stX[kMaxSubCap], stH[kMaxSubCap];
+    int stL[kMaxSubCap];
+    auto startQuad = [&](double xq) {
+        xd = xq; lo = 0.0; hi = 1.0; level = 0; sp = 0; Ih = 0.0; nInt = 0; qst = 0;
+        if (fixed) {
+            j = 0;
+        } else {
+            hA = xd * G0;  // evalNode at t = 0
+            if (isinf(G0)) qst |= kStatusInf;
+            else if (isnan(hA)) qst |= kStatusNaN;
+            j = -1;
+        }
+    };
+
+    for (;;) {
+        // Hand the next points to the lanes that need one.
+        const unsigned needMask = __ballot_sync(kFull, need);
+        if (needMask) {
+            const int leader = __ffs(needMask) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(prm.queue, __popc(needMask));
+            base = __shfl_sync(kFull, base, leader);
+            if (need) {
+                const long long slot = (long long)base + __popc(needMask & ((1u << lane) - 1u));
+                need = false;
+                if (slot < N) {
+                    i = prm.perm ? (long long)prm.perm[N - 1 - slot] : slot;
+                    // fullOut = [x1; outputs so far] (TriangularMap.cpp:146-184); the
+                    // last coordinate is the initial guess.
+                    const long long xi = (prm.x1Cols == 1) ? 0 : i;
+                    bool hasNan = false;
+                    double x0 = 0.0;
+                    for (int d = 0; d < D; ++d) {
+                        double v = 0.0;
+                        if (d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+                        else if (d - prm.extra < comp) v = prm.out[(long long)(d - prm.extra) * prm.outRs + i * prm.outCs];
+                        hasNan |= isnan(v);
+                        x0 = v;
+                    }
+                    if (hasNan) {
+                        // (MonotoneComponent.h:407-413)
+                        prm.out[(long long)comp * prm.outRs + i * prm.outCs] = nan;
+                        if (prm.info) prm.info[(long long)comp * prm.infoStride + i] = 0;
+                        need = true;
+                    } else {
+                        yd = prm.r[(long long)comp * prm.rRs + i * prm.rCs];
+                        f0 = 0.0;
+#pragma unroll
+                        for (int k = 0; k <= PMAX; ++k) {
+                            A.a[k] = prm.acoef[(long long)k * N + i];
+                            f0 = fma(A.a[k], prm.bc.v0[k], f0);
+                        }
+                        scaleCoeffs<BASIS, PMAX>(A.a, P, prm.bc, as);
+                        NodeVal<PMAX, false, 0> V0;
+                        int s0 = 0;
+                        evalNode<BASIS, POS, PMAX, false, 0>(0.0, 1.0, as, P, prm.bc, nugget, V0, s0);
+                        G0 = V0.h;
+                        rs.start(x0);
+                        startQuad(x0);
+                        have = true;
+                    }
+                } else {
+                    have = false;
+                }
+            }
+        }
+        if (!__any_sync(kFull, have || need)) break;
+        if (!have) continue;
+
+        // One integrand node.
+        double t, m = 0.0, s = 0.0;
+        if (fixed) {
+            t = 0.5 * (1.0 + Q.fPts[j]);
+        } else if (j < 0) {
+            t = 1.0;
+        } else {
+            m = 0.5 * (lo + hi);
+            s = 0.5 * (hi - lo);
+            t = (j == 0) ? m : m + s * sOff[j];
+        }
+        NodeVal<PMAX, false, 0> V;
+        evalNode<BASIS, POS, PMAX, false, 0>(t, xd, as, P, prm.bc, nugget, V, qst);
+        const double h = V.h;
+        bool qdone = false;
+        double T = 0.0;
+        if (fixed) {
+            Ih = fma(0.5 * Q.fWts[j], h, Ih);
+            if (++j == nPer) {
+                qdone = true;
+                T = (qst & (kStatusInf | kStatusNaN)) ? nan : Ih;
+            }
+        } else if (j < 0) {
+            hB = h;
+            if (qst & (kStatusInf | kStatusNaN)) { qdone = true; T = nan; }
+            else j = 0;
+        } else {
+            if (j == 0) {
+                hM = h;
+                ic = (s * Q.cWts[0]) * hA;
+                ic = fma(s * Q.cWts[cM], hM, ic);
+                ic = fma(s * Q.cWts[cR], hB, ic);
+                const double w0 = s * Q.fWts[0], wM = s * Q.fWts[fM], wR = s * Q.fWts[fR];
+                ih = w0 * hA;
+                ih = fma(wM, hM, ih);
+                ih = fma(wR, hB, ih);
+            } else {
+                if (sIsC[j]) ic = fma(s * sCw[j], h, ic);
+                ih = fma(s * sFw[j], h, ih);
+            }
+            if (++j == nPer) {
+                j = 0;
+                if (qst & (kStatusInf | kStatusNaN)) {
+                    qdone = true;
+                    T = nan;
+                } else {
+                    const double err = fabs(ih - ic);
+                    const double tol = fmax(Q.relTol * fabs(ic), Q.absTol);
+                    const bool accept = ((err < tol) || (level == Q.maxSub - 1)) && (level >= Q.minSub);
+                    if (accept) {
+                        Ih += ih;
+                        if (sp == 0) {
+                            qdone = true;
+                            T = Ih;
+                        } else {
+                            --sp;
+                            lo = hi;
+                            hA = hB;
+                            hi = stX[sp];
+                            level = stL[sp];
+                            hB = stH[sp];
+                        }
+                    } else {
+                        stX[sp] = hi;
+                        stL[sp] = level + 1;
+                        stH[sp] = hB;
+                        ++sp;
+                        hi = m;
+                        hB = hM;
+                        ++level;
+                    }
+                    if (!qdone && ++nInt >= Q.maxIntervals) {
+                        qst |= kStatusBudget;
+                        qdone = true;
+                        T = nan;
+                    }
+                }
+            }
+        }
+        if (!qdone) continue;
+        // The quadrature is done: one solver step with T(x) = integral + f(x_<D, 0).
+        stAll |= qst;
+        int dummy = 0;
+        const InverseEval<BASIS, POS, PMAX> f{A, P, f0, &prm.quad, &prm.bc, nugget, &dummy};
+        rs.step_(T + f0, yd, f, prm.xtol, prm.ytol, kBracketIts, prm.method);
+        if (rs.phase == RootSolve::kDone) {
+            prm.out[(long long)comp * prm.outRs + i * prm.outCs] = rs.result;
+            if (prm.info) prm.info[(long long)comp * prm.infoStride + i] = rs.info;
+            if (rs.info < 0) stAll |= kStatusNoBracket;
+            have = false;
+            need = true;
+        } else {
+            startQuad(rs.x);
+        }
     }
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }
@@ -1237,6 +1526,27 @@ cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t s
     if (prm.keyPass) {
         if constexpr (BASIS == kBasisSigmoid) return cudaErrorInvalidValue;
         else kern = inverseKeyKernel<BASIS, POS, PMAX>;
+    }
+    if (prm.queuePass) {
+        // Persistent: as many 128-thread blocks as are resident at once (at
+        // most one per 128 points).
+        if constexpr (BASIS == kBasisSigmoid) {
+            return cudaErrorInvalidValue;
+        } else {
+            if (prm.tpb != 128 || !prm.queue || !prm.acoef) return cudaErrorInvalidValue;
+            kern = inverseQueueKernel<BASIS, POS, PMAX>;
+            int perSM = 0, dev = 0, nSM = 0;
+            cudaError_t e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 128, 0)) != cudaSuccess) return e;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            const long long need = (prm.N + 127) / 128;
+            const int grid = (int)std::max(1LL, std::min(need, (long long)std::max(1, perSM) * nSM));
+            kern<<<grid, 128, 0, stream>>>(prm);
+            e = cudaGetLastError();
+            countLaunches(stream, 1);
+            return e;
+        }
     }
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

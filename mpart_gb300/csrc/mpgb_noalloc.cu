@@ -12,11 +12,16 @@
 //  * the array holds kNoAllocScratchBytes (64 MiB); a call needing more is
 //    rejected with MPGB_ERR_INVALID_ARGUMENT and a message giving both sizes;
 //  * every GPU that loads the library holds its own copy of the array until
-//    the process exits;
+//    the process exits.  With CUDA's lazy module loading (the default) the
+//    driver loads the module holding the array, and reserves its memory,
+//    when the array's address is first looked up; that look-up is done when
+//    a map is created on the device (reserveNoAllocScratch, called by every
+//    monotone component's constructor), so the entry point's own calls
+//    reserve nothing.  Should that look-up have failed, the first call on
+//    the device makes it (and then reserves the array); make that first
+//    call during start-up, before any stream capture;
 //  * all calls share the array, which keeps the last call's contents, so
-//    calls that overlap on the GPU (different streams, or threads) race;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress); make that first call before any stream capture.
+//    calls that overlap on the GPU (different streams, or threads) race.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -59,6 +64,22 @@ void* scratchBase() {
     return g_base[dev];
 }
 
+}  // namespace noalloc
+
+// Looks up (and so, under lazy module loading, reserves) the scratch array
+// of the current device; called when a monotone component is created.  A
+// failure is not an error here: the entry point's first call repeats the
+// look-up and reports it.
+void reserveNoAllocScratch() noexcept {
+    try {
+        noalloc::scratchBase();
+    } catch (...) {
+        cudaGetLastError();
+    }
+}
+
+namespace noalloc {
+
 struct GatherDesc {
     const double* src;
     const int32_t* slotTerm;
@@ -86,14 +107,16 @@ struct Carve {
     }
 };
 
-bool onDevice(const void* p) {
+// Device memory of the current device, or managed memory (the kernels run
+// on the current device and read these pointers directly).
+bool onDevice(const void* p, int dev) {
     if (!p) return true;
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
 }
 
 void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, const mpgb_matrix& lsens,
@@ -113,9 +136,12 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         throw std::invalid_argument("out_logdet must hold N values");
     if (outLogDet.data && nComps != 1)
         throw std::invalid_argument("the no-allocation entry point returns log-determinants of one-component maps only");
-    if (!onDevice(pts.data) || !onDevice(sens.data) || !onDevice(lsens.data) || !onDevice(outEval.data) ||
-        !onDevice(outLogDet.data) || !onDevice(coeffGrad))
-        throw std::invalid_argument("the no-allocation entry point takes device pointers only");
+    int curDev = 0;
+    MPGB_CUDA(cudaGetDevice(&curDev));
+    if (!onDevice(pts.data, curDev) || !onDevice(sens.data, curDev) || !onDevice(lsens.data, curDev) ||
+        !onDevice(outEval.data, curDev) || !onDevice(outLogDet.data, curDev) || !onDevice(coeffGrad, curDev))
+        throw std::invalid_argument(
+            "the no-allocation entry point takes device pointers of the current device (or managed memory) only");
     const MapOptions& o = map.Options();
     if (!o.contDeriv)
         throw std::invalid_argument("contDeriv = false (discrete derivative) is not provided without allocation.");
@@ -247,7 +273,8 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
     MPGB_CUDA(cudaMemcpyAsync(&st, dStatus, sizeof(int), cudaMemcpyDeviceToHost, stream));
     MPGB_CUDA(cudaStreamSynchronize(stream));
     if (st & kStatusInf)
-        throw IntegrandError("FusedForwardAdjoint (no allocation): MonotoneIntegrand: g(df(...)) overflowed.");
+        throw IntegrandError(
+            "FusedForwardAdjoint (no allocation): MonotoneIntegrand: nan was encountered in value of g(df(...)).");
     if (st & kStatusBudget)
         throw std::runtime_error("FusedForwardAdjoint (no allocation): adaptive quadrature exceeded its interval budget.");
 }

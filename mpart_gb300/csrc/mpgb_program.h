@@ -38,6 +38,11 @@ void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b);
 // std::invalid_argument for enum values out of range.
 MapOptions mapOptionsFromC(const mpgb_map_options* o);
 
+// Looks up the no-allocation entry point's scratch array on the current
+// device (mpgb_noalloc.cu), so that the module holding it is loaded, and its
+// memory reserved, when maps are created rather than inside that entry point.
+void reserveNoAllocScratch() noexcept;
+
 // ---------------------------------------------------------------------------
 // Component program: the multi-index set reorganised as a prefix tree over
 // the leading coordinates (see mpgb_device.cuh for the factorisation).
@@ -208,6 +213,7 @@ struct ComponentProgram {
         dLeadDeg = toDevice(leadDeg);
         dRowOff = toDevice(rowOff);
         dNodeCIdx = toDevice(nodeCIdx);
+        reserveNoAllocScratch();
     }
     ~ComponentProgram() {
         cudaFree(dNodeA);

@@ -170,7 +170,14 @@ struct InverseParams {
     double* acoef;
     double* key;
     int keyPass;
-    int pad3_;
+    int method;  // kInverseITP (the reference's solver) or kInverseNewton
+    // Queue pass (queuePass = 1, monotone components, component compBegin):
+    // a persistent launch whose lanes take the points one at a time from
+    // *queue (zero on entry), in perm order from the expensive end, and solve
+    // each with the full bracket budget; a_k come from acoef.
+    int* queue;
+    int queuePass;
+    int pad4_;
     QuadParams quad;
     BasisConsts bc;
 };

@@ -24,7 +24,11 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+# MPGB_ORACLE_BUILD=timing selects the timing build (default floating-point
+# contraction) for CPU-baseline timings; every parity check uses the default,
+# strict build.
+_LIB_NAME = "liboracle_timing.so" if os.environ.get("MPGB_ORACLE_BUILD") == "timing" else "liboracle.so"
+_LIB_PATH = os.path.join(_HERE, "_build", _LIB_NAME)
 _lib = None
 
 BASIS_PROB_HERMITE = 0
@@ -354,6 +358,7 @@ class OracleComponent:
         self.input_dim = self.dim
         self.output_dim = 1
         self.nugget = float(nugget)
+        self.abs_tol, self.rel_tol = float(abs_tol), float(rel_tol)
         L = lib()
         d = self.dims if len(self.dims) else np.zeros(1, np.uint32)
         o = self.orders if len(self.orders) else np.zeros(1, np.uint32)

@@ -336,3 +336,92 @@ def test_inverse_round_trip_far_roots(oracle, basis, pos, scale, rscale, bound):
     assert ok.sum() > 500 and np.nanmax(np.abs(x)) > 7.0
     back = om.evaluate(coef, np.where(ok, x, 0.0))
     assert np.abs(back - r)[:, ok].max() < bound
+
+
+def _itp_reference(f, yd, x0, xtol, ftol):
+    """MParT/Utilities/RootFinding.h:20-178 (FindBracket, Find_x_ITP,
+    InverseSingleBracket) restated in plain Python floats, independently of
+    the oracle's C++."""
+    xlb = xub = x0
+    ylb = yub = f(x0)
+    step = 1.0
+    if ylb > yd:
+        xub, yub = xlb, ylb
+        for _ in range(128):
+            xlb = xub - step
+            ylb = f(xlb)
+            if abs((yub - ylb) / (xub - xlb)) < 1e-12 and (xub - xlb) > 10:
+                return math.nan
+            if ylb > yd:
+                yub, xub = ylb, xlb
+                step *= 2.0
+            else:
+                break
+        else:
+            return math.nan
+    else:
+        for _ in range(128):
+            xub = xlb + step
+            yub = f(xub)
+            if abs((yub - ylb) / (xub - xlb)) < 1e-12 and (xub - xlb) > 10:
+                return math.nan
+            if yub < yd:
+                ylb, xlb = yub, xub
+                step *= 2.0
+            else:
+                break
+        else:
+            return math.nan
+    if ylb > yd or yub < yd:
+        return math.nan
+    nhalf = math.ceil(math.log2(0.5 * (xub - xlb) / xtol))
+    for it in range(10000):
+        xb = 0.5 * (xub + xlb)
+        xf = (xub * ylb - xlb * yub) / (ylb - yub)
+        sigma = 1.0 if (xb - xf) > 0 else -1.0
+        delta = min(0.1 * (xub - xlb) ** 2, abs(xb - xf))
+        xf += delta * sigma
+        rho = min(xtol * 2.0 ** (nhalf + 1.0 - it) - 0.5 * (xub - xlb), abs(xf - xb))
+        xc = xb - sigma * rho
+        yc = f(xc)
+        if abs(yc - yd) < ftol:
+            return xc
+        if yc > yd:
+            xub, yub = xc, yc
+        else:
+            xlb, ylb = xc, yc
+        if (xub - xlb) < xtol or (yub - ylb) < ftol:
+            break
+    return 0.5 * (xub + xlb)
+
+
+def test_itp_sensitivity_to_last_bits(oracle):
+    """The oracle's Inverse is the reference's ITP to the bit (an independent
+    restatement of RootFinding.h over the oracle's own T gives identical
+    roots), and that solver stops at an iterate that moves by up to
+    xtol + ytol / slope when T changes in its last bits: with T scaled by
+    1 +- 1e-15 a large share of the C1 roots (first component, xtol = ytol =
+    1e-6) move by more than xtol.  Any other build of the reference (another
+    compiler, FMA contraction, another summation order -- the GPU's among
+    them) therefore agrees with it within the solver's tolerance, not within
+    xtol."""
+    O = oracle
+    om = O.OracleTriangularMap(2, 2, 3, normalize=True, posfunc=O.POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6,
+                               max_sub=30)
+    coef = np.random.default_rng(0).normal(0.0, 0.1, om.num_coeffs)
+    x = np.random.default_rng(1).standard_normal((2, 120))
+    r = om.evaluate(coef, x)
+    comp, c0 = om.comps[0], om.split(coef)[0]
+    ref = comp.inverse(c0, x[:1], r[0], 1e-6, 1e-6)
+    T = lambda v, s=1.0: float(comp.evaluate(c0, np.array([[v]]))[0]) * s
+    moved, ratio = 0, 0.0
+    for i in range(x.shape[1]):
+        a = _itp_reference(T, r[0, i], x[0, i], 1e-6, 1e-6)
+        assert a == ref[i]
+        slope = float(comp.cont_derivative(c0, np.array([[a]]))[0])
+        for s in (1.0 + 1e-15, 1.0 - 1e-15):
+            b = _itp_reference(lambda v: T(v, s), r[0, i], x[0, i], 1e-6, 1e-6)
+            moved += abs(a - b) > 1e-6
+            ratio = max(ratio, abs(a - b) / (1e-6 + 1e-6 / slope))
+    assert moved >= 0.1 * 2 * x.shape[1]
+    assert ratio <= 1.0 + 1e-9

@@ -7,6 +7,12 @@ results as mpgb_fused_fwd_adj -- checked here through the C ABI on two calls
 in a row, within the parity tolerance of the other GPU tests (1e-10 relative,
 floored at 1e-3 of the largest entry for the summed gradient).
 
+The results are also checked against the CPU oracle on a small triangular
+map, and a call on a freshly created map must change neither the device's
+free memory nor torch's caching allocator (the modules of the kernels it
+launches are loaded by a warm-up call first, as CUDA's lazy module loading
+does for any library's first launch of a kernel).
+
 This file is collected last on purpose."""
 import ctypes as C
 
@@ -78,3 +84,35 @@ def test_noalloc_triangular_map_and_size_limit(gpu):
     xb = z(16, 100000)
     with pytest.raises(ValueError, match="bytes of scratch"):
         _noalloc(M, big, xb, z(1, 100000), None, None, z(big.numCoeffs))
+
+
+def test_noalloc_matches_oracle_and_allocates_nothing(gpu, oracle):
+    import torch
+    M, O = gpu, oracle
+    coef = np.random.default_rng(0).normal(0.0, 0.1, 14)
+    n = 2000
+    xh = np.random.default_rng(1).standard_normal((2, n))
+    sh = np.random.default_rng(2).standard_normal((2, n))
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+    z = lambda *s: torch.zeros(*s, dtype=torch.float64, device="cuda")
+    # Warm-up on one map: the kernels' modules are loaded by their first launch.
+    warm = M.CreateTriangular(2, 2, 3, _opts(M))
+    warm.SetCoeffs(coef)
+    x, sens = dev(xh), dev(sh)
+    _noalloc(M, warm, x, sens, z(2, n), None, z(warm.numCoeffs))
+    # A fresh map and fresh outputs, all created before the measurement.
+    tm = M.CreateTriangular(2, 2, 3, _opts(M))
+    tm.SetCoeffs(coef)
+    ev, cg = z(2, n), z(tm.numCoeffs)
+    torch.cuda.synchronize()
+    free0, reserved0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+    for _ in range(2):
+        _noalloc(M, tm, x, sens, ev, None, cg)
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+        assert torch.cuda.memory_reserved() == reserved0
+        om = O.OracleTriangularMap(2, 2, 3, normalize=True, posfunc=O.POS_SOFTPLUS, abs_tol=1e-6, rel_tol=1e-6,
+                                   max_sub=30)
+        _close(ev.cpu().numpy(), om.evaluate(coef, xh))
+        ref = om.coeff_grad(coef, xh, sh).sum(axis=1) + om.logdet_coeff_grad(coef, xh).sum(axis=1)
+        _close(cg.cpu().numpy(), ref, floor=1e-3)
