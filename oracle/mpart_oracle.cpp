@@ -1079,9 +1079,13 @@ struct View2 {
 
 #define ORC_PARALLEL_FOR _Pragma("omp parallel for schedule(dynamic, 16)")
 
-// EvaluateSingle (MonotoneComponent.h:992-1017).
-static double evaluateSingle(const Component& C, double* cache, double* ws, double xd, const double* coeffs, long* nev, int* inf) {
-    Integrand ig{&C.ex, cache, xd, coeffs, dNone, C.nugget, C.pos};
+// EvaluateSingle (MonotoneComponent.h:992-1017).  Its nugget argument
+// defaults to 0: EvaluateImpl calls it without one (MonotoneComponent.h:290),
+// so Evaluate ignores MapOptions::nugget, while Inverse passes the
+// component's (SingleEvaluator, :434, :1085-1088).
+static double evaluateSingle(const Component& C, double* cache, double* ws, double xd, const double* coeffs, long* nev,
+                             int* inf, double nugget = 0.0) {
+    Integrand ig{&C.ex, cache, xd, coeffs, dNone, nugget, C.pos};
     double out = 0.0;
     C.quad.integrate(ws, ig, 1, 0, 1, &out);
     C.ex.fillCache2(cache, 0.0, dNone);
@@ -1398,7 +1402,7 @@ int orc_inverse(void* h, const double* coeffs, const double* xs, long numXs, lon
         }
         std::vector<double> cache(C.ex.cacheSize), ws(C.quad.wsSize(1));
         C.ex.fillCache1(cache.data(), pt.data(), dNone);
-        auto f = [&](double x) { return evaluateSingle(C, cache.data(), ws.data(), x, coeffs, nullptr, nullptr); };
+        auto f = [&](double x) { return evaluateSingle(C, cache.data(), ws.data(), x, coeffs, nullptr, nullptr, C.nugget); };
         int inf = 0;
         out[i * ostride] = inverseSingleBracket(ys[i * ystride], f, pt[D - 1], xtol, ytol, inf);
         if (info) info[i] = inf;

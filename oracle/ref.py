@@ -1,0 +1,165 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes front end of ``oracle/_ref/libmpart_ref.so``: MParT's own map classes
+(``src/ParameterizedFunctionBase.cpp``, ``src/ConditionalMapBase.cpp``,
+``src/TriangularMap.cpp``, the component factory registrations
+``src/MapFactoryImpl{4..9}.cpp`` and ``src/MultiIndices/*.cpp``, with the
+headers they include), compiled unchanged from the reference checkout by
+``oracle/ref.mk`` against the Kokkos / Eigen stand-ins in ``oracle/ref_shim/``.
+
+It exists only where the reference checkout does (the development host):
+``available()`` says whether it can be built.  The tests use it to pin the
+oracle's restatement, and the golden fixtures, to the reference itself.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_ref", "libmpart_ref.so")
+REF_DIR = os.environ.get("MPGB_REFERENCE_DIR", "/root/reference")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_up = C.POINTER(C.c_uint)
+
+# MapOptions enums (MParT/MapOptions.h)
+BASIS_PROB_HERMITE, BASIS_HERMITE_FUNCTIONS = 0, 2
+POS_EXP, POS_SOFTPLUS = 0, 1
+QUAD_CLENSHAW_CURTIS, QUAD_ADAPTIVE_SIMPSON, QUAD_ACC = 0, 1, 2
+
+
+def available() -> bool:
+    """The reference checkout is present (so the library can be built here)."""
+    return os.path.isdir(os.path.join(REF_DIR, "MParT")) and os.path.isdir(os.path.join(REF_DIR, "src"))
+
+
+def build():
+    subprocess.run(["make", "-s", "-j8", "-f", os.path.join(_HERE, "ref.mk"), f"REF={REF_DIR}"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB)
+        opt = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint, C.c_uint, C.c_uint, C.c_double,
+               C.c_int]
+        L.ref_triangular.restype = C.c_void_p
+        L.ref_triangular.argtypes = [C.c_uint, C.c_uint, C.c_uint] + opt
+        L.ref_component.restype = C.c_void_p
+        L.ref_component.argtypes = [C.c_uint, C.c_uint, _up, _up, _up] + opt
+        L.ref_free.argtypes = [C.c_void_p]
+        L.ref_last_error.restype = C.c_char_p
+        L.ref_sizes.argtypes = [C.c_void_p, _up, _up, _up]
+        L.ref_set_coeffs.argtypes = [C.c_void_p, _dp, C.c_long]
+        for f in ("ref_evaluate", "ref_logdet", "ref_logdet_coeff_grad", "ref_logdet_input_grad"):
+            getattr(L, f).argtypes = [C.c_void_p, _dp, C.c_long, _dp]
+        for f in ("ref_coeff_grad", "ref_gradient"):
+            getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, C.c_long, _dp]
+        L.ref_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, C.c_double, C.c_double, _dp]
+        _lib = L
+    return _lib
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class RefMap:
+    """A map of the reference: MapFactory::CreateTriangular(inputDim, outputDim,
+    totalOrder, options), or (``starts`` given) MapFactory::CreateComponent on
+    a compressed multi-index set.  Options as MapOptions (basisNorm true,
+    quadPts 5, AdaptiveClenshawCurtis unless given)."""
+
+    def __init__(self, input_dim, output_dim=None, order=None, basis="ProbabilistHermite", normalize=True,
+                 posfunc="SoftPlus", quad="AdaptiveClenshawCurtis", abs_tol=1e-6, rel_tol=1e-6, max_sub=30,
+                 min_sub=0, quad_pts=5, nugget=0.0, cont_deriv=True, starts=None, dims=None, orders=None):
+        b = {"ProbabilistHermite": BASIS_PROB_HERMITE, "HermiteFunctions": BASIS_HERMITE_FUNCTIONS}[basis]
+        p = {"Exp": POS_EXP, "SoftPlus": POS_SOFTPLUS}[posfunc]
+        q = {"AdaptiveSimpson": QUAD_ADAPTIVE_SIMPSON, "ClenshawCurtis": QUAD_CLENSHAW_CURTIS,
+             "AdaptiveClenshawCurtis": QUAD_ACC}[quad]
+        opt = (b, int(normalize), p, q, abs_tol, rel_tol, max_sub, min_sub, quad_pts, nugget, int(cont_deriv))
+        L = lib()
+        if starts is None:
+            self._h = L.ref_triangular(input_dim, output_dim, order, *opt)
+        else:
+            s = np.ascontiguousarray(starts, np.uint32)
+            d = np.ascontiguousarray(dims if len(dims) else [0], np.uint32)
+            o = np.ascontiguousarray(orders if len(orders) else [0], np.uint32)
+            self._keep = (s, d, o)
+            self._h = L.ref_component(input_dim, len(s) - 1, s.ctypes.data_as(_up), d.ctypes.data_as(_up),
+                                      o.ctypes.data_as(_up), *opt)
+        if not self._h:
+            raise RuntimeError(L.ref_last_error().decode())
+        a, b_, c = C.c_uint(), C.c_uint(), C.c_uint()
+        L.ref_sizes(self._h, C.byref(a), C.byref(b_), C.byref(c))
+        self.input_dim, self.output_dim, self.num_coeffs = a.value, b_.value, c.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ref_free(self._h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(lib().ref_last_error().decode())
+
+    def set_coeffs(self, coeffs):
+        c = _c(coeffs)
+        assert c.size == self.num_coeffs
+        self._check(lib().ref_set_coeffs(self._h, c.ctypes.data_as(_dp), c.size))
+
+    def evaluate(self, pts):
+        x = _c(pts)
+        out = np.zeros((self.output_dim, x.shape[1]))
+        self._check(lib().ref_evaluate(self._h, x.ctypes.data_as(_dp), x.shape[1], out.ctypes.data_as(_dp)))
+        return out
+
+    def logdet(self, pts):
+        x = _c(pts)
+        out = np.zeros(x.shape[1])
+        self._check(lib().ref_logdet(self._h, x.ctypes.data_as(_dp), x.shape[1], out.ctypes.data_as(_dp)))
+        return out
+
+    def coeff_grad(self, pts, sens):
+        x, s = _c(pts), _c(np.reshape(sens, (self.output_dim, -1)))
+        out = np.zeros((self.num_coeffs, x.shape[1]))
+        self._check(lib().ref_coeff_grad(self._h, x.ctypes.data_as(_dp), s.ctypes.data_as(_dp), x.shape[1],
+                                         out.ctypes.data_as(_dp)))
+        return out
+
+    def gradient(self, pts, sens):
+        x, s = _c(pts), _c(np.reshape(sens, (self.output_dim, -1)))
+        out = np.zeros((self.input_dim, x.shape[1]))
+        self._check(lib().ref_gradient(self._h, x.ctypes.data_as(_dp), s.ctypes.data_as(_dp), x.shape[1],
+                                       out.ctypes.data_as(_dp)))
+        return out
+
+    def logdet_coeff_grad(self, pts):
+        x = _c(pts)
+        out = np.zeros((self.num_coeffs, x.shape[1]))
+        self._check(lib().ref_logdet_coeff_grad(self._h, x.ctypes.data_as(_dp), x.shape[1], out.ctypes.data_as(_dp)))
+        return out
+
+    def logdet_input_grad(self, pts):
+        x = _c(pts)
+        out = np.zeros((self.input_dim, x.shape[1]))
+        self._check(lib().ref_logdet_input_grad(self._h, x.ctypes.data_as(_dp), x.shape[1], out.ctypes.data_as(_dp)))
+        return out
+
+    def inverse(self, x1, r, xtol=1e-6, ytol=1e-6):
+        """TriangularMap::InverseImpl with the components' xtol / ytol options;
+        x1 has up to inputDim rows (the rows past inputDim - outputDim are the
+        initial guesses, zero when absent)."""
+        r = _c(np.reshape(r, (self.output_dim, -1)))
+        n = r.shape[1]
+        x1 = _c(x1) if len(x1) else np.zeros((0, n))
+        out = np.zeros((self.output_dim, n))
+        self._check(lib().ref_inverse(self._h, x1.ctypes.data_as(_dp), x1.shape[0], r.ctypes.data_as(_dp), n,
+                                      xtol, ytol, out.ctypes.data_as(_dp)))
+        return out

@@ -1,0 +1,280 @@
+// ORACLE -- test infrastructure only.
+//
+// C entry points over MParT's own map classes, compiled from the reference's
+// sources unchanged (oracle/ref.mk builds this file together with
+// src/ParameterizedFunctionBase.cpp, src/ConditionalMapBase.cpp,
+// src/TriangularMap.cpp, src/MapFactoryImpl{4..9}.cpp, src/MultiIndices/*.cpp
+// and src/Utilities/Miscellaneous.cpp against the Kokkos and Eigen stand-ins
+// in oracle/ref_shim/).  Everything numeric -- the basis recurrences, the
+// expansion worker's caches and term loops, the MonotoneIntegrand, the
+// adaptive quadratures, the root finder, the TriangularMap component loops --
+// is the reference's code; this file only builds maps the way
+// MapFactory::CreateTriangular / CreateComponent do and forwards to the
+// maps' *Impl methods.  The tests use it to pin the oracle's C++ restatement
+// (and so the GPU) to the reference itself.
+//
+// Matrices are row-major rows x N arrays (coordinate d of point i at
+// d * N + i), the layout the reference's Python binding passes.
+#include <cstdio>
+#include <exception>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "MParT/ConditionalMapBase.h"
+#include "MParT/HermiteFunction.h"
+#include "MParT/MapFactory.h"
+#include "MParT/MapOptions.h"
+#include "MParT/MonotoneComponent.h"
+#include "MParT/MultiIndices/FixedMultiIndexSet.h"
+#include "MParT/MultivariateExpansionWorker.h"
+#include "MParT/OrthogonalPolynomial.h"
+#include "MParT/PositiveBijectors.h"
+#include "MParT/Quadrature.h"
+#include "MParT/TriangularMap.h"
+
+using namespace mpart;
+using Host = Kokkos::HostSpace;
+using Map = ConditionalMapBase<Host>;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct RefMap {
+    std::shared_ptr<Map> map;                 // the object the calls go to
+    std::vector<std::shared_ptr<Map>> comps;  // its components (one for a single component)
+};
+
+template <class F>
+int guard(F&& f) {
+    try {
+        f();
+        return 0;
+    } catch (std::exception const& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+MapOptions options(int basis, int basisNorm, int pos, int quad, double absTol, double relTol, unsigned maxSub,
+                   unsigned minSub, unsigned quadPts, double nugget, int contDeriv) {
+    MapOptions o;
+    o.basisType = (BasisTypes)basis;
+    o.basisNorm = basisNorm != 0;
+    o.posFuncType = (PosFuncTypes)pos;
+    o.quadType = (QuadTypes)quad;
+    o.quadAbsTol = absTol;
+    o.quadRelTol = relTol;
+    o.quadMaxSub = maxSub;
+    o.quadMinSub = minSub;
+    o.quadPts = quadPts;
+    o.nugget = nugget;
+    o.contDeriv = contDeriv != 0;
+    return o;
+}
+
+StridedMatrix<const double, Host> cmat(const double* p, long rows, long n) {
+    return StridedMatrix<const double, Host>(p, Kokkos::LayoutStride(rows, n, n, 1));
+}
+StridedMatrix<double, Host> mat(double* p, long rows, long n) {
+    return StridedMatrix<double, Host>(p, Kokkos::LayoutStride(rows, n, n, 1));
+}
+
+// MonotoneComponent::InverseImpl with the "xtol" / "ytol" options
+// (MonotoneComponent.h:330-443) for each concrete component type the
+// factory registrations in MapFactoryImpl{4..9}.cpp create.
+template <class Basis, class Pos, class Quad>
+using Comp = MonotoneComponent<MultivariateExpansionWorker<BasisEvaluator<BasisHomogeneity::Homogeneous, Basis>, Host>,
+                               Pos, Quad, Host>;
+
+template <class C>
+bool tryInverse(Map* m, StridedMatrix<const double, Host> const& x, StridedVector<const double, Host> const& r,
+                StridedVector<double, Host> out, std::map<std::string, std::string> const& opts) {
+    C* c = dynamic_cast<C*>(m);
+    if (!c) return false;
+    StridedVector<const double, Host> coeffs = c->Coeffs();
+    c->InverseImpl(x, r, coeffs, out, opts);
+    return true;
+}
+
+template <class... Cs>
+void inverseAny(Map* m, StridedMatrix<const double, Host> const& x, StridedVector<const double, Host> const& r,
+                StridedVector<double, Host> out, std::map<std::string, std::string> const& opts) {
+    if (!(tryInverse<Cs>(m, x, r, out, opts) || ...)) throw std::runtime_error("unsupported component type");
+}
+
+void componentInverse(Map* m, StridedMatrix<const double, Host> const& x, StridedVector<const double, Host> const& r,
+                      StridedVector<double, Host> out, std::map<std::string, std::string> const& opts) {
+    inverseAny<Comp<ProbabilistHermite, SoftPlus, AdaptiveClenshawCurtis<Host>>,
+               Comp<ProbabilistHermite, Exp, AdaptiveClenshawCurtis<Host>>,
+               Comp<HermiteFunction, SoftPlus, AdaptiveClenshawCurtis<Host>>,
+               Comp<HermiteFunction, Exp, AdaptiveClenshawCurtis<Host>>,
+               Comp<ProbabilistHermite, SoftPlus, AdaptiveSimpson<Host>>,
+               Comp<ProbabilistHermite, Exp, AdaptiveSimpson<Host>>,
+               Comp<HermiteFunction, SoftPlus, AdaptiveSimpson<Host>>,
+               Comp<HermiteFunction, Exp, AdaptiveSimpson<Host>>,
+               Comp<ProbabilistHermite, SoftPlus, ClenshawCurtisQuadrature<Host>>,
+               Comp<ProbabilistHermite, Exp, ClenshawCurtisQuadrature<Host>>,
+               Comp<HermiteFunction, SoftPlus, ClenshawCurtisQuadrature<Host>>,
+               Comp<HermiteFunction, Exp, ClenshawCurtisQuadrature<Host>>>(m, x, r, out, opts);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ref_last_error() { return g_err.c_str(); }
+
+// MapFactory::CreateTriangular (src/MapFactory.cpp:105-124): component i has
+// the total-order set of dimension i + extra + 1, made by the registered
+// factory function for the options (MapFactory::CreateComponent,
+// src/MapFactory.cpp:22-27); zero coefficients.
+void* ref_triangular(unsigned inputDim, unsigned outputDim, unsigned totalOrder, int basis, int basisNorm, int pos,
+                     int quad, double absTol, double relTol, unsigned maxSub, unsigned minSub, unsigned quadPts,
+                     double nugget, int contDeriv) {
+    RefMap* out = nullptr;
+    guard([&] {
+        const MapOptions o = options(basis, basisNorm, pos, quad, absTol, relTol, maxSub, minSub, quadPts, nugget,
+                                     contDeriv);
+        auto* r = new RefMap;
+        const unsigned extra = inputDim - outputDim;
+        for (unsigned i = 0; i < outputDim; ++i) {
+            FixedMultiIndexSet<Host> mset(i + extra + 1, totalOrder);
+            r->comps.push_back(MapFactory::CompFactoryImpl<Host>::GetFactoryFunction(o)(mset, o));
+        }
+        r->map = std::make_shared<TriangularMap<Host>>(r->comps);
+        Kokkos::View<const double*, Host> coeffs = Kokkos::View<double*, Host>("Component Coefficients",
+                                                                                 r->map->numCoeffs);
+        r->map->SetCoeffs(coeffs);
+        out = r;
+    });
+    return out;
+}
+
+// MapFactory::CreateComponent on a compressed multi-index set
+// (FixedMultiIndexSet(dim, nzStarts, nzDims, nzOrders)).
+void* ref_component(unsigned dim, unsigned numTerms, const unsigned* starts, const unsigned* dims,
+                    const unsigned* orders, int basis, int basisNorm, int pos, int quad, double absTol,
+                    double relTol, unsigned maxSub, unsigned minSub, unsigned quadPts, double nugget, int contDeriv) {
+    RefMap* out = nullptr;
+    guard([&] {
+        const MapOptions o = options(basis, basisNorm, pos, quad, absTol, relTol, maxSub, minSub, quadPts, nugget,
+                                     contDeriv);
+        const unsigned nnz = starts[numTerms];
+        Kokkos::View<unsigned*, Host> s("nzStarts", numTerms + 1), d("nzDims", nnz), r("nzOrders", nnz);
+        for (unsigned i = 0; i <= numTerms; ++i) s(i) = starts[i];
+        for (unsigned i = 0; i < nnz; ++i) {
+            d(i) = dims[i];
+            r(i) = orders[i];
+        }
+        FixedMultiIndexSet<Host> mset(dim, s, d, r);
+        auto* m = new RefMap;
+        m->map = MapFactory::CompFactoryImpl<Host>::GetFactoryFunction(o)(mset, o);
+        m->comps.push_back(m->map);
+        Kokkos::View<const double*, Host> coeffs = Kokkos::View<double*, Host>("Component Coefficients",
+                                                                                 m->map->numCoeffs);
+        m->map->SetCoeffs(coeffs);
+        out = m;
+    });
+    return out;
+}
+
+void ref_free(void* h) { delete (RefMap*)h; }
+
+int ref_sizes(void* h, unsigned* inputDim, unsigned* outputDim, unsigned* numCoeffs) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        *inputDim = m.inputDim;
+        *outputDim = m.outputDim;
+        *numCoeffs = m.numCoeffs;
+    });
+}
+
+// ParameterizedFunctionBase::SetCoeffs (deep copy, src/ParameterizedFunctionBase.cpp:185-207).
+int ref_set_coeffs(void* h, const double* c, long n) {
+    return guard([&] {
+        Kokkos::View<const double*, Host> v(c, (size_t)n);
+        ((RefMap*)h)->map->SetCoeffs(v);
+    });
+}
+
+int ref_evaluate(void* h, const double* pts, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.EvaluateImpl(cmat(pts, m.inputDim, n), mat(out, m.outputDim, n));
+    });
+}
+
+int ref_logdet(void* h, const double* pts, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.LogDeterminantImpl(cmat(pts, m.inputDim, n), StridedVector<double, Host>(out, (size_t)n));
+    });
+}
+
+int ref_coeff_grad(void* h, const double* pts, const double* sens, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.CoeffGradImpl(cmat(pts, m.inputDim, n), cmat(sens, m.outputDim, n), mat(out, m.numCoeffs, n));
+    });
+}
+
+int ref_gradient(void* h, const double* pts, const double* sens, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.GradientImpl(cmat(pts, m.inputDim, n), cmat(sens, m.outputDim, n), mat(out, m.inputDim, n));
+    });
+}
+
+int ref_logdet_coeff_grad(void* h, const double* pts, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.LogDeterminantCoeffGradImpl(cmat(pts, m.inputDim, n), mat(out, m.numCoeffs, n));
+    });
+}
+
+int ref_logdet_input_grad(void* h, const double* pts, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        m.LogDeterminantInputGradImpl(cmat(pts, m.inputDim, n), mat(out, m.inputDim, n));
+    });
+}
+
+// TriangularMap::InverseImpl / InverseInplace (src/TriangularMap.cpp:146-184)
+// with the components' "xtol" / "ytol" options, which the reference's
+// three-argument InverseImpl leaves at their defaults (1e-6).  x1 has x1Rows
+// (<= inputDim) rows; fullOut = [x1; 0] is solved in place, component by
+// component, and its last outputDim rows are returned.
+int ref_inverse(void* h, const double* x1, long x1Rows, const double* r, long n, double xtol, double ytol,
+                double* out) {
+    return guard([&] {
+        RefMap& rm = *(RefMap*)h;
+        auto& m = *rm.map;
+        const unsigned ipdim = m.inputDim, opdim = m.outputDim, extra = ipdim - opdim;
+        Kokkos::View<double**, Host> full("Full Output", ipdim, (size_t)n);
+        for (long d = 0; d < x1Rows; ++d)
+            for (long i = 0; i < n; ++i) full(d, i) = x1[d * n + i];
+        auto R = cmat(r, opdim, n);
+        std::map<std::string, std::string> opts;
+        char buf[64];
+        std::snprintf(buf, sizeof buf, "%.17g", xtol);
+        opts["xtol"] = buf;
+        std::snprintf(buf, sizeof buf, "%.17g", ytol);
+        opts["ytol"] = buf;
+        unsigned start = 0;
+        for (auto& c : rm.comps) {
+            StridedMatrix<const double, Host> subX =
+                Kokkos::subview(full, std::make_pair(0, int(c->inputDim)), Kokkos::ALL());
+            StridedVector<const double, Host> subR = Kokkos::subview(R, start, Kokkos::ALL());
+            StridedVector<double, Host> subOut = Kokkos::subview(full, extra + start, Kokkos::ALL());
+            componentInverse(c.get(), subX, subR, subOut, opts);
+            start += c->outputDim;
+        }
+        for (unsigned k = 0; k < opdim; ++k)
+            for (long i = 0; i < n; ++i) out[k * n + i] = full(extra + k, i);
+    });
+}
+
+}  // extern "C"

@@ -1,6 +1,17 @@
-"""Generates the golden fixtures in this directory from the CPU oracle.
+"""Generates the golden fixtures in this directory.
 
     python tests/golden/make_golden.py
+
+c1, c2, c3 and c5 hold the outputs of the reference itself: MParT's own
+sources compiled unchanged into oracle/_ref (oracle/ref.mk; needs the
+reference checkout), with the per-component FastGaussianReverseKL loss and
+gradient composed from the reference's Evaluate, LogDeterminant, CoeffGrad
+and LogDeterminantCoeffGrad as src/MapObjective.cpp:185-234 does (that file
+needs Eigen's LU and is not compiled).  Each output is also computed by the
+oracle's restatement, which must agree to the bit.  sig (the sigmoid
+expansions, whose factory lives in src/MapFactory.cpp with the affine maps)
+comes from the oracle.  c2's per-point integrand evaluation counts come from
+the oracle (the reference does not count them).
 
 Inputs come from numpy's default_rng with the seeds below and are stored in
 the fixtures next to the outputs, so the fixtures do not depend on the
@@ -21,6 +32,45 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle import oracle as O  # noqa: E402
+from oracle import ref as R  # noqa: E402
+
+
+def agree(ref_out, orc_out, what):
+    """The reference's output, after checking the oracle's equals it to the bit."""
+    a, b = np.asarray(ref_out), np.asarray(orc_out)
+    if not (a.shape == b.shape and np.all((a == b) | (np.isnan(a) & np.isnan(b)))):
+        raise SystemExit(f"oracle and reference differ on {what}")
+    return a
+
+
+def ref_kl(basis, posfunc, tol, coef_blocks, comps, x):
+    """FastGaussianReverseKLObjective::CommonEval<EvalGrad> per component
+    (src/MapObjective.cpp:185-234) from the reference's own calls:
+    loss = mean(0.5 T^2 - logdet), grad = mean(T dT/dc - dlogdet/dc)."""
+    loss, grad = [], []
+    for c, cc in zip(comps, coef_blocks):
+        r = R.RefMap(c.input_dim, starts=c.starts, dims=c.dims, orders=c.orders, basis=basis, posfunc=posfunc,
+                     abs_tol=tol, rel_tol=tol)
+        r.set_coeffs(cc)
+        pts = np.ascontiguousarray(x[:c.input_dim])
+        T = r.evaluate(pts)[0]
+        ld = r.logdet(pts)
+        n = pts.shape[1]
+        l = 0.0
+        for j in range(n):
+            l += 0.5 * T[j] * T[j] - ld[j]
+        loss.append(l / n)
+        grad.append((r.coeff_grad(pts, T[None, :]) - r.logdet_coeff_grad(pts)).sum(axis=1) / n)
+    return np.array(loss), np.concatenate(grad)
+
+
+def oracle_kl(tm, coef, x):
+    loss, grad = [], []
+    for i, c in enumerate(tm.comps):
+        l, g = O.fast_gaussian_reverse_kl(c, tm.split(coef)[i], x[:c.input_dim])
+        loss.append(l)
+        grad.append(g)
+    return np.array(loss), np.concatenate(grad)
 
 
 def banana(n, seed):
@@ -35,53 +85,68 @@ def banana(n, seed):
 
 def make_c1(n=500):
     tm = O.OracleTriangularMap(2, 2, 3)
+    ref = R.RefMap(2, 2, 3)
     coef = np.random.default_rng(0).normal(0.0, 0.1, tm.num_coeffs)
+    ref.set_coeffs(coef)
     x = np.random.default_rng(1).standard_normal((2, n))
     sens = np.random.default_rng(7).standard_normal((2, n))
-    r = tm.evaluate(coef, x)
-    loss, grad = [], []
-    for i, c in enumerate(tm.comps):
-        l, g = O.fast_gaussian_reverse_kl(c, tm.split(coef)[i], x[:c.input_dim])
-        loss.append(l)
-        grad.append(g)
-    return dict(coef=coef, x=x, sens=sens, evaluate=r, logdet=tm.logdet(coef, x),
-                inverse_warm=tm.inverse(coef, x, r), inverse_cold=tm.inverse(coef, np.zeros((0, n)), r),
-                coeff_grad=tm.coeff_grad(coef, x, sens), logdet_coeff_grad=tm.logdet_coeff_grad(coef, x),
-                gradient=tm.gradient(coef, x, sens), logdet_input_grad=tm.logdet_input_grad(coef, x),
-                kl_loss=np.array(loss), kl_grad=np.concatenate(grad))
+    r = agree(ref.evaluate(x), tm.evaluate(coef, x), "c1 evaluate")
+    loss, grad = ref_kl("ProbabilistHermite", "SoftPlus", 1e-6, tm.split(coef), tm.comps, x)
+    oloss, ograd = oracle_kl(tm, coef, x)
+    return dict(coef=coef, x=x, sens=sens, evaluate=r,
+                logdet=agree(ref.logdet(x), tm.logdet(coef, x), "c1 logdet"),
+                inverse_warm=agree(ref.inverse(x, r), tm.inverse(coef, x, r), "c1 inverse (warm)"),
+                inverse_cold=agree(ref.inverse(np.zeros((0, n)), r), tm.inverse(coef, np.zeros((0, n)), r),
+                                   "c1 inverse (cold)"),
+                coeff_grad=agree(ref.coeff_grad(x, sens), tm.coeff_grad(coef, x, sens), "c1 coeff_grad"),
+                logdet_coeff_grad=agree(ref.logdet_coeff_grad(x), tm.logdet_coeff_grad(coef, x),
+                                        "c1 logdet_coeff_grad"),
+                gradient=agree(ref.gradient(x, sens), tm.gradient(coef, x, sens), "c1 gradient"),
+                logdet_input_grad=agree(ref.logdet_input_grad(x), tm.logdet_input_grad(coef, x),
+                                        "c1 logdet_input_grad"),
+                kl_loss=agree(loss, oloss, "c1 kl loss"), kl_grad=agree(grad, ograd, "c1 kl grad"))
 
 
 def make_c2(n=200):
     s, d, o = O.total_order(8, 4)
     c = O.OracleComponent(8, s, d, o)
+    ref = R.RefMap(8, starts=s, dims=d, orders=o)
     coef = np.random.default_rng(0).normal(0.0, 0.05, c.num_terms)
+    ref.set_coeffs(coef)
     x = np.random.default_rng(1).standard_normal((8, n))
     sens = np.random.default_rng(2).standard_normal(n)
     ev, nev, _ = c.evaluate(coef, x, return_evals=True)
-    return dict(coef=coef, x=x, sens=sens, evaluate=ev, nevals=nev, logdet=c.logdet(coef, x),
-                coeff_grad_sum=c.coeff_grad(coef, x, sens).sum(axis=1),
-                logdet_coeff_grad_sum=c.logdet_coeff_grad(coef, x).sum(axis=1))
+    return dict(coef=coef, x=x, sens=sens, evaluate=agree(ref.evaluate(x)[0], ev, "c2 evaluate"), nevals=nev,
+                logdet=agree(ref.logdet(x), c.logdet(coef, x), "c2 logdet"),
+                coeff_grad_sum=agree(ref.coeff_grad(x, sens[None, :]), c.coeff_grad(coef, x, sens),
+                                     "c2 coeff_grad").sum(axis=1),
+                logdet_coeff_grad_sum=agree(ref.logdet_coeff_grad(x), c.logdet_coeff_grad(coef, x),
+                                            "c2 logdet_coeff_grad").sum(axis=1))
 
 
 def make_c3(n=300):
     tm = O.OracleTriangularMap(6, 6, 5, basis=O.BASIS_HERMITE_FUNCTIONS, posfunc=O.POS_EXP, abs_tol=1e-7,
                                rel_tol=1e-7)
+    ref = R.RefMap(6, 6, 5, basis="HermiteFunctions", posfunc="Exp", abs_tol=1e-7, rel_tol=1e-7)
     coef = np.random.default_rng(3).normal(0.0, 0.01, tm.num_coeffs)
+    ref.set_coeffs(coef)
     x = banana(n, 11)
-    loss, grad = [], []
-    for i, c in enumerate(tm.comps):
-        l, g = O.fast_gaussian_reverse_kl(c, tm.split(coef)[i], x[:c.input_dim])
-        loss.append(l)
-        grad.append(g)
-    return dict(coef=coef, x=x, evaluate=tm.evaluate(coef, x), logdet=tm.logdet(coef, x), kl_loss=np.array(loss),
-                kl_grad=np.concatenate(grad))
+    loss, grad = ref_kl("HermiteFunctions", "Exp", 1e-7, tm.split(coef), tm.comps, x)
+    oloss, ograd = oracle_kl(tm, coef, x)
+    return dict(coef=coef, x=x, evaluate=agree(ref.evaluate(x), tm.evaluate(coef, x), "c3 evaluate"),
+                logdet=agree(ref.logdet(x), tm.logdet(coef, x), "c3 logdet"),
+                kl_loss=agree(loss, oloss, "c3 kl loss"), kl_grad=agree(grad, ograd, "c3 kl grad"))
 
 
 def make_c5(n=64):
     tm = O.OracleTriangularMap(16, 16, 3, abs_tol=1e-8, rel_tol=1e-8)
+    ref = R.RefMap(16, 16, 3, abs_tol=1e-8, rel_tol=1e-8)
     coef = np.random.default_rng(0).normal(0.0, 0.03, tm.num_coeffs)
+    ref.set_coeffs(coef)
     r = np.random.default_rng(1).standard_normal((16, n))
-    return dict(coef=coef, r=r, inverse=tm.inverse(coef, np.zeros((0, n)), r, xtol=1e-10, ytol=1e-10))
+    return dict(coef=coef, r=r, inverse=agree(ref.inverse(np.zeros((0, n)), r, 1e-10, 1e-10),
+                                              tm.inverse(coef, np.zeros((0, n)), r, xtol=1e-10, ytol=1e-10),
+                                              "c5 inverse"))
 
 
 def make_sig(n=200):
