@@ -224,6 +224,16 @@ public:
     void KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, cudaStream_t stream = 0);
     // Same for one component only (onlyComp >= 0), or all (onlyComp = -1).
     void KLObjective(StridedMatrix const& pts, double* lossPerComp, double* grad, int onlyComp, cudaStream_t stream);
+    // The same objective through the reference objective's own call sequence,
+    // per component: Evaluate, LogDeterminant, CoeffGrad with sens = T and
+    // LogDeterminantCoeffGrad into dense numTerms x N scratch, then the
+    // reductions (FastGaussianReverseKLObjective::CommonEval,
+    // src/MapObjective.cpp:185-234).  T and Ld (N doubles each), DT and DL
+    // (largest numTerms x N doubles each) are device scratch.  KLObjective
+    // takes this route when the nugget is nonzero: Evaluate then integrates
+    // without it and CoeffGrad with it, two quadrature trees.
+    void KLObjectiveCalls(StridedMatrix const& pts, double* lossPerComp, double* grad, int onlyComp, double* T,
+                          double* Ld, double* DT, double* DL, cudaStream_t stream);
 
     int CheckStatus(cudaStream_t stream = 0);  // synchronise, read and clear the status word
     // Process points grouped by |x_D| (default on); results do not depend on it

@@ -316,6 +316,21 @@ public:
     void FusedForwardAdjoint(const StridedMatrix* pts, const StridedMatrix* sens, double lsensScale,
                              const StridedMatrix* outEval, const StridedMatrix* outLogDet, double* const* coeffGrad,
                              cudaStream_t s) {
+        bool anyEval = false;
+        for (size_t m = 0; m < maps_.size(); ++m) anyEval |= !outEval[m].empty();
+        if (maps_[0]->Options().nugget != 0.0 && anyEval) {
+            // Evaluate integrates without the nugget (MonotoneComponent.h:290),
+            // the coefficient adjoint with it: the values come from each map's
+            // Evaluate after the batch launch.
+            std::vector<StridedMatrix> none(maps_.size());
+            stage(pts, sens, lsensScale, none.data(), outLogDet, coeffGrad, s);
+            runKernel(items_, s);
+            finishOutputs(s);
+            checkStatus(s);
+            for (size_t m = 0; m < maps_.size(); ++m)
+                if (!outEval[m].empty()) maps_[m]->EvaluateImpl(pts[m], outEval[m], s);
+            return;
+        }
         stage(pts, sens, lsensScale, outEval, outLogDet, coeffGrad, s);
         runKernel(items_, s);
         finishOutputs(s);

@@ -324,6 +324,9 @@ struct MapWorkspace {
     DevBuf inverseDefer; // two-pass inverse: number of deferred points
     DevBuf inverseKey;   // inverse processing order: per-target sort keys
     DevBuf inverseA;     // inverse: a_k of the component being solved, (pmax + 1) x N
+    DevBuf inverseList;  // inverse: points left to the warp pass
+    DevBuf inverseStack; // inverse: the warp pass's interval stacks
+    DevBuf klT, klLd, klDT, klDL;  // KLObjectiveCalls scratch (nonzero nugget)
     bool ordering = true;
 };
 
@@ -671,6 +674,12 @@ constexpr int kTpb = 128;
 // within 7 of the initial guess are bracketed there, the rest wait for the
 // second pass.
 constexpr int kFirstPassBracketIts = 3;
+// Inverse of monotone components: integrand nodes a point may take in the
+// queue pass before the warp pass takes it over, and the warp pass's grid
+// (blocks of four warps per SM) and per-warp interval stack.
+constexpr int kQueueNodeBudget = 3072;
+constexpr int kWarpPassBlocksPerSM = 2;
+constexpr int kWarpStackCap = 2048;
 
 void checkMatrix(const StridedMatrix& m, int64_t rows, int64_t cols, const char* what, const char* fn) {
     if (m.rows != rows || m.cols != cols) {
@@ -825,6 +834,10 @@ void MonotoneMapBase::EvaluateImpl(StridedMatrix const& pts, StridedMatrix const
     uploadItems(W, items, stream);
     FusedParams p{};
     baseParams(W, opts_, p, N);
+    // The reference's EvaluateImpl calls EvaluateSingle without the nugget
+    // (MonotoneComponent.h:290): T integrates g(df) alone, whereas CoeffGrad,
+    // Gradient and Inverse integrate g(df) + nugget (:434, :721, :794).
+    p.nugget = 0.0;
     p.flags = kFlagEval;
     p.pts = pts.data; p.ptsRs = pts.rowStride; p.ptsCs = pts.colStride;
     p.outEval = output.data; p.evalRs = output.rowStride; p.evalCs = output.colStride;
@@ -995,7 +1008,7 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         Finish(stream, "Inverse");
         return;
     }
-    W.inverseDefer.ensure(sizeof(int), stream);
+    W.inverseDefer.ensure(4 * sizeof(int), stream);
     W.inverseKey.ensure((size_t)N * sizeof(double), stream);
     W.perm.ensure((size_t)N * sizeof(int), stream);
     W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
@@ -1010,6 +1023,10 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         // launch solves them, expensive ones first, one integrand node per
         // lane and loop iteration (inverseQueueKernel).
         W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
+        W.inverseList.ensure((size_t)N * sizeof(int), stream);
+        const int warpBlocks = kWarpPassBlocksPerSM * W.numSMs;
+        W.inverseStack.ensure((size_t)warpBlocks * 4 * kWarpStackCap * sizeof(QEntry), stream);
+        int* counters = W.inverseDefer.as<int>();  // [queue pass, deferred count, warp pass, -]
         for (int c = 0; c < p.nComps; ++c) {
             InverseParams k = p;
             k.compBegin = c;
@@ -1027,10 +1044,23 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
                 MPGB_CUDA(launchSortByLast(key, 1, N, W.sortHist.as<int>(), perm, stream));
                 q.perm = perm;
             }
-            MPGB_CUDA(cudaMemsetAsync(deferCount, 0, sizeof(int), stream));
-            q.queue = deferCount;
+            MPGB_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream));
+            q.queue = counters;
             q.queuePass = 1;
+            q.nodeBudget = kQueueNodeBudget;
+            q.deferList = W.inverseList.as<int>();
+            q.deferCount = counters + 1;
             MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
+            // The deferred points, one warp each.
+            InverseParams wp = q;
+            wp.queuePass = 0;
+            wp.nodeBudget = 0;
+            wp.warpPass = 1;
+            wp.queue = counters + 2;
+            wp.listCount = counters + 1;
+            wp.stack = W.inverseStack.as<QEntry>();
+            wp.stackCap = kWarpStackCap;
+            MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, wp, warpBlocks, stream));
         }
         Finish(stream, "Inverse");
         return;
@@ -1078,6 +1108,18 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
     if (!outLogDet.empty() && outLogDet.rows * outLogDet.cols != N)
         throw std::invalid_argument("FusedForwardAdjoint: out_logdet must hold N values.");
     if (!inputGrad.empty()) checkMatrix(inputGrad, inputDim, N, "input_grad", "FusedForwardAdjoint");
+    // Parts of the call whose integrand carries the nugget (CoeffGrad,
+    // Gradient, the discrete log-determinant, MonotoneComponent.h:622-965).
+    const bool nuggetParts = coeffGrad || !inputGrad.empty() || (!outLogDet.empty() && !opts_.contDeriv);
+    if (opts_.nugget != 0.0 && !outEval.empty() && nuggetParts) {
+        // The values are those of Evaluate, which integrates without the
+        // nugget, and the adjoints those of CoeffGrad / Gradient, which
+        // integrate with it (different quadrature trees): two passes.
+        FusedForwardAdjoint(pts, sens, logdetSens, logdetSensScale, StridedMatrix(), outLogDet, coeffGrad, inputGrad,
+                            stream);
+        EvaluateImpl(pts, outEval, stream);
+        return;
+    }
     Prepare(stream);
     MapWorkspace& W = *ws_;
     const int nComps = (int)parts_.size();
@@ -1105,6 +1147,7 @@ void MonotoneMapBase::FusedForwardAdjoint(StridedMatrix const& pts, StridedMatri
         if (!outEval.empty()) {
             p.flags |= kFlagEval;
             p.outEval = outEval.data; p.evalRs = outEval.rowStride; p.evalCs = outEval.colStride;
+            p.nugget = 0.0;  // (nothing else in this pass integrates with the nugget)
         }
         if (wantLogDet) {
             // Per-component log-dets into scratch rows, summed in component order below.
@@ -1298,6 +1341,25 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     if (onlyComp >= (int)parts_.size()) throw std::out_of_range("KLObjective: component index out of range.");
     Prepare(stream);
     MapWorkspace& W = *ws_;
+    if (opts_.nugget != 0.0) {
+        size_t maxTerms = 1;
+        for (auto& pt : parts_) maxTerms = std::max<size_t>(maxTerms, pt.prog->numTerms);
+        W.klT.ensure((size_t)N * sizeof(double), stream);
+        W.klLd.ensure((size_t)N * sizeof(double), stream);
+        W.klDT.ensure(maxTerms * N * sizeof(double), stream);
+        W.klDL.ensure(maxTerms * N * sizeof(double), stream);
+        KLObjectiveCalls(pts, lossPerComp, grad, onlyComp, W.klT.as<double>(), W.klLd.as<double>(),
+                         W.klDT.as<double>(), W.klDL.as<double>(), stream);
+        if (async_) return;
+        // (the calls went to the components, whose status words hold the flags)
+        int st = 0;
+        for (auto& pt : parts_)
+            if (auto* c = dynamic_cast<MonotoneMapBase*>(pt.owner)) st |= c->CheckStatus(stream);
+        if (st & kStatusInf)
+            throw IntegrandError("KLObjective: MonotoneIntegrand: nan was encountered in value of g(df(...)).");
+        if (st & kStatusBudget) throw std::runtime_error("KLObjective: adaptive quadrature exceeded its interval budget.");
+        return;
+    }
     KLPlan& P = klPlan(W, parts_, N, onlyComp, stream);
     W.partials.ensure(std::max<size_t>(1, P.partialDoubles) * sizeof(double), stream);
     W.lossPart.ensure(std::max(1, P.nItems) * sizeof(double), stream);
@@ -1319,6 +1381,30 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
                              P.nReduce, P.maxTerms, grad, W.lossPart.as<double>(), P.lossSlots.as<int>(),
                              1.0 / (double)N, lossPerComp, stream));
     Finish(stream, "KLObjective");
+}
+
+void MonotoneMapBase::KLObjectiveCalls(StridedMatrix const& pts, double* lossPerComp, double* grad, int onlyComp,
+                                       double* T, double* Ld, double* DT, double* DL, cudaStream_t stream) {
+    const long long n = pts.cols;
+    for (int c = 0; c < (int)parts_.size(); ++c) {
+        if (onlyComp >= 0 && c != onlyComp) continue;
+        const Part& p = parts_[c];
+        auto* comp = dynamic_cast<MonotoneMapBase*>(p.owner);
+        if (!comp || p.owner->numCoeffs != (unsigned)p.prog->numTerms)
+            throw std::invalid_argument("KLObjective: the reference call sequence needs a map of monotone components.");
+        const int nt = p.prog->numTerms;
+        StridedMatrix sl(pts.data, p.prog->D, n, pts.rowStride, pts.colStride);
+        StridedMatrix Tm(T, 1, n, n, 1), Lm(Ld, 1, n, n, 1), DTm(DT, nt, n, n, 1), DLm(DL, nt, n, n, 1);
+        // Asynchronous: the caller checks the status once for all components.
+        const bool wasAsync = comp->Async();
+        comp->SetAsync(true);
+        comp->EvaluateImpl(sl, Tm, stream);
+        comp->LogDeterminantImpl(sl, Lm, stream);
+        comp->CoeffGradImpl(sl, Tm, DTm, stream);
+        comp->LogDeterminantCoeffGradImpl(sl, DLm, stream);
+        comp->SetAsync(wasAsync);
+        MPGB_CUDA(launchDenseKLReduce(T, Ld, DT, DL, nt, n, lossPerComp + p.outRow, grad + p.mapCoeffOffset, stream));
+    }
 }
 
 // Implicit-function adjoint of the inverse.  For the functional

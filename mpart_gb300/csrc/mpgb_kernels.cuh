@@ -1259,6 +1259,7 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
     double xd = 0.0, lo = 0.0, hi = 1.0, hA = 0.0, hB = 0.0, hM = 0.0, ic = 0.0, ih = 0.0, Ih = 0.0;
     int level = 0, sp = 0, j = 0, qst = 0, stAll = 0;
     long long nInt = 0;
+    int nodes = 0;  // integrand nodes of the current point's solve
     double stX[kMaxSubCap], stH[kMaxSubCap];
     int stL[kMaxSubCap];
     auto startQuad = [&](double xq) {
@@ -1318,6 +1319,7 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
                         G0 = V0.h;
                         rs.start(x0);
                         startQuad(x0);
+                        nodes = 0;
                         have = true;
                     }
                 } else {
@@ -1342,6 +1344,14 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         NodeVal<PMAX, false, 0> V;
         evalNode<BASIS, POS, PMAX, false, 0>(t, xd, as, P, prm.bc, nugget, V, qst);
         const double h = V.h;
+        if (prm.nodeBudget > 0 && ++nodes > prm.nodeBudget) {
+            // An expensive solve (far root, wide quadratures): the warp pass
+            // solves it again from the start with 32 lanes per quadrature.
+            prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
+            have = false;
+            need = true;
+            continue;
+        }
         bool qdone = false;
         double T = 0.0;
         if (fixed) {
@@ -1424,6 +1434,218 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         }
     }
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
+}
+
+// Inverse of the points the queue pass left over (deferList), one warp per
+// point.  The solver state is the same in every lane; each quadrature of T
+// is shared by the 32 lanes: the pending intervals live on a per-warp stack
+// in global scratch (prm.stack, the leftmost on top), each round the lanes
+// take the top min(32, depth) entries, evaluate one interval each (its
+// midpoint, other coarse nodes and fine-only nodes, as `integrate`) and
+// replace it by its two halves or by an accepted marker; accepted markers
+// that reach the top are added to the integral in order.  The intervals,
+// their values, the accept tests and the order of the sum of accepted fine
+// values are those of the depth-first `integrate`, so T -- and every solver
+// iterate -- is bitwise the same as in one lane.  Near the stack's capacity
+// the rounds take one interval (a depth-first walk needs at most maxSub more
+// entries).
+template <int BASIS, int POS, int PMAX>
+__global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__ InverseParams prm) {
+    __shared__ double sOff[kMaxRulePts], sCw[kMaxRulePts], sFw[kMaxRulePts];
+    __shared__ int sIsC[kMaxRulePts];
+    __shared__ int sPer;
+    const QuadParams& Q = prm.quad;
+    const bool fixed = Q.kind == kQuadFixedCC;
+    const int cR = Q.nCoarse - 1, cM = cR / 2, fR = Q.nFine - 1, fM = fR / 2;
+    if (threadIdx.x == 0) {
+        int j = 1;
+        for (int i = 1; i < cR; ++i) {
+            if (i == cM) continue;
+            sOff[j] = Q.cPts[i]; sCw[j] = Q.cWts[i]; sFw[j] = Q.fWts[2 * i]; sIsC[j] = 1;
+            ++j;
+        }
+        for (int i = 1; i < Q.nFine; i += 2) {
+            sOff[j] = Q.fPts[i]; sCw[j] = 0.0; sFw[j] = Q.fWts[i]; sIsC[j] = 0;
+            ++j;
+        }
+        sPer = j;
+    }
+    __syncthreads();
+    const int nPer = sPer;
+    const int comp = prm.compBegin;
+    const CompDesc& c = prm.comps[comp];
+    const int D = c.D, P = c.P;
+    const long long N = prm.N;
+    const int lane = threadIdx.x & 31;
+    const unsigned kFull = 0xffffffffu;
+    const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+    const double nugget = prm.nugget;
+    const int cap = prm.stackCap;
+    QEntry* stk = prm.stack + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * cap;
+    const int listN = *prm.listCount;
+    int stAll = 0;
+
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(prm.queue, 1);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= listN) break;
+        const long long i = prm.deferList[k];
+        // The point (the same in every lane).
+        const long long xi = (prm.x1Cols == 1) ? 0 : i;
+        double x0 = 0.0;
+        for (int d = 0; d < D; ++d) {
+            double v = 0.0;
+            if (d < prm.x1Rows) v = prm.x1[d * prm.x1Rs + xi * prm.x1Cs];
+            else if (d - prm.extra < comp) v = prm.out[(long long)(d - prm.extra) * prm.outRs + i * prm.outCs];
+            x0 = v;
+        }
+        const double yd = prm.r[(long long)comp * prm.rRs + i * prm.rCs];
+        ACoef<PMAX> A;
+        double f0 = 0.0;
+#pragma unroll
+        for (int kk = 0; kk <= PMAX; ++kk) {
+            A.a[kk] = prm.acoef[(long long)kk * N + i];
+            f0 = fma(A.a[kk], prm.bc.v0[kk], f0);
+        }
+        double as[PMAX + 1];
+        scaleCoeffs<BASIS, PMAX>(A.a, P, prm.bc, as);
+        double G0;
+        {
+            NodeVal<PMAX, false, 0> V0;
+            int s0 = 0;
+            evalNode<BASIS, POS, PMAX, false, 0>(0.0, 1.0, as, P, prm.bc, nugget, V0, s0);
+            G0 = V0.h;
+        }
+        int dummy = 0;
+        const InverseEval<BASIS, POS, PMAX> f{A, P, f0, &prm.quad, &prm.bc, nugget, &dummy};
+        RootSolve rs;
+        rs.start(x0);
+        while (rs.phase != RootSolve::kDone) {
+            const double xd = rs.x;
+            // T(x) - f0: the quadrature of x (g(df(t x)) + nugget) over t in [0, 1].
+            int qst = 0;
+            double Ih = 0.0;  // (lane 0)
+            bool failed = false;
+            if (fixed) {
+                // one fixed rule: lane 0 alone
+                if (lane == 0) {
+                    for (int jn = 0; jn < Q.nFine; ++jn) {
+                        NodeVal<PMAX, false, 0> V;
+                        evalNode<BASIS, POS, PMAX, false, 0>(0.5 * (1.0 + Q.fPts[jn]), xd, as, P, prm.bc, nugget, V,
+                                                             qst);
+                        Ih = fma(0.5 * Q.fWts[jn], V.h, Ih);
+                    }
+                }
+                qst = __shfl_sync(kFull, qst, 0);
+                failed = (qst & (kStatusInf | kStatusNaN)) != 0;
+            } else {
+                const double hA0 = xd * G0;
+                if (isinf(G0)) qst |= kStatusInf;
+                else if (isnan(hA0)) qst |= kStatusNaN;
+                NodeVal<PMAX, false, 0> VB;
+                evalNode<BASIS, POS, PMAX, false, 0>(1.0, xd, as, P, prm.bc, nugget, VB, qst);
+                failed = (qst & (kStatusInf | kStatusNaN)) != 0;
+                int sp = 0;
+                if (!failed) {
+                    if (lane == 0) stk[0] = QEntry{0.0, hA0, VB.h, 0, 0};
+                    sp = 1;
+                    __syncwarp();
+                }
+                long long processed = 0;
+                while (sp > 0) {
+                    int m = min(32, sp);
+                    if (sp + m > cap - kMaxSubCap - 2) m = 1;
+                    const bool has = lane < m;
+                    QEntry e{0.0, 0.0, 0.0, 0, 1};
+                    if (has) e = stk[sp - 1 - lane];
+                    __syncwarp();
+                    const bool pend = has && !e.done;
+                    double ic = 0.0, ih = 0.0, hM = 0.0, mm = 0.0;
+                    int lst = 0;
+                    bool accept = false;
+                    if (pend) {
+                        const double lo = e.lo, hi = e.lo + ldexp(1.0, -e.level);
+                        mm = 0.5 * (lo + hi);
+                        const double s = 0.5 * (hi - lo);
+                        NodeVal<PMAX, false, 0> V;
+                        evalNode<BASIS, POS, PMAX, false, 0>(mm, xd, as, P, prm.bc, nugget, V, lst);
+                        hM = V.h;
+                        ic = (s * Q.cWts[0]) * e.hA;
+                        ic = fma(s * Q.cWts[cM], hM, ic);
+                        ic = fma(s * Q.cWts[cR], e.hB, ic);
+                        const double w0 = s * Q.fWts[0], wM = s * Q.fWts[fM], wR = s * Q.fWts[fR];
+                        ih = w0 * e.hA;
+                        ih = fma(wM, hM, ih);
+                        ih = fma(wR, e.hB, ih);
+                        for (int jn = 1; jn < nPer; ++jn) {
+                            evalNode<BASIS, POS, PMAX, false, 0>(mm + s * sOff[jn], xd, as, P, prm.bc, nugget, V, lst);
+                            if (sIsC[jn]) ic = fma(s * sCw[jn], V.h, ic);
+                            ih = fma(s * sFw[jn], V.h, ih);
+                        }
+                        const double err = fabs(ih - ic);
+                        const double tol = fmax(Q.relTol * fabs(ic), Q.absTol);
+                        accept = ((err < tol) || (e.level == Q.maxSub - 1)) && (e.level >= Q.minSub);
+                    }
+                    qst |= __reduce_or_sync(kFull, lst);
+                    if (qst & (kStatusInf | kStatusNaN)) {
+                        failed = true;
+                        break;
+                    }
+                    processed += __popc(__ballot_sync(kFull, pend));
+                    if (processed > Q.maxIntervals) {
+                        qst |= kStatusBudget;
+                        failed = true;
+                        break;
+                    }
+                    // New entries, the leftmost on top: lane j's outputs lie
+                    // below those of the lanes left of it.
+                    const int nout = !has ? 0 : ((pend && !accept) ? 2 : 1);
+                    int incl = nout;  // sum over lanes >= this one
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const int v = __shfl_down_sync(kFull, incl, off);
+                        if (lane + off < 32) incl += v;
+                    }
+                    const int total = __shfl_sync(kFull, incl, 0);
+                    const int base = sp - m + (incl - nout);
+                    if (has) {
+                        if (!pend) {
+                            stk[base] = e;
+                        } else if (accept) {
+                            stk[base] = QEntry{e.lo, ih, 0.0, e.level, 1};
+                        } else {
+                            stk[base] = QEntry{mm, hM, e.hB, e.level + 1, 0};         // right half
+                            stk[base + 1] = QEntry{e.lo, e.hA, hM, e.level + 1, 0};  // left half (on top)
+                        }
+                    }
+                    sp = sp - m + total;
+                    __syncwarp();
+                    // Accepted intervals that reach the top, in order.
+                    if (lane == 0) {
+                        while (sp > 0) {
+                            const QEntry t = stk[sp - 1];
+                            if (!t.done) break;
+                            Ih += t.hA;
+                            --sp;
+                        }
+                    }
+                    sp = __shfl_sync(kFull, sp, 0);
+                    __syncwarp();
+                }
+            }
+            stAll |= qst;
+            double T = __shfl_sync(kFull, Ih, 0);
+            if (failed) T = nan;
+            rs.step_(T + f0, yd, f, prm.xtol, prm.ytol, kBracketIts, prm.method);
+        }
+        if (lane == 0) {
+            prm.out[(long long)comp * prm.outRs + i * prm.outCs] = rs.result;
+            if (prm.info) prm.info[(long long)comp * prm.infoStride + i] = rs.info;
+            if (rs.info < 0) stAll |= kStatusNoBracket;
+        }
+    }
+    if (lane == 0 && prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }
 
 // Key pass of the Inverse for component compBegin (monotone components):
@@ -1527,6 +1749,22 @@ cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t s
         if constexpr (BASIS == kBasisSigmoid) return cudaErrorInvalidValue;
         else kern = inverseKeyKernel<BASIS, POS, PMAX>;
     }
+    if (prm.warpPass) {
+        // Persistent: nBlocks blocks of four warps (the host sized the stack
+        // scratch for them).
+        if constexpr (BASIS == kBasisSigmoid) {
+            return cudaErrorInvalidValue;
+        } else {
+            if (!prm.queue || !prm.acoef || !prm.stack || !prm.listCount || !prm.deferList ||
+                prm.stackCap < 4 * kMaxSubCap)
+                return cudaErrorInvalidValue;
+            kern = inverseWarpKernel<BASIS, POS, PMAX>;
+            kern<<<nBlocks, 128, 0, stream>>>(prm);
+            cudaError_t e = cudaGetLastError();
+            countLaunches(stream, 1);
+            return e;
+        }
+    }
     if (prm.queuePass) {
         // Persistent: as many 128-thread blocks as are resident at once (at
         // most one per 128 points).
@@ -1534,6 +1772,7 @@ cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t s
             return cudaErrorInvalidValue;
         } else {
             if (prm.tpb != 128 || !prm.queue || !prm.acoef) return cudaErrorInvalidValue;
+            if (prm.nodeBudget > 0 && (!prm.deferList || !prm.deferCount)) return cudaErrorInvalidValue;
             kern = inverseQueueKernel<BASIS, POS, PMAX>;
             int perSM = 0, dev = 0, nSM = 0;
             cudaError_t e;

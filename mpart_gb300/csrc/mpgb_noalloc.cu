@@ -233,7 +233,11 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         p.tpb = kTpbNA;
         p.pts = pts.data; p.ptsRs = pts.row_stride; p.ptsCs = pts.col_stride;
         p.flags = 0;
-        if (outEval.data) {
+        // Evaluate integrates without the nugget, the coefficient adjoint with
+        // it (MonotoneComponent.h:290, :721): with a nonzero nugget and both
+        // asked for, the values come from a second launch.
+        const bool valuesApart = o.nugget != 0.0 && outEval.data && coeffGrad;
+        if (outEval.data && !valuesApart) {
             p.flags |= kFlagEval;
             p.outEval = outEval.data; p.evalRs = outEval.row_stride; p.evalCs = outEval.col_stride;
         }
@@ -253,14 +257,21 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
             needJ = sens.data ? 1 : 0;
         }
         p.statusWord = dStatus;
-        p.nugget = o.nugget;
+        p.nugget = coeffGrad ? o.nugget : 0.0;
         p.dmax = dmax; p.nBmax = nBmax; p.depthMax = depthMax;
         buildLaunchConstants(o, p.quad, p.bc);
         const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, pmax, false);
         if (smem > 227 * 1024) throw std::invalid_argument("component too large for the shared-memory tile");
         const int basis = o.basisType == BasisTypes::HermiteFunctions ? kBasisHermiteFunctions : kBasisProbHermite;
         const int pos = o.posFuncType == PosFuncTypes::Exp ? kPosExp : kPosSoftPlus;
-        MPGB_CUDA(launchFused(basis, pos, pmax, p, (int)items.size(), needJ, 0, stream));
+        if (p.flags) MPGB_CUDA(launchFused(basis, pos, pmax, p, (int)items.size(), needJ, 0, stream));
+        if (valuesApart) {
+            FusedParams q = p;
+            q.flags = kFlagEval;
+            q.outEval = outEval.data; q.evalRs = outEval.row_stride; q.evalCs = outEval.col_stride;
+            q.nugget = 0.0;
+            MPGB_CUDA(launchFused(basis, pos, pmax, q, (int)items.size(), 0, 0, stream));
+        }
         if (coeffGrad) {
             const long long* rows = (const long long*)(base + oRows);
             for (int c = 0; c < nComps; ++c)

@@ -136,7 +136,9 @@ __device__ void integrand(const PlainComp& c, double* cache, double xd, bool par
         const double sc = xd * posGp(c.pos, df);
         for (int k = 0; k < c.T; ++k) out[1 + k] *= sc;
     }
-    out[0] = xd * (posG(c.pos, df) + c.nugget);
+    // (The value-only use is Evaluate, which integrates without the nugget,
+    // MonotoneComponent.h:290; CoeffGrad integrates with it, :721.)
+    out[0] = xd * (posG(c.pos, df) + (params ? c.nugget : 0.0));
 }
 
 // AdaptiveClenshawCurtis::Integrate with the reference's workspace layout.

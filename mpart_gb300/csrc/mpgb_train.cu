@@ -260,25 +260,9 @@ struct KLStep {
     void enqueue() {
         TR_CUDA(cudaMemcpyAsync(dCoef, hCoef.p, nc * sizeof(double), cudaMemcpyHostToDevice, s));
         if (mode == 3) {
-            const long long n = pts.cols;
-            for (auto& p : map.Parts()) {
-                auto* comp = dynamic_cast<MonotoneMapBase*>(p.owner);
-                const int nt = p.prog->numTerms;
-                StridedMatrix sl(pts.data, p.prog->D, n, pts.rowStride, pts.colStride);
-                StridedMatrix T(dT->p, 1, n, n, 1), Ld(dLd->p, 1, n, n, 1);
-                StridedMatrix DT(dDenseT->p, nt, n, n, 1), DL(dDenseL->p, nt, n, n, 1);
-                // Asynchronous like the batched modes: an overflowing trial
-                // shows as a non-finite objective; run() clears the status.
-                const bool wasAsync = comp->Async();
-                comp->SetAsync(true);
-                comp->EvaluateImpl(sl, T, s);
-                comp->LogDeterminantImpl(sl, Ld, s);
-                comp->CoeffGradImpl(sl, T, DT, s);
-                comp->LogDeterminantCoeffGradImpl(sl, DL, s);
-                comp->SetAsync(wasAsync);
-                TR_CUDA(launchDenseKLReduce(dT->p, dLd->p, dDenseT->p, dDenseL->p, nt, n, dLoss.p + p.outRow,
-                                            dGrad.p + p.mapCoeffOffset, s));
-            }
+            // (an overflowing trial shows as a non-finite objective; run()
+            // clears the status)
+            map.KLObjectiveCalls(pts, dLoss.p, dGrad.p, -1, dT->p, dLd->p, dDenseT->p, dDenseL->p, s);
         } else if (mode == 2) {
             for (unsigned c = 0; c < map.NumMonotoneComponents(); ++c) map.KLObjective(pts, dLoss.p, dGrad.p, (int)c, s);
         } else {

@@ -131,6 +131,14 @@ struct FusedParams {
     BasisConsts bc;
 };
 
+// An interval of the warp-shared adaptive quadrature (inverseWarpKernel):
+// [lo, lo + 2^-level] with the integrand at its ends, or (done = 1) an
+// accepted interval waiting to be summed, its fine-rule value in hA.
+struct QEntry {
+    double lo, hA, hB;
+    int level, done;
+};
+
 struct InverseParams {
     const CompDesc* comps;
     int nComps;
@@ -177,7 +185,17 @@ struct InverseParams {
     // each with the full bracket budget; a_k come from acoef.
     int* queue;
     int queuePass;
-    int pad4_;
+    // Queue pass: a point whose solve takes more than nodeBudget integrand
+    // nodes is left to the warp pass: its index goes to
+    // deferList[atomicAdd(deferCount, 1)] (nodeBudget 0: no limit).
+    int nodeBudget;
+    int* deferList;
+    // Warp pass (warpPass = 1): one warp per point of deferList (*listCount
+    // of them, taken through *queue), the lanes sharing each adaptive
+    // quadrature; stack: stackCap entries of scratch per warp of the grid.
+    QEntry* stack;
+    int stackCap;
+    int warpPass;
     QuadParams quad;
     BasisConsts bc;
 };

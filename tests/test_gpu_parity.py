@@ -647,3 +647,43 @@ def test_discrete_derivative_matches_oracle(gpu, oracle, basis, pos, quad):
     # as in the reference (MonotoneComponent.h:216-222)
     with pytest.raises(ValueError, match="Discrete derivative"):
         tm.LogDeterminantInputGrad(xs)
+
+
+def test_nugget_semantics_match_reference(gpu, oracle):
+    """With a nonzero nugget the reference's Evaluate integrates g(df) alone
+    (EvaluateImpl calls EvaluateSingle without it, MonotoneComponent.h:290)
+    while CoeffGrad, Gradient and Inverse integrate g(df) + nugget (:434,
+    :721, :794); the fused call, the KL objective and the batch give each
+    output the meaning of its reference call (tests/test_reference_pins.py
+    pins the oracle to the reference on this)."""
+    import torch
+    M, O = gpu, oracle
+    o = M.MapOptions(quadType=M.QuadTypes.AdaptiveClenshawCurtis, nugget=0.3)
+    tm = M.CreateTriangular(2, 2, 3, o)
+    om = O.OracleTriangularMap(2, 2, 3, nugget=0.3)
+    coef = np.random.default_rng(0).normal(0.0, 0.1, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    x = np.random.default_rng(1).standard_normal((2, 3000))
+    sens = np.random.default_rng(2).standard_normal((2, 3000))
+    assert_parity(H(tm.Evaluate(T(x))), om.evaluate(coef, x), what="Evaluate")
+    assert_parity(H(tm.LogDeterminant(T(x))), om.logdet(coef, x), what="LogDeterminant")
+    assert_parity(H(tm.CoeffGrad(T(x), T(sens))), om.coeff_grad(coef, x, sens), what="CoeffGrad")
+    assert_parity(H(tm.Gradient(T(x), T(sens))), om.gradient(coef, x, sens), what="Gradient")
+    r = om.evaluate(coef, x)
+    xi = H(tm.Inverse(T(np.zeros((0, 3000))), T(r), xtol=1e-10, ytol=1e-10))
+    assert_inverse_parity(om, coef, np.zeros((0, 3000)), r, xi, 1e-10, 1e-10)
+    assert np.abs(xi - x).max() > 1e-3  # the inverse solves T + nugget x = r
+    # fused call: values as Evaluate, gradient as CoeffGrad + LogDeterminantCoeffGrad
+    ev = torch.zeros(2, 3000, dtype=torch.float64, device="cuda")
+    cg = torch.zeros(tm.numCoeffs, dtype=torch.float64, device="cuda")
+    tm.FusedForwardAdjointImpl(T(x), sens=T(sens), logdet_sens_scale=1.0, out_eval=ev, coeff_grad=cg)
+    assert_parity(H(ev), om.evaluate(coef, x), what="fused values")
+    ref_cg = om.coeff_grad(coef, x, sens).sum(axis=1) + om.logdet_coeff_grad(coef, x).sum(axis=1)
+    assert_parity(H(cg), ref_cg, floor=1e-3, what="fused coefficient gradient")
+    # KL objective (FastGaussianReverseKL per component)
+    loss, grad = tm.KLObjective(T(x))
+    cs = om.split(coef)
+    for i, c in enumerate(om.comps):
+        l, g = O.fast_gaussian_reverse_kl(c, cs[i], np.ascontiguousarray(x[:c.input_dim]))
+        assert_parity(H(loss)[i:i + 1], [l], what=f"KL loss {i}")
+        assert_parity(H(grad)[om.offsets[i]:om.offsets[i + 1]], g, floor=1e-3, what=f"KL grad {i}")
