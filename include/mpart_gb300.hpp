@@ -239,6 +239,9 @@ public:
     // Process points grouped by |x_D| (default on); results do not depend on it
     // beyond summation order.
     void SetPointOrdering(bool on);
+    // The next KLObjective call orders the samples by |x_D| again (later
+    // calls order them by the interval counts of the call before).
+    void ResetKLOrder();
     // Grow-only device buffer `slot` (0..7) of at least `bytes`, for host staging.
     double* StagingBuffer(int slot, size_t bytes, cudaStream_t stream);
     MapOptions const& Options() const { return opts_; }

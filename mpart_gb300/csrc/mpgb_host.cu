@@ -302,6 +302,13 @@ struct KLPlan {
     DevBuf perm;
     const double* permPts = nullptr;
     long long permRs = 0, permCs = 0;
+    // Each call records every sample's quadrature interval count per
+    // component (costKey) and sorts by it, so the next call -- the next step
+    // of a training run, at nearby coefficients -- groups samples of similar
+    // cost in a warp; the first call sorts by |x_D|.  The order depends only
+    // on the samples and the coefficient history, so launch modes at the same
+    // history process the samples in the same order (bitwise-equal results).
+    DevBuf costKey;
     long long rcTotal = 0;  // rectifier cache of sigmoid expansions (doubles)
 };
 
@@ -646,6 +653,10 @@ void MonotoneMapBase::Finish(cudaStream_t stream, const char* fn) {
 
 void MonotoneMapBase::SetPointOrdering(bool on) { ws_->ordering = on; }
 
+void MonotoneMapBase::ResetKLOrder() {
+    for (auto& p : ws_->klPlans) p->permPts = nullptr;
+}
+
 double* MonotoneMapBase::StagingBuffer(int slot, size_t bytes, cudaStream_t stream) {
     if (slot < 0 || slot >= 8) throw std::invalid_argument("StagingBuffer: slot out of range.");
     ws_->stage[slot].ensure(bytes, stream);
@@ -675,9 +686,21 @@ constexpr int kTpb = 128;
 // second pass.
 constexpr int kFirstPassBracketIts = 3;
 // Inverse of monotone components: integrand nodes a point may take in the
-// queue pass before the warp pass takes it over, and the warp pass's grid
+// queue pass, and the width (intervals) of one of its quadratures, before the
+// warp pass takes it over; the warp pass's grid
 // (blocks of four warps per SM) and per-warp interval stack.
-constexpr int kQueueNodeBudget = 3072;
+constexpr int kQueueNodeBudget = 16384;
+// The width threshold balances the queue pass's tail (a few long serial
+// solves, which dominate with few targets) against the warp pass's cost (a
+// deferred point starts again, and narrow quadratures leave lanes idle),
+// which weighs more with many: 48 intervals at 100k targets, growing as
+// sqrt(N), at most 160 (measured on the 16-D inverse workload: ITP at 4M
+// targets 11.9 s with 48, 9.4 s with 160; at 100k targets 0.52 s with 48,
+// 0.79 s with 96).
+inline int queueWideQuad(long long N) {
+    const double w = 48.0 * std::sqrt((double)N / 1e5);
+    return (int)std::min(160.0, std::max(48.0, w));
+}
 constexpr int kWarpPassBlocksPerSM = 2;
 constexpr int kWarpStackCap = 2048;
 
@@ -1048,6 +1071,7 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
             q.queue = counters;
             q.queuePass = 1;
             q.nodeBudget = kQueueNodeBudget;
+            q.wideQuad = queueWideQuad(N);
             q.deferList = W.inverseList.as<int>();
             q.deferCount = counters + 1;
             MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
@@ -1374,12 +1398,26 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     p.items = P.items.as<WorkItem>();
     p.rcache = rectCache(W, P.rcTotal, stream);
     orderPointsKL(W, P, parts_, pts, p, onlyComp, stream);
+    const bool costOrder = p.perm != nullptr;
+    if (costOrder) {
+        P.costKey.ensure(parts_.size() * (size_t)N * sizeof(double), stream);
+        p.costKey = P.costKey.as<double>();
+        p.costStride = N;
+    }
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
     MPGB_CUDA(launchFused(W.basis, posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
     MPGB_CUDA(launchKLReduce(W.partials.as<double>(), P.rowBase.as<long long>(), P.reduceDesc.as<KLReduceDesc>(),
                              P.nReduce, P.maxTerms, grad, W.lossPart.as<double>(), P.lossSlots.as<int>(),
                              1.0 / (double)N, lossPerComp, stream));
+    if (costOrder) {
+        // the processing order of the next call
+        for (size_t c = 0; c < parts_.size(); ++c) {
+            if (onlyComp >= 0 && (int)c != onlyComp) continue;
+            MPGB_CUDA(launchSortByLast(P.costKey.as<double>() + c * (size_t)N, 1, N, W.sortHist.as<int>(),
+                                       P.perm.as<int>() + c * (size_t)N, stream));
+        }
+    }
     Finish(stream, "KLObjective");
 }
 

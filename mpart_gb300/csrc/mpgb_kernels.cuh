@@ -148,6 +148,7 @@ struct QuadOut {
     double J[NEEDJ ? PMAX : 1];
     double IE;
     double K[NEEDE == 2 ? PMAX : 1];
+    int nInt;  // intervals the quadrature visited (its cost)
 };
 
 // Per-order constants cs_k of the basis derivatives (see scaleCoeffs).
@@ -177,6 +178,7 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
 
     R.Ih = 0.0;
     R.IE = 0.0;
+    R.nInt = 1;
 #pragma unroll
     for (int k = 0; k < NJ; ++k) R.J[k] = 0.0;
 #pragma unroll
@@ -287,7 +289,10 @@ __device__ __forceinline__ void integrate(const double* a, int P, double xd, con
 #pragma unroll
                 for (int k = 0; k < NK; ++k) R.K[k] += iK[k];
             }
-            if (sp == 0) break;
+            if (sp == 0) {
+                R.nInt = (nIntervals + 1 > 0x7fffffffLL) ? 0x7fffffff : (int)(nIntervals + 1);
+                break;
+            }
             --sp;
             lo = hi;
             A = B;
@@ -564,7 +569,11 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
                 // its log-determinant is that of the quadrature approximation.)
                 const bool needT = (flags & (kFlagEval | kFlagCoefDenseT | kFlagKL)) != 0 ||
                                    (NEEDJ && (flags & (kFlagCoefReduced | kFlagInput))) || NEEDE == 2;
-                if (needT && active) integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
+                if (needT && active) {
+                    integrate<BASIS, POS, PMAX, NEEDJ, NEEDE>(a, P, xd, prm.quad, prm.bc, prm.nugget, R, st);
+                    // the point's cost in this component, a sort key for the next call
+                    if (!BATCH && prm.costKey) prm.costKey[(long long)ci * prm.costStride + i] = 0.125 * R.nInt;
+                }
                 T = R.Ih + f0;
                 // dT/dx_D: g(df(x)) (ContinuousDerivative) or the x_D-derivative of
                 // the quadrature approximation (DiscreteDerivative, MonotoneComponent.h:585-638).
@@ -1344,9 +1353,11 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         NodeVal<PMAX, false, 0> V;
         evalNode<BASIS, POS, PMAX, false, 0>(t, xd, as, P, prm.bc, nugget, V, qst);
         const double h = V.h;
-        if (prm.nodeBudget > 0 && ++nodes > prm.nodeBudget) {
-            // An expensive solve (far root, wide quadratures): the warp pass
-            // solves it again from the start with 32 lanes per quadrature.
+        // An expensive solve -- a quadrature wider than wideQuad intervals
+        // (a far iterate) or a solve longer than nodeBudget nodes -- is left
+        // to the warp pass, which solves it again from the start with 32
+        // lanes per quadrature.
+        if (prm.nodeBudget > 0 && (++nodes > prm.nodeBudget || nInt >= prm.wideQuad)) {
             prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
             have = false;
             need = true;

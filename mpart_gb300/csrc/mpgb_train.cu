@@ -208,6 +208,10 @@ struct KLStep {
           hGrad(m.numCoeffs), dLoss(m.outputDim), dGrad(m.numCoeffs), nc(m.numCoeffs), no(m.outputDim) {
         TR_CUDA(cudaStreamSynchronize(user));
         TR_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        // Every run starts from the |x_D| order of the samples, whatever
+        // earlier calls left, so that runs in different launch modes process
+        // the samples in the same orders (bitwise-equal trajectories).
+        map.ResetKLOrder();
         // Every step uploads hCoef: start from the map's current coefficients.
         TR_CUDA(cudaMemcpy(hCoef.p, dCoef, nc * sizeof(double), cudaMemcpyDefault));
         if (mode == 3) {

@@ -124,6 +124,10 @@ struct FusedParams {
     // the reduction, nCNodes x blockDim doubles per item at WorkItem::rcBase
     // (null: the reduction evaluates the rectifier again).
     double* rcache;
+    // Optional: per point and component, the quadrature's interval count / 8
+    // at costKey[c * costStride + i] (a sort key: the next call processes the
+    // points in order of it).
+    double* costKey; long long costStride;
     double nugget;
     int dmax, nBmax, depthMax;
     int negRows;            // kFlagImplicit: rows [0, negRows) of outInput are negated when written
@@ -186,9 +190,11 @@ struct InverseParams {
     int* queue;
     int queuePass;
     // Queue pass: a point whose solve takes more than nodeBudget integrand
-    // nodes is left to the warp pass: its index goes to
-    // deferList[atomicAdd(deferCount, 1)] (nodeBudget 0: no limit).
+    // nodes, or one of whose quadratures reaches wideQuad intervals, is left
+    // to the warp pass: its index goes to deferList[atomicAdd(deferCount, 1)]
+    // (nodeBudget 0: no limit).
     int nodeBudget;
+    int wideQuad;
     int* deferList;
     // Warp pass (warpPass = 1): one warp per point of deferList (*listCount
     // of them, taken through *queue), the lanes sharing each adaptive
