@@ -1,0 +1,171 @@
+// A C++ consumer of the library's boundary, compiled by g++ against the
+// installed headers and libmpart_gb300.so (tests/test_cpp_consumer.py):
+//
+//  * route 1, the C++ API of include/mpart_gb300.hpp, as MParT host code uses
+//    its own classes: MapFactory::CreateTriangular, SetCoeffs and the
+//    EvaluateImpl / LogDeterminantImpl / CoeffGradImpl / InverseImpl methods
+//    (MParT/MapFactory.h, MParT/ConditionalMapBase.h);
+//  * route 2, an adapter of the shape INTEGRATION.md shows for MParT's
+//    ConditionalMapBase<DeviceSpace>: it keeps an mpgb_map* and forwards
+//    each *Impl method to the C ABI of include/mpart_gb300.h.  DView stands
+//    in for the reference's StridedMatrix / StridedVector device views; the
+//    adapter uses only their data(), extent() and stride_0/1() members.
+//
+// Usage: cpp_consumer <in.bin> <out.bin>
+//   in.bin : int64 N, then 14 coefficients, x (2 x N), sens (2 x N) and
+//            r (2 x N, targets), row-major float64
+//   out.bin: per route, T (2 x N), log-det (N), CoeffGrad (14 x N) and
+//            Inverse(r) (2 x N)
+// The map is the 2 x 2 TriangularMap of total order 3, ProbabilistHermite +
+// SoftPlus, AdaptiveClenshawCurtis with tolerances 1e-6.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <stdexcept>
+#include <vector>
+
+#include "mpart_gb300.h"
+#include "mpart_gb300.hpp"
+
+namespace {
+
+void cuda(cudaError_t e) {
+    if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+}
+
+struct Dev {
+    double* p = nullptr;
+    size_t n = 0;
+    explicit Dev(size_t count) : n(count) { cuda(cudaMalloc(&p, std::max<size_t>(1, n) * sizeof(double))); }
+    Dev(const std::vector<double>& h) : Dev(h.size()) {
+        cuda(cudaMemcpy(p, h.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    ~Dev() { cudaFree(p); }
+    std::vector<double> host() const {
+        std::vector<double> h(n);
+        cuda(cudaMemcpy(h.data(), p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return h;
+    }
+};
+
+// Stand-in for a Kokkos LayoutStride device view.
+struct DView {
+    double* p;
+    int64_t e0, e1, s0, s1;
+    double* data() const { return p; }
+    int64_t extent(int i) const { return i == 0 ? e0 : e1; }
+    int64_t stride_0() const { return s0; }
+    int64_t stride_1() const { return s1; }
+};
+
+// The adapter of INTEGRATION.md (section 1), over the C ABI.
+class GB300Map {
+    mpgb_map* h_ = nullptr;
+    static mpgb_matrix M(DView const& v) { return {v.data(), v.extent(0), v.extent(1), v.stride_0(), v.stride_1()}; }
+    static void ok(int rc) {
+        if (rc == MPGB_ERR_INVALID_ARGUMENT) throw std::invalid_argument(mpgb_last_error());
+        if (rc != MPGB_OK) throw std::runtime_error(mpgb_last_error());
+    }
+
+public:
+    GB300Map(unsigned in, unsigned out, unsigned order, mpgb::MapOptions const& o) {
+        mpgb_map_options c;
+        ok(mpgb_map_options_default(&c));
+        c.basis_type = (int)o.basisType;
+        c.pos_func_type = (int)o.posFuncType;
+        c.quad_type = (int)o.quadType;
+        c.quad_abs_tol = o.quadAbsTol;
+        c.quad_rel_tol = o.quadRelTol;
+        c.quad_max_sub = o.quadMaxSub;
+        c.quad_min_sub = o.quadMinSub;
+        c.quad_pts = o.quadPts;
+        c.basis_norm = o.basisNorm;
+        c.nugget = o.nugget;
+        ok(mpgb_create_triangular(in, out, order, &c, &h_));
+    }
+    ~GB300Map() { mpgb_map_destroy(h_); }
+    void SetCoeffs(DView const& c) { ok(mpgb_set_coeffs(h_, c.data(), (unsigned)c.extent(0), 0, nullptr)); }
+    void EvaluateImpl(DView const& pts, DView const& out) { ok(mpgb_evaluate(h_, M(pts), M(out), nullptr)); }
+    void LogDeterminantImpl(DView const& pts, DView const& out) {
+        mpgb_matrix o{out.data(), 1, out.extent(0), out.extent(0), out.stride_0()};
+        ok(mpgb_log_determinant(h_, M(pts), o, nullptr));
+    }
+    void CoeffGradImpl(DView const& pts, DView const& sens, DView const& out) {
+        ok(mpgb_coeff_grad(h_, M(pts), M(sens), M(out), nullptr));
+    }
+    void InverseImpl(DView const& x1, DView const& r, DView const& out) {
+        ok(mpgb_inverse(h_, M(x1), M(r), M(out), 1e-6, 1e-6, nullptr, nullptr));
+    }
+};
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc != 3) {
+        std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);
+        return 2;
+    }
+    try {
+        FILE* f = std::fopen(argv[1], "rb");
+        if (!f) throw std::runtime_error("cannot open input");
+        int64_t N = 0;
+        if (std::fread(&N, sizeof N, 1, f) != 1) throw std::runtime_error("bad input");
+        const int nc = 14;
+        std::vector<double> coef(nc), x(2 * N), sens(2 * N), r(2 * N);
+        bool good = std::fread(coef.data(), 8, nc, f) == (size_t)nc && std::fread(x.data(), 8, 2 * N, f) == (size_t)(2 * N) &&
+                    std::fread(sens.data(), 8, 2 * N, f) == (size_t)(2 * N) && std::fread(r.data(), 8, 2 * N, f) == (size_t)(2 * N);
+        std::fclose(f);
+        if (!good) throw std::runtime_error("short input");
+
+        mpgb::MapOptions o;
+        o.quadType = mpgb::QuadTypes::AdaptiveClenshawCurtis;
+        o.quadAbsTol = o.quadRelTol = 1e-6;
+        Dev dc(coef), dx(x), ds(sens), dr(r);
+        std::vector<double> out;
+        auto append = [&](const Dev& d) {
+            auto h = d.host();
+            out.insert(out.end(), h.begin(), h.end());
+        };
+
+        // Route 1: the C++ API.
+        {
+            auto map = mpgb::MapFactory::CreateTriangular(2, 2, 3, o);
+            if (map->numCoeffs != (unsigned)nc) throw std::runtime_error("unexpected number of coefficients");
+            map->SetCoeffs(dc.p, nc);
+            Dev T(2 * N), ld(N), cg((size_t)nc * N), xi(2 * N);
+            const auto P = mpgb::StridedMatrix::RowMajor(dx.p, 2, N);
+            map->EvaluateImpl(P, mpgb::StridedMatrix::RowMajor(T.p, 2, N));
+            map->LogDeterminantImpl(P, mpgb::StridedMatrix::RowMajor(ld.p, 1, N));
+            map->CoeffGradImpl(P, mpgb::StridedMatrix::RowMajor(ds.p, 2, N), mpgb::StridedMatrix::RowMajor(cg.p, nc, N));
+            map->InverseImpl(mpgb::StridedMatrix(nullptr, 0, N, N, 1), mpgb::StridedMatrix::RowMajor(dr.p, 2, N),
+                             mpgb::StridedMatrix::RowMajor(xi.p, 2, N));
+            append(T);
+            append(ld);
+            append(cg);
+            append(xi);
+        }
+        // Route 2: the adapter over the C ABI.
+        {
+            GB300Map map(2, 2, 3, o);
+            map.SetCoeffs(DView{dc.p, nc, 1, 1, 1});
+            Dev T(2 * N), ld(N), cg((size_t)nc * N), xi(2 * N);
+            const DView P{dx.p, 2, N, N, 1};
+            map.EvaluateImpl(P, DView{T.p, 2, N, N, 1});
+            map.LogDeterminantImpl(P, DView{ld.p, N, 1, 1, 1});
+            map.CoeffGradImpl(P, DView{ds.p, 2, N, N, 1}, DView{cg.p, nc, N, N, 1});
+            map.InverseImpl(DView{nullptr, 0, N, N, 1}, DView{dr.p, 2, N, N, 1}, DView{xi.p, 2, N, N, 1});
+            append(T);
+            append(ld);
+            append(cg);
+            append(xi);
+        }
+        FILE* g = std::fopen(argv[2], "wb");
+        if (!g || std::fwrite(out.data(), 8, out.size(), g) != out.size()) throw std::runtime_error("cannot write output");
+        std::fclose(g);
+    } catch (std::exception const& e) {
+        std::fprintf(stderr, "cpp_consumer: %s\n", e.what());
+        return 1;
+    }
+    return 0;
+}
