@@ -702,7 +702,7 @@ inline int queueWideQuad(long long N) {
     return (int)std::min(160.0, std::max(48.0, w));
 }
 constexpr int kWarpPassBlocksPerSM = 2;
-constexpr int kWarpStackCap = 2048;
+constexpr int kWarpStackCap = 512;
 
 void checkMatrix(const StridedMatrix& m, int64_t rows, int64_t cols, const char* what, const char* fn) {
     if (m.rows != rows || m.cols != cols) {
@@ -1048,8 +1048,8 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         W.inverseA.ensure((size_t)(W.pmax + 1) * N * sizeof(double), stream);
         W.inverseList.ensure((size_t)N * sizeof(int), stream);
         const int warpBlocks = kWarpPassBlocksPerSM * W.numSMs;
-        W.inverseStack.ensure((size_t)warpBlocks * 4 * kWarpStackCap * sizeof(QEntry), stream);
-        int* counters = W.inverseDefer.as<int>();  // [queue pass, deferred count, warp pass, -]
+        W.inverseStack.ensure((size_t)warpBlocks * (128 / kWarpGroup) * kWarpStackCap * sizeof(QEntry), stream);
+        int* counters = W.inverseDefer.as<int>();  // [queue pass, deferred count, warp pass, queue drained]
         for (int c = 0; c < p.nComps; ++c) {
             InverseParams k = p;
             k.compBegin = c;
@@ -1074,8 +1074,9 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
             q.wideQuad = queueWideQuad(N);
             q.deferList = W.inverseList.as<int>();
             q.deferCount = counters + 1;
+            q.drained = counters + 3;
             MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
-            // The deferred points, one warp each.
+            // The deferred points, kWarpGroup lanes each.
             InverseParams wp = q;
             wp.queuePass = 0;
             wp.nodeBudget = 0;

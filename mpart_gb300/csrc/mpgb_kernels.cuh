@@ -1203,6 +1203,10 @@ __global__ void __launch_bounds__(256) inverseKernel(const __grid_constant__ Inv
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }
 
+// Queue pass: once the queue is empty, a solve that has taken kDrainNodes
+// integrand nodes (or more) is left to the warp pass.
+constexpr int kDrainNodes = 256;
+
 // Inverse of one monotone component (compBegin) from a queue of points, one
 // integrand node per lane and loop iteration.
 //
@@ -1333,6 +1337,9 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
                     }
                 } else {
                     have = false;
+                    // The queue is empty: from now on the launch ends with
+                    // the solves still running, one lane each.
+                    if (prm.drained) *(volatile int*)prm.drained = 1;
                 }
             }
         }
@@ -1357,7 +1364,13 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         // (a far iterate) or a solve longer than nodeBudget nodes -- is left
         // to the warp pass, which solves it again from the start with 32
         // lanes per quadrature.
-        if (prm.nodeBudget > 0 && (++nodes > prm.nodeBudget || nInt >= prm.wideQuad)) {
+        // Once the queue is empty, solves past kDrainNodes nodes go too: the
+        // warp pass runs them side by side, kWarpGroup lanes each, instead
+        // of one lane each in a few warps.
+        ++nodes;
+        const bool drainedNow = prm.drained && (nodes & 63) == 0 && nodes >= kDrainNodes &&
+                                *(volatile int*)prm.drained != 0;
+        if (prm.nodeBudget > 0 && (nodes > prm.nodeBudget || nInt >= prm.wideQuad || drainedNow)) {
             prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
             have = false;
             need = true;
@@ -1447,21 +1460,23 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
     if (prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }
 
-// Inverse of the points the queue pass left over (deferList), one warp per
-// point.  The solver state is the same in every lane; each quadrature of T
-// is shared by the 32 lanes: the pending intervals live on a per-warp stack
-// in global scratch (prm.stack, the leftmost on top), each round the lanes
-// take the top min(32, depth) entries, evaluate one interval each (its
-// midpoint, other coarse nodes and fine-only nodes, as `integrate`) and
-// replace it by its two halves or by an accepted marker; accepted markers
-// that reach the top are added to the integral in order.  The intervals,
-// their values, the accept tests and the order of the sum of accepted fine
-// values are those of the depth-first `integrate`, so T -- and every solver
-// iterate -- is bitwise the same as in one lane.  Near the stack's capacity
-// the rounds take one interval (a depth-first walk needs at most maxSub more
-// entries).
+// Inverse of the points the queue pass left over (deferList), one group of
+// G lanes per point (G = kWarpGroup; 32 / G points per warp).  The solver
+// state is the same in every lane of a group; each quadrature of T is shared
+// by the group's lanes: the pending intervals live on a per-group stack in
+// global scratch (prm.stack, the leftmost on top), each round the lanes take
+// the top min(G, depth) entries, evaluate one interval each (its midpoint,
+// other coarse nodes and fine-only nodes, as `integrate`) and replace it by
+// its two halves or by an accepted marker; accepted markers that reach the
+// top are added to the integral in order.  The intervals, their values, the
+// accept tests and the order of the sum of accepted fine values are those of
+// the depth-first `integrate`, so T -- and every solver iterate -- is bitwise
+// the same as in one lane.  Near the stack's capacity the rounds take one
+// interval (a depth-first walk needs at most maxSub more entries).
 template <int BASIS, int POS, int PMAX>
 __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__ InverseParams prm) {
+    constexpr int G = kWarpGroup;
+    static_assert(G == 4 || G == 8 || G == 16 || G == 32, "group size");
     __shared__ double sOff[kMaxRulePts], sCw[kMaxRulePts], sFw[kMaxRulePts];
     __shared__ int sIsC[kMaxRulePts];
     __shared__ int sPer;
@@ -1488,21 +1503,23 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
     const int D = c.D, P = c.P;
     const long long N = prm.N;
     const int lane = threadIdx.x & 31;
-    const unsigned kFull = 0xffffffffu;
+    const int gl = lane % G;  // lane within the group
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane - gl));
     const double nan = __longlong_as_double(0x7ff8000000000000ULL);
     const double nugget = prm.nugget;
     const int cap = prm.stackCap;
-    QEntry* stk = prm.stack + ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * cap;
+    const long long group = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+    QEntry* stk = prm.stack + group * cap;
     const int listN = *prm.listCount;
     int stAll = 0;
 
     for (;;) {
         int k = 0;
-        if (lane == 0) k = atomicAdd(prm.queue, 1);
-        k = __shfl_sync(kFull, k, 0);
+        if (gl == 0) k = atomicAdd(prm.queue, 1);
+        k = __shfl_sync(gmask, k, 0, G);
         if (k >= listN) break;
         const long long i = prm.deferList[k];
-        // The point (the same in every lane).
+        // The point (the same in every lane of the group).
         const long long xi = (prm.x1Cols == 1) ? 0 : i;
         double x0 = 0.0;
         for (int d = 0; d < D; ++d) {
@@ -1536,11 +1553,11 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
             const double xd = rs.x;
             // T(x) - f0: the quadrature of x (g(df(t x)) + nugget) over t in [0, 1].
             int qst = 0;
-            double Ih = 0.0;  // (lane 0)
+            double Ih = 0.0;  // (group lane 0)
             bool failed = false;
             if (fixed) {
-                // one fixed rule: lane 0 alone
-                if (lane == 0) {
+                // one fixed rule: the group's first lane alone
+                if (gl == 0) {
                     for (int jn = 0; jn < Q.nFine; ++jn) {
                         NodeVal<PMAX, false, 0> V;
                         evalNode<BASIS, POS, PMAX, false, 0>(0.5 * (1.0 + Q.fPts[jn]), xd, as, P, prm.bc, nugget, V,
@@ -1548,7 +1565,7 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                         Ih = fma(0.5 * Q.fWts[jn], V.h, Ih);
                     }
                 }
-                qst = __shfl_sync(kFull, qst, 0);
+                qst = __shfl_sync(gmask, qst, 0, G);
                 failed = (qst & (kStatusInf | kStatusNaN)) != 0;
             } else {
                 const double hA0 = xd * G0;
@@ -1559,18 +1576,18 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                 failed = (qst & (kStatusInf | kStatusNaN)) != 0;
                 int sp = 0;
                 if (!failed) {
-                    if (lane == 0) stk[0] = QEntry{0.0, hA0, VB.h, 0, 0};
+                    if (gl == 0) stk[0] = QEntry{0.0, hA0, VB.h, 0, 0};
                     sp = 1;
-                    __syncwarp();
+                    __syncwarp(gmask);
                 }
                 long long processed = 0;
                 while (sp > 0) {
-                    int m = min(32, sp);
+                    int m = min(G, sp);
                     if (sp + m > cap - kMaxSubCap - 2) m = 1;
-                    const bool has = lane < m;
+                    const bool has = gl < m;
                     QEntry e{0.0, 0.0, 0.0, 0, 1};
-                    if (has) e = stk[sp - 1 - lane];
-                    __syncwarp();
+                    if (has) e = stk[sp - 1 - gl];
+                    __syncwarp(gmask);
                     const bool pend = has && !e.done;
                     double ic = 0.0, ih = 0.0, hM = 0.0, mm = 0.0;
                     int lst = 0;
@@ -1598,12 +1615,12 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                         const double tol = fmax(Q.relTol * fabs(ic), Q.absTol);
                         accept = ((err < tol) || (e.level == Q.maxSub - 1)) && (e.level >= Q.minSub);
                     }
-                    qst |= __reduce_or_sync(kFull, lst);
+                    qst |= __reduce_or_sync(gmask, lst);
                     if (qst & (kStatusInf | kStatusNaN)) {
                         failed = true;
                         break;
                     }
-                    processed += __popc(__ballot_sync(kFull, pend));
+                    processed += __popc(__ballot_sync(gmask, pend) & gmask);
                     if (processed > Q.maxIntervals) {
                         qst |= kStatusBudget;
                         failed = true;
@@ -1612,13 +1629,13 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                     // New entries, the leftmost on top: lane j's outputs lie
                     // below those of the lanes left of it.
                     const int nout = !has ? 0 : ((pend && !accept) ? 2 : 1);
-                    int incl = nout;  // sum over lanes >= this one
+                    int incl = nout;  // sum over the group's lanes >= this one
 #pragma unroll
-                    for (int off = 1; off < 32; off <<= 1) {
-                        const int v = __shfl_down_sync(kFull, incl, off);
-                        if (lane + off < 32) incl += v;
+                    for (int off = 1; off < G; off <<= 1) {
+                        const int v = __shfl_down_sync(gmask, incl, off, G);
+                        if (gl + off < G) incl += v;
                     }
-                    const int total = __shfl_sync(kFull, incl, 0);
+                    const int total = __shfl_sync(gmask, incl, 0, G);
                     const int base = sp - m + (incl - nout);
                     if (has) {
                         if (!pend) {
@@ -1631,9 +1648,9 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                         }
                     }
                     sp = sp - m + total;
-                    __syncwarp();
+                    __syncwarp(gmask);
                     // Accepted intervals that reach the top, in order.
-                    if (lane == 0) {
+                    if (gl == 0) {
                         while (sp > 0) {
                             const QEntry t = stk[sp - 1];
                             if (!t.done) break;
@@ -1641,22 +1658,22 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
                             --sp;
                         }
                     }
-                    sp = __shfl_sync(kFull, sp, 0);
-                    __syncwarp();
+                    sp = __shfl_sync(gmask, sp, 0, G);
+                    __syncwarp(gmask);
                 }
             }
             stAll |= qst;
-            double T = __shfl_sync(kFull, Ih, 0);
+            double T = __shfl_sync(gmask, Ih, 0, G);
             if (failed) T = nan;
             rs.step_(T + f0, yd, f, prm.xtol, prm.ytol, kBracketIts, prm.method);
         }
-        if (lane == 0) {
+        if (gl == 0) {
             prm.out[(long long)comp * prm.outRs + i * prm.outCs] = rs.result;
             if (prm.info) prm.info[(long long)comp * prm.infoStride + i] = rs.info;
             if (rs.info < 0) stAll |= kStatusNoBracket;
         }
     }
-    if (lane == 0 && prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
+    if (gl == 0 && prm.statusWord && stAll) atomicOr(prm.statusWord, stAll);
 }
 
 // Key pass of the Inverse for component compBegin (monotone components):
@@ -1761,13 +1778,13 @@ cudaError_t launchInverseP(const InverseParams& prm, int nBlocks, cudaStream_t s
         else kern = inverseKeyKernel<BASIS, POS, PMAX>;
     }
     if (prm.warpPass) {
-        // Persistent: nBlocks blocks of four warps (the host sized the stack
-        // scratch for them).
+        // Persistent: nBlocks blocks of four warps, 128 / kWarpGroup groups
+        // each (the host sized the stack scratch for them).
         if constexpr (BASIS == kBasisSigmoid) {
             return cudaErrorInvalidValue;
         } else {
             if (!prm.queue || !prm.acoef || !prm.stack || !prm.listCount || !prm.deferList ||
-                prm.stackCap < 4 * kMaxSubCap)
+                prm.stackCap < 4 * kMaxSubCap || nBlocks < 1)
                 return cudaErrorInvalidValue;
             kern = inverseWarpKernel<BASIS, POS, PMAX>;
             kern<<<nBlocks, 128, 0, stream>>>(prm);

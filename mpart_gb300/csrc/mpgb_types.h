@@ -196,9 +196,11 @@ struct InverseParams {
     int nodeBudget;
     int wideQuad;
     int* deferList;
-    // Warp pass (warpPass = 1): one warp per point of deferList (*listCount
-    // of them, taken through *queue), the lanes sharing each adaptive
-    // quadrature; stack: stackCap entries of scratch per warp of the grid.
+    int* drained;  // set (to 1) by the first lane that finds the queue empty; zero on entry
+    // Warp pass (warpPass = 1): one group of kWarpGroup lanes per point of
+    // deferList (*listCount of them, taken through *queue), the lanes sharing
+    // each adaptive quadrature; stack: stackCap entries of scratch per group
+    // of the grid.
     QEntry* stack;
     int stackCap;
     int warpPass;
