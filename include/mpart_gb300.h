@@ -278,6 +278,14 @@ int mpgb_fused_fwd_adj_noalloc(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens,
  * call sequence (FastGaussianReverseKLObjective::CommonEval,
  * src/MapObjective.cpp:185-234: Evaluate, LogDeterminant, CoeffGrad and
  * LogDeterminantCoeffGrad into dense outputs, then reductions). */
+/* Optimisation algorithms (TrainOptions::opt_alg, MParT/TrainMap.h:21; NLopt
+ * is not used).  MPGB_OPT_SLSQP: the iteration of SLSQP, NLopt's LD_SLSQP and
+ * the reference's default, for a problem without constraints (damped-BFGS
+ * quasi-Newton with SLSQP's line search); MPGB_OPT_LBFGS: limited-memory BFGS
+ * (LD_LBFGS) with `memory` pairs. */
+#define MPGB_OPT_SLSQP 0
+#define MPGB_OPT_LBFGS 1
+
 typedef struct mpgb_train_options {
     int max_iters;
     int max_evals;
@@ -288,6 +296,7 @@ typedef struct mpgb_train_options {
     double gtol;
     int memory;
     int mode;
+    int algorithm;  /* MPGB_OPT_SLSQP (default) or MPGB_OPT_LBFGS */
 } mpgb_train_options;
 
 typedef struct mpgb_train_result {
@@ -347,12 +356,28 @@ int mpgb_train_map_adaptive(unsigned int n_sets, const unsigned int* num_terms, 
                             mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
                             mpgb_atm_result* result, unsigned int* final_num_terms, void* stream);
 
-/* Reduced margin of a set given densely (n rows of length dim): the terms outside
- * it whose backward neighbours are all inside (MultiIndexSet::ReducedMargin,
- * src/MultiIndices/MultiIndexSet.cpp:568-590), in this library's scan order.
- * Two-call: out == NULL queries n_out. */
+/* Multi-index sets given densely (n rows of length dim, the active terms in
+ * order) are rebuilt as the reference's MultiIndexSet builds them: the terms
+ * activated in order, each adding its forward and backward neighbours as
+ * inactive entries where they are new (src/MultiIndices/MultiIndexSet.cpp:
+ * AddActive, Activate, AddForwardNeighbors, AddBackwardNeighbors), no limiter.
+ *
+ * Reduced margin: the inactive entries whose existing backward neighbours are
+ * all active, in the order the set met them (MultiIndexSet::ReducedMargin,
+ * MultiIndexSet.cpp:568-590).  Two-call: out == NULL queries n_out. */
 int mpgb_reduced_margin(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
                         unsigned int* out, unsigned int cap_rows);
+
+/* MultiIndexSet::Expand (MultiIndexSet.cpp:739-766): activates the admissible
+ * forward neighbours of the frontier, in the reference's order.  terms_out
+ * receives the n_terms_out new terms (rows of length dim, in activation
+ * order); idx_out the n_idx_out active indices Expand returns (a term reached
+ * from several frontier terms appears once for each, as in the reference).
+ * Two-call: terms_out == idx_out == NULL queries the counts; cap bounds both
+ * outputs (rows / entries). */
+int mpgb_multi_index_expand(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_terms_out,
+                            unsigned int* terms_out, unsigned int* n_idx_out, unsigned int* idx_out,
+                            unsigned int cap);
 
 /* Multi-index set of a single component (compressed form); arrays may be NULL to query sizes. */
 int mpgb_component_multi_index(const mpgb_map* component, unsigned int* dim, unsigned int* num_terms,

@@ -726,10 +726,13 @@ def _sigmoid_starts(n, sumType):
 
 
 class TrainOptions:
-    """MParT/TrainMap.h:19-58, same field names and defaults.  The optimiser is
-    this library's L-BFGS whatever opt_alg names (NLopt is not used); opt_maxeval
-    bounds the objective evaluations per component, the tolerances are NLopt's
-    stopping rules (0 disables one), opt_stopval and opt_maxtime are not used."""
+    """MParT/TrainMap.h:19-58, same field names and defaults.  NLopt is not
+    used: opt_alg "LD_SLSQP" (the default) runs this library's restatement of
+    SLSQP's iteration for an unconstrained problem (a damped-BFGS quasi-Newton
+    method with SLSQP's line search), "LD_LBFGS" its limited-memory BFGS; other
+    names raise ValueError.  opt_maxeval bounds the objective evaluations per
+    component, the tolerances are NLopt's stopping rules (0 disables one),
+    opt_stopval and opt_maxtime are not used."""
 
     def __init__(self, **kw):
         self.opt_alg = "LD_SLSQP"
@@ -750,6 +753,10 @@ class TrainOptions:
         from ._capi import mpgb_train_options
         o = mpgb_train_options()
         check(load().mpgb_train_options_default(C.byref(o)))
+        algs = {"LD_SLSQP": 0, "LD_LBFGS": 1}
+        if self.opt_alg not in algs:
+            raise ValueError(f"opt_alg {self.opt_alg!r}: this library provides LD_SLSQP and LD_LBFGS")
+        o.algorithm = algs[self.opt_alg]
         o.max_iters = o.max_evals = int(self.opt_maxeval)
         o.ftol_rel, o.ftol_abs = float(self.opt_ftol_rel), float(self.opt_ftol_abs)
         o.xtol_rel, o.xtol_abs = float(self.opt_xtol_rel), float(self.opt_xtol_abs)
@@ -794,12 +801,13 @@ def CreateGaussianKLObjective(train, test=None, dim=0):
 
 
 def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, ftol_rel=0.0, ftol_abs=0.0,
-             xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0):
+             xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0, algorithm="LD_SLSQP"):
     """TrainMap(map, objective, options) (src/TrainMap.cpp:166-216) when samples
     is a KLObjective and max_iters a TrainOptions: returns the training objective.
 
     Otherwise the direct form: TrainMap with a standard-normal KL objective:
-    every component minimises its reverse KL with L-BFGS; samples is a CUDA
+    every component minimises its reverse KL with `algorithm` ("LD_SLSQP" or
+    "LD_LBFGS", see TrainOptions); samples is a CUDA
     float64 tensor, inputDim x N.  mode 0 replays one batched step from a CUDA
     graph, 1 launches it directly, 2 launches each component separately, 3 runs
     per component the reference objective's call sequence (Evaluate,
@@ -819,6 +827,10 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
     check(load().mpgb_train_options_default(C.byref(o)))
     o.max_iters, o.max_evals, o.memory, o.mode = int(max_iters), int(max_evals), int(memory), int(mode)
     o.ftol_rel, o.ftol_abs, o.xtol_rel, o.xtol_abs, o.gtol = ftol_rel, ftol_abs, xtol_rel, xtol_abs, gtol
+    algs = {"LD_SLSQP": 0, "LD_LBFGS": 1}
+    if algorithm not in algs:
+        raise ValueError(f"algorithm {algorithm!r}: this library provides LD_SLSQP and LD_LBFGS")
+    o.algorithm = algs[algorithm]
     loss = np.zeros(tmap.outputDim)
     r = mpgb_train_result()
     check(load().mpgb_train_map(tmap._h, _mat(samples), C.byref(o), C.c_void_p(loss.ctypes.data), C.byref(r),
@@ -941,9 +953,13 @@ def fp64_probe(blocks=152 * 8, threads=256, iters=4096):
 
 
 class MultiIndexSet:
-    """Adaptive multi-index set (MParT/MultiIndices/MultiIndexSet.h) with terms
-    in insertion order: what TrainMapAdaptive needs (total-order creation,
-    adding terms, the reduced margin, Fix)."""
+    """Adaptive multi-index set (MParT/MultiIndices/MultiIndexSet.h): the
+    active terms in activation order, and what TrainMapAdaptive needs
+    (total-order creation, adding terms, the reduced margin, Expand, Fix).
+    ReducedMargin and Expand rebuild the reference's bookkeeping of the set
+    (its entries numbered in order of appearance, mpgb_reduced_margin) by
+    activating the terms in order, so they meet the candidates in the
+    reference's order."""
 
     def __init__(self, length: int, multis=()):
         self.length = int(length)
@@ -988,8 +1004,9 @@ class MultiIndexSet:
         return np.ascontiguousarray(np.array(self._terms, dtype=np.uint32).reshape(len(self._terms), self.length))
 
     def ReducedMargin(self):
-        """Terms outside the set whose backward neighbours are all inside it
-        (MultiIndexSet::ReducedMargin, src/MultiIndices/MultiIndexSet.cpp:568-590)."""
+        """Terms outside the set whose backward neighbours are all inside it,
+        in the reference's order (MultiIndexSet::ReducedMargin,
+        src/MultiIndices/MultiIndexSet.cpp:568-590)."""
         U = C.POINTER(C.c_uint)
         dense = self._dense()
         n = C.c_uint()
@@ -1000,11 +1017,23 @@ class MultiIndexSet:
         return [out[k].copy() for k in range(n.value)]
 
     def Expand(self):
-        """Adds the reduced margin; returns the indices of the new terms."""
-        start = self.Size()
-        for m in self.ReducedMargin():
-            self._add(m)
-        return list(range(start, self.Size()))
+        """MultiIndexSet::Expand (src/MultiIndices/MultiIndexSet.cpp:739-766):
+        activates the admissible forward neighbours of the frontier in the
+        reference's order and returns their indices, a term reached from
+        several frontier terms once for each (as the reference's does)."""
+        U = C.POINTER(C.c_uint)
+        dense = self._dense()
+        nt, ni = C.c_uint(), C.c_uint()
+        check(load().mpgb_multi_index_expand(self.length, self.Size(), dense.ctypes.data_as(U), C.byref(nt), None,
+                                             C.byref(ni), None, 0))
+        cap = max(1, nt.value, ni.value)
+        terms = np.zeros((cap, self.length), dtype=np.uint32)
+        idx = np.zeros(cap, dtype=np.uint32)
+        check(load().mpgb_multi_index_expand(self.length, self.Size(), dense.ctypes.data_as(U), None,
+                                             terms.ctypes.data_as(U), None, idx.ctypes.data_as(U), cap))
+        for k in range(nt.value):
+            self._add(terms[k])
+        return [int(v) for v in idx[:ni.value]]
 
     def Fix(self, compress=True):
         return FixedMultiIndexSet.from_multis(self._dense()) if self.Size() else \

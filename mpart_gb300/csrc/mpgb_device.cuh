@@ -31,6 +31,10 @@ constexpr int kPosSoftPlus = 1;
 // reference keeps the branch path in a 32-bit unsigned (Quadrature.h:837,
 // :925-944), so maxSub <= 32 is its own limit as well.
 constexpr int kMaxSubCap = 32;
+// Fused kernel: resident 128-thread blocks per SM its register budget is
+// built for; reduced launches cut each component into this many work items
+// per SM.
+constexpr int kFusedBlocksPerSM = 4;
 // Inverse warp pass: lanes per deferred point (32 / kWarpGroup points per warp).
 constexpr int kWarpGroup = 8;
 // Largest nested Clenshaw-Curtis level (coarse 2^L+1, fine 2^(L+1)+1 points).

@@ -747,8 +747,8 @@ static std::vector<WorkItem> itemsAllComps(long long N, int nComps) {
 }
 
 // Items of style "one component, a set of tiles".  Heavier components first.
-// With reduced outputs each component is cut into at most 4 items per SM,
-// independently of the other components of the launch, so a batched launch
+// With reduced outputs each component is cut into at most kFusedBlocksPerSM
+// items per SM, independently of the other components of the launch, so a batched launch
 // and per-component launches produce the same partial rows.  Item k of a
 // component takes tiles k, k + nItems, k + 2 nItems, ...: points are processed
 // in order of |x_D| (quadrature cost grows with it), and striding gives every
@@ -769,7 +769,8 @@ static std::vector<WorkItem> itemsPerComp(const std::vector<MonotoneMapBase::Par
     if (itemsOfComp) itemsOfComp->assign(nComps, {});
     for (int c : order) {
         const long long nItemsC =
-            reduced ? std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * 4)) : nTiles;
+            reduced ? std::max<long long>(1, std::min<long long>(nTiles, (long long)numSMs * kFusedBlocksPerSM))
+                    : nTiles;
         for (long long t = 0; t < nItemsC; ++t) {
             WorkItem w{c, c + 1, (int)t, (int)((nTiles - t + nItemsC - 1) / nItemsC), 0, 0, (int)nItemsC, 0};
             if (reduced) {
@@ -1799,6 +1800,8 @@ int trainMapAdaptiveImpl(unsigned int n_sets, const unsigned int* num_terms, con
                          mpgb_atm_result* result, unsigned int* final_num_terms, void* stream, char* err, int errLen);
 int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_out,
                       unsigned int* out, unsigned int cap_rows);
+int expandImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_terms_out,
+               unsigned int* terms_out, unsigned int* n_idx_out, unsigned int* idx_out, unsigned int cap);
 int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
                    double* grad, void* stream, char* err, int errLen);
 }
@@ -2410,6 +2413,15 @@ int mpgb_reduced_margin(unsigned int dim, unsigned int n, const unsigned int* mu
     return guard([&] {
         if ((n && !multis) || dim == 0) throw std::invalid_argument("bad multi-index set");
         reducedMarginImpl(dim, n, multis, n_out, out, cap_rows);
+    });
+}
+
+int mpgb_multi_index_expand(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_terms_out,
+                            unsigned int* terms_out, unsigned int* n_idx_out, unsigned int* idx_out,
+                            unsigned int cap) {
+    return guard([&] {
+        if ((n && !multis) || dim == 0) throw std::invalid_argument("bad multi-index set");
+        expandImpl(dim, n, multis, n_terms_out, terms_out, n_idx_out, idx_out, cap);
     });
 }
 

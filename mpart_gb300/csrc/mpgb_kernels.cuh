@@ -358,15 +358,18 @@ struct SmemLayout {
     double* X;   // [dmax][tpb]        coordinates of the tile's points
     double* B;   // [nBmax][tpb+1]     leading-coordinate basis values
     double* S;   // [depthMax+1][tpb]  prefix-product stack
-    double* W;   // [PMAX+1][tpb]      per-point adjoint weights
+    double* W;   // [PMAX+1][tpb]      per-point adjoint weights (the rows of S: a
+                 //                    component writes W after its last use of S,
+                 //                    and the next component's phase A starts after
+                 //                    the reduction that reads W)
     double* GX;  // [dmax][tpb]        input gradient accumulators
     double* DS;  // [tri(depthMax+1)][tpb]  forward-mode derivative stack
     int bstride;
 };
 
 __host__ __device__ inline size_t smemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input) {
-    size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)(depthMax + 1) * tpb +
-               (size_t)(pmax + 1) * tpb;
+    const int sw = (depthMax + 1 > pmax + 1) ? depthMax + 1 : pmax + 1;
+    size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)sw * tpb;
     if (input) {
         n += (size_t)dmax * tpb + (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
     }
@@ -380,8 +383,9 @@ __device__ inline SmemLayout carveSmem(double* base, int tpb, int dmax, int nBma
     double* p = base;
     L.X = p; p += (size_t)dmax * tpb;
     L.B = p; p += (size_t)nBmax * (tpb + 1);
-    L.S = p; p += (size_t)(depthMax + 1) * tpb;
-    L.W = p; p += (size_t)(pmax + 1) * tpb;
+    L.S = p;
+    L.W = p;
+    p += (size_t)((depthMax + 1 > pmax + 1) ? depthMax + 1 : pmax + 1) * tpb;
     if (input) {
         L.GX = p; p += (size_t)dmax * tpb;
         L.DS = p;
@@ -818,7 +822,7 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
 }
 
 template <int BASIS, int POS, int PMAX, bool NEEDJ, int NEEDE>
-__global__ void __launch_bounds__(256) fusedKernel(const __grid_constant__ FusedParams prm) {
+__global__ void __launch_bounds__(128, kFusedBlocksPerSM) fusedKernel(const __grid_constant__ FusedParams prm) {
     extern __shared__ double smem[];
     fusedBody<BASIS, POS, PMAX, NEEDJ, NEEDE, false>(prm, prm.items[blockIdx.x], smem);
 }

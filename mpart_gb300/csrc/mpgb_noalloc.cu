@@ -178,7 +178,7 @@ void run(MonotoneMapBase& map, const mpgb_matrix& pts, const mpgb_matrix& sens, 
         dmax = std::max(dmax, p.D);
         nBmax = std::max(nBmax, p.nB);
         depthMax = std::max(depthMax, p.maxDepth);
-        const long long nItemsC = std::max<long long>(1, std::min<long long>(nTiles, (long long)sms * 4));
+        const long long nItemsC = std::max<long long>(1, std::min<long long>(nTiles, (long long)sms * kFusedBlocksPerSM));
         const long long tilesPer = (nTiles + nItemsC - 1) / nItemsC;
         rowOff[c] = (int)rowBase.size();
         for (long long t = 0; t < nTiles; t += tilesPer) {

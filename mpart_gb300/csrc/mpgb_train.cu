@@ -3,9 +3,11 @@
 // standard-normal density (src/TrainMap.cpp:144-164, :166-216).  The
 // reference hands each component to NLopt in turn; here every component's
 // optimiser runs in lockstep and one batched launch (optionally replayed from
-// a CUDA graph) evaluates all of their requests at once.  The optimiser is a
-// limited-memory BFGS (two-loop recursion, Nocedal & Wright Alg. 7.4 / 7.5)
-// with a backtracking Armijo line search; NLopt itself is not available.
+// a CUDA graph) evaluates all of their requests at once.  NLopt itself is not
+// available; two optimisers of this library's own stand in for its algorithms:
+// the iteration of SLSQP (the reference's default, LD_SLSQP) for a problem
+// without constraints, and a limited-memory BFGS (LD_LBFGS), both with
+// NLopt's stopping rules.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -13,6 +15,7 @@
 #include <limits>
 #include <map>
 #include <memory>
+#include <set>
 #include <sstream>
 #include <vector>
 
@@ -37,17 +40,25 @@ struct TrainOpts {
     int maxEvals = 1000;
     double ftolRel = 0.0, ftolAbs = 0.0, xtolRel = 0.0, xtolAbs = 0.0, gtol = 0.0;
     int memory = 10;
+    int algorithm = MPGB_OPT_SLSQP;
 };
 
-// Reverse-communication L-BFGS on one component's coefficients.
-class LBFGS {
-public:
-    enum State { kInit, kLineSearch, kDone };
-    LBFGS(const double* x0, int n, const TrainOpts& o) : n_(n), o_(o), x_(x0, x0 + n), trial_(x0, x0 + n) {}
+// NLopt's stopping test on one value: the change is below the absolute
+// tolerance or below the relative tolerance times the mean magnitude.
+bool relStop(double vold, double vnew, double reltol, double abstol) {
+    if (std::isinf(vold)) return false;
+    const double d = std::fabs(vnew - vold);
+    return d < abstol || d < reltol * 0.5 * (std::fabs(vnew) + std::fabs(vold)) || (reltol > 0 && vnew == vold);
+}
 
-    // Point the caller must evaluate next (valid unless done()).
+// Reverse-communication optimiser of one component's coefficients: the
+// caller evaluates the objective and gradient at request() and passes them
+// to tell() until done().
+class Optimizer {
+public:
+    virtual ~Optimizer() = default;
     const std::vector<double>& request() const { return trial_; }
-    bool done() const { return state_ == kDone; }
+    bool done() const { return done_; }
     int iterations() const { return iters_; }
     int evaluations() const { return evals_; }
     double f() const { return f_; }
@@ -57,13 +68,152 @@ public:
         for (double v : g_) s += v * v;
         return std::sqrt(s);
     }
+    virtual void tell(double f, const double* g) = 0;
 
-    void tell(double f, const double* g) {
+protected:
+    Optimizer(const double* x0, int n, const TrainOpts& o) : n_(n), o_(o), x_(x0, x0 + n), trial_(x0, x0 + n) {}
+    static double dot(const std::vector<double>& a, const std::vector<double>& b) {
+        double s = 0;
+        for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+        return s;
+    }
+    bool converged0() const { return o_.gtol > 0 && gradNorm() <= o_.gtol; }
+    // NLopt's tests between two iterates (and this library's iteration and
+    // gradient-norm limits).
+    bool stopAfter(double fOld, const std::vector<double>& xOld) const {
+        if (iters_ >= o_.maxIters || evals_ >= o_.maxEvals || converged0()) return true;
+        if (relStop(fOld, f_, o_.ftolRel, o_.ftolAbs)) return true;
+        bool allX = true;
+        for (int i = 0; i < n_ && allX; ++i) allX = relStop(xOld[i], x_[i], o_.xtolRel, o_.xtolAbs);
+        return allX;
+    }
+    int n_;
+    TrainOpts o_;
+    std::vector<double> x_, trial_, g_;
+    double f_ = 0;
+    bool done_ = false;
+    int iters_ = 0, evals_ = 0;
+};
+
+// The iteration of SLSQP (D. Kraft, "A software package for sequential
+// quadratic programming", DFVLR-FB 88-28, 1988) for a problem without
+// constraints or bounds, where its quadratic subproblem is min_d g'd +
+// d'Bd/2: a quasi-Newton method whose matrix B starts as the identity and
+// takes Powell's damped BFGS update (with s'u raised to 0.2 s'Bs where it is
+// smaller), and whose line search starts from the full step, accepts when the
+// decrease is at least a tenth of the linear prediction (or after ten
+// reductions), and otherwise shrinks the step by the minimiser of the
+// quadratic through the two values and the slope, at least to a tenth.
+// B^-1 is kept and updated directly (the inverse form of the same update:
+// with d = -B^-1 g exactly, B s = -alpha g), O(n^2) per iteration.  A
+// non-finite trial value shrinks the step by a tenth and is never accepted.
+class SLSQPU : public Optimizer {
+public:
+    SLSQPU(const double* x0, int n, const TrainOpts& o) : Optimizer(x0, n, o), H_((size_t)n * n, 0.0) {
+        for (int i = 0; i < n; ++i) H_[(size_t)i * n + i] = 1.0;
+    }
+    void tell(double f, const double* g) override {
         ++evals_;
-        if (state_ == kInit) {
+        if (first_) {
+            first_ = false;
             f_ = f;
             g_.assign(g, g + n_);
-            if (!std::isfinite(f) || converged0()) { state_ = kDone; return; }
+            if (!std::isfinite(f) || converged0()) { done_ = true; return; }
+            direction();
+            return;
+        }
+        const double h1 = f - f_;
+        const bool finite = std::isfinite(f);
+        if (finite && (h1 <= 0.1 * h3_ || line_ > 10)) {
+            const double fOld = f_;
+            const std::vector<double> xOld = x_, gOld = g_;
+            x_ = trial_;
+            f_ = f;
+            g_.assign(g, g + n_);
+            ++iters_;
+            update(gOld);
+            if (stopAfter(fOld, xOld)) { done_ = true; trial_ = x_; return; }
+            direction();
+            return;
+        }
+        if (evals_ >= o_.maxEvals || line_ > 40) { done_ = true; trial_ = x_; return; }
+        double a = finite ? h3_ / (2.0 * (h3_ - h1)) : 0.1;
+        if (!(a > 0.1)) a = 0.1;
+        alpha_ *= a;
+        h3_ *= a;
+        for (int i = 0; i < n_; ++i) { s_[i] *= a; trial_[i] = x_[i] + s_[i]; }
+        ++line_;
+    }
+
+private:
+    void direction() {
+        s_.assign(n_, 0.0);
+        for (int i = 0; i < n_; ++i) {
+            double v = 0;
+            const double* row = &H_[(size_t)i * n_];
+            for (int j = 0; j < n_; ++j) v += row[j] * g_[j];
+            s_[i] = -v;
+        }
+        h3_ = dot(g_, s_);
+        if (!(h3_ < 0)) {  // not a descent direction: back to the identity
+            std::fill(H_.begin(), H_.end(), 0.0);
+            for (int i = 0; i < n_; ++i) { H_[(size_t)i * n_ + i] = 1.0; s_[i] = -g_[i]; }
+            h3_ = dot(g_, s_);
+        }
+        alpha_ = 1.0;
+        line_ = 1;
+        for (int i = 0; i < n_; ++i) trial_[i] = x_[i] + s_[i];
+    }
+    void update(const std::vector<double>& gOld) {
+        // s_ is the step taken; B s = -alpha g_old.
+        std::vector<double> u(n_), v(n_);
+        for (int i = 0; i < n_; ++i) {
+            u[i] = g_[i] - gOld[i];
+            v[i] = -alpha_ * gOld[i];
+        }
+        double h1 = dot(s_, u);
+        const double h2 = dot(s_, v);
+        if (!(h2 > 0)) return;
+        const double h3 = 0.2 * h2;
+        if (h1 < h3) {
+            const double t = (h2 - h3) / (h2 - h1);
+            for (int i = 0; i < n_; ++i) u[i] = t * u[i] + (1.0 - t) * v[i];
+            h1 = h3;
+        }
+        // H <- (I - r s u') H (I - r u s') + r s s', r = 1 / s'u.
+        const double r = 1.0 / h1;
+        std::vector<double> Hu(n_);
+        for (int i = 0; i < n_; ++i) {
+            double w = 0;
+            const double* row = &H_[(size_t)i * n_];
+            for (int j = 0; j < n_; ++j) w += row[j] * u[j];
+            Hu[i] = w;
+        }
+        const double c = r * r * dot(u, Hu) + r;
+        for (int i = 0; i < n_; ++i) {
+            double* row = &H_[(size_t)i * n_];
+            for (int j = 0; j < n_; ++j) row[j] += c * s_[i] * s_[j] - r * (s_[i] * Hu[j] + Hu[i] * s_[j]);
+        }
+    }
+    std::vector<double> H_, s_;
+    double h3_ = 0, alpha_ = 1;
+    int line_ = 0;
+    bool first_ = true;
+};
+
+// Limited-memory BFGS (two-loop recursion, Nocedal & Wright Alg. 7.4 / 7.5)
+// with a backtracking Armijo line search.
+class LBFGS : public Optimizer {
+public:
+    LBFGS(const double* x0, int n, const TrainOpts& o) : Optimizer(x0, n, o) {}
+
+    void tell(double f, const double* g) override {
+        ++evals_;
+        if (first_) {
+            first_ = false;
+            f_ = f;
+            g_.assign(g, g + n_);
+            if (!std::isfinite(f) || converged0()) { done_ = true; return; }
             newDirection(true);
             return;
         }
@@ -72,12 +222,9 @@ public:
         if (std::isfinite(f) && f <= f_ + 1e-4 * alpha_ * gd) {
             // accept
             std::vector<double> s(n_), y(n_);
-            double maxdx = 0, maxrel = 0;
             for (int i = 0; i < n_; ++i) {
                 s[i] = trial_[i] - x_[i];
                 y[i] = g[i] - g_[i];
-                maxdx = std::max(maxdx, std::fabs(s[i]));
-                if (trial_[i] != 0) maxrel = std::max(maxrel, std::fabs(s[i]) / std::fabs(trial_[i]));
             }
             const double sy = dot(s, y);
             if (sy > 1e-12 * std::sqrt(dot(s, s) * dot(y, y))) {
@@ -90,14 +237,14 @@ public:
                     rho_.erase(rho_.begin());
                 }
             }
-            const double df = std::fabs(f - f_);
+            const double fOld = f_;
+            const std::vector<double> xOld = x_;
             x_ = trial_;
             f_ = f;
             g_.assign(g, g + n_);
             ++iters_;
-            if (iters_ >= o_.maxIters || evals_ >= o_.maxEvals || df <= o_.ftolAbs || df <= o_.ftolRel * std::fabs(f) ||
-                maxdx <= o_.xtolAbs || (o_.xtolRel > 0 && maxrel <= o_.xtolRel) || converged0()) {
-                state_ = kDone;
+            if (stopAfter(fOld, xOld)) {
+                done_ = true;
                 trial_ = x_;
                 return;
             }
@@ -106,7 +253,7 @@ public:
         }
         // backtrack (quadratic interpolation, safeguarded to [0.1, 0.5] of the step)
         if (evals_ >= o_.maxEvals || ++backtracks_ > 40) {
-            state_ = kDone;
+            done_ = true;
             trial_ = x_;
             return;
         }
@@ -119,13 +266,6 @@ public:
     }
 
 private:
-    static double dot(const std::vector<double>& a, const std::vector<double>& b) {
-        double s = 0;
-        for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
-        return s;
-    }
-    bool converged0() const { return o_.gtol > 0 && gradNorm() <= o_.gtol; }
-
     void newDirection(bool first) {
         // Two-loop recursion: d = -H g.
         std::vector<double> q = g_;
@@ -157,18 +297,21 @@ private:
         gPrevDir_ = g_;
         backtracks_ = 0;
         for (int i = 0; i < n_; ++i) trial_[i] = x_[i] + alpha_ * d_[i];
-        state_ = kLineSearch;
     }
 
-    int n_;
-    TrainOpts o_;
-    std::vector<double> x_, trial_, g_, d_, gPrevDir_;
-    double f_ = 0, alpha_ = 1;
+    std::vector<double> d_, gPrevDir_;
+    double alpha_ = 1;
     std::vector<std::vector<double>> S_, Y_;
     std::vector<double> rho_;
-    State state_ = kInit;
-    int iters_ = 0, evals_ = 0, backtracks_ = 0;
+    bool first_ = true;
+    int backtracks_ = 0;
 };
+
+std::unique_ptr<Optimizer> makeOptimizer(const double* x0, int n, const TrainOpts& o) {
+    if (o.algorithm == MPGB_OPT_LBFGS) return std::unique_ptr<Optimizer>(new LBFGS(x0, n, o));
+    if (o.algorithm == MPGB_OPT_SLSQP) return std::unique_ptr<Optimizer>(new SLSQPU(x0, n, o));
+    throw std::invalid_argument("TrainMap: unknown optimisation algorithm.");
+}
 
 struct Pinned {
     double* p = nullptr;
@@ -297,8 +440,8 @@ struct KLStep {
 namespace mpgb {
 
 // Standard-normal KL training of every component (src/TrainMap.cpp:144-164):
-// lockstep L-BFGS per component over one batched objective step per
-// iteration.  Throws; sets the map's coefficients to the result.
+// lockstep optimisers, one per component, over one batched objective step
+// per iteration.  Throws; sets the map's coefficients to the result.
 void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o, int mode, cudaStream_t s,
              double* loss_per_comp, mpgb_train_result* res) {
     // A map without coefficients starts from ones (src/TrainMap.cpp:168-176).
@@ -309,10 +452,12 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
     const auto& parts = map.Parts();
     std::vector<double> x0 = map.CoeffMap();
     KLStep step(map, pts, s, mode);
-    std::vector<LBFGS> opt;
-    for (auto& p : parts) opt.emplace_back(x0.data() + p.mapCoeffOffset, (int)(
-                                               (&p == &parts.back() ? map.numCoeffs : (&p + 1)->mapCoeffOffset) -
-                                               p.mapCoeffOffset), o);
+    std::vector<std::unique_ptr<Optimizer>> opt;
+    for (auto& p : parts)
+        opt.push_back(makeOptimizer(x0.data() + p.mapCoeffOffset,
+                                    (int)((&p == &parts.back() ? map.numCoeffs : (&p + 1)->mapCoeffOffset) -
+                                          p.mapCoeffOffset),
+                                    o));
     int steps = 0;
     double stepMs = 0.0;
     cudaEvent_t e0, e1;
@@ -322,9 +467,9 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
     while (true) {
         bool any = false;
         for (size_t c = 0; c < opt.size(); ++c) {
-            const auto& r = opt[c].request();
+            const auto& r = opt[c]->request();
             std::memcpy(step.hCoef.p + parts[c].mapCoeffOffset, r.data(), r.size() * sizeof(double));
-            any |= !opt[c].done();
+            any |= !opt[c]->done();
         }
         if (!any) break;
         TR_CUDA(cudaEventRecord(e0, step.s));
@@ -340,25 +485,25 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
         // back); only an overflow at the starting point is an error.
         map.CheckStatus(step.s);
         for (size_t c = 0; c < opt.size(); ++c)
-            if (!opt[c].done()) opt[c].tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
+            if (!opt[c]->done()) opt[c]->tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
     }
     const double totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     for (size_t c = 0; c < opt.size(); ++c)
-        if (!std::isfinite(opt[c].f()))
+        if (!std::isfinite(opt[c]->f()))
             throw IntegrandError("TrainMap: MonotoneIntegrand: the objective is not finite at the starting "
                                  "coefficients (g(df) overflowed).");
     std::vector<double> xf(map.numCoeffs);
     double total = 0, gn2 = 0;
     int iters = 0, evals = 0;
     for (size_t c = 0; c < opt.size(); ++c) {
-        gn2 += opt[c].gradNorm() * opt[c].gradNorm();
-        std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c].x().data(), opt[c].x().size() * sizeof(double));
-        if (loss_per_comp) loss_per_comp[c] = opt[c].f();
-        total += opt[c].f();
-        iters = std::max(iters, opt[c].iterations());
-        evals = std::max(evals, opt[c].evaluations());
+        gn2 += opt[c]->gradNorm() * opt[c]->gradNorm();
+        std::memcpy(xf.data() + parts[c].mapCoeffOffset, opt[c]->x().data(), opt[c]->x().size() * sizeof(double));
+        if (loss_per_comp) loss_per_comp[c] = opt[c]->f();
+        total += opt[c]->f();
+        iters = std::max(iters, opt[c]->iterations());
+        evals = std::max(evals, opt[c]->evaluations());
     }
     map.SetCoeffs(xf.data(), map.numCoeffs, true, s);
     if (res) {
@@ -382,6 +527,9 @@ TrainOpts trainOptsFromC(const mpgb_train_options* opts) {
     o.xtolAbs = opts->xtol_abs;
     o.gtol = opts->gtol;
     o.memory = opts->memory > 0 ? opts->memory : 10;
+    o.algorithm = opts->algorithm;
+    if (o.algorithm != MPGB_OPT_SLSQP && o.algorithm != MPGB_OPT_LBFGS)
+        throw std::invalid_argument("TrainOptions: algorithm must be MPGB_OPT_SLSQP or MPGB_OPT_LBFGS.");
     return o;
 }
 
@@ -448,49 +596,77 @@ int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, doubl
 // keep the sets with the best test objective.
 // ---------------------------------------------------------------------------
 
-// Multi-index set with terms in insertion order (the reference's
-// MultiIndexSet restricted to what the adaptive loop needs).
+// Multi-index set with the bookkeeping of the reference's MultiIndexSet
+// (src/MultiIndices/MultiIndexSet.cpp), which fixes the order in which the
+// adaptive loop meets its candidates: every multi-index the set has seen gets
+// a global number in order of first appearance; activating one adds its
+// forward neighbours m + e_d (d = 0..dim-1) and backward neighbours m - e_d
+// as inactive entries where they are new, and records the edges between
+// entries that exist (a sorted set of global numbers per entry and
+// direction).  Active terms keep their order of activation (the term and
+// coefficient order).  No limiter: every multi-index is allowed.  A set given
+// as a list of terms is rebuilt by activating them in order, which is how the
+// reference's total-order construction, += and Expand build theirs.
 struct AdaptiveSet {
     unsigned dim = 0;
-    std::vector<std::vector<unsigned>> terms;
-    std::map<std::vector<unsigned>, int> index;
+    std::vector<std::vector<unsigned>> terms;  // active terms, in activation order
+    std::vector<std::vector<unsigned>> all;    // every entry, by global number
+    std::map<std::vector<unsigned>, int> global;
+    std::vector<int> activeOf;                 // global number -> active index or -1
+    std::vector<int> globalOf;                 // active index -> global number
+    std::vector<std::set<int>> inE, outE;      // backward / forward edges by global number
 
-    bool has(const std::vector<unsigned>& m) const { return index.count(m) != 0; }
+    bool has(const std::vector<unsigned>& m) const {
+        auto it = global.find(m);
+        return it != global.end() && activeOf[it->second] >= 0;
+    }
+    // Activates m (a new entry if needed): MultiIndexSet::AddActive.
     void add(const std::vector<unsigned>& m) {
         if (m.size() != dim) throw std::invalid_argument("multi-index of the wrong length");
-        if (has(m)) return;
-        index[m] = (int)terms.size();
-        terms.push_back(m);
+        auto it = global.find(m);
+        activate(it != global.end() ? it->second : newEntry(m));
     }
-    // Terms outside the set whose backward neighbours (m - e_d for m_d > 0)
-    // are all in it, in the order met scanning the set's terms in order and,
-    // for each, the forward neighbours m + e_d for d = 0..dim-1.
-    std::vector<std::vector<unsigned>> reducedMargin() const {
-        std::vector<std::vector<unsigned>> out;
-        std::map<std::vector<unsigned>, int> seen;
-        for (const auto& t : terms) {
-            for (unsigned d = 0; d < dim; ++d) {
-                std::vector<unsigned> f = t;
-                ++f[d];
-                if (has(f) || seen.count(f)) continue;
-                bool admissible = true;
-                for (unsigned e = 0; e < dim && admissible; ++e) {
-                    if (f[e] == 0) continue;
-                    std::vector<unsigned> b = f;
-                    --b[e];
-                    admissible = has(b);
-                }
-                if (admissible) {
-                    seen[f] = 1;
-                    out.push_back(f);
-                }
-            }
+    // Active terms not yet expanded are given their forward neighbours that
+    // are admissible (every backward neighbour active), in the reference's
+    // order: the frontier's terms in activation order, each one's forward
+    // entries by global number (MultiIndexSet::Expand).  Returns the active
+    // indices of the new terms in that order, a term reached from several
+    // frontier terms once for each, as the reference's does.
+    std::vector<int> expand() {
+        std::vector<int> pending;
+        for (size_t a = 0; a < globalOf.size(); ++a) {
+            const int g = globalOf[a];
+            bool expandable = false;
+            for (int f : outE[g])
+                if (activeOf[f] < 0 && admissible(f)) { expandable = true; break; }
+            if (!expandable) continue;
+            for (int f : outE[g])
+                if (activeOf[f] < 0 && admissible(f)) pending.push_back(f);
+        }
+        std::vector<int> out;
+        for (int f : pending) {
+            activate(f);
+            out.push_back(activeOf[f]);
         }
         return out;
     }
-    FixedMultiIndexSet fix() const {
+    // Inactive entries whose existing backward neighbours are all active, by
+    // global number (MultiIndexSet::ReducedMargin).
+    std::vector<std::vector<unsigned>> reducedMargin() const {
+        std::vector<std::vector<unsigned>> out;
+        for (size_t g = 0; g < all.size(); ++g) {
+            if (activeOf[g] >= 0) continue;
+            bool ok = true;
+            for (int b : inE[g]) ok = ok && activeOf[b] >= 0;
+            if (ok) out.push_back(all[g]);
+        }
+        return out;
+    }
+    FixedMultiIndexSet fix() const { return fixTerms(dim, terms); }
+    // Compressed fixed set of the given terms, in their order (MultiIndexSet::Fix(true)).
+    static FixedMultiIndexSet fixTerms(unsigned dim, const std::vector<std::vector<unsigned>>& ts) {
         std::vector<unsigned> s{0}, d, o;
-        for (const auto& t : terms) {
+        for (const auto& t : ts) {
             for (unsigned e = 0; e < dim; ++e)
                 if (t[e]) {
                     d.push_back(e);
@@ -499,6 +675,63 @@ struct AdaptiveSet {
             s.push_back((unsigned)d.size());
         }
         return FixedMultiIndexSet(dim, s, d, o);
+    }
+
+private:
+    static unsigned nnz(const std::vector<unsigned>& m) {
+        unsigned n = 0;
+        for (unsigned v : m) n += v != 0;
+        return n;
+    }
+    bool admissible(int g) const {
+        if (activeOf[g] >= 0) return true;
+        unsigned n = 0;
+        for (int b : inE[g]) n += activeOf[b] >= 0;
+        return n == nnz(all[g]);
+    }
+    int newEntry(const std::vector<unsigned>& m) {
+        const int g = (int)all.size();
+        all.push_back(m);
+        global[m] = g;
+        activeOf.push_back(-1);
+        inE.emplace_back();
+        outE.emplace_back();
+        link(g, false);
+        return g;
+    }
+    // Edges between g and its existing neighbours; with grow, missing
+    // neighbours become new inactive entries (which link themselves).
+    void link(int g, bool grow) {
+        for (unsigned d = 0; d < dim; ++d) {
+            std::vector<unsigned> f = all[g];
+            ++f[d];
+            auto it = global.find(f);
+            if (it != global.end()) {
+                inE[it->second].insert(g);
+                outE[g].insert(it->second);
+            } else if (grow) {
+                newEntry(f);
+            }
+        }
+        for (unsigned d = 0; d < dim; ++d) {
+            if (all[g][d] == 0) continue;
+            std::vector<unsigned> b = all[g];
+            --b[d];
+            auto it = global.find(b);
+            if (it != global.end()) {
+                outE[it->second].insert(g);
+                inE[g].insert(it->second);
+            } else if (grow) {
+                newEntry(b);
+            }
+        }
+    }
+    void activate(int g) {
+        if (activeOf[g] >= 0) return;
+        activeOf[g] = (int)globalOf.size();
+        globalOf.push_back(g);
+        terms.push_back(all[g]);
+        link(g, true);
     }
 };
 
@@ -513,9 +746,9 @@ struct ATMOpts {
 
 namespace {
 
-std::shared_ptr<ConditionalMapBase> atmComponent(const AdaptiveSet& set, const MapOptions& o,
+std::shared_ptr<ConditionalMapBase> atmComponent(const FixedMultiIndexSet& set, const MapOptions& o,
                                                  const std::vector<double>& coeffs) {
-    auto c = MapFactory::CreateComponent(set.fix(), o);
+    auto c = MapFactory::CreateComponent(set, o);
     if (!coeffs.empty()) c->SetCoeffs(coeffs.data(), (unsigned)coeffs.size(), true);
     return c;
 }
@@ -577,7 +810,7 @@ std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& m
     unsigned size = 0;
     for (unsigned j = 0; j < nOut; ++j) {
         coeffs[j].assign(mset0[j].terms.size(), 0.0);
-        comps[j] = atmComponent(mset0[j], o.map, coeffs[j]);
+        comps[j] = atmComponent(mset0[j].fix(), o.map, coeffs[j]);
         size += (unsigned)mset0[j].terms.size();
     }
     auto map = build(comps);
@@ -586,52 +819,67 @@ std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& m
     double best = atmObjective(*map, test, nullptr, s);
     if (o.verbose) std::printf("TrainMapAdaptive: initial size %u, test objective %.10g\n", size, best);
     std::vector<AdaptiveSet> bestSets = mset0;
-    std::vector<std::vector<double>> bestCoeffs = coeffs;
     unsigned patience = 0, iterations = 0;
     double trainErr = 0.0;
 
     while (size < o.maxSize && patience < o.maxPatience) {
-        // Every component with its reduced margin appended (zero coefficients).
-        std::vector<std::vector<std::vector<unsigned>>> cand(nOut);
+        // Every component with its set expanded (MultiIndexSet::Expand): the
+        // new terms with zero coefficients, the others with their trained
+        // ones.  Terms beyond the largest last-input order the kernels are
+        // built for (kMaxLastOrder) cannot be represented: such candidates
+        // are left out of the expanded component and of the choice.
+        std::vector<AdaptiveSet> expanded(nOut);
+        std::vector<std::vector<int>> cand(nOut);  // Expand's active indices, in its order
+        std::vector<std::vector<int>> pos(nOut);   // active index -> coefficient of the expanded component
         std::vector<std::shared_ptr<ConditionalMapBase>> tmp(nOut);
         for (unsigned j = 0; j < nOut; ++j) {
-            AdaptiveSet e = mset0[j];
-            // Terms beyond the largest last-input order the kernels are built
-            // for (kMaxLastOrder) cannot be represented and are not candidates.
-            for (auto& m : e.reducedMargin())
-                if (m[e.dim - 1] <= (unsigned)kMaxLastOrder) cand[j].push_back(m);
-            for (auto& m : cand[j]) e.add(m);
-            std::vector<double> c = coeffs[j];
-            c.resize(e.terms.size(), 0.0);
-            tmp[j] = atmComponent(e, o.map, c);
+            expanded[j] = mset0[j];
+            cand[j] = expanded[j].expand();
+            const auto& ts = expanded[j].terms;
+            std::vector<std::vector<unsigned>> kept;
+            std::vector<double> c;
+            pos[j].assign(ts.size(), -1);
+            for (size_t t = 0; t < ts.size(); ++t) {
+                if (ts[t][expanded[j].dim - 1] > (unsigned)kMaxLastOrder) continue;
+                pos[j][t] = (int)kept.size();
+                kept.push_back(ts[t]);
+                c.push_back(t < coeffs[j].size() ? coeffs[j][t] : 0.0);
+            }
+            tmp[j] = atmComponent(AdaptiveSet::fixTerms(expanded[j].dim, kept), o.map, c);
         }
         auto mapTmp = build(tmp);
         std::vector<double> grad;
         atmObjective(*mapTmp, train, &grad, s);
-        // Largest |gradient| over the candidates below maxDegrees (first wins ties).
-        int bestBlock = -1, bestIdx = -1;
+        // Largest |gradient| over the candidates below maxDegrees, scanned in
+        // Expand's order with the first of equal values winning (findMaxGrad
+        // and maxDegreeRMFilter, src/TrainMapAdaptive.cpp:6-42).
+        int bestBlock = -1, bestTerm = -1;
         double bestVal = 0.0;
         unsigned off = 0;
         for (unsigned j = 0; j < nOut; ++j) {
-            const unsigned n0 = (unsigned)mset0[j].terms.size();
-            for (unsigned k = 0; k < cand[j].size(); ++k) {
+            for (int k : cand[j]) {
+                if (pos[j][k] < 0) continue;
+                const auto& t = expanded[j].terms[k];
                 bool bounded = false;
                 for (unsigned d = 0; d < mset0[j].dim && !o.maxDegrees.empty(); ++d)
-                    bounded |= cand[j][k][d] >= o.maxDegrees[d];
+                    bounded |= t[d] >= o.maxDegrees[d];
                 if (bounded) continue;
-                const double v = std::fabs(grad[off + n0 + k]);
+                const double v = std::fabs(grad[off + pos[j][k]]);
                 if (v > bestVal) {
                     bestVal = v;
                     bestBlock = (int)j;
-                    bestIdx = (int)k;
+                    bestTerm = k;
                 }
             }
-            off += n0 + (unsigned)cand[j].size();
+            off += tmp[j]->numCoeffs;
         }
         if (bestBlock < 0) break;  // nothing left to add
-        mset0[bestBlock].add(cand[bestBlock][bestIdx]);
-        coeffs[bestBlock].push_back(0.0);
-        for (unsigned j = 0; j < nOut; ++j) comps[j] = atmComponent(mset0[j], o.map, coeffs[j]);
+        mset0[bestBlock].add(expanded[bestBlock].terms[bestTerm]);
+        // The grown component starts again from zero coefficients (a new
+        // component from the factory, src/TrainMapAdaptive.cpp:217-226); the
+        // others keep their trained ones.
+        coeffs[bestBlock].assign(mset0[bestBlock].terms.size(), 0.0);
+        for (unsigned j = 0; j < nOut; ++j) comps[j] = atmComponent(mset0[j].fix(), o.map, coeffs[j]);
         ++size;
         map = build(comps);
         mpgb_train_result tr{};
@@ -644,7 +892,6 @@ std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& m
         if (testErr < best) {
             best = testErr;
             bestSets = mset0;
-            bestCoeffs = coeffs;
             patience = 0;
         }
         if (o.verbose)
@@ -652,12 +899,10 @@ std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& m
                         trainErr, testErr);
     }
 
-    // The best sets, trained once more.  The reference restarts them from zero
-    // coefficients; here they restart from the coefficients the search trained
-    // for them: from zero, terms of high order in the last input make the
-    // problem so badly scaled that L-BFGS (unlike NLopt's SLSQP) stalls.
+    // The best sets, trained from zero coefficients (src/TrainMapAdaptive.cpp:243-254).
     mset0 = bestSets;
-    for (unsigned j = 0; j < nOut; ++j) comps[j] = atmComponent(mset0[j], o.map, bestCoeffs[j]);
+    for (unsigned j = 0; j < nOut; ++j)
+        comps[j] = atmComponent(mset0[j].fix(), o.map, std::vector<double>(mset0[j].terms.size(), 0.0));
     map = build(comps);
     mpgb_train_result tr{};
     trainKL(*map, train, o.train, o.mode, s, nullptr, &tr);
@@ -729,6 +974,26 @@ int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* mult
     if (out) {
         if (cap_rows < rm.size()) throw std::invalid_argument("reduced margin: output too small");
         for (size_t k = 0; k < rm.size(); ++k) std::memcpy(out + k * dim, rm[k].data(), dim * sizeof(unsigned));
+    }
+    return MPGB_OK;
+}
+
+int expandImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_terms_out,
+               unsigned int* terms_out, unsigned int* n_idx_out, unsigned int* idx_out, unsigned int cap) {
+    AdaptiveSet s;
+    s.dim = dim;
+    for (unsigned t = 0; t < n; ++t) s.add(std::vector<unsigned>(multis + (size_t)t * dim, multis + (size_t)(t + 1) * dim));
+    const size_t n0 = s.terms.size();
+    const auto idx = s.expand();
+    const size_t nNew = s.terms.size() - n0;
+    if (n_terms_out) *n_terms_out = (unsigned)nNew;
+    if (n_idx_out) *n_idx_out = (unsigned)idx.size();
+    if (terms_out || idx_out) {
+        if (cap < nNew || cap < idx.size()) throw std::invalid_argument("Expand: output too small");
+        if (terms_out)
+            for (size_t k = 0; k < nNew; ++k) std::memcpy(terms_out + k * dim, s.terms[n0 + k].data(), dim * sizeof(unsigned));
+        if (idx_out)
+            for (size_t k = 0; k < idx.size(); ++k) idx_out[k] = (unsigned)idx[k];
     }
     return MPGB_OK;
 }

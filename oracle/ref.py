@@ -62,6 +62,7 @@ def lib():
         for f in ("ref_coeff_grad", "ref_gradient"):
             getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, C.c_long, _dp]
         L.ref_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, C.c_double, C.c_double, _dp]
+        L.ref_mset.argtypes = [C.c_uint, C.c_uint, _up, C.c_int, C.c_uint, _up, _up, _up, _up]
         _lib = L
     return _lib
 
@@ -163,3 +164,31 @@ class RefMap:
         self._check(lib().ref_inverse(self._h, x1.ctypes.data_as(_dp), x1.shape[0], r.ctypes.data_as(_dp), n,
                                       xtol, ytol, out.ctypes.data_as(_dp)))
         return out
+
+
+def _mset_call(terms, mode):
+    t = np.ascontiguousarray(np.asarray(terms, dtype=np.uint32).reshape(len(terms), -1))
+    dim = t.shape[1]
+    cap = 4 * (len(terms) + 1) * (dim + 1) + 64
+    out_t = np.zeros((cap, dim), dtype=np.uint32)
+    idx = np.zeros(cap, dtype=np.uint32)
+    nt, no = C.c_uint(), C.c_uint()
+    L = lib()
+    rc = L.ref_mset(dim, len(terms), t.ctypes.data_as(_up), mode, cap, out_t.ctypes.data_as(_up), C.byref(nt),
+                    idx.ctypes.data_as(_up), C.byref(no))
+    if rc != 0:
+        raise RuntimeError(L.ref_last_error().decode())
+    return out_t, nt.value, idx, no.value
+
+
+def mset_reduced_margin(terms):
+    """MultiIndexSet::ReducedMargin of the set built by += of terms in order."""
+    out_t, _, _, no = _mset_call(terms, 0)
+    return [tuple(int(v) for v in out_t[k]) for k in range(no)]
+
+
+def mset_expand(terms):
+    """MultiIndexSet::Expand of the set built by += of terms in order: (the
+    returned indices, the set's terms afterwards)."""
+    out_t, nt, idx, no = _mset_call(terms, 1)
+    return [int(v) for v in idx[:no]], [tuple(int(v) for v in out_t[k]) for k in range(nt)]

@@ -28,6 +28,7 @@
 #include "MParT/MapOptions.h"
 #include "MParT/MonotoneComponent.h"
 #include "MParT/MultiIndices/FixedMultiIndexSet.h"
+#include "MParT/MultiIndices/MultiIndexSet.h"
 #include "MParT/MultivariateExpansionWorker.h"
 #include "MParT/OrthogonalPolynomial.h"
 #include "MParT/PositiveBijectors.h"
@@ -274,6 +275,39 @@ int ref_inverse(void* h, const double* x1, long x1Rows, const double* r, long n,
         }
         for (unsigned k = 0; k < opdim; ++k)
             for (long i = 0; i < n; ++i) out[k * n + i] = full(extra + k, i);
+    });
+}
+
+// A MultiIndexSet built by += of the given terms in order (n rows of length
+// dim), then either its ReducedMargin() (mode 0: the terms, rows of length
+// dim, count in *nOut) or its Expand() (mode 1: the returned active indices in
+// idx, count in *nOut, and the set's terms after the expansion in terms, count
+// in *nTerms).  Outputs hold up to cap rows / entries.
+int ref_mset(unsigned dim, unsigned n, const unsigned* multis, int mode, unsigned cap, unsigned* terms,
+             unsigned* nTerms, unsigned* idx, unsigned* nOut) {
+    return guard([&] {
+        mpart::MultiIndexSet s(dim);
+        for (unsigned t = 0; t < n; ++t)
+            s += mpart::MultiIndex(std::vector<unsigned>(multis + (size_t)t * dim, multis + (size_t)(t + 1) * dim));
+        if (mode == 0) {
+            auto rm = s.ReducedMargin();
+            if (rm.size() > cap) throw std::runtime_error("ref_mset: output too small");
+            for (size_t k = 0; k < rm.size(); ++k) {
+                auto v = rm[k].Vector();
+                for (unsigned d = 0; d < dim; ++d) terms[k * dim + d] = v[d];
+            }
+            *nOut = (unsigned)rm.size();
+        } else {
+            auto ix = s.Expand();
+            if (ix.size() > cap || s.Size() > cap) throw std::runtime_error("ref_mset: output too small");
+            for (size_t k = 0; k < ix.size(); ++k) idx[k] = ix[k];
+            *nOut = (unsigned)ix.size();
+            for (unsigned k = 0; k < s.Size(); ++k) {
+                auto v = s.IndexToMulti(k).Vector();
+                for (unsigned d = 0; d < dim; ++d) terms[k * dim + d] = v[d];
+            }
+            *nTerms = s.Size();
+        }
     });
 }
 

@@ -44,10 +44,14 @@ def test_reduced_margin_matches_definition(M):
             assert len(rm) == len(set(rm))
             assert set(rm) == _brute_reduced_margin(s._terms, length)
             s += rm[rng.integers(len(rm))]  # stays downward closed
-    # scan order: terms in order, forward neighbours by increasing dimension
+    # the reference's order (entries by first appearance; Expand: the frontier's
+    # terms in order, each one's forward neighbours by first appearance, a term
+    # reached twice returned twice); tests/test_reference_pins.py checks it
+    # against the reference's MultiIndexSet on many sets
     s = M.MultiIndexSet.CreateTotalOrder(2, 1)
     assert [tuple(int(v) for v in m) for m in s.ReducedMargin()] == [(1, 1), (0, 2), (2, 0)]
-    assert s.Expand() == [3, 4, 5]
+    assert s.Expand() == [3, 4, 3, 5]
+    assert [tuple(int(v) for v in t) for t in s._terms][3:] == [(1, 1), (0, 2), (2, 0)]
 
 
 def test_option_defaults(M):

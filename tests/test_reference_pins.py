@@ -168,3 +168,41 @@ def test_nugget_enters_inverse_but_not_evaluate(oracle):
     xi = ref.inverse(np.zeros((0, 3)), y, 1e-12, 1e-12)
     same(xi, orc.inverse(coef, np.zeros((0, 3)), y, 1e-12, 1e-12), "Inverse")
     assert np.all(np.abs(xi - x) > 1e-3)
+
+
+def _grow(rng, length, steps, expand_every=0):
+    """A downward-closed set grown from a total-order set the way the adaptive
+    loop grows it: one reduced-margin term at a time (and, every expand_every
+    steps, a whole Expand)."""
+    import mpart_gb300 as M
+    s = M.MultiIndexSet.CreateTotalOrder(length, int(rng.integers(0, 3)))
+    sets = [list(s._terms)]
+    for k in range(steps):
+        if expand_every and k % expand_every == expand_every - 1:
+            s.Expand()
+        else:
+            rm = s.ReducedMargin()
+            s += rm[rng.integers(len(rm))]
+        sets.append(list(s._terms))
+    return sets
+
+
+def test_multi_index_set_order_matches_reference():
+    """MultiIndexSet::ReducedMargin and ::Expand, whose order decides which of
+    equal KL gradients TrainMapAdaptive picks, against the reference's own
+    MultiIndexSet on sets grown as the adaptive loop grows them: the same
+    terms in the same order, and Expand's returned indices (a term reached
+    from several frontier terms repeated) equal."""
+    import mpart_gb300 as M
+    rng = np.random.default_rng(5)
+    for length in (1, 2, 3, 4, 5):
+        for terms in _grow(rng, length, 10, expand_every=4):
+            s = M.MultiIndexSet(length, terms)
+            got_rm = [tuple(int(v) for v in m) for m in s.ReducedMargin()]
+            assert got_rm == R.mset_reduced_margin(terms), (length, terms)
+            ref_idx, ref_terms = R.mset_expand(terms)
+            got_idx = s.Expand()
+            assert got_idx == ref_idx, (length, terms)
+            assert [tuple(int(v) for v in t) for t in s._terms] == ref_terms
+    # the 2-D total-order-1 set: [1 1] is reached from [0 1] and [1 0]
+    assert R.mset_expand([(0, 0), (0, 1), (1, 0)])[0] == [3, 4, 3, 5]
