@@ -905,6 +905,14 @@ def run_gpu(args):
                      "flops_per_point": fpp, "evals_per_point": E},
         "clocks": clk.summary(),
     }
+    # Against the FP64 issue rate itself: 2 DFMA lanes per SM and clock (2
+    # FLOP each) at the SM clock sampled during the timed steps.
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = line["clocks"].get("sm_mhz") or line["clocks"].get("sm_max_mhz")
+    if mhz:
+        issue = sms * 2 * 2 * mhz * 1e6 / 1e12
+        line["roofline"]["issue_rate_peak"] = issue
+        line["roofline"]["frac_of_issue_rate"] = achieved / issue
     line["dense_coeff_grad"] = dense_coeff_grad(comp, x, s, N, dev)
     line["plain_path"] = plain_path(M, coef, x, s, N, dev)
     line["plain_path"]["fused_speedup"] = line["plain_path"]["ms_per_step"] / (t_step * 1e3)

@@ -54,8 +54,6 @@ struct Buf {
 // ---------------------------------------------------------------------------
 constexpr int kBuckets = 256;
 constexpr int kChunk = 1024;
-// Largest node cache of a batch launch (bytes).
-constexpr long long kBatchCacheBudget = 24LL << 30;
 
 struct SortSeg {
     const double* xd;
@@ -278,8 +276,6 @@ public:
             c.coeffOffset = (int)part.mapCoeffOffset; c.slotOffset = bc.slotOffset; c.cSegs = p.cSegs;
             c.nodeA = p.dNodeA; c.nodeSlot = p.dNodeSlot; c.nodeC = p.dNodeC; c.nodeCRows = p.dNodeCRows;
             c.slotTerm = p.dSlotTerm; c.leadDeg = p.dLeadDeg; c.rowOff = p.dRowOff;
-            c.nodeCIdx = p.dNodeCIdx;
-            maxCNodes_ = std::max(maxCNodes_, p.nCNodes);
             cd.push_back(c);
         }
         compDesc_.ensure(cd.size() * sizeof(CompDesc));
@@ -568,39 +564,9 @@ private:
         MPGB_CUDA(cudaMemsetAsync(counter_.p, 0, sizeof(int), s));
         FusedParams p = params();
         p.items = itemBuf_.as<WorkItem>();
-        nodeCache(p, (long long)items.size(), s);
         const size_t smem = fusedSmemBytes(tpb_, dmax_, nBmax_, depthMax_, pclass_, false);
         if (smem > 227 * 1024) throw std::invalid_argument("MapBatch: components too large for the shared-memory tile.");
         MPGB_CUDA(launchBatch(basis_, pos_, p, (int)items.size(), pclass_, counter_.as<int>(), s));
-    }
-
-    // Per-block node cache of the reduced adjoint: phase A keeps the prefix
-    // products of the deeper nodes (maxCNodes_ rows of tpb doubles per
-    // block) and the reduction reads them instead of forming them again --
-    // for the large components, tens of thousands of nodes a point, several
-    // multiplies per node.  Sized for the grid the launch uses (at most one
-    // block per item) within kBatchCacheBudget bytes
-    // and half the free device memory; the launch runs without it otherwise
-    // (or when its grid turns out larger).
-    void nodeCache(FusedParams& p, long long nItems, cudaStream_t s) {
-        p.rcache = nullptr;
-        p.rcBlockStride = p.rcCapacity = 0;
-        if (maxCNodes_ == 0) return;
-        const long long stride = (long long)maxCNodes_ * tpb_;
-        // (the batch kernel's register budget: 4 blocks an SM for order
-        // classes up to 4, 2 above)
-        const long long blocks = std::min<long long>(nItems, (pclass_ <= 4 ? 4LL : 2LL) * numSMs_);
-        const long long bytes = blocks * stride * (long long)sizeof(double);
-        if ((size_t)bytes > rcache_.n) {
-            size_t freeB = 0, totalB = 0;
-            MPGB_CUDA(cudaMemGetInfo(&freeB, &totalB));
-            if (bytes > kBatchCacheBudget || (size_t)bytes > (freeB + rcache_.n) / 2) return;
-            (void)s;
-            rcache_.ensure((size_t)bytes);
-        }
-        p.rcache = rcache_.as<double>();
-        p.rcBlockStride = stride;
-        p.rcCapacity = (long long)(rcache_.n / sizeof(double));
     }
 
     void finishOutputs(cudaStream_t s) {
@@ -697,11 +663,10 @@ private:
     int basis_ = 0, pos_ = 0;
     QuadParams quad_{};
     BasisConsts bc_{};
-    int dmax_ = 1, nBmax_ = 0, depthMax_ = 0, pclass_ = 2, totalSlots_ = 0, numSMs_ = 1, maxCNodes_ = 0;
+    int dmax_ = 1, nBmax_ = 0, depthMax_ = 0, pclass_ = 2, totalSlots_ = 0, numSMs_ = 1;
     int tpb_ = 128;
     std::map<std::pair<int, int>, int> tiles_;
     Buf gradScratch_;  // autotuning: coefficient adjoints of timed calls
-    Buf rcache_;       // per-block node cache of the reduced adjoint (nodeCache)
     std::vector<WorkItem> items_;
     std::vector<ReduceSeg> reduce_;
     std::vector<LogdetSeg> logdet_;

@@ -849,8 +849,7 @@ __global__ void __launch_bounds__(128, (MAXC <= 4) ? 4 : 2) batchKernel(const __
         const int k = next;
         __syncthreads();
         if (k >= nItems) break;
-        WorkItem item = prm.items[k];
-        item.rcBase = (long long)blockIdx.x * prm.rcBlockStride;
+        const WorkItem item = prm.items[k];
         const int P = prm.comps[item.c0].P;
         if (P <= 2) {
             fusedBody<BASIS, POS, 2, true, 0, true>(prm, item, smem);
@@ -1764,12 +1763,7 @@ cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int*
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&nSM, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     const int grid = std::max(1, std::min(nItems, std::max(1, perSM) * nSM));
-    FusedParams p = prm;
-    if (!p.rcache || p.rcBlockStride <= 0 || (long long)grid * p.rcBlockStride > p.rcCapacity) {
-        p.rcache = nullptr;
-        p.rcBlockStride = 0;
-    }
-    kern<<<grid, prm.tpb, smem, stream>>>(p, nItems, counter);
+    kern<<<grid, prm.tpb, smem, stream>>>(prm, nItems, counter);
     e = cudaGetLastError();
     countLaunches(stream, 1);
     return e;

@@ -124,11 +124,6 @@ struct FusedParams {
     // the reduction, nCNodes x blockDim doubles per item at WorkItem::rcBase
     // (null: the reduction evaluates the rectifier again).
     double* rcache;
-    // Persistent batch launches: each block keeps its node cache at
-    // rcache + blockIdx.x * rcBlockStride (the items it runs one after the
-    // other reuse it); the launch drops the cache when its grid needs more
-    // than rcCapacity doubles.
-    long long rcBlockStride, rcCapacity;
     // Optional: per point and component, the quadrature's interval count / 8
     // at costKey[c * costStride + i] (a sort key: the next call processes the
     // points in order of it).
