@@ -297,6 +297,9 @@ typedef struct mpgb_train_options {
     int memory;
     int mode;
     int algorithm;  /* MPGB_OPT_SLSQP (default) or MPGB_OPT_LBFGS */
+    int precondition; /* MPGB_OPT_LBFGS: 1 starts every iteration's inverse Hessian from the
+                         inverse of the mean squared per-point gradient of each coefficient at
+                         the starting coefficients (no counterpart in the reference) */
 } mpgb_train_options;
 
 typedef struct mpgb_train_result {
@@ -310,6 +313,13 @@ typedef struct mpgb_train_result {
 } mpgb_train_result;
 
 int mpgb_train_options_default(mpgb_train_options* opts);
+
+/* The optimisers of mpgb_train_map on host test problems (no GPU): problem 0 the
+ * extended Rosenbrock function from (-1.2, 1, ...) (n even), 1 the quadratic
+ * sum_i 10^(4i/(n-1)) (x_i - 1)^2 / 2 from 0.  diag_inverse (n entries or NULL)
+ * is the L-BFGS diagonal scaling.  Returns the final point, value and counts. */
+int mpgb_optimizer_self_test(int algorithm, int problem, int n, int max_iters, const double* diag_inverse,
+                             double* x_out, double* f_out, int* iterations, int* evaluations);
 
 /* TrainMap with a standard-normal KLObjective on a triangular map
  * (src/TrainMap.cpp:144-216): every component minimises its

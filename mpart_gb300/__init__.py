@@ -801,13 +801,15 @@ def CreateGaussianKLObjective(train, test=None, dim=0):
 
 
 def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, ftol_rel=0.0, ftol_abs=0.0,
-             xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0, algorithm="LD_SLSQP"):
+             xtol_rel=0.0, xtol_abs=0.0, gtol=0.0, memory=10, mode=0, algorithm="LD_SLSQP", precondition=False):
     """TrainMap(map, objective, options) (src/TrainMap.cpp:166-216) when samples
     is a KLObjective and max_iters a TrainOptions: returns the training objective.
 
     Otherwise the direct form: TrainMap with a standard-normal KL objective:
     every component minimises its reverse KL with `algorithm` ("LD_SLSQP" or
-    "LD_LBFGS", see TrainOptions); samples is a CUDA
+    "LD_LBFGS", see TrainOptions; with precondition, L-BFGS starts each
+    iteration's inverse Hessian from the inverse mean squared per-point
+    gradient of every coefficient at the start); samples is a CUDA
     float64 tensor, inputDim x N.  mode 0 replays one batched step from a CUDA
     graph, 1 launches it directly, 2 launches each component separately, 3 runs
     per component the reference objective's call sequence (Evaluate,
@@ -831,6 +833,7 @@ def TrainMap(tmap: ConditionalMapBase, samples, max_iters=100, max_evals=1000, f
     if algorithm not in algs:
         raise ValueError(f"algorithm {algorithm!r}: this library provides LD_SLSQP and LD_LBFGS")
     o.algorithm = algs[algorithm]
+    o.precondition = int(bool(precondition))
     loss = np.zeros(tmap.outputDim)
     r = mpgb_train_result()
     check(load().mpgb_train_map(tmap._h, _mat(samples), C.byref(o), C.c_void_p(loss.ctypes.data), C.byref(r),

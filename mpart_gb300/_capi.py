@@ -49,7 +49,7 @@ class mpgb_matrix(C.Structure):
 class mpgb_train_options(C.Structure):
     _fields_ = [("max_iters", C.c_int), ("max_evals", C.c_int), ("ftol_rel", C.c_double), ("ftol_abs", C.c_double),
                 ("xtol_rel", C.c_double), ("xtol_abs", C.c_double), ("gtol", C.c_double), ("memory", C.c_int),
-                ("mode", C.c_int), ("algorithm", C.c_int)]
+                ("mode", C.c_int), ("algorithm", C.c_int), ("precondition", C.c_int)]
 
 
 class mpgb_train_result(C.Structure):
@@ -126,6 +126,8 @@ SIGNATURES = {
                                           _MAPP, C.POINTER(mpgb_atm_result), _UP, C.c_void_p]),
     "mpgb_reduced_margin": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, C.c_uint]),
     "mpgb_multi_index_expand": (C.c_int, [C.c_uint, C.c_uint, _UP, _UP, _UP, _UP, _UP, C.c_uint]),
+    "mpgb_optimizer_self_test": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _DP, _DP, _DP, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int)]),
     "mpgb_component_multi_index": (C.c_int, [_MAP, _UP, _UP, _UP, _UP, _UP, _UP]),
     "mpgb_map_is_triangular": (C.c_int, [_MAP, C.POINTER(C.c_int)]),
     "mpgb_map_to_bytes": (C.c_int, [_MAP, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),

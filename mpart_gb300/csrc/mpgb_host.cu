@@ -1802,6 +1802,8 @@ int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* mult
                       unsigned int* out, unsigned int cap_rows);
 int expandImpl(unsigned int dim, unsigned int n, const unsigned int* multis, unsigned int* n_terms_out,
                unsigned int* terms_out, unsigned int* n_idx_out, unsigned int* idx_out, unsigned int cap);
+int optimizerSelfTestImpl(int algorithm, int which, int n, int maxIters, const double* dinv, double* xOut,
+                          double* fOut, int* itersOut, int* evalsOut);
 int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, double* ms_per_step, double* loss,
                    double* grad, void* stream, char* err, int errLen);
 }
@@ -2413,6 +2415,14 @@ int mpgb_reduced_margin(unsigned int dim, unsigned int n, const unsigned int* mu
     return guard([&] {
         if ((n && !multis) || dim == 0) throw std::invalid_argument("bad multi-index set");
         reducedMarginImpl(dim, n, multis, n_out, out, cap_rows);
+    });
+}
+
+int mpgb_optimizer_self_test(int algorithm, int problem, int n, int max_iters, const double* diag_inverse,
+                             double* x_out, double* f_out, int* iterations, int* evaluations) {
+    return guard([&] {
+        if (!x_out || !f_out || !iterations || !evaluations) throw std::invalid_argument("null output");
+        optimizerSelfTestImpl(algorithm, problem, n, max_iters, diag_inverse, x_out, f_out, iterations, evaluations);
     });
 }
 

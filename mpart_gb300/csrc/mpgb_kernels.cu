@@ -184,6 +184,27 @@ __global__ void denseKLReduceKernel(const double* T, const double* ld, const dou
     }
 }
 
+// Per term, the mean over points of the squared per-point KL gradient,
+// (dT_j - dL_j)^2 with the dense outputs of denseKLReduceKernel.
+__global__ void denseKLSquaresKernel(const double* dT, const double* dL, long long N, double invN, double* out) {
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    const double* a = dT + (long long)b * N;
+    const double* c = dL + (long long)b * N;
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+        const double g = a[i] - c[i];
+        s = fma(g, g, s);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[b] = red[0] * invN;
+}
+
 // FP64 peak probe: independent DFMA chains (8 per thread).
 __global__ void dfmaPeakKernel(double* out, int iters, double seed) {
     double x[8];
@@ -361,6 +382,15 @@ cudaError_t launchSortByLast(const double* xd, long long stride, long long N, in
     keyScatterKernel<<<nBlk, 32, 0, stream>>>(xd, stride, N, hist, perm);
     const cudaError_t e = cudaGetLastError();
     countLaunches(stream, 3);
+    return e;
+}
+
+cudaError_t launchDenseKLSquares(const double* dT, const double* dL, int nTerms, long long N, double* out,
+                                 cudaStream_t stream) {
+    if (nTerms <= 0 || N <= 0) return cudaSuccess;
+    denseKLSquaresKernel<<<nTerms, 256, 0, stream>>>(dT, dL, N, 1.0 / (double)N, out);
+    const cudaError_t e = cudaGetLastError();
+    countLaunches(stream, 1);
     return e;
 }
 

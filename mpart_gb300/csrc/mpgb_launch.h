@@ -42,6 +42,9 @@ cudaError_t launchSigmoidEval(const CompDesc& c, int maxOrder, const double* x, 
                               double* out, double* d1, double* d2, cudaStream_t stream);
 // Loss and gradient of the standard-normal reverse KL from dense outputs:
 // T, ld (N), dT = dT/dc scaled by T, dL = dlogdet/dc (nTerms x N, row-major).
+// Per term j of one component, mean_i (dT[j,i] - dL[j,i])^2 into out[j].
+cudaError_t launchDenseKLSquares(const double* dT, const double* dL, int nTerms, long long N, double* out,
+                                 cudaStream_t stream);
 cudaError_t launchDenseKLReduce(const double* T, const double* ld, const double* dT, const double* dL, int nTerms,
                                 long long N, double* loss, double* grad, cudaStream_t stream);
 

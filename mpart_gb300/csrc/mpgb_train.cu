@@ -41,6 +41,7 @@ struct TrainOpts {
     double ftolRel = 0.0, ftolAbs = 0.0, xtolRel = 0.0, xtolAbs = 0.0, gtol = 0.0;
     int memory = 10;
     int algorithm = MPGB_OPT_SLSQP;
+    bool precondition = false;  // L-BFGS: diagonal initial inverse Hessian from the squared per-point gradients
 };
 
 // NLopt's stopping test on one value: the change is below the absolute
@@ -205,7 +206,10 @@ private:
 // with a backtracking Armijo line search.
 class LBFGS : public Optimizer {
 public:
-    LBFGS(const double* x0, int n, const TrainOpts& o) : Optimizer(x0, n, o) {}
+    // dinv (optional, n entries): the diagonal of the initial inverse
+    // Hessian, scaled at every iteration by s'y / y'Dy of the newest pair.
+    LBFGS(const double* x0, int n, const TrainOpts& o, const double* dinv = nullptr)
+        : Optimizer(x0, n, o), dinv_(dinv ? std::vector<double>(dinv, dinv + n) : std::vector<double>()) {}
 
     void tell(double f, const double* g) override {
         ++evals_;
@@ -275,31 +279,42 @@ private:
             a[i] = rho_[i] * dot(S_[i], q);
             for (int j = 0; j < n_; ++j) q[j] -= a[i] * Y_[i][j];
         }
-        double gamma = 1.0;
-        if (m > 0) gamma = dot(S_[m - 1], Y_[m - 1]) / dot(Y_[m - 1], Y_[m - 1]);
-        for (int j = 0; j < n_; ++j) q[j] *= gamma;
+        if (dinv_.empty()) {
+            double gamma = 1.0;
+            if (m > 0) gamma = dot(S_[m - 1], Y_[m - 1]) / dot(Y_[m - 1], Y_[m - 1]);
+            for (int j = 0; j < n_; ++j) q[j] *= gamma;
+        } else {
+            double gamma = 1.0;
+            if (m > 0) {
+                double yDy = 0;
+                for (int j = 0; j < n_; ++j) yDy += Y_[m - 1][j] * dinv_[j] * Y_[m - 1][j];
+                gamma = dot(S_[m - 1], Y_[m - 1]) / yDy;
+            }
+            for (int j = 0; j < n_; ++j) q[j] *= gamma * dinv_[j];
+        }
         for (int i = 0; i < m; ++i) {
             const double b = rho_[i] * dot(Y_[i], q);
             for (int j = 0; j < n_; ++j) q[j] += S_[i][j] * (a[i] - b);
         }
         d_.resize(n_);
         for (int j = 0; j < n_; ++j) d_[j] = -q[j];
-        if (dot(d_, g_) >= 0) {  // not a descent direction: restart from steepest descent
+        if (dot(d_, g_) >= 0) {  // not a descent direction: restart from the (scaled) steepest descent
             S_.clear(); Y_.clear(); rho_.clear();
-            for (int j = 0; j < n_; ++j) d_[j] = -g_[j];
+            for (int j = 0; j < n_; ++j) d_[j] = -g_[j] * (dinv_.empty() ? 1.0 : dinv_[j]);
         }
         alpha_ = 1.0;
         if (first || S_.empty()) {
-            double gn = 0;
-            for (double v : g_) gn = std::max(gn, std::fabs(v));
-            alpha_ = gn > 0 ? std::min(1.0, 1.0 / gn) : 1.0;
+            // no curvature pair yet: no coefficient moves by more than 1
+            double dn = 0;
+            for (double v : d_) dn = std::max(dn, std::fabs(v));
+            alpha_ = dn > 0 ? std::min(1.0, 1.0 / dn) : 1.0;
         }
         gPrevDir_ = g_;
         backtracks_ = 0;
         for (int i = 0; i < n_; ++i) trial_[i] = x_[i] + alpha_ * d_[i];
     }
 
-    std::vector<double> d_, gPrevDir_;
+    std::vector<double> d_, gPrevDir_, dinv_;
     double alpha_ = 1;
     std::vector<std::vector<double>> S_, Y_;
     std::vector<double> rho_;
@@ -307,8 +322,8 @@ private:
     int backtracks_ = 0;
 };
 
-std::unique_ptr<Optimizer> makeOptimizer(const double* x0, int n, const TrainOpts& o) {
-    if (o.algorithm == MPGB_OPT_LBFGS) return std::unique_ptr<Optimizer>(new LBFGS(x0, n, o));
+std::unique_ptr<Optimizer> makeOptimizer(const double* x0, int n, const TrainOpts& o, const double* dinv) {
+    if (o.algorithm == MPGB_OPT_LBFGS) return std::unique_ptr<Optimizer>(new LBFGS(x0, n, o, dinv));
     if (o.algorithm == MPGB_OPT_SLSQP) return std::unique_ptr<Optimizer>(new SLSQPU(x0, n, o));
     throw std::invalid_argument("TrainMap: unknown optimisation algorithm.");
 }
@@ -439,6 +454,41 @@ struct KLStep {
 
 namespace mpgb {
 
+// The inverse of the mean squared per-point KL gradient of every coefficient
+// at the map's coefficients, 1 / (mean_i (d l_i / d c_j)^2 + eps), eps a
+// 1e-10 fraction of the component's largest mean: a diagonal scaling that
+// puts coefficients whose terms differ in magnitude by orders of magnitude
+// (high-order Hermite terms) on one footing for L-BFGS.  One pass of the
+// reference objective's call sequence with dense outputs per component.
+std::vector<double> inverseFisherDiagonal(MonotoneMapBase& map, StridedMatrix const& pts, cudaStream_t s) {
+    size_t maxTerms = 1;
+    for (auto& p : map.Parts()) {
+        if (!dynamic_cast<MonotoneMapBase*>(p.owner) || p.owner->numCoeffs != (unsigned)p.prog->numTerms)
+            throw std::invalid_argument("TrainMap: preconditioning needs a map made of monotone components.");
+        maxTerms = std::max<size_t>(maxTerms, p.prog->numTerms);
+    }
+    const size_t n = (size_t)pts.cols;
+    Dev T(n), Ld(n), DT(maxTerms * n), DL(maxTerms * n), loss(map.outputDim), grad(map.numCoeffs), sq(map.numCoeffs);
+    const auto& parts = map.Parts();
+    for (size_t c = 0; c < parts.size(); ++c) {
+        map.KLObjectiveCalls(pts, loss.p, grad.p, (int)c, T.p, Ld.p, DT.p, DL.p, s);
+        TR_CUDA(launchDenseKLSquares(DT.p, DL.p, parts[c].prog->numTerms, (long long)n, sq.p + parts[c].mapCoeffOffset,
+                                     s));
+    }
+    std::vector<double> d(map.numCoeffs);
+    TR_CUDA(cudaMemcpyAsync(d.data(), sq.p, d.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TR_CUDA(cudaStreamSynchronize(s));
+    map.CheckStatus(s);
+    for (size_t c = 0; c < parts.size(); ++c) {
+        const size_t off = parts[c].mapCoeffOffset, nt = parts[c].prog->numTerms;
+        double mx = 0;
+        for (size_t j = off; j < off + nt; ++j) mx = std::max(mx, d[j]);
+        const double eps = mx > 0 ? 1e-10 * mx : 1.0;
+        for (size_t j = off; j < off + nt; ++j) d[j] = 1.0 / (d[j] + eps);
+    }
+    return d;
+}
+
 // Standard-normal KL training of every component (src/TrainMap.cpp:144-164):
 // lockstep optimisers, one per component, over one batched objective step
 // per iteration.  Throws; sets the map's coefficients to the result.
@@ -451,13 +501,15 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
     }
     const auto& parts = map.Parts();
     std::vector<double> x0 = map.CoeffMap();
+    std::vector<double> dinv;
+    if (o.precondition && o.algorithm == MPGB_OPT_LBFGS) dinv = inverseFisherDiagonal(map, pts, s);
     KLStep step(map, pts, s, mode);
     std::vector<std::unique_ptr<Optimizer>> opt;
     for (auto& p : parts)
         opt.push_back(makeOptimizer(x0.data() + p.mapCoeffOffset,
                                     (int)((&p == &parts.back() ? map.numCoeffs : (&p + 1)->mapCoeffOffset) -
                                           p.mapCoeffOffset),
-                                    o));
+                                    o, dinv.empty() ? nullptr : dinv.data() + p.mapCoeffOffset));
     int steps = 0;
     double stepMs = 0.0;
     cudaEvent_t e0, e1;
@@ -528,6 +580,7 @@ TrainOpts trainOptsFromC(const mpgb_train_options* opts) {
     o.gtol = opts->gtol;
     o.memory = opts->memory > 0 ? opts->memory : 10;
     o.algorithm = opts->algorithm;
+    o.precondition = opts->precondition != 0;
     if (o.algorithm != MPGB_OPT_SLSQP && o.algorithm != MPGB_OPT_LBFGS)
         throw std::invalid_argument("TrainOptions: algorithm must be MPGB_OPT_SLSQP or MPGB_OPT_LBFGS.");
     return o;
@@ -975,6 +1028,49 @@ int reducedMarginImpl(unsigned int dim, unsigned int n, const unsigned int* mult
         if (cap_rows < rm.size()) throw std::invalid_argument("reduced margin: output too small");
         for (size_t k = 0; k < rm.size(); ++k) std::memcpy(out + k * dim, rm[k].data(), dim * sizeof(unsigned));
     }
+    return MPGB_OK;
+}
+
+// The optimisers on host test functions: 0 the extended Rosenbrock function
+// sum_i 100 (x_{2i+1} - x_{2i}^2)^2 + (1 - x_{2i})^2 from (-1.2, 1, ...),
+// 1 the quadratic sum_i 10^(4 i / (n - 1)) (x_i - 1)^2 / 2 from 0 (condition
+// number 10^4).  Returns the final point, objective and counts.
+int optimizerSelfTestImpl(int algorithm, int which, int n, int maxIters, const double* dinv, double* xOut,
+                          double* fOut, int* itersOut, int* evalsOut) {
+    if (n < 2 || (which == 0 && n % 2) || which < 0 || which > 1) throw std::invalid_argument("bad test problem");
+    TrainOpts o;
+    o.algorithm = algorithm;
+    o.maxIters = maxIters;
+    o.maxEvals = 20 * maxIters;
+    o.gtol = 1e-10;
+    std::vector<double> x0(n);
+    for (int i = 0; i < n; ++i) x0[i] = which == 0 ? ((i % 2) ? 1.0 : -1.2) : 0.0;
+    auto opt = makeOptimizer(x0.data(), n, o, dinv);
+    std::vector<double> g(n);
+    while (!opt->done()) {
+        const auto& x = opt->request();
+        double f = 0;
+        std::fill(g.begin(), g.end(), 0.0);
+        if (which == 0) {
+            for (int i = 0; i < n; i += 2) {
+                const double a = x[i + 1] - x[i] * x[i], b = 1.0 - x[i];
+                f += 100.0 * a * a + b * b;
+                g[i] += -400.0 * a * x[i] - 2.0 * b;
+                g[i + 1] += 200.0 * a;
+            }
+        } else {
+            for (int i = 0; i < n; ++i) {
+                const double w = std::pow(10.0, 4.0 * i / (n - 1)), d = x[i] - 1.0;
+                f += 0.5 * w * d * d;
+                g[i] = w * d;
+            }
+        }
+        opt->tell(f, g.data());
+    }
+    std::memcpy(xOut, opt->x().data(), n * sizeof(double));
+    *fOut = opt->f();
+    *itersOut = opt->iterations();
+    *evalsOut = opt->evaluations();
     return MPGB_OK;
 }
 
