@@ -524,6 +524,38 @@ def flops_per_point(evals_per_point):
         (sc + 2 * T)
 
 
+def reference_flops_per_point(evals_per_point):
+    """FP64 flops per point of the reference's own (unfactored) algorithm for
+    the same fused step, counted from its term loops
+    (MultivariateExpansionWorker.h, MonotoneIntegrand.h, MonotoneComponent.h):
+    per integrand node with the coefficient gradient (the Parameters part)
+      2 sum_{t with x_D} k_t   term products and coefficient FMAs of d_D f
+      + 3 (p_D + 1)            last-coordinate recurrence and its derivative
+      + 20                     g, g', weights, accumulation
+      + 3 T_D                  scale and coarse/fine sums per gradient entry
+    and per point once
+      3 sum_{d < D} (p_d + 1)  leading-coordinate recurrences
+      + 2 sum_t k_t + T        f(x_<D, 0) and its coefficient gradient,
+    with k_t the nonzero factors of term t, T_D the terms that contain x_D,
+    transcendentals at 1.  The fused kernel computes the same quantities
+    with fewer operations (prefix products, a_k sums), so this count divided
+    by the step time exceeds the FP64 peak; it says how much arithmetic the
+    factoring removes, not how busy the pipe is."""
+    from mpart_gb300 import FixedMultiIndexSet
+    ms = FixedMultiIndexSet(DIM, ORDER)
+    ks, kd, td = 0, 0, 0
+    for t in range(ms.Size()):
+        m = ms.IndexToMulti(t)
+        k = sum(1 for v in m if v > 0)
+        ks += k
+        if m[-1] > 0:
+            kd += k
+            td += 1
+    node = 2 * kd + 3 * (ORDER + 1) + 20 + 3 * td
+    fixed = 3 * (DIM - 1) * (ORDER + 1) + 2 * ks + ms.Size()
+    return evals_per_point * node + fixed
+
+
 def mean_evals(sample=20000):
     """Mean integrand evaluations per point from the oracle's node counts (the
     GPU follows the same subdivision tree)."""
@@ -912,7 +944,12 @@ def run_gpu(args):
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf, "traffic": traffic,
                      "peak_source": "DFMA probe in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                     "flops_per_point": fpp, "evals_per_point": E},
+                     "flops_per_point": fpp, "evals_per_point": E,
+                     "reference_algorithm": {
+                         "flops_per_point": reference_flops_per_point(E),
+                         "equivalent_tflops": reference_flops_per_point(E) * N / t_step / 1e12,
+                         "note": "flops of the reference's unfactored term loops for the same outputs; "
+                                 "above the FP64 peak because the fused kernel needs fewer"}},
         "clocks": clk.summary(),
     }
     # Against the FP64 issue rate itself: 2 DFMA lanes per SM and clock (2

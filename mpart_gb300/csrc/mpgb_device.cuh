@@ -35,6 +35,8 @@ constexpr int kMaxSubCap = 32;
 // built for; reduced launches cut each component into this many work items
 // per SM.
 constexpr int kFusedBlocksPerSM = 4;
+// Inverse: doubles of a saved root-solver state (RootSolve::save).
+constexpr int kSolveStateDoubles = 14;
 // Inverse warp pass: lanes per deferred point (32 / kWarpGroup points per warp).
 constexpr int kWarpGroup = 8;
 // Largest nested Clenshaw-Curtis level (coarse 2^L+1, fine 2^(L+1)+1 points).

@@ -333,6 +333,7 @@ struct MapWorkspace {
     DevBuf inverseA;     // inverse: a_k of the component being solved, (pmax + 1) x N
     DevBuf inverseList;  // inverse: points left to the warp pass
     DevBuf inverseStack; // inverse: the warp pass's interval stacks
+    DevBuf inverseState; // inverse: solver states of the points left to the warp pass
     DevBuf klT, klLd, klDT, klDL;  // KLObjectiveCalls scratch (nonzero nugget)
     bool ordering = true;
 };
@@ -1050,6 +1051,10 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
         W.inverseList.ensure((size_t)N * sizeof(int), stream);
         const int warpBlocks = kWarpPassBlocksPerSM * W.numSMs;
         W.inverseStack.ensure((size_t)warpBlocks * (128 / kWarpGroup) * kWarpStackCap * sizeof(QEntry), stream);
+        // Saved solver states for up to a quarter of the points (deferred
+        // points beyond it start their solves again).
+        const int stateCap = (int)std::min<long long>(N, N / 4 + 1024);
+        W.inverseState.ensure((size_t)stateCap * kSolveStateDoubles * sizeof(double), stream);
         int* counters = W.inverseDefer.as<int>();  // [queue pass, deferred count, warp pass, queue drained]
         for (int c = 0; c < p.nComps; ++c) {
             InverseParams k = p;
@@ -1076,6 +1081,8 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
             q.deferList = W.inverseList.as<int>();
             q.deferCount = counters + 1;
             q.drained = counters + 3;
+            q.deferState = W.inverseState.as<double>();
+            q.deferStateCap = stateCap;
             MPGB_CUDA(launchInverse(W.basis, posCode(opts_), W.pmax, q, nBlocks, stream));
             // The deferred points, kWarpGroup lanes each.
             InverseParams wp = q;

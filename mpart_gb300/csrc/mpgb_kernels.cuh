@@ -994,6 +994,18 @@ struct RootSolve {
         info = 0;
         x = x0;
     }
+    // The state as kSaveDoubles doubles (a deferred solve continues from it).
+    static constexpr int kSaveDoubles = kSolveStateDoubles;
+    __device__ void save(double* d) const {
+        d[0] = (double)phase; d[1] = (double)dir; d[2] = (double)info; d[3] = (double)it;
+        d[4] = x; d[5] = xlb; d[6] = ylb; d[7] = xub; d[8] = yub; d[9] = step;
+        d[10] = width; d[11] = widthPrev; d[12] = result; d[13] = nhalf;
+    }
+    __device__ void load(const double* d) {
+        phase = (int)d[0]; dir = (int)d[1]; info = (int)d[2]; it = (unsigned)d[3];
+        x = d[4]; xlb = d[5]; ylb = d[6]; xub = d[7]; yub = d[8]; step = d[9];
+        width = d[10]; widthPrev = d[11]; result = d[12]; nhalf = d[13];
+    }
     __device__ void finish(double r, int inf) {
         result = r;
         info = inf;
@@ -1366,8 +1378,8 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         const double h = V.h;
         // An expensive solve -- a quadrature wider than wideQuad intervals
         // (a far iterate) or a solve longer than nodeBudget nodes -- is left
-        // to the warp pass, which solves it again from the start with 32
-        // lanes per quadrature.
+        // to the warp pass, which continues it with kWarpGroup lanes per
+        // quadrature.
         // Once the queue is empty, solves past kDrainNodes nodes go too: the
         // warp pass runs them side by side, kWarpGroup lanes each, instead
         // of one lane each in a few warps.
@@ -1375,7 +1387,11 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         const bool drainedNow = prm.drained && (nodes & 63) == 0 && nodes >= kDrainNodes &&
                                 *(volatile int*)prm.drained != 0;
         if (prm.nodeBudget > 0 && (nodes > prm.nodeBudget || nInt >= prm.wideQuad || drainedNow)) {
-            prm.deferList[atomicAdd(prm.deferCount, 1)] = (int)i;
+            // The solver's state as of the current quadrature's start goes
+            // with the point (its earlier steps are not repeated).
+            const int slot = atomicAdd(prm.deferCount, 1);
+            prm.deferList[slot] = (int)i;
+            if (prm.deferState && slot < prm.deferStateCap) rs.save(prm.deferState + (long long)slot * RootSolve::kSaveDoubles);
             have = false;
             need = true;
             continue;
@@ -1465,7 +1481,8 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
 }
 
 // Inverse of the points the queue pass left over (deferList), one group of
-// G lanes per point (G = kWarpGroup; 32 / G points per warp).  The solver
+// G lanes per point (G = kWarpGroup; 32 / G points per warp), each solve
+// continuing from the state the queue pass saved for it (deferState).  The solver
 // state is the same in every lane of a group; each quadrature of T is shared
 // by the group's lanes: the pending intervals live on a per-group stack in
 // global scratch (prm.stack, the leftmost on top), each round the lanes take
@@ -1552,7 +1569,8 @@ __global__ void __launch_bounds__(128) inverseWarpKernel(const __grid_constant__
         int dummy = 0;
         const InverseEval<BASIS, POS, PMAX> f{A, P, f0, &prm.quad, &prm.bc, nugget, &dummy};
         RootSolve rs;
-        rs.start(x0);
+        if (prm.deferState && k < prm.deferStateCap) rs.load(prm.deferState + (long long)k * RootSolve::kSaveDoubles);
+        else rs.start(x0);
         while (rs.phase != RootSolve::kDone) {
             const double xd = rs.x;
             // T(x) - f0: the quadrature of x (g(df(t x)) + nugget) over t in [0, 1].

@@ -192,11 +192,16 @@ struct InverseParams {
     // Queue pass: a point whose solve takes more than nodeBudget integrand
     // nodes, or one of whose quadratures reaches wideQuad intervals, is left
     // to the warp pass: its index goes to deferList[atomicAdd(deferCount, 1)]
-    // (nodeBudget 0: no limit).
+    // and its solver state to deferState (nodeBudget 0: no limit).
     int nodeBudget;
     int wideQuad;
     int* deferList;
     int* drained;  // set (to 1) by the first lane that finds the queue empty; zero on entry
+    // The solver state of deferred point slot k (k < deferStateCap) at
+    // deferState + k * RootSolve::kSaveDoubles; the warp pass continues from
+    // it (null, or a slot past the cap: it starts the solve again).
+    double* deferState;
+    int deferStateCap;
     // Warp pass (warpPass = 1): one group of kWarpGroup lanes per point of
     // deferList (*listCount of them, taken through *queue), the lanes sharing
     // each adaptive quadrature; stack: stackCap entries of scratch per group

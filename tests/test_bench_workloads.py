@@ -58,3 +58,18 @@ def test_inverse_and_sigmoid_workloads():
     assert (bench.SIG_DIM, bench.SIG_ORDER, bench.SIG_NSIG, bench.SIG_N) == (8, 3, 5, 1_000_000)
     c = bench.sigmoid_centers(5)
     assert len(c) == 2 + 15 and np.all(np.isfinite(c))  # two edge terms, then 1 + 2 + ... + 5 centers
+
+
+def test_reference_flop_model():
+    """The reference-algorithm count: dim 8, order 4 has 495 terms, 165 of
+    them with x_D; per node 2 sum k_t (x_D terms) + 15 + 20 + 3 * 165."""
+    from mpart_gb300 import FixedMultiIndexSet
+    ms = FixedMultiIndexSet(bench.DIM, bench.ORDER)
+    terms = [ms.IndexToMulti(t) for t in range(ms.Size())]
+    kd = sum(sum(1 for v in m if v > 0) for m in terms if m[-1] > 0)
+    ks = sum(sum(1 for v in m if v > 0) for m in terms)
+    assert sum(1 for m in terms if m[-1] > 0) == 165
+    node = 2 * kd + 15 + 20 + 3 * 165
+    fixed = 3 * 7 * 5 + 2 * ks + 495
+    assert bench.reference_flops_per_point(10.0) == 10 * node + fixed
+    assert bench.reference_flops_per_point(10.0) > 5 * bench.flops_per_point(10.0)
