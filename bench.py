@@ -49,17 +49,20 @@ METRIC = "fused fwd+adjoint points/s (dim-8, order-4, FP64)"
 KL_DIM, KL_ORDER, KL_N, KL_TOL = 6, 5, 200_000, 1e-7
 # Training to convergence: L-BFGS with the diagonal preconditioner (the
 # inverse mean squared per-point gradient of every coefficient at the start)
-# until the gradient norm over all components is below KL_GTOL, at most
-# KL_MAX_ITERS iterations.  Without the preconditioner the high-order Hermite
-# terms make the problem so badly scaled that L-BFGS needs thousands of
-# iterations (3000 reach a gradient norm of 5.7, the preconditioned run 0.3 in
-# 1000).  SLSQP from zero did not finish 100 iterations in 15 minutes: its
-# trial steps (the first is the full negative gradient) make the integrand so
-# steep that the adaptive quadrature's cost per step grows by orders of
-# magnitude.
-KL_GTOL, KL_MAX_ITERS = 0.5, 3000
+# until an iteration changes a component's objective by less than KL_FTOL_REL
+# relative (NLopt's ftol_rel rule), at most KL_MAX_ITERS iterations.  The
+# gradient norm is reported but is no stopping rule here: the problem is so
+# ill-conditioned that a component's gradient norm falls below 0.05 while its
+# objective is still 0.05 above the optimum.  Without the preconditioner
+# L-BFGS needs thousands of iterations (3000 reach 0.290, the preconditioned
+# run 0.2746 in 1000).  SLSQP from zero did not finish 100 iterations in 15
+# minutes: its trial steps (the first is the full negative gradient) make the
+# integrand so steep that the adaptive quadrature's cost per step grows by
+# orders of magnitude.
+KL_FTOL_REL, KL_MAX_ITERS = 1e-7, 3000
 KL_ALG = "LD_LBFGS"
-KL_TRAIN = dict(max_iters=KL_MAX_ITERS, max_evals=3 * KL_MAX_ITERS, gtol=KL_GTOL, algorithm=KL_ALG, precondition=True)
+KL_TRAIN = dict(max_iters=KL_MAX_ITERS, max_evals=3 * KL_MAX_ITERS, ftol_rel=KL_FTOL_REL, algorithm=KL_ALG,
+                precondition=True)
 # CPU legs run in a child process on the oracle's timing build (the same
 # source with the compiler's default floating-point contraction, -O3
 # -fopenmp) with the threads bound one per core.
@@ -122,15 +125,17 @@ def kl_train(M, dev):
         "grad_max_abs_diff_over_max_per_component_fused": float(np.abs(steps[2][2] - steps[0][2]).max() / gscale),
     }
 
-    tm.SetCoeffs(np.zeros(tm.numCoeffs))
-    loss_p, r_p = M.TrainMap(tm, X, mode=2, **KL_TRAIN)
+    # (one fused launch set per component trains bitwise as the batched step
+    # does, checked by the tests; the reference call sequence sums in another
+    # order)
     tm.SetCoeffs(np.zeros(tm.numCoeffs))
     loss_r, r_r = M.TrainMap(tm, X, mode=3, **KL_TRAIN)
     return {
         "workload": f"TriangularMap {KL_DIM}-D, total order {KL_ORDER} ({tm.numCoeffs} coefficients), "
                     f"HermiteFunctions + Exp, ACC tol {KL_TOL}, {KL_N} banana samples, standard-normal KL, "
-                    f"L-BFGS with a diagonal preconditioner from zero coefficients to a gradient norm below "
-                    f"{KL_GTOL} (at most {KL_MAX_ITERS} iterations)",
+                    f"L-BFGS with a diagonal preconditioner from zero coefficients until an iteration changes "
+                    f"each component's objective by less than {KL_FTOL_REL} relative (at most {KL_MAX_ITERS} "
+                    f"iterations)",
         "objective": float(r_g["total_loss"]), "objective_per_component": [float(v) for v in loss_g],
         "grad_norm": float(r_g["grad_norm"]), "iterations": int(r_g["iterations"]),
         "steps": int(r_g["steps"]), "train_ms_per_step": float(r_g["ms_per_step"]),
@@ -140,9 +145,10 @@ def kl_train(M, dev):
         "batched_speedup_vs_reference_calls": ms[3] / ms[0],
         "batched_speedup_vs_per_component_fused": ms[2] / ms[0],
         "step_values_at_trained_coeffs": step_diff,
-        "train_objective_max_rel_diff_vs_per_component_fused": rel(loss_g, loss_p),
-        "train_objective_max_rel_diff_vs_reference_calls": rel(loss_g, loss_r),
+        "train_objective_reference_calls": float(r_r["total_loss"]),
+        "train_objective_max_abs_diff_vs_reference_calls": float(np.max(np.abs(loss_g - loss_r))),
         "train_objective_per_component_reference_calls": [float(v) for v in loss_r],
+        "reference_calls_train_iterations": int(r_r["iterations"]),
         "reference_calls_train_ms_per_step": float(r_r["ms_per_step"]),
     }, trained
 

@@ -30,7 +30,7 @@ def test_c2_workload_and_flop_model():
 
 def test_kl_workload_banana():
     assert (bench.KL_DIM, bench.KL_ORDER, bench.KL_N, bench.KL_TOL) == (6, 5, 200_000, 1e-7)
-    assert bench.KL_TRAIN["precondition"] and bench.KL_TRAIN["algorithm"] == "LD_LBFGS" and bench.KL_GTOL > 0
+    assert bench.KL_TRAIN["precondition"] and bench.KL_TRAIN["algorithm"] == "LD_LBFGS" and bench.KL_FTOL_REL > 0
     x = bench.banana(200_000)
     assert x.shape == (6, 200_000)
     assert abs(x[0].mean()) < 0.01 and abs(x[0].std() - 1.0) < 0.01
