@@ -35,6 +35,9 @@ constexpr int kMaxSubCap = 32;
 // built for; reduced launches cut each component into this many work items
 // per SM.
 constexpr int kFusedBlocksPerSM = 4;
+// Largest phase-A staging (coefficient doubles plus table words) a fused
+// launch keeps in shared memory.
+constexpr int kStageCap = 2048;
 // Inverse: doubles of a saved root-solver state (RootSolve::save).
 constexpr int kSolveStateDoubles = 14;
 // Inverse warp pass: lanes per deferred point (32 / kWarpGroup points per warp).
@@ -129,6 +132,22 @@ __device__ __forceinline__ void accumCoeffs(int nk, double phi, const double* __
 #define MPGB_ACC_CASE(K) \
     case K + 1:          \
         if constexpr (K <= PMAX) acc[K] = fma(__ldg(&cs[K]), phi, acc[K]); \
+        [[fallthrough]];
+        MPGB_ACC_CASE(12) MPGB_ACC_CASE(11) MPGB_ACC_CASE(10) MPGB_ACC_CASE(9) MPGB_ACC_CASE(8)
+        MPGB_ACC_CASE(7) MPGB_ACC_CASE(6) MPGB_ACC_CASE(5) MPGB_ACC_CASE(4) MPGB_ACC_CASE(3)
+        MPGB_ACC_CASE(2) MPGB_ACC_CASE(1) MPGB_ACC_CASE(0)
+#undef MPGB_ACC_CASE
+        default: break;
+    }
+}
+
+// accumCoeffs with the coefficients in shared memory.
+template <int PMAX>
+__device__ __forceinline__ void accumCoeffsShared(int nk, double phi, const double* cs, double* acc) {
+    switch (nk) {
+#define MPGB_ACC_CASE(K) \
+    case K + 1:          \
+        if constexpr (K <= PMAX) acc[K] = fma(cs[K], phi, acc[K]); \
         [[fallthrough]];
         MPGB_ACC_CASE(12) MPGB_ACC_CASE(11) MPGB_ACC_CASE(10) MPGB_ACC_CASE(9) MPGB_ACC_CASE(8)
         MPGB_ACC_CASE(7) MPGB_ACC_CASE(6) MPGB_ACC_CASE(5) MPGB_ACC_CASE(4) MPGB_ACC_CASE(3)

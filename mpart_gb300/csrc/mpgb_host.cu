@@ -322,6 +322,8 @@ struct MapWorkspace {
     QuadParams quad{};
     BasisConsts bc{};
     int pmax = 1, dmax = 1, nBmax = 0, depthMax = 0;
+    int stageNeed = 0;  // doubles of the largest phase-A staging among the monotone components (<= kStageCap)
+    int smemPerSM = 0;
     int basis = 0;  // kernel family: the options' basis, or kBasisSigmoid
     bool built = false;
     std::vector<std::unique_ptr<KLPlan>> klPlans;
@@ -594,7 +596,9 @@ void MonotoneMapBase::Prepare(cudaStream_t stream) {
             W.dmax = std::max(W.dmax, p.D);
             W.nBmax = std::max(W.nBmax, p.nB);
             W.depthMax = std::max(W.depthMax, p.maxDepth);
+            if (p.kind == 0 && p.nSlots + p.nNodes <= kStageCap) W.stageNeed = std::max(W.stageNeed, p.nSlots + p.nNodes);
         }
+        MPGB_CUDA(cudaDeviceGetAttribute(&W.smemPerSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
         W.totalSlots = slotOff;
         W.pmax = instantiatedPmax(pm);
         bool anySig = false, anyMono = false;
@@ -831,12 +835,23 @@ static void orderPoints(MapWorkspace& W, const std::vector<MonotoneMapBase::Part
     p.permStride = N;
 }
 
+// Phase A's inputs are staged in shared memory (FusedParams::stageDoubles)
+// when the staging does not lower the number of blocks an SM holds.
+static int stageDoubles(const MapWorkspace& W, const FusedParams& p, bool input) {
+    if (W.stageNeed == 0 || W.smemPerSM <= 0) return 0;
+    const size_t base = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, input) + 1024;
+    const size_t with = base + (size_t)W.stageNeed * sizeof(double);
+    auto blocks = [&](size_t b) { return std::min<size_t>(kFusedBlocksPerSM, (size_t)W.smemPerSM / b); };
+    return (with <= 227 * 1024 && blocks(with) == blocks(base)) ? W.stageNeed : 0;
+}
+
 static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nItems, int needJ, int needE,
                    cudaStream_t stream) {
     p.items = W.items.as<WorkItem>();
     if (nItems == 0) return;
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, (p.flags & kFlagInput) != 0);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
+    p.stageDoubles = stageDoubles(W, p, (p.flags & kFlagInput) != 0);
     // contDeriv = false: log-determinants and their coefficient adjoints come
     // from the quadrature's x_D-derivative (the kernel variant NEEDE = 2).
     if (!o.contDeriv && ((p.flags & (kFlagLogDet | kFlagCoefDenseL | kFlagKL)) ||
@@ -1415,6 +1430,7 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
     }
     const size_t smem = fusedSmemBytes(p.tpb, p.dmax, p.nBmax, p.depthMax, W.pmax, false);
     if (smem > 227 * 1024) throw std::invalid_argument("Component too large for the shared-memory tile.");
+    p.stageDoubles = stageDoubles(W, p, false);
     MPGB_CUDA(launchFused(W.basis, posCode(opts_), W.pmax, p, P.nItems, 1, opts_.contDeriv ? 0 : 2, stream));
     MPGB_CUDA(launchKLReduce(W.partials.as<double>(), P.rowBase.as<long long>(), P.reduceDesc.as<KLReduceDesc>(),
                              P.nReduce, P.maxTerms, grad, W.lossPart.as<double>(), P.lossSlots.as<int>(),

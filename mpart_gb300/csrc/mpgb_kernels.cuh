@@ -33,6 +33,7 @@ namespace mpgb {
 template <int PMAX, bool NEEDJ, int NEEDE>
 struct NodeVal {
     double h;
+    double gn;                   // g(df) + eps: at t = 1, the x_D-slope of T
     double F[NEEDJ ? PMAX : 1];  // x_D g'(df) phit'_k(y), k = 1..P
     double E;                    // d/dx_D of the integrand (MonotoneIntegrand.h:193-201)
     double K[NEEDE == 2 ? PMAX : 1];
@@ -107,7 +108,8 @@ __device__ __forceinline__ void evalNode(double t, double xd, const double* as, 
     }
     double g, gp;
     posEval<POS>(df, g, gp);
-    o.h = xd * (g + nugget);
+    o.gn = g + nugget;
+    o.h = xd * o.gn;
     if (isinf(g)) st |= kStatusInf;
     else if (isnan(o.h)) st |= kStatusNaN;
     if constexpr (NEEDE == 2) {
@@ -364,16 +366,18 @@ struct SmemLayout {
                  //                    the reduction that reads W)
     double* GX;  // [dmax][tpb]        input gradient accumulators
     double* DS;  // [tri(depthMax+1)][tpb]  forward-mode derivative stack
+    double* stage;  // [stageDoubles]  a component's gathered coefficients and prefix-tree tables (phase A)
     int bstride;
 };
 
-__host__ __device__ inline size_t smemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input) {
+__host__ __device__ inline size_t smemBytes(int tpb, int dmax, int nBmax, int depthMax, int pmax, bool input,
+                                            int stageDoubles = 0) {
     const int sw = (depthMax + 1 > pmax + 1) ? depthMax + 1 : pmax + 1;
     size_t n = (size_t)dmax * tpb + (size_t)nBmax * (tpb + 1) + (size_t)sw * tpb;
     if (input) {
         n += (size_t)dmax * tpb + (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
     }
-    return n * sizeof(double);
+    return (n + (size_t)stageDoubles) * sizeof(double);
 }
 
 __device__ inline SmemLayout carveSmem(double* base, int tpb, int dmax, int nBmax, int depthMax, int pmax,
@@ -388,10 +392,11 @@ __device__ inline SmemLayout carveSmem(double* base, int tpb, int dmax, int nBma
     p += (size_t)((depthMax + 1 > pmax + 1) ? depthMax + 1 : pmax + 1) * tpb;
     if (input) {
         L.GX = p; p += (size_t)dmax * tpb;
-        L.DS = p;
+        L.DS = p; p += (size_t)((depthMax + 1) * (depthMax + 2) / 2) * tpb;
     } else {
         L.GX = nullptr; L.DS = nullptr;
     }
+    L.stage = p;
     return L;
 }
 
@@ -437,6 +442,33 @@ __device__ __forceinline__ void phaseA(const CompDesc& c, const SmemLayout& L, i
         if (nk) {
             if (pc && depth >= kKeepMinDepth) pc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = phi;
             accumCoeffs<PMAX>(nk, phi, cm + __ldg(&c.nodeSlot[n]), a);
+        }
+    }
+}
+
+// Phase A from shared memory: the component's gathered coefficients (sCm,
+// nSlots doubles) and its nodeA / nodeSlot tables (sA, sS), staged by the
+// block for the tile.  The same operations in the same order as phaseA.
+template <int PMAX>
+__device__ __forceinline__ void phaseAStaged(const CompDesc& c, const SmemLayout& L, int tid, const double* sCm,
+                                             const uint32_t* sA, const uint32_t* sS, double* a, double* pc) {
+#pragma unroll
+    for (int k = 0; k <= PMAX; ++k) a[k] = 0.0;
+    const int tpb = blockDim.x;
+    L.S[tid] = 1.0;
+    for (int n = 0; n < c.nNodes; ++n) {
+        const uint32_t w = sA[n];
+        const int depth = w & 31;
+        const int nk = (w >> 5) & 31;
+        const int brow = w >> 18;
+        double phi = 1.0;
+        if (depth > 0) {
+            phi = L.S[(depth - 1) * tpb + tid] * L.B[brow * L.bstride + tid];
+            L.S[depth * tpb + tid] = phi;
+        }
+        if (nk) {
+            if (pc && depth >= kKeepMinDepth) pc[(long long)__ldg(&c.nodeCIdx[n]) * tpb + tid] = phi;
+            accumCoeffsShared<PMAX>(nk, phi, sCm + sS[n], a);
         }
     }
 }
@@ -528,8 +560,26 @@ __device__ __forceinline__ void fusedBody(const FusedParams& prm, const WorkItem
             // kept for the reduction below)
             // (monotone components: the products of the deeper prefix nodes)
             double* rc = (prm.rcache && (flags & kFlagCoefReduced)) ? prm.rcache + item.rcBase : nullptr;
-            if constexpr (BASIS == kBasisSigmoid) phaseARect<PMAX, POS>(c, L, tid, cm, a, rc);
-            else phaseA<PMAX>(c, L, tid, cm, a, rc);
+            if constexpr (BASIS == kBasisSigmoid) {
+                phaseARect<PMAX, POS>(c, L, tid, cm, a, rc);
+            } else if (c.nSlots + c.nNodes <= prm.stageDoubles) {
+                // The tree walk reads a coefficient and two table words per
+                // node, the same addresses in every lane: from shared memory
+                // (staged once per tile) rather than as uniform global loads.
+                double* sCm = L.stage;
+                uint32_t* sA = reinterpret_cast<uint32_t*>(L.stage + c.nSlots);
+                uint32_t* sS = sA + c.nNodes;
+                __syncthreads();
+                for (int k = tid; k < c.nSlots; k += tpb) sCm[k] = __ldg(&cm[k]);
+                for (int k = tid; k < c.nNodes; k += tpb) {
+                    sA[k] = __ldg(&c.nodeA[k]);
+                    sS[k] = __ldg(&c.nodeSlot[k]);
+                }
+                __syncthreads();
+                phaseAStaged<PMAX>(c, L, tid, sCm, sA, sS, a, rc);
+            } else {
+                phaseA<PMAX>(c, L, tid, cm, a, rc);
+            }
             const double xd = L.X[(c.D - 1) * tpb + tid];
 
             // wv[k] = dT/da_k; d1x, d2x: last-input basis derivatives at x_D;
@@ -897,17 +947,23 @@ struct InverseEval {
     __device__ double operator()(double x) const {
         return integrateValueNI<BASIS, POS, PMAX>(A, P, x, Q, bc, nugget, st) + f0;
     }
-    // dT/dx_D = g(df(x)) + nugget: no quadrature.
+    // dT/dx_D = g(df(x)) + nugget: no quadrature.  Formed as the integrand
+    // node at t = 1 forms it, so that the queue pass, which reads the slope
+    // off that node (KnownSlope), takes the same steps.
     __device__ double slope(double x) const {
-        double d1[PMAX + 1];
-        lastBasis<BASIS, PMAX, false, true, false>(x, P, *bc, nullptr, d1, nullptr);
-        double df = 0.0;
-#pragma unroll
-        for (int k = 0; k <= PMAX; ++k) df = fma(A.a[k], d1[k], df);
-        double g, gp;
-        posEval<POS>(df, g, gp);
-        return g + nugget;
+        double as[PMAX + 1];
+        scaleCoeffs<BASIS, PMAX>(A.a, P, *bc, as);
+        NodeVal<PMAX, false, 0> V;
+        int s = 0;
+        evalNode<BASIS, POS, PMAX, false, 0>(1.0, x, as, P, *bc, nugget, V, s);
+        return V.gn;
     }
+};
+
+// The slope at the point just evaluated, read off its quadrature's t = 1 node.
+struct KnownSlope {
+    double s;
+    __device__ double slope(double) const { return s; }
 };
 
 // T(x_<D, y) of a sigmoid expansion as a function of y (the reference's
@@ -1253,6 +1309,7 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
     const int cR = Q.nCoarse - 1, cM = cR / 2, fR = Q.nFine - 1, fM = fR / 2;
     if (threadIdx.x == 0) {
         // Nodes of an interval after its midpoint, in the order of `integrate`.
+        sOff[0] = 0.0; sCw[0] = 0.0; sFw[0] = 0.0; sIsC[0] = 1;
         int j = 1;
         for (int i = 1; i < cR; ++i) {
             if (i == cM) continue;
@@ -1285,7 +1342,7 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
     for (int k = 0; k <= PMAX; ++k) { A.a[k] = 0.0; as[k] = 0.0; }
     RootSolve rs;
     rs.phase = RootSolve::kDone;
-    double xd = 0.0, lo = 0.0, hi = 1.0, hA = 0.0, hB = 0.0, hM = 0.0, ic = 0.0, ih = 0.0, Ih = 0.0;
+    double xd = 0.0, lo = 0.0, hi = 1.0, hA = 0.0, hB = 0.0, hM = 0.0, ic = 0.0, ih = 0.0, Ih = 0.0, slopeB = 0.0;
     int level = 0, sp = 0, j = 0, qst = 0, stAll = 0;
     long long nInt = 0;
     int nodes = 0;  // integrand nodes of the current point's solve
@@ -1406,22 +1463,25 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
             }
         } else if (j < 0) {
             hB = h;
+            slopeB = V.gn;
             if (qst & (kStatusInf | kStatusNaN)) { qdone = true; T = nan; }
             else j = 0;
         } else {
-            if (j == 0) {
-                hM = h;
-                ic = (s * Q.cWts[0]) * hA;
-                ic = fma(s * Q.cWts[cM], hM, ic);
-                ic = fma(s * Q.cWts[cR], hB, ic);
-                const double w0 = s * Q.fWts[0], wM = s * Q.fWts[fM], wR = s * Q.fWts[fR];
-                ih = w0 * hA;
-                ih = fma(wM, hM, ih);
-                ih = fma(wR, hB, ih);
-            } else {
-                if (sIsC[j]) ic = fma(s * sCw[j], h, ic);
-                ih = fma(s * sFw[j], h, ih);
-            }
+            // The interval's sums, as `integrate` forms them: at the midpoint
+            // (j = 0) ic = (s c_0) hA + (s c_M) hM + (s c_R) hB and ih likewise
+            // with the fine weights; at a later node one more product.  Both
+            // cases as one sequence of selects, so that the lanes of a warp at
+            // different nodes issue one path.
+            const bool mid = (j == 0);
+            if (mid) hM = h;
+            const double cwj = mid ? Q.cWts[cM] : sCw[j];
+            const double fwj = mid ? Q.fWts[fM] : sFw[j];
+            const double icA = (s * Q.cWts[0]) * hA, ihA = (s * Q.fWts[0]) * hA;
+            const double icN = fma(s * cwj, h, mid ? icA : ic);
+            const double ihN = fma(s * fwj, h, mid ? ihA : ih);
+            const double icB = fma(s * Q.cWts[cR], hB, icN), ihB = fma(s * Q.fWts[fR], hB, ihN);
+            ic = mid ? icB : (sIsC[j] ? icN : ic);
+            ih = mid ? ihB : ihN;
             if (++j == nPer) {
                 j = 0;
                 if (qst & (kStatusInf | kStatusNaN)) {
@@ -1464,9 +1524,13 @@ __global__ void __launch_bounds__(128) inverseQueueKernel(const __grid_constant_
         if (!qdone) continue;
         // The quadrature is done: one solver step with T(x) = integral + f(x_<D, 0).
         stAll |= qst;
-        int dummy = 0;
-        const InverseEval<BASIS, POS, PMAX> f{A, P, f0, &prm.quad, &prm.bc, nugget, &dummy};
-        rs.step_(T + f0, yd, f, prm.xtol, prm.ytol, kBracketIts, prm.method);
+        if (fixed) {
+            int dummy = 0;
+            const InverseEval<BASIS, POS, PMAX> f{A, P, f0, &prm.quad, &prm.bc, nugget, &dummy};
+            rs.step_(T + f0, yd, f, prm.xtol, prm.ytol, kBracketIts, prm.method);
+        } else {
+            rs.step_(T + f0, yd, KnownSlope{slopeB}, prm.xtol, prm.ytol, kBracketIts, prm.method);
+        }
         if (rs.phase == RootSolve::kDone) {
             prm.out[(long long)comp * prm.outRs + i * prm.outCs] = rs.result;
             if (prm.info) prm.info[(long long)comp * prm.infoStride + i] = rs.info;
@@ -1740,7 +1804,7 @@ __global__ void __launch_bounds__(256) inverseKeyKernel(const __grid_constant__ 
 template <int BASIS, int POS, int PMAX>
 cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int needE, cudaStream_t stream) {
     const bool input = (prm.flags & kFlagInput) != 0;
-    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, input);
+    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, PMAX, input, prm.stageDoubles);
     auto run = [&](auto kern) -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

@@ -131,6 +131,11 @@ struct FusedParams {
     double nugget;
     int dmax, nBmax, depthMax;
     int negRows;            // kFlagImplicit: rows [0, negRows) of outInput are negated when written
+    // Shared-memory staging of phase A's inputs: components with nSlots +
+    // nNodes <= stageDoubles read their coefficients and prefix-tree tables
+    // from a block-staged copy (0: none; the launch adds stageDoubles to the
+    // block's shared memory).
+    int stageDoubles;
     QuadParams quad;
     BasisConsts bc;
 };
