@@ -261,6 +261,7 @@ public:
                 nBmax_ = std::max(nBmax_, pg->nB);
                 depthMax_ = std::max(depthMax_, pg->maxDepth);
                 pclass_ = std::max(pclass_, batchOrderClass(pg->P));
+                if (pg->nSlots + pg->nNodes <= kStageCap) stageNeed_ = std::max(stageNeed_, pg->nSlots + pg->nNodes);
             }
         }
         totalSlots_ = slot;
@@ -285,6 +286,7 @@ public:
         int dev = 0;
         MPGB_CUDA(cudaGetDevice(&dev));
         MPGB_CUDA(cudaDeviceGetAttribute(&numSMs_, cudaDevAttrMultiProcessorCount, dev));
+        MPGB_CUDA(cudaDeviceGetAttribute(&smemPerSM_, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
     }
 
     int NumMaps() const { return (int)maps_.size(); }
@@ -566,6 +568,15 @@ private:
         p.items = itemBuf_.as<WorkItem>();
         const size_t smem = fusedSmemBytes(tpb_, dmax_, nBmax_, depthMax_, pclass_, false);
         if (smem > 227 * 1024) throw std::invalid_argument("MapBatch: components too large for the shared-memory tile.");
+        // Phase A's inputs staged in shared memory for the components that fit
+        // kStageCap, when that leaves the blocks per SM unchanged (the batch
+        // kernel's register budget: 4 blocks for order classes up to 4, 2 above).
+        {
+            const size_t base = smem + 1024, with = base + (size_t)stageNeed_ * sizeof(double);
+            const size_t lb = pclass_ <= 4 ? 4 : 2;
+            auto blocks = [&](size_t b) { return std::min<size_t>(lb, (size_t)smemPerSM_ / b); };
+            p.stageDoubles = (stageNeed_ > 0 && with <= 227 * 1024 && blocks(with) == blocks(base)) ? stageNeed_ : 0;
+        }
         MPGB_CUDA(launchBatch(basis_, pos_, p, (int)items.size(), pclass_, counter_.as<int>(), s));
     }
 
@@ -663,7 +674,8 @@ private:
     int basis_ = 0, pos_ = 0;
     QuadParams quad_{};
     BasisConsts bc_{};
-    int dmax_ = 1, nBmax_ = 0, depthMax_ = 0, pclass_ = 2, totalSlots_ = 0, numSMs_ = 1;
+    int dmax_ = 1, nBmax_ = 0, depthMax_ = 0, pclass_ = 2, totalSlots_ = 0, numSMs_ = 1, stageNeed_ = 0,
+        smemPerSM_ = 0;
     int tpb_ = 128;
     std::map<std::pair<int, int>, int> tiles_;
     Buf gradScratch_;  // autotuning: coefficient adjoints of timed calls

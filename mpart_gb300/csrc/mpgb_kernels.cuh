@@ -1829,7 +1829,7 @@ cudaError_t launchFusedP(const FusedParams& prm, int nItems, int needJ, int need
 // most one per item); `counter` must be zero on entry.
 template <int BASIS, int POS>
 cudaError_t launchBatchP(const FusedParams& prm, int nItems, int pmaxClass, int* counter, cudaStream_t stream) {
-    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, pmaxClass, false);
+    const size_t smem = smemBytes(prm.tpb, prm.dmax, prm.nBmax, prm.depthMax, pmaxClass, false, prm.stageDoubles);
     void (*kern)(FusedParams, int, int*) = nullptr;
     switch (pmaxClass) {
         case 2: kern = batchKernel<BASIS, POS, 2>; break;
