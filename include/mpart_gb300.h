@@ -264,8 +264,9 @@ int mpgb_kl_objective(mpgb_map* map, mpgb_matrix pts, double* loss, double* grad
  * address is looked up once per device when a map is created there, which
  * under CUDA's lazy module loading is when the driver reserves the array; if
  * that look-up failed, the first call on the device makes it (and reserves
- * the array): make that first call during start-up, before any stream
- * capture.  Synchronises the stream before returning. */
+ * the array): make that first call during start-up.  Every call reads its
+ * status word back and synchronises the stream before returning, so no call
+ * can be captured into a CUDA graph. */
 int mpgb_fused_fwd_adj_noalloc(mpgb_map* map, mpgb_matrix pts, mpgb_matrix sens, mpgb_matrix logdet_sens,
                                double logdet_sens_scale, mpgb_matrix out_eval, mpgb_matrix out_logdet,
                                double* coeff_grad, void* stream);
