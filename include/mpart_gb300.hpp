@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <limits>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -341,5 +342,49 @@ std::shared_ptr<ConditionalMapBase> CreateSigmoidTriangular(unsigned int inputDi
 struct IntegrandError : public std::runtime_error {
     using std::runtime_error::runtime_error;
 };
+
+// MParT/TrainMap.h:19-58, same field names and defaults.  opt_alg "LD_SLSQP"
+// (SLSQP's iteration for an unconstrained problem) or "LD_LBFGS"
+// (limited-memory BFGS); NLopt is not used, so other names throw
+// std::invalid_argument.  The tolerances are NLopt's stopping rules;
+// opt_stopval and opt_maxtime are not used.
+struct TrainOptions {
+    std::string opt_alg = "LD_SLSQP";
+    double opt_stopval = -std::numeric_limits<double>::infinity();
+    double opt_ftol_rel = 1e-3;
+    double opt_ftol_abs = 1e-3;
+    double opt_xtol_rel = 1e-4;
+    double opt_xtol_abs = 1e-4;
+    int opt_maxeval = 1000;
+    double opt_maxtime = std::numeric_limits<double>::infinity();
+    int verbose = 0;
+};
+
+// KLObjective with the standard Gaussian reference density
+// (MParT/MapObjective.h, ObjectiveFactory::CreateGaussianKLObjective,
+// src/MapObjective.cpp:54-91): train and test are inputDim x N device
+// matrices that stay owned by the caller.
+class KLObjective {
+public:
+    KLObjective(StridedMatrix const& train, StridedMatrix const& test = StridedMatrix()) : train_(train), test_(test) {}
+    // -mean(log N(T(x)) + log det dT/dx) over the training / test samples: the
+    // components' reverse-KL losses plus (M/2) log 2 pi.
+    double TrainError(std::shared_ptr<ConditionalMapBase> const& map, cudaStream_t stream = 0) const;
+    double TestError(std::shared_ptr<ConditionalMapBase> const& map, cudaStream_t stream = 0) const;
+    StridedMatrix const& Train() const { return train_; }
+    StridedMatrix const& Test() const { return test_; }
+
+private:
+    StridedMatrix train_, test_;
+};
+
+// TrainMap(map, objective, options) (src/TrainMap.cpp:166-216) for a
+// standard-Gaussian KLObjective on a map of monotone components: every
+// component minimises its reverse KL (src/TrainMap.cpp:144-164), all of them
+// in lockstep over one batched GPU step per iteration.  A map whose
+// coefficients were never set starts from ones.  Returns the training error
+// (TrainError at the result).
+double TrainMap(std::shared_ptr<ConditionalMapBase> const& map, KLObjective const& objective,
+                TrainOptions const& options, cudaStream_t stream = 0);
 
 }  // namespace mpgb

@@ -586,6 +586,54 @@ TrainOpts trainOptsFromC(const mpgb_train_options* opts) {
     return o;
 }
 
+namespace {
+MonotoneMapBase& monotoneMap(std::shared_ptr<ConditionalMapBase> const& map) {
+    auto* m = dynamic_cast<MonotoneMapBase*>(map.get());
+    if (!m) throw std::invalid_argument("KLObjective: the map must be a monotone component or a TriangularMap of them.");
+    return *m;
+}
+double klError(MonotoneMapBase& m, StridedMatrix const& pts, cudaStream_t s) {
+    if (pts.rows < m.inputDim) throw std::invalid_argument("KLObjective: the samples have fewer rows than inputDim.");
+    StridedMatrix p(pts.data, m.inputDim, pts.cols, pts.rowStride, pts.colStride);
+    Dev loss(m.outputDim), g(m.numCoeffs);
+    m.KLObjective(p, loss.p, g.p, s);
+    std::vector<double> lh(m.outputDim);
+    TR_CUDA(cudaMemcpyAsync(lh.data(), loss.p, lh.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+    TR_CUDA(cudaStreamSynchronize(s));
+    double v = 0.5 * m.outputDim * std::log(2.0 * 3.14159265358979323846);
+    for (double l : lh) v += l;
+    return v;
+}
+}  // namespace
+
+double KLObjective::TrainError(std::shared_ptr<ConditionalMapBase> const& map, cudaStream_t stream) const {
+    return klError(monotoneMap(map), train_, stream);
+}
+
+double KLObjective::TestError(std::shared_ptr<ConditionalMapBase> const& map, cudaStream_t stream) const {
+    if (test_.empty()) throw std::invalid_argument("KLObjective::TestError: no test samples.");
+    return klError(monotoneMap(map), test_, stream);
+}
+
+double TrainMap(std::shared_ptr<ConditionalMapBase> const& map, KLObjective const& objective,
+                TrainOptions const& options, cudaStream_t stream) {
+    MonotoneMapBase& m = monotoneMap(map);
+    TrainOpts o;
+    if (options.opt_alg == "LD_SLSQP") o.algorithm = MPGB_OPT_SLSQP;
+    else if (options.opt_alg == "LD_LBFGS") o.algorithm = MPGB_OPT_LBFGS;
+    else throw std::invalid_argument("TrainOptions: opt_alg " + options.opt_alg + " is not provided (LD_SLSQP, LD_LBFGS).");
+    o.maxIters = o.maxEvals = options.opt_maxeval;
+    o.ftolRel = options.opt_ftol_rel;
+    o.ftolAbs = options.opt_ftol_abs;
+    o.xtolRel = options.opt_xtol_rel;
+    o.xtolAbs = options.opt_xtol_abs;
+    StridedMatrix const& t = objective.Train();
+    if (t.rows < m.inputDim) throw std::invalid_argument("TrainMap: the samples have fewer rows than inputDim.");
+    StridedMatrix p(t.data, m.inputDim, t.cols, t.rowStride, t.colStride);
+    trainKL(m, p, o, 0, stream, nullptr, nullptr);
+    return objective.TrainError(map, stream);
+}
+
 int trainMapImpl(void* mapObj, mpgb_matrix samples, const mpgb_train_options* opts, double* loss_per_comp,
                  mpgb_train_result* res, void* stream, char* err, int errLen) {
     try {

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "mpart_gb300.h"
@@ -101,9 +102,59 @@ public:
 
 }  // namespace
 
+// cpp_consumer train <in.bin> <out.bin>
+//   in.bin : int64 N, then samples (2 x N) row-major float64
+//   out.bin: the 14 trained coefficients, TrainMap's return value and
+//            KLObjective::TestError on the same samples
+// MParT's training through the C++ API (MParT/TrainMap.h, MParT/MapObjective.h):
+// KLObjective over device samples, TrainOptions with L-BFGS, TrainMap.
+static int trainMain(const char* in, const char* outPath) {
+    FILE* f = std::fopen(in, "rb");
+    if (!f) throw std::runtime_error("cannot open input");
+    int64_t N = 0;
+    if (std::fread(&N, sizeof N, 1, f) != 1) throw std::runtime_error("bad input");
+    std::vector<double> x(2 * N);
+    const bool good = std::fread(x.data(), 8, 2 * N, f) == (size_t)(2 * N);
+    std::fclose(f);
+    if (!good) throw std::runtime_error("short input");
+    mpgb::MapOptions o;
+    o.basisType = mpgb::BasisTypes::HermiteFunctions;
+    o.posFuncType = mpgb::PosFuncTypes::Exp;
+    o.quadType = mpgb::QuadTypes::AdaptiveClenshawCurtis;
+    o.quadAbsTol = o.quadRelTol = 1e-7;
+    Dev dx(x);
+    auto map = mpgb::MapFactory::CreateTriangular(2, 2, 3, o);
+    std::vector<double> zero(map->numCoeffs, 0.0);
+    Dev dc(zero);
+    map->SetCoeffs(dc.p, map->numCoeffs);
+    const auto S = mpgb::StridedMatrix::RowMajor(dx.p, 2, N);
+    mpgb::KLObjective obj(S, S);
+    mpgb::TrainOptions t;
+    t.opt_alg = "LD_LBFGS";
+    t.opt_maxeval = 30;
+    const double train = mpgb::TrainMap(map, obj, t);
+    const double test = obj.TestError(map);
+    std::vector<double> out(map->numCoeffs);
+    cuda(cudaMemcpy(out.data(), map->Coeffs(), out.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    out.push_back(train);
+    out.push_back(test);
+    FILE* g = std::fopen(outPath, "wb");
+    if (!g || std::fwrite(out.data(), 8, out.size(), g) != out.size()) throw std::runtime_error("cannot write output");
+    std::fclose(g);
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 4 && std::string(argv[1]) == "train") {
+        try {
+            return trainMain(argv[2], argv[3]);
+        } catch (std::exception const& e) {
+            std::fprintf(stderr, "cpp_consumer: %s\n", e.what());
+            return 1;
+        }
+    }
     if (argc != 3) {
-        std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]);
+        std::fprintf(stderr, "usage: %s in.bin out.bin | %s train in.bin out.bin\n", argv[0], argv[0]);
         return 2;
     }
     try {

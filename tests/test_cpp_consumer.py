@@ -71,3 +71,38 @@ def test_cpp_consumer_matches_oracle(tmp_path, oracle):
         assert_parity(ld, om.logdet(coef, x), what=f"{what}: LogDeterminant")
         assert_parity(cg, om.coeff_grad(coef, x, sens), what=f"{what}: CoeffGrad")
         assert_inverse_parity(om, coef, np.zeros((0, n)), r, xi, 1e-6, 1e-6)
+
+
+@pytest.mark.gpu
+def test_cpp_consumer_train_map(tmp_path, oracle):
+    """MParT's training through the C++ API (KLObjective, TrainOptions with
+    L-BFGS, TrainMap) on a 2 x 2 order-3 HermiteFunctions + Exp map: the value
+    TrainMap returns and KLObjective::TestError equal the oracle's KL objective
+    (the components' reverse-KL losses plus log 2 pi) at the coefficients it
+    trained, and training lowers it below its value at zero."""
+    O = oracle
+    exe = build_consumer(str(tmp_path))
+    n = 3000
+    rng = np.random.default_rng(4)
+    x1 = rng.standard_normal(n)
+    x = np.stack([x1, x1 ** 2 + 0.5 * rng.standard_normal(n)])
+    inp = os.path.join(str(tmp_path), "train_in.bin")
+    out = os.path.join(str(tmp_path), "train_out.bin")
+    with open(inp, "wb") as f:
+        f.write(np.int64(n).tobytes())
+        f.write(np.ascontiguousarray(x, dtype=np.float64).tobytes())
+    res = subprocess.run([exe, "train", inp, out], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    v = np.fromfile(out, dtype=np.float64)
+    coef, train, test = v[:-2], v[-2], v[-1]
+    om = O.OracleTriangularMap(2, 2, 3, basis=O.BASIS_HERMITE_FUNCTIONS, normalize=True, posfunc=O.POS_EXP,
+                               abs_tol=1e-7, rel_tol=1e-7)
+    assert coef.size == om.num_coeffs
+    cs = om.split(coef)
+    want = np.log(2.0 * np.pi) + sum(O.fast_gaussian_reverse_kl(c, cs[i], x[:c.input_dim])[0]
+                                     for i, c in enumerate(om.comps))
+    assert train == pytest.approx(want, rel=1e-10)
+    assert test == pytest.approx(want, rel=1e-10)
+    zero = np.log(2.0 * np.pi) + sum(O.fast_gaussian_reverse_kl(c, np.zeros(c.num_coeffs), x[:c.input_dim])[0]
+                                     for c in om.comps)
+    assert train < zero
