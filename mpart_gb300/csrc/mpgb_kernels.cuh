@@ -1293,7 +1293,10 @@ constexpr int kDrainNodes = 256;
 // and every step).  A lane whose solve ends writes the root and takes the
 // next point; one atomic per warp serves all its lanes that need one.  The
 // points come in perm order from the expensive end (root estimates from the
-// key pass), so the launch ends on cheap points.
+// key pass), so the launch ends on cheap points.  Solves that grow too long,
+// meet too wide a quadrature or are still running once the queue is empty go,
+// with their solver state, to the warp pass (inverseWarpKernel).  A Newton
+// step's slope is read off the quadrature's t = 1 node.
 //
 // The operations of each quadrature are those of `integrate`, in the same
 // order, so T and the solver's iterates are those of one sequential solve.
