@@ -343,7 +343,9 @@ public:
     // size, each (dimension, order) bucket's tiles per item by timing a launch
     // of that bucket's items alone; then whole calls (tables, sort, launch and
     // the gradient reduction, best of at least 3) of the starting tuning and
-    // of the tuned set per block size.  Returns the ms of the chosen one.
+    // of the tuned set per block size; then, on whole calls, halving and
+    // doubling the tiles of the four buckets with the most work.  Returns the
+    // ms of the chosen one.
     double Autotune(const StridedMatrix* pts, const StridedMatrix* sens, double lsensScale, int reps,
                     cudaStream_t s) {
         reps = std::max(1, reps);
@@ -381,6 +383,33 @@ public:
             SetTuning(tpb, tiles);
             const double ms = timeCall(pts, sens, lsensScale, callReps, s);
             if (ms < bestMs) { bestMs = ms; bestTpb = tpb; bestTiles = tiles; }
+        }
+        // Whole-call refinement: the persistent launch's length is set by how
+        // its largest items end, which timing a bucket alone does not see.
+        // For the buckets that carry the most work (estimated cost x tiles),
+        // try other tile counts one bucket at a time on complete calls and
+        // keep each change that makes the call faster by more than 0.5 %.
+        SetTuning(bestTpb, bestTiles);
+        {
+            std::map<std::pair<int, int>, double> work;
+            for (auto& c : comps_) work[{c.prog->D, c.prog->P}] += c.prog->weight * (double)pts[c.map].cols;
+            std::vector<std::pair<double, std::pair<int, int>>> order;
+            for (auto& w : work) order.push_back({-w.second, w.first});
+            std::sort(order.begin(), order.end());
+            const int kRefineBuckets = 4;
+            for (int q = 0; q < (int)order.size() && q < kRefineBuckets; ++q) {
+                const auto key = order[q].second;
+                const int cur = bestTiles[key];
+                for (int t : {std::max(1, cur / 2), cur * 2}) {
+                    if (t == cur) continue;
+                    auto trial = bestTiles;
+                    trial[key] = t;
+                    SetTuning(bestTpb, trial);
+                    const double ms = timeCall(pts, sens, lsensScale, callReps, s);
+                    if (ms < 0.995 * bestMs) { bestMs = ms; bestTiles = trial; }
+                }
+                SetTuning(bestTpb, bestTiles);
+            }
         }
         SetTuning(bestTpb, bestTiles);
         checkStatus(s);
