@@ -140,3 +140,15 @@ def test_train_map_starts_unset_coefficients_at_one(gpu):
         assert np.isfinite(loss).all()
         maps.append(np.asarray(tri.CoeffMap()))
     np.testing.assert_array_equal(maps[0], maps[1])
+
+
+def test_expand_and_options_errors(M):
+    """Bad arguments are refused on the host: an Expand of a zero-length set
+    through the C ABI, an optimiser name this library does not provide."""
+    import ctypes as C
+    lib = M.load()
+    n = C.c_uint()
+    assert lib.mpgb_multi_index_expand(0, 0, None, C.byref(n), None, C.byref(n), None, 0) != 0
+    with pytest.raises(ValueError):
+        M.TrainOptions(opt_alg="LN_COBYLA")._train_c()
+    assert M.TrainOptions()._train_c().algorithm == 0 and M.TrainOptions(opt_alg="LD_LBFGS")._train_c().algorithm == 1
