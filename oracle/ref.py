@@ -63,6 +63,9 @@ def lib():
             getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, C.c_long, _dp]
         L.ref_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, C.c_double, C.c_double, _dp]
         L.ref_mset.argtypes = [C.c_uint, C.c_uint, _up, C.c_int, C.c_uint, _up, _up, _up, _up]
+        L.ref_sigmoid.restype = C.c_void_p
+        L.ref_sigmoid.argtypes = [C.c_uint, C.c_uint, _up, _up, _up, _dp, _dp, _dp, C.c_uint, C.c_int, C.c_int]
+        L.ref_direct_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, _dp]
         _lib = L
     return _lib
 
@@ -163,6 +166,39 @@ class RefMap:
         out = np.zeros((self.output_dim, n))
         self._check(lib().ref_inverse(self._h, x1.ctypes.data_as(_dp), x1.shape[0], r.ctypes.data_as(_dp), n,
                                       xtol, ytol, out.ctypes.data_as(_dp)))
+        return out
+
+
+class RefSigmoid(RefMap):
+    """A sigmoid expansion of the reference, built as
+    MapFactory::CreateSigmoidComponent builds one (Sigmoid1d with SoftPlus
+    edges, HermiteFunction off the diagonal, RectifiedMultivariateExpansion,
+    or UnivariateExpansion for one input) from the given centers, widths and
+    weights and compressed multi-index set."""
+
+    def __init__(self, dim, starts, dims, orders, centers, widths, weights, sum_type="Linear", posfunc="SoftPlus"):
+        s = np.ascontiguousarray(starts, np.uint32)
+        d = np.ascontiguousarray(dims if len(dims) else [0], np.uint32)
+        o = np.ascontiguousarray(orders if len(orders) else [0], np.uint32)
+        c, w, wt = _c(centers), _c(widths), _c(weights)
+        self._keep = (s, d, o, c, w, wt)
+        L = lib()
+        self._h = L.ref_sigmoid(dim, len(s) - 1, s.ctypes.data_as(_up), d.ctypes.data_as(_up), o.ctypes.data_as(_up),
+                                c.ctypes.data_as(_dp), w.ctypes.data_as(_dp), wt.ctypes.data_as(_dp), c.size,
+                                {"Linear": 0, "Constant": 1}[sum_type], {"Exp": POS_EXP, "SoftPlus": POS_SOFTPLUS}[posfunc])
+        if not self._h:
+            raise RuntimeError(L.ref_last_error().decode())
+        a, b_, cc = C.c_uint(), C.c_uint(), C.c_uint()
+        L.ref_sizes(self._h, C.byref(a), C.byref(b_), C.byref(cc))
+        self.input_dim, self.output_dim, self.num_coeffs = a.value, b_.value, cc.value
+
+    def inverse(self, x1, r):
+        r = _c(np.reshape(r, (self.output_dim, -1)))
+        n = r.shape[1]
+        x1 = _c(x1) if len(x1) else np.zeros((0, n))
+        out = np.zeros((self.output_dim, n))
+        self._check(lib().ref_direct_inverse(self._h, x1.ctypes.data_as(_dp), x1.shape[0], r.ctypes.data_as(_dp), n,
+                                             out.ctypes.data_as(_dp)))
         return out
 
 

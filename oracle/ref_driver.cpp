@@ -33,7 +33,10 @@
 #include "MParT/OrthogonalPolynomial.h"
 #include "MParT/PositiveBijectors.h"
 #include "MParT/Quadrature.h"
+#include "MParT/RectifiedMultivariateExpansion.h"
+#include "MParT/Sigmoid.h"
 #include "MParT/TriangularMap.h"
+#include "MParT/UnivariateExpansion.h"
 
 using namespace mpart;
 using Host = Kokkos::HostSpace;
@@ -124,6 +127,29 @@ void componentInverse(Map* m, StridedMatrix<const double, Host> const& x, Stride
 
 }  // namespace
 
+// A sigmoid expansion as MapFactory::CreateSigmoidComponent builds one
+// (CreateSigmoidExpansionTemplate, src/MapFactory.cpp:258-281): Sigmoid1d
+// with SoftPlus edges from the given centers, widths and weights (the
+// factory's CreateSigmoid computes those; MapFactory.cpp is not compiled
+// here), then for one input UnivariateExpansion<Sigmoid1d> with maxOrder =
+// numTerms - 1, otherwise RectifiedMultivariateExpansion with
+// HermiteFunction off the diagonal and the positive bijector `pos` (Exp 0,
+// SoftPlus 1) as rectifier, over the compressed multi-index set.  sumType:
+// Linear 0, Constant 1.  Zero coefficients.
+template <class Rect>
+std::shared_ptr<Map> sigmoidExpansion(unsigned dim, FixedMultiIndexSet<Host> const& mset,
+                                      Kokkos::View<double*, Host> c, Kokkos::View<double*, Host> w,
+                                      Kokkos::View<double*, Host> wt, SigmoidSumSizeType sumType) {
+    using Sig = Sigmoid1d<Host, SigmoidTypeSpace::Logistic, SoftPlus>;
+    Sig sigmoid(c, w, wt, sumType);
+    if (dim == 1) return std::make_shared<UnivariateExpansion<Host, Sig>>(mset.Size() - 1, sigmoid);
+    using Eval = BasisEvaluator<BasisHomogeneity::OffdiagHomogeneous, Kokkos::pair<HermiteFunction, Sig>, Rect>;
+    Eval basisEval(dim, HermiteFunction(), sigmoid);
+    MultivariateExpansionWorker<Eval, Host> worker(mset, basisEval);
+    return std::make_shared<RectifiedMultivariateExpansion<Host, HermiteFunction, Sig, Rect>>(worker);
+}
+
+
 extern "C" {
 
 const char* ref_last_error() { return g_err.c_str(); }
@@ -182,7 +208,52 @@ void* ref_component(unsigned dim, unsigned numTerms, const unsigned* starts, con
     return out;
 }
 
+void* ref_sigmoid(unsigned dim, unsigned numTerms, const unsigned* starts, const unsigned* dims,
+                  const unsigned* orders, const double* centers, const double* widths, const double* weights,
+                  unsigned nCenters, int sumType, int pos) {
+    RefMap* out = nullptr;
+    guard([&] {
+        const unsigned nnz = starts[numTerms];
+        Kokkos::View<unsigned*, Host> s("nzStarts", numTerms + 1), d("nzDims", nnz), r("nzOrders", nnz);
+        for (unsigned i = 0; i <= numTerms; ++i) s(i) = starts[i];
+        for (unsigned i = 0; i < nnz; ++i) {
+            d(i) = dims[i];
+            r(i) = orders[i];
+        }
+        FixedMultiIndexSet<Host> mset(dim, s, d, r);
+        Kokkos::View<double*, Host> c("centers", nCenters), w("widths", nCenters), wt("weights", nCenters);
+        for (unsigned i = 0; i < nCenters; ++i) {
+            c(i) = centers[i];
+            w(i) = widths[i];
+            wt(i) = weights[i];
+        }
+        const SigmoidSumSizeType st = sumType ? SigmoidSumSizeType::Constant : SigmoidSumSizeType::Linear;
+        auto* m = new RefMap;
+        m->map = pos ? sigmoidExpansion<SoftPlus>(dim, mset, c, w, wt, st) : sigmoidExpansion<Exp>(dim, mset, c, w, wt, st);
+        m->comps.push_back(m->map);
+        Kokkos::View<const double*, Host> coeffs = Kokkos::View<double*, Host>("Component Coefficients",
+                                                                                 m->map->numCoeffs);
+        m->map->SetCoeffs(coeffs);
+        out = m;
+    });
+    return out;
+}
+
 void ref_free(void* h) { delete (RefMap*)h; }
+
+// The map's own ConditionalMapBase::InverseImpl (default options): for the
+// sigmoid expansions, whose solver is theirs (RectifiedMultivariateExpansion
+// and UnivariateExpansion InverseImpl).  x1 has inputDim - outputDim rows.
+int ref_direct_inverse(void* h, const double* x1, long x1Rows, const double* r, long n, double* out) {
+    return guard([&] {
+        auto& m = *((RefMap*)h)->map;
+        Kokkos::View<double**, Kokkos::LayoutRight, Host> x("x1", (size_t)std::max<long>(x1Rows, 0), (size_t)n);
+        for (long k = 0; k < x1Rows; ++k)
+            for (long i = 0; i < n; ++i) x(k, i) = x1[k * n + i];
+        StridedMatrix<const double, Host> xv = x;
+        m.InverseImpl(xv, cmat(r, m.outputDim, n), mat(out, m.outputDim, n));
+    });
+}
 
 int ref_sizes(void* h, unsigned* inputDim, unsigned* outputDim, unsigned* numCoeffs) {
     return guard([&] {

@@ -206,3 +206,43 @@ def test_multi_index_set_order_matches_reference():
             assert [tuple(int(v) for v in t) for t in s._terms] == ref_terms
     # the 2-D total-order-1 set: [1 1] is reached from [0 1] and [1 0]
     assert R.mset_expand([(0, 0), (0, 1), (1, 0)])[0] == [3, 4, 3, 5]
+
+
+@pytest.mark.parametrize("dim,sum_type,pos", [(1, "Linear", "SoftPlus"), (2, "Linear", "SoftPlus"),
+                                              (3, "Constant", "SoftPlus"), (3, "Linear", "Exp")])
+def test_sigmoid_expansion_matches_reference(oracle, dim, sum_type, pos):
+    """The sigmoid expansions against the reference's own Sigmoid1d,
+    RectifiedMultivariateExpansion and UnivariateExpansion (as
+    MapFactory::CreateSigmoidComponent assembles them), with the factory's
+    widths and weights from the oracle's restatement: every entry point, to
+    the bit; the Inverse (the classes' own solvers) to the solver tolerance."""
+    O = oracle
+    if sum_type == "Linear":
+        centers = np.array([-3.0, 3.0, 0.0, -1.0, 1.0, -2.0, 0.0, 2.0])  # three sigmoid terms
+        nsig, st = 3, O.SUM_LINEAR
+    else:
+        centers = np.array([-3.0, 3.0, 1.0, -1.0, 0.5])
+        nsig, st = 3, O.SUM_CONSTANT
+    oc, w, wt, starts = O.sigmoid_from_centers(centers, 1.5, st)
+    s, d, o = O.sigmoid_mset(dim, 2, 2, nsig)
+    orc = O.OracleSigmoidComponent(dim, s, d, o, (oc, w, wt, starts), O.POS_EXP if pos == "Exp" else O.POS_SOFTPLUS)
+    ref = R.RefSigmoid(dim, s, d, o, oc, w, wt, sum_type, pos)
+    assert ref.num_coeffs == orc.num_coeffs and ref.input_dim == dim
+    rng = np.random.default_rng(11 + dim)
+    # positive coefficients on the terms with a last-input factor keep the map monotone
+    diag = np.array([d[s[t + 1] - 1] == dim - 1 if s[t + 1] > s[t] else False for t in range(len(s) - 1)])
+    coef = np.where(diag, 0.1 + 0.2 * rng.random(orc.num_coeffs), 0.1 * rng.standard_normal(orc.num_coeffs))
+    if dim == 1:
+        coef[0] = 0.1 * rng.standard_normal()
+    x = rng.standard_normal((dim, 300)) * 1.5
+    sens = rng.standard_normal((1, 300))
+    ref.set_coeffs(coef)
+    same(ref.evaluate(x)[0], orc.evaluate(coef, x), "Evaluate")
+    same(ref.logdet(x), orc.logdet(coef, x), "LogDeterminant")
+    same(ref.coeff_grad(x, sens), orc.coeff_grad(coef, x, sens), "CoeffGrad")
+    same(ref.gradient(x, sens), orc.gradient(coef, x, sens), "Gradient")
+    same(ref.logdet_coeff_grad(x), orc.logdet_coeff_grad(coef, x), "LogDeterminantCoeffGrad")
+    same(ref.logdet_input_grad(x), orc.logdet_input_grad(coef, x), "LogDeterminantInputGrad")
+    r = orc.evaluate(coef, x)
+    xi = ref.inverse(x[:dim - 1], r)[0]
+    np.testing.assert_allclose(xi, x[dim - 1], atol=1e-5)
