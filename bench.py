@@ -150,7 +150,7 @@ def kl_train(M, dev):
         "train_objective_per_component_reference_calls": [float(v) for v in loss_r],
         "reference_calls_train_iterations": int(r_r["iterations"]),
         "reference_calls_train_ms_per_step": float(r_r["ms_per_step"]),
-    }, trained
+    }, trained, (np.asarray(steps[0][1]), np.asarray(steps[0][2]))
 
 
 def batch_specs(n_maps=64, seed=17):
@@ -448,7 +448,7 @@ def cpu_leg(name, **arrays):
         f = os.path.join(d, "in.npz")
         np.savez(f, **{k: np.asarray(v) for k, v in arrays.items()})
         env = dict(os.environ, **TIMING_ENV)
-        if name == "c2-parity":
+        if name in ("c2-parity", "kl-parity"):
             env.pop("MPGB_ORACLE_BUILD")  # parity: the strict build
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", name, "--cpu-in", f],
                            env=env, capture_output=True, text=True)
@@ -462,6 +462,7 @@ def run_cpu_leg(args):
     legs = {"c2": lambda: cpu_baseline(),
             "c2-parity": lambda: leg_c2_parity(a),
             "kl": lambda: kl_cpu_step_ms(a["coeffs"]),
+            "kl-parity": lambda: leg_kl_parity(a),
             "inverse": lambda: leg_inverse(a),
             "sigmoid": lambda: leg_sigmoid(a)}
     print(json.dumps(legs[args.cpu_leg]()), flush=True)
@@ -690,6 +691,42 @@ def cpu_baseline(target_seconds=12.0):
                       f"LogDeterminantCoeffGrad, gradients summed over points; {CPU_BUILD}"}
 
 
+def leg_kl_parity(a):
+    """The batched KL step's per-component objectives and coefficient
+    gradient at the trained coefficients against the oracle's parity build
+    (FastGaussianReverseKLObjective per component, src/MapObjective.cpp:185-234)
+    on all KL_N samples (child process): 1e-10 relative, the gradient (a mean
+    over samples) floored at 1e-3 of its largest entry."""
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    tmo = O.OracleTriangularMap(KL_DIM, KL_DIM, KL_ORDER, basis=O.BASIS_HERMITE_FUNCTIONS, posfunc=O.POS_EXP,
+                                abs_tol=KL_TOL, rel_tol=KL_TOL)
+    X = banana(KL_N)
+    t0 = time.perf_counter()
+    loss, grad = [], []
+    for comp, cc in zip(tmo.comps, tmo.split(np.asarray(a["coeffs"], dtype=np.float64))):
+        l, g = O.fast_gaussian_reverse_kl(comp, cc, np.ascontiguousarray(X[:comp.input_dim]))
+        loss.append(l)
+        grad.append(np.asarray(g))
+    dt = time.perf_counter() - t0
+    loss, grad = np.array(loss), np.concatenate(grad)
+
+    def check(g, r, floor):
+        scale = np.nanmax(np.abs(r))
+        tol = 1e-10 * np.maximum(np.abs(r), floor * scale)
+        bad = ~((g == r) | (np.isnan(g) & np.isnan(r)) | (np.abs(g - r) <= tol))
+        with np.errstate(invalid="ignore"):
+            rel = np.abs(g - r) / np.maximum(np.abs(r), floor * scale)
+        return {"entries": int(r.size), "outside_tol": int(bad.sum()),
+                "max_rel_err": float(np.nanmax(rel)) if np.isfinite(rel).any() else None}
+
+    return {"samples": KL_N, "oracle_s": dt,
+            "tolerance": "1e-10 relative (the gradient floored at 1e-3 of its largest entry)",
+            "objective_per_component": check(np.asarray(a["loss"]), loss, 0.0),
+            "coeff_grad": check(np.asarray(a["grad"]), grad, 1e-3)}
+
+
 def leg_c2_parity(a, chunk=50_000):
     """The timed run's outputs (T, log-det, reduced coefficient gradient)
     against the oracle's parity build on every one of the NPTS points (child
@@ -715,11 +752,13 @@ def leg_c2_parity(a, chunk=50_000):
     dt = time.perf_counter() - t0
 
     def check(g, r, floor):
-        scale = np.max(np.abs(r))
+        scale = np.nanmax(np.abs(r))
         tol = 1e-10 * np.maximum(np.abs(r), floor * scale)
-        bad = ~((g == r) | (np.abs(g - r) <= tol))
-        rel = np.abs(g - r) / np.maximum(np.abs(r), floor * scale)
-        return {"entries": int(r.size), "outside_tol": int(bad.sum()), "max_rel_err": float(rel.max())}
+        bad = ~((g == r) | (np.isnan(g) & np.isnan(r)) | (np.abs(g - r) <= tol))
+        with np.errstate(invalid="ignore"):
+            rel = np.abs(g - r) / np.maximum(np.abs(r), floor * scale)
+        return {"entries": int(r.size), "outside_tol": int(bad.sum()),
+                "max_rel_err": float(np.nanmax(rel)) if np.isfinite(rel).any() else None}
 
     return {"points": NPTS, "oracle_s": dt, "tolerance": "1e-10 relative (floor 1e-6 of the largest entry; "
                                                          "1e-3 for the gradient summed over points)",
@@ -975,7 +1014,11 @@ def run_gpu(args):
         line["parity_full"] = cpu_leg("c2-parity", T=out_T.cpu().numpy().reshape(-1), ld=out_ld.cpu().numpy(),
                                       cg=cg.cpu().numpy())
     if not args.no_kl:
-        kl, trained = kl_train(M, dev)
+        kl, trained, (kl_loss, kl_grad) = kl_train(M, dev)
+        if not args.no_parity:
+            # the batched step's values at the trained coefficients against the
+            # oracle on all KL_N samples
+            kl["parity_full"] = cpu_leg("kl-parity", coeffs=trained, loss=kl_loss, grad=kl_grad)
         kl["cpu_step"] = cpu_leg("kl", coeffs=trained)
         kl["cpu_step"]["speedup_graph"] = (kl["cpu_step"]["ms_per_step"] /
                                            kl["step_ms_at_trained_coeffs"]["graph_batched"])
