@@ -255,9 +255,10 @@ def batch_maps(M, dev, autotune=True):
 
 
 INV_DIM, INV_ORDER, INV_N, INV_TOL, INV_XTOL = 16, 3, 4_000_000, 1e-8, 1e-10
+INV_PARITY_N = 20_000
 
 
-def inverse_implicit(M, dev, cpu_seconds=8.0):
+def inverse_implicit(M, dev, cpu_seconds=8.0, parity=True):
     """Inverse at scale with implicit differentiation: a 16-D TriangularMap of
     total order 3 (969 terms in the last component), ProbHermite + SoftPlus,
     tol 1e-8, coefficients N(0, 0.03^2); 4,000,000 targets r ~ N(0, I_16);
@@ -312,6 +313,11 @@ def inverse_implicit(M, dev, cpu_seconds=8.0):
     # the oracle's Inverse on a bounded sample of the same targets (host cores)
     out["cpu_inverse"] = cpu_leg("inverse", coef=coef, r=r[:, :20000].cpu().numpy(), seconds=cpu_seconds)
     out["inverse_speedup_vs_cpu"] = out["inverse_points_per_s"] / out["cpu_inverse"]["points_per_s"]
+    if parity:
+        # the timed ITP roots of the first INV_PARITY_N targets against the
+        # oracle's ITP, component by component
+        out["parity_sample"] = cpu_leg("inverse-parity", coef=coef, r=r[:, :INV_PARITY_N].cpu().numpy(),
+                                       x=x[:, :INV_PARITY_N].cpu().numpy())
     return out
 
 
@@ -411,6 +417,48 @@ def leg_inverse(a):
             "sample": f"first {n2} targets, the oracle's Inverse (FindBracket + ITP); {CPU_BUILD}"}
 
 
+def leg_inverse_parity(a):
+    """The GPU's ITP roots against the oracle's (parity build), component by
+    component: the oracle solves component c from the GPU's own earlier
+    coordinates (child process).  The bar of the GPU tests: the same targets
+    without a root (NaN); roots within 2 (xtol + ytol / slope), and, for at
+    most 0.2 % of them (a last-bit change of T flipping an accept test of the
+    adaptive quadrature), within 2 (xtol + (ytol + tol (1 + |r|)) / slope)."""
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    om = O.OracleTriangularMap(INV_DIM, INV_DIM, INV_ORDER, abs_tol=INV_TOL, rel_tol=INV_TOL, max_sub=MAXSUB)
+    coef, r, xg = np.asarray(a["coef"]), np.asarray(a["r"]), np.asarray(a["x"])
+    n = r.shape[1]
+    cs = om.split(coef)
+    t0 = time.perf_counter()
+    nan_mismatch = strict_out = loose_out = roots = 0
+    worst = 0.0
+    for c, comp in enumerate(om.comps):
+        guess = np.zeros((comp.input_dim, n))
+        guess[:-1] = xg[:comp.input_dim - 1]
+        ref = comp.inverse(cs[c], guess, r[c], INV_XTOL, INV_XTOL)
+        got = xg[c]
+        nan_mismatch += int((np.isnan(ref) != np.isnan(got)).sum())
+        ok = ~np.isnan(ref) & ~np.isnan(got)
+        pt = guess.copy()
+        pt[-1] = np.where(ok, ref, 0.0)
+        slope = np.maximum(comp.cont_derivative(cs[c], pt), 1e-300)
+        diff = np.abs(got - ref)
+        bound = 2.0 * (INV_XTOL + INV_XTOL / slope)
+        loose = 2.0 * (INV_XTOL + (INV_XTOL + INV_TOL * (1.0 + np.abs(r[c]))) / slope)
+        strict_out += int((ok & (diff > bound)).sum())
+        loose_out += int((ok & (diff > loose)).sum())
+        roots += int(ok.sum())
+        if ok.any():
+            worst = max(worst, float(np.max(diff[ok] / bound[ok])))
+    return {"targets": n, "components": len(om.comps), "roots": roots, "oracle_s": time.perf_counter() - t0,
+            "nan_pattern_mismatches": nan_mismatch, "outside_2(xtol+ytol/slope)": strict_out,
+            "outside_loose_bound": loose_out, "max_diff_over_strict_bound": worst,
+            "bar": "NaN at the same targets; roots within 2 (xtol + ytol / slope) of the oracle's ITP, at most "
+                   "0.2 % within 2 (xtol + (ytol + tol (1 + |r|)) / slope) instead"}
+
+
 def leg_sigmoid(a):
     """The oracle's four reference calls per component of the sigmoid map on a
     bounded sample of its points (child process, timing build)."""
@@ -448,7 +496,7 @@ def cpu_leg(name, **arrays):
         f = os.path.join(d, "in.npz")
         np.savez(f, **{k: np.asarray(v) for k, v in arrays.items()})
         env = dict(os.environ, **TIMING_ENV)
-        if name in ("c2-parity", "kl-parity"):
+        if name in ("c2-parity", "kl-parity", "inverse-parity"):
             env.pop("MPGB_ORACLE_BUILD")  # parity: the strict build
         r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", name, "--cpu-in", f],
                            env=env, capture_output=True, text=True)
@@ -464,6 +512,7 @@ def run_cpu_leg(args):
             "kl": lambda: kl_cpu_step_ms(a["coeffs"]),
             "kl-parity": lambda: leg_kl_parity(a),
             "inverse": lambda: leg_inverse(a),
+            "inverse-parity": lambda: leg_inverse_parity(a),
             "sigmoid": lambda: leg_sigmoid(a)}
     print(json.dumps(legs[args.cpu_leg]()), flush=True)
 
@@ -1026,7 +1075,7 @@ def run_gpu(args):
     if not args.no_batch:
         line["batch_maps"] = batch_maps(M, dev)
     if not args.no_inverse:
-        line["inverse_implicit"] = inverse_implicit(M, dev)
+        line["inverse_implicit"] = inverse_implicit(M, dev, parity=not args.no_parity)
     if not args.no_sigmoid:
         line["sigmoid_maps"] = sigmoid_maps(M, dev)
     print(json.dumps(line), flush=True)
