@@ -1355,7 +1355,9 @@ static void orderPointsKL(MapWorkspace& W, KLPlan& P, const std::vector<Monotone
     if (P.permPts != pts.data || P.permRs != pts.rowStride || P.permCs != pts.colStride) {
         const size_t nComps = parts.size();
         P.perm.ensure(nComps * (size_t)N * sizeof(int), stream);
-        W.sortHist.ensure(sortScratchInts(N) * sizeof(int), stream);
+        // room for the step's all-component cost-order sort as well, which
+        // runs inside graph capture and so cannot allocate
+        W.sortHist.ensure(nComps * sortScratchInts(N) * sizeof(int), stream);
         for (size_t c = 0; c < nComps; ++c) {
             if (onlyComp >= 0 && (int)c != onlyComp) continue;
             const double* xd = pts.data + (int64_t)(parts[c].prog->D - 1) * pts.rowStride;
@@ -1436,12 +1438,12 @@ void MonotoneMapBase::KLObjective(StridedMatrix const& pts, double* lossPerComp,
                              P.nReduce, P.maxTerms, grad, W.lossPart.as<double>(), P.lossSlots.as<int>(),
                              1.0 / (double)N, lossPerComp, stream));
     if (costOrder) {
-        // the processing order of the next call
-        for (size_t c = 0; c < parts_.size(); ++c) {
-            if (onlyComp >= 0 && (int)c != onlyComp) continue;
-            MPGB_CUDA(launchSortByLast(P.costKey.as<double>() + c * (size_t)N, 1, N, W.sortHist.as<int>(),
-                                       P.perm.as<int>() + c * (size_t)N, stream));
-        }
+        // the processing order of the next call: every component's samples
+        // sorted in one launch set
+        const size_t c0 = onlyComp >= 0 ? (size_t)onlyComp : 0;
+        const int nSeg = onlyComp >= 0 ? 1 : (int)parts_.size();
+        MPGB_CUDA(launchSortByLastSegments(P.costKey.as<double>() + c0 * (size_t)N, 1, N, nSeg, N,
+                                           W.sortHist.as<int>(), P.perm.as<int>() + c0 * (size_t)N, N, stream));
     }
     Finish(stream, "KLObjective");
 }

@@ -57,7 +57,12 @@ constexpr int kSortChunk = 1024;
 
 __device__ __forceinline__ int sortKey(double x) { return sortBucket(x); }
 
-__global__ void keyHistKernel(const double* xd, long long stride, long long N, int* hist) {
+// Segment blockIdx.y of a multi-segment sort: keys at xd + y * keySeg,
+// histogram at hist + y * histSeg, permutation at perm + y * permSeg.
+__global__ void keyHistKernel(const double* xd, long long stride, long long N, int* hist, long long keySeg,
+                              long long histSeg) {
+    xd += blockIdx.y * keySeg;
+    hist += blockIdx.y * histSeg;
     __shared__ int h[kSortBuckets];
     for (int t = threadIdx.x; t < kSortBuckets; t += blockDim.x) h[t] = 0;
     __syncthreads();
@@ -71,7 +76,8 @@ __global__ void keyHistKernel(const double* xd, long long stride, long long N, i
 }
 
 // One block of kSortBuckets threads: hist[blk][b] -> first output slot of (blk, b).
-__global__ void keyScanKernel(int* hist, int nBlk) {
+__global__ void keyScanKernel(int* hist, int nBlk, long long histSeg) {
+    hist += blockIdx.x * histSeg;  // one block per segment
     __shared__ int tot[kSortBuckets];
     const int b = threadIdx.x;
     int s = 0;
@@ -96,7 +102,11 @@ __global__ void keyScanKernel(int* hist, int nBlk) {
 }
 
 // One warp per chunk, chunk order kept within each bucket.
-__global__ void keyScatterKernel(const double* xd, long long stride, long long N, const int* off, int* perm) {
+__global__ void keyScatterKernel(const double* xd, long long stride, long long N, const int* off, int* perm,
+                                 long long keySeg, long long histSeg, long long permSeg) {
+    xd += blockIdx.y * keySeg;
+    off += blockIdx.y * histSeg;
+    perm += blockIdx.y * permSeg;
     __shared__ int cnt[kSortBuckets];
     const int lane = threadIdx.x;
     for (int t = lane; t < kSortBuckets; t += 32) cnt[t] = 0;
@@ -375,11 +385,17 @@ size_t sortScratchInts(long long N) { return (size_t)((N + kSortChunk - 1) / kSo
 
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
                              cudaStream_t stream) {
-    if (N <= 0) return cudaSuccess;
+    return launchSortByLastSegments(xd, stride, 0, 1, N, hist, perm, 0, stream);
+}
+
+cudaError_t launchSortByLastSegments(const double* keys, long long stride, long long keySeg, int nSeg, long long N,
+                                     int* hist, int* perm, long long permSeg, cudaStream_t stream) {
+    if (N <= 0 || nSeg <= 0) return cudaSuccess;
     const int nBlk = (int)((N + kSortChunk - 1) / kSortChunk);
-    keyHistKernel<<<nBlk, 256, 0, stream>>>(xd, stride, N, hist);
-    keyScanKernel<<<1, kSortBuckets, 0, stream>>>(hist, nBlk);
-    keyScatterKernel<<<nBlk, 32, 0, stream>>>(xd, stride, N, hist, perm);
+    const long long histSeg = (long long)sortScratchInts(N);
+    keyHistKernel<<<dim3(nBlk, nSeg), 256, 0, stream>>>(keys, stride, N, hist, keySeg, histSeg);
+    keyScanKernel<<<nSeg, kSortBuckets, 0, stream>>>(hist, nBlk, histSeg);
+    keyScatterKernel<<<dim3(nBlk, nSeg), 32, 0, stream>>>(keys, stride, N, hist, perm, keySeg, histSeg, permSeg);
     const cudaError_t e = cudaGetLastError();
     countLaunches(stream, 3);
     return e;

@@ -33,6 +33,11 @@ cudaError_t launchKLReduce(const double* part, const long long* rowBase, const K
                            double* loss, cudaStream_t stream);
 // Stable counting sort of points by |x_D|: perm[j] = index of the j-th point.
 size_t sortScratchInts(long long N);
+// nSeg independent sorts in one launch set: keys of segment k at keys + k *
+// keySeg, its permutation at perm + k * permSeg; hist holds nSeg *
+// sortScratchInts(N) ints.
+cudaError_t launchSortByLastSegments(const double* keys, long long stride, long long keySeg, int nSeg, long long N,
+                                     int* hist, int* perm, long long permSeg, cudaStream_t stream);
 cudaError_t launchSortByLast(const double* xd, long long stride, long long N, int* hist, int* perm,
                              cudaStream_t stream);
 cudaError_t launchDfmaPeak(double* out, int blocks, int threads, int iters, cudaStream_t stream);
