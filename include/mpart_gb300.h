@@ -415,18 +415,35 @@ int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms)
  *   options: MapOptions::serialize (MParT/MapOptions.h:126-130);
  *   multi-index sets: FixedMultiIndexSet::save/load
  *     (MParT/MultiIndices/FixedMultiIndexSet.h:115-133).
- * MPGB_ARCHIVE_MAP is this library's whole-map archive (options, every
- * component's multi-index set, coefficients), the counterpart of the
- * reference's ToBytes / FromBytes / pickle, whose polymorphic cereal layout it
- * does not reproduce.  Writers use a two-call convention: *size always
- * receives the archive size, and the bytes are written when buf (cap bytes)
- * is large enough; buf == NULL only queries the size.
+ *   MPGB_ARCHIVE_MAP for monotone components and triangular maps of them:
+ *     the reference's ToBytes / FromBytes / pickle archive,
+ *     ParameterizedFunctionBase::Save / Load (MParT/ParameterizedFunctionBase.h:197-215;
+ *     bindings/python/src/ParameterizedFunctionBase.cpp:57-79), cereal's
+ *     polymorphic encoding of the map with its type names (as
+ *     "mpart::TriangularMap<Kokkos::HostSpace>"), the components' expansion,
+ *     quadrature, nugget and coefficient view, readable by the reference and
+ *     read from it.  The quadrature's integrand dimension in it is the one the
+ *     last reference-named operation left (Evaluate, LogDeterminant, ...).
+ * MPGB_ARCHIVE_MAP for maps of sigmoid expansions, which the reference does
+ * not archive, is this library's own (options, every component's multi-index
+ * set and Sigmoid1d arrays, coefficients).  Writers use a two-call
+ * convention: *size always receives the archive size, and the bytes are
+ * written when buf (cap bytes) is large enough; buf == NULL only queries the
+ * size.
  * ------------------------------------------------------------------------ */
 enum { MPGB_ARCHIVE_MAP = 0, MPGB_ARCHIVE_COEFFS = 1 };
 
 int mpgb_map_to_bytes(mpgb_map* map, int layout, unsigned char* buf, size_t cap, size_t* size);
-/* Rebuilds a component or triangular map (coefficients set) from an MPGB_ARCHIVE_MAP archive. */
+/* Rebuilds a component or triangular map from an MPGB_ARCHIVE_MAP archive (either
+ * layout) as the reference's Load does: components with the archive's
+ * coefficients, triangular maps with its moveCoeffs flag. */
 int mpgb_map_from_bytes(const unsigned char* buf, size_t size, mpgb_map** out);
+/* Host only (no device): reads a map archive in the reference's layout and
+ * writes it again from the description it holds (multi-index sets, options,
+ * quadrature state, coefficients and their view label), recomputing every
+ * derived field; an archive this library loads comes back unchanged.  Two-call
+ * convention as above. */
+int mpgb_map_archive_rewrite(const unsigned char* in, size_t in_size, unsigned char* buf, size_t cap, size_t* size);
 /* Reads an MPGB_ARCHIVE_COEFFS archive; coeffs (num_coeffs doubles, host) may be NULL to query sizes. */
 int mpgb_coeff_archive_read(const unsigned char* buf, size_t size, unsigned int* input_dim, unsigned int* output_dim,
                             unsigned int* num_coeffs, double* coeffs);

@@ -101,8 +101,15 @@ public:
     // (src/ParameterizedFunctionBase.cpp:185-207).  host = true for a host pointer.
     virtual void SetCoeffs(const double* coeffs, unsigned int n, bool host = false, cudaStream_t stream = 0);
     // Alias caller-owned device memory (src/ParameterizedFunctionBase.cpp:219-228).
-    virtual void WrapCoeffs(double* deviceCoeffs, unsigned int n);
+    virtual void WrapCoeffs(double* deviceCoeffs, unsigned int n) { WrapCoeffsLabeled(deviceCoeffs, n, std::string()); }
     double* Coeffs() const { return coeffs_; }
+    // Label of the coefficient view the reference would hold after the same
+    // calls, as its map archive records it: "ParameterizedFunctionBase<MemorySpace>
+    // Coefficients" for storage SetCoeffs allocated, "coeffs" for a
+    // TriangularMap built with moveCoeffs, "" for wrapped caller memory (an
+    // unmanaged view); a triangular map's components carry the map's label
+    // (src/ParameterizedFunctionBase.cpp:185-228, src/TriangularMap.cpp:38-98).
+    std::string const& CoeffLabel() const { return coeffLabel_; }
     bool CheckCoefficients() const { return coeffs_ != nullptr; }
     void CheckCoefficients(std::string const& functionName) const;
     std::vector<double> CoeffMap() const;  // host copy
@@ -122,6 +129,10 @@ public:
 
 protected:
     virtual void OnCoeffsChanged() {}
+    // WrapCoeffs with the label of the wrapped view.
+    virtual void WrapCoeffsLabeled(double* deviceCoeffs, unsigned int n, std::string const& label);
+    friend class TriangularMap;
+    std::string coeffLabel_;
     double* coeffs_ = nullptr;
     double* owned_ = nullptr;
     bool async_ = false;
@@ -309,10 +320,12 @@ class TriangularMap : public MonotoneMapBase {
 public:
     TriangularMap(std::vector<std::shared_ptr<ConditionalMapBase>> const& components, bool moveCoeffs = false);
     void SetCoeffs(const double* coeffs, unsigned int n, bool host = false, cudaStream_t stream = 0) override;
-    void WrapCoeffs(double* deviceCoeffs, unsigned int n) override;
     std::shared_ptr<ConditionalMapBase> GetComponent(unsigned int i) { return comps_.at(i); }
     unsigned int NumComponents() const { return (unsigned int)comps_.size(); }
     void FillCoeffBoundsImpl(double* lb, double* ub) const override;  // src/TriangularMap.cpp:313-325
+
+protected:
+    void WrapCoeffsLabeled(double* deviceCoeffs, unsigned int n, std::string const& label) override;
 
 private:
     std::vector<std::shared_ptr<ConditionalMapBase>> comps_;

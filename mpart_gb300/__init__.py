@@ -260,10 +260,19 @@ def _wrap_map(h, keep=()):
 
 def FromBytes(data: bytes):
     """ParameterizedFunctionBase.FromBytes: rebuilds a component or triangular
-    map (with its coefficients) from ConditionalMapBase.ToBytes()."""
+    map (with its coefficients) from ConditionalMapBase.ToBytes() or from the
+    reference's ToBytes / pickle archive."""
     h = C.c_void_p()
     check(load().mpgb_map_from_bytes(data, len(data), C.byref(h)))
     return _wrap_map(h)
+
+
+def RewriteMapArchive(data: bytes) -> bytes:
+    """Reads a map archive in the reference's layout and writes it again from
+    the map description it holds, on the host (no GPU): checks that this
+    library can load it; an archive it loads comes back unchanged."""
+    data = bytes(data)
+    return _archive(lambda buf, cap, size: load().mpgb_map_archive_rewrite(data, len(data), buf, cap, size))
 
 
 def _stream_of(*arrs):
@@ -495,7 +504,8 @@ class ConditionalMapBase:
             f.write(_archive(lambda buf, cap, size: load().mpgb_map_to_bytes(self._h, 1, buf, cap, size)))
 
     def ToBytes(self) -> bytes:
-        """The whole map (options, multi-index sets, coefficients); FromBytes rebuilds it."""
+        """The whole map, in the reference's ToBytes / pickle layout for monotone
+        components and triangular maps of them; FromBytes rebuilds it."""
         return _archive(lambda buf, cap, size: load().mpgb_map_to_bytes(self._h, 0, buf, cap, size))
 
     FromBytes = staticmethod(lambda data: FromBytes(data))

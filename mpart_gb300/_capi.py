@@ -132,6 +132,7 @@ SIGNATURES = {
     "mpgb_map_is_triangular": (C.c_int, [_MAP, C.POINTER(C.c_int)]),
     "mpgb_map_to_bytes": (C.c_int, [_MAP, C.c_int, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "mpgb_map_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, _MAPP]),
+    "mpgb_map_archive_rewrite": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "mpgb_coeff_archive_read": (C.c_int, [C.c_void_p, C.c_size_t, _UP, _UP, _UP, C.c_void_p]),
     "mpgb_options_to_bytes": (C.c_int, [C.POINTER(mpgb_map_options), C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "mpgb_options_from_bytes": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(mpgb_map_options)]),

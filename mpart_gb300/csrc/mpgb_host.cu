@@ -382,6 +382,7 @@ void ParameterizedFunctionBase::SetCoeffs(const double* coeffs, unsigned int n, 
     if (!coeffs_) {
         if (!owned_ && numCoeffs > 0) MPGB_CUDA(cudaMalloc(&owned_, numCoeffs * sizeof(double)));
         coeffs_ = owned_;
+        coeffLabel_ = "ParameterizedFunctionBase<MemorySpace> Coefficients";
     }
     if (numCoeffs > 0) {
         if (host) {
@@ -394,7 +395,7 @@ void ParameterizedFunctionBase::SetCoeffs(const double* coeffs, unsigned int n, 
     OnCoeffsChanged();
 }
 
-void ParameterizedFunctionBase::WrapCoeffs(double* deviceCoeffs, unsigned int n) {
+void ParameterizedFunctionBase::WrapCoeffsLabeled(double* deviceCoeffs, unsigned int n, std::string const& label) {
     if (n != numCoeffs) {
         std::ostringstream os;
         os << "Error in ParameterizedFunctionBase<MemorySpace>::WrapCoeffs.  Expected coefficient vector with size "
@@ -402,6 +403,7 @@ void ParameterizedFunctionBase::WrapCoeffs(double* deviceCoeffs, unsigned int n)
         throw std::invalid_argument(os.str());
     }
     coeffs_ = deviceCoeffs;
+    coeffLabel_ = label;
     OnCoeffsChanged();
 }
 
@@ -424,7 +426,7 @@ std::vector<double> ParameterizedFunctionBase::CoeffMap() const {
 // ---------------------------------------------------------------------------
 // MonotoneMapBase
 // ---------------------------------------------------------------------------
-static void ccRule(unsigned numPts, double* wts, double* pts) {
+void ccRule(unsigned numPts, double* wts, double* pts) {
     // Clenshaw-Curtis points and weights on [-1,1] (Quadrature.h:212-258).
     if (numPts == 1) { pts[0] = 0.0; wts[0] = 2.0; return; }
     for (unsigned i = 0; i < numPts; ++i) pts[i] = std::cos((numPts - (i + 1)) * kPiHost / (numPts - 1));
@@ -862,11 +864,29 @@ static void launch(MapWorkspace& W, const MapOptions& o, FusedParams& p, int nIt
     MPGB_CUDA(launchFused(W.basis, posCode(o), W.pmax, p, nItems, needJ, needE, stream));
 }
 
+// The quadrature dimension each reference operation leaves on its components
+// (ComponentProgram::quadDim): 1 after Evaluate and Inverse, 2 after the
+// discrete-derivative LogDeterminant and LogDeterminantCoeffGrad, inputs + 1
+// after Gradient, terms + 1 after CoeffGrad; the continuous-derivative
+// operations integrate nothing and leave it.
+enum class QuadDimRule { One, Two, InputsPlusOne, TermsPlusOne };
+
+static void noteQuadDim(std::vector<MonotoneMapBase::Part> const& parts, QuadDimRule rule) {
+    for (auto& pt : parts) {
+        ComponentProgram& g = *pt.prog;
+        g.quadDim = rule == QuadDimRule::One ? 1u
+                    : rule == QuadDimRule::Two ? 2u
+                    : rule == QuadDimRule::InputsPlusOne ? (unsigned)g.D + 1u
+                                                         : (unsigned)g.numTerms + 1u;
+    }
+}
+
 void MonotoneMapBase::EvaluateImpl(StridedMatrix const& pts, StridedMatrix const& output, cudaStream_t stream) {
     CheckCoefficients("Evaluate");
     const long long N = pts.cols;
     checkMatrix(pts, inputDim, N, "pts", "EvaluateImpl");
     checkMatrix(output, outputDim, N, "output", "EvaluateImpl");
+    noteQuadDim(parts_, QuadDimRule::One);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -891,6 +911,7 @@ void MonotoneMapBase::LogDeterminantImpl(StridedMatrix const& pts, StridedMatrix
     const long long N = pts.cols;
     checkMatrix(pts, inputDim, N, "pts", "LogDeterminantImpl");
     if (output.rows * output.cols != N) throw std::invalid_argument("LogDeterminantImpl: output must hold N values.");
+    if (!opts_.contDeriv) noteQuadDim(parts_, QuadDimRule::Two);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -913,6 +934,7 @@ void MonotoneMapBase::CoeffGradImpl(StridedMatrix const& pts, StridedMatrix cons
     checkMatrix(pts, inputDim, N, "pts", "CoeffGradImpl");
     checkMatrix(sens, outputDim, N, "sens", "CoeffGradImpl");
     checkMatrix(output, numCoeffs, N, "output", "CoeffGradImpl");
+    noteQuadDim(parts_, QuadDimRule::TermsPlusOne);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -935,6 +957,7 @@ void MonotoneMapBase::LogDeterminantCoeffGradImpl(StridedMatrix const& pts, Stri
     const long long N = pts.cols;
     checkMatrix(pts, inputDim, N, "pts", "LogDeterminantCoeffGradImpl");
     checkMatrix(output, numCoeffs, N, "output", "LogDeterminantCoeffGradImpl");
+    if (!opts_.contDeriv) noteQuadDim(parts_, QuadDimRule::Two);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -956,6 +979,7 @@ void MonotoneMapBase::GradientImpl(StridedMatrix const& pts, StridedMatrix const
     checkMatrix(pts, inputDim, N, "pts", "GradientImpl");
     checkMatrix(sens, outputDim, N, "sens", "GradientImpl");
     checkMatrix(output, inputDim, N, "output", "GradientImpl");
+    noteQuadDim(parts_, QuadDimRule::InputsPlusOne);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -1020,6 +1044,7 @@ void MonotoneMapBase::InverseImpl(StridedMatrix const& x1, StridedMatrix const& 
     }
     if (x1.rows > inputDim) throw std::invalid_argument("InverseImpl: x1 has too many rows.");
     checkMatrix(output, outputDim, N, "output", "InverseImpl");
+    noteQuadDim(parts_, QuadDimRule::One);
     if (N == 0) return;
     Prepare(stream);
     MapWorkspace& W = *ws_;
@@ -1699,7 +1724,7 @@ TriangularMap::TriangularMap(std::vector<std::shared_ptr<ConditionalMapBase>> co
         MPGB_CUDA(cudaMalloc(&owned_, std::max<size_t>(1, all.size()) * sizeof(double)));
         if (!all.empty())
             MPGB_CUDA(cudaMemcpy(owned_, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
-        WrapCoeffs(owned_, numCoeffs);
+        WrapCoeffsLabeled(owned_, numCoeffs, "coeffs");
     }
 }
 
@@ -1711,20 +1736,21 @@ void TriangularMap::FillCoeffBoundsImpl(double* lb, double* ub) const {
     }
 }
 
+// The components view slices of the map's coefficients, under its label.
 void TriangularMap::SetCoeffs(const double* coeffs, unsigned int n, bool host, cudaStream_t stream) {
     ConditionalMapBase::SetCoeffs(coeffs, n, host, stream);
     unsigned off = 0;
     for (auto& c : comps_) {
-        c->WrapCoeffs(coeffs_ + off, c->numCoeffs);
+        c->WrapCoeffsLabeled(coeffs_ + off, c->numCoeffs, coeffLabel_);
         off += c->numCoeffs;
     }
 }
 
-void TriangularMap::WrapCoeffs(double* deviceCoeffs, unsigned int n) {
-    ConditionalMapBase::WrapCoeffs(deviceCoeffs, n);
+void TriangularMap::WrapCoeffsLabeled(double* deviceCoeffs, unsigned int n, std::string const& label) {
+    ConditionalMapBase::WrapCoeffsLabeled(deviceCoeffs, n, label);
     unsigned off = 0;
     for (auto& c : comps_) {
-        c->WrapCoeffs(coeffs_ + off, c->numCoeffs);
+        c->WrapCoeffsLabeled(coeffs_ + off, c->numCoeffs, coeffLabel_);
         off += c->numCoeffs;
     }
 }

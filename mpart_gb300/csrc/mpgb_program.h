@@ -66,6 +66,11 @@ struct ComponentProgram {
     int32_t *dSlotTerm = nullptr, *dLeadDeg = nullptr, *dRowOff = nullptr, *dNodeCIdx = nullptr;
     // Work per point (FP64 operations of phases A and C), for load balancing.
     double weight = 1.0;
+    // Integrand dimension of the reference component's quadrature object,
+    // which its operations set in place (quad_.SetDim, MonotoneComponent.h:270,
+    // :401, :599, :697, :770, :940) and its map archive records; no effect on
+    // the computation here.
+    unsigned quadDim = 1;
     // Reduced adjoint: the tile's points are split into cSegs segments and the
     // block's threads take (node, segment) units, so that a few hundred nodes
     // still keep every thread busy; each segment has its own partial row.
@@ -233,6 +238,10 @@ struct ComponentProgram {
 
 // Records the message returned by mpgb_last_error() on this thread.
 void setLastError(const std::string& msg);
+
+// Clenshaw-Curtis points and weights on [-1, 1], as
+// ClenshawCurtisQuadrature::GetRule computes them (Quadrature.h:212-258).
+void ccRule(unsigned numPts, double* wts, double* pts);
 
 }  // namespace mpgb
 

@@ -15,14 +15,18 @@
 //   * FixedMultiIndexSet::save (MParT/MultiIndices/FixedMultiIndexSet.h:115-123):
 //     dim (uint32), isCompressed (byte), then the views nzStarts, nzDims,
 //     nzOrders, maxDegrees.
-// The whole-map archive (the reference's polymorphic ToBytes / pickle, which
-// depends on cereal's type registry) has a layout of its own: a tag, the
-// options, each monotone component's multi-index set, then the coefficient
-// archive; it rebuilds the same component or triangular map.
+// The whole-map archive of ToBytes / FromBytes / pickle is the reference's own
+// (ParameterizedFunctionBase::Save, cereal's polymorphic encoding; see
+// RefWriter below) for monotone components and triangular maps of them.
+// Sigmoid expansions, which the reference does not archive, have a layout of
+// this library's own: a tag, the options, each component's multi-index set and
+// Sigmoid1d arrays, then the coefficient archive.
 #include <cmath>
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <map>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -80,7 +84,12 @@ struct Reader {
     }
     template <class T>
     std::vector<T> view() {
-        str();  // label
+        std::string label;
+        return view<T>(label);
+    }
+    template <class T>
+    std::vector<T> view(std::string& label) {
+        label = str();
         const uint32_t len = pod<uint32_t>();
         need((size_t)len * sizeof(T));
         std::vector<T> v(len);
@@ -204,6 +213,401 @@ void components(const std::shared_ptr<ConditionalMapBase>& m, std::vector<const 
     throw std::invalid_argument("only monotone components, sigmoid expansions and triangular maps can be archived");
 }
 
+// ---------------------------------------------------------------------------
+// The reference's map archive: ParameterizedFunctionBase::Save / Load
+// (MParT/ParameterizedFunctionBase.h:197-215), behind its ToBytes, FromBytes
+// and pickle (bindings/python/src/ParameterizedFunctionBase.cpp:57-79).  It is
+// cereal's (v1.3.2) encoding of a shared_ptr to a polymorphic object: a uint32
+// type id (top bit set on the type's first use, followed by its registered
+// name as a string), then a uint32 object id (top bit set on the object's
+// first use, followed by the object's data); both count from 1 in order of
+// first use.
+//   * TriangularMap<Kokkos::HostSpace> (TriangularMap.h:130-138): its
+//     components as a vector of such pointers (uint64 count), the same vector
+//     again (ids only: every object has been written), then moveCoeffs, one
+//     byte: whether the map holds a coefficient view.
+//   * MonotoneComponent (MonotoneComponent.h:1037-1044): its
+//     MultivariateExpansionWorker (MultivariateExpansionWorker.h:406-412:
+//     input dimension, multi-index set, the 1-D basis's normalisation flag --
+//     HermiteFunction's is that of its PhysicistHermite, false -- the cache
+//     start positions and size); its quadrature (Quadrature.h:66-90 for
+//     every rule: integrand dimension, maximum dimension, workspace size,
+//     internal workspace; :422-435 for the adaptive rules: maxSub, minSub,
+//     absTol, relTol, error metric; :313-326 for fixed Clenshaw-Curtis:
+//     points, weights, count; :970-984 for adaptive Clenshaw-Curtis: the
+//     coarse and fine rules, the fine weights under the label "Coarse Pts" as
+//     the constructor names them, Quadrature.h:1054-1058); useContDeriv; the
+//     nugget; its coefficient view.
+// MapFactory builds every quadrature with maximum dimension 1, an external
+// workspace (none held) for the adaptive rules and a one-double internal one
+// for fixed Clenshaw-Curtis, and error metric QuadError::First
+// (src/MapFactoryImpl4.cpp:17-20, Impl5:17, Impl6:17).
+// Only the description of the map -- multi-index sets, options, the
+// quadrature's integrand dimension, coefficients and their view label -- is
+// kept; the writer recomputes the rest, and the reader checks it.
+// The reference's TriangularMap loader reads moveCoeffs from the byte after
+// the first component vector (the low byte of the second vector's count);
+// this reader follows the layout the writer produces.
+// ---------------------------------------------------------------------------
+
+constexpr uint32_t kNewId = 0x80000000u;
+
+struct RefComp {
+    FixedMultiIndexSet mset{1, 0};
+    MapOptions opts;
+    unsigned quadDim = 1;
+    bool hasCoeffs = false;
+    std::string label;
+    std::vector<double> coeffs;
+};
+
+struct RefNode {
+    bool triangular = false;
+    RefComp comp;                                     // a component
+    std::vector<std::shared_ptr<RefNode>> children;  // a triangular map
+    bool moveCoeffs = false;
+};
+
+const char* const kSpaces[2] = {"Kokkos::HostSpace", "mpart::DeviceSpace"};
+const BasisTypes kArchBases[2] = {BasisTypes::ProbabilistHermite, BasisTypes::HermiteFunctions};
+const PosFuncTypes kArchPos[2] = {PosFuncTypes::Exp, PosFuncTypes::SoftPlus};
+const QuadTypes kArchQuads[3] = {QuadTypes::AdaptiveClenshawCurtis, QuadTypes::ClenshawCurtis,
+                                 QuadTypes::AdaptiveSimpson};
+
+// Registered names: the arguments of CEREAL_REGISTER_TYPE as written
+// (src/TriangularMap.cpp:336, MParT/Utilities/Serialization.h:14-15 with the
+// arguments of src/MapFactoryImpl4.cpp-9.cpp).
+std::string triangularName(int space) { return std::string("mpart::TriangularMap<") + kSpaces[space] + ">"; }
+
+std::string componentName(BasisTypes b, PosFuncTypes p, QuadTypes q, int space) {
+    const std::string sp = kSpaces[space];
+    const char* basis = b == BasisTypes::HermiteFunctions ? "HermiteFunction" : "ProbabilistHermite";
+    const char* pos = p == PosFuncTypes::Exp ? "Exp" : "SoftPlus";
+    const char* quad = q == QuadTypes::AdaptiveClenshawCurtis ? "AdaptiveClenshawCurtis"
+                       : q == QuadTypes::AdaptiveSimpson     ? "AdaptiveSimpson"
+                                                             : "ClenshawCurtisQuadrature";
+    return "mpart::MonotoneComponent<mpart::MultivariateExpansionWorker<mpart::BasisEvaluator<"
+           "BasisHomogeneity::Homogeneous, " +
+           std::string(basis) + ">, " + sp + ">, mpart::" + pos + ", mpart::" + quad + "<" + sp + ">, " + sp + ">";
+}
+
+// Start of each 1-D basis block in the expansion's cache: an exclusive scan of
+// maxDegrees(i % dim) + 1 over 2 dim entries, then maxDegrees(dim - 1) + 1
+// (MultivariateExpansionWorker.h:19-39, :94-106); the cache size is the last.
+std::vector<unsigned> startPositions(const FixedMultiIndexSet& m) {
+    const unsigned dim = m.Length();
+    std::vector<unsigned> sp(2 * dim + 2);
+    unsigned run = 0;
+    for (unsigned i = 0; i < 2 * dim + 2; ++i) {
+        sp[i] = run;
+        run += (i < 2 * dim ? m.maxDegrees[i % dim] : m.maxDegrees[dim - 1]) + 1;
+    }
+    return sp;
+}
+
+// Workspace size for an integrand of dimension fdim (GetWorkspaceSize,
+// Quadrature.h:172, :520, :786).
+uint32_t workspaceSize(QuadTypes q, unsigned maxSub, unsigned fdim) {
+    if (q == QuadTypes::AdaptiveClenshawCurtis) return (maxSub + 5) * fdim + 2 * maxSub;
+    if (q == QuadTypes::AdaptiveSimpson) return (2 * maxSub + 5) * fdim + 2 * maxSub;
+    return fdim;
+}
+
+// Level of the adaptive Clenshaw-Curtis rule (src/MapFactoryImpl4.cpp:18).
+unsigned accLevel(unsigned quadPts) { return (unsigned)std::log2((double)(quadPts - 2u)); }
+
+class RefWriter {
+public:
+    Writer w;
+
+    void object(const std::shared_ptr<RefNode>& n) {
+        const std::string name =
+            n->triangular ? triangularName(0)
+                          : componentName(n->comp.opts.basisType, n->comp.opts.posFuncType, n->comp.opts.quadType, 0);
+        auto t = types_.find(name);
+        if (t == types_.end()) {
+            const uint32_t id = (uint32_t)types_.size() + 1;
+            types_.emplace(name, id);
+            w.pod<uint32_t>(id | kNewId);
+            w.str(name);
+        } else {
+            w.pod<uint32_t>(t->second);
+        }
+        auto o = objects_.find(n.get());
+        if (o != objects_.end()) {
+            w.pod<uint32_t>(o->second);
+            return;
+        }
+        const uint32_t id = (uint32_t)objects_.size() + 1;
+        objects_.emplace(n.get(), id);
+        w.pod<uint32_t>(id | kNewId);
+        if (n->triangular)
+            triangular(*n);
+        else
+            component(n->comp);
+    }
+
+private:
+    void triangular(const RefNode& n) {
+        for (int pass = 0; pass < 2; ++pass) {
+            w.pod<uint64_t>(n.children.size());
+            for (auto& c : n.children) object(c);
+        }
+        w.pod<uint8_t>(n.moveCoeffs ? 1 : 0);
+    }
+
+    void component(const RefComp& c) {
+        const FixedMultiIndexSet& m = c.mset;
+        const MapOptions& o = c.opts;
+        w.pod<uint32_t>(m.Length());
+        writeMset(w, m);
+        w.pod<uint8_t>(o.basisType != BasisTypes::HermiteFunctions && o.basisNorm ? 1 : 0);
+        const std::vector<unsigned> sp = startPositions(m);
+        w.view<unsigned int>("Indices for start of 1d basis evaluations", sp.data(), sp.size());
+        w.pod<uint32_t>(sp.back());
+
+        const bool fixed = o.quadType == QuadTypes::ClenshawCurtis;
+        w.pod<uint32_t>(c.quadDim);
+        w.pod<uint32_t>(1u);
+        w.pod<uint32_t>(workspaceSize(o.quadType, o.quadMaxSub, c.quadDim));
+        const double zero = 0.0;
+        if (fixed)
+            w.view<double>("Workspace", &zero, 1);
+        else
+            w.view<double>("", nullptr, 0);
+        if (fixed) {
+            std::vector<double> pts(o.quadPts), wts(o.quadPts);
+            ccRule(o.quadPts, wts.data(), pts.data());
+            w.view<double>("Points", pts.data(), pts.size());
+            w.view<double>("Weights", wts.data(), wts.size());
+            w.pod<uint32_t>(o.quadPts);
+        } else {
+            w.pod<uint32_t>(o.quadMaxSub);
+            w.pod<uint32_t>(o.quadMinSub);
+            w.pod<double>(o.quadAbsTol);
+            w.pod<double>(o.quadRelTol);
+            w.pod<uint32_t>(0u);  // QuadError::First
+            if (o.quadType == QuadTypes::AdaptiveClenshawCurtis) {
+                const unsigned level = accLevel(o.quadPts);
+                const unsigned nc = (1u << level) + 1, nf = (1u << (level + 1)) + 1;
+                std::vector<double> cp(nc), cw(nc), fp(nf), fw(nf);
+                ccRule(nc, cw.data(), cp.data());
+                ccRule(nf, fw.data(), fp.data());
+                w.view<double>("Coarse Pts", cp.data(), nc);
+                w.view<double>("Coarse Wts", cw.data(), nc);
+                w.view<double>("Fine Pts", fp.data(), nf);
+                w.view<double>("Coarse Pts", fw.data(), nf);
+            }
+        }
+        w.pod<uint8_t>(o.contDeriv ? 1 : 0);
+        w.pod<double>(o.nugget);
+        if (c.hasCoeffs)
+            w.view<double>(c.label, c.coeffs.data(), c.coeffs.size());
+        else
+            w.view<double>("", nullptr, 0);
+    }
+
+    std::map<std::string, uint32_t> types_;
+    std::map<const RefNode*, uint32_t> objects_;
+};
+
+class RefReader {
+public:
+    explicit RefReader(Reader& r) : r_(r) {}
+
+    std::shared_ptr<RefNode> object() {
+        const uint32_t tid = r_.pod<uint32_t>();
+        if (tid == 0) throw std::invalid_argument("map archive: null map pointer");
+        std::string name;
+        if (tid & kNewId) {
+            name = r_.str();
+            types_[tid & ~kNewId] = name;
+        } else {
+            auto it = types_.find(tid);
+            if (it == types_.end()) throw std::invalid_argument("map archive: unknown type id");
+            name = it->second;
+        }
+        const uint32_t oid = r_.pod<uint32_t>();
+        if (!(oid & kNewId)) {
+            auto it = objects_.find(oid);
+            if (it == objects_.end()) throw std::invalid_argument("map archive: unknown object id");
+            return it->second;
+        }
+        auto n = std::make_shared<RefNode>();
+        objects_[oid & ~kNewId] = n;
+        if (name == triangularName(0) || name == triangularName(1)) {
+            n->triangular = true;
+            triangular(*n);
+            return n;
+        }
+        for (int sp = 0; sp < 2; ++sp)
+            for (BasisTypes b : kArchBases)
+                for (PosFuncTypes p : kArchPos)
+                    for (QuadTypes q : kArchQuads)
+                        if (name == componentName(b, p, q, sp)) {
+                            n->comp.opts.basisType = b;
+                            n->comp.opts.posFuncType = p;
+                            n->comp.opts.quadType = q;
+                            component(n->comp);
+                            return n;
+                        }
+        if (name.rfind("mpart::MonotoneComponent<", 0) == 0)
+            throw std::invalid_argument(
+                "map archive: component basis not provided here (ProbabilistHermite and HermiteFunction only): " +
+                name);
+        throw std::invalid_argument("map archive: map type not provided here: " + name);
+    }
+
+private:
+    static void bad(const char* what) { throw std::invalid_argument(std::string("map archive: ") + what); }
+
+    void triangular(RefNode& n) {
+        const uint64_t count = r_.pod<uint64_t>();
+        if (count == 0 || count > r_.n - r_.off) bad("bad component count");
+        for (uint64_t i = 0; i < count; ++i) n.children.push_back(object());
+        // the component vector written again, ids only
+        const size_t mark = r_.off;
+        bool again = r_.n - r_.off >= 8 + 8 * count + 1 && r_.pod<uint64_t>() == count;
+        for (uint64_t i = 0; again && i < count; ++i) {
+            const uint32_t tid = r_.pod<uint32_t>(), oid = r_.pod<uint32_t>();
+            auto it = objects_.find(oid);
+            again = !(tid & kNewId) && types_.count(tid) && it != objects_.end() && it->second == n.children[i];
+        }
+        if (!again) r_.off = mark;
+        n.moveCoeffs = r_.pod<uint8_t>() != 0;
+    }
+
+    void component(RefComp& c) {
+        MapOptions& o = c.opts;
+        const uint32_t dim = r_.pod<uint32_t>();
+        c.mset = readMset(r_);
+        if (dim != c.mset.Length()) bad("expansion dimension does not match its multi-index set");
+        const uint8_t norm = r_.pod<uint8_t>();
+        if (o.basisType == BasisTypes::HermiteFunctions) {
+            if (norm != 0) bad("Hermite functions over normalised Hermite polynomials are not provided");
+        } else {
+            o.basisNorm = norm != 0;
+        }
+        const std::vector<unsigned> sp = r_.view<unsigned>();
+        const uint32_t cacheSize = r_.pod<uint32_t>();
+        if (sp != startPositions(c.mset) || cacheSize != sp.back())
+            bad("expansion cache layout does not match its multi-index set");
+
+        const bool fixed = o.quadType == QuadTypes::ClenshawCurtis;
+        const uint32_t fdim = r_.pod<uint32_t>(), maxDim = r_.pod<uint32_t>(), ws = r_.pod<uint32_t>();
+        const std::vector<double> internal = r_.view<double>();
+        if (maxDim != 1 || internal.size() != (fixed ? 1u : 0u))
+            bad("quadrature workspace not as MapFactory builds it (maximum dimension 1)");
+        if (fdim == 0) bad("quadrature of dimension 0");
+        if (fixed) {
+            const std::vector<double> pts = r_.view<double>(), wts = r_.view<double>();
+            const uint32_t numPts = r_.pod<uint32_t>();
+            if (pts.size() != numPts || wts.size() != numPts) bad("Clenshaw-Curtis rule sizes disagree");
+            o.quadPts = numPts;
+        } else {
+            o.quadMaxSub = r_.pod<uint32_t>();
+            o.quadMinSub = r_.pod<uint32_t>();
+            o.quadAbsTol = r_.pod<double>();
+            o.quadRelTol = r_.pod<double>();
+            if (r_.pod<uint32_t>() != 0) bad("quadrature error metrics other than QuadError::First are not provided");
+            if (o.quadType == QuadTypes::AdaptiveClenshawCurtis) {
+                const std::vector<double> cp = r_.view<double>(), cw = r_.view<double>();
+                const std::vector<double> fp = r_.view<double>(), fw = r_.view<double>();
+                unsigned level = 0;
+                while (level < 30 && (1u << level) + 1 < cp.size()) ++level;
+                if (cp.size() != (1u << level) + 1 || cw.size() != cp.size() ||
+                    fp.size() != (1u << (level + 1)) + 1 || fw.size() != fp.size())
+                    bad("adaptive Clenshaw-Curtis rule sizes disagree");
+                o.quadPts = (1u << (level + 1)) + 1;  // any quadPts of this level
+            }
+        }
+        if (ws != workspaceSize(o.quadType, o.quadMaxSub, fdim)) bad("quadrature workspace size disagrees");
+        c.quadDim = fdim;
+        o.contDeriv = r_.pod<uint8_t>() != 0;
+        o.nugget = r_.pod<double>();
+        c.coeffs = r_.view<double>(c.label);
+        // MonotoneComponent::load_and_construct (MonotoneComponent.h:1046-1062)
+        // keeps coefficients only of the right size.
+        c.hasCoeffs = c.coeffs.size() == c.mset.Size() && !c.coeffs.empty();
+        if (!c.hasCoeffs) c.coeffs.clear();
+    }
+
+    Reader& r_;
+    std::map<uint32_t, std::string> types_;
+    std::map<uint32_t, std::shared_ptr<RefNode>> objects_;
+};
+
+// The archive's description of a map of this library, or null when it holds
+// a component the reference cannot archive (sigmoid expansions).
+std::shared_ptr<RefNode> describe(const std::shared_ptr<ConditionalMapBase>& m,
+                                  std::map<const ConditionalMapBase*, std::shared_ptr<RefNode>>& memo) {
+    auto it = memo.find(m.get());
+    if (it != memo.end()) return it->second;
+    auto n = std::make_shared<RefNode>();
+    if (auto* t = dynamic_cast<TriangularMap*>(m.get())) {
+        n->triangular = true;
+        for (unsigned i = 0; i < t->NumComponents(); ++i) {
+            auto c = describe(t->GetComponent(i), memo);
+            if (!c) return nullptr;
+            n->children.push_back(c);
+        }
+        n->moveCoeffs = t->CheckCoefficients() && t->numCoeffs > 0;
+    } else if (auto* c = dynamic_cast<MonotoneComponent*>(m.get())) {
+        RefComp& rc = n->comp;
+        rc.mset = c->GetMultiIndexSet();
+        rc.opts = c->Options();
+        rc.quadDim = c->Parts().at(0).prog->quadDim;
+        rc.hasCoeffs = c->CheckCoefficients() && c->numCoeffs > 0;
+        rc.label = c->CoeffLabel();
+        if (rc.hasCoeffs) rc.coeffs = c->CoeffMap();
+    } else {
+        return nullptr;
+    }
+    memo[m.get()] = n;
+    return n;
+}
+
+// The map the reference's Load builds: components constructed with their
+// coefficients (copied: MonotoneComponent.h:1057, ParameterizedFunctionBase.h:35),
+// triangular maps with their moveCoeffs flag (TriangularMap.h:141-149).
+std::shared_ptr<ConditionalMapBase> build(const std::shared_ptr<RefNode>& n,
+                                          std::map<const RefNode*, std::shared_ptr<ConditionalMapBase>>& memo) {
+    auto it = memo.find(n.get());
+    if (it != memo.end()) return it->second;
+    std::shared_ptr<ConditionalMapBase> m;
+    if (n->triangular) {
+        std::vector<std::shared_ptr<ConditionalMapBase>> comps;
+        for (auto& c : n->children) comps.push_back(build(c, memo));
+        m = std::make_shared<TriangularMap>(comps, n->moveCoeffs);
+    } else {
+        auto c = std::make_shared<MonotoneComponent>(n->comp.mset, n->comp.opts);
+        if (n->comp.hasCoeffs) c->SetCoeffs(n->comp.coeffs.data(), (unsigned)n->comp.coeffs.size(), true);
+        c->Parts().at(0).prog->quadDim = n->comp.quadDim;
+        m = c;
+    }
+    memo[n.get()] = m;
+    return m;
+}
+
+bool isRefArchive(const unsigned char* buf, size_t size) {
+    if (size < 4) return false;
+    uint32_t first;
+    std::memcpy(&first, buf, 4);
+    return (first & kNewId) != 0;
+}
+
+std::shared_ptr<RefNode> readRefArchive(const unsigned char* buf, size_t size) {
+    Reader r(buf, size);
+    RefReader rr(r);
+    return rr.object();
+}
+
+std::vector<unsigned char> writeRefArchive(const std::shared_ptr<RefNode>& root) {
+    RefWriter rw;
+    rw.object(root);
+    return rw.w.b;
+}
+
 const char* const kSigLabels[4] = {"Sigmoid centers", "Sigmoid widths", "Sigmoid weights", "Sigmoid starting indices"};
 
 // Map archive: tag, options, kind (0 component, 1 triangular map; +2 for
@@ -211,6 +615,10 @@ const char* const kSigLabels[4] = {"Sigmoid centers", "Sigmoid widths", "Sigmoid
 // (and, for sigmoid expansions, the Sigmoid1d arrays and edge/sum options),
 // then the coefficient archive.
 std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m) {
+    {
+        std::map<const ConditionalMapBase*, std::shared_ptr<RefNode>> memo;
+        if (auto root = describe(m, memo)) return writeRefArchive(root);
+    }
     auto* mono = dynamic_cast<MonotoneMapBase*>(m.get());
     if (!mono) throw std::invalid_argument("only monotone components, sigmoid expansions and triangular maps can be archived");
     std::vector<const MonotoneMapBase*> comps;
@@ -245,6 +653,10 @@ std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m
 }
 
 std::shared_ptr<ConditionalMapBase> mapFromBytes(const unsigned char* buf, size_t size) {
+    if (isRefArchive(buf, size)) {
+        std::map<const RefNode*, std::shared_ptr<ConditionalMapBase>> memo;
+        return build(readRefArchive(buf, size), memo);
+    }
     Reader r(buf, size);
     if (r.str() != kMapTag) throw std::invalid_argument("not a map archive written by this library");
     MapOptions o = readOptions(r);
@@ -329,6 +741,14 @@ int mpgb_map_to_bytes(mpgb_map* map, int layout, unsigned char* buf, size_t cap,
         } else {
             throw std::invalid_argument("unknown archive layout");
         }
+    });
+}
+
+int mpgb_map_archive_rewrite(const unsigned char* in, size_t in_size, unsigned char* buf, size_t cap, size_t* size) {
+    return serialGuard([&] {
+        if (!in) throw std::invalid_argument("null argument");
+        if (!isRefArchive(in, in_size)) throw std::invalid_argument("not a map archive in the reference's layout");
+        emit(writeRefArchive(readRefArchive(in, in_size)), buf, cap, size);
     });
 }
 

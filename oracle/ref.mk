@@ -1,8 +1,9 @@
 # ORACLE -- test infrastructure only.
 #
 # Builds oracle/_ref/libmpart_ref.so from the reference's own sources, where
-# they lie (REF, read-only), compiled unchanged against the serial Kokkos and
-# minimal Eigen stand-ins in oracle/ref_shim/, plus oracle/ref_driver.cpp
+# they lie (REF, read-only), compiled unchanged against the serial Kokkos,
+# minimal Eigen and save-side cereal stand-ins in oracle/ref_shim/ (with the
+# reference's archive support on, MPART_HAS_CEREAL), plus oracle/ref_driver.cpp
 # (C entry points).  Outputs go to oracle/_ref/ only.  The reference's own
 # build system is not used: these are the few sources of the monotone-
 # component path (map base classes, TriangularMap, the component factory
@@ -17,7 +18,7 @@ REF ?= /root/reference
 HERE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT := $(HERE)_ref
 CXX ?= g++
-CXXFLAGS := -O2 -std=c++17 -fPIC -ffp-contract=off -fno-fast-math -w -I$(HERE)ref_shim -I$(REF)
+CXXFLAGS := -O2 -std=c++17 -fPIC -ffp-contract=off -fno-fast-math -w -DMPART_HAS_CEREAL -I$(HERE)ref_shim -I$(REF)
 
 SRCS := src/ParameterizedFunctionBase.cpp src/ConditionalMapBase.cpp src/TriangularMap.cpp \
         src/MapFactoryImpl4.cpp src/MapFactoryImpl5.cpp src/MapFactoryImpl6.cpp \
@@ -26,7 +27,7 @@ SRCS := src/ParameterizedFunctionBase.cpp src/ConditionalMapBase.cpp src/Triangu
         src/MultiIndices/MultiIndexSet.cpp src/MultiIndices/MultiIndexLimiter.cpp \
         src/MultiIndices/MultiIndexNeighborhood.cpp src/Utilities/Miscellaneous.cpp
 OBJS := $(addprefix $(OUT)/obj/,$(notdir $(SRCS:.cpp=.o))) $(OUT)/obj/ref_driver.o
-SHIMS := $(HERE)ref_shim/Kokkos_Core.hpp $(HERE)ref_shim/Eigen/Core
+SHIMS := $(HERE)ref_shim/Kokkos_Core.hpp $(HERE)ref_shim/Eigen/Core $(HERE)ref_shim/cereal/cereal.hpp
 
 all: $(OUT)/libmpart_ref.so
 

@@ -5,7 +5,8 @@ ctypes front end of ``oracle/_ref/libmpart_ref.so``: MParT's own map classes
 ``src/TriangularMap.cpp``, the component factory registrations
 ``src/MapFactoryImpl{4..9}.cpp`` and ``src/MultiIndices/*.cpp``, with the
 headers they include), compiled unchanged from the reference checkout by
-``oracle/ref.mk`` against the Kokkos / Eigen stand-ins in ``oracle/ref_shim/``.
+``oracle/ref.mk`` against the Kokkos / Eigen / cereal (save side) stand-ins in
+``oracle/ref_shim/``, with the reference's archive support on.
 
 It exists only where the reference checkout does (the development host):
 ``available()`` says whether it can be built.  The tests use it to pin the
@@ -66,6 +67,10 @@ def lib():
         L.ref_sigmoid.restype = C.c_void_p
         L.ref_sigmoid.argtypes = [C.c_uint, C.c_uint, _up, _up, _up, _dp, _dp, _dp, C.c_uint, C.c_int, C.c_int]
         L.ref_direct_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, _dp]
+        L.ref_to_bytes.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.ref_wrap_coeffs.argtypes = [C.c_void_p, _dp, C.c_long]
+        L.ref_triangular_from.restype = C.c_void_p
+        L.ref_triangular_from.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
         _lib = L
     return _lib
 
@@ -112,6 +117,37 @@ class RefMap:
     def _check(self, rc):
         if rc != 0:
             raise RuntimeError(lib().ref_last_error().decode())
+
+    @classmethod
+    def triangular_from(cls, comps):
+        """TriangularMap(components, moveCoeffs=true) over RefMap components
+        (each with coefficients set); they must outlive the result."""
+        L = lib()
+        arr = (C.c_void_p * len(comps))(*[c._h for c in comps])
+        self = cls.__new__(cls)
+        self._comps = list(comps)
+        self._h = L.ref_triangular_from(arr, len(comps))
+        if not self._h:
+            raise RuntimeError(L.ref_last_error().decode())
+        a, b_, c = C.c_uint(), C.c_uint(), C.c_uint()
+        L.ref_sizes(self._h, C.byref(a), C.byref(b_), C.byref(c))
+        self.input_dim, self.output_dim, self.num_coeffs = a.value, b_.value, c.value
+        return self
+
+    def to_bytes(self) -> bytes:
+        """The reference's ToBytes / pickle archive of this map
+        (ParameterizedFunctionBase::Save through the cereal stand-in)."""
+        n = C.c_size_t()
+        self._check(lib().ref_to_bytes(self._h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._check(lib().ref_to_bytes(self._h, buf, n.value, C.byref(n)))
+        return buf.raw[:n.value]
+
+    def wrap_coeffs(self, coeffs):
+        """WrapCoeffs on this array's memory (kept alive by the map object)."""
+        self._wrapped = _c(coeffs).copy()
+        assert self._wrapped.size == self.num_coeffs
+        self._check(lib().ref_wrap_coeffs(self._h, self._wrapped.ctypes.data_as(_dp), self._wrapped.size))
 
     def set_coeffs(self, coeffs):
         c = _c(coeffs)

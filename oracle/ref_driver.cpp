@@ -16,9 +16,11 @@
 // Matrices are row-major rows x N arrays (coordinate d of point i at
 // d * N + i), the layout the reference's Python binding passes.
 #include <cstdio>
+#include <cstring>
 #include <exception>
 #include <map>
 #include <memory>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -240,6 +242,43 @@ void* ref_sigmoid(unsigned dim, unsigned numTerms, const unsigned* starts, const
 }
 
 void ref_free(void* h) { delete (RefMap*)h; }
+
+// ParameterizedFunctionBase::Save (ParameterizedFunctionBase.h:197-202), the
+// archive of the reference's ToBytes / pickle
+// (bindings/python/src/ParameterizedFunctionBase.cpp:57-61), through the
+// cereal stand-in.  *size receives the archive's size; the bytes are written
+// when cap holds at least that many.
+int ref_to_bytes(void* h, unsigned char* buf, size_t cap, size_t* size) {
+    return guard([&] {
+        std::stringstream ss;
+        ((RefMap*)h)->map->Save(ss);
+        const std::string b = ss.str();
+        *size = b.size();
+        if (buf && cap >= b.size()) std::memcpy(buf, b.data(), b.size());
+    });
+}
+
+// ParameterizedFunctionBase::WrapCoeffs on caller memory, as the Python
+// binding's WrapCoeffs does (an unmanaged view of the array, ToKokkos:
+// bindings/python/src/ParameterizedFunctionBase.cpp:25-27).  The memory must
+// outlive the map.
+int ref_wrap_coeffs(void* h, double* c, long n) {
+    return guard([&] { ((RefMap*)h)->map->WrapCoeffs(Kokkos::View<double*, Host>(c, (size_t)n)); });
+}
+
+// TriangularMap(components, moveCoeffs = true) over the components of maps
+// made here (src/TriangularMap.cpp:10-58): the components' coefficients are
+// copied into one new view.  The component handles stay owned by their maps.
+void* ref_triangular_from(void* const* comps, unsigned n) {
+    RefMap* out = nullptr;
+    guard([&] {
+        auto* r = new RefMap;
+        for (unsigned i = 0; i < n; ++i) r->comps.push_back(((RefMap*)comps[i])->map);
+        r->map = std::make_shared<TriangularMap<Host>>(r->comps, true);
+        out = r;
+    });
+    return out;
+}
 
 // The map's own ConditionalMapBase::InverseImpl (default options): for the
 // sigmoid expansions, whose solver is theirs (RectifiedMultivariateExpansion

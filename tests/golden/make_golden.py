@@ -22,9 +22,20 @@ point counts:
   c3  6-D triangular map, total order 5, HermiteFunctions + Exp, tol 1e-7, banana samples
   c5  16-D triangular map, total order 3, tol 1e-8, inverse to xtol 1e-10
   sig 3-D sigmoid triangular map, total order 2, three sigmoid terms (SoftPlus)
+
+archive holds the reference's ToBytes / pickle archives
+(ParameterizedFunctionBase::Save, with the cereal stand-in of
+oracle/ref_shim/cereal) of maps built by its factory, by TriangularMap with
+moveCoeffs and by WrapCoeffs, each after a sequence of operations (which set
+the components' quadrature dimension that the archive records), with the
+reference's evaluation of each map.  The case table (ARCHIVE_CASES) is stored
+in the fixture as JSON.
+
+    python tests/golden/make_golden.py [name ...]   # only the named fixtures
 """
 import os
 import sys
+import zlib
 
 import numpy as np
 
@@ -175,8 +186,115 @@ def make_sig(n=200):
                 inverse_cold=tm.inverse(coef, np.zeros((0, n)), r))
 
 
+# build: "triangular" (MapFactory::CreateTriangular, then SetCoeffs),
+# "component" (CreateComponent on the total-order set, then SetCoeffs),
+# "moved" (TriangularMap(components, moveCoeffs=true) of CreateComponent
+# components with coefficients), "wrapped" (CreateTriangular, then WrapCoeffs
+# on caller memory).  ops run in order on x (and sens) after an Evaluate.
+# The reference's fixed ClenshawCurtis rule keeps a one-double internal
+# workspace, so its operations that integrate more than one function
+# (CoeffGrad, Gradient, the discrete-derivative log-determinant) fail its
+# assertion fdim <= maxDim (Quadrature.h:174-183); its cases run Evaluate and
+# Inverse only.
+ARCHIVE_CASES = [
+    dict(name="tri_ph_softplus_acc", build="triangular", in_dim=3, out_dim=2, order=3,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="AdaptiveClenshawCurtis"), ops=[]),
+    dict(name="tri_hf_exp_acc_coeffgrad", build="triangular", in_dim=4, out_dim=2, order=2,
+         opts=dict(basis="HermiteFunctions", posfunc="Exp", quad="AdaptiveClenshawCurtis", abs_tol=1e-7,
+                   rel_tol=1e-7, max_sub=20, quad_pts=9), ops=["coeff_grad"]),
+    dict(name="tri_ph_exp_cc_unnormalised", build="triangular", in_dim=2, out_dim=2, order=4,
+         opts=dict(basis="ProbabilistHermite", posfunc="Exp", quad="ClenshawCurtis", quad_pts=6, normalize=False),
+         ops=["evaluate", "inverse"]),
+    dict(name="tri_ph_softplus_as_discrete_logdet", build="triangular", in_dim=3, out_dim=3, order=2,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="AdaptiveSimpson", cont_deriv=False,
+                   nugget=0.05, min_sub=1, max_sub=12), ops=["logdet"]),
+    dict(name="tri_hf_softplus_acc_gradient", build="triangular", in_dim=3, out_dim=2, order=3,
+         opts=dict(basis="HermiteFunctions", posfunc="SoftPlus", quad="AdaptiveClenshawCurtis"), ops=["gradient"]),
+    dict(name="tri_ph_softplus_acc_discrete_ldcg", build="triangular", in_dim=2, out_dim=1, order=3,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="AdaptiveClenshawCurtis", cont_deriv=False),
+         ops=["logdet_coeff_grad"]),
+    dict(name="tri_ph_softplus_acc_inverse", build="triangular", in_dim=3, out_dim=2, order=2,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="AdaptiveClenshawCurtis"),
+         ops=["coeff_grad", "inverse"]),
+    dict(name="comp_ph_softplus_acc", build="component", in_dim=4, out_dim=1, order=3,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="AdaptiveClenshawCurtis", nugget=0.01),
+         ops=["coeff_grad"]),
+    dict(name="moved_hf_exp_as", build="moved", in_dim=3, out_dim=2, order=2,
+         opts=dict(basis="HermiteFunctions", posfunc="Exp", quad="AdaptiveSimpson"), ops=[]),
+    dict(name="wrapped_ph_softplus_cc", build="wrapped", in_dim=2, out_dim=2, order=2,
+         opts=dict(basis="ProbabilistHermite", posfunc="SoftPlus", quad="ClenshawCurtis", quad_pts=5), ops=[]),
+]
+
+
+def _ref_archive_map(case, coef):
+    """The reference map of an ARCHIVE_CASES entry, its coefficients set
+    (the components, kept alive, for the moved case)."""
+    o = case["opts"]
+    if case["build"] == "component":
+        s, d, r = O.total_order(case["in_dim"], case["order"])
+        m = R.RefMap(case["in_dim"], starts=s, dims=d, orders=r, **o)
+        m.set_coeffs(coef)
+        return m
+    if case["build"] == "moved":
+        extra = case["in_dim"] - case["out_dim"]
+        comps, off = [], 0
+        for i in range(case["out_dim"]):
+            s, d, r = O.total_order(extra + i + 1, case["order"])
+            c = R.RefMap(extra + i + 1, starts=s, dims=d, orders=r, **o)
+            c.set_coeffs(coef[off:off + c.num_coeffs])
+            off += c.num_coeffs
+            comps.append(c)
+        return R.RefMap.triangular_from(comps)
+    m = R.RefMap(case["in_dim"], case["out_dim"], case["order"], **o)
+    if case["build"] == "wrapped":
+        m.wrap_coeffs(coef)
+    else:
+        m.set_coeffs(coef)
+    return m
+
+
+def make_archive(n=40):
+    import json
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal((4, n))
+    sens = rng.standard_normal((4, n))
+    out = dict(x=x, sens=sens, cases=np.array(json.dumps(ARCHIVE_CASES)))
+    for case in ARCHIVE_CASES:
+        name, ind, outd = case["name"], case["in_dim"], case["out_dim"]
+        dims = [ind] if case["build"] == "component" else [ind - outd + i + 1 for i in range(outd)]
+        ncoef = sum(len(O.total_order(d, case["order"])[0]) - 1 for d in dims)
+        coef = np.random.default_rng(zlib.crc32(name.encode())).normal(0.0, 0.1, ncoef)
+        m = _ref_archive_map(case, coef)
+        xi = x[:ind]
+        ev = m.evaluate(xi)
+        for op in case["ops"]:
+            if op == "evaluate":
+                m.evaluate(xi)
+            elif op == "coeff_grad":
+                m.coeff_grad(xi, sens[:outd])
+            elif op == "gradient":
+                m.gradient(xi, sens[:outd])
+            elif op == "logdet":
+                m.logdet(xi)
+            elif op == "logdet_coeff_grad":
+                m.logdet_coeff_grad(xi)
+            elif op == "inverse":
+                m.inverse(xi[:ind - outd], ev)
+            else:
+                raise ValueError(op)
+        out[f"{name}__coef"] = coef
+        out[f"{name}__eval"] = ev
+        out[f"{name}__bytes"] = np.frombuffer(m.to_bytes(), np.uint8).copy()
+    return out
+
+
 if __name__ == "__main__":
     O.build()
-    for name, fn in (("c1", make_c1), ("c2", make_c2), ("c3", make_c3), ("c5", make_c5), ("sig", make_sig)):
+    makers = (("c1", make_c1), ("c2", make_c2), ("c3", make_c3), ("c5", make_c5), ("sig", make_sig),
+              ("archive", make_archive))
+    only = set(sys.argv[1:])
+    for name, fn in makers:
+        if only and name not in only:
+            continue
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **fn())
         print("wrote", name)
