@@ -431,13 +431,17 @@ public:
         if (!(oid & kNewId)) {
             auto it = objects_.find(oid);
             if (it == objects_.end()) throw std::invalid_argument("map archive: unknown object id");
+            for (const RefNode* o : open_)
+                if (o == it->second.get()) throw std::invalid_argument("map archive: a map contains itself");
             return it->second;
         }
         auto n = std::make_shared<RefNode>();
         objects_[oid & ~kNewId] = n;
         if (name == triangularName(0) || name == triangularName(1)) {
             n->triangular = true;
+            open_.push_back(n.get());
             triangular(*n);
+            open_.pop_back();
             return n;
         }
         for (int sp = 0; sp < 2; ++sp)
@@ -535,6 +539,7 @@ private:
     Reader& r_;
     std::map<uint32_t, std::string> types_;
     std::map<uint32_t, std::shared_ptr<RefNode>> objects_;
+    std::vector<const RefNode*> open_;  // triangular maps being read
 };
 
 // The archive's description of a map of this library, or null when it holds

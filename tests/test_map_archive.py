@@ -259,6 +259,12 @@ def test_archive_reader_rejects_what_it_cannot_load(M, fixture):
     # an archive in this library's own layout (sigmoid maps) is not the reference's
     with pytest.raises(ValueError):
         M.RewriteMapArchive(struct.pack("<Q", 3) + b"abc")
+    # a triangular map listed as its own component
+    name = b"mpart::TriangularMap<Kokkos::HostSpace>"
+    loop = struct.pack("<I", 0x80000001) + struct.pack("<Q", len(name)) + name + struct.pack("<I", 0x80000001)
+    loop += struct.pack("<Q", 1) + struct.pack("<II", 1, 1) + struct.pack("<B", 0)
+    with pytest.raises(ValueError, match="contains itself"):
+        M.RewriteMapArchive(loop)
 
 
 # ---- GPU ---------------------------------------------------------------------
