@@ -444,7 +444,10 @@ int mpgb_map_from_bytes(const unsigned char* buf, size_t size, mpgb_map** out);
  * derived field; an archive this library loads comes back unchanged.  Two-call
  * convention as above. */
 int mpgb_map_archive_rewrite(const unsigned char* in, size_t in_size, unsigned char* buf, size_t cap, size_t* size);
-/* Reads an MPGB_ARCHIVE_COEFFS archive; coeffs (num_coeffs doubles, host) may be NULL to query sizes. */
+/* Reads an MPGB_ARCHIVE_COEFFS archive; coeffs (num_coeffs doubles, host) may be NULL to query sizes.
+ * The archive of a map without coefficients holds an empty view: coeffs is then not written.
+ * MPGB_ARCHIVE_COEFFS writes the map's coefficient view under its label (as the reference's
+ * Serialize writes obj.Coeffs()), empty when no coefficients are set. */
 int mpgb_coeff_archive_read(const unsigned char* buf, size_t size, unsigned int* input_dim, unsigned int* output_dim,
                             unsigned int* num_coeffs, double* coeffs);
 int mpgb_options_to_bytes(const mpgb_map_options* opts, unsigned char* buf, size_t cap, size_t* size);

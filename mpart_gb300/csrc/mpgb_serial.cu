@@ -150,8 +150,11 @@ void writeMset(Writer& w, const FixedMultiIndexSet& m) {
     w.view<unsigned int>("Maximum degrees", m.maxDegrees.data(), m.maxDegrees.size());
 }
 
-// The uncompressed form stores every dimension of every term (nzStarts[k] =
-// k dim); it is converted to the compressed one by dropping zero orders.
+// The uncompressed form stores every dimension of every term, term k at
+// [k dim, (k + 1) dim); the reference leaves the last of its numTerms + 1
+// starts unset (SetupTerms, src/MultiIndices/FixedMultiIndexSet.cpp:141-160),
+// so the terms are counted from the orders.  It is converted to the
+// compressed form by dropping zero orders.
 FixedMultiIndexSet readMset(Reader& r) {
     const uint32_t dim = r.pod<uint32_t>();
     const bool compressed = r.pod<uint8_t>() != 0;
@@ -160,12 +163,16 @@ FixedMultiIndexSet readMset(Reader& r) {
     auto orders = r.view<unsigned int>();
     r.view<unsigned int>();  // maxDegrees: recomputed
     if (starts.empty()) throw std::invalid_argument("multi-index archive: no term starts");
-    if (dims.size() != orders.size() || starts.back() != dims.size())
+    if (dims.size() != orders.size()) throw std::invalid_argument("multi-index archive: inconsistent sizes");
+    if (compressed) {
+        if (starts.back() != dims.size()) throw std::invalid_argument("multi-index archive: inconsistent sizes");
+        return FixedMultiIndexSet(dim, starts, dims, orders);
+    }
+    if (dim == 0 || orders.size() % dim != 0 || starts.size() != orders.size() / dim + 1)
         throw std::invalid_argument("multi-index archive: inconsistent sizes");
-    if (compressed) return FixedMultiIndexSet(dim, starts, dims, orders);
     std::vector<unsigned> s{0}, d, o;
     for (size_t t = 0; t + 1 < starts.size(); ++t) {
-        for (unsigned j = starts[t]; j < starts[t + 1]; ++j)
+        for (size_t j = t * dim; j < (t + 1) * dim; ++j)
             if (orders[j] != 0) {
                 d.push_back(dims[j]);
                 o.push_back(orders[j]);
@@ -175,12 +182,23 @@ FixedMultiIndexSet readMset(Reader& r) {
     return FixedMultiIndexSet(dim, s, d, o);
 }
 
-void writeCoeffs(Writer& w, const ConditionalMapBase& m) {
+// The reference's Serialize writes the map's own coefficient view
+// (obj.Coeffs()): its label, and no elements when no coefficients are set.
+// The sigmoid-map archive of this library (own = true) always carries
+// numCoeffs values (zeros when unset) under the default label.
+void writeCoeffs(Writer& w, const ConditionalMapBase& m, bool own = false) {
     w.pod<uint32_t>(m.inputDim);
     w.pod<uint32_t>(m.outputDim);
     w.pod<uint32_t>(m.numCoeffs);
-    const std::vector<double> c = m.CheckCoefficients() ? m.CoeffMap() : std::vector<double>(m.numCoeffs, 0.0);
-    w.view<double>(kCoeffLabel, c.data(), c.size());
+    if (m.CheckCoefficients()) {
+        const std::vector<double> c = m.CoeffMap();
+        w.view<double>(own ? std::string(kCoeffLabel) : m.CoeffLabel(), c.data(), c.size());
+    } else if (own) {
+        const std::vector<double> z(m.numCoeffs, 0.0);
+        w.view<double>(kCoeffLabel, z.data(), z.size());
+    } else {
+        w.view<double>("", nullptr, 0);
+    }
 }
 
 struct CoeffArchive {
@@ -188,13 +206,16 @@ struct CoeffArchive {
     std::vector<double> c;
 };
 
-CoeffArchive readCoeffs(Reader& r) {
+// allowEmpty: the archive of a map without coefficients (DeserializeMap
+// returns its empty view, bindings/python/src/Serialization.cpp:22-30).
+CoeffArchive readCoeffs(Reader& r, bool allowEmpty = false) {
     CoeffArchive a;
     a.in = r.pod<uint32_t>();
     a.out = r.pod<uint32_t>();
     a.n = r.pod<uint32_t>();
     a.c = r.view<double>();
-    if (a.c.size() != a.n) throw std::invalid_argument("coefficient archive: size does not match numCoeffs");
+    if (a.c.size() != a.n && !(allowEmpty && a.c.empty()))
+        throw std::invalid_argument("coefficient archive: size does not match numCoeffs");
     return a;
 }
 
@@ -653,7 +674,7 @@ std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m
             writeMset(w, static_cast<const MonotoneComponent*>(c)->GetMultiIndexSet());
         }
     }
-    writeCoeffs(w, *m);
+    writeCoeffs(w, *m, true);
     return w.b;
 }
 
@@ -769,11 +790,11 @@ int mpgb_coeff_archive_read(const unsigned char* buf, size_t size, unsigned int*
     return serialGuard([&] {
         if (!buf) throw std::invalid_argument("null archive");
         Reader r(buf, size);
-        const CoeffArchive a = readCoeffs(r);
+        const CoeffArchive a = readCoeffs(r, true);
         if (input_dim) *input_dim = a.in;
         if (output_dim) *output_dim = a.out;
         if (num_coeffs) *num_coeffs = a.n;
-        if (coeffs && a.n) std::memcpy(coeffs, a.c.data(), a.n * sizeof(double));
+        if (coeffs && !a.c.empty()) std::memcpy(coeffs, a.c.data(), a.n * sizeof(double));
     });
 }
 

@@ -69,10 +69,51 @@ def lib():
         L.ref_direct_inverse.argtypes = [C.c_void_p, _dp, C.c_long, _dp, C.c_long, _dp]
         L.ref_to_bytes.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]
         L.ref_wrap_coeffs.argtypes = [C.c_void_p, _dp, C.c_long]
+        out = [C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.ref_options_bytes.argtypes = opt + out
+        L.ref_mset_bytes.argtypes = [C.c_uint, C.c_uint, _up, _up, _up] + out
+        L.ref_coeff_archive.argtypes = [C.c_void_p] + out
         L.ref_triangular_from.restype = C.c_void_p
         L.ref_triangular_from.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
         _lib = L
     return _lib
+
+
+def _bytes(call):
+    n = C.c_size_t()
+    if call(None, 0, C.byref(n)) != 0:
+        raise RuntimeError(lib().ref_last_error().decode())
+    buf = C.create_string_buffer(max(1, n.value))
+    if call(buf, n.value, C.byref(n)) != 0:
+        raise RuntimeError(lib().ref_last_error().decode())
+    return buf.raw[:n.value]
+
+
+def options_bytes(basis="ProbabilistHermite", normalize=True, posfunc="SoftPlus", quad="AdaptiveClenshawCurtis",
+                  abs_tol=1e-6, rel_tol=1e-6, max_sub=30, min_sub=0, quad_pts=5, nugget=0.0, cont_deriv=True):
+    """MapOptions.Serialize's archive (MapOptions::serialize)."""
+    b = {"ProbabilistHermite": BASIS_PROB_HERMITE, "HermiteFunctions": BASIS_HERMITE_FUNCTIONS}[basis]
+    p = {"Exp": POS_EXP, "SoftPlus": POS_SOFTPLUS}[posfunc]
+    q = {"AdaptiveSimpson": QUAD_ADAPTIVE_SIMPSON, "ClenshawCurtis": QUAD_CLENSHAW_CURTIS,
+         "AdaptiveClenshawCurtis": QUAD_ACC}[quad]
+    return _bytes(lambda buf, cap, n: lib().ref_options_bytes(b, int(normalize), p, q, abs_tol, rel_tol, max_sub,
+                                                              min_sub, quad_pts, nugget, int(cont_deriv), buf,
+                                                              cap, n))
+
+
+def mset_bytes(dim, starts=None, dims=None, orders=None, dense=None):
+    """FixedMultiIndexSet.Serialize's archive of the compressed set (starts,
+    dims, orders) or of the uncompressed one (dense: terms x dim orders)."""
+    if dense is not None:
+        d = np.ascontiguousarray(dense, np.uint32)
+        return _bytes(lambda buf, cap, n: lib().ref_mset_bytes(dim, d.shape[0], None, None, d.ctypes.data_as(_up),
+                                                               buf, cap, n))
+    s = np.ascontiguousarray(starts, np.uint32)
+    dd = np.ascontiguousarray(dims if len(dims) else [0], np.uint32)
+    o = np.ascontiguousarray(orders if len(orders) else [0], np.uint32)
+    return _bytes(lambda buf, cap, n: lib().ref_mset_bytes(dim, len(s) - 1, s.ctypes.data_as(_up),
+                                                           dd.ctypes.data_as(_up), o.ctypes.data_as(_up), buf,
+                                                           cap, n))
 
 
 def _c(a):
@@ -133,6 +174,11 @@ class RefMap:
         L.ref_sizes(self._h, C.byref(a), C.byref(b_), C.byref(c))
         self.input_dim, self.output_dim, self.num_coeffs = a.value, b_.value, c.value
         return self
+
+    def coeff_archive(self) -> bytes:
+        """ParameterizedFunctionBase.Serialize's archive: inputDim, outputDim,
+        numCoeffs and the coefficient view."""
+        return _bytes(lambda buf, cap, n: lib().ref_coeff_archive(self._h, buf, cap, n))
 
     def to_bytes(self) -> bytes:
         """The reference's ToBytes / pickle archive of this map

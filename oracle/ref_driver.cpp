@@ -152,6 +152,22 @@ std::shared_ptr<Map> sigmoidExpansion(unsigned dim, FixedMultiIndexSet<Host> con
 }
 
 
+// Runs write on a cereal binary archive in memory; *size receives the archive
+// size and buf (cap bytes) the bytes when large enough.
+template <class F>
+int archiveTo(unsigned char* buf, size_t cap, size_t* size, F&& write) {
+    return guard([&] {
+        std::stringstream ss;
+        {
+            cereal::BinaryOutputArchive ar(ss);
+            write(ar);
+        }
+        const std::string b = ss.str();
+        *size = b.size();
+        if (buf && cap >= b.size()) std::memcpy(buf, b.data(), b.size());
+    });
+}
+
 extern "C" {
 
 const char* ref_last_error() { return g_err.c_str(); }
@@ -255,6 +271,50 @@ int ref_to_bytes(void* h, unsigned char* buf, size_t cap, size_t* size) {
         const std::string b = ss.str();
         *size = b.size();
         if (buf && cap >= b.size()) std::memcpy(buf, b.data(), b.size());
+    });
+}
+
+// The Python binding's Serialize methods write these archives to a file;
+// here the same archive calls go to memory: MapOptions
+// (bindings/python/src/MapOptions.cpp:74-78), FixedMultiIndexSet
+// (bindings/python/src/MultiIndex.cpp:243-248; compressed from nz arrays, or
+// uncompressed from every term's dim orders when dims is null) and the
+// coefficient archive (bindings/python/src/ParameterizedFunctionBase.cpp:51-56).
+int ref_options_bytes(int basis, int basisNorm, int pos, int quad, double absTol, double relTol, unsigned maxSub,
+                      unsigned minSub, unsigned quadPts, double nugget, int contDeriv, unsigned char* buf, size_t cap,
+                      size_t* size) {
+    return archiveTo(buf, cap, size, [&](cereal::BinaryOutputArchive& ar) {
+        const MapOptions o = options(basis, basisNorm, pos, quad, absTol, relTol, maxSub, minSub, quadPts, nugget,
+                                     contDeriv);
+        ar(o);
+    });
+}
+
+int ref_mset_bytes(unsigned dim, unsigned numTerms, const unsigned* starts, const unsigned* dims,
+                   const unsigned* orders, unsigned char* buf, size_t cap, size_t* size) {
+    return archiveTo(buf, cap, size, [&](cereal::BinaryOutputArchive& ar) {
+        if (dims) {
+            const unsigned nnz = starts[numTerms];
+            Kokkos::View<unsigned*, Host> s("nzStarts", numTerms + 1), d("nzDims", nnz), r("nzOrders", nnz);
+            for (unsigned i = 0; i <= numTerms; ++i) s(i) = starts[i];
+            for (unsigned i = 0; i < nnz; ++i) {
+                d(i) = dims[i];
+                r(i) = orders[i];
+            }
+            ar(FixedMultiIndexSet<Host>(dim, s, d, r));
+        } else {
+            Kokkos::View<unsigned*, Host> r("orders", (size_t)numTerms * dim);
+            for (size_t i = 0; i < (size_t)numTerms * dim; ++i) r(i) = orders[i];
+            ar(FixedMultiIndexSet<Host>(dim, r));
+        }
+    });
+}
+
+int ref_coeff_archive(void* h, unsigned char* buf, size_t cap, size_t* size) {
+    return archiveTo(buf, cap, size, [&](cereal::BinaryOutputArchive& ar) {
+        const Map& obj = *((RefMap*)h)->map;
+        ar(obj.inputDim, obj.outputDim, obj.numCoeffs);
+        ar(obj.Coeffs());
     });
 }
 

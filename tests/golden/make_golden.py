@@ -28,7 +28,8 @@ archive holds the reference's ToBytes / pickle archives
 oracle/ref_shim/cereal) of maps built by its factory, by TriangularMap with
 moveCoeffs and by WrapCoeffs, each after a sequence of operations (which set
 the components' quadrature dimension that the archive records), with the
-reference's evaluation of each map.  The case table (ARCHIVE_CASES) is stored
+reference's evaluation of each map and its coefficient archive (the Python
+binding's Serialize).  The case table (ARCHIVE_CASES) is stored
 in the fixture as JSON.
 
     python tests/golden/make_golden.py [name ...]   # only the named fixtures
@@ -285,6 +286,7 @@ def make_archive(n=40):
         out[f"{name}__coef"] = coef
         out[f"{name}__eval"] = ev
         out[f"{name}__bytes"] = np.frombuffer(m.to_bytes(), np.uint8).copy()
+        out[f"{name}__serialize"] = np.frombuffer(m.coeff_archive(), np.uint8).copy()
     return out
 
 

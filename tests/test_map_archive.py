@@ -320,7 +320,7 @@ def _run_ops(m, case, x, sens, ev):
 
 
 @pytest.mark.gpu
-def test_maps_archive_to_the_reference_bytes(gpu, fixture):
+def test_maps_archive_to_the_reference_bytes(gpu, fixture, tmp_path):
     import torch
     M = gpu
     z, cases = fixture
@@ -334,6 +334,10 @@ def test_maps_archive_to_the_reference_bytes(gpu, fixture):
         np.testing.assert_allclose(out, ev, rtol=1e-10, atol=1e-12, err_msg=name)
         _run_ops(m, case, x, sens, ev)
         assert m.ToBytes() == z[name + "__bytes"].tobytes(), name
+        # the binding's Serialize: dimensions and the coefficient view, label included
+        path = tmp_path / (name + ".bin")
+        m.Serialize(path)
+        assert path.read_bytes() == z[name + "__serialize"].tobytes(), name
         del keep
 
 

@@ -2,9 +2,11 @@
 (ParameterizedFunctionBase.Serialize / DeserializeMap), MapOptions and
 FixedMultiIndexSet, byte for byte, and the whole-map archive behind
 ToBytes / FromBytes / pickle.  The expected bytes are assembled here from the
-layout itself: cereal's binary archive writes values back to back in native
+layout itself -- cereal's binary archive writes values back to back in native
 (little-endian) order, strings as a uint64 length and their bytes, and Kokkos
-views as (label, uint32 extent, elements) (MParT/Utilities/Serialization.h)."""
+views as (label, uint32 extent, elements) (MParT/Utilities/Serialization.h) --
+and, where the reference checkout is present, taken from the reference's own
+save functions (oracle/_ref with the cereal stand-in)."""
 import pickle
 import struct
 
@@ -77,8 +79,9 @@ def test_multi_index_set_archive_layout_and_round_trip(M, tmp_path):
 
 def test_multi_index_set_archive_uncompressed_form(M):
     # isCompressed = false stores every dimension of every term; zeros are dropped on load.
+    # The reference leaves the last term start unset (0).
     multis = [[0, 0], [1, 0], [0, 2], [1, 1]]
-    starts = [2 * k for k in range(len(multis) + 1)]
+    starts = [2 * k for k in range(len(multis))] + [0]
     dims = [d for _ in multis for d in (0, 1)]
     orders = [o for m in multis for o in m]
     data = (struct.pack("<IB", 2, 0) + _view("nzStarts", starts, "I") + _view("nzDims", dims, "I") +
@@ -86,6 +89,76 @@ def test_multi_index_set_archive_uncompressed_form(M):
     ms = M.FixedMultiIndexSet.FromBytes(data)
     assert [list(ms.IndexToMulti(i)) for i in range(ms.Size())] == multis
     np.testing.assert_array_equal(ms.nzStarts, [0, 0, 1, 2, 4])
+
+
+def _ref():
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("reference checkout not present")
+    return ref
+
+
+@pytest.mark.parametrize("basis,pos,quad", [("ProbabilistHermite", "SoftPlus", "AdaptiveClenshawCurtis"),
+                                            ("HermiteFunctions", "Exp", "AdaptiveSimpson"),
+                                            ("ProbabilistHermite", "Exp", "ClenshawCurtis")])
+@pytest.mark.parametrize("norm,cont", [(True, True), (False, False)])
+def test_map_options_archive_is_the_references(M, basis, pos, quad, norm, cont):
+    """Byte for byte against MapOptions::serialize run by the reference
+    (oracle/_ref with the cereal stand-in), and read back."""
+    ref = _ref()
+    kw = dict(abs_tol=3e-7, rel_tol=2e-6, max_sub=17, min_sub=2, quad_pts=9, nugget=0.125)
+    want = ref.options_bytes(basis=basis, normalize=norm, posfunc=pos, quad=quad, cont_deriv=cont, **kw)
+    q = {"AdaptiveClenshawCurtis": M.QuadTypes.AdaptiveClenshawCurtis, "ClenshawCurtis": M.QuadTypes.ClenshawCurtis,
+         "AdaptiveSimpson": M.QuadTypes.AdaptiveSimpson}[quad]
+    o = M.MapOptions(basisType=getattr(M.BasisTypes, basis), posFuncType=getattr(M.PosFuncTypes, pos), quadType=q,
+                     quadAbsTol=3e-7, quadRelTol=2e-6, quadMaxSub=17, quadMinSub=2, quadPts=9, contDeriv=cont,
+                     basisNorm=norm, nugget=0.125)
+    assert o.ToBytes() == want
+    assert M.MapOptions.FromBytes(want) == o
+
+
+def test_multi_index_set_archive_is_the_references(M, oracle):
+    """Byte for byte against FixedMultiIndexSet::save run by the reference, for
+    total-order sets and a set with unsorted nonzeros; the reference's
+    uncompressed form reads back as the same set."""
+    ref = _ref()
+    for dim, order in [(1, 0), (1, 4), (3, 2), (5, 3)]:
+        s, d, o = oracle.total_order(dim, order)
+        ms = M.FixedMultiIndexSet(dim, order)
+        assert ms.ToBytes() == ref.mset_bytes(dim, s, d, o), (dim, order)
+    # unsorted nonzeros in a term after the first: the reference's insertion
+    # sort (src/MultiIndices/FixedMultiIndexSet.cpp:74-93) steps its unsigned
+    # index below zero when the first term's nonzeros are unsorted
+    starts, dims, orders = [0, 1, 3, 4, 7], [1, 2, 0, 1, 3, 0, 1], [2, 1, 3, 2, 1, 2, 4]
+    ms = M.FixedMultiIndexSet(4, nzStarts=np.array(starts, np.uint32), nzDims=np.array(dims, np.uint32),
+                              nzOrders=np.array(orders, np.uint32))
+    assert ms.ToBytes() == ref.mset_bytes(4, starts, dims, orders)
+    multis = [[0, 0, 0], [1, 0, 2], [0, 3, 0], [2, 1, 1]]
+    back = M.FixedMultiIndexSet.FromBytes(ref.mset_bytes(3, dense=multis))
+    assert [list(back.IndexToMulti(i)) for i in range(back.Size())] == multis
+
+
+def test_coefficient_archive_is_the_references(M, tmp_path):
+    """DeserializeMap reads the reference's Serialize archive of a map with
+    coefficients, and of one without (an empty view)."""
+    ref = _ref()
+    m = ref.RefMap(3, 2, 2)
+    c = np.random.default_rng(4).normal(size=m.num_coeffs)
+    m.set_coeffs(c)
+    (tmp_path / "map.bin").write_bytes(m.coeff_archive())
+    i, o, coeffs = M.DeserializeMap(tmp_path / "map.bin")
+    assert (i, o) == (3, 2)
+    np.testing.assert_array_equal(coeffs, c)
+    comps = [ref.RefMap(d, starts=s, dims=dd, orders=oo) for d, (s, dd, oo) in
+             ((1, ([0, 0, 1], [0], [1])), (2, ([0, 0, 1, 2], [0, 1], [1, 1])))]
+    for comp in comps:
+        comp.set_coeffs(np.ones(comp.num_coeffs))
+    moved = ref.RefMap.triangular_from(comps)
+    data = moved.coeff_archive()
+    assert b"coeffs" in data  # the moved view's label
+    (tmp_path / "moved.bin").write_bytes(data)
+    i, o, coeffs = M.DeserializeMap(tmp_path / "moved.bin")
+    assert (i, o) == (2, 2) and np.all(coeffs == 1.0)
 
 
 def test_deserialize_map_reads_the_coefficient_archive(M, tmp_path):
