@@ -17,13 +17,16 @@ import numpy as np
 
 from . import _capi
 from ._capi import IntegrandError, MpgbError, check, load, mpgb_map_options, mpgb_matrix
+from .multiindex import (And, Anisotropic, Dimension, MaxDegree, MultiIndex, MultiIndexSet, NoneLim,  # noqa: F401
+                         NonzeroDiag, Or, Separable, TotalOrder, Xor)
 
 __all__ = [
     "BasisTypes", "PosFuncTypes", "QuadTypes", "MapOptions", "FixedMultiIndexSet", "ConditionalMapBase",
     "TriangularMap", "CreateComponent", "CreateTriangular", "IntegrandError", "MpgbError", "load", "DeserializeMap",
     "FromBytes", "MapBatch", "TrainMap", "TrainOptions", "KLObjective", "CreateGaussianKLObjective", "MultiIndexSet",
     "ATMOptions", "TrainMapAdaptive", "SigmoidTypes", "EdgeTypes", "SigmoidSumSizeType", "SigmoidComponent",
-    "CreateSigmoidComponent", "CreateSigmoidTriangular", "Sigmoid1d",
+    "CreateSigmoidComponent", "CreateSigmoidTriangular", "Sigmoid1d", "MultiIndex", "TotalOrder", "Dimension",
+    "Anisotropic", "MaxDegree", "NoneLim", "Separable", "NonzeroDiag", "And", "Or", "Xor", "RewriteMapArchive",
 ]
 
 
@@ -188,6 +191,35 @@ class FixedMultiIndexSet:
         for j in range(self.nzStarts[i], self.nzStarts[i + 1]):
             m[self.nzDims[j]] = self.nzOrders[j]
         return m
+
+    def __len__(self):
+        return self.dim
+
+    def MaxDegrees(self):
+        """Largest order of each input over the terms (FixedMultiIndexSet::MaxDegrees)."""
+        out = np.zeros(self.dim, dtype=np.uint32)
+        if self.nzDims.size:
+            np.maximum.at(out, self.nzDims, self.nzOrders)
+        return out
+
+    def MultiToIndex(self, multi):
+        """Index of the term equal to multi, or -1 (FixedMultiIndexSet::MultiToIndex)."""
+        want = np.asarray(list(multi), dtype=np.int64)
+        if want.size != self.dim:
+            return -1
+        for i in range(self.Size()):
+            if np.array_equal(self.IndexToMulti(i), want):
+                return i
+        return -1
+
+    def NonzeroDiagonalEntries(self):
+        """Terms with a nonzero last entry (FixedMultiIndexSet::NonzeroDiagonalEntries)."""
+        return [i for i in range(self.Size())
+                if any(self.nzDims[j] == self.dim - 1 for j in range(self.nzStarts[i], self.nzStarts[i + 1]))]
+
+    def ToDevice(self):
+        """The set serves host and device alike: itself."""
+        return self
 
     def ToBytes(self) -> bytes:
         """The reference's cereal archive of the set (MParT/MultiIndices/FixedMultiIndexSet.h:115-123)."""
@@ -965,94 +997,6 @@ def fp64_probe(blocks=152 * 8, threads=256, iters=4096):
     return flops / (ms.value * 1e-3) / 1e12, ms.value
 
 
-class MultiIndexSet:
-    """Adaptive multi-index set (MParT/MultiIndices/MultiIndexSet.h): the
-    active terms in activation order, and what TrainMapAdaptive needs
-    (total-order creation, adding terms, the reduced margin, Expand, Fix).
-    ReducedMargin and Expand rebuild the reference's bookkeeping of the set
-    (its entries numbered in order of appearance, mpgb_reduced_margin) by
-    activating the terms in order, so they meet the candidates in the
-    reference's order."""
-
-    def __init__(self, length: int, multis=()):
-        self.length = int(length)
-        self._terms = []
-        self._index = {}
-        for m in multis:
-            self._add(m)
-
-    @staticmethod
-    def CreateTotalOrder(length: int, maxOrder: int):
-        ms = FixedMultiIndexSet(length, maxOrder)
-        return MultiIndexSet(length, [tuple(int(v) for v in ms.IndexToMulti(i)) for i in range(ms.Size())])
-
-    def _add(self, m):
-        m = tuple(int(v) for v in m)
-        if len(m) != self.length:
-            raise ValueError("multi-index of the wrong length")
-        if m not in self._index:
-            self._index[m] = len(self._terms)
-            self._terms.append(m)
-
-    def __iadd__(self, m):
-        self._add(m)
-        return self
-
-    def Size(self):
-        return len(self._terms)
-
-    def Length(self):
-        return self.length
-
-    def __len__(self):
-        return self.length
-
-    def __getitem__(self, i):
-        return np.array(self._terms[i], dtype=np.uint32)
-
-    def Multis(self):
-        return [np.array(t, dtype=np.uint32) for t in self._terms]
-
-    def _dense(self):
-        return np.ascontiguousarray(np.array(self._terms, dtype=np.uint32).reshape(len(self._terms), self.length))
-
-    def ReducedMargin(self):
-        """Terms outside the set whose backward neighbours are all inside it,
-        in the reference's order (MultiIndexSet::ReducedMargin,
-        src/MultiIndices/MultiIndexSet.cpp:568-590)."""
-        U = C.POINTER(C.c_uint)
-        dense = self._dense()
-        n = C.c_uint()
-        check(load().mpgb_reduced_margin(self.length, self.Size(), dense.ctypes.data_as(U), C.byref(n), None, 0))
-        out = np.zeros((max(1, n.value), self.length), dtype=np.uint32)
-        check(load().mpgb_reduced_margin(self.length, self.Size(), dense.ctypes.data_as(U), None,
-                                         out.ctypes.data_as(U), n.value))
-        return [out[k].copy() for k in range(n.value)]
-
-    def Expand(self):
-        """MultiIndexSet::Expand (src/MultiIndices/MultiIndexSet.cpp:739-766):
-        activates the admissible forward neighbours of the frontier in the
-        reference's order and returns their indices, a term reached from
-        several frontier terms once for each (as the reference's does)."""
-        U = C.POINTER(C.c_uint)
-        dense = self._dense()
-        nt, ni = C.c_uint(), C.c_uint()
-        check(load().mpgb_multi_index_expand(self.length, self.Size(), dense.ctypes.data_as(U), C.byref(nt), None,
-                                             C.byref(ni), None, 0))
-        cap = max(1, nt.value, ni.value)
-        terms = np.zeros((cap, self.length), dtype=np.uint32)
-        idx = np.zeros(cap, dtype=np.uint32)
-        check(load().mpgb_multi_index_expand(self.length, self.Size(), dense.ctypes.data_as(U), None,
-                                             terms.ctypes.data_as(U), None, idx.ctypes.data_as(U), cap))
-        for k in range(nt.value):
-            self._add(terms[k])
-        return [int(v) for v in idx[:ni.value]]
-
-    def Fix(self, compress=True):
-        return FixedMultiIndexSet.from_multis(self._dense()) if self.Size() else \
-            FixedMultiIndexSet(self.length, nzStarts=[0])
-
-
 class ATMOptions(MapOptions, TrainOptions):
     """ATMOptions (MParT/TrainMapAdaptive.h:19-47): map options, training
     options and maxPatience, maxSize, maxDegrees (a multi-index of inputDim
@@ -1088,6 +1032,10 @@ def TrainMapAdaptive(mset0, objective: KLObjective, options: ATMOptions | None =
     in place by the selected sets, as in the reference."""
     from ._capi import mpgb_atm_options, mpgb_atm_result
     options = options or ATMOptions()
+    # The adaptive loop grows each set from its terms in order, without a limiter.
+    if any(not isinstance(m.GetLimiter(), NoneLim) for m in mset0):
+        raise ValueError("TrainMapAdaptive: limiters on the initial multi-index sets are not supported; bound the "
+                         "degrees with ATMOptions.maxDegrees")
     o = mpgb_atm_options()
     check(load().mpgb_atm_options_default(C.byref(o)))
     o.map = options._c()

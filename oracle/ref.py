@@ -73,6 +73,7 @@ def lib():
         L.ref_options_bytes.argtypes = opt + out
         L.ref_mset_bytes.argtypes = [C.c_uint, C.c_uint, _up, _up, _up] + out
         L.ref_coeff_archive.argtypes = [C.c_void_p] + out
+        L.ref_mset_report.argtypes = [C.c_uint, C.c_uint, _up, C.c_int, C.c_uint, C.c_int, _up, _dp] + out
         L.ref_triangular_from.restype = C.c_void_p
         L.ref_triangular_from.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
         _lib = L
@@ -297,6 +298,21 @@ def _mset_call(terms, mode):
     if rc != 0:
         raise RuntimeError(L.ref_last_error().decode())
     return out_t, nt.value, idx, no.value
+
+
+def mset_report(dim, terms=(), mode=0, order=0, lim_kind=0, u=(0, 0, 0), w=()):
+    """The text report of the reference's MultiIndexSet (ref_mset_report in
+    oracle/ref_driver.cpp): mode 0 += of terms under the limiter, 1
+    CreateTotalOrder(dim, order), 2 CreateTensorProduct(dim, order), 3 += of
+    terms then SetLimiter; limiter kinds as documented there."""
+    t = np.ascontiguousarray(np.asarray(terms, dtype=np.uint32).reshape(-1, dim) if len(terms) else
+                             np.zeros((1, dim), np.uint32))
+    uu = np.ascontiguousarray(list(u) + [0] * (3 - len(u)), np.uint32)
+    ww = np.ascontiguousarray(list(w) if len(w) else [0.0], np.float64)
+    n = len(terms)
+    return _bytes(lambda buf, cap, sz: lib().ref_mset_report(dim, n, t.ctypes.data_as(_up), mode, order, lim_kind,
+                                                             uu.ctypes.data_as(_up), ww.ctypes.data_as(_dp), buf,
+                                                             cap, sz)).decode()
 
 
 def mset_reduced_margin(terms):

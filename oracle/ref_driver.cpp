@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <exception>
+#include <functional>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -30,6 +31,7 @@
 #include "MParT/MapOptions.h"
 #include "MParT/MonotoneComponent.h"
 #include "MParT/MultiIndices/FixedMultiIndexSet.h"
+#include "MParT/MultiIndices/MultiIndexLimiter.h"
 #include "MParT/MultiIndices/MultiIndexSet.h"
 #include "MParT/MultivariateExpansionWorker.h"
 #include "MParT/OrthogonalPolynomial.h"
@@ -478,6 +480,117 @@ int ref_mset(unsigned dim, unsigned n, const unsigned* multis, int mode, unsigne
             }
             *nTerms = s.Size();
         }
+    });
+}
+
+// A report of MParT's MultiIndexSet for the set tests: mode 0 builds it by
+// += of the n terms (rows of length dim) under the limiter, mode 1 is
+// CreateTotalOrder(dim, order), mode 2 CreateTensorProduct(dim, order), mode 3
+// builds it by += without a limiter and then calls SetLimiter.  Limiter kinds:
+// 0 None, 1 TotalOrder(u0), 2 Dimension(u0, u1), 3 Anisotropic(w[0..dim),
+// w[dim]), 4 MaxDegree(u0, dim), 5 Separable, 6 NonzeroDiag,
+// 7 And(TotalOrder(u0), MaxDegree(u1, dim)), 8 Or(Dimension(u0, u1),
+// TotalOrder(u2)), 9 Xor(TotalOrder(u0), NonzeroDiag).  The report lists the
+// set's terms, MaxOrders, Frontier, StrictFrontier, Margin, ReducedMargin,
+// ReducedMarginDim for every dimension, IsExpandable / NumForward /
+// NumActiveForward of every term, NonzeroDiagonalEntries, IsAdmissible of the
+// margin, Expand() and Expand(i) for every term (on copies), and the union
+// with the total-order set of order 1.  Written as text into buf (two-call
+// convention, as ref_to_bytes).
+int ref_mset_report(unsigned dim, unsigned n, const unsigned* multis, int mode, unsigned order, int limKind,
+                    const unsigned* u, const double* w, char* buf, size_t cap, size_t* size) {
+    return guard([&] {
+        using mpart::MultiIndex;
+        using mpart::MultiIndexSet;
+        namespace L = mpart::MultiIndexLimiter;
+        std::function<bool(MultiIndex const&)> lim;
+        switch (limKind) {
+            case 0: lim = L::None(); break;
+            case 1: lim = L::TotalOrder(u[0]); break;
+            case 2: lim = L::Dimension(u[0], u[1]); break;
+            case 3: lim = L::Anisotropic(std::vector<double>(w, w + dim), w[dim]); break;
+            case 4: lim = L::MaxDegree(u[0], dim); break;
+            case 5: lim = L::Separable(); break;
+            case 6: lim = L::NonzeroDiag(); break;
+            case 7: lim = L::And(L::TotalOrder(u[0]), L::MaxDegree(u[1], dim)); break;
+            case 8: lim = L::Or(L::Dimension(u[0], u[1]), L::TotalOrder(u[2])); break;
+            case 9: lim = L::Xor(L::TotalOrder(u[0]), L::NonzeroDiag()); break;
+            default: throw std::invalid_argument("unknown limiter kind");
+        }
+        auto term = [&](unsigned t) {
+            return MultiIndex(std::vector<unsigned>(multis + (size_t)t * dim, multis + (size_t)(t + 1) * dim));
+        };
+        MultiIndexSet s(dim);
+        std::ostringstream os;
+        if (mode == 1) {
+            s = MultiIndexSet::CreateTotalOrder(dim, order, lim);
+        } else if (mode == 2) {
+            s = MultiIndexSet::CreateTensorProduct(dim, order, lim);
+        } else if (mode == 0) {
+            s = MultiIndexSet(dim, lim);
+            for (unsigned t = 0; t < n; ++t) s += term(t);
+        } else {
+            for (unsigned t = 0; t < n; ++t) s += term(t);
+            try {
+                s.SetLimiter(lim);
+            } catch (std::invalid_argument const&) {
+                os << "setlimiter rejected\n";
+            }
+        }
+        auto multisOut = [&](std::vector<MultiIndex> const& ms) {
+            std::string r;
+            for (size_t k = 0; k < ms.size(); ++k) r += (k ? ";" : "") + ms[k].String();
+            return r;
+        };
+        auto ints = [&](auto const& v) {
+            std::string r;
+            for (size_t k = 0; k < v.size(); ++k) r += (k ? "," : "") + std::to_string(v[k]);
+            return r;
+        };
+        auto termsOf = [&](MultiIndexSet const& x) {
+            std::vector<MultiIndex> t;
+            for (unsigned k = 0; k < x.Size(); ++k) t.push_back(x.IndexToMulti(k));
+            return multisOut(t);
+        };
+        os << "size " << s.Size() << "\n";
+        os << "terms " << termsOf(s) << "\n";
+        os << "maxorders " << ints(s.MaxOrders()) << "\n";
+        os << "frontier " << ints(s.Frontier()) << "\n";
+        os << "strict " << ints(s.StrictFrontier()) << "\n";
+        const auto margin = s.Margin();
+        os << "margin " << multisOut(margin) << "\n";
+        os << "rmargin " << multisOut(s.ReducedMargin()) << "\n";
+        for (unsigned d = 0; d < dim; ++d) os << "rmargin_dim" << d << " " << multisOut(s.ReducedMarginDim(d)) << "\n";
+        std::vector<unsigned> ex, nf, na;
+        for (unsigned k = 0; k < s.Size(); ++k) {
+            ex.push_back(s.IsExpandable(k));
+            nf.push_back(s.NumForward(k));
+            na.push_back(s.NumActiveForward(k));
+        }
+        os << "expandable " << ints(ex) << "\n";
+        os << "nforward " << ints(nf) << "\n";
+        os << "nactiveforward " << ints(na) << "\n";
+        os << "nzdiag " << ints(s.NonzeroDiagonalEntries()) << "\n";
+        std::vector<unsigned> adm;
+        for (auto const& m : margin) adm.push_back(s.IsAdmissible(m));
+        os << "margin_admissible " << ints(adm) << "\n";
+        {
+            MultiIndexSet c = s;
+            const auto ix = c.Expand();
+            os << "expand " << ints(ix) << " | " << termsOf(c) << "\n";
+        }
+        for (unsigned k = 0; k < s.Size(); ++k) {
+            MultiIndexSet c = s;
+            os << "expand" << k << " " << ints(c.Expand(k)) << "\n";
+        }
+        {
+            MultiIndexSet c = s;
+            const unsigned added = c.Union(MultiIndexSet::CreateTotalOrder(dim, 1));
+            os << "union " << added << " | " << termsOf(c) << "\n";
+        }
+        const std::string r = os.str();
+        *size = r.size();
+        if (buf && cap >= r.size()) std::memcpy(buf, r.data(), r.size());
     });
 }
 
