@@ -9,8 +9,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
+#include <initializer_list>
+#include <iosfwd>
 #include <limits>
+#include <map>
 #include <memory>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -87,8 +92,170 @@ private:
     void CalculateMaxDegrees();
 };
 
+// MParT/MultiIndices/MultiIndex.h: a multi-index (stored densely).
+class MultiIndex {
+public:
+    MultiIndex() = default;
+    explicit MultiIndex(unsigned int length, unsigned int val = 0) : v_(length, val) {}
+    MultiIndex(std::vector<unsigned int> const& v) : v_(v) {}
+    MultiIndex(std::initializer_list<unsigned int> v) : v_(v) {}
+    std::vector<unsigned int> const& Vector() const { return v_; }
+    unsigned int Length() const { return (unsigned int)v_.size(); }
+    unsigned int Sum() const;
+    unsigned int Max() const;
+    unsigned int NumNz() const;
+    bool HasNonzeroEnd() const { return !v_.empty() && v_.back() != 0; }
+    // Get(Length()) reads 0; larger indices throw std::out_of_range (MultiIndex::Get).
+    unsigned int Get(unsigned int i) const;
+    // Sets entry i; returns whether it was nonzero (MultiIndex::Set).
+    bool Set(unsigned int i, unsigned int val);
+    std::string String() const;  // entries separated by spaces
+    bool operator==(MultiIndex const& b) const { return v_ == b.v_; }
+    bool operator!=(MultiIndex const& b) const { return v_ != b.v_; }
+    // MultiIndex::operator<: length, total order, maximum, then entry by entry.
+    bool operator<(MultiIndex const& b) const;
+    bool operator>(MultiIndex const& b) const { return b < *this; }
+    bool operator<=(MultiIndex const& b) const { return !(*this > b); }
+    bool operator>=(MultiIndex const& b) const { return !(*this < b); }
+
+private:
+    std::vector<unsigned int> v_;
+};
+
+using LimiterType = std::function<bool(MultiIndex const&)>;
+
+// MParT/MultiIndices/MultiIndexLimiter.h.
+namespace MultiIndexLimiter {
+struct TotalOrder {
+    explicit TotalOrder(unsigned int totalOrder) : totalOrder(totalOrder) {}
+    bool operator()(MultiIndex const& m) const { return m.Sum() <= totalOrder; }
+    unsigned int totalOrder;
+};
+// Nonzero entries only in [lowerDim, lowerDim + length).
+struct Dimension {
+    Dimension(unsigned int lowerDim, unsigned int length) : lowerDim(lowerDim), length(length) {}
+    bool operator()(MultiIndex const& m) const;
+    unsigned int lowerDim, length;
+};
+// prod_i weights[i]^m[i] >= epsilon; weights in [0, 1], epsilon in (0, 1).
+struct Anisotropic {
+    Anisotropic(std::vector<double> const& weights, double epsilon);
+    bool operator()(MultiIndex const& m) const;
+    std::vector<double> weights;
+    double epsilon;
+};
+struct MaxDegree {
+    MaxDegree(unsigned int maxDegree, unsigned int length) : maxDegrees(length, maxDegree) {}
+    explicit MaxDegree(std::vector<unsigned int> const& maxDegrees) : maxDegrees(maxDegrees) {}
+    bool operator()(MultiIndex const& m) const;
+    std::vector<unsigned int> maxDegrees;
+};
+struct None {
+    bool operator()(MultiIndex const&) const { return true; }
+};
+// No cross terms with the last input.
+struct Separable {
+    bool operator()(MultiIndex const& m) const {
+        return !m.HasNonzeroEnd() || m.Sum() == m.Get(m.Length() - 1);
+    }
+};
+struct NonzeroDiag {
+    bool operator()(MultiIndex const& m) const { return m.HasNonzeroEnd(); }
+};
+struct And {
+    And(LimiterType a, LimiterType b) : a(std::move(a)), b(std::move(b)) {}
+    bool operator()(MultiIndex const& m) const { return a(m) && b(m); }
+    LimiterType a, b;
+};
+struct Or {
+    Or(LimiterType a, LimiterType b) : a(std::move(a)), b(std::move(b)) {}
+    bool operator()(MultiIndex const& m) const { return a(m) || b(m); }
+    LimiterType a, b;
+};
+struct Xor {
+    Xor(LimiterType a, LimiterType b) : a(std::move(a)), b(std::move(b)) {}
+    bool operator()(MultiIndex const& m) const { return a(m) != b(m); }
+    LimiterType a, b;
+};
+}  // namespace MultiIndexLimiter
+
+// MParT/MultiIndices/MultiIndexSet.h (src/MultiIndices/MultiIndexSet.cpp):
+// the active terms in activation order and the reference's bookkeeping that
+// orders every query -- each multi-index seen gets a global number in order
+// of first appearance, activating one adds the forward and backward
+// neighbours the limiter allows as inactive entries, and edges are ordered
+// sets of global numbers.
+class MultiIndexSet {
+public:
+    explicit MultiIndexSet(unsigned int length, LimiterType const& limiter = MultiIndexLimiter::None());
+    static MultiIndexSet CreateTotalOrder(unsigned int length, unsigned int maxOrder,
+                                          LimiterType const& limiter = MultiIndexLimiter::None());
+    static MultiIndexSet CreateTensorProduct(unsigned int length, unsigned int maxDegree,
+                                             LimiterType const& limiter = MultiIndexLimiter::None());
+    // The active terms, in order (the compressed form either way).
+    FixedMultiIndexSet Fix(bool compress = true) const;
+
+    void SetLimiter(LimiterType const& limiter);
+    LimiterType GetLimiter() const { return limiter_; }
+    // Whether a limiter was given (at construction or by SetLimiter).
+    bool HasLimiter() const { return hasLimiter_; }
+
+    unsigned int Length() const { return length_; }
+    unsigned int Size() const { return (unsigned int)a2g_.size(); }
+    std::vector<unsigned int> const& MaxOrders() const { return maxOrders_; }
+    MultiIndex IndexToMulti(unsigned int activeIndex) const { return all_.at(a2g_.at(activeIndex)); }
+    MultiIndex at(int activeIndex) const { return IndexToMulti((unsigned int)activeIndex); }
+    MultiIndex const& operator[](int activeIndex) const { return all_[a2g_[activeIndex]]; }
+    int MultiToIndex(MultiIndex const& m) const;  // active index, or -1
+    std::vector<unsigned int> NonzeroDiagonalEntries() const;
+
+    int AddActive(MultiIndex const& m);  // active index, or -1 when the limiter refuses it
+    MultiIndexSet& operator+=(MultiIndex const& m) {
+        AddActive(m);
+        return *this;
+    }
+    MultiIndexSet& operator+=(MultiIndexSet const& rhs) {
+        Union(rhs);
+        return *this;
+    }
+    unsigned int Union(MultiIndexSet const& rhs);  // number of terms that became active
+    void Activate(MultiIndex const& m);           // an admissible entry of the set
+
+    bool IsActive(MultiIndex const& m) const;
+    bool IsAdmissible(MultiIndex const& m) const;
+    bool IsExpandable(unsigned int activeIndex) const;
+    unsigned int NumActiveForward(unsigned int activeIndex) const;
+    unsigned int NumForward(unsigned int activeIndex) const;
+    std::vector<unsigned int> Frontier() const;
+    std::vector<unsigned int> StrictFrontier() const;
+    std::vector<MultiIndex> Margin() const;
+    std::vector<MultiIndex> ReducedMargin() const;
+    std::vector<MultiIndex> ReducedMarginDim(unsigned int dim) const;
+    std::vector<unsigned int> Expand(unsigned int activeIndex);
+    std::vector<unsigned int> Expand();
+
+private:
+    int addMulti(MultiIndex const& m);
+    int addInactive(MultiIndex const& m);
+    void addForward(int g, bool addInactive);
+    void addBackward(int g, bool addInactive);
+    void activate(int g);
+    bool active(int g) const { return g2a_[g] >= 0; }
+    bool admissible(int g) const;
+
+    unsigned int length_;
+    LimiterType limiter_;
+    bool hasLimiter_ = false;
+    std::vector<MultiIndex> all_;
+    std::map<std::vector<unsigned int>, int> global_;
+    std::vector<int> g2a_, a2g_;
+    std::vector<std::set<int>> in_, out_;
+    std::vector<unsigned int> maxOrders_;
+};
+
 struct ComponentProgram;
 struct MapWorkspace;
+class ConditionalMapBase;
 
 // MParT/ParameterizedFunctionBase.h
 class ParameterizedFunctionBase {
@@ -103,6 +270,11 @@ public:
     // Alias caller-owned device memory (src/ParameterizedFunctionBase.cpp:219-228).
     virtual void WrapCoeffs(double* deviceCoeffs, unsigned int n) { WrapCoeffsLabeled(deviceCoeffs, n, std::string()); }
     double* Coeffs() const { return coeffs_; }
+    // ParameterizedFunctionBase::Save / Load (MParT/ParameterizedFunctionBase.h:197-215):
+    // the whole map in the reference's archive (what its ToBytes / pickle
+    // write), for monotone components and triangular maps of them.
+    void Save(std::ostream& os) const;
+    static std::shared_ptr<ConditionalMapBase> Load(std::istream& is);
     // Label of the coefficient view the reference would hold after the same
     // calls, as its map archive records it: "ParameterizedFunctionBase<MemorySpace>
     // Coefficients" for storage SetCoeffs allocated, "coeffs" for a
@@ -399,5 +571,21 @@ private:
 // (TrainError at the result).
 double TrainMap(std::shared_ptr<ConditionalMapBase> const& map, KLObjective const& objective,
                 TrainOptions const& options, cudaStream_t stream = 0);
+
+// MParT/TrainMapAdaptive.h:19-47: map and training options, maxPatience,
+// maxSize and maxDegrees (a multi-index of inputDim entries, or empty).
+struct ATMOptions : public MapOptions, public TrainOptions {
+    unsigned int maxPatience = 10;
+    unsigned int maxSize = std::numeric_limits<int>::max();
+    MultiIndex maxDegrees;
+};
+
+// TrainMapAdaptive (src/TrainMapAdaptive.cpp:44-271): grows each output's
+// set one reduced-margin term at a time and returns the triangular map of
+// the best sets, which replace mset0.  The sets grow from their terms in
+// order without a limiter: sets that carry one are refused
+// (std::invalid_argument); maxDegrees bounds the degrees.
+std::shared_ptr<ConditionalMapBase> TrainMapAdaptive(std::vector<MultiIndexSet>& mset0, KLObjective const& objective,
+                                                     ATMOptions const& options, cudaStream_t stream = 0);
 
 }  // namespace mpgb

@@ -24,6 +24,9 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <istream>
+#include <iterator>
+#include <ostream>
 #include <limits>
 #include <map>
 #include <memory>
@@ -565,20 +568,21 @@ private:
 
 // The archive's description of a map of this library, or null when it holds
 // a component the reference cannot archive (sigmoid expansions).
-std::shared_ptr<RefNode> describe(const std::shared_ptr<ConditionalMapBase>& m,
+std::shared_ptr<RefNode> describe(const ConditionalMapBase* m,
                                   std::map<const ConditionalMapBase*, std::shared_ptr<RefNode>>& memo) {
-    auto it = memo.find(m.get());
+    auto it = memo.find(m);
     if (it != memo.end()) return it->second;
     auto n = std::make_shared<RefNode>();
-    if (auto* t = dynamic_cast<TriangularMap*>(m.get())) {
+    if (auto* t = dynamic_cast<const TriangularMap*>(m)) {
         n->triangular = true;
-        for (unsigned i = 0; i < t->NumComponents(); ++i) {
-            auto c = describe(t->GetComponent(i), memo);
+        auto* tm = const_cast<TriangularMap*>(t);
+        for (unsigned i = 0; i < tm->NumComponents(); ++i) {
+            auto c = describe(tm->GetComponent(i).get(), memo);
             if (!c) return nullptr;
             n->children.push_back(c);
         }
         n->moveCoeffs = t->CheckCoefficients() && t->numCoeffs > 0;
-    } else if (auto* c = dynamic_cast<MonotoneComponent*>(m.get())) {
+    } else if (auto* c = dynamic_cast<const MonotoneComponent*>(m)) {
         RefComp& rc = n->comp;
         rc.mset = c->GetMultiIndexSet();
         rc.opts = c->Options();
@@ -589,7 +593,7 @@ std::shared_ptr<RefNode> describe(const std::shared_ptr<ConditionalMapBase>& m,
     } else {
         return nullptr;
     }
-    memo[m.get()] = n;
+    memo[m] = n;
     return n;
 }
 
@@ -643,7 +647,7 @@ const char* const kSigLabels[4] = {"Sigmoid centers", "Sigmoid widths", "Sigmoid
 std::vector<unsigned char> mapBytes(const std::shared_ptr<ConditionalMapBase>& m) {
     {
         std::map<const ConditionalMapBase*, std::shared_ptr<RefNode>> memo;
-        if (auto root = describe(m, memo)) return writeRefArchive(root);
+        if (auto root = describe(m.get(), memo)) return writeRefArchive(root);
     }
     auto* mono = dynamic_cast<MonotoneMapBase*>(m.get());
     if (!mono) throw std::invalid_argument("only monotone components, sigmoid expansions and triangular maps can be archived");
@@ -749,6 +753,26 @@ void emit(const std::vector<unsigned char>& b, unsigned char* buf, size_t cap, s
 
 
 }  // namespace
+
+void ParameterizedFunctionBase::Save(std::ostream& os) const {
+    auto* m = dynamic_cast<const ConditionalMapBase*>(this);
+    std::map<const ConditionalMapBase*, std::shared_ptr<RefNode>> memo;
+    auto root = m ? describe(m, memo) : nullptr;
+    if (!root)
+        throw std::invalid_argument("Save: only monotone components and triangular maps of them have the reference's "
+                                    "archive.");
+    const std::vector<unsigned char> b = writeRefArchive(root);
+    os.write(reinterpret_cast<const char*>(b.data()), (std::streamsize)b.size());
+    if (!os) throw std::runtime_error("Save: failed to write to the stream.");
+}
+
+std::shared_ptr<ConditionalMapBase> ParameterizedFunctionBase::Load(std::istream& is) {
+    std::vector<unsigned char> b((std::istreambuf_iterator<char>(is)), std::istreambuf_iterator<char>());
+    if (!isRefArchive(b.data(), b.size())) throw std::invalid_argument("Load: not a map archive in the reference's layout.");
+    std::map<const RefNode*, std::shared_ptr<ConditionalMapBase>> memo;
+    return build(readRefArchive(b.data(), b.size()), memo);
+}
+
 }  // namespace mpgb
 
 using namespace mpgb;

@@ -1020,6 +1020,45 @@ std::shared_ptr<ConditionalMapBase> trainMapAdaptive(std::vector<AdaptiveSet>& m
     return map;
 }
 
+// The C++ TrainMapAdaptive: the sets' terms in order go to the adaptive loop
+// (which rebuilds the reference's bookkeeping from them), and the selected
+// sets come back as MultiIndexSets of those terms.
+std::shared_ptr<ConditionalMapBase> TrainMapAdaptive(std::vector<MultiIndexSet>& mset0, KLObjective const& objective,
+                                                     ATMOptions const& options, cudaStream_t stream) {
+    std::vector<AdaptiveSet> sets(mset0.size());
+    for (size_t j = 0; j < mset0.size(); ++j) {
+        if (mset0[j].HasLimiter())
+            throw std::invalid_argument("TrainMapAdaptive: limiters on the initial multi-index sets are not "
+                                        "supported; bound the degrees with ATMOptions::maxDegrees.");
+        sets[j].dim = mset0[j].Length();
+        for (unsigned int k = 0; k < mset0[j].Size(); ++k) sets[j].add(mset0[j].IndexToMulti(k).Vector());
+        if (sets[j].terms.empty()) throw std::invalid_argument("TrainMapAdaptive: empty multi-index set.");
+    }
+    ATMOpts o;
+    o.map = options;
+    if (options.opt_alg == "LD_SLSQP") o.train.algorithm = MPGB_OPT_SLSQP;
+    else if (options.opt_alg == "LD_LBFGS") o.train.algorithm = MPGB_OPT_LBFGS;
+    else throw std::invalid_argument("TrainOptions: opt_alg " + options.opt_alg + " is not provided (LD_SLSQP, LD_LBFGS).");
+    o.train.maxIters = o.train.maxEvals = options.opt_maxeval;
+    o.train.ftolRel = options.opt_ftol_rel;
+    o.train.ftolAbs = options.opt_ftol_abs;
+    o.train.xtolRel = options.opt_xtol_rel;
+    o.train.xtolAbs = options.opt_xtol_abs;
+    o.maxPatience = options.maxPatience;
+    o.maxSize = options.maxSize;
+    o.maxDegrees = options.maxDegrees.Vector();
+    o.verbose = options.verbose;
+    StridedMatrix const& train = objective.Train();
+    StridedMatrix const& test = objective.Test().empty() ? train : objective.Test();
+    auto map = trainMapAdaptive(sets, train, test, o, stream, nullptr);
+    for (size_t j = 0; j < mset0.size(); ++j) {
+        MultiIndexSet s(sets[j].dim);
+        for (auto const& t : sets[j].terms) s += MultiIndex(t);
+        mset0[j] = s;
+    }
+    return map;
+}
+
 int trainMapAdaptiveImpl(unsigned int n_sets, const unsigned int* num_terms, const unsigned int* multis,
                          mpgb_matrix train, mpgb_matrix test, const mpgb_atm_options* opts, mpgb_map** out,
                          mpgb_atm_result* result, unsigned int* final_num_terms, void* stream, char* err, int errLen) {

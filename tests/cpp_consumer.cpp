@@ -15,13 +15,17 @@
 //   in.bin : int64 N, then 14 coefficients, x (2 x N), sens (2 x N) and
 //            r (2 x N, targets), row-major float64
 //   out.bin: per route, T (2 x N), log-det (N), CoeffGrad (14 x N) and
-//            Inverse(r) (2 x N)
+//            Inverse(r) (2 x N); then T (2 x N) of route 1's map after
+//            Save / Load
+// (and the train, mset and atm modes below)
 // The map is the 2 x 2 TriangularMap of total order 3, ProbabilistHermite +
 // SoftPlus, AdaptiveClenshawCurtis with tolerances 1e-6.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -144,10 +148,189 @@ static int trainMain(const char* in, const char* outPath) {
     return 0;
 }
 
-int main(int argc, char** argv) {
-    if (argc == 4 && std::string(argv[1]) == "train") {
+// cpp_consumer mset <specs.txt> <reports.txt>   (host only)
+//   specs: one case per line, "dim mode order kind u0 u1 u2 nw w[nw] nt
+//   t[nt * dim]"; reports: for each case the report of the MultiIndexSet of
+//   the C++ API, in the format of the reference driver's ref_mset_report
+//   (oracle/ref_driver.cpp), cases separated by "====" lines.  mode 0 adds the
+//   terms under the limiter, 1 CreateTotalOrder, 2 CreateTensorProduct, 3 adds
+//   them and calls SetLimiter; limiter kinds as in ref_mset_report.
+static std::string msetReport(unsigned dim, int mode, unsigned order, int kind, const unsigned* u,
+                              std::vector<double> const& w, std::vector<unsigned> const& t) {
+    namespace L = mpgb::MultiIndexLimiter;
+    using mpgb::MultiIndex;
+    using mpgb::MultiIndexSet;
+    mpgb::LimiterType lim;
+    switch (kind) {
+        case 0: lim = L::None(); break;
+        case 1: lim = L::TotalOrder(u[0]); break;
+        case 2: lim = L::Dimension(u[0], u[1]); break;
+        case 3: lim = L::Anisotropic(std::vector<double>(w.begin(), w.begin() + dim), w[dim]); break;
+        case 4: lim = L::MaxDegree(u[0], dim); break;
+        case 5: lim = L::Separable(); break;
+        case 6: lim = L::NonzeroDiag(); break;
+        case 7: lim = L::And(L::TotalOrder(u[0]), L::MaxDegree(u[1], dim)); break;
+        case 8: lim = L::Or(L::Dimension(u[0], u[1]), L::TotalOrder(u[2])); break;
+        case 9: lim = L::Xor(L::TotalOrder(u[0]), L::NonzeroDiag()); break;
+        default: throw std::invalid_argument("unknown limiter kind");
+    }
+    const size_t nt = t.size() / dim;
+    auto term = [&](size_t k) { return MultiIndex(std::vector<unsigned>(t.begin() + k * dim, t.begin() + (k + 1) * dim)); };
+    std::ostringstream os;
+    MultiIndexSet s(dim);
+    if (mode == 1) {
+        s = MultiIndexSet::CreateTotalOrder(dim, order, lim);
+    } else if (mode == 2) {
+        s = MultiIndexSet::CreateTensorProduct(dim, order, lim);
+    } else if (mode == 0) {
+        s = MultiIndexSet(dim, lim);
+        for (size_t k = 0; k < nt; ++k) s += term(k);
+    } else {
+        for (size_t k = 0; k < nt; ++k) s += term(k);
         try {
-            return trainMain(argv[2], argv[3]);
+            s.SetLimiter(lim);
+        } catch (std::invalid_argument const&) {
+            os << "setlimiter rejected\n";
+        }
+    }
+    auto multis = [](std::vector<MultiIndex> const& v) {
+        std::string r;
+        for (size_t k = 0; k < v.size(); ++k) r += (k ? ";" : "") + v[k].String();
+        return r;
+    };
+    auto ints = [](std::vector<unsigned> const& v) {
+        std::string r;
+        for (size_t k = 0; k < v.size(); ++k) r += (k ? "," : "") + std::to_string(v[k]);
+        return r;
+    };
+    auto termsOf = [&](MultiIndexSet const& x) {
+        std::vector<MultiIndex> v;
+        for (unsigned k = 0; k < x.Size(); ++k) v.push_back(x.IndexToMulti(k));
+        return multis(v);
+    };
+    os << "size " << s.Size() << "\n";
+    os << "terms " << termsOf(s) << "\n";
+    os << "maxorders " << ints(s.MaxOrders()) << "\n";
+    os << "frontier " << ints(s.Frontier()) << "\n";
+    os << "strict " << ints(s.StrictFrontier()) << "\n";
+    const auto margin = s.Margin();
+    os << "margin " << multis(margin) << "\n";
+    os << "rmargin " << multis(s.ReducedMargin()) << "\n";
+    for (unsigned d = 0; d < dim; ++d) os << "rmargin_dim" << d << " " << multis(s.ReducedMarginDim(d)) << "\n";
+    std::vector<unsigned> ex, nf, na, adm;
+    for (unsigned k = 0; k < s.Size(); ++k) {
+        ex.push_back(s.IsExpandable(k));
+        nf.push_back(s.NumForward(k));
+        na.push_back(s.NumActiveForward(k));
+    }
+    os << "expandable " << ints(ex) << "\n";
+    os << "nforward " << ints(nf) << "\n";
+    os << "nactiveforward " << ints(na) << "\n";
+    os << "nzdiag " << ints(s.NonzeroDiagonalEntries()) << "\n";
+    for (auto const& m : margin) adm.push_back(s.IsAdmissible(m));
+    os << "margin_admissible " << ints(adm) << "\n";
+    {
+        MultiIndexSet c = s;
+        const auto ix = c.Expand();
+        os << "expand " << ints(ix) << " | " << termsOf(c) << "\n";
+    }
+    for (unsigned k = 0; k < s.Size(); ++k) {
+        MultiIndexSet c = s;
+        os << "expand" << k << " " << ints(c.Expand(k)) << "\n";
+    }
+    {
+        MultiIndexSet c = s;
+        const unsigned added = c.Union(MultiIndexSet::CreateTotalOrder(dim, 1));
+        os << "union " << added << " | " << termsOf(c) << "\n";
+    }
+    return os.str();
+}
+
+static int msetMain(const char* in, const char* outPath) {
+    std::ifstream f(in);
+    std::ofstream g(outPath);
+    std::string line;
+    while (std::getline(f, line)) {
+        if (line.empty()) continue;
+        std::istringstream ls(line);
+        unsigned dim, order, u[3], nw, nt;
+        int mode, kind;
+        ls >> dim >> mode >> order >> kind >> u[0] >> u[1] >> u[2] >> nw;
+        std::vector<double> w(nw);
+        for (auto& x : w) ls >> x;
+        ls >> nt;
+        std::vector<unsigned> t((size_t)nt * dim);
+        for (auto& x : t) ls >> x;
+        if (!ls) throw std::runtime_error("bad spec line");
+        g << msetReport(dim, mode, order, kind, u, w, t) << "====\n";
+    }
+    return g ? 0 : 1;
+}
+
+// cpp_consumer atm <in.bin> <out.bin>
+//   in.bin : int64 N, then samples (2 x N) row-major float64
+//   out.bin: per output j, the number of terms and the terms (dim j+1 each),
+//            as float64, then the trained coefficients, KLObjective::TrainError
+//            of the returned map, and 1 when mset0 came back equal to the
+//            components' multi-index sets (else 0)
+// MParT's adaptive training through the C++ API (MParT/TrainMapAdaptive.h):
+// total-order-1 starting sets, HermiteFunctions + Exp, L-BFGS, maxSize 8.
+static int atmMain(const char* in, const char* outPath) {
+    FILE* f = std::fopen(in, "rb");
+    if (!f) throw std::runtime_error("cannot open input");
+    int64_t N = 0;
+    if (std::fread(&N, sizeof N, 1, f) != 1) throw std::runtime_error("bad input");
+    std::vector<double> x(2 * N);
+    const bool good = std::fread(x.data(), 8, 2 * N, f) == (size_t)(2 * N);
+    std::fclose(f);
+    if (!good) throw std::runtime_error("short input");
+    Dev dx(x);
+    const auto S = mpgb::StridedMatrix::RowMajor(dx.p, 2, N);
+    mpgb::KLObjective obj(S, S);
+    std::vector<mpgb::MultiIndexSet> msets;
+    for (unsigned d = 0; d < 2; ++d) msets.push_back(mpgb::MultiIndexSet::CreateTotalOrder(d + 1, 1));
+    mpgb::ATMOptions o;
+    o.basisType = mpgb::BasisTypes::HermiteFunctions;
+    o.posFuncType = mpgb::PosFuncTypes::Exp;
+    o.quadType = mpgb::QuadTypes::AdaptiveClenshawCurtis;
+    o.quadAbsTol = o.quadRelTol = 1e-7;
+    o.opt_alg = "LD_LBFGS";
+    o.opt_maxeval = 40;
+    o.maxSize = 8;
+    auto map = mpgb::TrainMapAdaptive(msets, obj, o);
+    auto* tm = dynamic_cast<mpgb::TriangularMap*>(map.get());
+    if (!tm) throw std::runtime_error("TrainMapAdaptive did not return a TriangularMap");
+    std::vector<double> out;
+    bool same = true;
+    for (unsigned j = 0; j < 2; ++j) {
+        const auto& s = msets[j];
+        out.push_back(s.Size());
+        for (unsigned k = 0; k < s.Size(); ++k)
+            for (unsigned v : s.IndexToMulti(k).Vector()) out.push_back(v);
+        auto* c = dynamic_cast<mpgb::MonotoneComponent*>(tm->GetComponent(j).get());
+        const auto fx = s.Fix();
+        same = same && c && c->GetMultiIndexSet().nzStarts == fx.nzStarts && c->GetMultiIndexSet().nzDims == fx.nzDims &&
+               c->GetMultiIndexSet().nzOrders == fx.nzOrders;
+    }
+    std::vector<double> coef(map->numCoeffs);
+    cuda(cudaMemcpy(coef.data(), map->Coeffs(), coef.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    out.insert(out.end(), coef.begin(), coef.end());
+    out.push_back(obj.TrainError(map));
+    out.push_back(same ? 1.0 : 0.0);
+    FILE* g = std::fopen(outPath, "wb");
+    if (!g || std::fwrite(out.data(), 8, out.size(), g) != out.size()) throw std::runtime_error("cannot write output");
+    std::fclose(g);
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc == 4 && (std::string(argv[1]) == "train" || std::string(argv[1]) == "mset" ||
+                      std::string(argv[1]) == "atm")) {
+        try {
+            const std::string m = argv[1];
+            return m == "train" ? trainMain(argv[2], argv[3])
+                   : m == "mset" ? msetMain(argv[2], argv[3])
+                                 : atmMain(argv[2], argv[3]);
         } catch (std::exception const& e) {
             std::fprintf(stderr, "cpp_consumer: %s\n", e.what());
             return 1;
@@ -173,7 +356,7 @@ int main(int argc, char** argv) {
         o.quadType = mpgb::QuadTypes::AdaptiveClenshawCurtis;
         o.quadAbsTol = o.quadRelTol = 1e-6;
         Dev dc(coef), dx(x), ds(sens), dr(r);
-        std::vector<double> out;
+        std::vector<double> out, reloaded;
         auto append = [&](const Dev& d) {
             auto h = d.host();
             out.insert(out.end(), h.begin(), h.end());
@@ -195,6 +378,14 @@ int main(int argc, char** argv) {
             append(ld);
             append(cg);
             append(xi);
+            // ParameterizedFunctionBase::Save / Load: the reloaded map evaluates
+            // the same points (appended after both routes).
+            std::stringstream ss;
+            map->Save(ss);
+            auto back = mpgb::ParameterizedFunctionBase::Load(ss);
+            Dev T2(2 * N);
+            back->EvaluateImpl(P, mpgb::StridedMatrix::RowMajor(T2.p, 2, N));
+            reloaded = T2.host();
         }
         // Route 2: the adapter over the C ABI.
         {
@@ -211,6 +402,7 @@ int main(int argc, char** argv) {
             append(cg);
             append(xi);
         }
+        out.insert(out.end(), reloaded.begin(), reloaded.end());
         FILE* g = std::fopen(argv[2], "wb");
         if (!g || std::fwrite(out.data(), 8, out.size(), g) != out.size()) throw std::runtime_error("cannot write output");
         std::fclose(g);
