@@ -99,7 +99,8 @@ public:
     explicit MultiIndex(unsigned int length, unsigned int val = 0) : v_(length, val) {}
     MultiIndex(std::vector<unsigned int> const& v) : v_(v) {}
     MultiIndex(std::initializer_list<unsigned int> v) : v_(v) {}
-    std::vector<unsigned int> const& Vector() const { return v_; }
+    // A copy, as the reference's MultiIndex::Vector returns (safe on temporaries).
+    std::vector<unsigned int> Vector() const { return v_; }
     unsigned int Length() const { return (unsigned int)v_.size(); }
     unsigned int Sum() const;
     unsigned int Max() const;
