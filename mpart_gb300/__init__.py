@@ -137,12 +137,25 @@ def _options_from_fields(fields):
 
 
 class FixedMultiIndexSet:
-    """Compressed multi-index set (MParT/MultiIndices/FixedMultiIndexSet.h).
-    ``FixedMultiIndexSet(dim, maxOrder)`` is the total-order set in the
-    reference's term order (src/MultiIndices/FixedMultiIndexSet.cpp:508-549)."""
+    """Compressed multi-index set (MParT/MultiIndices/FixedMultiIndexSet.h),
+    with the reference binding's constructors
+    (bindings/python/src/MultiIndex.cpp:195-222): ``FixedMultiIndexSet(dim,
+    maxOrder)`` is the total-order set in the reference's term order
+    (src/MultiIndices/FixedMultiIndexSet.cpp:508-549);
+    ``FixedMultiIndexSet(dim, orders)`` takes every term's orders one term
+    after another; ``FixedMultiIndexSet(dim, nzStarts, nzDims, nzOrders)`` the
+    compressed arrays (also as keywords)."""
 
-    def __init__(self, dim: int, maxOrder: int | None = None, *, nzStarts=None, nzDims=None, nzOrders=None):
+    def __init__(self, dim: int, maxOrder=None, *compressed, nzStarts=None, nzDims=None, nzOrders=None):
         self.dim = int(dim)
+        if compressed:
+            if len(compressed) != 2:
+                raise TypeError("FixedMultiIndexSet(dim, nzStarts, nzDims, nzOrders)")
+            nzStarts, (nzDims, nzOrders), maxOrder = maxOrder, compressed, None
+        elif maxOrder is not None and not isinstance(maxOrder, (int, np.integer)):
+            dense = np.asarray(maxOrder, dtype=np.int64).reshape(-1, self.dim)
+            other = FixedMultiIndexSet.from_multis(dense)
+            nzStarts, nzDims, nzOrders, maxOrder = other.nzStarts, other.nzDims, other.nzOrders, None
         if maxOrder is not None:
             starts, dims, orders = [], [], []
             work = [0] * self.dim

@@ -152,3 +152,15 @@ def test_sets_from_arrays_and_fix():
     t = M.MultiIndexSet.CreateTotalOrder(2, 2)
     with pytest.raises(ValueError, match="not valid with the new limiter"):
         t.SetLimiter(M.TotalOrder(1))
+
+
+def test_fixed_set_constructors_of_the_binding():
+    """FixedMultiIndexSet(dim, orders) with every term's orders in turn,
+    (dim, nzStarts, nzDims, nzOrders) positionally, and (dim, maxOrder)
+    (bindings/python/src/MultiIndex.cpp:195-222)."""
+    a = M.FixedMultiIndexSet(2, np.array([0, 0, 1, 0, 0, 2, 1, 1], np.uint32))
+    assert [list(a.IndexToMulti(i)) for i in range(a.Size())] == [[0, 0], [1, 0], [0, 2], [1, 1]]
+    b = M.FixedMultiIndexSet(3, np.array([0, 0, 1, 2]), np.array([0, 1]), np.array([2, 1]))
+    assert [list(b.IndexToMulti(i)) for i in range(b.Size())] == [[0, 0, 0], [2, 0, 0], [0, 1, 0]]
+    assert M.FixedMultiIndexSet(2, 2).Size() == 6
+    assert M.MultiIndexSet.CreateTotalOrder(2, 2).fix(True).ToBytes() == M.FixedMultiIndexSet(2, 2).ToBytes()
