@@ -320,6 +320,18 @@ def RewriteMapArchive(data: bytes) -> bytes:
     return _archive(lambda buf, cap, size: load().mpgb_map_archive_rewrite(data, len(data), buf, cap, size))
 
 
+def __getattr__(name):
+    """The torch wrappers and mpart_has_torch, imported on first use (as the
+    reference's package exports them when torch is present)."""
+    if name in ("TorchConditionalMapBase", "TorchParameterizedFunctionBase"):
+        from . import torch as _t
+        return getattr(_t, name)
+    if name == "mpart_has_torch":
+        import importlib.util
+        return importlib.util.find_spec("torch") is not None
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
+
+
 def _stream_of(*arrs):
     for a in arrs:
         if a is not None and _is_torch(a) and a.is_cuda:

@@ -97,6 +97,27 @@ class MpartTorchInverse(torch.autograd.Function):
         return g_x1, g_r, g_c, None
 
 
+class TorchParameterizedFunctionBase(torch.nn.Module):
+    """TorchParameterizedFunctionBase (bindings/python/package/torch.py):
+    f(x) as a torch module, differentiable in x and in the coefficients (held
+    as a Parameter when store_coeffs)."""
+
+    def __init__(self, f, store_coeffs=True, dtype=torch.double, device="cuda"):
+        super().__init__()
+        self.f = f
+        self.dtype = dtype
+        if store_coeffs:
+            self.coeffs = torch.nn.Parameter(torch.tensor(f.CoeffMap(), dtype=dtype, device=device))
+        else:
+            self.coeffs = None
+
+    def forward(self, x, coeffs=None):
+        coeffs = self.coeffs if coeffs is None else coeffs
+        if coeffs is None:
+            raise RuntimeError('Must either set store_coeffs=True in constructor or pass coeffs to forward function.')
+        return MpartTorchAutograd.apply(x.T, coeffs, self.f, False).T
+
+
 class TorchConditionalMapBase(torch.nn.Module):
 
     def __init__(self, f, store_coeffs=True, return_logdet=False, dtype=torch.double, device="cuda"):

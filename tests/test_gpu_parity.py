@@ -452,6 +452,28 @@ def test_torch_autograd(gpu, oracle):
     assert_parity(H(x.grad).T, ref_x, what="autograd input grad")
 
 
+def test_torch_parameterized_function_base(gpu, oracle):
+    """TorchParameterizedFunctionBase (bindings/python/package/torch.py): f(x)
+    as a torch module; its coefficient and input gradients are the oracle's."""
+    import torch
+    M, O = gpu, oracle
+    tm = M.CreateTriangular(2, 2, 3, opts(M))
+    om = oracle_tri(O, 2, 2, 3)
+    coef = np.random.default_rng(2).normal(0.0, 0.1, tm.numCoeffs)
+    tm.SetCoeffs(coef)
+    mod = M.TorchParameterizedFunctionBase(tm)
+    x = torch.tensor(np.random.default_rng(3).standard_normal((40, 2)), dtype=torch.float64, device="cuda",
+                     requires_grad=True)
+    y = mod(x)
+    (y ** 2).sum().backward()
+    xn = H(x).T
+    yr = om.evaluate(coef, xn)
+    assert_parity(H(y).T, yr, what="TorchParameterizedFunctionBase forward")
+    assert_parity(H(mod.coeffs.grad), om.coeff_grad(coef, xn, 2 * yr).sum(axis=1), floor=1e-3,
+                  what="TorchParameterizedFunctionBase coeff grad")
+    assert_parity(H(x.grad).T, om.gradient(coef, xn, 2 * yr), what="TorchParameterizedFunctionBase input grad")
+
+
 def test_plain_path_matches_oracle(gpu, oracle):
     """The reference-structured comparator gives the same results."""
     import torch

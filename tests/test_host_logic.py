@@ -79,3 +79,12 @@ def test_sigmoid_start_indices():
                        sumType=M.SigmoidSumSizeType.Constant).startInds.tolist() == [2, 3, 4]
     with pytest.raises(ValueError):
         M.Sigmoid1d(np.zeros(6), np.ones(6), np.ones(6))
+
+
+def test_torch_wrappers_are_exported_lazily():
+    """The package exports the torch wrappers and mpart_has_torch as the
+    reference's does, importing torch only when they are asked for."""
+    import mpart_gb300 as M
+    assert M.mpart_has_torch is True
+    assert M.TorchParameterizedFunctionBase.__name__ == "TorchParameterizedFunctionBase"
+    assert M.TorchConditionalMapBase.__name__ == "TorchConditionalMapBase"
