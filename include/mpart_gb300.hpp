@@ -1,8 +1,10 @@
 // C++ API of the GB300 monotone-component path.  Mirrors the reference's
 // host classes (MParT/ParameterizedFunctionBase.h, MParT/ConditionalMapBase.h,
 // MParT/TriangularMap.h, MParT/MapFactory.h, MParT/MapOptions.h,
-// MParT/MultiIndices/FixedMultiIndexSet.h) with device pointers in place of
-// Kokkos device views.  Every *Impl call takes caller-allocated outputs, like
+// MParT/MultiIndices/FixedMultiIndexSet.h, MultiIndex.h, MultiIndexLimiter.h,
+// MultiIndexSet.h, MParT/MapObjective.h, MParT/TrainMap.h,
+// MParT/TrainMapAdaptive.h) with device pointers in place of Kokkos device
+// views.  Every *Impl call takes caller-allocated outputs, like
 // the reference's virtual *Impl methods; calls are stream ordered and, unless
 // the object is put in asynchronous mode, synchronous from the host's view.
 #pragma once
