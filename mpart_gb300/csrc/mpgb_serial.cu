@@ -463,6 +463,7 @@ public:
         objects_[oid & ~kNewId] = n;
         if (name == triangularName(0) || name == triangularName(1)) {
             n->triangular = true;
+            if (open_.size() >= kMaxNesting) bad("triangular maps nested too deeply");
             open_.push_back(n.get());
             triangular(*n);
             open_.pop_back();
@@ -560,6 +561,7 @@ private:
         if (!c.hasCoeffs) c.coeffs.clear();
     }
 
+    static constexpr size_t kMaxNesting = 256;  // bounds the reader's recursion
     Reader& r_;
     std::map<uint32_t, std::string> types_;
     std::map<uint32_t, std::shared_ptr<RefNode>> objects_;

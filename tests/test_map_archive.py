@@ -265,6 +265,12 @@ def test_archive_reader_rejects_what_it_cannot_load(M, fixture):
     loop += struct.pack("<Q", 1) + struct.pack("<II", 1, 1) + struct.pack("<B", 0)
     with pytest.raises(ValueError, match="contains itself"):
         M.RewriteMapArchive(loop)
+    # triangular maps nested a thousand deep (each holding the next)
+    deep = struct.pack("<I", 0x80000001) + struct.pack("<Q", len(name)) + name + struct.pack("<I", 0x80000001)
+    for k in range(1000):
+        deep += struct.pack("<Q", 1) + struct.pack("<II", 1, 0x80000002 + k)
+    with pytest.raises(ValueError, match="nested too deeply"):
+        M.RewriteMapArchive(deep)
 
 
 # ---- GPU ---------------------------------------------------------------------
