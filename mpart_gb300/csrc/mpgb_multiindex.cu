@@ -99,7 +99,7 @@ bool MaxDegree::operator()(MultiIndex const& m) const {
 
 // ---- MultiIndexSet -------------------------------------------------------------
 MultiIndexSet::MultiIndexSet(unsigned int length, LimiterType const& limiter)
-    : length_(length), limiter_(limiter), maxOrders_(length, 0) {
+    : length_(length), limiter_(limiter ? limiter : LimiterType(MultiIndexLimiter::None())), maxOrders_(length, 0) {
     hasLimiter_ = limiter_.target<MultiIndexLimiter::None>() == nullptr;
 }
 
@@ -270,7 +270,7 @@ unsigned int MultiIndexSet::Union(MultiIndexSet const& rhs) {
 }
 
 void MultiIndexSet::SetLimiter(LimiterType const& limiter) {
-    limiter_ = limiter;
+    limiter_ = limiter ? limiter : LimiterType(MultiIndexLimiter::None());
     hasLimiter_ = limiter_.target<MultiIndexLimiter::None>() == nullptr;
     for (size_t g = 0; g < all_.size(); ++g) {  // all_ may grow: new entries are visited too
         if (active((int)g)) {

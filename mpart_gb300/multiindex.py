@@ -253,6 +253,8 @@ class MultiIndexSet:
     # -- construction (MultiIndexSet::CreateTotalOrder / CreateTensorProduct) --
     @staticmethod
     def CreateTotalOrder(length, maxOrder, limiter=None):
+        if int(length) <= 0:
+            raise ValueError("MultiIndexSet::CreateTotalOrder: length must be positive")
         limiter = limiter or NoneLim()
         out = MultiIndexSet(int(length), limiter)
         base = [0] * int(length)
@@ -275,6 +277,8 @@ class MultiIndexSet:
 
     @staticmethod
     def CreateTensorProduct(length, maxOrder, limiter=None):
+        if int(length) <= 0:
+            raise ValueError("MultiIndexSet::CreateTensorProduct: length must be positive")
         limiter = limiter or NoneLim()
         out = MultiIndexSet(int(length), limiter)
         base = [0] * int(length)

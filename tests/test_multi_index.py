@@ -152,6 +152,8 @@ def test_sets_from_arrays_and_fix():
     t = M.MultiIndexSet.CreateTotalOrder(2, 2)
     with pytest.raises(ValueError, match="not valid with the new limiter"):
         t.SetLimiter(M.TotalOrder(1))
+    with pytest.raises(ValueError, match="length must be positive"):
+        M.MultiIndexSet.CreateTotalOrder(0, 2)
 
 
 def test_fixed_set_constructors_of_the_binding():
