@@ -129,8 +129,9 @@ MultiIndexSet MultiIndexSet::CreateTotalOrder(unsigned int length, unsigned int 
                                               LimiterType const& limiter) {
     if (length == 0) throw std::invalid_argument("MultiIndexSet::CreateTotalOrder: length must be positive.");
     MultiIndexSet out(length, limiter);
+    const LimiterType lim = out.GetLimiter();
     std::vector<unsigned int> base(length, 0);
-    fillSet(out, base, 0, maxOrder, true, limiter);
+    fillSet(out, base, 0, maxOrder, true, lim);
     return out;
 }
 
@@ -138,8 +139,9 @@ MultiIndexSet MultiIndexSet::CreateTensorProduct(unsigned int length, unsigned i
                                                  LimiterType const& limiter) {
     if (length == 0) throw std::invalid_argument("MultiIndexSet::CreateTensorProduct: length must be positive.");
     MultiIndexSet out(length, limiter);
+    const LimiterType lim = out.GetLimiter();
     std::vector<unsigned int> base(length, 0);
-    fillSet(out, base, 0, maxDegree, false, limiter);
+    fillSet(out, base, 0, maxDegree, false, lim);
     return out;
 }
 
