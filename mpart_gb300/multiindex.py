@@ -225,8 +225,10 @@ class MultiIndexSet:
     terms: one row per term, added in order) or MultiIndexSet(length, terms)."""
 
     def __init__(self, *args):
+        if not args or len(args) > 2:
+            raise TypeError("MultiIndexSet(length[, limiter]), MultiIndexSet(length, terms) or MultiIndexSet(multis)")
         terms = ()
-        if args and isinstance(args[0], (int, np.integer)):
+        if isinstance(args[0], (int, np.integer)):
             length, limiter = int(args[0]), NoneLim()
             if len(args) > 1:
                 if callable(args[1]):

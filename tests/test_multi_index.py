@@ -154,6 +154,8 @@ def test_sets_from_arrays_and_fix():
         t.SetLimiter(M.TotalOrder(1))
     with pytest.raises(ValueError, match="length must be positive"):
         M.MultiIndexSet.CreateTotalOrder(0, 2)
+    with pytest.raises(TypeError):
+        M.MultiIndexSet()
 
 
 def test_fixed_set_constructors_of_the_binding():
