@@ -11,6 +11,7 @@ from __future__ import annotations
 import ctypes as C
 import enum
 import math
+import os
 from typing import Sequence
 
 import numpy as np
@@ -27,6 +28,7 @@ __all__ = [
     "ATMOptions", "TrainMapAdaptive", "SigmoidTypes", "EdgeTypes", "SigmoidSumSizeType", "SigmoidComponent",
     "CreateSigmoidComponent", "CreateSigmoidTriangular", "Sigmoid1d", "MultiIndex", "TotalOrder", "Dimension",
     "Anisotropic", "MaxDegree", "NoneLim", "Separable", "NonzeroDiag", "And", "Or", "Xor", "RewriteMapArchive",
+    "Initialize", "Concurrency",
 ]
 
 
@@ -310,6 +312,24 @@ def FromBytes(data: bytes):
     h = C.c_void_p()
     check(load().mpgb_map_from_bytes(data, len(data), C.byref(h)))
     return _wrap_map(h)
+
+
+def Initialize(opts=None):
+    """MParT's Initialize(dict) (bindings/python/src/CommonPybindUtilities.cpp:15-27)
+    hands its options to Kokkos; the CUDA runtime here starts on first use, so
+    the options are accepted and have no effect."""
+    return None
+
+
+def Concurrency():
+    """Threads the execution space runs at once, as Kokkos'
+    DefaultExecutionSpace::concurrency() reports (CommonPybindUtilities.cpp:32):
+    on a GPU its SMs times the threads resident per SM, else the host cores."""
+    import torch
+    if torch.cuda.is_available():
+        p = torch.cuda.get_device_properties(torch.cuda.current_device())
+        return int(p.multi_processor_count * getattr(p, "max_threads_per_multi_processor", 2048))
+    return os.cpu_count() or 1
 
 
 def RewriteMapArchive(data: bytes) -> bytes:

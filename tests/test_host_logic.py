@@ -88,3 +88,17 @@ def test_torch_wrappers_are_exported_lazily():
     assert M.mpart_has_torch is True
     assert M.TorchParameterizedFunctionBase.__name__ == "TorchParameterizedFunctionBase"
     assert M.TorchConditionalMapBase.__name__ == "TorchConditionalMapBase"
+
+
+def test_initialize_and_concurrency():
+    """MParT's Initialize(dict) and Concurrency() exist with their meanings:
+    options accepted, and the number of threads the execution space runs."""
+    import os
+
+    import mpart_gb300 as M
+    assert M.Initialize({"kokkos-num-threads": 4}) is None
+    n = M.Concurrency()
+    assert isinstance(n, int) and n >= 1
+    import torch
+    if not torch.cuda.is_available():
+        assert n == (os.cpu_count() or 1)
