@@ -647,42 +647,30 @@ private:
             finishOutputs(s);
         };
         call();  // warm-up
-        cudaEvent_t e0, e1;
-        MPGB_CUDA(cudaEventCreate(&e0));
-        MPGB_CUDA(cudaEventCreate(&e1));
+        EventPair ev;
         double best = 1e300;
         for (int r = 0; r < reps; ++r) {
-            MPGB_CUDA(cudaEventRecord(e0, s));
+            MPGB_CUDA(cudaEventRecord(ev.a, s));
             call();
-            MPGB_CUDA(cudaEventRecord(e1, s));
-            MPGB_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            MPGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            best = std::min(best, (double)ms);
+            MPGB_CUDA(cudaEventRecord(ev.b, s));
+            MPGB_CUDA(cudaEventSynchronize(ev.b));
+            best = std::min(best, (double)ev.ms());
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         checkStatus(s);
         return best;
     }
 
     double timeKernel(const std::vector<WorkItem>& items, int reps, cudaStream_t s) {
         runKernel(items, s);  // warm-up
-        cudaEvent_t e0, e1;
-        MPGB_CUDA(cudaEventCreate(&e0));
-        MPGB_CUDA(cudaEventCreate(&e1));
+        EventPair ev;
         double best = 1e300;
         for (int r = 0; r < reps; ++r) {
-            MPGB_CUDA(cudaEventRecord(e0, s));
+            MPGB_CUDA(cudaEventRecord(ev.a, s));
             runKernel(items, s);
-            MPGB_CUDA(cudaEventRecord(e1, s));
-            MPGB_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            MPGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            best = std::min(best, (double)ms);
+            MPGB_CUDA(cudaEventRecord(ev.b, s));
+            MPGB_CUDA(cudaEventSynchronize(ev.b));
+            best = std::min(best, (double)ev.ms());
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         return best;
     }
 

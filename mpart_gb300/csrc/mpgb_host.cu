@@ -2509,21 +2509,15 @@ int mpgb_component_multi_index(const mpgb_map* component, unsigned int* dim, uns
 int mpgb_fp64_probe(int blocks, int threads, int iters, void* stream, float* ms) {
     return guard([&] {
         cudaStream_t s = (cudaStream_t)stream;
-        double* d = nullptr;
-        MPGB_CUDA(cudaMalloc(&d, 8));
-        cudaEvent_t e0, e1;
-        MPGB_CUDA(cudaEventCreate(&e0));
-        MPGB_CUDA(cudaEventCreate(&e1));
-        MPGB_CUDA(cudaEventRecord(e0, s));
-        MPGB_CUDA(launchDfmaPeak(d, blocks, threads, iters, s));
-        MPGB_CUDA(cudaEventRecord(e1, s));
-        MPGB_CUDA(cudaEventSynchronize(e1));
-        float t = 0;
-        MPGB_CUDA(cudaEventElapsedTime(&t, e0, e1));
-        if (ms) *ms = t;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        cudaFree(d);
+        double* raw = nullptr;
+        MPGB_CUDA(cudaMalloc(&raw, 8));
+        std::unique_ptr<double, cudaError_t (*)(void*)> d(raw, cudaFree);
+        EventPair ev;
+        MPGB_CUDA(cudaEventRecord(ev.a, s));
+        MPGB_CUDA(launchDfmaPeak(d.get(), blocks, threads, iters, s));
+        MPGB_CUDA(cudaEventRecord(ev.b, s));
+        MPGB_CUDA(cudaEventSynchronize(ev.b));
+        if (ms) *ms = ev.ms();
     });
 }
 

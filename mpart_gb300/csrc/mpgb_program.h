@@ -31,6 +31,32 @@ struct CudaError : public std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// Two CUDA events for timing, destroyed on every exit path.
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        MPGB_CUDA(cudaEventCreate(&a));
+        const cudaError_t e = cudaEventCreate(&b);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(a);
+            a = nullptr;
+            MPGB_CUDA(e);
+        }
+    }
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    // Milliseconds between the two events (b must have completed).
+    float ms() const {
+        float t = 0;
+        MPGB_CUDA(cudaEventElapsedTime(&t, a, b));
+        return t;
+    }
+};
+
 // Quadrature rules (AdaptiveClenshawCurtis) and basis constants for a launch.
 void buildLaunchConstants(const MapOptions& o, QuadParams& q, BasisConsts& b);
 

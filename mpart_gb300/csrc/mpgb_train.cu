@@ -512,9 +512,7 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
                                     o, dinv.empty() ? nullptr : dinv.data() + p.mapCoeffOffset));
     int steps = 0;
     double stepMs = 0.0;
-    cudaEvent_t e0, e1;
-    TR_CUDA(cudaEventCreate(&e0));
-    TR_CUDA(cudaEventCreate(&e1));
+    EventPair ev;
     const auto t0 = std::chrono::steady_clock::now();
     while (true) {
         bool any = false;
@@ -524,13 +522,11 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
             any |= !opt[c]->done();
         }
         if (!any) break;
-        TR_CUDA(cudaEventRecord(e0, step.s));
+        TR_CUDA(cudaEventRecord(ev.a, step.s));
         step.run();
-        TR_CUDA(cudaEventRecord(e1, step.s));
-        TR_CUDA(cudaEventSynchronize(e1));
-        float ms = 0;
-        TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        stepMs += ms;
+        TR_CUDA(cudaEventRecord(ev.b, step.s));
+        TR_CUDA(cudaEventSynchronize(ev.b));
+        stepMs += ev.ms();
         ++steps;
         // A trial point whose integrand overflows gives its component a
         // non-finite objective, which the line search rejects (it steps
@@ -540,8 +536,6 @@ void trainKL(MonotoneMapBase& map, StridedMatrix const& pts, TrainOpts const& o,
             if (!opt[c]->done()) opt[c]->tell(step.hLoss.p[c], step.hGrad.p + parts[c].mapCoeffOffset);
     }
     const double totalMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     for (size_t c = 0; c < opt.size(); ++c)
         if (!std::isfinite(opt[c]->f()))
             throw IntegrandError("TrainMap: MonotoneIntegrand: the objective is not finite at the starting "
@@ -665,21 +659,15 @@ int klStepTimeImpl(void* mapObj, mpgb_matrix samples, int mode, int steps, doubl
         std::vector<double> x0 = map->CoeffMap();
         std::memcpy(step.hCoef.p, x0.data(), x0.size() * sizeof(double));
         for (int i = 0; i < 3; ++i) step.run();
-        cudaEvent_t e0, e1;
-        TR_CUDA(cudaEventCreate(&e0));
-        TR_CUDA(cudaEventCreate(&e1));
+        EventPair ev;
         double tot = 0;
         for (int i = 0; i < steps; ++i) {
-            TR_CUDA(cudaEventRecord(e0, step.s));
+            TR_CUDA(cudaEventRecord(ev.a, step.s));
             step.run();
-            TR_CUDA(cudaEventRecord(e1, step.s));
-            TR_CUDA(cudaEventSynchronize(e1));
-            float ms = 0;
-            TR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            tot += ms;
+            TR_CUDA(cudaEventRecord(ev.b, step.s));
+            TR_CUDA(cudaEventSynchronize(ev.b));
+            tot += ev.ms();
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
         *ms_per_step = tot / steps;
         if (loss) std::memcpy(loss, step.hLoss.p, map->outputDim * sizeof(double));
         if (grad) std::memcpy(grad, step.hGrad.p, map->numCoeffs * sizeof(double));
