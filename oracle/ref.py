@@ -74,6 +74,7 @@ def lib():
         L.ref_mset_bytes.argtypes = [C.c_uint, C.c_uint, _up, _up, _up] + out
         L.ref_coeff_archive.argtypes = [C.c_void_p] + out
         L.ref_mset_report.argtypes = [C.c_uint, C.c_uint, _up, C.c_int, C.c_uint, C.c_int, _up, _dp] + out
+        L.ref_multi_order.argtypes = [C.c_uint, C.c_uint, _up, C.c_void_p, _up, _up]
         L.ref_triangular_from.restype = C.c_void_p
         L.ref_triangular_from.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
         _lib = L
@@ -313,6 +314,21 @@ def mset_report(dim, terms=(), mode=0, order=0, lim_kind=0, u=(0, 0, 0), w=()):
     return _bytes(lambda buf, cap, sz: lib().ref_mset_report(dim, n, t.ctypes.data_as(_up), mode, order, lim_kind,
                                                              uu.ctypes.data_as(_up), ww.ctypes.data_as(_dp), buf,
                                                              cap, sz)).decode()
+
+
+def multi_order(terms):
+    """(less, nzdiag): less[i, j] = terms[i] < terms[j] by MultiIndex::operator<,
+    and NonzeroDiagonalEntries of the FixedMultiIndexSet of the distinct terms
+    added in order (MultiIndexSet += then Fix)."""
+    t = np.ascontiguousarray(terms, dtype=np.uint32)
+    n, dim = t.shape
+    less = np.zeros((n, n), np.uint8)
+    nz = np.zeros(max(1, n), np.uint32)
+    cnt = C.c_uint()
+    if lib().ref_multi_order(dim, n, t.ctypes.data_as(_up), less.ctypes.data_as(C.c_void_p), nz.ctypes.data_as(_up),
+                             C.byref(cnt)) != 0:
+        raise RuntimeError(lib().ref_last_error().decode())
+    return less.astype(bool), [int(v) for v in nz[:cnt.value]]
 
 
 def mset_reduced_margin(terms):

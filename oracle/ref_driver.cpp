@@ -483,6 +483,25 @@ int ref_mset(unsigned dim, unsigned n, const unsigned* multis, int mode, unsigne
     });
 }
 
+// For n multi-indices (rows of length dim): less[i * n + j] = (m_i < m_j) by
+// MultiIndex::operator<, and, for the FixedMultiIndexSet of these terms
+// (compressed), its NonzeroDiagonalEntries in nzdiag (count in *nNz).
+int ref_multi_order(unsigned dim, unsigned n, const unsigned* multis, unsigned char* less, unsigned* nzdiag,
+                    unsigned* nNz) {
+    return guard([&] {
+        std::vector<mpart::MultiIndex> ms;
+        for (unsigned t = 0; t < n; ++t)
+            ms.emplace_back(std::vector<unsigned>(multis + (size_t)t * dim, multis + (size_t)(t + 1) * dim));
+        for (unsigned i = 0; i < n; ++i)
+            for (unsigned j = 0; j < n; ++j) less[(size_t)i * n + j] = ms[i] < ms[j];
+        mpart::MultiIndexSet s(dim);
+        for (auto const& m : ms) s += m;
+        const auto nz = s.Fix(true).NonzeroDiagonalEntries();
+        for (size_t k = 0; k < nz.size(); ++k) nzdiag[k] = nz[k];
+        *nNz = (unsigned)nz.size();
+    });
+}
+
 // A report of MParT's MultiIndexSet for the set tests: mode 0 builds it by
 // += of the n terms (rows of length dim) under the limiter, mode 1 is
 // CreateTotalOrder(dim, order), mode 2 CreateTensorProduct(dim, order), mode 3

@@ -168,3 +168,21 @@ def test_fixed_set_constructors_of_the_binding():
     assert [list(b.IndexToMulti(i)) for i in range(b.Size())] == [[0, 0, 0], [2, 0, 0], [0, 1, 0]]
     assert M.FixedMultiIndexSet(2, 2).Size() == 6
     assert M.MultiIndexSet.CreateTotalOrder(2, 2).fix(True).ToBytes() == M.FixedMultiIndexSet(2, 2).ToBytes()
+
+
+def test_multi_index_order_and_diagonal_entries_match_reference():
+    """MultiIndex::operator< (length, total order, maximum, then entries) and
+    FixedMultiIndexSet::NonzeroDiagonalEntries against the reference's."""
+    ref = _ref()
+    rng = np.random.default_rng(3)
+    for dim in (1, 2, 3, 5):
+        terms = [tuple(int(v) for v in rng.integers(0, 3, dim)) for _ in range(25)]
+        less, nzdiag = ref.multi_order(terms)
+        ms = [M.MultiIndex(t) for t in terms]
+        got = np.array([[a < b for b in ms] for a in ms])
+        np.testing.assert_array_equal(got, less)
+        s = M.MultiIndexSet(dim)
+        for t in terms:
+            s += t
+        assert s.fix(True).NonzeroDiagonalEntries() == nzdiag
+        assert s.NonzeroDiagonalEntries() == nzdiag
